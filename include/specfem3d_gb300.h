@@ -1,0 +1,267 @@
+/*
+ * specfem3d_gb300 — C ABI of the GB300 (sm_103a) spectral-element time step.
+ *
+ * Two layers:
+ *
+ * 1. Drop-in entry points with the exact names and argument lists of the
+ *    reference's Fortran-callable GPU layer (the .cu files of src/gpu, declared through
+ *    FC_FUNC_(name,NAME), which gfortran resolves to `name_`).  Every argument
+ *    is passed by reference, Fortran LOGICALs arrive as int*, index arrays hold
+ *    the Fortran 1-based values, host arrays keep the Fortran layouts listed in
+ *    the comments.  Each declaration cites the reference function it replaces.
+ *    Like the reference these return void; on an error they record a status
+ *    (read it with sf3d_last_error) instead of aborting, unless the environment
+ *    variable SF3D_ABORT_ON_ERROR=1 asks for the reference's exit(1).
+ *
+ * 2. sf3d_* entry points of this library (status-returning): error queries,
+ *    whole-run time loops captured in CUDA graphs, and the batched-shot API.
+ *
+ * realw is float (the reference GPU build is single precision only,
+ * src/gpu/mesh_constants_gpu.h:80-87).
+ */
+#ifndef SPECFEM3D_GB300_H
+#define SPECFEM3D_GB300_H
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+typedef float realw;
+
+/* ---------------------------------------------------------------------------
+ * status API (no reference counterpart: the reference aborts on any error)
+ * ------------------------------------------------------------------------- */
+#define SF3D_OK 0
+#define SF3D_ERR_ARG 1      /* invalid argument or size */
+#define SF3D_ERR_CUDA 2     /* CUDA runtime error */
+#define SF3D_ERR_STATE 3    /* call out of order / handle not prepared */
+#define SF3D_ERR_UNSTABLE 4 /* wavefield blew up (NaN/Inf or above threshold) */
+
+int sf3d_last_error(char *msg, int msg_len);  /* returns last status, copies message */
+void sf3d_clear_error(void);
+int sf3d_version(void);
+
+/* ---------------------------------------------------------------------------
+ * setup — src/gpu/initialize_gpu.cu, src/gpu/prepare_mesh_constants_cuda.cu
+ * ------------------------------------------------------------------------- */
+
+/* initialize_gpu_device (initialize_gpu.cu:535): selects device myrank % count,
+ * returns the visible device count. */
+void initialize_gpu_device_(int *myrank_f, int *ncuda_devices);
+
+/* prepare_constants_device (prepare_mesh_constants_cuda.cu:70-119, argument list
+ * as called from specfem3D/prepare_gpu.f90:67-101).  Allocates the Mesh handle
+ * and stores it in *Mesh_pointer.  Layouts: xix..gammaz (5,5,5,NSPEC_IRREGULAR),
+ * ibool (5,5,5,NSPEC_AB), abs_boundary_ijk (3,25,nfaces), abs_boundary_normal
+ * (3,25,nfaces), abs_boundary_jacobian2Dw (25,nfaces), sourcearrays
+ * (NSOURCES,3,5,5,5), xir/etar/gammar (5,nrec_local), nu_rec/nu_source
+ * (3,3,nrec)/(3,3,NSOURCES) in double. */
+void prepare_constants_device_(long *Mesh_pointer, int *h_NGLLX, int *NSPEC_AB, int *NGLOB_AB,
+                               int *NSPEC_IRREGULAR, int *h_irregular_element_number,
+                               realw *h_xix, realw *h_xiy, realw *h_xiz, realw *h_etax,
+                               realw *h_etay, realw *h_etaz, realw *h_gammax, realw *h_gammay,
+                               realw *h_gammaz, realw *xix_regular, realw *jacobian_regular,
+                               int *h_ibool, int *num_interfaces_ext_mesh,
+                               int *max_nibool_interfaces_ext_mesh,
+                               int *h_nibool_interfaces_ext_mesh, int *h_ibool_interfaces_ext_mesh,
+                               realw *h_hprime_xx, realw *h_hprimewgll_xx, realw *h_wgllwgll_xy,
+                               realw *h_wgllwgll_xz, realw *h_wgllwgll_yz,
+                               int *STACEY_ABSORBING_CONDITIONS, int *h_abs_boundary_ispec,
+                               int *h_abs_boundary_ijk, realw *h_abs_boundary_normal,
+                               realw *h_abs_boundary_jacobian2Dw, int *h_num_abs_boundary_faces,
+                               int *h_ispec_is_inner, int *NSOURCES, int *nsources_local_f,
+                               realw *h_sourcearrays, int *h_islice_selected_source,
+                               int *h_ispec_selected_source, int *h_ispec_selected_rec, int *nrec,
+                               int *nrec_local, int *SIMULATION_TYPE, int *USE_MESH_COLORING_GPU_f,
+                               int *nspec_acoustic, int *nspec_elastic, int *ispec_is_acoustic,
+                               int *ispec_is_elastic, int *h_myrank, int *SAVE_FORWARD,
+                               realw *h_xir, realw *h_etar, realw *h_gammar, double *nu_rec,
+                               double *nu_source, int *h_islice_selected_rec,
+                               int *nlength_seismogram, int *SAVE_SEISMOGRAMS_DISPLACEMENT,
+                               int *SAVE_SEISMOGRAMS_VELOCITY, int *SAVE_SEISMOGRAMS_ACCELERATION,
+                               int *SAVE_SEISMOGRAMS_PRESSURE, int *h_NB_RUNS_ACOUSTIC_GPU,
+                               int *FAULT_SIMULATION, int *UNDO_ATTENUATION_AND_OR_PML,
+                               int *PML_CONDITIONS);
+
+/* prepare_fields_elastic_device (prepare_mesh_constants_cuda.cu:657-998;
+ * specfem3D/prepare_gpu.f90:138-165).  rmass{x,y,z} (NGLOB), rho_vp/rho_vs/
+ * kappav/muv (5,5,5,NSPEC), phase_ispec_inner_elastic (num_phase_ispec,2),
+ * R_* / factor_common* (N_SLS,5,5,5,NSPEC), epsilondev_* (5,5,5,NSPEC),
+ * alphaval/betaval/gammaval (N_SLS). */
+void prepare_fields_elastic_device_(long *Mesh_pointer, realw *rmassx, realw *rmassy, realw *rmassz,
+                                    realw *rho_vp, realw *rho_vs, realw *h_kappav, realw *h_muv,
+                                    int *num_phase_ispec_elastic, int *phase_ispec_inner_elastic,
+                                    realw *b_absorb_field, int *b_reclen_field,
+                                    int *COMPUTE_AND_STORE_STRAIN, realw *epsilondev_xx,
+                                    realw *epsilondev_yy, realw *epsilondev_xy,
+                                    realw *epsilondev_xz, realw *epsilondev_yz, int *ATTENUATION,
+                                    int *R_size, realw *R_xx, realw *R_yy, realw *R_xy,
+                                    realw *R_xz, realw *R_yz, realw *factor_common,
+                                    realw *R_trace, realw *epsilondev_trace,
+                                    realw *factor_common_kappa, realw *alphaval, realw *betaval,
+                                    realw *gammaval, int *APPROXIMATE_OCEAN_LOAD,
+                                    realw *rmass_ocean_load, int *NOISE_TOMOGRAPHY,
+                                    realw *free_surface_normal, int *free_surface_ispec,
+                                    int *free_surface_ijk, int *num_free_surface_faces,
+                                    int *ACOUSTIC_SIMULATION, int *num_colors_outer_elastic,
+                                    int *num_colors_inner_elastic, int *num_elem_colors_elastic,
+                                    int *ANISOTROPY, realw *c11store, realw *c12store,
+                                    realw *c13store, realw *c14store, realw *c15store,
+                                    realw *c16store, realw *c22store, realw *c23store,
+                                    realw *c24store, realw *c25store, realw *c26store,
+                                    realw *c33store, realw *c34store, realw *c35store,
+                                    realw *c36store, realw *c44store, realw *c45store,
+                                    realw *c46store, realw *c55store, realw *c56store,
+                                    realw *c66store);
+
+/* prepare_cleanup_device (prepare_mesh_constants_cuda.cu:1552): frees the handle. */
+void prepare_cleanup_device_(long *Mesh_pointer, int *ACOUSTIC_SIMULATION, int *ELASTIC_SIMULATION,
+                             int *NOISE_TOMOGRAPHY);
+
+/* ---------------------------------------------------------------------------
+ * hot path — one call each per time step, in iterate_time.F90 order
+ * ------------------------------------------------------------------------- */
+
+/* update_displacement_cuda (update_displacement_cuda.cu:39-188): Newmark predictor
+ * u += dt v + dt^2/2 a; v += dt/2 a; a = 0 on the forward (1), backward (3) or both (0) fields. */
+void update_displacement_cuda_(long *Mesh_pointer, realw *deltat_F, realw *deltatover2_F,
+                               realw *deltatsqover2_F, int *FORWARD_OR_ADJOINT);
+
+/* compute_forces_viscoelastic_cuda (compute_forces_viscoelastic_cuda.cu:1115-1278):
+ * elastic stiffness of the elements of phase iphase (1 outer, 2 inner), gathered
+ * through ibool and scatter-added into accel; attenuation memory variables and
+ * strain updated when requested. */
+void compute_forces_viscoelastic_cuda_(long *Mesh_pointer, int *iphase, realw *deltat,
+                                       int *nspec_outer_elastic, int *nspec_inner_elastic,
+                                       int *COMPUTE_AND_STORE_STRAIN, int *ATTENUATION,
+                                       int *FORWARD_OR_ADJOINT_f);
+
+/* compute_stacey_viscoelastic_cuda (compute_stacey_viscoelastic_cuda.cu:39-222):
+ * absorbing traction on the Stacey faces (iphase 1 only). */
+void compute_stacey_viscoelastic_cuda_(long *Mesh_pointer, int *iphasef, realw *b_absorb_field,
+                                       int *FORWARD_OR_ADJOINT_f);
+
+/* compute_add_sources_el_cuda (compute_add_sources_viscoelastic_cuda.cu:39-100):
+ * accel += sourcearrays * stf, stf given per source for this step (FP64 host). */
+void compute_add_sources_el_cuda_(long *Mesh_pointer, double *h_stf_pre_compute, int *h_NSOURCES);
+
+/* compute_add_sources_el_s3_cuda (compute_add_sources_viscoelastic_cuda.cu:~105):
+ * same on the backward/reconstructed field. */
+void compute_add_sources_el_s3_cuda_(long *Mesh_pointer, double *h_stf_pre_compute, int *h_NSOURCES);
+
+/* kernel_3_a_cuda (update_displacement_cuda.cu:287-380): a *= rmass{x,y,z};
+ * v += dt/2 a (fused mass + corrector without ocean load). */
+void kernel_3_a_cuda_(long *Mesh_pointer, realw *deltatover2_F, realw *b_deltatover2_F,
+                      int *APPROXIMATE_OCEAN_LOAD, int *FORWARD_OR_ADJOINT);
+
+/* kernel_3_b_cuda (update_displacement_cuda.cu:382): corrector only (ocean-load path). */
+void kernel_3_b_cuda_(long *Mesh_pointer, realw *deltatover2_F, realw *b_deltatover2_F,
+                      int *FORWARD_OR_ADJOINT);
+
+/* compute_seismograms_cuda (write_seismograms_cuda.cu:34-373): receiver
+ * interpolation into the device trace buffer (NDIM,nrec_local,nlength); the
+ * buffer is copied to the host arrays when full or at it == it_end. */
+void compute_seismograms_cuda_(long *Mesh_pointer_f, realw *seismograms_d, realw *seismograms_v,
+                               realw *seismograms_a, realw *seismograms_p, int *seismo_currentf,
+                               int *nlength_seismogramf, int *itf, int *it_endf,
+                               int *ACOUSTIC_SIMULATION, int *ELASTIC_SIMULATION,
+                               int *USE_TRICK_FOR_BETTER_PRESSURE);
+
+/* ---------------------------------------------------------------------------
+ * transfers — src/gpu/transfer_fields_cuda.cu
+ * ------------------------------------------------------------------------- */
+void transfer_fields_el_to_device_(int *size, realw *displ, realw *veloc, realw *accel, long *Mesh_pointer);   /* :45 */
+void transfer_fields_el_from_device_(int *size, realw *displ, realw *veloc, realw *accel, long *Mesh_pointer); /* :95 */
+void transfer_b_fields_to_device_(int *size, realw *b_displ, realw *b_veloc, realw *b_accel, long *Mesh_pointer);
+void transfer_b_fields_from_device_(int *size, realw *b_displ, realw *b_veloc, realw *b_accel, long *Mesh_pointer);
+void transfer_displ_from_device_(int *size, realw *displ, long *Mesh_pointer);
+void transfer_displ_to_device_(int *size, realw *displ, long *Mesh_pointer);
+void transfer_veloc_from_device_(int *size, realw *veloc, long *Mesh_pointer);
+void transfer_veloc_to_device_(int *size, realw *veloc, long *Mesh_pointer);
+void transfer_accel_from_device_(int *size, realw *accel, long *Mesh_pointer);
+void transfer_accel_to_device_(int *size, realw *accel, long *Mesh_pointer);
+void transfer_b_displ_from_device_(int *size, realw *b_displ, long *Mesh_pointer);
+void transfer_b_displ_to_device_(int *size, realw *b_displ, long *Mesh_pointer);
+/* transfer_rmemory_from_device / transfer_strain_from_device
+ * (transfer_fields_cuda.cu:~560-640): R_* (N_SLS,5,5,5,NSPEC), epsilondev_* (5,5,5,NSPEC). */
+void transfer_rmemory_from_device_(long *Mesh_pointer, realw *R_xx, realw *R_yy, realw *R_xy,
+                                   realw *R_xz, realw *R_yz, realw *R_trace, int *size_R);
+void transfer_strain_from_device_(long *Mesh_pointer, realw *epsilondev_xx, realw *epsilondev_yy,
+                                  realw *epsilondev_xy, realw *epsilondev_xz, realw *epsilondev_yz,
+                                  realw *epsilondev_trace, int *size_epsilondev);
+
+/* ---------------------------------------------------------------------------
+ * adjoint (SIMULATION_TYPE = 3) — src/gpu/compute_kernels_cuda.cu,
+ * prepare_mesh_constants_cuda.cu:999 and :1306
+ * ------------------------------------------------------------------------- */
+void prepare_fields_elastic_adj_dev_(long *Mesh_pointer, int *size_f, realw *epsilon_trace_over_3,
+                                     realw *b_epsilondev_xx, realw *b_epsilondev_yy,
+                                     realw *b_epsilondev_xy, realw *b_epsilondev_xz,
+                                     realw *b_epsilondev_yz, realw *b_epsilon_trace_over_3,
+                                     int *R_size, realw *b_R_xx, realw *b_R_yy, realw *b_R_xy,
+                                     realw *b_R_xz, realw *b_R_yz, realw *b_R_trace,
+                                     realw *b_epsilondev_trace, realw *b_alphaval,
+                                     realw *b_betaval, realw *b_gammaval, int *ANISOTROPIC_KL,
+                                     int *APPROXIMATE_HESS_KL);
+void prepare_sim2_or_3_const_device_(long *Mesh_pointer, int *nadj_rec_local,
+                                     int *NTSTEP_BETWEEN_READ_ADJSRC, realw *hxir_adjstore,
+                                     realw *hetar_adjstore, realw *hgammar_adjstore, int *nrec,
+                                     int *h_islice_selected_rec, int *h_ispec_selected_rec);
+/* add_sources_el_sim_type_2_or_3 (compute_add_sources_viscoelastic_cuda.cu:224):
+ * h_source_adjoint (3, nadj_rec_local, NTSTEP_BETWEEN_READ_ADJSRC). */
+void add_sources_el_sim_type_2_or_3_(long *Mesh_pointer, realw *h_source_adjoint, int *nrec,
+                                     int *nadj_rec_local, int *NTSTEP_BETWEEN_READ_ADJSRC, int *it);
+/* compute_strain_cuda (compute_strain_cuda.cu): deviatoric strain and trace/3 of the
+ * forward (1) or backward (3) displacement, used by the checkpointed adjoint. */
+void compute_strain_cuda_(long *Mesh_pointer, int *FORWARD_OR_ADJOINT);
+/* compute_kernels_elastic_cuda (compute_kernels_cuda.cu:39): rho/mu/kappa kernels
+ * accumulated on the device in FP64. */
+void compute_kernels_elastic_cuda_(long *Mesh_pointer, realw *deltat_f);
+/* transfer_kernels_el_to_host (transfer_fields_cuda.cu:~700): (5,5,5,NSPEC). */
+void transfer_kernels_el_to_host_(long *Mesh_pointer, realw *h_rho_kl, realw *h_mu_kl,
+                                  realw *h_kappa_kl, realw *h_cijkl_kl, int *NSPEC_AB);
+
+/* FP64 sensitivity kernels (5,5,5,NSPEC) straight from the device accumulators
+ * (no reference counterpart: the reference accumulates in single precision). */
+int sf3d_get_kernels_f64(long *Mesh_pointer, double *h_rho_kl, double *h_mu_kl, double *h_kappa_kl);
+
+/* ---------------------------------------------------------------------------
+ * library entry points (no reference counterpart)
+ * ------------------------------------------------------------------------- */
+
+/* Upload a whole-run source time function table (NSOURCES, nstep) in FP64;
+ * the device copy is rounded to FP32 like the per-step stf of the reference. */
+int sf3d_set_stf_table(long *Mesh_pointer, const double *h_stf, int nsources, int nstep);
+
+/* Run time steps it_begin..it_end (1-based, inclusive) of the forward elastic
+ * scheme entirely on the device: fused corrector+predictor, Stacey, sources,
+ * stiffness, displacement seismograms.  Steps are captured in CUDA graphs of
+ * steps_per_graph steps (0 = no graphs).  Leaves the fields as the per-call
+ * ABI leaves them after the same steps.  flags bit 0: record the device time
+ * of every stiffness launch (read back with sf3d_last_timing). */
+int sf3d_iterate_time(long *Mesh_pointer, int it_begin, int it_end, realw deltat, int steps_per_graph,
+                      int flags);
+
+/* Copy the device trace buffer (3, nrec_local, nlength) to the host. */
+int sf3d_get_seismograms(long *Mesh_pointer, realw *h_seismograms);
+
+/* Device time of the stiffness kernel launches of the last sf3d_iterate_time
+ * call, in ms (CUDA events on the compute stream), and their count. */
+int sf3d_last_timing(long *Mesh_pointer, float *stiffness_ms, int *stiffness_launches,
+                     float *total_ms, int *total_launches);
+
+/* Synchronise the compute stream and report the first stored status. */
+int sf3d_synchronize(long *Mesh_pointer);
+
+/* Raw device pointer of a named field ("displ", "veloc", "accel", ...) for
+ * in-HBM benchmarking and zero-copy interop; NULL if unknown. */
+void *sf3d_device_ptr(long *Mesh_pointer, const char *name);
+
+/* Stability check (check_stability.f90:408): max |displ| over the device field;
+ * returns SF3D_ERR_UNSTABLE if NaN/Inf or above threshold. */
+int sf3d_check_stability(long *Mesh_pointer, realw threshold, realw *max_norm);
+
+#ifdef __cplusplus
+}
+#endif
+#endif

@@ -1,0 +1,419 @@
+"""ctypes front end of the CPU oracle (TEST INFRASTRUCTURE ONLY).
+
+Only ``tests/``, ``__graft_entry__.smoke()`` and ``bench.py``'s CPU-baseline leg
+may import this module; it is the checker, never the product.  It builds
+``liboracle_f32.so`` / ``liboracle_f64.so`` from ``sem_oracle.c`` and restates
+the reference's database generation for a regular layered block:
+
+* mesher geometry + GLL coordinates   (generate_databases/calc_jacobian.f90:148-178)
+* global numbering                    (shared/get_global.f90:28-141)
+* Jacobian, regular/irregular split   (generate_databases/calc_jacobian.f90:28-360)
+* materials                           (generate_databases/get_model.F90:289-301)
+* mass matrices incl. Stacey term     (shared/define_mass_matrices.f90:28-442,
+                                       specfem3D/prepare_timerun.F90:246-388)
+* absorbing faces                     (generate_databases/get_absorbing_boundary.F90)
+* source/receiver location + arrays   (specfem3D/locate_point.f90,
+                                       specfem3D/compute_arrays_source.f90:29-149)
+* source time function table          (specfem3D/comp_source_time_function.f90,
+                                       specfem3D/setup_sources_receivers.f90:482-491)
+"""
+from __future__ import annotations
+
+import ctypes
+import os
+import subprocess
+import threading
+
+import numpy as np
+
+_HERE = os.path.dirname(os.path.abspath(__file__))
+_BUILD = os.path.join(_HERE, "_build")
+_SRC = os.path.join(_HERE, "sem_oracle.c")
+_LOCK = threading.Lock()
+_LIBS: dict = {}
+
+NGLL = 5
+NGLL3 = 125
+N_SLS = 3
+
+
+def build(force: bool = False) -> None:
+    """Compile both precisions of the oracle with gcc (OpenMP)."""
+    os.makedirs(_BUILD, exist_ok=True)
+    for tag, extra in (("f32", []), ("f64", ["-DORACLE_DOUBLE"])):
+        out = os.path.join(_BUILD, f"liboracle_{tag}.so")
+        if (not force and os.path.exists(out)
+                and os.path.getmtime(out) >= max(os.path.getmtime(_SRC),
+                                                 os.path.getmtime(os.path.join(_HERE, "sem_oracle.h")))):
+            continue
+        cmd = ["gcc", "-O2", "-fPIC", "-fopenmp", "-shared", *extra, "-o", out, _SRC, "-lm"]
+        subprocess.run(cmd, check=True)
+
+
+def lib(precision: str = "f32") -> ctypes.CDLL:
+    with _LOCK:
+        if precision not in _LIBS:
+            build()
+            L = ctypes.CDLL(os.path.join(_BUILD, f"liboracle_{precision}.so"))
+            vp = ctypes.c_void_p
+            L.orc_sim_new.restype = vp
+            L.orc_sim_free.argtypes = [vp]
+            L.orc_set_ptr.argtypes = [vp, ctypes.c_char_p, vp]
+            L.orc_set_int.argtypes = [vp, ctypes.c_char_p, ctypes.c_int]
+            L.orc_get_int.argtypes = [vp, ctypes.c_char_p, ctypes.POINTER(ctypes.c_int)]
+            L.orc_set_real.argtypes = [vp, ctypes.c_char_p, ctypes.c_double]
+            L.orc_step.argtypes = [vp]
+            L.orc_run.argtypes = [vp, ctypes.c_int]
+            L.orc_compute_forces_elastic.argtypes = [vp, ctypes.c_int]
+            L.orc_stf.restype = ctypes.c_double
+            L.orc_stf.argtypes = [ctypes.c_int, ctypes.c_double, ctypes.c_double]
+            L.orc_get_global.restype = ctypes.c_int
+            L.orc_get_global.argtypes = [ctypes.c_long, vp, vp, vp, vp, ctypes.c_double]
+            L.orc_mesh_regular.argtypes = [ctypes.c_int] * 3 + [ctypes.c_double] * 4 + [vp] * 5
+            L.orc_calc_jacobian_all.restype = ctypes.c_int
+            L.orc_calc_jacobian_all.argtypes = [ctypes.c_int, vp, vp, vp, vp, vp]
+            L.orc_mass_stacey_elastic.argtypes = [ctypes.c_int, ctypes.c_double] + [vp] * 10
+            L.orc_invert_mass.argtypes = [ctypes.c_int, vp, vp, vp, vp, ctypes.c_int]
+            L.orc_face_geometry.argtypes = [vp, ctypes.c_int, vp, vp, vp]
+            L.orc_locate_point.restype = ctypes.c_int
+            L.orc_locate_point.argtypes = [ctypes.c_int, vp, vp, vp, vp] + [ctypes.c_double] * 3 + [vp] * 3
+            L.orc_lagrange_any.argtypes = [ctypes.c_double, vp, vp, vp]
+            L.orc_gll.argtypes = [vp, vp]
+            L.orc_derivation_matrices.argtypes = [vp] * 6
+            L.orc_source_array_cmt.argtypes = ([ctypes.c_int, vp, vp, ctypes.c_float if precision == "f32" else ctypes.c_double]
+                                               + [ctypes.c_double] * 9 + [vp])
+            L.orc_source_array_force.argtypes = [ctypes.c_double] * 6 + [vp]
+            L.orc_realw_size.restype = ctypes.c_int
+            _LIBS[precision] = L
+        return _LIBS[precision]
+
+
+def _p(a: np.ndarray) -> int:
+    return a.ctypes.data
+
+
+def real_dtype(precision: str):
+    return np.float32 if precision == "f32" else np.float64
+
+
+class OracleSim:
+    """One oracle simulation: numpy arrays handed to the C struct by name."""
+
+    def __init__(self, precision: str = "f32"):
+        self.precision = precision
+        self.L = lib(precision)
+        self.h = self.L.orc_sim_new()
+        self._keep: dict = {}
+
+    def __del__(self):
+        try:
+            self.L.orc_sim_free(self.h)
+        except Exception:
+            pass
+
+    def set(self, name: str, arr: np.ndarray) -> np.ndarray:
+        if not arr.flags.c_contiguous:
+            arr = np.ascontiguousarray(arr)
+        self._keep[name] = arr
+        if self.L.orc_set_ptr(self.h, name.encode(), _p(arr)) != 0:
+            raise KeyError(name)
+        return arr
+
+    def get(self, name: str) -> np.ndarray:
+        return self._keep[name]
+
+    def seti(self, name: str, v: int) -> None:
+        if self.L.orc_set_int(self.h, name.encode(), int(v)) != 0:
+            raise KeyError(name)
+
+    def geti(self, name: str) -> int:
+        v = ctypes.c_int(0)
+        if self.L.orc_get_int(self.h, name.encode(), ctypes.byref(v)) != 0:
+            raise KeyError(name)
+        return v.value
+
+    def setr(self, name: str, v: float) -> None:
+        if self.L.orc_set_real(self.h, name.encode(), float(v)) != 0:
+            raise KeyError(name)
+
+    def step(self, n: int = 1) -> None:
+        self.L.orc_run(self.h, int(n))
+
+    def forces(self, backward: bool = False) -> None:
+        self.L.orc_compute_forces_elastic(self.h, int(backward))
+
+
+# ----------------------------------------------------------------------------
+# database generation restated from the reference (regular layered block)
+# ----------------------------------------------------------------------------
+
+def gll():
+    L = lib("f64")
+    x = np.zeros(NGLL)
+    w = np.zeros(NGLL)
+    L.orc_gll(_p(x), _p(w))
+    return x, w
+
+
+def derivation_matrices(precision: str = "f32"):
+    L = lib(precision)
+    rd = real_dtype(precision)
+    hp, hpw, wxy, wxz, wyz = (np.zeros(25, rd) for _ in range(5))
+    hpd = np.zeros(25)
+    L.orc_derivation_matrices(_p(hp), _p(hpw), _p(wxy), _p(wxz), _p(wyz), _p(hpd))
+    return dict(hprime_xx=hp, hprimewgll_xx=hpw, wgllwgll_xy=wxy, wgllwgll_xz=wxz, wgllwgll_yz=wyz,
+                hprime_d=hpd)
+
+
+def lagrange_any(xi: float):
+    L = lib("f64")
+    x, _ = gll()
+    h = np.zeros(NGLL)
+    hp = np.zeros(NGLL)
+    L.orc_lagrange_any(float(xi), _p(x), _p(h), _p(hp))
+    return h, hp
+
+
+def stf_table(kind: str, param: float, tshift: float, t0: float, dt: float, nstep: int) -> np.ndarray:
+    """FP64 source time function at t = (it-1) dt - t0 - tshift
+    (compute_add_sources_viscoelastic.F90:80-100)."""
+    L = lib("f64")
+    k = {"heaviside": 0, "ricker": 1, "gaussian": 2}[kind]
+    return np.array([L.orc_stf(k, (it - 1) * dt - t0 - tshift, param) for it in range(1, nstep + 1)])
+
+
+def build_database(cfg: dict, precision: str = "f32", material=None) -> dict:
+    """Run the restated setup chain for a regular layered block.
+
+    ``cfg`` uses the schema of :func:`specfem3d_gb300.meshgen.normalize_config`.
+    ``material`` optionally gives (rho, vp, vs) per GLL point (125*nspec each,
+    float32) for models that are not piecewise constant by layer.
+    """
+    L = lib(precision)
+    rd = real_dtype(precision)
+    nx, ny = int(cfg["nx"]), int(cfg["ny"])
+    zlev = np.asarray(cfg["zlev"], dtype=np.float64)
+    nz = len(zlev) - 1
+    nspec = nx * ny * nz
+    npt = NGLL3 * nspec
+    anchors = np.zeros(24 * nspec)
+    xs, ys, zs = np.zeros(npt), np.zeros(npt), np.zeros(npt)
+    L.orc_mesh_regular(nx, ny, nz, float(cfg["x0"]), float(cfg["x1"]), float(cfg["y0"]), float(cfg["y1"]),
+                       _p(zlev), _p(anchors), _p(xs), _p(ys), _p(zs))
+    ibool = np.zeros(npt, np.int32)
+    xtol = 1e-10 * abs(float(cfg["x1"]) - float(cfg["x0"]))
+    xc, yc, zc = xs.copy(), ys.copy(), zs.copy()
+    nglob = L.orc_get_global(npt, _p(xc), _p(yc), _p(zc), _p(ibool), xtol)
+    del xc, yc, zc
+    metric = [np.zeros(npt, rd) for _ in range(10)]
+    mptrs = (ctypes.c_void_p * 10)(*[_p(m) for m in metric])
+    irreg = np.zeros(nspec, np.int32)
+    xr = (ctypes.c_float if precision == "f32" else ctypes.c_double)(0)
+    jr = (ctypes.c_float if precision == "f32" else ctypes.c_double)(0)
+    nirr = L.orc_calc_jacobian_all(nspec, _p(anchors), ctypes.addressof(mptrs), _p(irreg),
+                                   ctypes.addressof(xr), ctypes.addressof(jr))
+    names = ["xix", "xiy", "xiz", "etax", "etay", "etaz", "gammax", "gammay", "gammaz", "jacobian"]
+    db = {n: m[: NGLL3 * max(nirr, 1)].copy() for n, m in zip(names, metric)}
+    db.update(nspec=nspec, nglob=nglob, nspec_irregular=nirr, ibool=ibool, irregular_element_number=irreg,
+              xix_regular=float(xr.value), jacobian_regular=float(jr.value), anchors=anchors,
+              xstore=xs, ystore=ys, zstore=zs)
+    # materials: per element layer, optionally per GLL point
+    if material is None:
+        lay = np.repeat(np.asarray(cfg["elem_layer"], np.int64), NGLL3)
+        rho = np.asarray([m["rho"] for m in cfg["layers"]], np.float32)[lay]
+        vp = np.asarray([m["vp"] for m in cfg["layers"]], np.float32)[lay]
+        vs = np.asarray([m["vs"] for m in cfg["layers"]], np.float32)[lay]
+    else:
+        rho, vp, vs = (np.asarray(a, np.float32) for a in material)
+    rho_r, vp_r, vs_r = rho.astype(rd), vp.astype(rd), vs.astype(rd)
+    db["rhostore"] = rho_r
+    db["kappastore"] = (rho_r * (vp_r * vp_r - rd(4.0 / 3.0) * vs_r * vs_r)).astype(rd)
+    db["mustore"] = (rho_r * vs_r * vs_r).astype(rd)
+    db["rho_vp"] = (rho_r * vp_r).astype(rd)
+    db["rho_vs"] = (rho_r * vs_r).astype(rd)
+    db["vp"] = vp
+    db["vs"] = vs
+    # absorbing faces: xmin, xmax, ymin, ymax, bottom (and top if requested)
+    faces = []
+    ex = np.arange(nspec) % nx
+    ey = (np.arange(nspec) // nx) % ny
+    ez = np.arange(nspec) // (nx * ny)
+    want = cfg.get("absorbing", ["xmin", "xmax", "ymin", "ymax", "bottom"])
+    conds = {"xmin": (1, ex == 0), "xmax": (2, ex == nx - 1), "ymin": (3, ey == 0), "ymax": (4, ey == ny - 1),
+             "bottom": (5, ez == 0), "top": (6, ez == nz - 1)}
+    for name in ["xmin", "xmax", "ymin", "ymax", "bottom", "top"]:
+        if name in want:
+            iface, sel = conds[name]
+            faces += [(int(e) + 1, iface) for e in np.nonzero(sel)[0]]
+    nf = len(faces)
+    abs_ispec = np.array([f[0] for f in faces], np.int32)
+    abs_ijk = np.zeros(3 * 25 * nf, np.int32)
+    abs_jw = np.zeros(25 * nf, rd)
+    abs_n = np.zeros(3 * 25 * nf, rd)
+    for f, (ispec, iface) in enumerate(faces):
+        ijk = np.zeros(75, np.int32)
+        jw = np.zeros(25, rd)
+        nn = np.zeros(75, rd)
+        L.orc_face_geometry(_p(anchors[24 * (ispec - 1):]), iface, _p(ijk), _p(jw), _p(nn))
+        abs_ijk[75 * f:75 * f + 75] = ijk
+        abs_jw[25 * f:25 * f + 25] = jw
+        abs_n[75 * f:75 * f + 75] = nn
+    db.update(num_abs_boundary_faces=nf, abs_boundary_ispec=abs_ispec, abs_boundary_ijk=abs_ijk,
+              abs_boundary_jacobian2Dw=abs_jw, abs_boundary_normal=abs_n)
+    # mass matrices
+    dt = float(cfg["dt"])
+    rmass = np.zeros(nglob, rd)
+    _mass_elastic(L, precision, nspec, nglob, db, rmass)
+    rmx, rmy, rmz = np.zeros(nglob, rd), np.zeros(nglob, rd), np.zeros(nglob, rd)
+    stacey = bool(cfg.get("stacey", True)) and nf > 0
+    if stacey:
+        L.orc_mass_stacey_elastic(nglob, dt, _p(ibool), _p(db["rho_vp"]), _p(db["rho_vs"]), nf, _p(abs_ispec),
+                                  _p(abs_ijk), _p(abs_n), _p(abs_jw), _p(rmx), _p(rmy), _p(rmz))
+    L.orc_invert_mass(nglob, _p(rmass), _p(rmx), _p(rmy), _p(rmz), int(stacey))
+    db.update(rmass=rmass, rmassx=rmx, rmassy=rmy, rmassz=rmz, stacey=int(stacey))
+    db.update(derivation_matrices(precision))
+    # sources and receivers
+    _sources_receivers(L, precision, cfg, db)
+    return db
+
+
+def _mass_elastic(L, precision, nspec, nglob, db, rmass):
+    fn = L.orc_mass_elastic
+    rt = ctypes.c_float if precision == "f32" else ctypes.c_double
+    fn.argtypes = [ctypes.c_int, ctypes.c_int] + [ctypes.c_void_p] * 4 + [rt, ctypes.c_void_p]
+    fn(nspec, nglob, _p(db["ibool"]), _p(db["rhostore"]), _p(db["jacobian"]), _p(db["irregular_element_number"]),
+       rt(db["jacobian_regular"]), _p(rmass))
+
+
+def _sources_receivers(L, precision, cfg, db):
+    rd = real_dtype(precision)
+    nspec = db["nspec"]
+    names = ["xix", "xiy", "xiz", "etax", "etay", "etaz", "gammax", "gammay", "gammaz", "jacobian"]
+    mptrs = (ctypes.c_void_p * 10)(*[_p(db[n]) for n in names])
+    xgl, _ = gll()
+    srcs = cfg.get("sources", [])
+    ns = len(srcs)
+    sa = np.zeros((ns, 3, NGLL3), rd)  # (isrc, c, ijk) -> stored (NSOURCES,3,5,5,5) column-major
+    isel = np.zeros(ns, np.int32)
+    loc = np.zeros((ns, 3))
+    for i, s in enumerate(srcs):
+        xi, eta, ga = ctypes.c_double(), ctypes.c_double(), ctypes.c_double()
+        ispec = L.orc_locate_point(nspec, _p(db["anchors"]), _p(db["xstore"]), _p(db["ystore"]), _p(db["zstore"]),
+                                   float(s["x"]), float(s["y"]), float(s["z"]), ctypes.addressof(xi),
+                                   ctypes.addressof(eta), ctypes.addressof(ga))
+        isel[i] = ispec
+        loc[i] = (xi.value, eta.value, ga.value)
+        out = np.zeros(3 * NGLL3, rd)
+        if s.get("type", "cmt") == "cmt":
+            Mxx, Myy, Mzz, Mxy, Mxz, Myz = (float(v) for v in s["M"])
+            rt = ctypes.c_float if precision == "f32" else ctypes.c_double
+            L.orc_source_array_cmt(ispec, _p(db["irregular_element_number"]), ctypes.addressof(mptrs),
+                                   rt(db["xix_regular"]), xi.value, eta.value, ga.value,
+                                   Mxx, Myy, Mzz, Mxy, Mxz, Myz, _p(out))
+        else:
+            f = [float(v) for v in s["F"]]
+            L.orc_source_array_force(xi.value, eta.value, ga.value, f[0], f[1], f[2], _p(out))
+        sa[i] = out.reshape(NGLL3, 3).T
+    # Fortran sourcearrays(NSOURCES,NDIM,NGLLX,NGLLY,NGLLZ): isrc fastest
+    db["sourcearrays"] = np.ascontiguousarray(sa.transpose(2, 1, 0)).reshape(-1)
+    db["ispec_selected_source"] = isel
+    db["source_xi_eta_gamma"] = loc
+    recs = cfg.get("receivers", [])
+    nr = len(recs)
+    irec = np.zeros(nr, np.int32)
+    hx, he, hg = np.zeros((nr, NGLL)), np.zeros((nr, NGLL)), np.zeros((nr, NGLL))
+    rloc = np.zeros((nr, 3))
+    for r, (x, y, z) in enumerate(recs):
+        xi, eta, ga = ctypes.c_double(), ctypes.c_double(), ctypes.c_double()
+        ispec = L.orc_locate_point(nspec, _p(db["anchors"]), _p(db["xstore"]), _p(db["ystore"]), _p(db["zstore"]),
+                                   float(x), float(y), float(z), ctypes.addressof(xi), ctypes.addressof(eta),
+                                   ctypes.addressof(ga))
+        irec[r] = ispec
+        rloc[r] = (xi.value, eta.value, ga.value)
+        hx[r], _ = lagrange_any(xi.value)
+        he[r], _ = lagrange_any(eta.value)
+        hg[r], _ = lagrange_any(ga.value)
+    db.update(ispec_selected_rec=irec, hxir=hx.reshape(-1), hetar=he.reshape(-1), hgammar=hg.reshape(-1),
+              receiver_xi_eta_gamma=rloc, nrec=nr, nsources=ns)
+
+
+def source_time_functions(cfg: dict) -> np.ndarray:
+    """(NSOURCES, NSTEP) FP64 table following setup_sources_receivers.f90:482-491
+    for t0 and get_stf_viscoelastic (compute_add_sources_viscoelastic.F90:837-932)."""
+    srcs = cfg.get("sources", [])
+    dt, nstep = float(cfg["dt"]), int(cfg["nstep"])
+    if not srcs:
+        return np.zeros((0, nstep))
+    kinds = [s.get("stf", "ricker") for s in srcs]
+    params = [float(s["f0"]) if k == "ricker" else float(s["hdur"]) for s, k in zip(srcs, kinds)]
+    tsh = np.array([float(s.get("tshift", 0.0)) for s in srcs])
+    tsh = tsh - tsh.min() if len(srcs) > 1 else np.zeros(1)
+    if all(k == "ricker" for k in kinds):
+        t0 = -1.2 * min(ts - 1.0 / p for ts, p in zip(tsh, params))
+    else:
+        t0 = -2.0 * min(ts - p for ts, p in zip(tsh, params))
+    if "t0" in cfg:
+        t0 = float(cfg["t0"])
+    return np.stack([stf_table(k, p, ts, t0, dt, nstep) for k, p, ts in zip(kinds, params, tsh)]), t0
+
+
+def make_sim(db: dict, cfg: dict, precision: str = "f32", nthreads: int = 1) -> OracleSim:
+    """Oracle forward simulation set up from database arrays (either the ones
+    from :func:`build_database` or the product's generator, same names)."""
+    rd = real_dtype(precision)
+    s = OracleSim(precision)
+    nspec, nglob = int(db["nspec"]), int(db["nglob"])
+    s.seti("nspec", nspec)
+    s.seti("nglob", nglob)
+    s.seti("nspec_irregular", int(db["nspec_irregular"]))
+    s.seti("nthreads", nthreads)
+    for n in ["ibool", "irregular_element_number", "abs_boundary_ispec", "abs_boundary_ijk", "ispec_selected_source",
+              "ispec_selected_rec"]:
+        s.set(n, np.asarray(db[n], np.int32))
+    for n in ["xix", "xiy", "xiz", "etax", "etay", "etaz", "gammax", "gammay", "gammaz", "jacobian", "kappastore",
+              "mustore", "rho_vp", "rho_vs", "rmassx", "rmassy", "rmassz", "hprime_xx", "hprimewgll_xx",
+              "wgllwgll_xy", "wgllwgll_xz", "wgllwgll_yz", "abs_boundary_normal", "abs_boundary_jacobian2Dw",
+              "sourcearrays"]:
+        s.set(n, np.asarray(db[n], rd))
+    for n in ["hxir", "hetar", "hgammar"]:
+        s.set(n, np.asarray(db[n], np.float64))
+    s.setr("xix_regular", db["xix_regular"])
+    s.setr("jacobian_regular", db["jacobian_regular"])
+    s.seti("num_abs_boundary_faces", int(db["num_abs_boundary_faces"]) if db.get("stacey", 1) else 0)
+    s.seti("stacey", int(db.get("stacey", 1)))
+    dt = float(cfg["dt"])
+    dtr = rd(dt)
+    s.setr("deltat", dtr)
+    s.setr("deltatover2", dtr / rd(2))
+    s.setr("deltatsqover2", dtr * dtr / rd(2))
+    nstep = int(cfg["nstep"])
+    s.seti("nstep", nstep)
+    ns = int(db["nsources"])
+    s.seti("nsources", ns)
+    if ns:
+        stf = np.asarray(db["stf"], np.float64).reshape(ns, nstep)
+        s.set("stf", np.ascontiguousarray(stf.T).reshape(-1))
+    nr = int(db["nrec"])
+    s.seti("nrec", nr)
+    if nr:
+        s.set("seismograms", np.zeros(3 * nr * nstep))
+    for n in ["displ", "veloc", "accel"]:
+        s.set(n, np.zeros(3 * nglob, rd))
+    att = int(db.get("attenuation", 0))
+    s.seti("attenuation", att)
+    s.seti("compute_and_store_strain", att)
+    if att:
+        for n in ["alphaval", "betaval", "gammaval", "factor_common", "factor_common_kappa"]:
+            s.set(n, np.asarray(db[n], rd))
+        for n in ["R_xx", "R_yy", "R_xy", "R_xz", "R_yz", "R_trace"]:
+            s.set(n, np.zeros(N_SLS * NGLL3 * nspec, rd))
+        for n in ["epsilondev_xx", "epsilondev_yy", "epsilondev_xy", "epsilondev_xz", "epsilondev_yz",
+                  "epsilondev_trace"]:
+            s.set(n, np.zeros(NGLL3 * nspec, rd))
+    return s
+
+
+def seismograms(sim: OracleSim) -> np.ndarray:
+    """(nrec, 3, nstep) traces recorded so far."""
+    nr, nstep = sim.geti("nrec"), sim.geti("nstep")
+    return sim.get("seismograms").reshape(nstep, nr, 3).transpose(1, 2, 0)

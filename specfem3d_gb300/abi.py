@@ -1,0 +1,135 @@
+"""ctypes binding of libspecfem3d_gb300.so.
+
+This is the binding a Python (or ctypes-speaking) caller uses; a Fortran solver
+links the same symbols directly (they carry gfortran's `name_` mangling).
+Loading fails loudly when the library has not been built: there is no CPU
+fallback behind this module.
+"""
+from __future__ import annotations
+
+import ctypes
+import os
+
+import numpy as np
+
+from . import build as _build
+
+P = ctypes.c_void_p
+_INT_P = ctypes.POINTER(ctypes.c_int)
+_LIB = None
+
+HEADER = os.path.join(os.path.dirname(os.path.dirname(os.path.abspath(__file__))), "include", "specfem3d_gb300.h")
+
+
+def header_signatures(path: str = HEADER) -> dict:
+    """{name: (return type, [argument declarations])} of every function declared
+    in include/specfem3d_gb300.h."""
+    import re
+    txt = open(path).read()
+    txt = re.sub(r"/\*.*?\*/", " ", txt, flags=re.S)
+    out = {}
+    for m in re.finditer(r"\b(void\s*\*\s*|void\s+|int\s+)(\w+)\s*\(([^;{]*?)\)\s*;", txt):
+        args = [a.strip() for a in m.group(3).split(",") if a.strip() and a.strip() != "void"]
+        out[m.group(2)] = (m.group(1).replace(" ", "").strip(), args)
+    return out
+
+
+# the reference-named entry points: void, every argument by reference
+_FC_VOID = {n: len(a) for n, (r, a) in header_signatures().items() if n.endswith("_") and r == "void"}
+
+
+def lib_path() -> str:
+    return _build.lib_path()
+
+
+def load() -> ctypes.CDLL:
+    """Load the CUDA library (raises if it is missing)."""
+    global _LIB
+    if _LIB is not None:
+        return _LIB
+    path = lib_path()
+    if not os.path.exists(path):
+        raise RuntimeError(f"{path} is missing: run specfem3d_gb300.build.build() (needs nvcc); "
+                           "there is no CPU fallback for the GPU path")
+    L = ctypes.CDLL(path)
+    for name, n in _FC_VOID.items():
+        f = getattr(L, name)
+        f.restype = None
+        f.argtypes = [P] * n
+    L.sf3d_last_error.restype = ctypes.c_int
+    L.sf3d_last_error.argtypes = [ctypes.c_char_p, ctypes.c_int]
+    L.sf3d_clear_error.restype = None
+    L.sf3d_version.restype = ctypes.c_int
+    L.sf3d_set_stf_table.restype = ctypes.c_int
+    L.sf3d_set_stf_table.argtypes = [P, P, ctypes.c_int, ctypes.c_int]
+    L.sf3d_iterate_time.restype = ctypes.c_int
+    L.sf3d_iterate_time.argtypes = [P, ctypes.c_int, ctypes.c_int, ctypes.c_float, ctypes.c_int, ctypes.c_int]
+    L.sf3d_get_seismograms.restype = ctypes.c_int
+    L.sf3d_get_seismograms.argtypes = [P, P]
+    L.sf3d_last_timing.restype = ctypes.c_int
+    L.sf3d_last_timing.argtypes = [P, P, P, P, P]
+    L.sf3d_synchronize.restype = ctypes.c_int
+    L.sf3d_synchronize.argtypes = [P]
+    L.sf3d_device_ptr.restype = P
+    L.sf3d_device_ptr.argtypes = [P, ctypes.c_char_p]
+    L.sf3d_check_stability.restype = ctypes.c_int
+    L.sf3d_check_stability.argtypes = [P, ctypes.c_float, P]
+    L.sf3d_get_kernels_f64.restype = ctypes.c_int
+    L.sf3d_get_kernels_f64.argtypes = [P, P, P, P]
+    _LIB = L
+    return L
+
+
+def exported_symbols():
+    return list(header_signatures())
+
+
+class SF3DError(RuntimeError):
+    pass
+
+
+def check() -> None:
+    """Raise SF3DError if the library recorded an error (and clear it)."""
+    L = load()
+    buf = ctypes.create_string_buffer(512)
+    code = L.sf3d_last_error(buf, 512)
+    if code != 0:
+        L.sf3d_clear_error()
+        raise SF3DError(f"specfem3d_gb300 error {code}: {buf.value.decode()}")
+
+
+# ---------------------------------------------------------------------------
+# by-reference argument helpers
+# ---------------------------------------------------------------------------
+
+class Args:
+    """Keeps the ctypes scalars / arrays of one call alive and hands out pointers."""
+
+    def __init__(self):
+        self._keep = []
+
+    def i(self, v) -> int:
+        c = ctypes.c_int(int(v))
+        self._keep.append(c)
+        return ctypes.addressof(c)
+
+    def f(self, v) -> int:
+        c = ctypes.c_float(float(v))
+        self._keep.append(c)
+        return ctypes.addressof(c)
+
+    def a(self, arr, dtype) -> int:
+        if arr is None:
+            arr = np.zeros(1, dtype)
+        arr = np.ascontiguousarray(arr, dtype=dtype)
+        self._keep.append(arr)
+        return arr.ctypes.data
+
+    def ai(self, arr) -> int:
+        return self.a(arr, np.int32)
+
+    def af(self, arr) -> int:
+        return self.a(arr, np.float32)
+
+    def ad(self, arr) -> int:
+        return self.a(arr, np.float64)

@@ -1,0 +1,206 @@
+"""Workload definitions: the synthetic meshes, models, sources and receivers.
+
+A configuration is a plain dict (the schema read by :mod:`specfem3d_gb300.meshgen`):
+
+``nx, ny``            elements along x and y
+``x0, x1, y0, y1``    horizontal extent (m)
+``zlev``              vertical node levels of the element layers, bottom to top (m)
+``elem_layer``        material layer of each element (len nx*ny*nz), or None
+``layers``            list of {rho, vp, vs[, Qmu, Qkappa]} per material layer
+``absorbing``         faces with Stacey conditions (free surface on the others)
+``sources``           list of {type: cmt|force, x, y, z, M: [Mxx,Myy,Mzz,Mxy,Mxz,Myz] (N.m)
+                      | F: [fx,fy,fz], stf: ricker|heaviside|gaussian, f0|hdur, tshift}
+``receivers``         list of (x, y, z)
+``dt, nstep``         time step and number of steps
+``attenuation``       bool (N_SLS = 3 standard linear solids)
+
+The named workloads follow the benchmark definitions of the project:
+``refex``  the reference's example homogeneous_halfspace_HEX8_elastic_absorbing_Stacey_5sides
+           (36x36x16 hexes over 134x134x60 km, DT 0.05, CMT with Heaviside stf);
+``cfg0``   homogeneous block 10x10x5 km, 24x24x12 hexes, Ricker 2 Hz CMT, 25 receivers;
+``cfg1``   layered viscoelastic 20x20x10 km, 128x128x64 hexes (~67.6 M points), 400 receivers;
+``cfg3``   64x64x32 hexes of the cfg1 domain without attenuation, 32 CMT shots.
+"""
+from __future__ import annotations
+
+import math
+
+import numpy as np
+
+COURANT_SUGGESTED = 0.5
+GLL_MIN_SPACING = (1.0 - math.sqrt(3.0 / 7.0)) / 2.0  # smallest GLL gap / element edge, NGLL=5
+
+
+def significant_dt(dt: float) -> float:
+    """Cut a suggested time step to two significant digits with the half-digit
+    rule of get_timestep_limit_significant_digit (shared/read_parameter_file.F90:1456-1497)."""
+    lpow = int(2.0 - math.log10(dt))
+    fac = 10.0 ** lpow
+    ival = int(fac * dt)
+    if fac * dt - ival >= 0.5:
+        return (ival + 0.5) / fac
+    return ival / fac
+
+
+def cfl_dt(cfg: dict) -> float:
+    """dt = COURANT_SUGGESTED * min GLL distance / vmax per element, minimum over
+    elements, rounded (shared/check_mesh_resolution.f90:278-300)."""
+    nx, ny = cfg["nx"], cfg["ny"]
+    dx = (cfg["x1"] - cfg["x0"]) / nx
+    dy = (cfg["y1"] - cfg["y0"]) / ny
+    zlev = np.asarray(cfg["zlev"])
+    best = math.inf
+    lay_of_ez = _layer_of_ez(cfg)
+    for ez in range(len(zlev) - 1):
+        dz = zlev[ez + 1] - zlev[ez]
+        lay = cfg["layers"][lay_of_ez[ez]]
+        vmax = max(lay["vp"], lay["vs"]) * cfg.get("vmax_factor", 1.0)
+        dmin = GLL_MIN_SPACING * min(dx, dy, dz)
+        best = min(best, significant_dt(COURANT_SUGGESTED * dmin / vmax))
+    return best
+
+
+def _layer_of_ez(cfg):
+    nz = len(cfg["zlev"]) - 1
+    if cfg.get("layer_counts"):
+        out = []
+        for li, n in enumerate(cfg["layer_counts"]):
+            out += [li] * n
+        return out
+    return [0] * nz
+
+
+def layered_zlev(z_bottom: float, interfaces_top_down, counts_top_down):
+    """Node levels for conforming layers: interfaces given top-down (z values,
+    first = top surface), element counts per layer top-down."""
+    tops = list(interfaces_top_down) + [z_bottom]
+    levels = []
+    for li in reversed(range(len(counts_top_down))):
+        za, zb, n = tops[li + 1], tops[li], counts_top_down[li]
+        seg = [za + (zb - za) * q / n for q in range(n)]
+        levels += seg
+    levels.append(tops[0])
+    return levels
+
+
+def random_moment_tensor(rng: np.random.Generator):
+    """Seeded N(0,1) symmetric 3x3 tensor normalised to unit Frobenius norm (N.m):
+    returns [Mxx, Myy, Mzz, Mxy, Mxz, Myz]."""
+    a = rng.standard_normal((3, 3))
+    m = 0.5 * (a + a.T)
+    m /= np.linalg.norm(m)
+    return [float(m[0, 0]), float(m[1, 1]), float(m[2, 2]), float(m[0, 1]), float(m[0, 2]), float(m[1, 2])]
+
+
+def finish(cfg: dict) -> dict:
+    """Fill derived fields (elem_layer, dt) of a configuration."""
+    nz = len(cfg["zlev"]) - 1
+    lay = _layer_of_ez(cfg)
+    if cfg.get("elem_layer") is None:
+        cfg["elem_layer"] = np.repeat(np.asarray(lay, np.int32), cfg["nx"] * cfg["ny"])
+    if cfg.get("dt") is None:
+        cfg["dt"] = cfl_dt(cfg)
+    cfg.setdefault("absorbing", ["xmin", "xmax", "ymin", "ymax", "bottom"])
+    cfg.setdefault("stacey", True)
+    cfg.setdefault("attenuation", False)
+    assert len(cfg["elem_layer"]) == cfg["nx"] * cfg["ny"] * nz
+    return cfg
+
+
+def refex(nstep: int = 5000) -> dict:
+    """The reference example homogeneous_halfspace_HEX8_elastic_absorbing_Stacey_5sides:
+    CMTSOLUTION (dyne.cm, r/t/p) mapped to x/y/z N.m (get_cmt.f90:424,
+    locate_source.F90:210-223); STATIONS lat -> y, lon -> x."""
+    Mrr, Mtt, Mpp, Mrt, Mrp, Mtp = -7.6e27, 7.7e27, -2.0e26, -2.5e28, 4.0e26, -2.5e27
+    s = 1e-7
+    M = [Mpp * s, Mtt * s, Mrr * s, -Mtp * s, Mrp * s, -Mrt * s]
+    cfg = dict(nx=36, ny=36, x0=0.0, x1=134000.0, y0=0.0, y1=134000.0,
+               zlev=list(np.linspace(-60000.0, 0.0, 17)), elem_layer=None,
+               layers=[dict(rho=2300.0, vp=2800.0, vs=1500.0)], dt=0.05, nstep=nstep,
+               sources=[dict(type="cmt", x=67000.0, y=67000.0, z=-30000.0, M=M, stf="heaviside", hdur=5.0)],
+               receivers=[(x, 67000.0, 0.0) for x in (22732.14, 34696.43, 46660.71, 58625.00)],
+               station_names=["X20", "X30", "X40", "X50"])
+    return finish(cfg)
+
+
+def cfg0(nstep: int = 2000, seed: int = 2024) -> dict:
+    rng = np.random.default_rng(seed)
+    g = np.linspace(1000.0, 9000.0, 5)
+    cfg = dict(nx=24, ny=24, x0=0.0, x1=10000.0, y0=0.0, y1=10000.0,
+               zlev=list(np.linspace(-5000.0, 0.0, 13)), elem_layer=None,
+               layers=[dict(rho=2300.0, vp=2800.0, vs=1500.0)], dt=None, nstep=nstep,
+               sources=[dict(type="cmt", x=5000.0, y=5000.0, z=-2500.0, M=random_moment_tensor(rng),
+                             stf="ricker", f0=2.0)],
+               receivers=[(float(x), float(y), 0.0) for y in g for x in g])
+    return finish(cfg)
+
+
+def cfg1(nstep: int = 4000, seed: int = 2025, nx: int = 128, ny: int = 128, counts=(13, 26, 25)) -> dict:
+    """Layered viscoelastic block; conforming vertical counts 13/26/25 (top-down)
+    make every element a non-cube box, i.e. the irregular-element path."""
+    rng = np.random.default_rng(seed)
+    zlev = layered_zlev(-10000.0, [0.0, -2000.0, -6000.0], list(counts))
+    layers = [dict(rho=2000.0, vp=2000.0, vs=1000.0, Qmu=40.0, Qkappa=9999.0),
+              dict(rho=2500.0, vp=4000.0, vs=2300.0, Qmu=150.0, Qkappa=9999.0),
+              dict(rho=2800.0, vp=6000.0, vs=3460.0, Qmu=400.0, Qkappa=9999.0)]
+    # layer index per element row, bottom to top
+    lay_bottom_up = []
+    for li in reversed(range(3)):
+        lay_bottom_up += [li] * counts[li]
+    g = np.linspace(500.0, 19500.0, 20)
+    cfg = dict(nx=nx, ny=ny, x0=0.0, x1=20000.0, y0=0.0, y1=20000.0, zlev=zlev,
+               layer_counts=None, elem_layer=np.repeat(np.asarray(lay_bottom_up, np.int32), nx * ny),
+               layers=layers, dt=None, nstep=nstep, attenuation=True,
+               sources=[dict(type="cmt", x=10000.0, y=10000.0, z=-8000.0, M=random_moment_tensor(rng),
+                             stf="ricker", f0=2.0)],
+               receivers=[(float(x), float(y), 0.0) for y in g for x in g])
+    cfg["dt"] = _cfl_dt_by_rows(cfg, lay_bottom_up)
+    return finish(cfg)
+
+
+def _cfl_dt_by_rows(cfg, lay_rows):
+    dx = (cfg["x1"] - cfg["x0"]) / cfg["nx"]
+    dy = (cfg["y1"] - cfg["y0"]) / cfg["ny"]
+    zlev = cfg["zlev"]
+    best = math.inf
+    for ez, li in enumerate(lay_rows):
+        dz = zlev[ez + 1] - zlev[ez]
+        lay = cfg["layers"][li]
+        dmin = GLL_MIN_SPACING * min(dx, dy, dz)
+        best = min(best, significant_dt(COURANT_SUGGESTED * dmin / max(lay["vp"], lay["vs"])))
+    return best
+
+
+def small_layered(nx=6, ny=5, counts=(2, 2, 3), nstep=200, attenuation=True, seed=7) -> dict:
+    """Small irregular (non-cube) layered block for parity tests (cfg1 physics)."""
+    cfg = cfg1(nstep=nstep, seed=seed, nx=nx, ny=ny, counts=counts)
+    cfg["x1"] = 20000.0 * nx / 128
+    cfg["y1"] = 20000.0 * ny / 128
+    z1 = -2000.0 * counts[0] / 13
+    z2 = z1 - 4000.0 * counts[1] / 26
+    cfg["zlev"] = layered_zlev(z2 - 4000.0 * counts[2] / 25, [0.0, z1, z2], list(counts))
+    lay_bottom_up = []
+    for li in reversed(range(3)):
+        lay_bottom_up += [li] * counts[li]
+    cfg["elem_layer"] = np.repeat(np.asarray(lay_bottom_up, np.int32), nx * ny)
+    cfg["attenuation"] = attenuation
+    cx, cy = cfg["x1"] / 2, cfg["y1"] / 2
+    cfg["sources"][0].update(x=cx + 37.0, y=cy - 21.0, z=0.55 * cfg["zlev"][0])
+    cfg["receivers"] = [(cx * 0.5, cy * 0.5, 0.0), (cx * 1.3, cy * 0.7, 0.0), (cx, cy, 0.5 * cfg["zlev"][0])]
+    cfg["dt"] = _cfl_dt_by_rows(cfg, lay_bottom_up)
+    return finish(cfg)
+
+
+def cfg3(nstep: int = 3000, nshots: int = 32, seed: int = 2026) -> dict:
+    rng = np.random.default_rng(seed)
+    zlev = list(np.linspace(-10000.0, 0.0, 33))
+    g = np.linspace(1000.0, 19000.0, 5)
+    shots = []
+    for _ in range(nshots):
+        shots.append(dict(type="cmt", x=float(rng.uniform(1000, 19000)), y=float(rng.uniform(1000, 19000)),
+                          z=-float(rng.uniform(2000, 8000)), M=random_moment_tensor(rng), stf="ricker", f0=2.0))
+    cfg = dict(nx=64, ny=64, x0=0.0, x1=20000.0, y0=0.0, y1=20000.0, zlev=zlev, elem_layer=None,
+               layers=[dict(rho=2400.0, vp=3000.0, vs=1700.0)], dt=None, nstep=nstep,
+               sources=shots[:1], shots=shots,
+               receivers=[(float(x), float(y), 0.0) for y in g for x in g], vmax_factor=1.05)
+    return finish(cfg)

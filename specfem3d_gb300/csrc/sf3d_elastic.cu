@@ -1,0 +1,268 @@
+// Elastic / viscoelastic stiffness kernel (sm_103a).
+//
+// Computes, for every element of a phase list, the weak-form internal force
+// exactly as compute_forces_viscoelastic.F90:250-860 does on the CPU:
+//   gather u (and dt*v with attenuation) through ibool -> 5-wide derivative
+//   contractions with hprime -> metric -> strain, isotropic stress minus the
+//   memory variables -> J sigma grad(xi) -> transposed contractions with
+//   hprimewgll -> weighted scatter-add (red.global.add.f32) into accel ->
+//   memory-variable update (compute_element_att_memory.f90:28-157).
+//
+// Mapping: one 128-thread CTA per element, thread p < 125 owns GLL point
+// p = i + 5j + 25k.  Every per-element HBM stream (ibool, metric, moduli,
+// memory variables, strains, attenuation factors) is one aligned 512-byte row
+// per array and is issued before the first barrier, so each CTA keeps its
+// whole element (up to ~21 KB) in flight; the contractions exchange values
+// through shared memory.  The 5-wide contractions stay on the FP32 pipes: they
+// are far too small to feed the tensor cores.
+#include "sf3d_internal.h"
+
+namespace sf3d {
+
+namespace {
+
+template <bool ATT, bool STRAIN>
+__global__ void __launch_bounds__(NGLL3_PAD, 4) stiffness_kernel(const StiffnessArgs a) {
+  __shared__ float s_gll[NGLL3];
+  __shared__ float s_u[3][NGLL3_PAD];
+  __shared__ float s_v[ATT ? 3 : 1][NGLL3_PAD];
+  __shared__ float s_t[9][NGLL3_PAD];
+
+  const int t = threadIdx.x;
+  const int e = a.phase ? __ldg(a.phase + blockIdx.x) : (int)blockIdx.x;
+  const bool active = t < NGLL3;
+  const int k = t / NGLL2, j = (t / NGLLX) % NGLLX, i = t % NGLLX;
+  const long eo = (long)e * NGLL3_PAD + t;
+  const int ir = __ldg(a.irregular + e);
+
+  // ---- issue every HBM load of this element up front ------------------------
+  int iglob = 0;
+  float ux = 0.f, uy = 0.f, uz = 0.f, vx = 0.f, vy = 0.f, vz = 0.f;
+  float m[9];
+#pragma unroll
+  for (int q = 0; q < 9; ++q) m[q] = 0.f;
+  float kap = 0.f, mu = 0.f;
+  float R[6][NSLS], eold[6], fc[NSLS], fck[NSLS];
+#pragma unroll
+  for (int c = 0; c < 6; ++c) {
+    eold[c] = 0.f;
+#pragma unroll
+    for (int s = 0; s < NSLS; ++s) R[c][s] = 0.f;
+  }
+#pragma unroll
+  for (int s = 0; s < NSLS; ++s) fc[s] = fck[s] = 0.f;
+  if (active) {
+    iglob = __ldg(a.ibool + eo);
+    kap = __ldg(a.kappav + eo);
+    mu = __ldg(a.muv + eo);
+    if (ir >= 0) {
+      const long mo = (long)ir * NGLL3_PAD + t;
+#pragma unroll
+      for (int q = 0; q < 9; ++q) m[q] = __ldg(a.m[q] + mo);
+    }
+    if (ATT) {
+      const long so = (long)e * (NSLS * NGLL3_PAD) + t;
+#pragma unroll
+      for (int c = 0; c < 6; ++c)
+#pragma unroll
+        for (int s = 0; s < NSLS; ++s) R[c][s] = a.R[c][so + s * NGLL3_PAD];
+#pragma unroll
+      for (int c = 0; c < 6; ++c) eold[c] = a.eps[c][eo];
+#pragma unroll
+      for (int s = 0; s < NSLS; ++s) {
+        fc[s] = __ldg(a.fc + so + s * NGLL3_PAD);
+        fck[s] = __ldg(a.fck + so + s * NGLL3_PAD);
+      }
+    }
+    ux = a.displ[3L * iglob];
+    uy = a.displ[3L * iglob + 1];
+    uz = a.displ[3L * iglob + 2];
+    if (ATT) {
+      vx = a.deltat * a.veloc[3L * iglob];
+      vy = a.deltat * a.veloc[3L * iglob + 1];
+      vz = a.deltat * a.veloc[3L * iglob + 2];
+    }
+  }
+  if (t < NGLL3) s_gll[t] = __ldg(a.gll + t);
+  s_u[0][t] = ux;
+  s_u[1][t] = uy;
+  s_u[2][t] = uz;
+  if (ATT) {
+    s_v[0][t] = vx;
+    s_v[1][t] = vy;
+    s_v[2][t] = vz;
+  }
+  __syncthreads();
+
+  // ---- gradient, strain, stress ---------------------------------------------
+  float epsl[6] = {0.f, 0.f, 0.f, 0.f, 0.f, 0.f};
+  if (active) {
+    const float* hp = s_gll;  // hprime(i2,i1) = hp[i2 + 5 i1]
+    float t1x = 0.f, t2x = 0.f, t3x = 0.f, t1y = 0.f, t2y = 0.f, t3y = 0.f, t1z = 0.f, t2z = 0.f, t3z = 0.f;
+#pragma unroll
+    for (int l = 0; l < NGLLX; ++l) {
+      const float h1 = hp[i + NGLLX * l], h2 = hp[j + NGLLX * l], h3 = hp[k + NGLLX * l];
+      const int p1 = l + NGLLX * j + NGLL2 * k, p2 = i + NGLLX * l + NGLL2 * k, p3 = i + NGLLX * j + NGLL2 * l;
+      t1x = fmaf(s_u[0][p1], h1, t1x); t1y = fmaf(s_u[1][p1], h1, t1y); t1z = fmaf(s_u[2][p1], h1, t1z);
+      t2x = fmaf(s_u[0][p2], h2, t2x); t2y = fmaf(s_u[1][p2], h2, t2y); t2z = fmaf(s_u[2][p2], h2, t2z);
+      t3x = fmaf(s_u[0][p3], h3, t3x); t3y = fmaf(s_u[1][p3], h3, t3y); t3z = fmaf(s_u[2][p3], h3, t3z);
+    }
+    float a1x = t1x, a2x = t2x, a3x = t3x, a1y = t1y, a2y = t2y, a3y = t3y, a1z = t1z, a2z = t2z, a3z = t3z;
+    if (ATT) {
+#pragma unroll
+      for (int l = 0; l < NGLLX; ++l) {
+        const float h1 = hp[i + NGLLX * l], h2 = hp[j + NGLLX * l], h3 = hp[k + NGLLX * l];
+        const int p1 = l + NGLLX * j + NGLL2 * k, p2 = i + NGLLX * l + NGLL2 * k, p3 = i + NGLLX * j + NGLL2 * l;
+        a1x = fmaf(s_v[0][p1], h1, a1x); a1y = fmaf(s_v[1][p1], h1, a1y); a1z = fmaf(s_v[2][p1], h1, a1z);
+        a2x = fmaf(s_v[0][p2], h2, a2x); a2y = fmaf(s_v[1][p2], h2, a2y); a2z = fmaf(s_v[2][p2], h2, a2z);
+        a3x = fmaf(s_v[0][p3], h3, a3x); a3y = fmaf(s_v[1][p3], h3, a3y); a3z = fmaf(s_v[2][p3], h3, a3z);
+      }
+    }
+    const float xr = a.xix_regular;
+    const float xix = m[0], xiy = m[1], xiz = m[2], etax = m[3], etay = m[4], etaz = m[5];
+    const float gammax = m[6], gammay = m[7], gammaz = m[8];
+    float dxx, dxy, dxz, dyx, dyy, dyz, dzx, dzy, dzz;
+    if (ir >= 0) {
+      dxx = xix * t1x + etax * t2x + gammax * t3x;
+      dxy = xiy * t1x + etay * t2x + gammay * t3x;
+      dxz = xiz * t1x + etaz * t2x + gammaz * t3x;
+      dyx = xix * t1y + etax * t2y + gammax * t3y;
+      dyy = xiy * t1y + etay * t2y + gammay * t3y;
+      dyz = xiz * t1y + etaz * t2y + gammaz * t3y;
+      dzx = xix * t1z + etax * t2z + gammax * t3z;
+      dzy = xiy * t1z + etay * t2z + gammay * t3z;
+      dzz = xiz * t1z + etaz * t2z + gammaz * t3z;
+    } else {
+      dxx = xr * t1x; dxy = xr * t2x; dxz = xr * t3x;
+      dyx = xr * t1y; dyy = xr * t2y; dyz = xr * t3y;
+      dzx = xr * t1z; dzy = xr * t2z; dzz = xr * t3z;
+    }
+    if (STRAIN) {
+      float sxx, sxy, sxz, syx, syy, syz, szx, szy, szz;
+      if (ATT) {
+        if (ir >= 0) {
+          sxx = xix * a1x + etax * a2x + gammax * a3x;
+          sxy = xiy * a1x + etay * a2x + gammay * a3x;
+          sxz = xiz * a1x + etaz * a2x + gammaz * a3x;
+          syx = xix * a1y + etax * a2y + gammax * a3y;
+          syy = xiy * a1y + etay * a2y + gammay * a3y;
+          syz = xiz * a1y + etaz * a2y + gammaz * a3y;
+          szx = xix * a1z + etax * a2z + gammax * a3z;
+          szy = xiy * a1z + etay * a2z + gammay * a3z;
+          szz = xiz * a1z + etaz * a2z + gammaz * a3z;
+        } else {
+          sxx = xr * a1x; sxy = xr * a2x; sxz = xr * a3x;
+          syx = xr * a1y; syy = xr * a2y; syz = xr * a3y;
+          szx = xr * a1z; szy = xr * a2z; szz = xr * a3z;
+        }
+      } else {
+        sxx = dxx; sxy = dxy; sxz = dxz; syx = dyx; syy = dyy; syz = dyz; szx = dzx; szy = dzy; szz = dzz;
+      }
+      const float templ = (1.f / 3.f) * (sxx + syy + szz);
+      epsl[5] = sxx + syy + szz;
+      epsl[0] = sxx - templ;
+      epsl[1] = syy - templ;
+      epsl[2] = 0.5f * (sxy + syx);
+      epsl[3] = 0.5f * (szx + sxz);
+      epsl[4] = 0.5f * (szy + syz);
+      if (a.eps_trace_over_3) a.eps_trace_over_3[eo] = templ;
+    }
+    const float l2m = kap + (4.f / 3.f) * mu;
+    const float lam = l2m - 2.f * mu;
+    float sig_xx = l2m * dxx + lam * (dyy + dzz);
+    float sig_yy = l2m * dyy + lam * (dxx + dzz);
+    float sig_zz = l2m * dzz + lam * (dxx + dyy);
+    float sig_xy = mu * (dxy + dyx);
+    float sig_xz = mu * (dzx + dxz);
+    float sig_yz = mu * (dzy + dyz);
+    if (ATT) {
+      float sR[6];
+#pragma unroll
+      for (int c = 0; c < 6; ++c) sR[c] = R[c][0] + R[c][1] + R[c][2];
+      sig_xx = sig_xx - sR[0] - sR[5];
+      sig_yy = sig_yy - sR[1] - sR[5];
+      sig_zz = sig_zz + sR[0] + sR[1] - sR[5];
+      sig_xy -= sR[2];
+      sig_xz -= sR[3];
+      sig_yz -= sR[4];
+    }
+    if (ir >= 0) {
+      // the device recomputes J = 1/det(d xi / d x) from the stored metric
+      const float jac = 1.f / (xix * (etay * gammaz - etaz * gammay) - xiy * (etax * gammaz - etaz * gammax) +
+                               xiz * (etax * gammay - etay * gammax));
+      s_t[0][t] = jac * (sig_xx * xix + sig_xy * xiy + sig_xz * xiz);
+      s_t[1][t] = jac * (sig_xy * xix + sig_yy * xiy + sig_yz * xiz);
+      s_t[2][t] = jac * (sig_xz * xix + sig_yz * xiy + sig_zz * xiz);
+      s_t[3][t] = jac * (sig_xx * etax + sig_xy * etay + sig_xz * etaz);
+      s_t[4][t] = jac * (sig_xy * etax + sig_yy * etay + sig_yz * etaz);
+      s_t[5][t] = jac * (sig_xz * etax + sig_yz * etay + sig_zz * etaz);
+      s_t[6][t] = jac * (sig_xx * gammax + sig_xy * gammay + sig_xz * gammaz);
+      s_t[7][t] = jac * (sig_xy * gammax + sig_yy * gammay + sig_yz * gammaz);
+      s_t[8][t] = jac * (sig_xz * gammax + sig_yz * gammay + sig_zz * gammaz);
+    } else {
+      const float js = a.jacobian_regular * xr;
+      s_t[0][t] = js * sig_xx; s_t[1][t] = js * sig_xy; s_t[2][t] = js * sig_xz;
+      s_t[3][t] = js * sig_xy; s_t[4][t] = js * sig_yy; s_t[5][t] = js * sig_yz;
+      s_t[6][t] = js * sig_xz; s_t[7][t] = js * sig_yz; s_t[8][t] = js * sig_zz;
+    }
+  }
+  __syncthreads();
+
+  // ---- transposed contractions and scatter-add --------------------------------
+  if (active) {
+    const float* hpw = s_gll + NGLL2;  // hprimewgll(i2,i1) = hpw[i2 + 5 i1]
+    float n1x = 0.f, n2x = 0.f, n3x = 0.f, n1y = 0.f, n2y = 0.f, n3y = 0.f, n1z = 0.f, n2z = 0.f, n3z = 0.f;
+#pragma unroll
+    for (int l = 0; l < NGLLX; ++l) {
+      const float f1 = hpw[l + NGLLX * i], f2 = hpw[l + NGLLX * j], f3 = hpw[l + NGLLX * k];
+      const int p1 = l + NGLLX * j + NGLL2 * k, p2 = i + NGLLX * l + NGLL2 * k, p3 = i + NGLLX * j + NGLL2 * l;
+      n1x = fmaf(s_t[0][p1], f1, n1x); n1y = fmaf(s_t[1][p1], f1, n1y); n1z = fmaf(s_t[2][p1], f1, n1z);
+      n2x = fmaf(s_t[3][p2], f2, n2x); n2y = fmaf(s_t[4][p2], f2, n2y); n2z = fmaf(s_t[5][p2], f2, n2z);
+      n3x = fmaf(s_t[6][p3], f3, n3x); n3y = fmaf(s_t[7][p3], f3, n3y); n3z = fmaf(s_t[8][p3], f3, n3z);
+    }
+    const float fac1 = s_gll[4 * NGLL2 + j + NGLLX * k];  // wgllwgll_yz(j,k)
+    const float fac2 = s_gll[3 * NGLL2 + i + NGLLX * k];  // wgllwgll_xz(i,k)
+    const float fac3 = s_gll[2 * NGLL2 + i + NGLLX * j];  // wgllwgll_xy(i,j)
+    const float ax = fac1 * n1x + fac2 * n2x + fac3 * n3x;
+    const float ay = fac1 * n1y + fac2 * n2y + fac3 * n3y;
+    const float az = fac1 * n1z + fac2 * n2z + fac3 * n3z;
+    atomicAdd(a.accel + 3L * iglob, -ax);
+    atomicAdd(a.accel + 3L * iglob + 1, -ay);
+    atomicAdd(a.accel + 3L * iglob + 2, -az);
+
+    if (ATT) {
+      const long so = (long)e * (NSLS * NGLL3_PAD) + t;
+      const float fkap = kap, fmu = mu;
+#pragma unroll
+      for (int s = 0; s < NSLS; ++s) {
+        const float al = a.alpha[s], be = a.beta[s], ga = a.gamma[s];
+        const float fk = fkap * fck[s];
+        a.R[5][so + s * NGLL3_PAD] = al * R[5][s] + fk * (be * eold[5] + ga * epsl[5]);
+        const float fm = fmu * fc[s];
+#pragma unroll
+        for (int c = 0; c < 5; ++c) a.R[c][so + s * NGLL3_PAD] = al * R[c][s] + fm * (be * eold[c] + ga * epsl[c]);
+      }
+    }
+    if (STRAIN) {
+      if (ATT) a.eps[5][eo] = epsl[5];
+#pragma unroll
+      for (int c = 0; c < 5; ++c)
+        if (a.eps[c]) a.eps[c][eo] = epsl[c];
+    }
+  }
+}
+
+}  // namespace
+
+void launch_stiffness(const StiffnessArgs& a, bool att, bool store_strain, cudaStream_t s) {
+  if (a.nelem <= 0) return;
+  dim3 grid(a.nelem), block(NGLL3_PAD);
+  if (att)
+    stiffness_kernel<true, true><<<grid, block, 0, s>>>(a);
+  else if (store_strain)
+    stiffness_kernel<false, true><<<grid, block, 0, s>>>(a);
+  else
+    stiffness_kernel<false, false><<<grid, block, 0, s>>>(a);
+}
+
+}  // namespace sf3d

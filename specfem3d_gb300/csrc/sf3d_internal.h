@@ -1,0 +1,189 @@
+// Internal definitions of the GB300 spectral-element library.
+//
+// Device layout (chosen for coalesced, 16-byte-aligned element streams on HBM):
+//   * per-element arrays are stored element-major with a 128-point stride
+//     (125 GLL points + 3 pad), so each element's array is one aligned 512-byte
+//     row: ibool[e*128 + p] (0-based global index), kappa/mu[e*128 + p],
+//     metric m[e_irr*128 + p] for irregular elements only;
+//   * attenuation memory variables are [e][sls][128] (three 512-byte rows per
+//     element and component), epsilondev [e][128];
+//   * wavefields keep the reference's interleaved (3, NGLOB) layout so the
+//     host transfers of the Fortran arrays are plain copies.
+#pragma once
+
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+#include <string>
+#include <vector>
+
+#include "../../include/specfem3d_gb300.h"
+
+#define NGLLX 5
+#define NGLL2 25
+#define NGLL3 125
+#define NGLL3_PAD 128
+#define NSLS 3
+
+namespace sf3d {
+
+// Records the first error; returns false on failure so callers can bail out.
+bool set_error(int code, const std::string& msg);
+bool cuda_ok(cudaError_t e, const char* what);
+#define SF3D_CUDA(call)                           \
+  do {                                            \
+    if (!::sf3d::cuda_ok((call), #call)) return;  \
+  } while (0)
+#define SF3D_CUDA_RET(call, ret)                      \
+  do {                                                \
+    if (!::sf3d::cuda_ok((call), #call)) return ret;  \
+  } while (0)
+
+struct Fields {
+  float* displ = nullptr;
+  float* veloc = nullptr;
+  float* accel = nullptr;
+  // attenuation memory variables [e][sls][128] and strains [e][128]
+  float* R[6] = {nullptr, nullptr, nullptr, nullptr, nullptr, nullptr};  // xx yy xy xz yz trace
+  float* eps[6] = {nullptr, nullptr, nullptr, nullptr, nullptr, nullptr};  // xx yy xy xz yz trace
+  float* eps_trace_over_3 = nullptr;                                      // [e][128]
+};
+
+struct Mesh {
+  int nspec = 0, nglob = 0, nspec_irregular = 0;
+  float xix_regular = 0.f, jacobian_regular = 0.f;
+  int simulation_type = 1;
+  int save_forward = 0;
+
+  // geometry / material (element-major, 128 stride)
+  int* d_ibool = nullptr;                // [nspec][128] 0-based
+  int* d_irregular = nullptr;            // [nspec] 0-based irregular index, -1 if regular
+  float* d_metric[9] = {};               // [nspec_irr][128] xix xiy xiz etax etay etaz gammax gammay gammaz
+  float* d_kappav = nullptr;             // [nspec][128]
+  float* d_muv = nullptr;                // [nspec][128]
+  float* d_rho_vp = nullptr;             // [nspec][128]
+  float* d_rho_vs = nullptr;             // [nspec][128]
+  float* d_rmassx = nullptr;             // [nglob]
+  float* d_rmassy = nullptr;
+  float* d_rmassz = nullptr;
+  float h_hprime[25] = {}, h_hprimewgll[25] = {}, h_wxy[25] = {}, h_wxz[25] = {}, h_wyz[25] = {};
+  float* d_gll = nullptr;                // [5*25]: hprime, hprimewgll, wxy, wxz, wyz
+
+  // phases: [2][num_phase_ispec] 0-based element lists
+  int num_phase_ispec = 0;
+  int nspec_outer = 0, nspec_inner = 0;
+  int* d_phase_ispec = nullptr;
+
+  // Stacey
+  int stacey = 0;
+  int num_abs_faces = 0;
+  int* d_abs_ispec = nullptr;            // [nf] 0-based
+  int* d_abs_pt = nullptr;               // [nf][25] element-local point index p = i+5j+25k
+  float* d_abs_normal = nullptr;         // [nf][25][3]
+  float* d_abs_jw = nullptr;             // [nf][25]
+
+  // sources
+  int nsources = 0, nsources_local = 0;
+  float* d_sourcearrays = nullptr;       // [nsrc][128][3] (point-major, xyz innermost)
+  int* d_ispec_src = nullptr;            // [nsrc] 0-based
+  int* h_ispec_src = nullptr;
+  float* d_stf_step = nullptr;           // [nsrc] stf of the current ABI call
+  float* d_stf_table = nullptr;          // [nstep][nsrc]
+  int stf_nstep = 0;
+
+  // receivers
+  int nrec = 0, nrec_local = 0;
+  int nlength_seismogram = 0;
+  int save_d = 0, save_v = 0, save_a = 0, save_p = 0;
+  int* d_ispec_rec = nullptr;            // [nrec_local] 0-based
+  float* d_hxir = nullptr;               // [nrec_local][5] each
+  float* d_hetar = nullptr;
+  float* d_hgammar = nullptr;
+  float* d_nu_rec = nullptr;             // [nrec_local][9]
+  float* d_seismo_d = nullptr;           // (3, nrec_local, nlength)
+  float* d_seismo_v = nullptr;
+  float* d_seismo_a = nullptr;
+
+  // attenuation
+  int attenuation = 0;
+  int compute_and_store_strain = 0;
+  float alphaval[NSLS] = {}, betaval[NSLS] = {}, gammaval[NSLS] = {};
+  float b_alphaval[NSLS] = {}, b_betaval[NSLS] = {}, b_gammaval[NSLS] = {};
+  float* d_factor_common = nullptr;      // [nspec][3][128]
+  float* d_factor_common_kappa = nullptr;
+
+  Fields f;   // forward (or adjoint) field
+  Fields b;   // backward / reconstructed field (SIMULATION_TYPE == 3)
+
+  // adjoint kernels (SIMULATION_TYPE == 3): [nspec][128], FP64 accumulation
+  double* d_rho_kl = nullptr;
+  double* d_mu_kl = nullptr;
+  double* d_kappa_kl = nullptr;
+  int nadj_rec_local = 0;
+  int ntstep_between_read_adjsrc = 0;
+  int* d_ispec_adj = nullptr;             // [nadj_rec_local] 0-based
+  float* d_hxir_adj = nullptr;            // [nadj][5]
+  float* d_hetar_adj = nullptr;
+  float* d_hgammar_adj = nullptr;
+  float* d_source_adjoint = nullptr;      // (3, nadj, NTSTEP_BETWEEN_READ_ADJSRC)
+
+  // device step counter for graph-captured time loops, and completion counter
+  int* d_it = nullptr;
+  unsigned long long* d_stamps = nullptr;  // per-step stiffness start/end (globaltimer ns)
+  unsigned int* d_done = nullptr;
+  float* d_scratch = nullptr;             // reduction scratch
+
+  cudaStream_t stream = nullptr;
+  cudaEvent_t ev0 = nullptr, ev1 = nullptr;
+  float last_stiff_ms = 0.f, last_total_ms = 0.f;
+  int last_stiff_launches = 0, last_total_launches = 0;
+
+  // staging buffer for layout conversions
+  float* d_stage = nullptr;
+  size_t stage_bytes = 0;
+};
+
+inline Mesh* get_mesh(long* p) {
+  if (!p || *p == 0) {
+    set_error(SF3D_ERR_STATE, "Mesh_pointer is not prepared");
+    return nullptr;
+  }
+  return reinterpret_cast<Mesh*>(*p);
+}
+
+// element-major upload of a (5,5,5,n) host array into [n][128]
+bool upload_padded(float** d, const float* h, long n, cudaStream_t s);
+bool upload_padded_int_minus1(int** d, const int* h, long n, cudaStream_t s);
+bool upload_sls_padded(float** d, const float* h, long n, cudaStream_t s);
+bool download_padded(float* h, const float* d, long n, Mesh* mp);
+bool download_sls_padded(float* h, const float* d, long n, Mesh* mp);
+bool alloc_zero(void** d, size_t bytes);
+bool ensure_stage(Mesh* mp, size_t bytes);
+
+// kernels launched from several translation units
+struct StiffnessArgs {
+  int nelem;
+  const int* phase;             // element list (0-based) or nullptr (identity)
+  const int* ibool;
+  const int* irregular;
+  const float* m[9];
+  const float* kappav;
+  const float* muv;
+  const float* gll;             // hprime, hprimewgll, wxy, wxz, wyz
+  float xix_regular;
+  float jacobian_regular;
+  float deltat;
+  const float* displ;
+  const float* veloc;
+  float* accel;
+  float* R[6];
+  float* eps[6];
+  float* eps_trace_over_3;
+  const float* fc;
+  const float* fck;
+  float alpha[NSLS], beta[NSLS], gamma[NSLS];
+};
+
+void launch_stiffness(const StiffnessArgs& a, bool att, bool store_strain, cudaStream_t s);
+
+}  // namespace sf3d

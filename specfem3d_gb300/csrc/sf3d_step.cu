@@ -1,0 +1,624 @@
+// Time scheme, boundary terms, sources, receivers and the graph-captured
+// forward time loop.
+//
+// Per-call entry points keep the semantics of the reference's
+// update_displacement_cuda.cu, compute_forces_viscoelastic_cuda.cu,
+// compute_stacey_viscoelastic_cuda.cu, compute_add_sources_viscoelastic_cuda.cu
+// and write_seismograms_cuda.cu.  sf3d_iterate_time replaces the Fortran
+// time loop (iterate_time.F90:219-330) for the forward elastic case: it fuses
+// the corrector of step n-1 with the predictor of step n into one streaming
+// pass, reads the step index from device memory, and captures blocks of steps
+// into CUDA graphs so a step costs four graph nodes and no host round trip.
+#include <math.h>
+#include <string.h>
+
+#include <vector>
+
+#include "sf3d_internal.h"
+
+namespace sf3d {
+namespace {
+
+inline unsigned nblk(long n, int b) { return (unsigned)((n + b - 1) / b); }
+
+// Newmark predictor (update_displacement_scheme.f90:359-410,
+// kernels/UpdateDispVeloc_kernel.cu): u += dt v + dt^2/2 a; v += dt/2 a; a = 0.
+__global__ void predictor_kernel(float* __restrict__ d, float* __restrict__ v, float* __restrict__ a, long n,
+                                 float dt, float dt2, float dtsq2) {
+  long i = (long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  const float ai = a[i], vi = v[i];
+  d[i] = d[i] + dt * vi + dtsq2 * ai;
+  v[i] = vi + dt2 * ai;
+  a[i] = 0.f;
+}
+
+// Mass matrix + corrector (kernels/kernel_3_cuda_device.cu,
+// compute_forces_viscoelastic_calling_routine.F90:369-416).
+__global__ void mass_corrector_kernel(float* __restrict__ v, float* __restrict__ a, const float* __restrict__ rmx,
+                                      const float* __restrict__ rmy, const float* __restrict__ rmz, long nglob,
+                                      float dt2) {
+  long g = (long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (g >= nglob) return;
+  const float ax = a[3 * g] * rmx[g], ay = a[3 * g + 1] * rmy[g], az = a[3 * g + 2] * rmz[g];
+  a[3 * g] = ax; a[3 * g + 1] = ay; a[3 * g + 2] = az;
+  v[3 * g] += dt2 * ax; v[3 * g + 1] += dt2 * ay; v[3 * g + 2] += dt2 * az;
+}
+
+__global__ void corrector_kernel(float* __restrict__ v, const float* __restrict__ a, long n, float dt2) {
+  long i = (long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  v[i] += dt2 * a[i];
+}
+
+// Corrector of step n-1 fused with the predictor of step n: one read and one
+// write of u, v, a per point instead of two passes.  Arithmetic per value is
+// identical to mass_corrector_kernel followed by predictor_kernel.
+__global__ void corrector_predictor_kernel(float* __restrict__ d, float* __restrict__ v, float* __restrict__ a,
+                                           const float* __restrict__ rmx, const float* __restrict__ rmy,
+                                           const float* __restrict__ rmz, long nglob, float dt, float dt2,
+                                           float dtsq2) {
+  long g = (long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (g >= nglob) return;
+  const float rm[3] = {rmx[g], rmy[g], rmz[g]};
+#pragma unroll
+  for (int c = 0; c < 3; ++c) {
+    const long i = 3 * g + c;
+    const float ac = a[i] * rm[c];
+    const float vh = v[i] + dt2 * ac;
+    d[i] = d[i] + dt * vh + dtsq2 * ac;
+    v[i] = vh + dt2 * ac;
+    a[i] = 0.f;
+  }
+}
+
+// Stacey absorbing traction (compute_stacey_viscoelastic.F90:90-130,
+// kernels/compute_stacey_elastic_kernel.cu): one thread per face GLL point.
+__global__ void stacey_kernel(int nfaces, const int* __restrict__ abs_ispec, const int* __restrict__ abs_pt,
+                              const float* __restrict__ normal, const float* __restrict__ jw,
+                              const int* __restrict__ ibool, const float* __restrict__ rho_vp,
+                              const float* __restrict__ rho_vs, const float* __restrict__ veloc,
+                              float* __restrict__ accel, float* __restrict__ record) {
+  long idx = (long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (idx >= (long)nfaces * NGLL2) return;
+  const int f = (int)(idx / NGLL2);
+  const int e = abs_ispec[f];
+  const long q = (long)e * NGLL3_PAD + abs_pt[idx];
+  const int g = ibool[q];
+  const float vx = veloc[3L * g], vy = veloc[3L * g + 1], vz = veloc[3L * g + 2];
+  const float nx = normal[3 * idx], ny = normal[3 * idx + 1], nz = normal[3 * idx + 2];
+  const float vn = vx * nx + vy * ny + vz * nz;
+  const float rvp = rho_vp[q], rvs = rho_vs[q];
+  const float tx = rvp * vn * nx + rvs * (vx - vn * nx);
+  const float ty = rvp * vn * ny + rvs * (vy - vn * ny);
+  const float tz = rvp * vn * nz + rvs * (vz - vn * nz);
+  const float w = jw[idx];
+  atomicAdd(accel + 3L * g, -tx * w);
+  atomicAdd(accel + 3L * g + 1, -ty * w);
+  atomicAdd(accel + 3L * g + 2, -tz * w);
+  if (record) {
+    record[3 * idx] = tx * w;
+    record[3 * idx + 1] = ty * w;
+    record[3 * idx + 2] = tz * w;
+  }
+}
+
+// Replay of a stored boundary record on the backward field
+// (kernels/compute_stacey_elastic_kernel.cu:111-147).
+__global__ void stacey_replay_kernel(int nfaces, const int* __restrict__ abs_ispec, const int* __restrict__ abs_pt,
+                                     const int* __restrict__ ibool, const float* __restrict__ record,
+                                     float* __restrict__ accel) {
+  long idx = (long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (idx >= (long)nfaces * NGLL2) return;
+  const int f = (int)(idx / NGLL2);
+  const int g = ibool[(long)abs_ispec[f] * NGLL3_PAD + abs_pt[idx]];
+  atomicAdd(accel + 3L * g, -record[3 * idx]);
+  atomicAdd(accel + 3L * g + 1, -record[3 * idx + 1]);
+  atomicAdd(accel + 3L * g + 2, -record[3 * idx + 2]);
+}
+
+// Point sources (compute_add_sources_viscoelastic.F90:100-140,
+// kernels/compute_add_sources_kernel.cu): block = source, thread = GLL point.
+// The stf comes either from a per-call array or from the whole-run table at
+// the device step counter (*d_it, 1-based).
+__global__ void sources_kernel(int nsrc, const int* __restrict__ ispec_src, const float* __restrict__ sa,
+                               const float* __restrict__ stf_step, const float* __restrict__ stf_table,
+                               const int* __restrict__ d_it, int stf_nstep, const int* __restrict__ ibool,
+                               float* __restrict__ accel) {
+  const int is = blockIdx.x, p = threadIdx.x;
+  if (is >= nsrc || p >= NGLL3) return;
+  const int e = ispec_src[is];
+  if (e < 0) return;
+  float stf;
+  if (stf_table) {
+    const int it = *d_it;
+    if (it < 1 || it > stf_nstep) return;
+    stf = stf_table[(long)(it - 1) * nsrc + is];
+  } else {
+    stf = stf_step[is];
+  }
+  const int g = ibool[(long)e * NGLL3_PAD + p];
+  const float* s = sa + ((long)is * NGLL3_PAD + p) * 3;
+  atomicAdd(accel + 3L * g, s[0] * stf);
+  atomicAdd(accel + 3L * g + 1, s[1] * stf);
+  atomicAdd(accel + 3L * g + 2, s[2] * stf);
+}
+
+// Receiver interpolation (compute_interpolated_dva.f90:28-110,
+// kernels/compute_elastic_seismogram_kernel.cu): block = receiver; warp-shuffle
+// tree sum of h_xi h_eta h_gamma u over the 125 points, then rotation by nu.
+// With advance != 0 the last block to finish increments the device step
+// counter (threadfence completion pattern, no spinning).
+__global__ void seismogram_kernel(int nrec, const int* __restrict__ ispec_rec, const float* __restrict__ hx,
+                                  const float* __restrict__ he, const float* __restrict__ hg,
+                                  const float* __restrict__ nu, const int* __restrict__ ibool,
+                                  const float* __restrict__ field, float* __restrict__ seismo, int nlength,
+                                  int slot, const int* __restrict__ d_it_slot, int* d_it, unsigned int* d_done,
+                                  int advance) {
+  __shared__ float red[3][4];
+  const int r = blockIdx.x, t = threadIdx.x;
+  float s0 = 0.f, s1 = 0.f, s2 = 0.f;
+  if (r < nrec && t < NGLL3) {
+    const int e = ispec_rec[r];
+    const int k = t / NGLL2, j = (t / NGLLX) % NGLLX, i = t % NGLLX;
+    const float h = hx[5 * r + i] * he[5 * r + j] * hg[5 * r + k];
+    const int g = ibool[(long)e * NGLL3_PAD + t];
+    s0 = h * field[3L * g];
+    s1 = h * field[3L * g + 1];
+    s2 = h * field[3L * g + 2];
+  }
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) {
+    s0 += __shfl_down_sync(0xffffffffu, s0, o);
+    s1 += __shfl_down_sync(0xffffffffu, s1, o);
+    s2 += __shfl_down_sync(0xffffffffu, s2, o);
+  }
+  if ((t & 31) == 0) {
+    red[0][t >> 5] = s0;
+    red[1][t >> 5] = s1;
+    red[2][t >> 5] = s2;
+  }
+  __syncthreads();
+  if (t == 0 && r < nrec) {
+    const float u0 = red[0][0] + red[0][1] + red[0][2] + red[0][3];
+    const float u1 = red[1][0] + red[1][1] + red[1][2] + red[1][3];
+    const float u2 = red[2][0] + red[2][1] + red[2][2] + red[2][3];
+    const float* n = nu + 9 * r;  // nu(3,3) column-major
+    int sl = d_it_slot ? ((*d_it_slot - 1) % nlength) : slot;
+    float* o = seismo + 3L * (r + (long)nrec * sl);
+    o[0] = n[0] * u0 + n[3] * u1 + n[6] * u2;
+    o[1] = n[1] * u0 + n[4] * u1 + n[7] * u2;
+    o[2] = n[2] * u0 + n[5] * u1 + n[8] * u2;
+  }
+  if (advance && t == 0) {
+    __threadfence();
+    unsigned prev = atomicAdd(d_done, 1u);
+    if (prev == gridDim.x - 1) {
+      *d_it += 1;
+      *d_done = 0u;
+      __threadfence();
+    }
+  }
+}
+
+__global__ void advance_it_kernel(int* d_it) { *d_it += 1; }
+__global__ void set_it_kernel(int* d_it, int v) { *d_it = v; }
+
+// max |u| over the field (check_stability.f90:408), NaN-propagating
+__global__ void maxabs_kernel(const float* __restrict__ x, long n, float* __restrict__ out) {
+  float m = 0.f;
+  for (long i = (long)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (long)gridDim.x * blockDim.x) {
+    float v = fabsf(x[i]);
+    if (!(v <= m)) m = v;  // keeps NaN
+  }
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) {
+    float w = __shfl_down_sync(0xffffffffu, m, o);
+    if (!(w <= m)) m = w;
+  }
+  if ((threadIdx.x & 31) == 0) {
+    unsigned int* ui = reinterpret_cast<unsigned int*>(out);
+    if (m != m)
+      atomicExch(ui + 1, 1u);
+    else
+      atomicMax(ui, __float_as_uint(m));  // non-negative floats order like their bits
+  }
+}
+
+Fields* pick(Mesh* mp, int fwd_or_adj) { return fwd_or_adj == 3 ? &mp->b : &mp->f; }
+
+StiffnessArgs stiffness_args(Mesh* mp, Fields& F, int iphase, float deltat, bool att, bool strain, bool backward) {
+  StiffnessArgs a;
+  memset(&a, 0, sizeof(a));
+  a.nelem = iphase == 1 ? mp->nspec_outer : mp->nspec_inner;
+  a.phase = mp->d_phase_ispec ? mp->d_phase_ispec + (long)(iphase - 1) * mp->num_phase_ispec : nullptr;
+  a.ibool = mp->d_ibool;
+  a.irregular = mp->d_irregular;
+  for (int q = 0; q < 9; ++q) a.m[q] = mp->d_metric[q];
+  a.kappav = mp->d_kappav;
+  a.muv = mp->d_muv;
+  a.gll = mp->d_gll;
+  a.xix_regular = mp->xix_regular;
+  a.jacobian_regular = mp->jacobian_regular;
+  a.deltat = deltat;
+  a.displ = F.displ;
+  a.veloc = F.veloc;
+  a.accel = F.accel;
+  for (int c = 0; c < 6; ++c) { a.R[c] = F.R[c]; a.eps[c] = F.eps[c]; }
+  a.eps_trace_over_3 = (mp->simulation_type == 3) ? F.eps_trace_over_3 : nullptr;
+  a.fc = mp->d_factor_common;
+  a.fck = mp->d_factor_common_kappa;
+  for (int s = 0; s < NSLS; ++s) {
+    a.alpha[s] = backward ? mp->b_alphaval[s] : mp->alphaval[s];
+    a.beta[s] = backward ? mp->b_betaval[s] : mp->betaval[s];
+    a.gamma[s] = backward ? mp->b_gammaval[s] : mp->gammaval[s];
+  }
+  (void)att; (void)strain;
+  return a;
+}
+
+}  // namespace
+}  // namespace sf3d
+
+using namespace sf3d;
+
+extern "C" {
+
+void update_displacement_cuda_(long* Mesh_pointer, realw* deltat_F, realw* deltatover2_F, realw* deltatsqover2_F,
+                               int* FORWARD_OR_ADJOINT) {
+  Mesh* mp = get_mesh(Mesh_pointer);
+  if (!mp) return;
+  Fields* F = pick(mp, *FORWARD_OR_ADJOINT == 1 ? 1 : 3);
+  if (!F->displ) { set_error(SF3D_ERR_STATE, "update_displacement_cuda: field not allocated"); return; }
+  const long n = 3L * mp->nglob;
+  predictor_kernel<<<nblk(n, 256), 256, 0, mp->stream>>>(F->displ, F->veloc, F->accel, n, *deltat_F,
+                                                          *deltatover2_F, *deltatsqover2_F);
+  cuda_ok(cudaGetLastError(), "predictor_kernel");
+}
+
+void compute_forces_viscoelastic_cuda_(long* Mesh_pointer, int* iphase, realw* deltat, int* nspec_outer_elastic,
+                                       int* nspec_inner_elastic, int* COMPUTE_AND_STORE_STRAIN, int* ATTENUATION,
+                                       int* FORWARD_OR_ADJOINT_f) {
+  Mesh* mp = get_mesh(Mesh_pointer);
+  if (!mp) return;
+  const int fa = *FORWARD_OR_ADJOINT_f;
+  if (fa != 0 && fa != 1 && fa != 3) { set_error(SF3D_ERR_ARG, "invalid FORWARD_OR_ADJOINT"); return; }
+  if (*iphase != 1 && *iphase != 2) { set_error(SF3D_ERR_ARG, "iphase must be 1 or 2"); return; }
+  mp->nspec_outer = *nspec_outer_elastic;
+  mp->nspec_inner = *nspec_inner_elastic;
+  const int nel = *iphase == 1 ? mp->nspec_outer : mp->nspec_inner;
+  if (nel < 0 || nel > mp->nspec || (nel > 0 && mp->num_phase_ispec < nel)) {
+    set_error(SF3D_ERR_ARG, "nspec_outer/inner_elastic exceeds the phase element lists");
+    return;
+  }
+  const bool att = *ATTENUATION && mp->attenuation;
+  const bool strain = *COMPUTE_AND_STORE_STRAIN && mp->compute_and_store_strain;
+  if (fa == 1 || fa == 0) {
+    StiffnessArgs a = stiffness_args(mp, mp->f, *iphase, *deltat, att, strain, false);
+    launch_stiffness(a, att, strain, mp->stream);
+  }
+  if ((fa == 3 || fa == 0) && mp->b.displ) {
+    StiffnessArgs a = stiffness_args(mp, mp->b, *iphase, *deltat, att, strain, true);
+    launch_stiffness(a, att && mp->b.R[0] != nullptr, strain && mp->b.eps[0] != nullptr, mp->stream);
+  }
+  cuda_ok(cudaGetLastError(), "stiffness_kernel");
+}
+
+void compute_stacey_viscoelastic_cuda_(long* Mesh_pointer, int* iphasef, realw* b_absorb_field,
+                                       int* FORWARD_OR_ADJOINT_f) {
+  Mesh* mp = get_mesh(Mesh_pointer);
+  if (!mp) return;
+  if (*iphasef != 1 || !mp->stacey || mp->num_abs_faces == 0) return;
+  const int fa = *FORWARD_OR_ADJOINT_f;
+  const long n = (long)mp->num_abs_faces * NGLL2;
+  const bool store = (fa == 1) && mp->save_forward && mp->simulation_type == 1 && b_absorb_field;
+  if (store && !ensure_stage(mp, sizeof(float) * 3 * n)) return;
+  if (fa == 1 || fa == 0) {
+    stacey_kernel<<<nblk(n, 128), 128, 0, mp->stream>>>(mp->num_abs_faces, mp->d_abs_ispec, mp->d_abs_pt,
+                                                        mp->d_abs_normal, mp->d_abs_jw, mp->d_ibool, mp->d_rho_vp,
+                                                        mp->d_rho_vs, mp->f.veloc, mp->f.accel,
+                                                        store ? mp->d_stage : nullptr);
+    if (!cuda_ok(cudaGetLastError(), "stacey_kernel")) return;
+    if (store) {
+      SF3D_CUDA(cudaMemcpyAsync(b_absorb_field, mp->d_stage, sizeof(float) * 3 * n, cudaMemcpyDeviceToHost,
+                                mp->stream));
+      SF3D_CUDA(cudaStreamSynchronize(mp->stream));
+    }
+  }
+  if ((fa == 3 || fa == 0) && mp->b.displ) {
+    if (b_absorb_field && mp->simulation_type == 3) {
+      // replay of the boundary record stored by the forward run
+      if (!ensure_stage(mp, sizeof(float) * 3 * n)) return;
+      SF3D_CUDA(cudaMemcpyAsync(mp->d_stage, b_absorb_field, sizeof(float) * 3 * n, cudaMemcpyHostToDevice,
+                                mp->stream));
+      stacey_replay_kernel<<<nblk(n, 128), 128, 0, mp->stream>>>(mp->num_abs_faces, mp->d_abs_ispec, mp->d_abs_pt,
+                                                                 mp->d_ibool, mp->d_stage, mp->b.accel);
+    } else {
+      // recomputed (checkpointed) backward field: same traction from b_veloc
+      stacey_kernel<<<nblk(n, 128), 128, 0, mp->stream>>>(mp->num_abs_faces, mp->d_abs_ispec, mp->d_abs_pt,
+                                                          mp->d_abs_normal, mp->d_abs_jw, mp->d_ibool, mp->d_rho_vp,
+                                                          mp->d_rho_vs, mp->b.veloc, mp->b.accel, nullptr);
+    }
+    cuda_ok(cudaGetLastError(), "stacey_kernel(b)");
+  }
+}
+
+static void add_sources(long* Mesh_pointer, double* h_stf, int* h_NSOURCES, bool backward) {
+  Mesh* mp = get_mesh(Mesh_pointer);
+  if (!mp) return;
+  if (*h_NSOURCES != mp->nsources) { set_error(SF3D_ERR_ARG, "NSOURCES does not match prepare_constants_device"); return; }
+  if (mp->nsources == 0 || mp->nsources_local == 0) return;
+  Fields* F = backward ? &mp->b : &mp->f;
+  if (!F->accel) { set_error(SF3D_ERR_STATE, "field not allocated"); return; }
+  std::vector<float> stf(mp->nsources);
+  for (int i = 0; i < mp->nsources; ++i) stf[i] = (float)h_stf[i];
+  SF3D_CUDA(cudaMemcpyAsync(mp->d_stf_step, stf.data(), sizeof(float) * mp->nsources, cudaMemcpyHostToDevice,
+                            mp->stream));
+  sources_kernel<<<mp->nsources, NGLL3_PAD, 0, mp->stream>>>(mp->nsources, mp->d_ispec_src, mp->d_sourcearrays,
+                                                             mp->d_stf_step, nullptr, nullptr, 0, mp->d_ibool,
+                                                             F->accel);
+  // the host stf buffer is reused by the caller on the next step
+  SF3D_CUDA(cudaStreamSynchronize(mp->stream));
+  cuda_ok(cudaGetLastError(), "sources_kernel");
+}
+
+void compute_add_sources_el_cuda_(long* Mesh_pointer, double* h_stf_pre_compute, int* h_NSOURCES) {
+  add_sources(Mesh_pointer, h_stf_pre_compute, h_NSOURCES, false);
+}
+void compute_add_sources_el_s3_cuda_(long* Mesh_pointer, double* h_stf_pre_compute, int* h_NSOURCES) {
+  add_sources(Mesh_pointer, h_stf_pre_compute, h_NSOURCES, true);
+}
+
+void kernel_3_a_cuda_(long* Mesh_pointer, realw* deltatover2_F, realw* b_deltatover2_F, int* APPROXIMATE_OCEAN_LOAD,
+                      int* FORWARD_OR_ADJOINT) {
+  Mesh* mp = get_mesh(Mesh_pointer);
+  if (!mp) return;
+  if (*FORWARD_OR_ADJOINT != 1 && *FORWARD_OR_ADJOINT != 3) { set_error(SF3D_ERR_ARG, "invalid FORWARD_OR_ADJOINT"); return; }
+  if (*APPROXIMATE_OCEAN_LOAD) { set_error(SF3D_ERR_ARG, "ocean load is not supported"); return; }
+  Fields* F = pick(mp, *FORWARD_OR_ADJOINT);
+  const float dt2 = *FORWARD_OR_ADJOINT == 1 ? *deltatover2_F : *b_deltatover2_F;
+  mass_corrector_kernel<<<nblk(mp->nglob, 256), 256, 0, mp->stream>>>(F->veloc, F->accel, mp->d_rmassx, mp->d_rmassy,
+                                                                     mp->d_rmassz, mp->nglob, dt2);
+  cuda_ok(cudaGetLastError(), "mass_corrector_kernel");
+}
+
+void kernel_3_b_cuda_(long* Mesh_pointer, realw* deltatover2_F, realw* b_deltatover2_F, int* FORWARD_OR_ADJOINT) {
+  Mesh* mp = get_mesh(Mesh_pointer);
+  if (!mp) return;
+  Fields* F = pick(mp, *FORWARD_OR_ADJOINT);
+  const float dt2 = *FORWARD_OR_ADJOINT == 1 ? *deltatover2_F : *b_deltatover2_F;
+  const long n = 3L * mp->nglob;
+  corrector_kernel<<<nblk(n, 256), 256, 0, mp->stream>>>(F->veloc, F->accel, n, dt2);
+  cuda_ok(cudaGetLastError(), "corrector_kernel");
+}
+
+void compute_seismograms_cuda_(long* Mesh_pointer_f, realw* seismograms_d, realw* seismograms_v,
+                               realw* seismograms_a, realw* seismograms_p, int* seismo_currentf,
+                               int* nlength_seismogramf, int* itf, int* it_endf, int* ACOUSTIC_SIMULATION,
+                               int* ELASTIC_SIMULATION, int* USE_TRICK_FOR_BETTER_PRESSURE) {
+  (void)seismograms_p; (void)ACOUSTIC_SIMULATION; (void)ELASTIC_SIMULATION;
+  Mesh* mp = get_mesh(Mesh_pointer_f);
+  if (!mp) return;
+  if (mp->nrec_local == 0) return;
+  const int cur = *seismo_currentf - 1;
+  const int nlen = *nlength_seismogramf;
+  if (nlen != mp->nlength_seismogram || cur < 0 || cur >= nlen) {
+    set_error(SF3D_ERR_ARG, "seismo_current / nlength_seismogram out of range");
+    return;
+  }
+  // kernel simulations record the reconstructed forward field
+  Fields* F = mp->simulation_type == 3 ? &mp->b : &mp->f;
+  struct { int on; float* field; float* dst; } kinds[3] = {
+      {mp->save_d, F->displ, mp->d_seismo_d}, {mp->save_v, F->veloc, mp->d_seismo_v}, {mp->save_a, F->accel, mp->d_seismo_a}};
+  for (auto& kd : kinds) {
+    if (!kd.on || !kd.field) continue;
+    seismogram_kernel<<<mp->nrec_local, NGLL3_PAD, 0, mp->stream>>>(
+        mp->nrec_local, mp->d_ispec_rec, mp->d_hxir, mp->d_hetar, mp->d_hgammar, mp->d_nu_rec, mp->d_ibool, kd.field,
+        kd.dst, nlen, cur, nullptr, nullptr, nullptr, 0);
+  }
+  if (!cuda_ok(cudaGetLastError(), "seismogram_kernel")) return;
+  if (cur == nlen - 1 || *itf == *it_endf) {
+    const size_t bytes = sizeof(float) * 3 * (size_t)mp->nrec_local * nlen;
+    const bool trick = USE_TRICK_FOR_BETTER_PRESSURE && *USE_TRICK_FOR_BETTER_PRESSURE;
+    if (mp->save_d && !trick && seismograms_d)
+      SF3D_CUDA(cudaMemcpyAsync(seismograms_d, mp->d_seismo_d, bytes, cudaMemcpyDeviceToHost, mp->stream));
+    if (mp->save_v && !trick && seismograms_v)
+      SF3D_CUDA(cudaMemcpyAsync(seismograms_v, mp->d_seismo_v, bytes, cudaMemcpyDeviceToHost, mp->stream));
+    if (mp->save_a && !trick && seismograms_a)
+      SF3D_CUDA(cudaMemcpyAsync(seismograms_a, mp->d_seismo_a, bytes, cudaMemcpyDeviceToHost, mp->stream));
+    SF3D_CUDA(cudaStreamSynchronize(mp->stream));
+  }
+}
+
+int sf3d_set_stf_table(long* Mesh_pointer, const double* h_stf, int nsources, int nstep) {
+  Mesh* mp = get_mesh(Mesh_pointer);
+  if (!mp) return SF3D_ERR_STATE;
+  if (nsources != mp->nsources || nstep <= 0 || (nsources > 0 && !h_stf)) {
+    set_error(SF3D_ERR_ARG, "sf3d_set_stf_table: size mismatch");
+    return SF3D_ERR_ARG;
+  }
+  std::vector<float> tab((size_t)nstep * nsources);
+  for (int it = 0; it < nstep; ++it)
+    for (int is = 0; is < nsources; ++is) tab[(size_t)it * nsources + is] = (float)h_stf[is + (size_t)nsources * it];
+  cudaFree(mp->d_stf_table);
+  mp->d_stf_table = nullptr;
+  if (!alloc_zero((void**)&mp->d_stf_table, sizeof(float) * tab.size())) return SF3D_ERR_CUDA;
+  SF3D_CUDA_RET(cudaMemcpy(mp->d_stf_table, tab.data(), sizeof(float) * tab.size(), cudaMemcpyHostToDevice),
+                SF3D_ERR_CUDA);
+  mp->stf_nstep = nstep;
+  return SF3D_OK;
+}
+
+__global__ void stamp_kernel(unsigned long long* stamps, const int* d_it, int which, int nmax) {
+  unsigned long long t;
+  asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t));
+  const int it = *d_it;
+  if (it >= 1 && it <= nmax) stamps[2 * (it - 1) + which] = t;
+}
+
+// One fused forward step on the compute stream; the predictor of this step is
+// fused with the corrector of the previous one unless first_step.
+static int enqueue_step(Mesh* mp, float dt, float dt2, float dtsq2, bool first_step, unsigned long long* stamps,
+                        int nmax) {
+  Fields& F = mp->f;
+  cudaStream_t s = mp->stream;
+  int launches = 0;
+  if (first_step) {
+    const long n = 3L * mp->nglob;
+    predictor_kernel<<<nblk(n, 256), 256, 0, s>>>(F.displ, F.veloc, F.accel, n, dt, dt2, dtsq2);
+  } else {
+    corrector_predictor_kernel<<<nblk(mp->nglob, 256), 256, 0, s>>>(F.displ, F.veloc, F.accel, mp->d_rmassx,
+                                                                    mp->d_rmassy, mp->d_rmassz, mp->nglob, dt, dt2,
+                                                                    dtsq2);
+  }
+  ++launches;
+  if (mp->stacey && mp->num_abs_faces > 0) {
+    const long n = (long)mp->num_abs_faces * NGLL2;
+    stacey_kernel<<<nblk(n, 128), 128, 0, s>>>(mp->num_abs_faces, mp->d_abs_ispec, mp->d_abs_pt, mp->d_abs_normal,
+                                                mp->d_abs_jw, mp->d_ibool, mp->d_rho_vp, mp->d_rho_vs, F.veloc,
+                                                F.accel, nullptr);
+    ++launches;
+  }
+  if (mp->nsources > 0 && mp->d_stf_table) {
+    sources_kernel<<<mp->nsources, NGLL3_PAD, 0, s>>>(mp->nsources, mp->d_ispec_src, mp->d_sourcearrays, nullptr,
+                                                      mp->d_stf_table, mp->d_it, mp->stf_nstep, mp->d_ibool, F.accel);
+    ++launches;
+  }
+  const bool att = mp->attenuation != 0;
+  const bool strain = mp->compute_and_store_strain != 0;
+  for (int iphase = 1; iphase <= 2; ++iphase) {
+    StiffnessArgs a = stiffness_args(mp, F, iphase, dt, att, strain, false);
+    if (a.nelem <= 0) continue;
+    if (stamps && iphase == 2) stamp_kernel<<<1, 1, 0, s>>>(stamps, mp->d_it, 0, nmax);
+    launch_stiffness(a, att, strain, s);
+    if (stamps && iphase == 2) stamp_kernel<<<1, 1, 0, s>>>(stamps, mp->d_it, 1, nmax);
+    ++launches;
+  }
+  if (mp->nrec_local > 0 && mp->save_d) {
+    seismogram_kernel<<<mp->nrec_local, NGLL3_PAD, 0, s>>>(mp->nrec_local, mp->d_ispec_rec, mp->d_hxir, mp->d_hetar,
+                                                           mp->d_hgammar, mp->d_nu_rec, mp->d_ibool, F.displ,
+                                                           mp->d_seismo_d, mp->nlength_seismogram, 0, mp->d_it,
+                                                           mp->d_it, mp->d_done, 1);
+  } else {
+    advance_it_kernel<<<1, 1, 0, s>>>(mp->d_it);
+  }
+  ++launches;
+  return launches;
+}
+
+int sf3d_iterate_time(long* Mesh_pointer, int it_begin, int it_end, realw deltat, int steps_per_graph, int flags) {
+  Mesh* mp = get_mesh(Mesh_pointer);
+  if (!mp) return SF3D_ERR_STATE;
+  if (!mp->f.displ) { set_error(SF3D_ERR_STATE, "prepare_fields_elastic_device not called"); return SF3D_ERR_STATE; }
+  if (it_begin < 1 || it_end < it_begin) { set_error(SF3D_ERR_ARG, "invalid it range"); return SF3D_ERR_ARG; }
+  if (mp->nrec_local > 0 && mp->save_d && it_end > mp->nlength_seismogram) {
+    set_error(SF3D_ERR_ARG, "it_end exceeds nlength_seismogram");
+    return SF3D_ERR_ARG;
+  }
+  if (mp->nsources > 0 && (!mp->d_stf_table || it_end > mp->stf_nstep)) {
+    set_error(SF3D_ERR_STATE, "sf3d_set_stf_table must cover it_end");
+    return SF3D_ERR_STATE;
+  }
+  if (mp->num_phase_ispec <= 0) { set_error(SF3D_ERR_STATE, "phase element lists not prepared"); return SF3D_ERR_STATE; }
+  if (mp->nspec_outer == 0 && mp->nspec_inner == 0) mp->nspec_inner = mp->num_phase_ispec;
+  const float dt = deltat, dt2 = deltat / 2.f, dtsq2 = deltat * deltat / 2.f;
+  const bool timing = (flags & 1) != 0;
+  const int nsteps = it_end - it_begin + 1;
+  if (timing) {
+    cudaFree(mp->d_stamps);
+    mp->d_stamps = nullptr;
+    if (!alloc_zero((void**)&mp->d_stamps, sizeof(unsigned long long) * 2 * (size_t)it_end)) return SF3D_ERR_CUDA;
+  }
+  cudaStream_t s = mp->stream;
+  set_it_kernel<<<1, 1, 0, s>>>(mp->d_it, it_begin);
+  SF3D_CUDA_RET(cudaMemsetAsync(mp->d_done, 0, sizeof(unsigned int), s), SF3D_ERR_CUDA);
+  SF3D_CUDA_RET(cudaEventRecord(mp->ev0, s), SF3D_ERR_CUDA);
+  int launches = 0;
+  auto step = [&](bool first) {
+    launches += enqueue_step(mp, dt, dt2, dtsq2, first, timing ? mp->d_stamps : nullptr, it_end);
+  };
+  step(true);
+  int remaining = nsteps - 1;
+  const int K = steps_per_graph > 0 ? steps_per_graph : 0;
+  if (K > 0 && remaining >= K) {
+    cudaGraph_t graph = nullptr;
+    cudaGraphExec_t exec = nullptr;
+    int per_block = 0;
+    SF3D_CUDA_RET(cudaStreamBeginCapture(s, cudaStreamCaptureModeThreadLocal), SF3D_ERR_CUDA);
+    for (int q = 0; q < K; ++q) per_block += enqueue_step(mp, dt, dt2, dtsq2, false, timing ? mp->d_stamps : nullptr, it_end);
+    SF3D_CUDA_RET(cudaStreamEndCapture(s, &graph), SF3D_ERR_CUDA);
+    SF3D_CUDA_RET(cudaGraphInstantiate(&exec, graph, 0), SF3D_ERR_CUDA);
+    while (remaining >= K) {
+      if (!cuda_ok(cudaGraphLaunch(exec, s), "cudaGraphLaunch")) break;
+      launches += per_block;
+      remaining -= K;
+    }
+    cudaGraphExecDestroy(exec);
+    cudaGraphDestroy(graph);
+  }
+  while (remaining > 0) { step(false); --remaining; }
+  mass_corrector_kernel<<<nblk(mp->nglob, 256), 256, 0, s>>>(mp->f.veloc, mp->f.accel, mp->d_rmassx, mp->d_rmassy,
+                                                             mp->d_rmassz, mp->nglob, dt2);
+  ++launches;
+  SF3D_CUDA_RET(cudaEventRecord(mp->ev1, s), SF3D_ERR_CUDA);
+  SF3D_CUDA_RET(cudaEventSynchronize(mp->ev1), SF3D_ERR_CUDA);
+  if (!cuda_ok(cudaGetLastError(), "sf3d_iterate_time")) return SF3D_ERR_CUDA;
+  cudaEventElapsedTime(&mp->last_total_ms, mp->ev0, mp->ev1);
+  mp->last_total_launches = launches;
+  mp->last_stiff_launches = 0;
+  mp->last_stiff_ms = 0.f;
+  if (timing) {
+    std::vector<unsigned long long> st(2 * (size_t)it_end);
+    SF3D_CUDA_RET(cudaMemcpy(st.data(), mp->d_stamps, sizeof(unsigned long long) * st.size(), cudaMemcpyDeviceToHost),
+                  SF3D_ERR_CUDA);
+    double ns = 0;
+    for (int it = it_begin; it <= it_end; ++it) {
+      const unsigned long long a = st[2 * (it - 1)], b = st[2 * (it - 1) + 1];
+      if (b > a) { ns += (double)(b - a); ++mp->last_stiff_launches; }
+    }
+    mp->last_stiff_ms = (float)(ns * 1e-6);
+  }
+  return sf3d_last_error(nullptr, 0);
+}
+
+int sf3d_last_timing(long* Mesh_pointer, float* stiffness_ms, int* stiffness_launches, float* total_ms,
+                     int* total_launches) {
+  Mesh* mp = get_mesh(Mesh_pointer);
+  if (!mp) return SF3D_ERR_STATE;
+  if (stiffness_ms) *stiffness_ms = mp->last_stiff_ms;
+  if (stiffness_launches) *stiffness_launches = mp->last_stiff_launches;
+  if (total_ms) *total_ms = mp->last_total_ms;
+  if (total_launches) *total_launches = mp->last_total_launches;
+  return SF3D_OK;
+}
+
+int sf3d_get_seismograms(long* Mesh_pointer, realw* h) {
+  Mesh* mp = get_mesh(Mesh_pointer);
+  if (!mp) return SF3D_ERR_STATE;
+  if (!mp->d_seismo_d || mp->nrec_local == 0) return SF3D_OK;
+  const size_t bytes = sizeof(float) * 3 * (size_t)mp->nrec_local * mp->nlength_seismogram;
+  SF3D_CUDA_RET(cudaMemcpyAsync(h, mp->d_seismo_d, bytes, cudaMemcpyDeviceToHost, mp->stream), SF3D_ERR_CUDA);
+  SF3D_CUDA_RET(cudaStreamSynchronize(mp->stream), SF3D_ERR_CUDA);
+  return SF3D_OK;
+}
+
+int sf3d_check_stability(long* Mesh_pointer, realw threshold, realw* max_norm) {
+  Mesh* mp = get_mesh(Mesh_pointer);
+  if (!mp) return SF3D_ERR_STATE;
+  if (!mp->f.displ) return SF3D_ERR_STATE;
+  SF3D_CUDA_RET(cudaMemsetAsync(mp->d_scratch, 0, sizeof(float) * 2, mp->stream), SF3D_ERR_CUDA);
+  maxabs_kernel<<<4 * 152, 256, 0, mp->stream>>>(mp->f.displ, 3L * mp->nglob, mp->d_scratch);
+  float h[2];
+  SF3D_CUDA_RET(cudaMemcpyAsync(h, mp->d_scratch, sizeof(h), cudaMemcpyDeviceToHost, mp->stream), SF3D_ERR_CUDA);
+  SF3D_CUDA_RET(cudaStreamSynchronize(mp->stream), SF3D_ERR_CUDA);
+  unsigned nanflag;
+  memcpy(&nanflag, &h[1], 4);
+  if (max_norm) *max_norm = nanflag ? NAN : h[0];
+  if (nanflag || !(h[0] < threshold) || isinf(h[0])) {
+    set_error(SF3D_ERR_UNSTABLE, "wavefield is unstable (NaN/Inf or above threshold)");
+    return SF3D_ERR_UNSTABLE;
+  }
+  return SF3D_OK;
+}
+
+}  // extern "C"

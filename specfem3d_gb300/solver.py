@@ -1,0 +1,207 @@
+"""Host driver of the GPU time step: the caller side of the C ABI.
+
+``GPUSolver`` does what the Fortran solver does around the reference's GPU
+layer: it hands the mesh databases to prepare_constants_device and
+prepare_fields_elastic_device (specfem3D/prepare_gpu.f90:67-165), then either
+replays the per-step call sequence of iterate_time
+(specfem3D/iterate_time.F90:219-330 with
+compute_forces_viscoelastic_calling_routine.F90:107-417) through the same entry
+points, or runs whole step blocks on the device with sf3d_iterate_time.
+Everything below goes through libspecfem3d_gb300.so; nothing is computed on
+the CPU.
+"""
+from __future__ import annotations
+
+import ctypes
+
+import numpy as np
+
+from . import abi
+
+NGLL3 = 125
+N_SLS = 3
+
+
+class GPUSolver:
+    def __init__(self, db: dict, cfg: dict, nlength: int | None = None, simulation_type: int = 1,
+                 save_forward: bool = False, record=("displ",)):
+        self.L = abi.load()
+        self.db, self.cfg = db, cfg
+        self.nspec, self.nglob = int(db["nspec"]), int(db["nglob"])
+        self.nstep = int(cfg["nstep"])
+        self.nlength = int(nlength or self.nstep)
+        self.nrec = int(db["nrec"])
+        self.nsources = int(db["nsources"])
+        self.attenuation = int(db.get("attenuation", 0))
+        self.simulation_type = simulation_type
+        dt = np.float32(cfg["dt"])
+        self.deltat = dt
+        self.deltatover2 = np.float32(dt / np.float32(2))
+        self.deltatsqover2 = np.float32(dt * dt / np.float32(2))
+        self.mesh = ctypes.c_long(0)
+        self.mp = ctypes.addressof(self.mesh)
+        self.record = record
+        self._prepare_constants(db, save_forward)
+        self._prepare_fields(db)
+        self.it = 1
+
+    # ------------------------------------------------------------------ setup
+    def _prepare_constants(self, db, save_forward):
+        A = abi.Args()
+        nspec, nirr = self.nspec, int(db["nspec_irregular"])
+        nrec = self.nrec
+        nu = np.tile(np.eye(3).reshape(-1, order="F"), max(nrec, 1))
+        hx = np.asarray(db["hxir"], np.float32)
+        he = np.asarray(db["hetar"], np.float32)
+        hg = np.asarray(db["hgammar"], np.float32)
+        args = [
+            self.mp, A.i(5), A.i(nspec), A.i(self.nglob), A.i(nirr), A.ai(db["irregular_element_number"]),
+            *(A.af(db[n]) for n in ("xix", "xiy", "xiz", "etax", "etay", "etaz", "gammax", "gammay", "gammaz")),
+            A.f(db["xix_regular"]), A.f(db["jacobian_regular"]), A.ai(db["ibool"]),
+            A.i(0), A.i(0), A.ai(None), A.ai(None),
+            A.af(db["hprime_xx"]), A.af(db["hprimewgll_xx"]), A.af(db["wgllwgll_xy"]), A.af(db["wgllwgll_xz"]),
+            A.af(db["wgllwgll_yz"]),
+            A.i(int(db.get("stacey", 1))), A.ai(db["abs_boundary_ispec"]), A.ai(db["abs_boundary_ijk"]),
+            A.af(db["abs_boundary_normal"]), A.af(db["abs_boundary_jacobian2Dw"]),
+            A.i(int(db["num_abs_boundary_faces"]) if db.get("stacey", 1) else 0),
+            A.ai(np.ones(nspec, np.int32)), A.i(self.nsources), A.i(self.nsources), A.af(db["sourcearrays"]),
+            A.ai(np.zeros(max(self.nsources, 1), np.int32)), A.ai(db["ispec_selected_source"]),
+            A.ai(db["ispec_selected_rec"]), A.i(nrec), A.i(nrec), A.i(self.simulation_type), A.i(0),
+            A.i(0), A.i(nspec), A.ai(np.zeros(nspec, np.int32)), A.ai(np.ones(nspec, np.int32)), A.i(0),
+            A.i(int(save_forward)), A.af(hx), A.af(he), A.af(hg), A.ad(nu), A.ad(nu),
+            A.ai(np.zeros(max(nrec, 1), np.int32)), A.i(self.nlength),
+            A.i(int("displ" in self.record)), A.i(int("veloc" in self.record)), A.i(int("accel" in self.record)),
+            A.i(0), A.i(1), A.i(0), A.i(0), A.i(0),
+        ]
+        self.L.prepare_constants_device_(*args)
+        abi.check()
+
+    def _prepare_fields(self, db):
+        A = abi.Args()
+        nspec = self.nspec
+        phase = np.zeros((nspec, 2), np.int32)
+        phase[:, 1] = np.arange(1, nspec + 1)
+        att = self.attenuation
+        strain = int(att or self.simulation_type == 3)
+        zsls = np.zeros(N_SLS * NGLL3 * nspec, np.float32) if att else None
+        zeps = np.zeros(NGLL3 * nspec, np.float32) if strain else None
+        args = [
+            self.mp, A.af(db["rmassx"]), A.af(db["rmassy"]), A.af(db["rmassz"]), A.af(db["rho_vp"]),
+            A.af(db["rho_vs"]), A.af(db["kappastore"]), A.af(db["mustore"]), A.i(nspec),
+            A.ai(phase.reshape(-1, order="F")), A.af(None), A.i(0), A.i(strain),
+            *(A.af(zeps) for _ in range(5)), A.i(att), A.i(N_SLS * NGLL3 * nspec if att else 1),
+            *(A.af(zsls) for _ in range(5)), A.af(db.get("factor_common") if att else None),
+            A.af(zsls), A.af(zeps), A.af(db.get("factor_common_kappa") if att else None),
+            A.af(db.get("alphaval", np.zeros(3))), A.af(db.get("betaval", np.zeros(3))),
+            A.af(db.get("gammaval", np.zeros(3))), A.i(0), A.af(None), A.i(0), A.af(None), A.ai(None), A.ai(None),
+            A.i(0), A.i(0), A.i(0), A.i(0), A.ai(None), A.i(0), *(A.af(None) for _ in range(21)),
+        ]
+        self.L.prepare_fields_elastic_device_(*args)
+        abi.check()
+        self.strain = strain
+        if self.nsources:
+            stf = np.ascontiguousarray(np.asarray(db["stf"], np.float64).reshape(self.nsources, -1).T)
+            if self.L.sf3d_set_stf_table(self.mp, stf.ctypes.data, self.nsources, stf.shape[0]) != 0:
+                abi.check()
+
+    # ---------------------------------------------------------- one step (ABI)
+    def step(self):
+        """One time step through the per-call entry points, in the reference's order."""
+        L, A, it = self.L, abi.Args(), self.it
+        one = A.i(1)
+        L.update_displacement_cuda_(self.mp, A.f(self.deltat), A.f(self.deltatover2), A.f(self.deltatsqover2), one)
+        for iphase in (1, 2):
+            L.compute_forces_viscoelastic_cuda_(self.mp, A.i(iphase), A.f(self.deltat), A.i(0), A.i(self.nspec),
+                                                A.i(self.strain), A.i(self.attenuation), one)
+            if iphase == 1:
+                L.compute_stacey_viscoelastic_cuda_(self.mp, A.i(1), A.af(None), one)
+                if self.nsources:
+                    stf = np.ascontiguousarray(np.asarray(self.db["stf"], np.float64).reshape(self.nsources, -1)[:, it - 1])
+                    L.compute_add_sources_el_cuda_(self.mp, A.ad(stf), A.i(self.nsources))
+        L.kernel_3_a_cuda_(self.mp, A.f(self.deltatover2), A.f(0.0), A.i(0), one)
+        if self.nrec:
+            if not hasattr(self, "_seis_host"):
+                self._seis_host = np.zeros(3 * self.nrec * self.nlength, np.float32)
+            z = self._seis_host.ctypes.data
+            cur = (it - 1) % self.nlength + 1
+            L.compute_seismograms_cuda_(self.mp, z, z, z, z, A.i(cur), A.i(self.nlength), A.i(it),
+                                        A.i(self.nstep), A.i(0), A.i(1), A.i(0))
+        self.it += 1
+
+    def run_per_call(self, nsteps: int):
+        for _ in range(nsteps):
+            self.step()
+        abi.check()
+
+    # ------------------------------------------------- whole step blocks (fused)
+    def run(self, nsteps: int, steps_per_graph: int = 50, timing: bool = False):
+        """nsteps time steps on the device (fused predictor/corrector, graph-captured)."""
+        rc = self.L.sf3d_iterate_time(self.mp, self.it, self.it + nsteps - 1, float(self.deltat),
+                                      int(steps_per_graph), int(bool(timing)))
+        if rc != 0:
+            abi.check()
+        self.it += nsteps
+
+    def last_timing(self):
+        sm, sl, tm, tl = ctypes.c_float(), ctypes.c_int(), ctypes.c_float(), ctypes.c_int()
+        self.L.sf3d_last_timing(self.mp, ctypes.addressof(sm), ctypes.addressof(sl), ctypes.addressof(tm),
+                                ctypes.addressof(tl))
+        return dict(stiffness_ms=sm.value, stiffness_launches=sl.value, total_ms=tm.value, total_launches=tl.value)
+
+    # ----------------------------------------------------------------- outputs
+    def seismograms(self) -> np.ndarray:
+        """(nrec, 3, nlength) displacement traces."""
+        out = np.zeros(3 * self.nrec * self.nlength, np.float32)
+        if self.nrec:
+            self.L.sf3d_get_seismograms(self.mp, out.ctypes.data)
+            abi.check()
+        return out.reshape(self.nlength, self.nrec, 3).transpose(1, 2, 0)
+
+    def fields(self):
+        A = abi.Args()
+        d, v, a = (np.zeros(3 * self.nglob, np.float32) for _ in range(3))
+        self.L.transfer_fields_el_from_device_(A.i(3 * self.nglob), d.ctypes.data, v.ctypes.data, a.ctypes.data,
+                                               self.mp)
+        abi.check()
+        return d, v, a
+
+    def set_fields(self, d, v, a):
+        A = abi.Args()
+        self.L.transfer_fields_el_to_device_(A.i(3 * self.nglob), A.af(d), A.af(v), A.af(a), self.mp)
+        abi.check()
+
+    def memory_variables(self):
+        A = abi.Args()
+        n = N_SLS * NGLL3 * self.nspec
+        R = [np.zeros(n, np.float32) for _ in range(6)]
+        self.L.transfer_rmemory_from_device_(self.mp, *(r.ctypes.data for r in R), A.i(n))
+        abi.check()
+        E = [np.zeros(NGLL3 * self.nspec, np.float32) for _ in range(6)]
+        self.L.transfer_strain_from_device_(self.mp, *(e.ctypes.data for e in E), A.i(NGLL3 * self.nspec))
+        abi.check()
+        return R, E
+
+    def forces_only(self, iphase: int = 2):
+        """One stiffness pass (compute_forces_viscoelastic_cuda) on the current fields."""
+        A = abi.Args()
+        self.L.compute_forces_viscoelastic_cuda_(self.mp, A.i(iphase), A.f(self.deltat), A.i(0), A.i(self.nspec),
+                                                 A.i(self.strain), A.i(self.attenuation), A.i(1))
+        self.L.sf3d_synchronize(self.mp)
+        abi.check()
+
+    def check_stability(self, threshold: float = 1e25):
+        m = ctypes.c_float()
+        rc = self.L.sf3d_check_stability(self.mp, float(threshold), ctypes.addressof(m))
+        return rc, m.value
+
+    def close(self):
+        if self.mesh.value:
+            A = abi.Args()
+            self.L.prepare_cleanup_device_(self.mp, A.i(0), A.i(1), A.i(0))
+            self.mesh.value = 0
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass

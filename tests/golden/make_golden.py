@@ -1,0 +1,42 @@
+"""Extract the reference's golden seismograms into compact fixtures.
+
+Run in a checkout where the SPECFEM3D reference tree is available (its path is
+the first argument, default /root/reference).  It reads the ASCII
+traces (.semd) committed under the reference's example REF_SEIS directories and writes
+float32 arrays (station, component, sample) plus the time axis to
+tests/golden/*.npz.  The fixtures are used by the oracle and GPU parity tests,
+which never read the reference tree at run time.
+"""
+import os
+import sys
+
+import numpy as np
+
+EX = "EXAMPLES/applications"
+STATIONS = ["X20", "X30", "X40", "X50"]
+
+
+def read(root, example, ext):
+    d = os.path.join(root, EX, example, "REF_SEIS")
+    traces, t = [], None
+    for st in STATIONS:
+        comps = []
+        for c in "XYZ":
+            a = np.loadtxt(os.path.join(d, f"DB.{st}.BX{c}.{ext}"))
+            t = a[:, 0]
+            comps.append(a[:, 1])
+        traces.append(comps)
+    return np.asarray(traces, np.float32), np.asarray(t, np.float64)
+
+
+def main():
+    root = sys.argv[1] if len(sys.argv) > 1 else "/root/reference"
+    out = os.path.dirname(os.path.abspath(__file__))
+    d, t = read(root, "homogeneous_halfspace_HEX8_elastic_absorbing_Stacey_5sides", "semd")
+    np.savez_compressed(os.path.join(out, "refex_stacey5sides.npz"), displ=d, t=t, stations=np.array(STATIONS))
+    nd, t2 = read(root, "homogeneous_halfspace_HEX8_elastic_no_absorbing", "semd")
+    np.savez_compressed(os.path.join(out, "refex_no_absorbing.npz"), displ=nd, t=t2, stations=np.array(STATIONS))
+
+
+if __name__ == "__main__":
+    main()
