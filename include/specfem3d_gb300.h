@@ -168,6 +168,53 @@ void compute_seismograms_cuda_(long *Mesh_pointer_f, realw *seismograms_d, realw
                                int *USE_TRICK_FOR_BETTER_PRESSURE);
 
 /* ---------------------------------------------------------------------------
+ * fluid domain and fluid-solid coupling — src/gpu/compute_forces_acoustic_cuda.cu,
+ * compute_stacey_acoustic_cuda.cu, compute_coupling_cuda.cu, update_displacement_cuda.cu
+ * ------------------------------------------------------------------------- */
+
+/* prepare_fields_acoustic_device (prepare_mesh_constants_cuda.cu:434): rmass_acoustic
+ * (NGLOB), rhostore/kappastore (5,5,5,NSPEC), phase lists (num,2), free-surface and
+ * coupling faces (ispec, ijk (3,25,nf), normal (3,25,nf) pointing out of the fluid). */
+void prepare_fields_acoustic_device_(long *Mesh_pointer, realw *rmass_acoustic, realw *rhostore,
+                                     realw *kappastore, int *num_phase_ispec_acoustic,
+                                     int *phase_ispec_inner_acoustic, int *NOISE_TOMOGRAPHY,
+                                     int *num_free_surface_faces, int *free_surface_ispec,
+                                     int *free_surface_ijk, int *b_reclen_potential,
+                                     realw *b_absorb_potential, int *ELASTIC_SIMULATION,
+                                     int *num_coupling_ac_el_faces, int *coupling_ac_el_ispec,
+                                     int *coupling_ac_el_ijk, realw *coupling_ac_el_normal,
+                                     realw *coupling_ac_el_jacobian2Dw, int *num_colors_outer_acoustic,
+                                     int *num_colors_inner_acoustic, int *num_elem_colors_acoustic);
+/* compute_forces_acoustic_cuda (compute_forces_acoustic_cuda.cu:238): fluid stiffness. */
+void compute_forces_acoustic_cuda_(long *Mesh_pointer, int *iphase, int *nspec_outer_acoustic,
+                                   int *nspec_inner_acoustic, int *FORWARD_OR_ADJOINT_f);
+/* acoustic_enforce_free_surf_cuda (compute_forces_acoustic_cuda.cu:334). */
+void acoustic_enforce_free_surf_cuda_(long *Mesh_pointer, int *ABSORB_INSTEAD_OF_FREE_SURFACE,
+                                      int *FORWARD_OR_ADJOINT);
+/* update_displacement_ac_cuda (update_displacement_cuda.cu:192): potential predictor. */
+void update_displacement_ac_cuda_(long *Mesh_pointer, realw *deltat_F, realw *deltatover2_F,
+                                  realw *deltatsqover2_F, int *FORWARD_OR_ADJOINT);
+/* kernel_3_acoustic_cuda (update_displacement_cuda.cu:448): mass + corrector. */
+void kernel_3_acoustic_cuda_(long *Mesh_pointer, realw *deltatover2_F, realw *b_deltatover2_F,
+                             int *FORWARD_OR_ADJOINT_f);
+/* compute_stacey_acoustic_cuda (compute_stacey_acoustic_cuda.cu:39). */
+void compute_stacey_acoustic_cuda_(long *Mesh_pointer, int *iphasef, realw *h_b_absorb_potential,
+                                   int *FORWARD_OR_ADJOINT_f);
+/* compute_coupling_ac_el_cuda / compute_coupling_el_ac_cuda (compute_coupling_cuda.cu:39, :135). */
+void compute_coupling_ac_el_cuda_(long *Mesh_pointer, int *iphasef, int *num_coupling_ac_el_facesf,
+                                  int *FORWARD_OR_ADJOINT);
+void compute_coupling_el_ac_cuda_(long *Mesh_pointer, int *iphasef, int *num_coupling_ac_el_facesf,
+                                  int *FORWARD_OR_ADJOINT);
+/* compute_add_sources_ac_cuda (compute_add_sources_acoustic_cuda.cu:65): pressure sources. */
+void compute_add_sources_ac_cuda_(long *Mesh_pointer, int *NSOURCESf, double *h_stf_pre_compute,
+                                  int *run_number_of_the_source);
+/* transfer_fields_ac_to_device / _from_device (transfer_fields_cuda.cu): potentials (NGLOB). */
+void transfer_fields_ac_to_device_(int *size, realw *potential_acoustic, realw *potential_dot_acoustic,
+                                   realw *potential_dot_dot_acoustic, long *Mesh_pointer);
+void transfer_fields_ac_from_device_(int *size, realw *potential_acoustic, realw *potential_dot_acoustic,
+                                     realw *potential_dot_dot_acoustic, long *Mesh_pointer);
+
+/* ---------------------------------------------------------------------------
  * transfers — src/gpu/transfer_fields_cuda.cu
  * ------------------------------------------------------------------------- */
 void transfer_fields_el_to_device_(int *size, realw *displ, realw *veloc, realw *accel, long *Mesh_pointer);   /* :45 */
@@ -235,7 +282,8 @@ int sf3d_set_stf_table(long *Mesh_pointer, const double *h_stf, int nsources, in
 
 /* Run time steps it_begin..it_end (1-based, inclusive) of the forward elastic
  * scheme entirely on the device: fused corrector+predictor, Stacey, sources,
- * stiffness, displacement seismograms.  Steps are captured in CUDA graphs of
+ * stiffness, displacement seismograms (trace slot (it-1) mod nlength_seismogram).
+ * Steps are captured in CUDA graphs of
  * steps_per_graph steps (0 = no graphs).  Leaves the fields as the per-call
  * ABI leaves them after the same steps.  flags bit 0: record the device time
  * of every stiffness launch (read back with sf3d_last_timing). */

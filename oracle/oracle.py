@@ -274,6 +274,10 @@ def build_database(cfg: dict, precision: str = "f32", material=None) -> dict:
     db.update(derivation_matrices(precision))
     # sources and receivers
     _sources_receivers(L, precision, cfg, db)
+    db["stf"], db["t0"] = source_time_functions(cfg)
+    db["attenuation"] = int(bool(cfg.get("attenuation", False)))
+    if db["attenuation"]:
+        db.update(attenuation_setup(db, cfg, precision))
     return db
 
 
@@ -343,7 +347,7 @@ def source_time_functions(cfg: dict) -> np.ndarray:
     srcs = cfg.get("sources", [])
     dt, nstep = float(cfg["dt"]), int(cfg["nstep"])
     if not srcs:
-        return np.zeros((0, nstep))
+        return np.zeros((0, nstep)), 0.0
     kinds = [s.get("stf", "ricker") for s in srcs]
     params = [float(s["f0"]) if k == "ricker" else float(s["hdur"]) for s, k in zip(srcs, kinds)]
     tsh = np.array([float(s.get("tshift", 0.0)) for s in srcs])
@@ -417,3 +421,218 @@ def seismograms(sim: OracleSim) -> np.ndarray:
     """(nrec, 3, nstep) traces recorded so far."""
     nr, nstep = sim.geti("nrec"), sim.geti("nstep")
     return sim.get("seismograms").reshape(nstep, nr, 3).transpose(1, 2, 0)
+
+
+# ----------------------------------------------------------------------------
+# attenuation (shared/get_attenuation_model.f90, specfem3D/prepare_attenuation.f90)
+# ----------------------------------------------------------------------------
+
+ATTENUATION_COMP_MAXIMUM = 9000.0
+ATTENUATION_F0_REFERENCE = 18.0  # the reference's default Par_file value
+
+
+def min_resolved_period(db: dict) -> float:
+    """check_mesh_resolution.f90:200-280 in single precision: per element
+    (max corner edge / (NGLL-1)) / min(vp, vs) * NPTS_PER_WAVELENGTH, maximum over
+    elements."""
+    f32 = np.float32
+    nspec = db["nspec"]
+    an = db["anchors"].reshape(nspec, 8, 3).astype(f32)
+    edges = [(0, 1), (3, 2), (4, 5), (7, 6), (0, 3), (1, 2), (4, 7), (5, 6), (0, 4), (1, 5), (3, 7), (2, 6)]
+    d2 = np.stack([((an[:, a] - an[:, b]) ** 2).sum(axis=1) for a, b in edges], axis=1).astype(f32)
+    emax = np.sqrt(d2.max(axis=1)).astype(f32)
+    kap = db["kappastore"].reshape(nspec, NGLL3).astype(f32)
+    mu = db["mustore"].reshape(nspec, NGLL3).astype(f32)
+    rho = db["rhostore"].reshape(nspec, NGLL3).astype(f32)
+    vp = np.sqrt((kap + f32(4.0 / 3.0) * mu) / rho).astype(f32)
+    vs = np.sqrt(mu / rho).astype(f32)
+    vmin = np.minimum(vp.min(axis=1), vs.min(axis=1))
+    pmax = (emax / f32(NGLL - 1)) / vmin * f32(5.0)
+    return float(pmax.max())
+
+
+def attenuation_setup(db: dict, cfg: dict, precision: str = "f32") -> dict:
+    """Restated attenuation set-up: factor_common(_kappa) (N_SLS,5,5,5,NSPEC),
+    unrelaxed-modulus scaling of mustore/kappastore, alpha/beta/gamma values."""
+    L = lib(precision)
+    rd = real_dtype(precision)
+    dp = ctypes.POINTER(ctypes.c_double)
+    L.orc_attenuation_constants.argtypes = [ctypes.c_double, dp, dp, dp, dp]
+    L.orc_attenuation_factors.argtypes = [ctypes.c_double, dp, ctypes.c_double, ctypes.c_double,
+                                          ctypes.c_double, ctypes.c_double, dp, dp, dp, dp]
+    mrp = min_resolved_period(db)
+    tau_sigma = (ctypes.c_double * N_SLS)()
+    fc, tmin, tmax = ctypes.c_double(), ctypes.c_double(), ctypes.c_double()
+    L.orc_attenuation_constants(mrp, tau_sigma, ctypes.byref(fc), ctypes.byref(tmin), ctypes.byref(tmax))
+    ts = np.array(tau_sigma[:])
+    tau_f = ts.astype(rd)
+    tauinv = (rd(1) / tau_f).astype(rd)
+    nspec = db["nspec"]
+    lay = np.asarray(cfg["elem_layer"], np.int64)
+    cache = {}
+
+    def factors(Q):
+        Q = min(max(float(Q), 1.0), ATTENUATION_COMP_MAXIMUM)
+        if Q not in cache:
+            beta = (ctypes.c_double * N_SLS)()
+            omsb, sf = ctypes.c_double(), ctypes.c_double()
+            te = (ctypes.c_double * N_SLS)()
+            L.orc_attenuation_factors(Q, tau_sigma, tmin.value, tmax.value, fc.value, ATTENUATION_F0_REFERENCE,
+                                      beta, ctypes.byref(omsb), ctypes.byref(sf), te)
+            cache[Q] = (np.array(beta[:]), omsb.value, sf.value)
+        return cache[Q]
+
+    fcm = np.zeros((nspec, NGLL3, N_SLS), rd)
+    fck = np.zeros((nspec, NGLL3, N_SLS), rd)
+    smu = np.ones((nspec, NGLL3), rd)
+    skap = np.ones((nspec, NGLL3), rd)
+    for li, m in enumerate(cfg["layers"]):
+        sel = lay == li
+        if not sel.any():
+            continue
+        bm, om, sm = factors(np.float32(m["Qmu"]))
+        bk, ok_, sk = factors(np.float32(m.get("Qkappa", 9999.0)))
+        fcm[sel] = ((2.0 * bm * tauinv.astype(np.float64)) / om).astype(rd)
+        fck[sel] = ((bk * tauinv.astype(np.float64)) / ok_).astype(rd)
+        smu[sel] = rd(sm)
+        skap[sel] = rd(sk)
+    out = dict(factor_common=np.ascontiguousarray(fcm).reshape(-1),
+               factor_common_kappa=np.ascontiguousarray(fck).reshape(-1),
+               mustore=(db["mustore"] * smu.reshape(-1)).astype(rd),
+               kappastore=(db["kappastore"] * skap.reshape(-1)).astype(rd),
+               tau_sigma=tau_f, f_c_source=fc.value, min_period=tmin.value, max_period=tmax.value,
+               min_resolved_period=mrp)
+    al, be, ga = (np.zeros(N_SLS, rd) for _ in range(3))
+    rt = ctypes.c_float if precision == "f32" else ctypes.c_double
+    L.orc_attenuation_memory_values.argtypes = [ctypes.c_void_p, rt, ctypes.c_void_p, ctypes.c_void_p,
+                                                ctypes.c_void_p]
+    L.orc_attenuation_memory_values(_p(tau_f), rt(rd(cfg["dt"])), _p(al), _p(be), _p(ga))
+    out.update(alphaval=al, betaval=be, gammaval=ga, attenuation=1)
+    return out
+
+
+# ----------------------------------------------------------------------------
+# fluid domain set-up (generate_databases/get_coupling_surfaces.f90:240-380,
+# shared/define_mass_matrices.f90:100-160, :460-520)
+# ----------------------------------------------------------------------------
+
+_FACE_CORNERS = {1: [(0, 0, 0), (0, 4, 0), (0, 4, 4), (0, 0, 4)], 2: [(4, 0, 0), (4, 4, 0), (4, 4, 4), (4, 0, 4)],
+                 3: [(0, 0, 0), (4, 0, 0), (4, 0, 4), (0, 0, 4)], 4: [(0, 4, 0), (4, 4, 0), (4, 4, 4), (0, 4, 4)],
+                 5: [(0, 0, 0), (4, 0, 0), (4, 4, 0), (0, 4, 0)], 6: [(0, 0, 4), (4, 0, 4), (4, 4, 4), (0, 4, 4)]}
+_FACE_MID = {1: (0, 2, 2), 2: (4, 2, 2), 3: (2, 0, 2), 4: (2, 4, 2), 5: (2, 2, 0), 6: (2, 2, 4)}
+
+
+def fluid_setup(db: dict, cfg: dict, precision: str = "f32") -> dict:
+    """Fluid flags, fluid-solid coupling faces (every face of a fluid element whose
+    four corners and midpoint are shared with solid elements, first time seen),
+    free-surface faces and the fluid mass matrix with its Stacey term."""
+    L = lib(precision)
+    rd = real_dtype(precision)
+    nspec, nglob = db["nspec"], db["nglob"]
+    ib = db["ibool"].reshape(nspec, NGLL3) - 1
+    vs = np.asarray(db["vs"], np.float32).reshape(nspec, NGLL3)
+    isac = (vs == 0).all(axis=1)
+    out = {"ispec_is_acoustic": isac.astype(np.int32)}
+    elastic_flag = np.zeros(nglob, np.int32)
+    for e in np.nonzero(~isac)[0]:
+        elastic_flag[ib[e]] = 1
+    mask = np.zeros(nglob, bool)
+    faces = []
+    for e in np.nonzero(isac)[0]:
+        for f in range(1, 7):
+            corners = [ib[e][i + 5 * j + 25 * k] for i, j, k in _FACE_CORNERS[f]]
+            if all(elastic_flag[c] >= 1 for c in corners):
+                i, j, k = _FACE_MID[f]
+                mid = ib[e][i + 5 * j + 25 * k]
+                fijk = np.zeros(75, np.int32)
+                jw = np.zeros(25, rd)
+                nn = np.zeros(75, rd)
+                L.orc_face_geometry(_p(db["anchors"][24 * e:]), f, _p(fijk), _p(jw), _p(nn))
+                pts = [ib[e][(fijk[3 * g] - 1) + 5 * (fijk[3 * g + 1] - 1) + 25 * (fijk[3 * g + 2] - 1)] for g in range(25)]
+                if not mask[mid] and elastic_flag[mid] >= 1:
+                    faces.append((e + 1, fijk, jw, nn))
+                mask[pts] = True
+    nf = len(faces)
+    out["num_coupling_ac_el_faces"] = nf
+    out["coupling_ac_el_ispec"] = np.array([f[0] for f in faces], np.int32)
+    out["coupling_ac_el_ijk"] = np.concatenate([f[1] for f in faces]) if nf else np.zeros(0, np.int32)
+    out["coupling_ac_el_jacobian2Dw"] = np.concatenate([f[2] for f in faces]) if nf else np.zeros(0, rd)
+    out["coupling_ac_el_normal"] = np.concatenate([f[3] for f in faces]) if nf else np.zeros(0, rd)
+    # free surface: top faces of the block (face 6 of the top element row)
+    nx, ny = int(cfg["nx"]), int(cfg["ny"])
+    nz = len(cfg["zlev"]) - 1
+    top = np.arange(nx * ny * (nz - 1), nx * ny * nz)
+    fs_ijk = np.zeros(75, np.int32)
+    _jw = np.zeros(25, rd)
+    _n = np.zeros(75, rd)
+    L.orc_face_geometry(_p(db["anchors"]), 6, _p(fs_ijk), _p(_jw), _p(_n))
+    out["num_free_surface_faces"] = len(top)
+    out["free_surface_ispec"] = (top + 1).astype(np.int32)
+    out["free_surface_ijk"] = np.tile(fs_ijk, len(top))
+    # fluid mass matrix: sum J w / kappa, plus dt/2 jw / (rho vp) on absorbing faces
+    x, w = gll()
+    w3 = np.array([w[i] * w[j] * w[k] for k in range(5) for j in range(5) for i in range(5)])
+    irr = db["irregular_element_number"]
+    rma = np.zeros(nglob, rd)
+    kap = db["kappastore"].reshape(nspec, NGLL3)
+    for e in np.nonzero(isac)[0]:
+        jl = (db["jacobian"].reshape(-1, NGLL3)[irr[e] - 1] if irr[e] else np.full(NGLL3, db["jacobian_regular"]))
+        terms = (jl.astype(np.float64) * w3 / kap[e].astype(np.float64)).astype(rd)
+        for p in range(NGLL3):
+            rma[ib[e][p]] += terms[p]
+    if db.get("stacey", 0):
+        dt2 = rd(0.5 * float(cfg["dt"]))
+        nfa = db["num_abs_boundary_faces"]
+        for fidx in range(nfa):
+            e = db["abs_boundary_ispec"][fidx] - 1
+            if not isac[e]:
+                continue
+            for g in range(25):
+                i, j, k = (db["abs_boundary_ijk"][3 * (g + 25 * fidx) + c] - 1 for c in range(3))
+                q = e * NGLL3 + i + 5 * j + 25 * k
+                rma[ib[e][i + 5 * j + 25 * k]] += db["abs_boundary_jacobian2Dw"][g + 25 * fidx] * (dt2 / db["rho_vp"][q])
+    rma[rma <= 0] = 1
+    out["rmass_acoustic"] = (rd(1) / rma).astype(rd)
+    # solid mass only over solid elements
+    m = np.zeros(nglob, rd)
+    for e in np.nonzero(~isac)[0]:
+        jl = (db["jacobian"].reshape(-1, NGLL3)[irr[e] - 1] if irr[e] else np.full(NGLL3, db["jacobian_regular"]))
+        terms = (jl.astype(np.float64) * w3 * db["rhostore"].reshape(nspec, NGLL3)[e].astype(np.float64)).astype(rd)
+        for p in range(NGLL3):
+            m[ib[e][p]] += terms[p]
+    out["rmass_solid"] = m
+    return out
+
+
+def make_coupled_sim(db: dict, cfg: dict, precision: str = "f32", nthreads: int = 1) -> OracleSim:
+    """Oracle coupled fluid-solid simulation on the given database arrays."""
+    rd = real_dtype(precision)
+    s = make_sim(db, cfg, precision, nthreads)
+    isac = np.asarray(db["ispec_is_acoustic"], np.int32)
+    s.set("ispec_is_acoustic", isac)
+    el = (np.nonzero(isac == 0)[0] + 1).astype(np.int32)
+    ac = (np.nonzero(isac)[0] + 1).astype(np.int32)
+    s.set("elastic_list", el)
+    s.seti("n_elastic", len(el))
+    s.set("acoustic_list", ac)
+    s.seti("n_acoustic", len(ac))
+    s.set("rhostore", np.asarray(db["rhostore"], rd))
+    for n in ["potential", "potential_dot", "potential_dot_dot"]:
+        s.set(n, np.zeros(int(db["nglob"]), rd))
+    s.set("rmass_acoustic", np.asarray(db["rmass_acoustic"], rd))
+    s.seti("num_coupling_faces", int(db["num_coupling_ac_el_faces"]))
+    s.set("coupling_ispec", np.asarray(db["coupling_ac_el_ispec"], np.int32))
+    s.set("coupling_ijk", np.asarray(db["coupling_ac_el_ijk"], np.int32))
+    s.set("coupling_normal", np.asarray(db["coupling_ac_el_normal"], rd))
+    s.set("coupling_jacobian2Dw", np.asarray(db["coupling_ac_el_jacobian2Dw"], rd))
+    s.seti("num_free_surface_faces", int(db["num_free_surface_faces"]))
+    s.set("free_surface_ispec", np.asarray(db["free_surface_ispec"], np.int32))
+    s.set("free_surface_ijk", np.asarray(db["free_surface_ijk"], np.int32))
+    recs = np.asarray(db["ispec_selected_rec"], np.int64) - 1
+    s.set("rec_is_acoustic", isac[recs].astype(np.int32) if len(recs) else np.zeros(1, np.int32))
+    s.L.orc_run_coupled.argtypes = [ctypes.c_void_p, ctypes.c_int]
+    return s
+
+
+def run_coupled(sim: OracleSim, nsteps: int) -> None:
+    sim.L.orc_run_coupled(sim.h, int(nsteps))

@@ -37,12 +37,16 @@ static const orc_field k_ptr_fields[] = {
   F(nu_rec), F(seismograms), F(displ), F(veloc), F(accel), F(b_displ), F(b_veloc), F(b_accel),
   F(b_epsilondev_xx), F(b_epsilondev_yy), F(b_epsilondev_xy), F(b_epsilondev_xz),
   F(b_epsilondev_yz), F(b_epsilon_trace_over_3), F(rho_kl), F(mu_kl), F(kappa_kl),
-  F(source_adjoint), F(hxir_adj), F(hetar_adj), F(hgammar_adj),
+  F(source_adjoint), F(hxir_adj), F(hetar_adj), F(hgammar_adj), F(elastic_list), F(acoustic_list),
+  F(ispec_is_acoustic), F(potential), F(potential_dot), F(potential_dot_dot), F(rmass_acoustic),
+  F(coupling_ispec), F(coupling_ijk), F(coupling_normal), F(coupling_jacobian2Dw), F(free_surface_ispec),
+  F(free_surface_ijk), F(rec_is_acoustic),
 };
 static const orc_field k_int_fields[] = {
   F(nspec), F(nglob), F(nspec_irregular), F(nsources), F(nrec), F(nstep), F(it),
   F(attenuation), F(stacey), F(compute_and_store_strain), F(simulation_type), F(nthreads),
-  F(record_what), F(num_abs_boundary_faces),
+  F(record_what), F(num_abs_boundary_faces), F(n_elastic), F(n_acoustic), F(num_coupling_faces),
+  F(num_free_surface_faces),
 };
 static const orc_field k_real_fields[] = {
   F(xix_regular), F(jacobian_regular), F(deltat), F(deltatover2), F(deltatsqover2),
@@ -55,7 +59,7 @@ int orc_realw_size(void) { return (int)sizeof(realw); }
 
 orc_sim *orc_sim_new(void) {
   orc_sim *s = (orc_sim *)calloc(1, sizeof(orc_sim));
-  if (s) { s->nthreads = 1; s->record_what = 1; s->simulation_type = 1; s->it = 1; }
+  if (s) { s->nthreads = 1; s->record_what = 1; s->simulation_type = 1; s->it = 1; s->n_elastic = -1; }
   return s;
 }
 void orc_sim_free(orc_sim *s) { free(s); }
@@ -892,17 +896,22 @@ void orc_compute_forces_elastic(orc_sim *s, int backward) {
   realw dt = backward ? s->b_deltat : s->deltat;
   realw **E = backward ? bep : eps;
   realw *tr3 = backward ? s->b_epsilon_trace_over_3 : s->epsilon_trace_over_3;
+  const int n = s->n_elastic < 0 ? s->nspec : s->n_elastic;
 #ifdef _OPENMP
   omp_set_num_threads(s->nthreads > 0 ? s->nthreads : 1);
 #pragma omp parallel for schedule(static)
 #endif
-  for (int ispec = 0; ispec < s->nspec; ++ispec) element_forces(s, ispec, d, v, a, dt, R, E, tr3, backward);
+  for (int q = 0; q < n; ++q) {
+    const int ispec = s->n_elastic < 0 ? q : s->elastic_list[q] - 1;
+    element_forces(s, ispec, d, v, a, dt, R, E, tr3, backward);
+  }
 }
 
 /* compute_stacey_viscoelastic_forward (compute_stacey_viscoelastic.F90:32-206) */
 void orc_stacey_elastic(orc_sim *s, const realw *veloc, realw *accel) {
   for (int f = 0; f < s->num_abs_boundary_faces; ++f) {
     int ispec = s->abs_boundary_ispec[f] - 1;
+    if (s->ispec_is_acoustic && s->ispec_is_acoustic[ispec]) continue;
     for (int g = 0; g < NGLL2; ++g) {
       const int *ijk = s->abs_boundary_ijk + 3 * (g + NGLL2 * f);
       long p = IJK(ijk[0] - 1, ijk[1] - 1, ijk[2] - 1) + (long)NGLL3 * ispec;
@@ -925,6 +934,7 @@ void orc_add_sources(orc_sim *s, realw *accel, int it) {
   for (int isrc = 0; isrc < s->nsources; ++isrc) {
     realw stf = (realw)s->stf[isrc + (long)s->nsources * (it - 1)];
     int ispec = s->ispec_selected_source[isrc] - 1;
+    if (s->ispec_is_acoustic && s->ispec_is_acoustic[ispec]) continue;
     for (int p = 0; p < NGLL3; ++p) {
       long ig = s->ibool[(long)NGLL3 * ispec + p] - 1;
       for (int c = 0; c < 3; ++c)
@@ -938,6 +948,20 @@ void orc_add_sources(orc_sim *s, realw *accel, int it) {
 void orc_seismograms(orc_sim *s, const realw *field, int it) {
   for (int r = 0; r < s->nrec; ++r) {
     int ispec = s->ispec_selected_rec[r] - 1;
+    if (s->rec_is_acoustic && s->rec_is_acoustic[r]) {
+      /* pressure = - sum h chi_dot_dot (compute_interpolated_dva.f90:280-300) */
+      double pd = 0.0;
+      for (int k = 0; k < NGLL; ++k)
+        for (int j = 0; j < NGLL; ++j)
+          for (int i = 0; i < NGLL; ++i) {
+            double h = s->hxir[i + NGLL * r] * s->hetar[j + NGLL * r] * s->hgammar[k + NGLL * r];
+            long ig = s->ibool[IJK(i, j, k) + (long)NGLL3 * ispec] - 1;
+            pd -= h * (double)s->potential_dot_dot[ig];
+          }
+      for (int c = 0; c < 3; ++c)
+        s->seismograms[c + 3 * (r + (long)s->nrec * (it - 1))] = c == 0 ? (double)(realw)pd : 0.0;
+      continue;
+    }
     double u[3] = {0, 0, 0};
     for (int k = 0; k < NGLL; ++k)
       for (int j = 0; j < NGLL; ++j)
@@ -979,4 +1003,343 @@ void orc_step(orc_sim *s) {
 
 void orc_run(orc_sim *s, int nsteps) {
   for (int n = 0; n < nsteps; ++n) orc_step(s);
+}
+
+/* ------------------------------------------------------------------------- */
+/* attenuation model (shared/get_attenuation_model.f90)                       */
+/* ------------------------------------------------------------------------- */
+
+#define ATT_NF 100
+static double g_att_f[ATT_NF], g_att_tau_s[N_SLS], g_att_iQ;
+
+/* attenuation_maxwell + attenuation_eval (get_attenuation_model.f90:1100-1215) */
+static double att_eval(const double *tau_eps) {
+  const double PI = 3.14159265358979;
+  double sum = 0.0, iQ2 = g_att_iQ * g_att_iQ;
+  for (int i = 0; i < ATT_NF; ++i) {
+    double w = 2.0 * PI * pow(10.0, g_att_f[i]), A = 0.0, B = 0.0;
+    for (int j = 0; j < N_SLS; ++j) {
+      double denom = 1.0 + w * w * g_att_tau_s[j] * g_att_tau_s[j];
+      A += (1.0 + (w * w * tau_eps[j] * g_att_tau_s[j])) / denom;
+      B += w * (tau_eps[j] - g_att_tau_s[j]) / denom;
+    }
+    double td = B / A;
+    sum += sqrt(((td - g_att_iQ) * (td - g_att_iQ)) / iQ2);
+  }
+  return sum;
+}
+
+/* bubble sort of fv with permutation (qsort_local, :1558-1607) */
+static void att_sort(double *fv, int *place, int n) {
+  for (int j = 0; j < n; ++j) place[j] = j;
+  for (int j = 0; j < n; ++j)
+    for (int k = 0; k < n - 1 - j; ++k)
+      if (fv[k + 1] < fv[k]) {
+        double r = fv[k]; fv[k] = fv[k + 1]; fv[k + 1] = r;
+        int t = place[k]; place[k] = place[k + 1]; place[k + 1] = t;
+      }
+}
+
+/* Nelder-Mead search of fminsearch (:1222-1473) with tolx = tolf = 1e-4. */
+static void att_fminsearch(double *x) {
+  const int n = N_SLS;
+  const double rho = 1.0, chi = 2.0, psi = 0.5, sigma = 0.5, tolx = 1.0e-4, tolf = 1.0e-4;
+  const int maxiter = 200 * n, maxfun = 200 * n;
+  double v[N_SLS][N_SLS + 1], fv[N_SLS + 1], vt[N_SLS][N_SLS + 1];
+  int place[N_SLS + 1];
+  for (int i = 0; i < n; ++i) v[i][0] = x[i];
+  fv[0] = att_eval(x);
+  for (int j = 0; j < n; ++j) {
+    double y[N_SLS];
+    for (int i = 0; i < n; ++i) y[i] = x[i];
+    y[j] = y[j] != 0.0 ? (1.0 + 0.05) * y[j] : 0.00025;
+    for (int i = 0; i < n; ++i) v[i][j + 1] = y[i];
+    fv[j + 1] = att_eval(y);
+  }
+  att_sort(fv, place, n + 1);
+  for (int j = 0; j <= n; ++j) for (int i = 0; i < n; ++i) vt[i][j] = v[i][place[j]];
+  memcpy(v, vt, sizeof(v));
+  int itercount = 1, func_evals = n + 1;
+  while (func_evals < maxfun && itercount < maxiter) {
+    double ms = 0.0, mv = 0.0;
+    for (int i = 0; i < n; ++i) for (int j = 1; j <= n; ++j) { double z = fabs(v[i][j] - v[i][0]); if (z > ms) ms = z; }
+    for (int j = 1; j <= n; ++j) { double z = fabs(fv[0] - fv[j]); if (z > mv) mv = z; }
+    if (ms <= tolx && mv <= tolf) break;
+    double xbar[N_SLS], xr[N_SLS], xe[N_SLS], xc[N_SLS], xcc[N_SLS];
+    for (int i = 0; i < n; ++i) { xbar[i] = 0; for (int j = 0; j < n; ++j) xbar[i] += v[i][j]; xbar[i] /= (double)n; }
+    for (int i = 0; i < n; ++i) xr[i] = (1 + rho) * xbar[i] - rho * v[i][n];
+    double fxr = att_eval(xr); func_evals++;
+    int shrink = 0;
+    if (fxr < fv[0]) {
+      for (int i = 0; i < n; ++i) xe[i] = (1 + rho * chi) * xbar[i] - rho * chi * v[i][n];
+      double fxe = att_eval(xe); func_evals++;
+      if (fxe < fxr) { for (int i = 0; i < n; ++i) v[i][n] = xe[i]; fv[n] = fxe; }
+      else { for (int i = 0; i < n; ++i) v[i][n] = xr[i]; fv[n] = fxr; }
+    } else if (fxr < fv[n - 1]) {
+      for (int i = 0; i < n; ++i) v[i][n] = xr[i];
+      fv[n] = fxr;
+    } else {
+      if (fxr < fv[n]) {
+        for (int i = 0; i < n; ++i) xc[i] = (1 + psi * rho) * xbar[i] - psi * rho * v[i][n];
+        double fxc = att_eval(xc); func_evals++;
+        if (fxc <= fxr) { for (int i = 0; i < n; ++i) v[i][n] = xc[i]; fv[n] = fxc; } else shrink = 1;
+      } else {
+        for (int i = 0; i < n; ++i) xcc[i] = (1 - psi) * xbar[i] + psi * v[i][n];
+        double fxcc = att_eval(xcc); func_evals++;
+        if (fxcc < fv[n]) { for (int i = 0; i < n; ++i) v[i][n] = xcc[i]; fv[n] = fxcc; } else shrink = 1;
+      }
+      if (shrink) {
+        for (int j = 1; j <= n; ++j) {
+          double xx[N_SLS];
+          for (int i = 0; i < n; ++i) { v[i][j] = v[i][0] + sigma * (v[i][j] - v[i][0]); xx[i] = v[i][j]; }
+          fv[j] = att_eval(xx);
+        }
+        func_evals += n;
+      }
+    }
+    att_sort(fv, place, n + 1);
+    for (int j = 0; j <= n; ++j) for (int i = 0; i < n; ++i) vt[i][j] = v[i][place[j]];
+    memcpy(v, vt, sizeof(v));
+    itercount++;
+  }
+  for (int i = 0; i < n; ++i) x[i] = v[i][0];
+}
+
+/* get_attenuation_periods / _tau_sigma / _source_freq (:702-810) from the
+ * minimum resolved period; outputs tau_sigma (double), f_c_source, band. */
+void orc_attenuation_constants(double min_resolved_period_f32, double *tau_sigma, double *f_c_source,
+                               double *min_period, double *max_period) {
+  const double PI = 3.14159265358979;
+  float minp = (float)(0.99f * (float)min_resolved_period_f32);
+  *min_period = minp;
+  *max_period = *min_period * pow(10.0, 1.75);
+  double f1 = 1.0 / *max_period, f2 = 1.0 / *min_period;
+  double e1 = log10(f1), e2 = log10(f2), d = (e2 - e1) / ((double)N_SLS - 1);
+  for (int i = 0; i < N_SLS; ++i) tau_sigma[i] = 1.0 / (PI * 2.0 * pow(10.0, e1 + i * 1.0 * d));
+  *f_c_source = pow(10.0, 0.5 * (log10(f1) + log10(f2)));
+}
+
+/* get_attenuation_tau_eps via attenuation_invert_by_simplex (:838-1058) and the
+ * derived factors (get_attenuation_property_values, _scale_factor, :599-694).
+ * Outputs beta(N_SLS), one_minus_sum_beta, scale_factor for one Q value. */
+void orc_attenuation_factors(double Q, const double *tau_sigma, double min_period, double max_period,
+                             double f_c_source, double f0_reference, double *beta, double *one_minus_sum_beta,
+                             double *scale_factor, double *tau_eps_out) {
+  const double PI = 3.141592653589793, TWO_PI = 2.0 * PI;
+  double tau_eps[N_SLS];
+  double f1 = 1.0 / max_period, f2 = 1.0 / min_period, e1 = log10(f1), e2 = log10(f2);
+  for (int i = 0; i < ATT_NF; ++i) g_att_f[i] = e1 + (i * 1.0 * (e2 - e1) / ((ATT_NF - 1) * 1.0));
+  for (int i = 0; i < N_SLS; ++i) g_att_tau_s[i] = tau_sigma[i];
+  g_att_iQ = 1.0 / Q;
+  for (int i = 0; i < N_SLS; ++i) tau_eps[i] = tau_sigma[i] + (tau_sigma[i] * 2.0 / Q);
+  att_fminsearch(tau_eps);
+  double s = 0.0;
+  for (int i = 0; i < N_SLS; ++i) { beta[i] = tau_eps[i] / tau_sigma[i]; s += beta[i]; beta[i] -= 1.0; }
+  *one_minus_sum_beta = s;
+  double mu0 = 1.0 + 2.0 * log(f_c_source / f0_reference) / (PI * Q);
+  double x1 = 1.0, x2 = 1.0;
+  for (int i = 0; i < N_SLS; ++i) {
+    double ak = tau_eps[i] / tau_sigma[i] - 1.0;
+    x1 += ak / N_SLS;
+    x2 += ak / (1.0 + 1.0 / pow(TWO_PI * f_c_source * tau_sigma[i], 2)) / N_SLS;
+  }
+  *scale_factor = (x1 / x2) * mu0;
+  if (tau_eps_out) for (int i = 0; i < N_SLS; ++i) tau_eps_out[i] = tau_eps[i];
+}
+
+/* get_attenuation_memory_values (:464-493) in CUSTOM_REAL. */
+void orc_attenuation_memory_values(const realw *tau_s, realw deltat, realw *alphaval, realw *betaval,
+                                   realw *gammaval) {
+  for (int i = 0; i < N_SLS; ++i) {
+    realw ti = (realw)-1 / tau_s[i];
+    realw d2 = deltat * deltat, d3 = d2 * deltat, d4 = d3 * deltat;
+    alphaval[i] = (realw)1.0 + deltat * ti + d2 * (ti * ti) / (realw)2 + d3 * (ti * ti * ti) / (realw)6 +
+                  d4 * (ti * ti * ti * ti) / (realw)24;
+    betaval[i] = deltat / (realw)2 + d2 * ti / (realw)3 + d3 * (ti * ti) / (realw)8 + d4 * (ti * ti * ti) / (realw)24;
+    gammaval[i] = deltat / (realw)2 + d2 * ti / (realw)6 + d3 * (ti * ti) / (realw)24;
+  }
+}
+
+/* ------------------------------------------------------------------------- */
+/* acoustic domain and fluid-solid coupling                                   */
+/* ------------------------------------------------------------------------- */
+
+/* Acoustic stiffness of one element (compute_forces_acoustic.F90:130-340):
+ * chi_dot_dot -= w . hprimewgll^T (J/rho grad(xi) . grad chi). */
+static void element_forces_acoustic(const orc_sim *s, int ispec, const realw *pot, realw *pot_dd) {
+  const realw *hp = s->hprime_xx, *hpw = s->hprimewgll_xx;
+  realw chi[NGLL3], t1[NGLL3], t2[NGLL3], t3[NGLL3];
+  const int *ib = s->ibool + (long)NGLL3 * ispec;
+  for (int p = 0; p < NGLL3; ++p) chi[p] = pot[ib[p] - 1];
+  for (int k = 0; k < NGLL; ++k)
+    for (int j = 0; j < NGLL; ++j)
+      for (int i = 0; i < NGLL; ++i) {
+        realw a = 0, b = 0, c = 0;
+        for (int l = 0; l < NGLL; ++l) {
+          a += chi[IJK(l, j, k)] * hp[i + NGLL * l];
+          b += chi[IJK(i, l, k)] * hp[j + NGLL * l];
+          c += chi[IJK(i, j, l)] * hp[k + NGLL * l];
+        }
+        int p = IJK(i, j, k);
+        t1[p] = a; t2[p] = b; t3[p] = c;
+      }
+  const int ir = s->irregular_element_number[ispec];
+  const long mo = (long)NGLL3 * (ir - 1);
+  for (int p = 0; p < NGLL3; ++p) {
+    realw rho_inv = (realw)1.0 / s->rhostore[(long)NGLL3 * ispec + p];
+    if (ir) {
+      realw xixl = s->xix[mo + p], xiyl = s->xiy[mo + p], xizl = s->xiz[mo + p];
+      realw etaxl = s->etax[mo + p], etayl = s->etay[mo + p], etazl = s->etaz[mo + p];
+      realw gxl = s->gammax[mo + p], gyl = s->gammay[mo + p], gzl = s->gammaz[mo + p];
+      realw jl = s->jacobian[mo + p];
+      realw dx = xixl * t1[p] + etaxl * t2[p] + gxl * t3[p];
+      realw dy = xiyl * t1[p] + etayl * t2[p] + gyl * t3[p];
+      realw dz = xizl * t1[p] + etazl * t2[p] + gzl * t3[p];
+      t1[p] = rho_inv * jl * (xixl * dx + xiyl * dy + xizl * dz);
+      t2[p] = rho_inv * jl * (etaxl * dx + etayl * dy + etazl * dz);
+      t3[p] = rho_inv * jl * (gxl * dx + gyl * dy + gzl * dz);
+    } else {
+      realw f = rho_inv * s->jacobian_regular * s->xix_regular * s->xix_regular;
+      t1[p] = f * t1[p]; t2[p] = f * t2[p]; t3[p] = f * t3[p];
+    }
+  }
+  for (int k = 0; k < NGLL; ++k)
+    for (int j = 0; j < NGLL; ++j)
+      for (int i = 0; i < NGLL; ++i) {
+        realw a = 0, b = 0, c = 0;
+        for (int l = 0; l < NGLL; ++l) {
+          a += t1[IJK(l, j, k)] * hpw[l + NGLL * i];
+          b += t2[IJK(i, l, k)] * hpw[l + NGLL * j];
+          c += t3[IJK(i, j, l)] * hpw[l + NGLL * k];
+        }
+        long g = ib[IJK(i, j, k)] - 1;
+        realw add = s->wgllwgll_yz[j + NGLL * k] * a + s->wgllwgll_xz[i + NGLL * k] * b + s->wgllwgll_xy[i + NGLL * j] * c;
+#pragma omp atomic
+        pot_dd[g] -= add;
+      }
+}
+
+void orc_compute_forces_acoustic(orc_sim *s) {
+#ifdef _OPENMP
+  omp_set_num_threads(s->nthreads > 0 ? s->nthreads : 1);
+#pragma omp parallel for schedule(static)
+#endif
+  for (int q = 0; q < s->n_acoustic; ++q) element_forces_acoustic(s, s->acoustic_list[q] - 1, s->potential, s->potential_dot_dot);
+}
+
+/* compute_stacey_acoustic_forward (compute_stacey_acoustic.f90:79-125) */
+static void stacey_acoustic(orc_sim *s) {
+  for (int f = 0; f < s->num_abs_boundary_faces; ++f) {
+    int ispec = s->abs_boundary_ispec[f] - 1;
+    if (!s->ispec_is_acoustic || !s->ispec_is_acoustic[ispec]) continue;
+    for (int g = 0; g < NGLL2; ++g) {
+      const int *ijk = s->abs_boundary_ijk + 3 * (g + NGLL2 * f);
+      long p = IJK(ijk[0] - 1, ijk[1] - 1, ijk[2] - 1) + (long)NGLL3 * ispec;
+      long ig = s->ibool[p] - 1;
+      realw rhol = s->rhostore[p];
+      realw cpl = (realw)sqrt((double)(s->kappastore[p] / rhol));
+      realw jw = s->abs_boundary_jacobian2Dw[g + NGLL2 * f];
+      realw absorbl = s->potential_dot[ig] * jw / cpl / rhol;
+      s->potential_dot_dot[ig] -= absorbl;
+    }
+  }
+}
+
+/* compute_coupling_acoustic_el (compute_coupling_acoustic_el.f90:70-150):
+ * chi_dot_dot += jw (u . n), n pointing out of the fluid. */
+static void coupling_acoustic_el(orc_sim *s) {
+  for (int f = 0; f < s->num_coupling_faces; ++f) {
+    int ispec = s->coupling_ispec[f] - 1;
+    for (int g = 0; g < NGLL2; ++g) {
+      const int *ijk = s->coupling_ijk + 3 * (g + NGLL2 * f);
+      long ig = s->ibool[IJK(ijk[0] - 1, ijk[1] - 1, ijk[2] - 1) + (long)NGLL3 * ispec] - 1;
+      const realw *n = s->coupling_normal + 3 * (g + NGLL2 * f);
+      realw dn = s->displ[3 * ig] * n[0] + s->displ[3 * ig + 1] * n[1] + s->displ[3 * ig + 2] * n[2];
+      s->potential_dot_dot[ig] += s->coupling_jacobian2Dw[g + NGLL2 * f] * dn;
+    }
+  }
+}
+
+/* compute_coupling_viscoelastic_ac (compute_coupling_viscoelastic_ac.f90:70-160):
+ * accel += jw n (-chi_dot_dot). */
+static void coupling_elastic_ac(orc_sim *s) {
+  for (int f = 0; f < s->num_coupling_faces; ++f) {
+    int ispec = s->coupling_ispec[f] - 1;
+    for (int g = 0; g < NGLL2; ++g) {
+      const int *ijk = s->coupling_ijk + 3 * (g + NGLL2 * f);
+      long ig = s->ibool[IJK(ijk[0] - 1, ijk[1] - 1, ijk[2] - 1) + (long)NGLL3 * ispec] - 1;
+      const realw *n = s->coupling_normal + 3 * (g + NGLL2 * f);
+      realw pr = -s->potential_dot_dot[ig];
+      realw jw = s->coupling_jacobian2Dw[g + NGLL2 * f];
+      s->accel[3 * ig] += jw * n[0] * pr;
+      s->accel[3 * ig + 1] += jw * n[1] * pr;
+      s->accel[3 * ig + 2] += jw * n[2] * pr;
+    }
+  }
+}
+
+/* compute_add_sources_acoustic (compute_add_sources_acoustic.f90:100-126):
+ * chi_dot_dot -= sourcearray(1) stf / kappa for sources in fluid elements. */
+static void add_sources_acoustic(orc_sim *s, int it) {
+  for (int isrc = 0; isrc < s->nsources; ++isrc) {
+    int ispec = s->ispec_selected_source[isrc] - 1;
+    if (!s->ispec_is_acoustic || !s->ispec_is_acoustic[ispec]) continue;
+    realw stf = (realw)s->stf[isrc + (long)s->nsources * (it - 1)];
+    for (int p = 0; p < NGLL3; ++p) {
+      long q = (long)NGLL3 * ispec + p;
+      long ig = s->ibool[q] - 1;
+      s->potential_dot_dot[ig] -= s->sourcearrays[isrc + (long)s->nsources * (0 + 3 * p)] * stf / s->kappastore[q];
+    }
+  }
+}
+
+/* acoustic_enforce_free_surface (compute_forces_acoustic_calling_routine.f90:754-810) */
+static void enforce_free_surface(orc_sim *s) {
+  for (int f = 0; f < s->num_free_surface_faces; ++f) {
+    int ispec = s->free_surface_ispec[f] - 1;
+    if (!s->ispec_is_acoustic[ispec]) continue;
+    for (int g = 0; g < NGLL2; ++g) {
+      const int *ijk = s->free_surface_ijk + 3 * (g + NGLL2 * f);
+      long ig = s->ibool[IJK(ijk[0] - 1, ijk[1] - 1, ijk[2] - 1) + (long)NGLL3 * ispec] - 1;
+      s->potential[ig] = 0; s->potential_dot[ig] = 0; s->potential_dot_dot[ig] = 0;
+    }
+  }
+}
+
+/* One coupled fluid-solid step (iterate_time.F90:219-300 with
+ * compute_forces_acoustic_calling_routine.f90:54-343 then
+ * compute_forces_viscoelastic_calling_routine.F90:107-417). */
+void orc_step_coupled(orc_sim *s) {
+  long n3 = 3L * s->nglob;
+  newmark_predictor(n3, s->displ, s->veloc, s->accel, s->deltat, s->deltatover2, s->deltatsqover2);
+  newmark_predictor(s->nglob, s->potential, s->potential_dot, s->potential_dot_dot, s->deltat, s->deltatover2,
+                    s->deltatsqover2);
+  /* fluid */
+  enforce_free_surface(s);
+  if (s->stacey) stacey_acoustic(s);
+  if (s->num_coupling_faces) coupling_acoustic_el(s);
+  if (s->nsources > 0 && s->stf) add_sources_acoustic(s, s->it);
+  orc_compute_forces_acoustic(s);
+  for (long g = 0; g < s->nglob; ++g) {
+    s->potential_dot_dot[g] *= s->rmass_acoustic[g];
+    s->potential_dot[g] += s->deltatover2 * s->potential_dot_dot[g];
+  }
+  enforce_free_surface(s);
+  /* solid */
+  if (s->stacey && s->num_abs_boundary_faces > 0) orc_stacey_elastic(s, s->veloc, s->accel);
+  if (s->num_coupling_faces) coupling_elastic_ac(s);
+  if (s->nsources > 0 && s->stf) orc_add_sources(s, s->accel, s->it);
+  orc_compute_forces_elastic(s, 0);
+  for (long g = 0; g < s->nglob; ++g) {
+    s->accel[3 * g] *= s->rmassx[g];
+    s->accel[3 * g + 1] *= s->rmassy[g];
+    s->accel[3 * g + 2] *= s->rmassz[g];
+  }
+  for (long i = 0; i < n3; ++i) s->veloc[i] += s->deltatover2 * s->accel[i];
+  if (s->nrec > 0 && s->seismograms) orc_seismograms(s, s->displ, s->it);
+  s->it++;
+}
+
+void orc_run_coupled(orc_sim *s, int nsteps) {
+  for (int n = 0; n < nsteps; ++n) orc_step_coupled(s);
 }

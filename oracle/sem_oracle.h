@@ -83,6 +83,16 @@ typedef struct orc_sim {
   double *rho_kl, *mu_kl, *kappa_kl;   /* (125, nspec) accumulated in FP64 */
   realw *source_adjoint;               /* (3, nrec, nstep) adjoint source traces */
   double *hxir_adj, *hetar_adj, *hgammar_adj;
+
+  /* acoustic domain and fluid-solid coupling */
+  int n_elastic, n_acoustic;           /* element lists (1-based ispec); n_elastic<0: all elastic */
+  int *elastic_list, *acoustic_list;
+  int *ispec_is_acoustic;              /* (nspec) 0/1 */
+  realw *potential, *potential_dot, *potential_dot_dot, *rmass_acoustic;
+  int num_coupling_faces, *coupling_ispec, *coupling_ijk;
+  realw *coupling_normal, *coupling_jacobian2Dw;
+  int num_free_surface_faces, *free_surface_ispec, *free_surface_ijk;
+  int *rec_is_acoustic;                /* (nrec) records pressure when 1 */
 } orc_sim;
 
 #endif

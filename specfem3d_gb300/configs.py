@@ -118,7 +118,10 @@ def refex(nstep: int = 5000) -> dict:
                zlev=list(np.linspace(-60000.0, 0.0, 17)), elem_layer=None,
                layers=[dict(rho=2300.0, vp=2800.0, vs=1500.0)], dt=0.05, nstep=nstep,
                sources=[dict(type="cmt", x=67000.0, y=67000.0, z=-30000.0, M=M, stf="heaviside", hdur=5.0)],
-               receivers=[(x, 67000.0, 0.0) for x in (22732.14, 34696.43, 46660.71, 58625.00)],
+               # the REF_SEIS run located its stations at the coordinates printed in its
+               # output_solver.txt (22732.0996, 34696.3984, ...): STATIONS values kept to
+               # six significant digits
+               receivers=[(x, 67000.0, 0.0) for x in (22732.1, 34696.4, 46660.7, 58625.0)],
                station_names=["X20", "X30", "X40", "X50"])
     return finish(cfg)
 
@@ -204,3 +207,47 @@ def cfg3(nstep: int = 3000, nshots: int = 32, seed: int = 2026) -> dict:
                sources=shots[:1], shots=shots,
                receivers=[(float(x), float(y), 0.0) for y in g for x in g], vmax_factor=1.05)
     return finish(cfg)
+
+
+def cfg2(nstep: int = 3000, nx: int = 96, ny: int = 96, nz: int = 48, fluid_layers: int = 8, seed: int = 2027) -> dict:
+    """Coupled fluid/solid block: the top sixth of the depth is water
+    (vp 1500, rho 1020), the rest a solid of (3000, 1700, 2400) carrying a seeded
+    +-5 % Gaussian-correlated perturbation (1 km correlation length); pressure
+    source (3 Hz Ricker) in the water; hydrophones at mid water depth.  The
+    domain is the 20x20x10 km block of the layered workload."""
+    zlev = list(np.linspace(-10000.0, 0.0, nz + 1))
+    rows = [1] * (nz - fluid_layers) + [0] * fluid_layers
+    zf = zlev[nz - fluid_layers]
+    g = np.linspace(20000.0 / 32, 20000.0 - 20000.0 / 32, 16)
+    x1 = 20000.0 * nx / 96
+    y1 = 20000.0 * ny / 96
+    g = np.linspace(x1 / 32, x1 - x1 / 32, 16)
+    cfg = dict(nx=nx, ny=ny, x0=0.0, x1=x1, y0=0.0, y1=y1, zlev=[float(z) for z in zlev],
+               elem_layer=np.repeat(np.asarray(rows, np.int32), nx * ny),
+               layers=[dict(rho=1020.0, vp=1500.0, vs=0.0), dict(rho=2400.0, vp=3000.0, vs=1700.0)],
+               dt=None, nstep=nstep, perturbation=dict(corr_len=1000.0, seed=seed),
+               sources=[dict(type="force", x=x1 / 2 + 13.0, y=y1 / 2 - 7.0, z=zf / 2, F=[1.0, 1.0, 1.0],
+                             stf="ricker", f0=3.0)],
+               receivers=[(float(x), float(y), float(zf / 2)) for y in g for x in g], record=("pressure",),
+               vmax_factor=1.05)
+    cfg["dt"] = _cfl_dt_by_rows(cfg, rows) if False else None
+    cfg = finish(cfg)
+    # CFL over both materials with the perturbation bound
+    dx = x1 / nx
+    dz = 10000.0 / nz
+    dmin = GLL_MIN_SPACING * min(dx, dz)
+    cfg["dt"] = significant_dt(COURANT_SUGGESTED * dmin / (3000.0 * 1.05))
+    return cfg
+
+
+def small_coupled(nx: int = 5, ny: int = 4, nz: int = 6, fluid_layers: int = 2, nstep: int = 300) -> dict:
+    """Small coupled block with the cfg2 physics for parity tests."""
+    cfg = cfg2(nstep=nstep, nx=nx, ny=ny, nz=nz, fluid_layers=fluid_layers)
+    h = 20000.0 / 96
+    cfg["x1"], cfg["y1"] = nx * h, ny * h
+    cfg["zlev"] = [float(-nz * h + q * h) for q in range(nz + 1)]
+    zf = cfg["zlev"][nz - fluid_layers]
+    cfg["sources"][0].update(x=cfg["x1"] / 2 + 13.0, y=cfg["y1"] / 2 - 7.0, z=zf / 2)
+    cfg["receivers"] = [(cfg["x1"] * 0.3, cfg["y1"] * 0.4, zf / 2), (cfg["x1"] * 0.7, cfg["y1"] * 0.6, zf / 2),
+                        (cfg["x1"] * 0.5, cfg["y1"] * 0.5, zf / 2 - 3.0)]
+    return cfg

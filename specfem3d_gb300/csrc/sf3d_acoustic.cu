@@ -1,0 +1,443 @@
+// Acoustic (fluid) domain and fluid-solid coupling.
+//
+// Replaces prepare_fields_acoustic_device (prepare_mesh_constants_cuda.cu:434),
+// compute_forces_acoustic_cuda / acoustic_enforce_free_surf_cuda
+// (compute_forces_acoustic_cuda.cu:238, :334), update_displacement_ac_cuda and
+// kernel_3_acoustic_cuda (update_displacement_cuda.cu:192, :448),
+// compute_stacey_acoustic_cuda (compute_stacey_acoustic_cuda.cu:39),
+// compute_coupling_ac_el_cuda / compute_coupling_el_ac_cuda
+// (compute_coupling_cuda.cu:39, :135), compute_add_sources_ac_cuda
+// (compute_add_sources_acoustic_cuda.cu:65) and the acoustic transfers.
+// The physics follows the reference CPU routines cited on each kernel.
+#include <vector>
+
+#include "sf3d_internal.h"
+
+namespace sf3d {
+namespace {
+
+inline unsigned nblk(long n, int b) { return (unsigned)((n + b - 1) / b); }
+
+// chi_dot_dot -= w . hprimewgll^T ( J/rho grad(xi) . grad chi )
+// (compute_forces_acoustic.F90:130-340); one 128-thread CTA per element.
+__global__ void __launch_bounds__(NGLL3_PAD, 8)
+    acoustic_stiffness_kernel(int nelem, const int* __restrict__ phase, const int* __restrict__ ibool,
+                              const int* __restrict__ irregular, const float* __restrict__ m0,
+                              const float* __restrict__ m1, const float* __restrict__ m2, const float* __restrict__ m3,
+                              const float* __restrict__ m4, const float* __restrict__ m5,
+                              const float* __restrict__ m6, const float* __restrict__ m7,
+                              const float* __restrict__ m8, const float* __restrict__ rhostore,
+                              const float* __restrict__ gll, float xix_regular, float jacobian_regular,
+                              const float* __restrict__ pot, float* __restrict__ pot_dd) {
+  __shared__ float s_gll[NGLL3];
+  __shared__ float s_chi[NGLL3_PAD];
+  __shared__ float s_t[3][NGLL3_PAD];
+  const int t = threadIdx.x;
+  const int e = phase ? __ldg(phase + blockIdx.x) : (int)blockIdx.x;
+  const bool active = t < NGLL3;
+  const int k = t / NGLL2, j = (t / NGLLX) % NGLLX, i = t % NGLLX;
+  const long eo = (long)e * NGLL3_PAD + t;
+  const int ir = __ldg(irregular + e);
+  int g = 0;
+  float rho = 1.f;
+  float m[9] = {0.f, 0.f, 0.f, 0.f, 0.f, 0.f, 0.f, 0.f, 0.f};
+  if (active) {
+    g = __ldg(ibool + eo);
+    rho = __ldg(rhostore + eo);
+    if (ir >= 0) {
+      const long mo = (long)ir * NGLL3_PAD + t;
+      m[0] = __ldg(m0 + mo); m[1] = __ldg(m1 + mo); m[2] = __ldg(m2 + mo);
+      m[3] = __ldg(m3 + mo); m[4] = __ldg(m4 + mo); m[5] = __ldg(m5 + mo);
+      m[6] = __ldg(m6 + mo); m[7] = __ldg(m7 + mo); m[8] = __ldg(m8 + mo);
+    }
+    s_chi[t] = pot[g];
+  }
+  if (t < NGLL3) s_gll[t] = __ldg(gll + t);
+  __syncthreads();
+  if (active) {
+    float a = 0.f, b = 0.f, c = 0.f;
+#pragma unroll
+    for (int l = 0; l < NGLLX; ++l) {
+      a = fmaf(s_chi[l + NGLLX * j + NGLL2 * k], s_gll[i + NGLLX * l], a);
+      b = fmaf(s_chi[i + NGLLX * l + NGLL2 * k], s_gll[j + NGLLX * l], b);
+      c = fmaf(s_chi[i + NGLLX * j + NGLL2 * l], s_gll[k + NGLLX * l], c);
+    }
+    const float rho_inv = 1.f / rho;
+    if (ir >= 0) {
+      const float jac = 1.f / (m[0] * (m[4] * m[8] - m[5] * m[7]) - m[1] * (m[3] * m[8] - m[5] * m[6]) +
+                               m[2] * (m[3] * m[7] - m[4] * m[6]));
+      const float dx = m[0] * a + m[3] * b + m[6] * c;
+      const float dy = m[1] * a + m[4] * b + m[7] * c;
+      const float dz = m[2] * a + m[5] * b + m[8] * c;
+      const float f = rho_inv * jac;
+      s_t[0][t] = f * (m[0] * dx + m[1] * dy + m[2] * dz);
+      s_t[1][t] = f * (m[3] * dx + m[4] * dy + m[5] * dz);
+      s_t[2][t] = f * (m[6] * dx + m[7] * dy + m[8] * dz);
+    } else {
+      const float f = rho_inv * jacobian_regular * xix_regular * xix_regular;
+      s_t[0][t] = f * a;
+      s_t[1][t] = f * b;
+      s_t[2][t] = f * c;
+    }
+  }
+  __syncthreads();
+  if (active) {
+    const float* hpw = s_gll + NGLL2;
+    float a = 0.f, b = 0.f, c = 0.f;
+#pragma unroll
+    for (int l = 0; l < NGLLX; ++l) {
+      a = fmaf(s_t[0][l + NGLLX * j + NGLL2 * k], hpw[l + NGLLX * i], a);
+      b = fmaf(s_t[1][i + NGLLX * l + NGLL2 * k], hpw[l + NGLLX * j], b);
+      c = fmaf(s_t[2][i + NGLLX * j + NGLL2 * l], hpw[l + NGLLX * k], c);
+    }
+    const float add = s_gll[4 * NGLL2 + j + NGLLX * k] * a + s_gll[3 * NGLL2 + i + NGLLX * k] * b +
+                      s_gll[2 * NGLL2 + i + NGLLX * j] * c;
+    atomicAdd(pot_dd + g, -add);
+  }
+}
+
+// Sommerfeld condition on the faces of fluid elements
+// (compute_stacey_acoustic.f90:98-125): chi_dd -= chi_dot jw / (cp rho)
+__global__ void stacey_acoustic_kernel(int nfaces, const int* __restrict__ abs_ispec, const int* __restrict__ abs_pt,
+                                       const float* __restrict__ jw, const int* __restrict__ is_acoustic,
+                                       const int* __restrict__ ibool, const float* __restrict__ rhostore,
+                                       const float* __restrict__ kappav, const float* __restrict__ pot_dot,
+                                       float* __restrict__ pot_dd) {
+  long idx = (long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (idx >= (long)nfaces * NGLL2) return;
+  const int e = abs_ispec[idx / NGLL2];
+  if (!is_acoustic[e]) return;
+  const long q = (long)e * NGLL3_PAD + abs_pt[idx];
+  const int g = ibool[q];
+  const float rhol = rhostore[q];
+  const float cpl = sqrtf(kappav[q] / rhol);
+  atomicAdd(pot_dd + g, -(pot_dot[g] * jw[idx] / cpl / rhol));
+}
+
+// chi_dd += jw (u . n)   (compute_coupling_acoustic_el.f90:70-150)
+__global__ void coupling_ac_el_kernel(int nfaces, const int* __restrict__ cp_ispec, const int* __restrict__ cp_pt,
+                                      const float* __restrict__ normal, const float* __restrict__ jw,
+                                      const int* __restrict__ ibool, const float* __restrict__ displ, float sign,
+                                      float* __restrict__ pot_dd) {
+  long idx = (long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (idx >= (long)nfaces * NGLL2) return;
+  const int g = ibool[(long)cp_ispec[idx / NGLL2] * NGLL3_PAD + cp_pt[idx]];
+  const float dn = displ[3L * g] * normal[3 * idx] + displ[3L * g + 1] * normal[3 * idx + 1] +
+                   displ[3L * g + 2] * normal[3 * idx + 2];
+  atomicAdd(pot_dd + g, jw[idx] * (sign * dn));
+}
+
+// accel += jw n (-chi_dd)   (compute_coupling_viscoelastic_ac.f90:70-160)
+__global__ void coupling_el_ac_kernel(int nfaces, const int* __restrict__ cp_ispec, const int* __restrict__ cp_pt,
+                                      const float* __restrict__ normal, const float* __restrict__ jw,
+                                      const int* __restrict__ ibool, const float* __restrict__ pot_dd, float sign,
+                                      float* __restrict__ accel) {
+  long idx = (long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (idx >= (long)nfaces * NGLL2) return;
+  const int g = ibool[(long)cp_ispec[idx / NGLL2] * NGLL3_PAD + cp_pt[idx]];
+  const float pr = sign * (-pot_dd[g]);
+  const float w = jw[idx];
+  atomicAdd(accel + 3L * g, w * normal[3 * idx] * pr);
+  atomicAdd(accel + 3L * g + 1, w * normal[3 * idx + 1] * pr);
+  atomicAdd(accel + 3L * g + 2, w * normal[3 * idx + 2] * pr);
+}
+
+// chi = chi_dot = chi_dd = 0 on the free surface of fluid elements
+// (compute_forces_acoustic_calling_routine.f90:754-810)
+__global__ void free_surface_kernel(int nfaces, const int* __restrict__ fs_ispec, const int* __restrict__ fs_pt,
+                                    const int* __restrict__ is_acoustic, const int* __restrict__ ibool,
+                                    float* __restrict__ pot, float* __restrict__ pot_dot, float* __restrict__ pot_dd) {
+  long idx = (long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (idx >= (long)nfaces * NGLL2) return;
+  const int e = fs_ispec[idx / NGLL2];
+  if (!is_acoustic[e]) return;
+  const int g = ibool[(long)e * NGLL3_PAD + fs_pt[idx]];
+  pot[g] = 0.f;
+  pot_dot[g] = 0.f;
+  pot_dd[g] = 0.f;
+}
+
+// chi_dd -= sourcearray(1) stf / kappa for sources in fluid elements
+// (compute_add_sources_acoustic.f90:100-126)
+__global__ void sources_acoustic_kernel(int nsrc, const int* __restrict__ ispec_src, const int* __restrict__ is_acoustic,
+                                        const float* __restrict__ sa, const float* __restrict__ stf,
+                                        const int* __restrict__ ibool, const float* __restrict__ kappav,
+                                        float* __restrict__ pot_dd) {
+  const int is = blockIdx.x, p = threadIdx.x;
+  if (is >= nsrc || p >= NGLL3) return;
+  const int e = ispec_src[is];
+  if (e < 0 || !is_acoustic[e]) return;
+  const long q = (long)e * NGLL3_PAD + p;
+  atomicAdd(pot_dd + ibool[q], -(sa[((long)is * NGLL3_PAD + p) * 3] * stf[is] / kappav[q]));
+}
+
+__global__ void predictor_scalar_kernel(float* __restrict__ d, float* __restrict__ v, float* __restrict__ a, long n,
+                                        float dt, float dt2, float dtsq2) {
+  long i = (long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  const float ai = a[i], vi = v[i];
+  d[i] = d[i] + dt * vi + dtsq2 * ai;
+  v[i] = vi + dt2 * ai;
+  a[i] = 0.f;
+}
+
+// kernel_3_acoustic: chi_dd *= rmass_acoustic; chi_dot += dt/2 chi_dd
+__global__ void mass_corrector_scalar_kernel(float* __restrict__ v, float* __restrict__ a,
+                                             const float* __restrict__ rmass, long n, float dt2) {
+  long i = (long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  const float ai = a[i] * rmass[i];
+  a[i] = ai;
+  v[i] += dt2 * ai;
+}
+
+}  // namespace
+
+// pressure seismograms (compute_interpolated_dva.f90:280-300): p = - sum h chi_dd
+__global__ void pressure_seismogram_kernel(int nrec, const int* __restrict__ ispec_rec,
+                                           const int* __restrict__ rec_is_acoustic, const float* __restrict__ hx,
+                                           const float* __restrict__ he, const float* __restrict__ hg,
+                                           const int* __restrict__ ibool, const float* __restrict__ pot_dd,
+                                           float* __restrict__ seismo_p, int slot) {
+  __shared__ float red[4];
+  const int r = blockIdx.x, t = threadIdx.x;
+  float s = 0.f;
+  if (r < nrec && t < NGLL3 && rec_is_acoustic[r]) {
+    const int k = t / NGLL2, j = (t / NGLLX) % NGLLX, i = t % NGLLX;
+    const float h = hx[5 * r + i] * he[5 * r + j] * hg[5 * r + k];
+    s = -h * pot_dd[ibool[(long)ispec_rec[r] * NGLL3_PAD + t]];
+  }
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) s += __shfl_down_sync(0xffffffffu, s, o);
+  if ((t & 31) == 0) red[t >> 5] = s;
+  __syncthreads();
+  if (t == 0 && r < nrec) seismo_p[r + (long)nrec * slot] = red[0] + red[1] + red[2] + red[3];
+}
+
+void launch_pressure_seismograms(Mesh* mp, int slot) {
+  if (!mp->d_seismo_p || mp->nrec_local == 0 || !mp->d_potential_dot_dot) return;
+  pressure_seismogram_kernel<<<mp->nrec_local, NGLL3_PAD, 0, mp->stream>>>(
+      mp->nrec_local, mp->d_ispec_rec, mp->d_rec_is_acoustic, mp->d_hxir, mp->d_hetar, mp->d_hgammar, mp->d_ibool,
+      mp->d_potential_dot_dot, mp->d_seismo_p, slot);
+}
+
+}  // namespace sf3d
+
+using namespace sf3d;
+
+static bool copy_faces(const int* h_ispec, const int* h_ijk, int nf, long nspec, int** d_ispec, int** d_pt,
+                       cudaStream_t s) {
+  std::vector<int> isp(nf), pt((size_t)nf * NGLL2);
+  for (int f = 0; f < nf; ++f) {
+    isp[f] = h_ispec[f] - 1;
+    if (isp[f] < 0 || isp[f] >= nspec) return set_error(SF3D_ERR_ARG, "face ispec out of range");
+    for (int g = 0; g < NGLL2; ++g) {
+      const int* ijk = h_ijk + 3 * (g + NGLL2 * f);
+      for (int c = 0; c < 3; ++c)
+        if (ijk[c] < 1 || ijk[c] > 5) return set_error(SF3D_ERR_ARG, "face ijk out of range");
+      pt[(size_t)f * NGLL2 + g] = (ijk[0] - 1) + NGLLX * (ijk[1] - 1) + NGLL2 * (ijk[2] - 1);
+    }
+  }
+  return alloc_zero((void**)d_ispec, sizeof(int) * nf) &&
+         copy_sync(*d_ispec, isp.data(), sizeof(int) * nf, cudaMemcpyHostToDevice, s) &&
+         alloc_zero((void**)d_pt, sizeof(int) * pt.size()) &&
+         copy_sync(*d_pt, pt.data(), sizeof(int) * pt.size(), cudaMemcpyHostToDevice, s);
+}
+
+extern "C" {
+
+void prepare_fields_acoustic_device_(long* Mesh_pointer, realw* rmass_acoustic, realw* rhostore, realw* kappastore,
+                                     int* num_phase_ispec_acoustic, int* phase_ispec_inner_acoustic,
+                                     int* NOISE_TOMOGRAPHY, int* num_free_surface_faces, int* free_surface_ispec,
+                                     int* free_surface_ijk, int* b_reclen_potential, realw* b_absorb_potential,
+                                     int* ELASTIC_SIMULATION, int* num_coupling_ac_el_faces,
+                                     int* coupling_ac_el_ispec, int* coupling_ac_el_ijk,
+                                     realw* coupling_ac_el_normal, realw* coupling_ac_el_jacobian2Dw,
+                                     int* num_colors_outer_acoustic, int* num_colors_inner_acoustic,
+                                     int* num_elem_colors_acoustic) {
+  (void)b_reclen_potential; (void)b_absorb_potential; (void)num_colors_outer_acoustic;
+  (void)num_colors_inner_acoustic; (void)num_elem_colors_acoustic;
+  Mesh* mp = get_mesh(Mesh_pointer);
+  if (!mp) return;
+  if (NOISE_TOMOGRAPHY && *NOISE_TOMOGRAPHY) { set_error(SF3D_ERR_ARG, "noise tomography is not supported"); return; }
+  if (!mp->d_ispec_is_acoustic) { set_error(SF3D_ERR_STATE, "ispec_is_acoustic not given to prepare_constants_device"); return; }
+  const long nspec = mp->nspec, nglob = mp->nglob;
+  cudaStream_t s = mp->stream;
+  bool ok = alloc_zero((void**)&mp->d_potential, sizeof(float) * nglob) &&
+            alloc_zero((void**)&mp->d_potential_dot, sizeof(float) * nglob) &&
+            alloc_zero((void**)&mp->d_potential_dot_dot, sizeof(float) * nglob) &&
+            alloc_zero((void**)&mp->d_rmass_acoustic, sizeof(float) * nglob) &&
+            copy_sync(mp->d_rmass_acoustic, rmass_acoustic, sizeof(float) * nglob, cudaMemcpyHostToDevice, s);
+  ok = ok && upload_padded(&mp->d_rhostore, rhostore, nspec, s);
+  if (ok && !mp->d_kappav) ok = upload_padded(&mp->d_kappav, kappastore, nspec, s);
+  mp->num_phase_ispec_ac = *num_phase_ispec_acoustic;
+  if (ok && mp->num_phase_ispec_ac > 0) {
+    std::vector<int> ph((size_t)2 * mp->num_phase_ispec_ac);
+    for (size_t q = 0; q < ph.size() && ok; ++q) {
+      ph[q] = phase_ispec_inner_acoustic[q] - 1;
+      if (ph[q] >= nspec) ok = set_error(SF3D_ERR_ARG, "phase_ispec_inner_acoustic out of range");
+    }
+    ok = ok && alloc_zero((void**)&mp->d_phase_ispec_ac, sizeof(int) * ph.size()) &&
+         copy_sync(mp->d_phase_ispec_ac, ph.data(), sizeof(int) * ph.size(), cudaMemcpyHostToDevice, s);
+  }
+  mp->num_free_surface_faces = *num_free_surface_faces;
+  if (ok && mp->num_free_surface_faces > 0)
+    ok = copy_faces(free_surface_ispec, free_surface_ijk, mp->num_free_surface_faces, nspec, &mp->d_fs_ispec,
+                    &mp->d_fs_pt, s);
+  mp->num_coupling_faces = (ELASTIC_SIMULATION && *ELASTIC_SIMULATION) ? *num_coupling_ac_el_faces : 0;
+  if (ok && mp->num_coupling_faces > 0) {
+    const int nf = mp->num_coupling_faces;
+    ok = copy_faces(coupling_ac_el_ispec, coupling_ac_el_ijk, nf, nspec, &mp->d_cp_ispec, &mp->d_cp_pt, s) &&
+         alloc_zero((void**)&mp->d_cp_normal, sizeof(float) * 3 * NGLL2 * nf) &&
+         copy_sync(mp->d_cp_normal, coupling_ac_el_normal, sizeof(float) * 3 * NGLL2 * nf, cudaMemcpyHostToDevice,
+                   s) &&
+         alloc_zero((void**)&mp->d_cp_jw, sizeof(float) * NGLL2 * nf) &&
+         copy_sync(mp->d_cp_jw, coupling_ac_el_jacobian2Dw, sizeof(float) * NGLL2 * nf, cudaMemcpyHostToDevice, s);
+  }
+  mp->has_acoustic = ok ? 1 : 0;
+}
+
+void compute_forces_acoustic_cuda_(long* Mesh_pointer, int* iphase, int* nspec_outer_acoustic,
+                                   int* nspec_inner_acoustic, int* FORWARD_OR_ADJOINT_f) {
+  Mesh* mp = get_mesh(Mesh_pointer);
+  if (!mp) return;
+  if (!mp->has_acoustic) { set_error(SF3D_ERR_STATE, "prepare_fields_acoustic_device not called"); return; }
+  if (*FORWARD_OR_ADJOINT_f != 1) { set_error(SF3D_ERR_ARG, "acoustic adjoint fields are not supported"); return; }
+  mp->nspec_outer_ac = *nspec_outer_acoustic;
+  mp->nspec_inner_ac = *nspec_inner_acoustic;
+  const int nel = *iphase == 1 ? mp->nspec_outer_ac : mp->nspec_inner_ac;
+  if (nel < 0 || nel > mp->num_phase_ispec_ac) { set_error(SF3D_ERR_ARG, "nspec_outer/inner_acoustic too large"); return; }
+  if (nel == 0) return;
+  const int* ph = mp->d_phase_ispec_ac + (long)(*iphase - 1) * mp->num_phase_ispec_ac;
+  acoustic_stiffness_kernel<<<nel, NGLL3_PAD, 0, mp->stream>>>(
+      nel, ph, mp->d_ibool, mp->d_irregular, mp->d_metric[0], mp->d_metric[1], mp->d_metric[2], mp->d_metric[3],
+      mp->d_metric[4], mp->d_metric[5], mp->d_metric[6], mp->d_metric[7], mp->d_metric[8], mp->d_rhostore, mp->d_gll,
+      mp->xix_regular, mp->jacobian_regular, mp->d_potential, mp->d_potential_dot_dot);
+  cuda_ok(cudaGetLastError(), "acoustic_stiffness_kernel");
+}
+
+void acoustic_enforce_free_surf_cuda_(long* Mesh_pointer, int* ABSORB_INSTEAD_OF_FREE_SURFACE,
+                                      int* FORWARD_OR_ADJOINT) {
+  (void)FORWARD_OR_ADJOINT;
+  Mesh* mp = get_mesh(Mesh_pointer);
+  if (!mp || !mp->has_acoustic) return;
+  if (*ABSORB_INSTEAD_OF_FREE_SURFACE || mp->num_free_surface_faces == 0) return;
+  const long n = (long)mp->num_free_surface_faces * NGLL2;
+  free_surface_kernel<<<nblk(n, 128), 128, 0, mp->stream>>>(mp->num_free_surface_faces, mp->d_fs_ispec, mp->d_fs_pt,
+                                                             mp->d_ispec_is_acoustic, mp->d_ibool, mp->d_potential,
+                                                             mp->d_potential_dot, mp->d_potential_dot_dot);
+  cuda_ok(cudaGetLastError(), "free_surface_kernel");
+}
+
+void update_displacement_ac_cuda_(long* Mesh_pointer, realw* deltat_F, realw* deltatover2_F, realw* deltatsqover2_F,
+                                  int* FORWARD_OR_ADJOINT) {
+  (void)FORWARD_OR_ADJOINT;
+  Mesh* mp = get_mesh(Mesh_pointer);
+  if (!mp || !mp->has_acoustic) return;
+  const long n = mp->nglob;
+  predictor_scalar_kernel<<<nblk(n, 256), 256, 0, mp->stream>>>(mp->d_potential, mp->d_potential_dot,
+                                                                mp->d_potential_dot_dot, n, *deltat_F, *deltatover2_F,
+                                                                *deltatsqover2_F);
+  cuda_ok(cudaGetLastError(), "predictor_scalar_kernel");
+}
+
+void kernel_3_acoustic_cuda_(long* Mesh_pointer, realw* deltatover2_F, realw* b_deltatover2_F,
+                             int* FORWARD_OR_ADJOINT_f) {
+  (void)b_deltatover2_F; (void)FORWARD_OR_ADJOINT_f;
+  Mesh* mp = get_mesh(Mesh_pointer);
+  if (!mp || !mp->has_acoustic) return;
+  const long n = mp->nglob;
+  mass_corrector_scalar_kernel<<<nblk(n, 256), 256, 0, mp->stream>>>(mp->d_potential_dot, mp->d_potential_dot_dot,
+                                                                     mp->d_rmass_acoustic, n, *deltatover2_F);
+  cuda_ok(cudaGetLastError(), "mass_corrector_scalar_kernel");
+}
+
+void compute_stacey_acoustic_cuda_(long* Mesh_pointer, int* iphasef, realw* h_b_absorb_potential,
+                                   int* FORWARD_OR_ADJOINT_f) {
+  (void)h_b_absorb_potential; (void)FORWARD_OR_ADJOINT_f;
+  Mesh* mp = get_mesh(Mesh_pointer);
+  if (!mp || !mp->has_acoustic) return;
+  if (*iphasef != 1 || !mp->stacey || mp->num_abs_faces == 0) return;
+  const long n = (long)mp->num_abs_faces * NGLL2;
+  stacey_acoustic_kernel<<<nblk(n, 128), 128, 0, mp->stream>>>(mp->num_abs_faces, mp->d_abs_ispec, mp->d_abs_pt,
+                                                                mp->d_abs_jw, mp->d_ispec_is_acoustic, mp->d_ibool,
+                                                                mp->d_rhostore, mp->d_kappav, mp->d_potential_dot,
+                                                                mp->d_potential_dot_dot);
+  cuda_ok(cudaGetLastError(), "stacey_acoustic_kernel");
+}
+
+void compute_coupling_ac_el_cuda_(long* Mesh_pointer, int* iphasef, int* num_coupling_ac_el_facesf,
+                                  int* FORWARD_OR_ADJOINT) {
+  Mesh* mp = get_mesh(Mesh_pointer);
+  if (!mp || !mp->has_acoustic) return;
+  if (*iphasef != 1 || mp->num_coupling_faces == 0) return;
+  if (*num_coupling_ac_el_facesf != mp->num_coupling_faces) { set_error(SF3D_ERR_ARG, "coupling face count mismatch"); return; }
+  const float sign = (mp->simulation_type != 1 && *FORWARD_OR_ADJOINT == 1) ? -1.f : 1.f;
+  const long n = (long)mp->num_coupling_faces * NGLL2;
+  coupling_ac_el_kernel<<<nblk(n, 128), 128, 0, mp->stream>>>(mp->num_coupling_faces, mp->d_cp_ispec, mp->d_cp_pt,
+                                                               mp->d_cp_normal, mp->d_cp_jw, mp->d_ibool, mp->f.displ,
+                                                               sign, mp->d_potential_dot_dot);
+  cuda_ok(cudaGetLastError(), "coupling_ac_el_kernel");
+}
+
+void compute_coupling_el_ac_cuda_(long* Mesh_pointer, int* iphasef, int* num_coupling_ac_el_facesf,
+                                  int* FORWARD_OR_ADJOINT) {
+  Mesh* mp = get_mesh(Mesh_pointer);
+  if (!mp || !mp->has_acoustic) return;
+  if (*iphasef != 1 || mp->num_coupling_faces == 0) return;
+  if (*num_coupling_ac_el_facesf != mp->num_coupling_faces) { set_error(SF3D_ERR_ARG, "coupling face count mismatch"); return; }
+  const float sign = (mp->simulation_type != 1 && *FORWARD_OR_ADJOINT == 1) ? -1.f : 1.f;
+  const long n = (long)mp->num_coupling_faces * NGLL2;
+  coupling_el_ac_kernel<<<nblk(n, 128), 128, 0, mp->stream>>>(mp->num_coupling_faces, mp->d_cp_ispec, mp->d_cp_pt,
+                                                               mp->d_cp_normal, mp->d_cp_jw, mp->d_ibool,
+                                                               mp->d_potential_dot_dot, sign, mp->f.accel);
+  cuda_ok(cudaGetLastError(), "coupling_el_ac_kernel");
+}
+
+void compute_add_sources_ac_cuda_(long* Mesh_pointer, int* NSOURCESf, double* h_stf_pre_compute,
+                                  int* run_number_of_the_source) {
+  (void)run_number_of_the_source;
+  Mesh* mp = get_mesh(Mesh_pointer);
+  if (!mp || !mp->has_acoustic) return;
+  if (mp->nsources_local == 0 || mp->nsources == 0) return;
+  if (*NSOURCESf != mp->nsources) { set_error(SF3D_ERR_ARG, "NSOURCES mismatch"); return; }
+  std::vector<float> stf(mp->nsources);
+  for (int i = 0; i < mp->nsources; ++i) stf[i] = (float)h_stf_pre_compute[i];
+  SF3D_CUDA(cudaMemcpyAsync(mp->d_stf_step, stf.data(), sizeof(float) * mp->nsources, cudaMemcpyHostToDevice,
+                            mp->stream));
+  sources_acoustic_kernel<<<mp->nsources, NGLL3_PAD, 0, mp->stream>>>(mp->nsources, mp->d_ispec_src,
+                                                                      mp->d_ispec_is_acoustic, mp->d_sourcearrays,
+                                                                      mp->d_stf_step, mp->d_ibool, mp->d_kappav,
+                                                                      mp->d_potential_dot_dot);
+  SF3D_CUDA(cudaStreamSynchronize(mp->stream));
+  cuda_ok(cudaGetLastError(), "sources_acoustic_kernel");
+}
+
+static void xfer_ac(int* size, realw* a, realw* b, realw* c, long* Mesh_pointer, bool to_device) {
+  Mesh* mp = get_mesh(Mesh_pointer);
+  if (!mp) return;
+  if (!mp->has_acoustic) { set_error(SF3D_ERR_STATE, "acoustic fields not allocated"); return; }
+  if (*size != mp->nglob) { set_error(SF3D_ERR_ARG, "acoustic transfer size must be NGLOB_AB"); return; }
+  float* d[3] = {mp->d_potential, mp->d_potential_dot, mp->d_potential_dot_dot};
+  realw* h[3] = {a, b, c};
+  for (int q = 0; q < 3; ++q) {
+    if (!h[q]) continue;
+    if (to_device)
+      SF3D_CUDA(cudaMemcpyAsync(d[q], h[q], sizeof(float) * mp->nglob, cudaMemcpyHostToDevice, mp->stream));
+    else
+      SF3D_CUDA(cudaMemcpyAsync(h[q], d[q], sizeof(float) * mp->nglob, cudaMemcpyDeviceToHost, mp->stream));
+  }
+  SF3D_CUDA(cudaStreamSynchronize(mp->stream));
+}
+
+void transfer_fields_ac_to_device_(int* size, realw* potential_acoustic, realw* potential_dot_acoustic,
+                                   realw* potential_dot_dot_acoustic, long* Mesh_pointer) {
+  xfer_ac(size, potential_acoustic, potential_dot_acoustic, potential_dot_dot_acoustic, Mesh_pointer, true);
+}
+
+void transfer_fields_ac_from_device_(int* size, realw* potential_acoustic, realw* potential_dot_acoustic,
+                                     realw* potential_dot_dot_acoustic, long* Mesh_pointer) {
+  xfer_ac(size, potential_acoustic, potential_dot_acoustic, potential_dot_dot_acoustic, Mesh_pointer, false);
+}
+
+}  // extern "C"

@@ -186,12 +186,12 @@ void prepare_sim2_or_3_const_device_(long* Mesh_pointer, int* nadj_rec_local, in
     if (v < 0 || v >= mp->nspec) { set_error(SF3D_ERR_ARG, "ispec_selected_rec out of range"); return; }
   const size_t nl = (size_t)mp->nadj_rec_local;
   bool ok = alloc_zero((void**)&mp->d_ispec_adj, sizeof(int) * nl) &&
-            cuda_ok(cudaMemcpy(mp->d_ispec_adj, isp.data(), sizeof(int) * nl, cudaMemcpyHostToDevice), "copy");
+            copy_sync(mp->d_ispec_adj, isp.data(), sizeof(int) * nl, cudaMemcpyHostToDevice, mp->stream);
   float** dst[3] = {&mp->d_hxir_adj, &mp->d_hetar_adj, &mp->d_hgammar_adj};
   realw* src[3] = {hxir_adjstore, hetar_adjstore, hgammar_adjstore};
   for (int q = 0; q < 3 && ok; ++q)
     ok = alloc_zero((void**)dst[q], sizeof(float) * 5 * nl) &&
-         cuda_ok(cudaMemcpy(*dst[q], src[q], sizeof(float) * 5 * nl, cudaMemcpyHostToDevice), "copy");
+         copy_sync(*dst[q], src[q], sizeof(float) * 5 * nl, cudaMemcpyHostToDevice, mp->stream);
   ok = ok && alloc_zero((void**)&mp->d_source_adjoint, sizeof(float) * 3 * nl * mp->ntstep_between_read_adjsrc);
 }
 
@@ -268,7 +268,7 @@ int sf3d_get_kernels_f64(long* Mesh_pointer, double* h_rho_kl, double* h_mu_kl, 
   double* h[3] = {h_rho_kl, h_mu_kl, h_kappa_kl};
   double* d[3] = {mp->d_rho_kl, mp->d_mu_kl, mp->d_kappa_kl};
   for (int q = 0; q < 3; ++q) {
-    SF3D_CUDA_RET(cudaMemcpy(tmp.data(), d[q], sizeof(double) * tmp.size(), cudaMemcpyDeviceToHost), SF3D_ERR_CUDA);
+    if (!copy_sync(tmp.data(), d[q], sizeof(double) * tmp.size(), cudaMemcpyDeviceToHost, mp->stream)) return SF3D_ERR_CUDA;
     for (long e = 0; e < mp->nspec; ++e)
       for (int p = 0; p < NGLL3; ++p) h[q][e * NGLL3 + p] = tmp[e * NGLL3_PAD + p];
   }

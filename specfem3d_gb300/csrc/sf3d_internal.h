@@ -127,6 +127,27 @@ struct Mesh {
   float* d_hgammar_adj = nullptr;
   float* d_source_adjoint = nullptr;      // (3, nadj, NTSTEP_BETWEEN_READ_ADJSRC)
 
+  // acoustic domain and fluid-solid coupling
+  int* d_ispec_is_acoustic = nullptr;     // [nspec] 0/1
+  int has_acoustic = 0;
+  float* d_rhostore = nullptr;            // [nspec][128]
+  float* d_potential = nullptr;
+  float* d_potential_dot = nullptr;
+  float* d_potential_dot_dot = nullptr;
+  float* d_rmass_acoustic = nullptr;
+  int num_phase_ispec_ac = 0, nspec_outer_ac = 0, nspec_inner_ac = 0;
+  int* d_phase_ispec_ac = nullptr;        // [2][num_phase_ispec_ac] 0-based
+  int num_free_surface_faces = 0;
+  int* d_fs_ispec = nullptr;              // [nf] 0-based
+  int* d_fs_pt = nullptr;                 // [nf][25]
+  int num_coupling_faces = 0;
+  int* d_cp_ispec = nullptr;
+  int* d_cp_pt = nullptr;
+  float* d_cp_normal = nullptr;           // [nf][25][3]
+  float* d_cp_jw = nullptr;               // [nf][25]
+  float* d_seismo_p = nullptr;            // (nrec_local, nlength)
+  int* d_rec_is_acoustic = nullptr;       // [nrec_local]
+
   // device step counter for graph-captured time loops, and completion counter
   int* d_it = nullptr;
   unsigned long long* d_stamps = nullptr;  // per-step stiffness start/end (globaltimer ns)
@@ -158,6 +179,11 @@ bool upload_sls_padded(float** d, const float* h, long n, cudaStream_t s);
 bool download_padded(float* h, const float* d, long n, Mesh* mp);
 bool download_sls_padded(float* h, const float* d, long n, Mesh* mp);
 bool alloc_zero(void** d, size_t bytes);
+// stream-ordered copy that returns when the copy has completed
+inline bool copy_sync(void* dst, const void* src, size_t bytes, cudaMemcpyKind kind, cudaStream_t s) {
+  return cuda_ok(cudaMemcpyAsync(dst, src, bytes, kind, s), "cudaMemcpyAsync") &&
+         cuda_ok(cudaStreamSynchronize(s), "cudaStreamSynchronize");
+}
 bool ensure_stage(Mesh* mp, size_t bytes);
 
 // kernels launched from several translation units
@@ -185,5 +211,6 @@ struct StiffnessArgs {
 };
 
 void launch_stiffness(const StiffnessArgs& a, bool att, bool store_strain, cudaStream_t s);
+void launch_pressure_seismograms(Mesh* mp, int slot);
 
 }  // namespace sf3d

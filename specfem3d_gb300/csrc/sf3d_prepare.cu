@@ -40,10 +40,14 @@ bool cuda_ok(cudaError_t e, const char* what) {
   return set_error(SF3D_ERR_CUDA, std::string(what) + ": " + cudaGetErrorString(e));
 }
 
+// Allocates and zeroes device memory.  The memset runs on the legacy default
+// stream, which does not order with the library's non-blocking stream, so the
+// device is synchronised before anything can be queued behind it.
 bool alloc_zero(void** d, size_t bytes) {
   if (bytes == 0) bytes = 16;
   if (!cuda_ok(cudaMalloc(d, bytes), "cudaMalloc")) return false;
-  return cuda_ok(cudaMemset(*d, 0, bytes), "cudaMemset");
+  if (!cuda_ok(cudaMemset(*d, 0, bytes), "cudaMemset")) return false;
+  return cuda_ok(cudaDeviceSynchronize(), "cudaDeviceSynchronize");
 }
 
 bool ensure_stage(Mesh* mp, size_t bytes) {
@@ -240,7 +244,7 @@ void prepare_constants_device_(long* Mesh_pointer, int* h_NGLLX, int* NSPEC_AB, 
                                int* UNDO_ATTENUATION_AND_OR_PML, int* PML_CONDITIONS) {
   (void)num_interfaces_ext_mesh; (void)max_nibool_interfaces_ext_mesh; (void)h_nibool_interfaces_ext_mesh;
   (void)h_ibool_interfaces_ext_mesh; (void)h_ispec_is_inner; (void)USE_MESH_COLORING_GPU_f;
-  (void)nspec_acoustic; (void)nspec_elastic; (void)ispec_is_acoustic; (void)ispec_is_elastic;
+  (void)nspec_elastic; (void)ispec_is_elastic;
   (void)FAULT_SIMULATION; (void)UNDO_ATTENUATION_AND_OR_PML; (void)nu_source;
   if (!Mesh_pointer) { set_error(SF3D_ERR_ARG, "Mesh_pointer is NULL"); return; }
   *Mesh_pointer = 0;
@@ -371,6 +375,23 @@ void prepare_constants_device_(long* Mesh_pointer, int* h_NGLLX, int* NSPEC_AB, 
     if (ok && mp->save_v) ok = alloc_zero((void**)&mp->d_seismo_v, sz);
     if (ok && mp->save_a) ok = alloc_zero((void**)&mp->d_seismo_a, sz);
   }
+  // fluid elements (always kept: the seismogram and source routines need them)
+  if (ok) {
+    std::vector<int> isac(nspec, 0);
+    if (ispec_is_acoustic && nspec_acoustic && *nspec_acoustic > 0)
+      for (long e = 0; e < nspec; ++e) isac[e] = ispec_is_acoustic[e] ? 1 : 0;
+    ok = copy_in((void**)&mp->d_ispec_is_acoustic, isac.data(), sizeof(int) * nspec, s);
+    if (ok && mp->nrec_local > 0) {
+      std::vector<int> racs;
+      for (int r = 0; r < mp->nrec; ++r) {
+        if (h_islice_selected_rec && h_islice_selected_rec[r] != myrank) continue;
+        racs.push_back(isac[h_ispec_selected_rec[r] - 1]);
+      }
+      ok = copy_in((void**)&mp->d_rec_is_acoustic, racs.data(), sizeof(int) * racs.size(), s);
+      if (ok && mp->save_p)
+        ok = alloc_zero((void**)&mp->d_seismo_p, sizeof(float) * (size_t)mp->nrec_local * mp->nlength_seismogram);
+    }
+  }
   if (ok) ok = alloc_zero((void**)&mp->d_it, sizeof(int) * 4);
   if (ok) ok = alloc_zero((void**)&mp->d_done, sizeof(unsigned int) * 4);
   if (ok) ok = alloc_zero((void**)&mp->d_scratch, sizeof(float) * 4096);
@@ -423,6 +444,7 @@ void prepare_fields_elastic_device_(long* Mesh_pointer, realw* rmassx, realw* rm
   ok = ok && copy_in((void**)&mp->d_rmassx, rmassx, sizeof(float) * nglob, s);
   ok = ok && copy_in((void**)&mp->d_rmassy, rmassy, sizeof(float) * nglob, s);
   ok = ok && copy_in((void**)&mp->d_rmassz, rmassz, sizeof(float) * nglob, s);
+  if (mp->d_kappav) { cudaFree(mp->d_kappav); mp->d_kappav = nullptr; }
   ok = ok && upload_padded(&mp->d_kappav, h_kappav, nspec, s);
   ok = ok && upload_padded(&mp->d_muv, h_muv, nspec, s);
   if (mp->stacey && mp->num_abs_faces > 0) {
@@ -481,6 +503,11 @@ void prepare_cleanup_device_(long* Mesh_pointer, int* ACOUSTIC_SIMULATION, int* 
   cudaFree(mp->d_rho_kl); cudaFree(mp->d_mu_kl); cudaFree(mp->d_kappa_kl);
   cudaFree(mp->d_ispec_adj); cudaFree(mp->d_hxir_adj); cudaFree(mp->d_hetar_adj); cudaFree(mp->d_hgammar_adj);
   cudaFree(mp->d_source_adjoint);
+  cudaFree(mp->d_ispec_is_acoustic); cudaFree(mp->d_rhostore); cudaFree(mp->d_potential);
+  cudaFree(mp->d_potential_dot); cudaFree(mp->d_potential_dot_dot); cudaFree(mp->d_rmass_acoustic);
+  cudaFree(mp->d_phase_ispec_ac); cudaFree(mp->d_fs_ispec); cudaFree(mp->d_fs_pt); cudaFree(mp->d_cp_ispec);
+  cudaFree(mp->d_cp_pt); cudaFree(mp->d_cp_normal); cudaFree(mp->d_cp_jw); cudaFree(mp->d_seismo_p);
+  cudaFree(mp->d_rec_is_acoustic);
   cudaFree(mp->d_it); cudaFree(mp->d_stamps); cudaFree(mp->d_done); cudaFree(mp->d_scratch); cudaFree(mp->d_stage);
   if (mp->ev0) cudaEventDestroy(mp->ev0);
   if (mp->ev1) cudaEventDestroy(mp->ev1);

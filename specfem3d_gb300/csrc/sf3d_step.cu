@@ -34,15 +34,18 @@ __global__ void predictor_kernel(float* __restrict__ d, float* __restrict__ v, f
 }
 
 // Mass matrix + corrector (kernels/kernel_3_cuda_device.cu,
-// compute_forces_viscoelastic_calling_routine.F90:369-416).
+// compute_forces_viscoelastic_calling_routine.F90:369-416), unit-stride over (3, NGLOB).
 __global__ void mass_corrector_kernel(float* __restrict__ v, float* __restrict__ a, const float* __restrict__ rmx,
                                       const float* __restrict__ rmy, const float* __restrict__ rmz, long nglob,
                                       float dt2) {
-  long g = (long)blockIdx.x * blockDim.x + threadIdx.x;
-  if (g >= nglob) return;
-  const float ax = a[3 * g] * rmx[g], ay = a[3 * g + 1] * rmy[g], az = a[3 * g + 2] * rmz[g];
-  a[3 * g] = ax; a[3 * g + 1] = ay; a[3 * g + 2] = az;
-  v[3 * g] += dt2 * ax; v[3 * g + 1] += dt2 * ay; v[3 * g + 2] += dt2 * az;
+  const long i = (long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= 3 * nglob) return;
+  const long g = i / 3;
+  const int c = (int)(i - 3 * g);
+  const float rm = c == 0 ? __ldg(rmx + g) : (c == 1 ? __ldg(rmy + g) : __ldg(rmz + g));
+  const float ac = a[i] * rm;
+  a[i] = ac;
+  v[i] += dt2 * ac;
 }
 
 __global__ void corrector_kernel(float* __restrict__ v, const float* __restrict__ a, long n, float dt2) {
@@ -53,23 +56,23 @@ __global__ void corrector_kernel(float* __restrict__ v, const float* __restrict_
 
 // Corrector of step n-1 fused with the predictor of step n: one read and one
 // write of u, v, a per point instead of two passes.  Arithmetic per value is
-// identical to mass_corrector_kernel followed by predictor_kernel.
+// identical to mass_corrector_kernel followed by predictor_kernel.  Threads walk
+// the interleaved (3, NGLOB) arrays with unit stride so every access is
+// coalesced; the mass value comes from the component's rmass array.
 __global__ void corrector_predictor_kernel(float* __restrict__ d, float* __restrict__ v, float* __restrict__ a,
                                            const float* __restrict__ rmx, const float* __restrict__ rmy,
                                            const float* __restrict__ rmz, long nglob, float dt, float dt2,
                                            float dtsq2) {
-  long g = (long)blockIdx.x * blockDim.x + threadIdx.x;
-  if (g >= nglob) return;
-  const float rm[3] = {rmx[g], rmy[g], rmz[g]};
-#pragma unroll
-  for (int c = 0; c < 3; ++c) {
-    const long i = 3 * g + c;
-    const float ac = a[i] * rm[c];
-    const float vh = v[i] + dt2 * ac;
-    d[i] = d[i] + dt * vh + dtsq2 * ac;
-    v[i] = vh + dt2 * ac;
-    a[i] = 0.f;
-  }
+  const long i = (long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= 3 * nglob) return;
+  const long g = i / 3;
+  const int c = (int)(i - 3 * g);
+  const float rm = c == 0 ? __ldg(rmx + g) : (c == 1 ? __ldg(rmy + g) : __ldg(rmz + g));
+  const float ac = a[i] * rm;
+  const float vh = v[i] + dt2 * ac;
+  d[i] = d[i] + dt * vh + dtsq2 * ac;
+  v[i] = vh + dt2 * ac;
+  a[i] = 0.f;
 }
 
 // Stacey absorbing traction (compute_stacey_viscoelastic.F90:90-130,
@@ -78,11 +81,13 @@ __global__ void stacey_kernel(int nfaces, const int* __restrict__ abs_ispec, con
                               const float* __restrict__ normal, const float* __restrict__ jw,
                               const int* __restrict__ ibool, const float* __restrict__ rho_vp,
                               const float* __restrict__ rho_vs, const float* __restrict__ veloc,
-                              float* __restrict__ accel, float* __restrict__ record) {
+                              float* __restrict__ accel, float* __restrict__ record,
+                              const int* __restrict__ is_acoustic) {
   long idx = (long)blockIdx.x * blockDim.x + threadIdx.x;
   if (idx >= (long)nfaces * NGLL2) return;
   const int f = (int)(idx / NGLL2);
   const int e = abs_ispec[f];
+  if (is_acoustic[e]) return;
   const long q = (long)e * NGLL3_PAD + abs_pt[idx];
   const int g = ibool[q];
   const float vx = veloc[3L * g], vy = veloc[3L * g + 1], vz = veloc[3L * g + 2];
@@ -124,11 +129,11 @@ __global__ void stacey_replay_kernel(int nfaces, const int* __restrict__ abs_isp
 __global__ void sources_kernel(int nsrc, const int* __restrict__ ispec_src, const float* __restrict__ sa,
                                const float* __restrict__ stf_step, const float* __restrict__ stf_table,
                                const int* __restrict__ d_it, int stf_nstep, const int* __restrict__ ibool,
-                               float* __restrict__ accel) {
+                               float* __restrict__ accel, const int* __restrict__ is_acoustic) {
   const int is = blockIdx.x, p = threadIdx.x;
   if (is >= nsrc || p >= NGLL3) return;
   const int e = ispec_src[is];
-  if (e < 0) return;
+  if (e < 0 || is_acoustic[e]) return;
   float stf;
   if (stf_table) {
     const int it = *d_it;
@@ -317,7 +322,7 @@ void compute_stacey_viscoelastic_cuda_(long* Mesh_pointer, int* iphasef, realw* 
     stacey_kernel<<<nblk(n, 128), 128, 0, mp->stream>>>(mp->num_abs_faces, mp->d_abs_ispec, mp->d_abs_pt,
                                                         mp->d_abs_normal, mp->d_abs_jw, mp->d_ibool, mp->d_rho_vp,
                                                         mp->d_rho_vs, mp->f.veloc, mp->f.accel,
-                                                        store ? mp->d_stage : nullptr);
+                                                        store ? mp->d_stage : nullptr, mp->d_ispec_is_acoustic);
     if (!cuda_ok(cudaGetLastError(), "stacey_kernel")) return;
     if (store) {
       SF3D_CUDA(cudaMemcpyAsync(b_absorb_field, mp->d_stage, sizeof(float) * 3 * n, cudaMemcpyDeviceToHost,
@@ -337,7 +342,8 @@ void compute_stacey_viscoelastic_cuda_(long* Mesh_pointer, int* iphasef, realw* 
       // recomputed (checkpointed) backward field: same traction from b_veloc
       stacey_kernel<<<nblk(n, 128), 128, 0, mp->stream>>>(mp->num_abs_faces, mp->d_abs_ispec, mp->d_abs_pt,
                                                           mp->d_abs_normal, mp->d_abs_jw, mp->d_ibool, mp->d_rho_vp,
-                                                          mp->d_rho_vs, mp->b.veloc, mp->b.accel, nullptr);
+                                                          mp->d_rho_vs, mp->b.veloc, mp->b.accel, nullptr,
+                                                          mp->d_ispec_is_acoustic);
     }
     cuda_ok(cudaGetLastError(), "stacey_kernel(b)");
   }
@@ -356,7 +362,7 @@ static void add_sources(long* Mesh_pointer, double* h_stf, int* h_NSOURCES, bool
                             mp->stream));
   sources_kernel<<<mp->nsources, NGLL3_PAD, 0, mp->stream>>>(mp->nsources, mp->d_ispec_src, mp->d_sourcearrays,
                                                              mp->d_stf_step, nullptr, nullptr, 0, mp->d_ibool,
-                                                             F->accel);
+                                                             F->accel, mp->d_ispec_is_acoustic);
   // the host stf buffer is reused by the caller on the next step
   SF3D_CUDA(cudaStreamSynchronize(mp->stream));
   cuda_ok(cudaGetLastError(), "sources_kernel");
@@ -377,7 +383,7 @@ void kernel_3_a_cuda_(long* Mesh_pointer, realw* deltatover2_F, realw* b_deltato
   if (*APPROXIMATE_OCEAN_LOAD) { set_error(SF3D_ERR_ARG, "ocean load is not supported"); return; }
   Fields* F = pick(mp, *FORWARD_OR_ADJOINT);
   const float dt2 = *FORWARD_OR_ADJOINT == 1 ? *deltatover2_F : *b_deltatover2_F;
-  mass_corrector_kernel<<<nblk(mp->nglob, 256), 256, 0, mp->stream>>>(F->veloc, F->accel, mp->d_rmassx, mp->d_rmassy,
+  mass_corrector_kernel<<<nblk(3L * mp->nglob, 256), 256, 0, mp->stream>>>(F->veloc, F->accel, mp->d_rmassx, mp->d_rmassy,
                                                                      mp->d_rmassz, mp->nglob, dt2);
   cuda_ok(cudaGetLastError(), "mass_corrector_kernel");
 }
@@ -416,6 +422,7 @@ void compute_seismograms_cuda_(long* Mesh_pointer_f, realw* seismograms_d, realw
         mp->nrec_local, mp->d_ispec_rec, mp->d_hxir, mp->d_hetar, mp->d_hgammar, mp->d_nu_rec, mp->d_ibool, kd.field,
         kd.dst, nlen, cur, nullptr, nullptr, nullptr, 0);
   }
+  if (mp->save_p) launch_pressure_seismograms(mp, cur);
   if (!cuda_ok(cudaGetLastError(), "seismogram_kernel")) return;
   if (cur == nlen - 1 || *itf == *it_endf) {
     const size_t bytes = sizeof(float) * 3 * (size_t)mp->nrec_local * nlen;
@@ -426,7 +433,21 @@ void compute_seismograms_cuda_(long* Mesh_pointer_f, realw* seismograms_d, realw
       SF3D_CUDA(cudaMemcpyAsync(seismograms_v, mp->d_seismo_v, bytes, cudaMemcpyDeviceToHost, mp->stream));
     if (mp->save_a && !trick && seismograms_a)
       SF3D_CUDA(cudaMemcpyAsync(seismograms_a, mp->d_seismo_a, bytes, cudaMemcpyDeviceToHost, mp->stream));
+    std::vector<float> pbuf;
+    if (mp->save_p && mp->d_seismo_p && seismograms_p) {
+      pbuf.resize((size_t)mp->nrec_local * nlen);
+      SF3D_CUDA(cudaMemcpyAsync(pbuf.data(), mp->d_seismo_p, sizeof(float) * pbuf.size(), cudaMemcpyDeviceToHost,
+                                mp->stream));
+    }
     SF3D_CUDA(cudaStreamSynchronize(mp->stream));
+    // pressure goes to component 1 of the (NDIM, nrec_local, nlength) host array
+    for (int jt = 0; jt < (int)(pbuf.empty() ? 0 : nlen); ++jt)
+      for (int r = 0; r < mp->nrec_local; ++r) {
+        float* o = seismograms_p + 3L * (r + (long)mp->nrec_local * jt);
+        o[0] = pbuf[r + (size_t)mp->nrec_local * jt];
+        o[1] = 0.f;
+        o[2] = 0.f;
+      }
   }
 }
 
@@ -443,8 +464,7 @@ int sf3d_set_stf_table(long* Mesh_pointer, const double* h_stf, int nsources, in
   cudaFree(mp->d_stf_table);
   mp->d_stf_table = nullptr;
   if (!alloc_zero((void**)&mp->d_stf_table, sizeof(float) * tab.size())) return SF3D_ERR_CUDA;
-  SF3D_CUDA_RET(cudaMemcpy(mp->d_stf_table, tab.data(), sizeof(float) * tab.size(), cudaMemcpyHostToDevice),
-                SF3D_ERR_CUDA);
+  if (!copy_sync(mp->d_stf_table, tab.data(), sizeof(float) * tab.size(), cudaMemcpyHostToDevice, mp->stream)) return SF3D_ERR_CUDA;
   mp->stf_nstep = nstep;
   return SF3D_OK;
 }
@@ -467,7 +487,7 @@ static int enqueue_step(Mesh* mp, float dt, float dt2, float dtsq2, bool first_s
     const long n = 3L * mp->nglob;
     predictor_kernel<<<nblk(n, 256), 256, 0, s>>>(F.displ, F.veloc, F.accel, n, dt, dt2, dtsq2);
   } else {
-    corrector_predictor_kernel<<<nblk(mp->nglob, 256), 256, 0, s>>>(F.displ, F.veloc, F.accel, mp->d_rmassx,
+    corrector_predictor_kernel<<<nblk(3L * mp->nglob, 256), 256, 0, s>>>(F.displ, F.veloc, F.accel, mp->d_rmassx,
                                                                     mp->d_rmassy, mp->d_rmassz, mp->nglob, dt, dt2,
                                                                     dtsq2);
   }
@@ -476,12 +496,13 @@ static int enqueue_step(Mesh* mp, float dt, float dt2, float dtsq2, bool first_s
     const long n = (long)mp->num_abs_faces * NGLL2;
     stacey_kernel<<<nblk(n, 128), 128, 0, s>>>(mp->num_abs_faces, mp->d_abs_ispec, mp->d_abs_pt, mp->d_abs_normal,
                                                 mp->d_abs_jw, mp->d_ibool, mp->d_rho_vp, mp->d_rho_vs, F.veloc,
-                                                F.accel, nullptr);
+                                                F.accel, nullptr, mp->d_ispec_is_acoustic);
     ++launches;
   }
   if (mp->nsources > 0 && mp->d_stf_table) {
     sources_kernel<<<mp->nsources, NGLL3_PAD, 0, s>>>(mp->nsources, mp->d_ispec_src, mp->d_sourcearrays, nullptr,
-                                                      mp->d_stf_table, mp->d_it, mp->stf_nstep, mp->d_ibool, F.accel);
+                                                      mp->d_stf_table, mp->d_it, mp->stf_nstep, mp->d_ibool, F.accel,
+                                                      mp->d_ispec_is_acoustic);
     ++launches;
   }
   const bool att = mp->attenuation != 0;
@@ -511,10 +532,6 @@ int sf3d_iterate_time(long* Mesh_pointer, int it_begin, int it_end, realw deltat
   if (!mp) return SF3D_ERR_STATE;
   if (!mp->f.displ) { set_error(SF3D_ERR_STATE, "prepare_fields_elastic_device not called"); return SF3D_ERR_STATE; }
   if (it_begin < 1 || it_end < it_begin) { set_error(SF3D_ERR_ARG, "invalid it range"); return SF3D_ERR_ARG; }
-  if (mp->nrec_local > 0 && mp->save_d && it_end > mp->nlength_seismogram) {
-    set_error(SF3D_ERR_ARG, "it_end exceeds nlength_seismogram");
-    return SF3D_ERR_ARG;
-  }
   if (mp->nsources > 0 && (!mp->d_stf_table || it_end > mp->stf_nstep)) {
     set_error(SF3D_ERR_STATE, "sf3d_set_stf_table must cover it_end");
     return SF3D_ERR_STATE;
@@ -557,7 +574,7 @@ int sf3d_iterate_time(long* Mesh_pointer, int it_begin, int it_end, realw deltat
     cudaGraphDestroy(graph);
   }
   while (remaining > 0) { step(false); --remaining; }
-  mass_corrector_kernel<<<nblk(mp->nglob, 256), 256, 0, s>>>(mp->f.veloc, mp->f.accel, mp->d_rmassx, mp->d_rmassy,
+  mass_corrector_kernel<<<nblk(3L * mp->nglob, 256), 256, 0, s>>>(mp->f.veloc, mp->f.accel, mp->d_rmassx, mp->d_rmassy,
                                                              mp->d_rmassz, mp->nglob, dt2);
   ++launches;
   SF3D_CUDA_RET(cudaEventRecord(mp->ev1, s), SF3D_ERR_CUDA);
@@ -569,8 +586,7 @@ int sf3d_iterate_time(long* Mesh_pointer, int it_begin, int it_end, realw deltat
   mp->last_stiff_ms = 0.f;
   if (timing) {
     std::vector<unsigned long long> st(2 * (size_t)it_end);
-    SF3D_CUDA_RET(cudaMemcpy(st.data(), mp->d_stamps, sizeof(unsigned long long) * st.size(), cudaMemcpyDeviceToHost),
-                  SF3D_ERR_CUDA);
+    if (!copy_sync(st.data(), mp->d_stamps, sizeof(unsigned long long) * st.size(), cudaMemcpyDeviceToHost, mp->stream)) return SF3D_ERR_CUDA;
     double ns = 0;
     for (int it = it_begin; it <= it_end; ++it) {
       const unsigned long long a = st[2 * (it - 1)], b = st[2 * (it - 1) + 1];

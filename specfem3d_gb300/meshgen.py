@@ -227,6 +227,9 @@ def build_database(cfg: dict, material=None, dtype=np.float32) -> dict:
         db[n] = zero.copy()
     db["jacobian"] = per_elem(dx * dy * dz / 8.0)
     # materials
+    if material is None and cfg.get("perturbation"):
+        from . import models
+        material = models.perturbed_material(cfg, **cfg["perturbation"])
     if material is None:
         lay = np.asarray(cfg["elem_layer"], np.int64)
         L = cfg["layers"]
@@ -236,19 +239,26 @@ def build_database(cfg: dict, material=None, dtype=np.float32) -> dict:
     else:
         rho, vp, vs = (np.asarray(a, np.float32) for a in material)
     r, p, s = rho.astype(dtype), vp.astype(dtype), vs.astype(dtype)
+    # fluid elements: zero shear velocity (generate_databases/get_model.F90 sets
+    # ispec_is_acoustic for vs == 0)
+    db["ispec_is_acoustic"] = (np.asarray(vs, np.float32).reshape(nspec, NGLL3) == 0).all(axis=1).astype(np.int32)
     db["rhostore"] = r
     db["kappastore"] = r * (p * p - dtype(4.0 / 3.0) * s * s)
     db["mustore"] = r * s * s
     db["rho_vp"] = r * p
     db["rho_vs"] = r * s
-    # absorbing faces
+    # absorbing faces, fluid-solid coupling faces, free surface
     _absorbing(cfg, B, db, dtype)
+    _coupling_and_free_surface(cfg, B, db, dtype)
     # mass matrices
     _mass(cfg, B, db, dtype)
     db.update(derivation_matrices())
     # sources / receivers / stf
     _sources_receivers(cfg, B, db, dtype)
     db["attenuation"] = int(bool(cfg.get("attenuation", False)))
+    if db["attenuation"]:
+        from . import attenuation
+        db.update(attenuation.setup(cfg, db))
     return db
 
 
@@ -305,6 +315,66 @@ def _absorbing(cfg, B, db, dtype):
     db["stacey"] = int(db["num_abs_boundary_faces"] > 0)
 
 
+def _face_pts(iface):
+    """Element-local point indices of face iface (1..6) in face GLL order
+    (get_element_face_gll_indices, shared/get_element_face.f90:169-279)."""
+    a = np.arange(5)
+    A, Bb = np.meshgrid(a, a, indexing="xy")
+    A, Bb = A.reshape(-1), Bb.reshape(-1)
+    if iface in (1, 2):
+        i, j, k = np.full(25, 0 if iface == 1 else 4), A, Bb
+    elif iface in (3, 4):
+        i, j, k = A, np.full(25, 0 if iface == 3 else 4), Bb
+    else:
+        i, j, k = A, Bb, np.full(25, 0 if iface == 5 else 4)
+    return np.stack([i, j, k], axis=-1)
+
+
+def _coupling_and_free_surface(cfg, B, db, dtype):
+    """Fluid-solid coupling faces seen from the fluid element, normal pointing out
+    of the fluid, in element then face order (generate_databases/get_coupling_surfaces.f90:270-380);
+    free-surface faces = top faces of the block (face 6)."""
+    isac = db["ispec_is_acoustic"].astype(bool)
+    nspec = B.nspec
+    e = np.arange(nspec)
+    ex, ey, ez = B.elem_xyz(e)
+    ispecs, ijks, jws, normals = [], [], [], []
+    if isac.any() and (~isac).any():
+        nb = {1: (ex > 0, e - 1), 2: (ex < B.nx - 1, e + 1), 3: (ey > 0, e - B.nx), 4: (ey < B.ny - 1, e + B.nx),
+              5: (ez > 0, e - B.nx * B.ny), 6: (ez < B.nz - 1, e + B.nx * B.ny)}
+        flag = np.zeros((nspec, 7), bool)
+        for f in range(1, 7):
+            has, other = nb[f]
+            flag[:, f] = isac & has & ~isac[np.where(has, other, 0)]
+        for el in np.nonzero(flag.any(axis=1))[0]:
+            fx, fy, fz = (int(v) for v in B.elem_xyz(el))
+            dx = B.xl[fx + 1] - B.xl[fx]; dy = B.yl[fy + 1] - B.yl[fy]; dz = B.zl[fz + 1] - B.zl[fz]
+            for f in range(1, 7):
+                if not flag[el, f]:
+                    continue
+                pts = _face_pts(f)
+                a = np.arange(5)
+                A, Bb = np.meshgrid(a, a, indexing="xy")
+                w = (WGLL[A.reshape(-1)] * WGLL[Bb.reshape(-1)])
+                jac2 = {1: dy * dz, 2: dy * dz, 3: dx * dz, 4: dx * dz, 5: dx * dy, 6: dx * dy}[f] / 4.0
+                n = np.zeros(3)
+                n[(f - 1) // 2] = -1.0 if f % 2 == 1 else 1.0
+                ispecs.append(el + 1)
+                ijks.append(pts + 1)
+                jws.append(jac2 * w)
+                normals.append(np.broadcast_to(n, (25, 3)))
+    nc = len(ispecs)
+    db["num_coupling_ac_el_faces"] = nc
+    db["coupling_ac_el_ispec"] = np.asarray(ispecs, np.int32)
+    db["coupling_ac_el_ijk"] = (np.asarray(ijks, np.int32).reshape(-1) if nc else np.zeros(0, np.int32))
+    db["coupling_ac_el_jacobian2Dw"] = (np.asarray(jws, dtype).reshape(-1) if nc else np.zeros(0, dtype))
+    db["coupling_ac_el_normal"] = (np.asarray(normals, dtype).reshape(-1) if nc else np.zeros(0, dtype))
+    top = np.nonzero(ez == B.nz - 1)[0]
+    db["num_free_surface_faces"] = len(top)
+    db["free_surface_ispec"] = (top + 1).astype(np.int32)
+    db["free_surface_ijk"] = np.tile((_face_pts(6) + 1).reshape(-1), len(top)).astype(np.int32)
+
+
 def _mass(cfg, B, db, dtype):
     nspec, nglob = B.nspec, B.nglob
     irr = db["irregular_element_number"]
@@ -317,9 +387,31 @@ def _mass(cfg, B, db, dtype):
     if (~reg).any():
         jel[~reg] = db["jacobian"].reshape(-1, NGLL3)[irr[~reg] - 1, 0]
     rho = db["rhostore"].reshape(nspec, NGLL3).astype(np.float64)
+    isac = db["ispec_is_acoustic"].astype(bool)
+    ib = db["ibool"].reshape(nspec, NGLL3).astype(np.int64) - 1
     terms = (jel[:, None] * w3[None, :] * rho).astype(dtype).astype(np.float64)
-    rmass = np.bincount(db["ibool"].astype(np.int64) - 1, weights=terms.reshape(-1), minlength=nglob)
+    terms[isac] = 0.0
+    rmass = np.bincount(ib.reshape(-1), weights=terms.reshape(-1), minlength=nglob)
     rmass = rmass.astype(dtype)
+    if isac.any():
+        # rmass_acoustic = 1 / (sum J w / kappa + Stacey term) (define_mass_matrices.f90:120-160, :488-520)
+        kap = db["kappastore"].reshape(nspec, NGLL3).astype(np.float64)
+        ta = np.zeros_like(terms)
+        ta[isac] = (jel[isac, None] * w3[None, :] / kap[isac]).astype(dtype)
+        rma = np.bincount(ib.reshape(-1), weights=ta.reshape(-1), minlength=nglob).astype(dtype)
+        if db["stacey"]:
+            nf = db["num_abs_boundary_faces"]
+            isp = db["abs_boundary_ispec"] - 1
+            ijk = db["abs_boundary_ijk"].reshape(nf, 25, 3) - 1
+            pt = ijk[..., 0] + 5 * ijk[..., 1] + 25 * ijk[..., 2]
+            q = isp[:, None] * NGLL3 + pt
+            sel = isac[isp]
+            sn = dtype(0.5 * float(cfg["dt"])) / db["rho_vp"][q[sel]]
+            add = db["abs_boundary_jacobian2Dw"].reshape(nf, 25)[sel] * sn
+            rma = rma + np.bincount(db["ibool"][q[sel]].reshape(-1).astype(np.int64) - 1,
+                                    weights=add.astype(np.float64).reshape(-1), minlength=nglob).astype(dtype)
+        rma[rma <= 0] = 1
+        db["rmass_acoustic"] = (dtype(1) / rma).astype(dtype)
     mx = rmass.copy(); my = rmass.copy(); mz = rmass.copy()
     if db["stacey"]:
         dt2 = dtype(0.5 * float(cfg["dt"]))
@@ -333,9 +425,10 @@ def _mass(cfg, B, db, dtype):
         vn = dt2 * (n[..., 0] + n[..., 1] + n[..., 2])
         jw = db["abs_boundary_jacobian2Dw"].reshape(nf, 25)
         g = db["ibool"][q].astype(np.int64) - 1
+        el = ~isac[isp]
         for c, m in enumerate((mx, my, mz)):
             t = rvp * vn * n[..., c] + rvs * (dt2 - vn * n[..., c])
-            add = np.bincount(g.reshape(-1), weights=(t * jw).astype(np.float64).reshape(-1), minlength=nglob)
+            add = np.bincount(g[el].reshape(-1), weights=(t * jw)[el].astype(np.float64).reshape(-1), minlength=nglob)
             m += add.astype(dtype)
     for m in (mx, my, mz):
         m[m <= 0] = 1

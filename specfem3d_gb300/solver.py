@@ -40,9 +40,13 @@ class GPUSolver:
         self.deltatsqover2 = np.float32(dt * dt / np.float32(2))
         self.mesh = ctypes.c_long(0)
         self.mp = ctypes.addressof(self.mesh)
-        self.record = record
+        self.record = tuple(cfg.get("record", record))
+        self.isac = np.asarray(db.get("ispec_is_acoustic", np.zeros(self.nspec, np.int32)), np.int32)
+        self.coupled = bool(self.isac.any())
         self._prepare_constants(db, save_forward)
         self._prepare_fields(db)
+        if self.coupled:
+            self._prepare_acoustic(db)
         self.it = 1
 
     # ------------------------------------------------------------------ setup
@@ -67,11 +71,11 @@ class GPUSolver:
             A.ai(np.ones(nspec, np.int32)), A.i(self.nsources), A.i(self.nsources), A.af(db["sourcearrays"]),
             A.ai(np.zeros(max(self.nsources, 1), np.int32)), A.ai(db["ispec_selected_source"]),
             A.ai(db["ispec_selected_rec"]), A.i(nrec), A.i(nrec), A.i(self.simulation_type), A.i(0),
-            A.i(0), A.i(nspec), A.ai(np.zeros(nspec, np.int32)), A.ai(np.ones(nspec, np.int32)), A.i(0),
-            A.i(int(save_forward)), A.af(hx), A.af(he), A.af(hg), A.ad(nu), A.ad(nu),
+            A.i(int(self.isac.sum())), A.i(int(nspec - self.isac.sum())), A.ai(self.isac), A.ai(1 - self.isac),
+            A.i(0), A.i(int(save_forward)), A.af(hx), A.af(he), A.af(hg), A.ad(nu), A.ad(nu),
             A.ai(np.zeros(max(nrec, 1), np.int32)), A.i(self.nlength),
             A.i(int("displ" in self.record)), A.i(int("veloc" in self.record)), A.i(int("accel" in self.record)),
-            A.i(0), A.i(1), A.i(0), A.i(0), A.i(0),
+            A.i(int("pressure" in self.record)), A.i(1), A.i(0), A.i(0), A.i(0),
         ]
         self.L.prepare_constants_device_(*args)
         abi.check()
@@ -79,15 +83,17 @@ class GPUSolver:
     def _prepare_fields(self, db):
         A = abi.Args()
         nspec = self.nspec
-        phase = np.zeros((nspec, 2), np.int32)
-        phase[:, 1] = np.arange(1, nspec + 1)
+        solid = np.nonzero(self.isac == 0)[0] + 1
+        self.nspec_elastic = len(solid)
+        phase = np.zeros((max(len(solid), 1), 2), np.int32)
+        phase[:len(solid), 1] = solid
         att = self.attenuation
         strain = int(att or self.simulation_type == 3)
         zsls = np.zeros(N_SLS * NGLL3 * nspec, np.float32) if att else None
         zeps = np.zeros(NGLL3 * nspec, np.float32) if strain else None
         args = [
             self.mp, A.af(db["rmassx"]), A.af(db["rmassy"]), A.af(db["rmassz"]), A.af(db["rho_vp"]),
-            A.af(db["rho_vs"]), A.af(db["kappastore"]), A.af(db["mustore"]), A.i(nspec),
+            A.af(db["rho_vs"]), A.af(db["kappastore"]), A.af(db["mustore"]), A.i(phase.shape[0]),
             A.ai(phase.reshape(-1, order="F")), A.af(None), A.i(0), A.i(strain),
             *(A.af(zeps) for _ in range(5)), A.i(att), A.i(N_SLS * NGLL3 * nspec if att else 1),
             *(A.af(zsls) for _ in range(5)), A.af(db.get("factor_common") if att else None),
@@ -104,20 +110,60 @@ class GPUSolver:
             if self.L.sf3d_set_stf_table(self.mp, stf.ctypes.data, self.nsources, stf.shape[0]) != 0:
                 abi.check()
 
+    def _prepare_acoustic(self, db):
+        """prepare_fields_acoustic_device (specfem3D/prepare_gpu.f90:170-200)."""
+        A = abi.Args()
+        fluid = np.nonzero(self.isac)[0] + 1
+        self.nspec_acoustic = len(fluid)
+        phase = np.zeros((len(fluid), 2), np.int32)
+        phase[:, 1] = fluid
+        nfs = int(db["num_free_surface_faces"])
+        ncp = int(db["num_coupling_ac_el_faces"])
+        self.ncoupling = ncp
+        self.L.prepare_fields_acoustic_device_(
+            self.mp, A.af(db["rmass_acoustic"]), A.af(db["rhostore"]), A.af(db["kappastore"]), A.i(len(fluid)),
+            A.ai(phase.reshape(-1, order="F")), A.i(0), A.i(nfs), A.ai(db["free_surface_ispec"]),
+            A.ai(db["free_surface_ijk"]), A.i(0), A.af(None), A.i(1), A.i(ncp), A.ai(db["coupling_ac_el_ispec"]),
+            A.ai(db["coupling_ac_el_ijk"]), A.af(db["coupling_ac_el_normal"]),
+            A.af(db["coupling_ac_el_jacobian2Dw"]), A.i(0), A.i(0), A.ai(None))
+        abi.check()
+
     # ---------------------------------------------------------- one step (ABI)
+    def _stf_now(self, it):
+        return np.ascontiguousarray(np.asarray(self.db["stf"], np.float64).reshape(self.nsources, -1)[:, it - 1])
+
+    def _acoustic_step(self, A, it):
+        """compute_forces_acoustic_forward_calling (compute_forces_acoustic_calling_routine.f90:54-343)."""
+        L, one = self.L, A.i(1)
+        L.acoustic_enforce_free_surf_cuda_(self.mp, A.i(0), one)
+        for iphase in (1, 2):
+            L.compute_forces_acoustic_cuda_(self.mp, A.i(iphase), A.i(0), A.i(self.nspec_acoustic), one)
+            if iphase == 1:
+                L.compute_stacey_acoustic_cuda_(self.mp, A.i(1), A.af(None), one)
+                L.compute_coupling_ac_el_cuda_(self.mp, A.i(1), A.i(self.ncoupling), one)
+                if self.nsources:
+                    L.compute_add_sources_ac_cuda_(self.mp, A.i(self.nsources), A.ad(self._stf_now(it)), A.i(1))
+        L.kernel_3_acoustic_cuda_(self.mp, A.f(self.deltatover2), A.f(0.0), one)
+        L.acoustic_enforce_free_surf_cuda_(self.mp, A.i(0), one)
+
     def step(self):
         """One time step through the per-call entry points, in the reference's order."""
         L, A, it = self.L, abi.Args(), self.it
         one = A.i(1)
         L.update_displacement_cuda_(self.mp, A.f(self.deltat), A.f(self.deltatover2), A.f(self.deltatsqover2), one)
+        if self.coupled:
+            L.update_displacement_ac_cuda_(self.mp, A.f(self.deltat), A.f(self.deltatover2),
+                                           A.f(self.deltatsqover2), one)
+            self._acoustic_step(A, it)
         for iphase in (1, 2):
-            L.compute_forces_viscoelastic_cuda_(self.mp, A.i(iphase), A.f(self.deltat), A.i(0), A.i(self.nspec),
-                                                A.i(self.strain), A.i(self.attenuation), one)
+            L.compute_forces_viscoelastic_cuda_(self.mp, A.i(iphase), A.f(self.deltat), A.i(0),
+                                                A.i(self.nspec_elastic), A.i(self.strain), A.i(self.attenuation), one)
             if iphase == 1:
                 L.compute_stacey_viscoelastic_cuda_(self.mp, A.i(1), A.af(None), one)
+                if self.coupled:
+                    L.compute_coupling_el_ac_cuda_(self.mp, A.i(1), A.i(self.ncoupling), one)
                 if self.nsources:
-                    stf = np.ascontiguousarray(np.asarray(self.db["stf"], np.float64).reshape(self.nsources, -1)[:, it - 1])
-                    L.compute_add_sources_el_cuda_(self.mp, A.ad(stf), A.i(self.nsources))
+                    L.compute_add_sources_el_cuda_(self.mp, A.ad(self._stf_now(it)), A.i(self.nsources))
         L.kernel_3_a_cuda_(self.mp, A.f(self.deltatover2), A.f(0.0), A.i(0), one)
         if self.nrec:
             if not hasattr(self, "_seis_host"):
@@ -150,12 +196,23 @@ class GPUSolver:
 
     # ----------------------------------------------------------------- outputs
     def seismograms(self) -> np.ndarray:
-        """(nrec, 3, nlength) displacement traces."""
+        """(nrec, 3, nlength) displacement traces (pressure runs: the per-call
+        path's host array, pressure in component 0)."""
+        if "pressure" in self.record:
+            return self._seis_host.reshape(self.nlength, self.nrec, 3).transpose(1, 2, 0).copy()
         out = np.zeros(3 * self.nrec * self.nlength, np.float32)
         if self.nrec:
             self.L.sf3d_get_seismograms(self.mp, out.ctypes.data)
             abi.check()
         return out.reshape(self.nlength, self.nrec, 3).transpose(1, 2, 0)
+
+    def potentials(self):
+        A = abi.Args()
+        p, pd, pdd = (np.zeros(self.nglob, np.float32) for _ in range(3))
+        self.L.transfer_fields_ac_from_device_(A.i(self.nglob), p.ctypes.data, pd.ctypes.data, pdd.ctypes.data,
+                                               self.mp)
+        abi.check()
+        return p, pd, pdd
 
     def fields(self):
         A = abi.Args()
@@ -184,8 +241,9 @@ class GPUSolver:
     def forces_only(self, iphase: int = 2):
         """One stiffness pass (compute_forces_viscoelastic_cuda) on the current fields."""
         A = abi.Args()
-        self.L.compute_forces_viscoelastic_cuda_(self.mp, A.i(iphase), A.f(self.deltat), A.i(0), A.i(self.nspec),
-                                                 A.i(self.strain), A.i(self.attenuation), A.i(1))
+        self.L.compute_forces_viscoelastic_cuda_(self.mp, A.i(iphase), A.f(self.deltat), A.i(0),
+                                                 A.i(self.nspec_elastic), A.i(self.strain), A.i(self.attenuation),
+                                                 A.i(1))
         self.L.sf3d_synchronize(self.mp)
         abi.check()
 
