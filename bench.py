@@ -20,7 +20,8 @@ Metric: GLL-point updates per second = NGLOB x steps / device time.
   solver, OpenMP over all host cores) on a bounded sample of the same physics.
 
 ``--impl reference`` times that CPU implementation alone (the reference's
-Fortran solver cannot be built here).  Under torchrun with N>1
+Fortran solver needs its autotools build, MPI and generated headers, so the
+C restatement stands in for it).  Under torchrun with N>1
 every rank runs an independent replica of the workload (no data-path
 collective) and rank 0 reports the whole-job throughput.
 """
@@ -117,7 +118,7 @@ def cpu_baseline(steps: int, nthreads: int):
     block of the same layered viscoelastic model (irregular elements, Stacey)."""
     from oracle import oracle as O
     from specfem3d_gb300 import configs, meshgen
-    cfg = configs.cfg1(nstep=steps + 2, nx=32, ny=32, counts=(4, 6, 6))
+    cfg = configs.layered_viscoelastic(nstep=steps + 2, nx=32, ny=32, counts=(4, 6, 6))
     cfg["x1"] = 20000.0 * 32 / 128
     cfg["y1"] = 20000.0 * 32 / 128
     db = meshgen.build_database(cfg)
@@ -127,6 +128,37 @@ def cpu_baseline(steps: int, nthreads: int):
     sim.step(steps)
     dt = time.perf_counter() - t
     return db["nglob"] * steps / dt, dict(nspec=db["nspec"], nglob=db["nglob"], steps=steps, seconds=dt)
+
+
+def adjoint_leg(nshots: int):
+    """Seconds per shot of the checkpointed misfit gradient on the 64x64x32-element
+    gradient workload (3000 steps, checkpoints every 200 steps): forward from rest,
+    then the reverse sweep with recomputation; observed traces from the true model."""
+    from specfem3d_gb300 import configs, gradient as G, meshgen
+    from specfem3d_gb300.solver import GPUSolver
+    cfg = configs.adjoint_gradient(nshots=nshots)
+    db_true = meshgen.build_database(cfg, material=G.true_material(cfg))
+    observed = []
+    for i in range(nshots):
+        c = G.shot_config(cfg, i)
+        c["record"] = ("displ",)
+        s = GPUSolver(G.shot_database(db_true, cfg, i), c, nlength=cfg["nstep"])
+        s.run(cfg["nstep"], steps_per_graph=50)
+        observed.append(s.seismograms())
+        s.close()
+    del db_true
+    db0 = meshgen.build_database(cfg, material=G.background_material(cfg))
+    t0 = time.perf_counter()
+    J, grad, timing = G.misfit_gradient(lambda i: G.shot_database(db0, cfg, i), cfg, observed,
+                                        cfg["checkpoint_every"])
+    wall = time.perf_counter() - t0
+    fwd = sum(t[0] for t in timing) / 1000.0
+    bwd = sum(t[1] for t in timing) / 1000.0
+    return {"unit": "s/shot", "s_per_shot": wall / nshots, "device_s_per_shot": (fwd + bwd) / nshots,
+            "forward_s_per_shot": fwd / nshots, "backward_s_per_shot": bwd / nshots, "shots": nshots,
+            "nstep": cfg["nstep"], "checkpoint_every": cfg["checkpoint_every"], "nspec": db0["nspec"],
+            "nglob": db0["nglob"], "misfit": J, "gradient_dtype": "f64 accumulation, f32 fields",
+            "workload": "64x64x32 hexes, 20x20x10 km, perturbed background, +3% vs blob true model"}
 
 
 def run_reference(args, rank):
@@ -140,7 +172,7 @@ def run_reference(args, rank):
     line = {"metric": METRIC, "value": val, "unit": UNIT, "n_gpus": args.gpus, "steps": steps,
             "warmup": args.warmup, "ms_per_step": 1000 * info["seconds"] / steps, "higher_is_better": True,
             "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
-            "config": {"workload": "cfg1 layered viscoelastic block, CPU sample", "sample_elements": info["nspec"]},
+            "config": {"workload": "layered viscoelastic block, CPU sample", "sample_elements": info["nspec"]},
             "impl": "reference",
             "cpu_baseline": {"value": val, "unit": UNIT, "cores": nthreads, "kind": "port", "sample": sample},
             "e2e": {"value": val, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
@@ -159,6 +191,13 @@ def main():
     ap.add_argument("--e2e-steps", type=int, default=50)
     ap.add_argument("--cpu-steps", type=int, default=40)
     ap.add_argument("--no-cpu", action="store_true")
+    ap.add_argument("--variant", type=int, default=-1,
+                    help="stiffness kernel variant (sf3d_set_stiffness_variant); -1: autotune at rest")
+    ap.add_argument("--adjoint", type=int, default=0,
+                    help="also time the checkpointed misfit gradient over this many shots of the "
+                         "8-shot 64x64x32 gradient workload (0: skip)")
+    ap.add_argument("--roofline-steps", type=int, default=20,
+                    help="steps whose stiffness launches are bracketed by CUDA events")
     args = ap.parse_args()
     rank = int(os.environ.get("RANK", "0"))
     world = int(os.environ.get("WORLD_SIZE", "1"))
@@ -177,12 +216,14 @@ def main():
         A = abi.Args()
         L.initialize_gpu_device_(A.i(lr), A.i(0))
     W, K = max(3, args.warmup), max(1, args.steps)
+    Kr = max(3, min(K, args.roofline_steps))
+    nstep_total = W + K + Kr + args.e2e_steps + 2
     if args.small:
-        cfg = configs.cfg1(nstep=W + K + args.e2e_steps + 2, nx=32, ny=32, counts=(4, 6, 6))
-        workload = "cfg1-physics 32x32x16 block (reduced)"
+        cfg = configs.layered_viscoelastic(nstep=nstep_total, nx=32, ny=32, counts=(4, 6, 6))
+        workload = "layered viscoelastic 32x32x16 block (reduced)"
     else:
-        cfg = configs.cfg1(nstep=W + K + args.e2e_steps + 2)
-        workload = "cfg1: layered viscoelastic 20x20x10 km, 128x128x64 hexes, N_SLS=3, Stacey 5 faces"
+        cfg = configs.layered_viscoelastic(nstep=nstep_total)
+        workload = "layered viscoelastic 20x20x10 km, 128x128x64 hexes, N_SLS=3, Stacey 5 faces"
     t0 = time.perf_counter()
     db = meshgen.build_database(cfg)
     t_db = time.perf_counter() - t0
@@ -191,13 +232,29 @@ def main():
     g = solver.GPUSolver(db, cfg, nlength=1)
     t_up = time.perf_counter() - t0
     # ---------------- value: device-resident, graph-captured steps ----------------
+    if args.variant >= 0:
+        g.set_stiffness_variant(args.variant)
+        autotune = None
+    else:
+        # fields are at rest: time every stiffness variant and keep the fastest
+        ms = (ctypes.c_float * 5)()
+        best = ctypes.c_int()
+        if L.sf3d_autotune_stiffness(g.mp, 3, ms, ctypes.addressof(best)) != 0:
+            abi.check()
+        autotune = {"ms_per_variant": [round(float(x), 4) for x in ms], "chosen": best.value}
+        args.variant = best.value
     g.run(W, steps_per_graph=args.graph)
     L.sf3d_synchronize(g.mp)
     if dist:
         dist.barrier()
     with ClockSampler() as clk:
-        g.run(K, steps_per_graph=args.graph, timing=True)
-    tm = g.last_timing()
+        g.run(K, steps_per_graph=args.graph)
+        tm = g.last_timing()
+        # kernel-level timing: CUDA events on the compute stream around every
+        # stiffness launch (steps launched one by one, not through a graph)
+        g.run(Kr, steps_per_graph=0, timing=True)
+        tk = g.last_timing()
+    abi.check()
     total_ms = tm["total_ms"]
     if dist:
         import torch
@@ -205,7 +262,7 @@ def main():
         dist.all_reduce(t, op=dist.ReduceOp.MAX)
         total_ms = float(t.item())
     value = nglob * K * world / (total_ms / 1000.0)
-    stiff_ms = tm["stiffness_ms"] / max(tm["stiffness_launches"], 1)
+    stiff_ms = tk["stiffness_ms"] / max(tk["stiffness_launches"], 1)
     bytes_launch = 33000.0 * nspec + 48.0 * nglob
     peak, peak_kind = _peaks()
     achieved = bytes_launch / (stiff_ms / 1000.0) / 1e9
@@ -235,15 +292,21 @@ def main():
         "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
                      "peak_kind": peak_kind,
                      "traffic": (traffic_pe * nspec if traffic_pe else None),
-                     "kernel": "stiffness_kernel<att>", "algorithmic_bytes_per_launch": bytes_launch,
-                     "mean_launch_ms": stiff_ms},
+                     "kernel": ("stiffness_pipe_kernel<att>" if args.variant == 1 else
+                                f"stiffness_kernel<att, {[4, 0, 5, 6, 7][args.variant]} CTAs/SM>"),
+                     "autotune": autotune,
+                     "algorithmic_bytes_per_launch": bytes_launch,
+                     "mean_launch_ms": stiff_ms, "timed_launches": tk["stiffness_launches"]},
         "e2e": {"value": e2e_value, "unit": UNIT, "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h,
                 "steps": Ke, "path": "per-call FC_FUNC_ entry points"},
         "gpu_launches": tm["total_launches"],
+        "gpu_launches_note": "kernels launched by the timed sf3d_iterate_time call (value)",
         "clocks": clk.summary(),
         "setup": {"database_s": t_db, "upload_s": t_up},
         "stable": rc == 0,
     }
+    if args.adjoint > 0:
+        line["adjoint"] = adjoint_leg(args.adjoint)
     if rank == 0 and not args.no_cpu:
         cv, info = cpu_baseline(args.cpu_steps, os.cpu_count() or 1)
         line["cpu_baseline"] = {"value": cv, "unit": UNIT, "cores": os.cpu_count() or 1, "kind": "port",

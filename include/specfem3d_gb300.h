@@ -294,9 +294,88 @@ int sf3d_iterate_time(long *Mesh_pointer, int it_begin, int it_end, realw deltat
 int sf3d_get_seismograms(long *Mesh_pointer, realw *h_seismograms);
 
 /* Device time of the stiffness kernel launches of the last sf3d_iterate_time
- * call, in ms (CUDA events on the compute stream), and their count. */
+ * call with flags bit 0 set, in ms (a pair of CUDA events recorded on the
+ * compute stream around each step's stiffness launches), their count, and the
+ * event-timed total of the call. */
 int sf3d_last_timing(long *Mesh_pointer, float *stiffness_ms, int *stiffness_launches,
                      float *total_ms, int *total_launches);
+
+/* Select the elastic stiffness kernel.  All variants compute the same
+ * arithmetic in the same order:
+ *   0, 2, 3, 4: one 128-thread CTA per element, compiled for 4, 5, 6, 7
+ *               resident CTAs per SM (register budget 128, 96, 80, 72);
+ *   1:          persistent CTAs fed by a three-stage bulk-copy (TMA) pipeline.
+ * Default 3 (the fastest on GB300 for the layered viscoelastic workload).
+ * No reference counterpart (the reference compiles one Kernel_2 per
+ * configuration). */
+int sf3d_set_stiffness_variant(long *Mesh_pointer, int variant);
+
+/* Time every stiffness variant over `reps` full passes and keep the fastest.
+ * Must run on a wavefield at rest (after prepare_fields_elastic_device, before
+ * the first step): zero fields make the passes leave every array unchanged;
+ * returns SF3D_ERR_STATE otherwise.  ms_per_variant (5 floats) and
+ * best_variant may be NULL.  No reference counterpart. */
+int sf3d_autotune_stiffness(long *Mesh_pointer, int reps, float *ms_per_variant, int *best_variant);
+
+/* ------------------------------------------------------------------------
+ * Inter-slice assembly of accel through the MPI interface buffers
+ * (assemble_MPI_vector_cuda.cu; called from
+ * compute_forces_viscoelastic_calling_routine.F90:140-160,286-310 and
+ * assemble_MPI_vector.f90:790-880).  Buffers are (NDIM, max_nibool_interfaces_ext_mesh,
+ * num_interfaces_ext_mesh); the interface lists come from prepare_constants_device. */
+/* assemble_MPI_vector_cuda.cu:42 — pack accel (or b_accel) and copy to the host */
+void transfer_boun_accel_from_device_(long *Mesh_pointer, realw *send_accel_buffer,
+                                      const int *FORWARD_OR_ADJOINT);
+/* assemble_MPI_vector_cuda.cu:120 — pack accel and start the copy to pinned memory */
+void transfer_boundary_from_device_a_(long *Mesh_pointer, const int *nspec_outer_elastic);
+/* assemble_MPI_vector_cuda.cu:449 — wait for that copy, hand the buffer to MPI (iphase 2) */
+void sync_copy_from_device_(long *Mesh_pointer, int *iphase, realw *send_buffer);
+/* assemble_MPI_vector_cuda.cu:174 — start the upload of the received buffer */
+void transfer_boundary_to_device_a_(long *Mesh_pointer, realw *buffer_recv_vector_ext_mesh,
+                                    const int *num_interfaces_ext_mesh,
+                                    const int *max_nibool_interfaces_ext_mesh);
+/* assemble_MPI_vector_cuda.cu:205 — upload the received buffer and add it into accel */
+void transfer_asmbl_accel_to_device_(long *Mesh_pointer, realw *buffer_recv_vector_ext_mesh,
+                                     const int *num_interfaces_ext_mesh,
+                                     const int *max_nibool_interfaces_ext_mesh,
+                                     const int *nibool_interfaces_ext_mesh,
+                                     const int *ibool_interfaces_ext_mesh, const int *FORWARD_OR_ADJOINT);
+/* assemble_MPI_vector_cuda.cu:305 — add the buffer uploaded by transfer_boundary_to_device_a */
+void transfer_sync_accel_to_device_(long *Mesh_pointer, realw *buffer_recv_vector_ext_mesh,
+                                    const int *num_interfaces_ext_mesh,
+                                    const int *max_nibool_interfaces_ext_mesh,
+                                    const int *nibool_interfaces_ext_mesh,
+                                    const int *ibool_interfaces_ext_mesh, const int *FORWARD_OR_ADJOINT);
+
+/* ------------------------------------------------------------------------
+ * Checkpointed discrete-adjoint gradient of a waveform misfit (elastic, no
+ * attenuation).  Replaces the reference's SIMULATION_TYPE=3 pairing of an
+ * adjoint run with a backward reconstruction (iterate_time.F90:219-330,
+ * compute_kernels.f90:67-226) by forward recomputation from HBM checkpoints
+ * (the scheme of iterate_time_undoatt.F90:29-632).  The gradient is the exact
+ * derivative of the discrete misfit J(seismograms) with respect to rho, kappa
+ * and mu at every GLL point, accumulated in FP64.  No reference counterpart
+ * as a single call; the kernel formulas are compute_kernels.f90:151-186.
+ *
+ * Order: sf3d_gradient_setup -> sf3d_gradient_forward (from rest, records the
+ * displacement seismograms, which needs nlength_seismogram >= nstep) -> the
+ * caller forms dJ/d(seismogram) -> sf3d_gradient_set_residual ->
+ * sf3d_gradient_backward -> sf3d_gradient_get.  The backward pass recomputes
+ * the forward field, so the forward wavefield arrays hold an intermediate
+ * state afterwards. */
+/* Allocate checkpoints every checkpoint_every steps plus one segment of
+ * recomputed fields; *device_bytes receives the HBM footprint. */
+int sf3d_gradient_setup(long *Mesh_pointer, int nstep, int checkpoint_every, double *device_bytes);
+/* Forward run of nstep steps from rest with checkpoints (stf from sf3d_set_stf_table). */
+int sf3d_gradient_forward(long *Mesh_pointer, realw deltat);
+/* dJ/d(seismogram sample), layout (3, nrec_local, nstep) like seismograms_d. */
+int sf3d_gradient_set_residual(long *Mesh_pointer, const realw *residual);
+/* Reverse sweep: recompute each segment, apply the transposed steps, accumulate. */
+int sf3d_gradient_backward(long *Mesh_pointer, realw deltat);
+/* dJ/drho, dJ/dkappa, dJ/dmu per GLL point, layout (5,5,5,NSPEC); any may be NULL. */
+int sf3d_gradient_get(long *Mesh_pointer, double *g_rho, double *g_kappa, double *g_mu);
+/* Free the gradient buffers (also freed by prepare_cleanup_device). */
+int sf3d_gradient_release(long *Mesh_pointer);
 
 /* Synchronise the compute stream and report the first stored status. */
 int sf3d_synchronize(long *Mesh_pointer);

@@ -68,6 +68,21 @@ def load() -> ctypes.CDLL:
     L.sf3d_get_seismograms.argtypes = [P, P]
     L.sf3d_last_timing.restype = ctypes.c_int
     L.sf3d_last_timing.argtypes = [P, P, P, P, P]
+    L.sf3d_set_stiffness_variant.restype = ctypes.c_int
+    L.sf3d_set_stiffness_variant.argtypes = [P, ctypes.c_int]
+    L.sf3d_autotune_stiffness.restype = ctypes.c_int
+    L.sf3d_autotune_stiffness.argtypes = [P, ctypes.c_int, P, P]
+    for name in ("sf3d_gradient_forward", "sf3d_gradient_backward"):
+        getattr(L, name).restype = ctypes.c_int
+        getattr(L, name).argtypes = [P, ctypes.c_float]
+    L.sf3d_gradient_setup.restype = ctypes.c_int
+    L.sf3d_gradient_setup.argtypes = [P, ctypes.c_int, ctypes.c_int, P]
+    L.sf3d_gradient_set_residual.restype = ctypes.c_int
+    L.sf3d_gradient_set_residual.argtypes = [P, P]
+    L.sf3d_gradient_get.restype = ctypes.c_int
+    L.sf3d_gradient_get.argtypes = [P, P, P, P]
+    L.sf3d_gradient_release.restype = ctypes.c_int
+    L.sf3d_gradient_release.argtypes = [P]
     L.sf3d_synchronize.restype = ctypes.c_int
     L.sf3d_synchronize.argtypes = [P]
     L.sf3d_device_ptr.restype = P

@@ -17,9 +17,13 @@ A configuration is a plain dict (the schema read by :mod:`specfem3d_gb300.meshge
 The named workloads follow the benchmark definitions of the project:
 ``refex``  the reference's example homogeneous_halfspace_HEX8_elastic_absorbing_Stacey_5sides
            (36x36x16 hexes over 134x134x60 km, DT 0.05, CMT with Heaviside stf);
-``cfg0``   homogeneous block 10x10x5 km, 24x24x12 hexes, Ricker 2 Hz CMT, 25 receivers;
-``cfg1``   layered viscoelastic 20x20x10 km, 128x128x64 hexes (~67.6 M points), 400 receivers;
-``cfg3``   64x64x32 hexes of the cfg1 domain without attenuation, 32 CMT shots.
+``homogeneous_block``     homogeneous elastic block 10x10x5 km, 24x24x12 hexes, Ricker 2 Hz
+                          CMT, 25 receivers (the CPU-runnable plain forward);
+``layered_viscoelastic``  three-layer viscoelastic block 20x20x10 km, 128x128x64 hexes
+                          (~67.6 M points), N_SLS = 3, 400 receivers;
+``coupled_fluid_solid``   96x96x48 hexes, top sixth water over a perturbed elastic solid,
+                          pressure source, 256 hydrophones;
+``batched_shots``         64x64x32 hexes of the layered domain without attenuation, 32 CMT shots.
 """
 from __future__ import annotations
 
@@ -126,7 +130,7 @@ def refex(nstep: int = 5000) -> dict:
     return finish(cfg)
 
 
-def cfg0(nstep: int = 2000, seed: int = 2024) -> dict:
+def homogeneous_block(nstep: int = 2000, seed: int = 2024) -> dict:
     rng = np.random.default_rng(seed)
     g = np.linspace(1000.0, 9000.0, 5)
     cfg = dict(nx=24, ny=24, x0=0.0, x1=10000.0, y0=0.0, y1=10000.0,
@@ -138,7 +142,7 @@ def cfg0(nstep: int = 2000, seed: int = 2024) -> dict:
     return finish(cfg)
 
 
-def cfg1(nstep: int = 4000, seed: int = 2025, nx: int = 128, ny: int = 128, counts=(13, 26, 25)) -> dict:
+def layered_viscoelastic(nstep: int = 4000, seed: int = 2025, nx: int = 128, ny: int = 128, counts=(13, 26, 25)) -> dict:
     """Layered viscoelastic block; conforming vertical counts 13/26/25 (top-down)
     make every element a non-cube box, i.e. the irregular-element path."""
     rng = np.random.default_rng(seed)
@@ -175,8 +179,8 @@ def _cfl_dt_by_rows(cfg, lay_rows):
 
 
 def small_layered(nx=6, ny=5, counts=(2, 2, 3), nstep=200, attenuation=True, seed=7) -> dict:
-    """Small irregular (non-cube) layered block for parity tests (cfg1 physics)."""
-    cfg = cfg1(nstep=nstep, seed=seed, nx=nx, ny=ny, counts=counts)
+    """Small irregular (non-cube) layered block for parity tests (layered_viscoelastic physics)."""
+    cfg = layered_viscoelastic(nstep=nstep, seed=seed, nx=nx, ny=ny, counts=counts)
     cfg["x1"] = 20000.0 * nx / 128
     cfg["y1"] = 20000.0 * ny / 128
     z1 = -2000.0 * counts[0] / 13
@@ -194,7 +198,7 @@ def small_layered(nx=6, ny=5, counts=(2, 2, 3), nstep=200, attenuation=True, see
     return finish(cfg)
 
 
-def cfg3(nstep: int = 3000, nshots: int = 32, seed: int = 2026) -> dict:
+def batched_shots(nstep: int = 3000, nshots: int = 32, seed: int = 2026) -> dict:
     rng = np.random.default_rng(seed)
     zlev = list(np.linspace(-10000.0, 0.0, 33))
     g = np.linspace(1000.0, 19000.0, 5)
@@ -204,12 +208,52 @@ def cfg3(nstep: int = 3000, nshots: int = 32, seed: int = 2026) -> dict:
                           z=-float(rng.uniform(2000, 8000)), M=random_moment_tensor(rng), stf="ricker", f0=2.0))
     cfg = dict(nx=64, ny=64, x0=0.0, x1=20000.0, y0=0.0, y1=20000.0, zlev=zlev, elem_layer=None,
                layers=[dict(rho=2400.0, vp=3000.0, vs=1700.0)], dt=None, nstep=nstep,
+               perturbation=dict(corr_len=1000.0, seed=2027),
                sources=shots[:1], shots=shots,
                receivers=[(float(x), float(y), 0.0) for y in g for x in g], vmax_factor=1.05)
-    return finish(cfg)
+    cfg = finish(cfg)
+    # CFL with the +-5 % perturbation bound on vp
+    cfg["dt"] = significant_dt(COURANT_SUGGESTED * GLL_MIN_SPACING * (20000.0 / 64) / (3000.0 * 1.05))
+    return cfg
 
 
-def cfg2(nstep: int = 3000, nx: int = 96, ny: int = 96, nz: int = 48, fluid_layers: int = 8, seed: int = 2027) -> dict:
+def adjoint_gradient(nstep: int = 3000, nshots: int = 8, checkpoint_every: int = 200) -> dict:
+    """Misfit-gradient workload: the batched-shots mesh and background model with
+    its first ``nshots`` shots; observed data come from the true model, the
+    background with a Gaussian blob of +3 % vs (1.5 km radius) at the block
+    centre, 5 km deep."""
+    cfg = batched_shots(nstep=nstep, nshots=32)
+    cfg["shots"] = cfg["shots"][:nshots]
+    cfg["sources"] = cfg["shots"][:1]
+    cfg["blob"] = dict(center=(10000.0, 10000.0, -5000.0), radius=1500.0, dlnvs=0.03)
+    cfg["checkpoint_every"] = checkpoint_every
+    return cfg
+
+
+def small_adjoint(nstep: int = 600, nshots: int = 2, n: int = 12, seed: int = 31) -> dict:
+    """Scaled-down misfit-gradient workload for tests: n x n x n/2 elements of the
+    batched-shots element size (312.5 m), same background physics and blob
+    (radius scaled to the block), ``nshots`` Ricker 2 Hz CMT shots."""
+    rng = np.random.default_rng(seed)
+    h = 20000.0 / 64
+    nz = max(2, n // 2)
+    L, D = n * h, nz * h
+    shots = [dict(type="cmt", x=float(rng.uniform(0.25, 0.75) * L), y=float(rng.uniform(0.25, 0.75) * L),
+                  z=-float(rng.uniform(0.3, 0.7) * D), M=random_moment_tensor(rng), stf="ricker", f0=2.0)
+             for _ in range(nshots)]
+    g = np.linspace(0.1 * L, 0.9 * L, 5)
+    cfg = dict(nx=n, ny=n, x0=0.0, x1=L, y0=0.0, y1=L, zlev=[float(-D + q * h) for q in range(nz + 1)],
+               elem_layer=None, layers=[dict(rho=2400.0, vp=3000.0, vs=1700.0)], dt=None, nstep=nstep,
+               perturbation=dict(corr_len=1000.0, seed=2027), sources=shots[:1], shots=shots,
+               receivers=[(float(x), float(y), 0.0) for y in g for x in g])
+    cfg = finish(cfg)
+    cfg["dt"] = significant_dt(COURANT_SUGGESTED * GLL_MIN_SPACING * h / (3000.0 * 1.05))
+    cfg["blob"] = dict(center=(0.5 * L, 0.5 * L, -0.5 * D), radius=0.15 * L, dlnvs=0.03)
+    cfg["checkpoint_every"] = max(1, nstep // 7)
+    return cfg
+
+
+def coupled_fluid_solid(nstep: int = 3000, nx: int = 96, ny: int = 96, nz: int = 48, fluid_layers: int = 8, seed: int = 2027) -> dict:
     """Coupled fluid/solid block: the top sixth of the depth is water
     (vp 1500, rho 1020), the rest a solid of (3000, 1700, 2400) carrying a seeded
     +-5 % Gaussian-correlated perturbation (1 km correlation length); pressure
@@ -241,8 +285,8 @@ def cfg2(nstep: int = 3000, nx: int = 96, ny: int = 96, nz: int = 48, fluid_laye
 
 
 def small_coupled(nx: int = 5, ny: int = 4, nz: int = 6, fluid_layers: int = 2, nstep: int = 300) -> dict:
-    """Small coupled block with the cfg2 physics for parity tests."""
-    cfg = cfg2(nstep=nstep, nx=nx, ny=ny, nz=nz, fluid_layers=fluid_layers)
+    """Small coupled block with the coupled_fluid_solid physics for parity tests."""
+    cfg = coupled_fluid_solid(nstep=nstep, nx=nx, ny=ny, nz=nz, fluid_layers=fluid_layers)
     h = 20000.0 / 96
     cfg["x1"], cfg["y1"] = nx * h, ny * h
     cfg["zlev"] = [float(-nz * h + q * h) for q in range(nz + 1)]

@@ -277,6 +277,11 @@ void prepare_fields_acoustic_device_(long* Mesh_pointer, realw* rmass_acoustic, 
       ph[q] = phase_ispec_inner_acoustic[q] - 1;
       if (ph[q] >= nspec) ok = set_error(SF3D_ERR_ARG, "phase_ispec_inner_acoustic out of range");
     }
+    for (int c = 0; c < 2; ++c) {
+      int n = 0;
+      while (n < mp->num_phase_ispec_ac && ph[(size_t)c * mp->num_phase_ispec_ac + n] >= 0) ++n;
+      mp->phase_valid_ac[c] = n;
+    }
     ok = ok && alloc_zero((void**)&mp->d_phase_ispec_ac, sizeof(int) * ph.size()) &&
          copy_sync(mp->d_phase_ispec_ac, ph.data(), sizeof(int) * ph.size(), cudaMemcpyHostToDevice, s);
   }
@@ -306,7 +311,11 @@ void compute_forces_acoustic_cuda_(long* Mesh_pointer, int* iphase, int* nspec_o
   mp->nspec_outer_ac = *nspec_outer_acoustic;
   mp->nspec_inner_ac = *nspec_inner_acoustic;
   const int nel = *iphase == 1 ? mp->nspec_outer_ac : mp->nspec_inner_ac;
-  if (nel < 0 || nel > mp->num_phase_ispec_ac) { set_error(SF3D_ERR_ARG, "nspec_outer/inner_acoustic too large"); return; }
+  if (*iphase != 1 && *iphase != 2) { set_error(SF3D_ERR_ARG, "iphase must be 1 or 2"); return; }
+  if (nel < 0 || nel > mp->phase_valid_ac[*iphase - 1]) {
+    set_error(SF3D_ERR_ARG, "nspec_outer/inner_acoustic exceeds the phase element lists");
+    return;
+  }
   if (nel == 0) return;
   const int* ph = mp->d_phase_ispec_ac + (long)(*iphase - 1) * mp->num_phase_ispec_ac;
   acoustic_stiffness_kernel<<<nel, NGLL3_PAD, 0, mp->stream>>>(

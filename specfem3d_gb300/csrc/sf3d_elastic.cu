@@ -21,8 +21,8 @@ namespace sf3d {
 
 namespace {
 
-template <bool ATT, bool STRAIN>
-__global__ void __launch_bounds__(NGLL3_PAD, 4) stiffness_kernel(const StiffnessArgs a) {
+template <bool ATT, bool STRAIN, int MINB>
+__global__ void __launch_bounds__(NGLL3_PAD, MINB) stiffness_kernel(const StiffnessArgs a) {
   __shared__ float s_gll[NGLL3];
   __shared__ float s_u[3][NGLL3_PAD];
   __shared__ float s_v[ATT ? 3 : 1][NGLL3_PAD];
@@ -252,17 +252,30 @@ __global__ void __launch_bounds__(NGLL3_PAD, 4) stiffness_kernel(const Stiffness
   }
 }
 
-}  // namespace
-
-void launch_stiffness(const StiffnessArgs& a, bool att, bool store_strain, cudaStream_t s) {
-  if (a.nelem <= 0) return;
+template <int MINB>
+void launch_minb(const StiffnessArgs& a, bool att, bool store_strain, cudaStream_t s) {
   dim3 grid(a.nelem), block(NGLL3_PAD);
   if (att)
-    stiffness_kernel<true, true><<<grid, block, 0, s>>>(a);
+    stiffness_kernel<true, true, MINB><<<grid, block, 0, s>>>(a);
   else if (store_strain)
-    stiffness_kernel<false, true><<<grid, block, 0, s>>>(a);
+    stiffness_kernel<false, true, MINB><<<grid, block, 0, s>>>(a);
   else
-    stiffness_kernel<false, false><<<grid, block, 0, s>>>(a);
+    stiffness_kernel<false, false, MINB><<<grid, block, 0, s>>>(a);
+}
+
+}  // namespace
+
+// blocks_per_sm: the register budget the kernel is compiled for (4..7 CTAs of
+// 128 threads per SM; more CTAs keep more elements' loads in flight, fewer
+// let the compiler keep every load of an element in registers).
+void launch_stiffness(const StiffnessArgs& a, bool att, bool store_strain, cudaStream_t s, int blocks_per_sm) {
+  if (a.nelem <= 0) return;
+  switch (blocks_per_sm) {
+    case 5: launch_minb<5>(a, att, store_strain, s); break;
+    case 6: launch_minb<6>(a, att, store_strain, s); break;
+    case 7: launch_minb<7>(a, att, store_strain, s); break;
+    default: launch_minb<4>(a, att, store_strain, s); break;
+  }
 }
 
 }  // namespace sf3d

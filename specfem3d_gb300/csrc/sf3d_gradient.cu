@@ -1,0 +1,499 @@
+// Checkpointed discrete-adjoint gradient of a waveform misfit (sm_103a).
+//
+// The reference computes sensitivity kernels (SIMULATION_TYPE = 3) by running
+// the adjoint wavefield forward in reversed time next to a backward
+// reconstruction of the forward field from stored Stacey boundary values
+// (iterate_time.F90:219-330, compute_forces_viscoelastic_calling_routine.F90:443-686,
+// compute_kernels.f90:67-226), or, with UNDO_ATTENUATION_AND_OR_PML, by
+// recomputing the forward field from snapshots (iterate_time_undoatt.F90:29-632).
+// This module follows the second route, entirely in HBM:
+//
+//   forward  : the fused elastic step of sf3d_iterate_time from rest; the raw
+//              step state (displ, veloc, accel before the mass matrix) is
+//              copied to a checkpoint slot every `every` steps;
+//   backward : for each segment, last to first, the forward steps of the
+//              segment are recomputed from its checkpoint, storing the
+//              displacement and the force of every step; then the exact
+//              transpose of each Newmark step is applied in reverse order.
+//
+// With the explicit Newmark step (n -> n+1)
+//     ut = u + dt v + dt^2/2 a,   vt = v + dt/2 a,
+//     a' = M^-1 (f - K ut - B vt),   v' = vt + dt/2 a',   u' = ut,
+// (K: stiffness, B: Stacey damping, M: mass incl. its Stacey term, all
+// symmetric) and misfit J = sum_n r_n(u_n), the transpose step is
+//     uh' += dJ/du'                         (receiver residual, transposed interpolation)
+//     p    = -M^-1 (ah' + dt/2 vh')
+//     uth  = uh' + K p,   vth = vh' + B p
+//     uh   = uth,  vh = dt uth + vth,  ah = dt^2/2 uth + dt/2 vth
+// and the gradient contributions of the step are
+//     dJ/dkappa_(e,p) += w_p J_p tr eps(p) tr eps(ut)
+//     dJ/dmu_(e,p)    += w_p J_p 2 dev eps(p) : dev eps(ut)
+//     dJ/drho_(e,p)   += w_p J_p p . a'           (mass-matrix dependence)
+// accumulated in FP64 per GLL point.  K p and B p reuse the forward stiffness
+// and Stacey kernels (both operators are symmetric).  These are the reference's
+// kernel formulas (compute_kernels.f90:151-186: kappa from the strain traces,
+// mu from the deviatoric strains, rho from the acceleration-displacement
+// product) evaluated on the discrete adjoint field, so the gradient is the
+// exact derivative of the discrete misfit for model perturbations that leave
+// the Stacey faces unchanged.
+#include <math.h>
+#include <string.h>
+
+#include <vector>
+
+#include "sf3d_internal.h"
+
+namespace sf3d {
+namespace {
+
+inline unsigned nblk(long n, int b) { return (unsigned)((n + b - 1) / b); }
+
+// uh(iglob) += sum over receivers of h_xi h_eta h_gamma nu^T residual(:, r, slot)
+__global__ void adj_residual_kernel(int nrec, const int* __restrict__ ispec_rec, const float* __restrict__ hx,
+                                    const float* __restrict__ he, const float* __restrict__ hg,
+                                    const float* __restrict__ nu, const int* __restrict__ ibool,
+                                    const float* __restrict__ residual, int slot, float* __restrict__ uh) {
+  const int r = blockIdx.x, t = threadIdx.x;
+  if (r >= nrec || t >= NGLL3) return;
+  const int e = ispec_rec[r];
+  const int k = t / NGLL2, j = (t / NGLLX) % NGLLX, i = t % NGLLX;
+  const float h = hx[5 * r + i] * he[5 * r + j] * hg[5 * r + k];
+  const float* res = residual + 3L * (r + (long)nrec * slot);
+  const float* n = nu + 9 * r;  // nu(3,3) column-major: seismogram = nu u
+  const float w0 = n[0] * res[0] + n[1] * res[1] + n[2] * res[2];
+  const float w1 = n[3] * res[0] + n[4] * res[1] + n[5] * res[2];
+  const float w2 = n[6] * res[0] + n[7] * res[1] + n[8] * res[2];
+  const int g = ibool[(long)e * NGLL3_PAD + t];
+  atomicAdd(uh + 3L * g, h * w0);
+  atomicAdd(uh + 3L * g + 1, h * w1);
+  atomicAdd(uh + 3L * g + 2, h * w2);
+}
+
+// p = -M^-1 (ah + dt/2 vh); clears the K p and B p accumulators
+__global__ void adj_p_kernel(const float* __restrict__ vh, const float* __restrict__ ah,
+                             const float* __restrict__ rmx, const float* __restrict__ rmy,
+                             const float* __restrict__ rmz, long nglob, float dt2, float* __restrict__ p,
+                             float* __restrict__ kp, float* __restrict__ bp) {
+  const long i = (long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= 3 * nglob) return;
+  const long g = i / 3;
+  const int c = (int)(i - 3 * g);
+  const float rm = c == 0 ? __ldg(rmx + g) : (c == 1 ? __ldg(rmy + g) : __ldg(rmz + g));
+  p[i] = -rm * (ah[i] + dt2 * vh[i]);
+  kp[i] = 0.f;
+  bp[i] = 0.f;
+}
+
+// kp = -K p and bp = -B p: uth = uh - kp, vth = vh - bp; back through the predictor
+__global__ void adj_update_kernel(float* __restrict__ uh, float* __restrict__ vh, float* __restrict__ ah,
+                                  const float* __restrict__ kp, const float* __restrict__ bp, long n, float dt,
+                                  float dt2, float dtsq2) {
+  const long i = (long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  const float ut = uh[i] - kp[i];
+  const float vt = vh[i] - bp[i];
+  uh[i] = ut;
+  vh[i] = dt * ut + vt;
+  ah[i] = dtsq2 * ut + dt2 * vt;
+}
+
+struct GradArgs {
+  int nelem;
+  const int* phase;
+  const int* ibool;
+  const int* irregular;
+  const float* m[9];
+  const float* gll;
+  float xix_regular, jacobian_regular;
+  float w[NGLLX];
+  float uscale;        // power of two bringing the forward field near 1
+  const float* p;      // adjoint field p_n
+  const float* u;      // forward displacement after step n
+  const float* araw;   // forward force after step n (before the mass matrix)
+  const float* rmx;
+  const float* rmy;
+  const float* rmz;
+  double* g_rho;
+  double* g_kappa;
+  double* g_mu;
+};
+
+// Gradient of the 3x3 displacement derivative of a field staged in shared memory.
+__device__ __forceinline__ void local_grad(const float (*s)[NGLL3_PAD], const float* hp, int i, int j, int k,
+                                           float t[3][3]) {
+#pragma unroll
+  for (int c = 0; c < 3; ++c) t[c][0] = t[c][1] = t[c][2] = 0.f;
+#pragma unroll
+  for (int l = 0; l < NGLLX; ++l) {
+    const float h1 = hp[i + NGLLX * l], h2 = hp[j + NGLLX * l], h3 = hp[k + NGLLX * l];
+    const int p1 = l + NGLLX * j + NGLL2 * k, p2 = i + NGLLX * l + NGLL2 * k, p3 = i + NGLLX * j + NGLL2 * l;
+#pragma unroll
+    for (int c = 0; c < 3; ++c) {
+      t[c][0] = fmaf(s[c][p1], h1, t[c][0]);
+      t[c][1] = fmaf(s[c][p2], h2, t[c][1]);
+      t[c][2] = fmaf(s[c][p3], h3, t[c][2]);
+    }
+  }
+}
+
+// One CTA per element, thread = GLL point: strains of p and u, FP64 accumulation.
+__global__ void __launch_bounds__(NGLL3_PAD) grad_accum_kernel(const GradArgs a) {
+  __shared__ float s_h[NGLL2];
+  __shared__ float s_p[3][NGLL3_PAD];
+  __shared__ float s_u[3][NGLL3_PAD];
+  const int t = threadIdx.x;
+  const int e = a.phase ? __ldg(a.phase + blockIdx.x) : (int)blockIdx.x;
+  const bool active = t < NGLL3;
+  const int k = t / NGLL2, j = (t / NGLLX) % NGLLX, i = t % NGLLX;
+  const long eo = (long)e * NGLL3_PAD + t;
+  float pa = 0.f;
+  if (t < NGLL2) s_h[t] = __ldg(a.gll + t);
+  if (active) {
+    const int g = __ldg(a.ibool + eo);
+#pragma unroll
+    for (int c = 0; c < 3; ++c) {
+      s_p[c][t] = a.p[3L * g + c];
+      s_u[c][t] = a.u[3L * g + c] * a.uscale;
+    }
+    pa = s_p[0][t] * (a.araw[3L * g] * a.uscale * __ldg(a.rmx + g)) +
+         s_p[1][t] * (a.araw[3L * g + 1] * a.uscale * __ldg(a.rmy + g)) +
+         s_p[2][t] * (a.araw[3L * g + 2] * a.uscale * __ldg(a.rmz + g));
+  }
+  __syncthreads();
+  if (!active) return;
+  float tp[3][3], tu[3][3];
+  local_grad(s_p, s_h, i, j, k, tp);
+  local_grad(s_u, s_h, i, j, k, tu);
+  const int ir = __ldg(a.irregular + e);
+  // d[c][x]: derivative of component c along x, y, z
+  float dp[3][3], du[3][3], jac;
+  if (ir >= 0) {
+    float m[9];
+    const long mo = (long)ir * NGLL3_PAD + t;
+#pragma unroll
+    for (int q = 0; q < 9; ++q) m[q] = __ldg(a.m[q] + mo);
+    // m = xix xiy xiz etax etay etaz gammax gammay gammaz
+#pragma unroll
+    for (int c = 0; c < 3; ++c) {
+#pragma unroll
+      for (int x = 0; x < 3; ++x) {
+        dp[c][x] = m[x] * tp[c][0] + m[3 + x] * tp[c][1] + m[6 + x] * tp[c][2];
+        du[c][x] = m[x] * tu[c][0] + m[3 + x] * tu[c][1] + m[6 + x] * tu[c][2];
+      }
+    }
+    jac = 1.f / (m[0] * (m[4] * m[8] - m[5] * m[7]) - m[1] * (m[3] * m[8] - m[5] * m[6]) +
+                 m[2] * (m[3] * m[7] - m[4] * m[6]));
+  } else {
+#pragma unroll
+    for (int c = 0; c < 3; ++c)
+#pragma unroll
+      for (int x = 0; x < 3; ++x) {
+        dp[c][x] = a.xix_regular * tp[c][x];
+        du[c][x] = a.xix_regular * tu[c][x];
+      }
+    jac = a.jacobian_regular;
+  }
+  const float trp = dp[0][0] + dp[1][1] + dp[2][2];
+  const float tru = du[0][0] + du[1][1] + du[2][2];
+  float dd = 0.f;
+#pragma unroll
+  for (int x = 0; x < 3; ++x) dd += (dp[x][x] - trp * (1.f / 3.f)) * (du[x][x] - tru * (1.f / 3.f));
+  const float exy_p = 0.5f * (dp[0][1] + dp[1][0]), exz_p = 0.5f * (dp[0][2] + dp[2][0]),
+              eyz_p = 0.5f * (dp[1][2] + dp[2][1]);
+  const float exy_u = 0.5f * (du[0][1] + du[1][0]), exz_u = 0.5f * (du[0][2] + du[2][0]),
+              eyz_u = 0.5f * (du[1][2] + du[2][1]);
+  dd += 2.f * (exy_p * exy_u + exz_p * exz_u + eyz_p * eyz_u);
+  const double wj = (double)(a.w[i] * a.w[j] * a.w[k]) * (double)jac;
+  a.g_kappa[eo] += wj * (double)trp * (double)tru;
+  a.g_mu[eo] += wj * 2.0 * (double)dd;
+  a.g_rho[eo] += wj * (double)pa;
+}
+
+bool alloc_f(float** d, size_t n) { return alloc_zero((void**)d, sizeof(float) * n); }
+
+}  // namespace
+
+void free_grad(Mesh* mp) {
+  GradState* G = mp->grad;
+  if (!G) return;
+  cudaFree(G->ckpt); cudaFree(G->seg_u); cudaFree(G->seg_a);
+  cudaFree(G->adj_u); cudaFree(G->adj_v); cudaFree(G->adj_a);
+  cudaFree(G->p); cudaFree(G->kp); cudaFree(G->bp); cudaFree(G->residual);
+  cudaFree(G->g_rho); cudaFree(G->g_kappa); cudaFree(G->g_mu);
+  delete G;
+  mp->grad = nullptr;
+}
+
+namespace {
+
+bool grad_ready(Mesh* mp) {
+  if (!mp->grad) return set_error(SF3D_ERR_STATE, "sf3d_gradient_setup not called");
+  if (mp->num_phase_ispec <= 0) return set_error(SF3D_ERR_STATE, "phase element lists not prepared");
+  default_phase_counts(mp);
+  return true;
+}
+
+void save_state(Mesh* mp, float* dst, cudaStream_t s) {
+  const size_t n3 = 3ull * mp->nglob;
+  cudaMemcpyAsync(dst, mp->f.displ, sizeof(float) * n3, cudaMemcpyDeviceToDevice, s);
+  cudaMemcpyAsync(dst + n3, mp->f.veloc, sizeof(float) * n3, cudaMemcpyDeviceToDevice, s);
+  cudaMemcpyAsync(dst + 2 * n3, mp->f.accel, sizeof(float) * n3, cudaMemcpyDeviceToDevice, s);
+}
+
+void load_state(Mesh* mp, const float* src, cudaStream_t s) {
+  const size_t n3 = 3ull * mp->nglob;
+  cudaMemcpyAsync(mp->f.displ, src, sizeof(float) * n3, cudaMemcpyDeviceToDevice, s);
+  cudaMemcpyAsync(mp->f.veloc, src + n3, sizeof(float) * n3, cudaMemcpyDeviceToDevice, s);
+  cudaMemcpyAsync(mp->f.accel, src + 2 * n3, sizeof(float) * n3, cudaMemcpyDeviceToDevice, s);
+}
+
+void zero_state(Mesh* mp, cudaStream_t s) {
+  const size_t n3 = 3ull * mp->nglob;
+  cudaMemsetAsync(mp->f.displ, 0, sizeof(float) * n3, s);
+  cudaMemsetAsync(mp->f.veloc, 0, sizeof(float) * n3, s);
+  cudaMemsetAsync(mp->f.accel, 0, sizeof(float) * n3, s);
+}
+
+// One transposed Newmark step n (0-based): u = displacement after step n,
+// araw = force after step n.
+void adjoint_step(Mesh* mp, int n, const float* u, const float* araw, float dt, float dt2, float dtsq2) {
+  GradState* G = mp->grad;
+  cudaStream_t s = mp->stream;
+  const long n3 = 3L * mp->nglob;
+  if (mp->nrec_local > 0)
+    adj_residual_kernel<<<mp->nrec_local, NGLL3_PAD, 0, s>>>(mp->nrec_local, mp->d_ispec_rec, mp->d_hxir,
+                                                             mp->d_hetar, mp->d_hgammar, mp->d_nu_rec, mp->d_ibool,
+                                                             G->residual, n, G->adj_u);
+  adj_p_kernel<<<nblk(n3, 256), 256, 0, s>>>(G->adj_v, G->adj_a, mp->d_rmassx, mp->d_rmassy, mp->d_rmassz,
+                                             mp->nglob, dt2, G->p, G->kp, G->bp);
+  launch_stacey(mp, G->p, G->bp, s);
+  Fields tmp;
+  tmp.displ = G->p;
+  tmp.veloc = G->p;
+  tmp.accel = G->kp;
+  for (int iphase = 1; iphase <= 2; ++iphase) {
+    StiffnessArgs a = stiffness_args(mp, tmp, iphase, dt, false, false, false);
+    if (a.nelem <= 0) continue;
+    run_stiffness(mp, a, false, false, s);
+    GradArgs ga;
+    memset(&ga, 0, sizeof(ga));
+    ga.nelem = a.nelem;
+    ga.phase = a.phase;
+    ga.ibool = mp->d_ibool;
+    ga.irregular = mp->d_irregular;
+    for (int q = 0; q < 9; ++q) ga.m[q] = mp->d_metric[q];
+    ga.gll = mp->d_gll;
+    ga.xix_regular = mp->xix_regular;
+    ga.jacobian_regular = mp->jacobian_regular;
+    for (int q = 0; q < NGLLX; ++q) ga.w[q] = G->wgll[q];
+    ga.uscale = G->u_scale;
+    ga.p = G->p;
+    ga.u = u;
+    ga.araw = araw;
+    ga.rmx = mp->d_rmassx;
+    ga.rmy = mp->d_rmassy;
+    ga.rmz = mp->d_rmassz;
+    ga.g_rho = G->g_rho;
+    ga.g_kappa = G->g_kappa;
+    ga.g_mu = G->g_mu;
+    grad_accum_kernel<<<a.nelem, NGLL3_PAD, 0, s>>>(ga);
+  }
+  adj_update_kernel<<<nblk(n3, 256), 256, 0, s>>>(G->adj_u, G->adj_v, G->adj_a, G->kp, G->bp, n3, dt, dt2, dtsq2);
+}
+
+}  // namespace
+}  // namespace sf3d
+
+using namespace sf3d;
+
+extern "C" {
+
+int sf3d_gradient_setup(long* Mesh_pointer, int nstep, int checkpoint_every, double* device_bytes) {
+  Mesh* mp = get_mesh(Mesh_pointer);
+  if (!mp) return SF3D_ERR_STATE;
+  if (!mp->f.displ) { set_error(SF3D_ERR_STATE, "prepare_fields_elastic_device not called"); return SF3D_ERR_STATE; }
+  if (mp->attenuation) {
+    set_error(SF3D_ERR_ARG, "sf3d_gradient: attenuation is not supported (elastic misfit gradient only)");
+    return SF3D_ERR_ARG;
+  }
+  if (mp->has_acoustic) {
+    set_error(SF3D_ERR_ARG, "sf3d_gradient: acoustic elements are not supported");
+    return SF3D_ERR_ARG;
+  }
+  if (nstep < 1 || checkpoint_every < 1) { set_error(SF3D_ERR_ARG, "sf3d_gradient: nstep and checkpoint_every must be >= 1"); return SF3D_ERR_ARG; }
+  if (mp->nrec_local > 0 && (!mp->d_seismo_d || mp->nlength_seismogram < nstep)) {
+    set_error(SF3D_ERR_ARG, "sf3d_gradient: the displacement seismogram buffer must hold nstep samples");
+    return SF3D_ERR_ARG;
+  }
+  if (mp->nsources > 0 && (!mp->d_stf_table || mp->stf_nstep < nstep)) {
+    set_error(SF3D_ERR_STATE, "sf3d_set_stf_table must cover nstep");
+    return SF3D_ERR_STATE;
+  }
+  free_grad(mp);
+  GradState* G = new GradState();
+  mp->grad = G;
+  G->nstep = nstep;
+  G->every = checkpoint_every < nstep ? checkpoint_every : nstep;
+  const int nseg = (nstep + G->every - 1) / G->every;
+  G->nckpt = nseg - 1;  // segment 0 starts from rest
+  const size_t n3 = 3ull * mp->nglob;
+  const size_t npt = (size_t)mp->nspec * NGLL3_PAD;
+  bool ok = true;
+  if (G->nckpt > 0) ok = ok && alloc_f(&G->ckpt, (size_t)G->nckpt * 3 * n3);
+  ok = ok && alloc_f(&G->seg_u, (size_t)G->every * n3) && alloc_f(&G->seg_a, (size_t)G->every * n3);
+  ok = ok && alloc_f(&G->adj_u, n3) && alloc_f(&G->adj_v, n3) && alloc_f(&G->adj_a, n3);
+  ok = ok && alloc_f(&G->p, n3) && alloc_f(&G->kp, n3) && alloc_f(&G->bp, n3);
+  ok = ok && alloc_f(&G->residual, 3ull * (mp->nrec_local > 0 ? mp->nrec_local : 1) * nstep);
+  ok = ok && alloc_zero((void**)&G->g_rho, sizeof(double) * npt) && alloc_zero((void**)&G->g_kappa, sizeof(double) * npt) &&
+       alloc_zero((void**)&G->g_mu, sizeof(double) * npt);
+  if (!ok) {
+    free_grad(mp);
+    return SF3D_ERR_CUDA;
+  }
+  for (int q = 0; q < NGLLX; ++q) G->wgll[q] = (float)sqrt((double)mp->h_wxy[q + NGLLX * q]);
+  G->bytes = sizeof(float) * ((size_t)G->nckpt * 3 * n3 + 2ull * G->every * n3 + 6 * n3 +
+                              3ull * (mp->nrec_local > 0 ? mp->nrec_local : 1) * nstep) +
+             3 * sizeof(double) * npt;
+  if (device_bytes) *device_bytes = (double)G->bytes;
+  return SF3D_OK;
+}
+
+int sf3d_gradient_forward(long* Mesh_pointer, realw deltat) {
+  Mesh* mp = get_mesh(Mesh_pointer);
+  if (!mp) return SF3D_ERR_STATE;
+  if (!grad_ready(mp)) return SF3D_ERR_STATE;
+  GradState* G = mp->grad;
+  const float dt = deltat, dt2 = deltat / 2.f, dtsq2 = deltat * deltat / 2.f;
+  cudaStream_t s = mp->stream;
+  const size_t n3 = 3ull * mp->nglob;
+  zero_state(mp, s);
+  launch_set_it(mp, 1, s);
+  SF3D_CUDA_RET(cudaMemsetAsync(mp->d_done, 0, sizeof(unsigned int), s), SF3D_ERR_CUDA);
+  SF3D_CUDA_RET(cudaEventRecord(mp->ev0, s), SF3D_ERR_CUDA);
+  int launches = 0;
+  for (int n = 0; n < G->nstep; ++n) {
+    launches += enqueue_step(mp, dt, dt2, dtsq2, n == 0, nullptr);
+    const int next = n + 1;
+    if (next % G->every == 0 && next < G->nstep) save_state(mp, G->ckpt + (size_t)(next / G->every - 1) * 3 * n3, s);
+  }
+  launch_mass_corrector(mp, dt2, s);
+  SF3D_CUDA_RET(cudaEventRecord(mp->ev1, s), SF3D_ERR_CUDA);
+  SF3D_CUDA_RET(cudaEventSynchronize(mp->ev1), SF3D_ERR_CUDA);
+  if (!cuda_ok(cudaGetLastError(), "sf3d_gradient_forward")) return SF3D_ERR_CUDA;
+  cudaEventElapsedTime(&mp->last_total_ms, mp->ev0, mp->ev1);
+  mp->last_total_launches = launches + 1;
+  if (!check_kernel_error(mp)) return SF3D_ERR_CUDA;
+  // scale of the forward field for the FP32 strain products of the gradient:
+  // the largest recorded displacement (a 1 N.m source gives ~1e-19 m)
+  G->u_scale = 1.f;
+  if (mp->nrec_local > 0) {
+    float mx = 0.f;
+    if (!device_maxabs(mp, mp->d_seismo_d, 3L * mp->nrec_local * mp->nlength_seismogram, &mx)) return SF3D_ERR_CUDA;
+    if (mx > 0.f && mx < 3.0e38f) {
+      int ex = 0;
+      frexpf(mx, &ex);
+      G->u_scale = ldexpf(1.f, -ex);
+    }
+  }
+  return sf3d_last_error(nullptr, 0);
+}
+
+int sf3d_gradient_set_residual(long* Mesh_pointer, const realw* residual) {
+  Mesh* mp = get_mesh(Mesh_pointer);
+  if (!mp) return SF3D_ERR_STATE;
+  if (!grad_ready(mp)) return SF3D_ERR_STATE;
+  if (mp->nrec_local == 0) return SF3D_OK;
+  if (!residual) { set_error(SF3D_ERR_ARG, "sf3d_gradient_set_residual: null residual"); return SF3D_ERR_ARG; }
+  // Waveform residuals of small sources can be far below 1 (1e-20 for a 1 N.m
+  // moment tensor), which would push the adjoint field and the strain products
+  // of the gradient below the FP32 normal range.  The residual is therefore
+  // scaled by a power of two that brings its maximum near 1; the gradient is
+  // linear in the residual and sf3d_gradient_get divides the scale out in FP64.
+  const size_t n = 3ull * mp->nrec_local * mp->grad->nstep;
+  float mx = 0.f;
+  for (size_t q = 0; q < n; ++q) {
+    const float a = fabsf(residual[q]);
+    if (!(a <= 3.0e38f)) { set_error(SF3D_ERR_ARG, "sf3d_gradient_set_residual: NaN or Inf in the residual"); return SF3D_ERR_ARG; }
+    mx = a > mx ? a : mx;
+  }
+  int ex = 0;
+  if (mx > 0.f) frexpf(mx, &ex);
+  const double scale = ldexp(1.0, -ex);
+  std::vector<float> tmp(n);
+  for (size_t q = 0; q < n; ++q) tmp[q] = (float)((double)residual[q] * scale);
+  mp->grad->res_scale = scale;
+  if (!copy_sync(mp->grad->residual, tmp.data(), sizeof(float) * n, cudaMemcpyHostToDevice, mp->stream))
+    return SF3D_ERR_CUDA;
+  return SF3D_OK;
+}
+
+int sf3d_gradient_backward(long* Mesh_pointer, realw deltat) {
+  Mesh* mp = get_mesh(Mesh_pointer);
+  if (!mp) return SF3D_ERR_STATE;
+  if (!grad_ready(mp)) return SF3D_ERR_STATE;
+  GradState* G = mp->grad;
+  const float dt = deltat, dt2 = deltat / 2.f, dtsq2 = deltat * deltat / 2.f;
+  cudaStream_t s = mp->stream;
+  const size_t n3 = 3ull * mp->nglob;
+  const size_t npt = (size_t)mp->nspec * NGLL3_PAD;
+  SF3D_CUDA_RET(cudaMemsetAsync(G->adj_u, 0, sizeof(float) * n3, s), SF3D_ERR_CUDA);
+  SF3D_CUDA_RET(cudaMemsetAsync(G->adj_v, 0, sizeof(float) * n3, s), SF3D_ERR_CUDA);
+  SF3D_CUDA_RET(cudaMemsetAsync(G->adj_a, 0, sizeof(float) * n3, s), SF3D_ERR_CUDA);
+  SF3D_CUDA_RET(cudaMemsetAsync(G->g_rho, 0, sizeof(double) * npt, s), SF3D_ERR_CUDA);
+  SF3D_CUDA_RET(cudaMemsetAsync(G->g_kappa, 0, sizeof(double) * npt, s), SF3D_ERR_CUDA);
+  SF3D_CUDA_RET(cudaMemsetAsync(G->g_mu, 0, sizeof(double) * npt, s), SF3D_ERR_CUDA);
+  SF3D_CUDA_RET(cudaMemsetAsync(mp->d_done, 0, sizeof(unsigned int), s), SF3D_ERR_CUDA);
+  SF3D_CUDA_RET(cudaEventRecord(mp->ev0, s), SF3D_ERR_CUDA);
+  const int nseg = G->nckpt + 1;
+  for (int j = nseg - 1; j >= 0; --j) {
+    const int n0 = j * G->every;
+    const int len = (n0 + G->every <= G->nstep) ? G->every : G->nstep - n0;
+    if (j == 0)
+      zero_state(mp, s);
+    else
+      load_state(mp, G->ckpt + (size_t)(j - 1) * 3 * n3, s);
+    launch_set_it(mp, n0 + 1, s);
+    for (int q = 0; q < len; ++q) {
+      enqueue_step(mp, dt, dt2, dtsq2, j == 0 && q == 0, nullptr);
+      cudaMemcpyAsync(G->seg_u + (size_t)q * n3, mp->f.displ, sizeof(float) * n3, cudaMemcpyDeviceToDevice, s);
+      cudaMemcpyAsync(G->seg_a + (size_t)q * n3, mp->f.accel, sizeof(float) * n3, cudaMemcpyDeviceToDevice, s);
+    }
+    for (int q = len - 1; q >= 0; --q)
+      adjoint_step(mp, n0 + q, G->seg_u + (size_t)q * n3, G->seg_a + (size_t)q * n3, dt, dt2, dtsq2);
+    if (!cuda_ok(cudaGetLastError(), "sf3d_gradient_backward")) return SF3D_ERR_CUDA;
+  }
+  SF3D_CUDA_RET(cudaEventRecord(mp->ev1, s), SF3D_ERR_CUDA);
+  SF3D_CUDA_RET(cudaEventSynchronize(mp->ev1), SF3D_ERR_CUDA);
+  if (!cuda_ok(cudaGetLastError(), "sf3d_gradient_backward")) return SF3D_ERR_CUDA;
+  cudaEventElapsedTime(&mp->last_total_ms, mp->ev0, mp->ev1);
+  if (!check_kernel_error(mp)) return SF3D_ERR_CUDA;
+  return sf3d_last_error(nullptr, 0);
+}
+
+int sf3d_gradient_get(long* Mesh_pointer, double* g_rho, double* g_kappa, double* g_mu) {
+  Mesh* mp = get_mesh(Mesh_pointer);
+  if (!mp) return SF3D_ERR_STATE;
+  if (!mp->grad) { set_error(SF3D_ERR_STATE, "sf3d_gradient_setup not called"); return SF3D_ERR_STATE; }
+  const size_t npt = (size_t)mp->nspec * NGLL3_PAD;
+  std::vector<double> tmp(npt);
+  double* outs[3] = {g_rho, g_kappa, g_mu};
+  const double* srcs[3] = {mp->grad->g_rho, mp->grad->g_kappa, mp->grad->g_mu};
+  for (int q = 0; q < 3; ++q) {
+    if (!outs[q]) continue;
+    if (!copy_sync(tmp.data(), srcs[q], sizeof(double) * npt, cudaMemcpyDeviceToHost, mp->stream)) return SF3D_ERR_CUDA;
+    const double unscale = 1.0 / (mp->grad->res_scale * (double)mp->grad->u_scale);
+    for (long e = 0; e < mp->nspec; ++e)
+      for (int p = 0; p < NGLL3; ++p) outs[q][e * NGLL3 + p] = tmp[e * NGLL3_PAD + p] * unscale;
+  }
+  return SF3D_OK;
+}
+
+int sf3d_gradient_release(long* Mesh_pointer) {
+  Mesh* mp = get_mesh(Mesh_pointer);
+  if (!mp) return SF3D_ERR_STATE;
+  cudaStreamSynchronize(mp->stream);
+  free_grad(mp);
+  return SF3D_OK;
+}
+
+}  // extern "C"

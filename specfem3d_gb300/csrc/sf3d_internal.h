@@ -49,6 +49,28 @@ struct Fields {
   float* eps_trace_over_3 = nullptr;                                      // [e][128]
 };
 
+// Checkpointed discrete-adjoint gradient state (sf3d_gradient_*).
+struct GradState {
+  int nstep = 0, every = 0, nckpt = 0;
+  float* ckpt = nullptr;       // [nckpt][3][3*nglob]: displ, veloc, accel at segment starts
+  float* seg_u = nullptr;      // [every][3*nglob]: displacement after each step of a segment
+  float* seg_a = nullptr;      // [every][3*nglob]: force after each step (before the mass matrix)
+  float* adj_u = nullptr;      // adjoint of displacement, velocity, acceleration [3*nglob]
+  float* adj_v = nullptr;
+  float* adj_a = nullptr;
+  float* p = nullptr;          // -M^-1 (adjoint of the new acceleration) [3*nglob]
+  float* kp = nullptr;         // -K p   [3*nglob]
+  float* bp = nullptr;         // -B p   [3*nglob]
+  float* residual = nullptr;   // (3, nrec, nstep): dJ/d(seismogram sample)
+  double* g_rho = nullptr;     // [nspec][128] dJ/d(rho), dJ/d(kappa), dJ/d(mu) per GLL point
+  double* g_kappa = nullptr;
+  double* g_mu = nullptr;
+  float wgll[NGLLX] = {};
+  double res_scale = 1.0;      // power of two applied to the residual (undone in sf3d_gradient_get)
+  float u_scale = 1.f;         // power of two applied to the forward field in the strain products
+  size_t bytes = 0;
+};
+
 struct Mesh {
   int nspec = 0, nglob = 0, nspec_irregular = 0;
   float xix_regular = 0.f, jacobian_regular = 0.f;
@@ -71,6 +93,7 @@ struct Mesh {
 
   // phases: [2][num_phase_ispec] 0-based element lists
   int num_phase_ispec = 0;
+  int phase_valid[2] = {0, 0};           // leading in-range entries of each phase column
   int nspec_outer = 0, nspec_inner = 0;
   int* d_phase_ispec = nullptr;
 
@@ -136,6 +159,7 @@ struct Mesh {
   float* d_potential_dot_dot = nullptr;
   float* d_rmass_acoustic = nullptr;
   int num_phase_ispec_ac = 0, nspec_outer_ac = 0, nspec_inner_ac = 0;
+  int phase_valid_ac[2] = {0, 0};
   int* d_phase_ispec_ac = nullptr;        // [2][num_phase_ispec_ac] 0-based
   int num_free_surface_faces = 0;
   int* d_fs_ispec = nullptr;              // [nf] 0-based
@@ -150,12 +174,27 @@ struct Mesh {
 
   // device step counter for graph-captured time loops, and completion counter
   int* d_it = nullptr;
-  unsigned long long* d_stamps = nullptr;  // per-step stiffness start/end (globaltimer ns)
   unsigned int* d_done = nullptr;
   float* d_scratch = nullptr;             // reduction scratch
+  int* d_kerr = nullptr;                  // kernel error word (bounded waits that timed out)
+  GradState* grad = nullptr;              // checkpointed adjoint gradient (optional)
+
+  // MPI interfaces of this slice (inter-slice assembly of accel)
+  int num_interfaces = 0, max_nibool_interfaces = 0;
+  long size_mpi_buffer = 0;               // NDIM * max_nibool * num_interfaces
+  int* d_nibool_interfaces = nullptr;     // [num_interfaces]
+  int* d_ibool_interfaces = nullptr;      // [num_interfaces][max_nibool] 0-based
+  float* d_send_accel_buffer = nullptr;   // (3, max_nibool, num_interfaces)
+  float* d_b_send_accel_buffer = nullptr;
+  float* h_send_accel_buffer = nullptr;   // pinned staging
+  float* h_recv_accel_buffer = nullptr;
+  cudaStream_t copy_stream = nullptr;
+  cudaEvent_t ev_pack = nullptr;          // packing done on the compute stream
+  int stiffness_variant = 3;              // see variant_blocks_per_sm; 1: persistent bulk-copy pipeline
 
   cudaStream_t stream = nullptr;
   cudaEvent_t ev0 = nullptr, ev1 = nullptr;
+  std::vector<cudaEvent_t> tev;           // timing mode: start/end event per stiffness step
   float last_stiff_ms = 0.f, last_total_ms = 0.f;
   int last_stiff_launches = 0, last_total_launches = 0;
 
@@ -210,7 +249,40 @@ struct StiffnessArgs {
   float alpha[NSLS], beta[NSLS], gamma[NSLS];
 };
 
-void launch_stiffness(const StiffnessArgs& a, bool att, bool store_strain, cudaStream_t s);
+void launch_stiffness(const StiffnessArgs& a, bool att, bool store_strain, cudaStream_t s, int blocks_per_sm);
+void launch_stiffness_pipelined(const StiffnessArgs& a, bool att, bool store_strain, int* err, cudaStream_t s);
+// stiffness kernel variants (sf3d_set_stiffness_variant / sf3d_autotune_stiffness)
+constexpr int kNumStiffnessVariants = 5;
+inline int variant_blocks_per_sm(int v) { return v == 0 ? 4 : (v == 2 ? 5 : (v == 3 ? 6 : (v == 4 ? 7 : 0))); }
+void free_grad(Mesh* mp);
+// max |x| over n values on the compute stream (NaN if any value is NaN); synchronises
+bool device_maxabs(Mesh* mp, const float* x, long n, float* out);
+// inter-slice assembly buffers (sf3d_assemble.cu)
+bool prepare_interfaces(Mesh* mp, int num_interfaces, int max_nibool, const int* nibool, const int* ibool_interfaces);
+void free_interfaces(Mesh* mp);
+// default element counts of the two elastic phases for the fused drivers
+inline void default_phase_counts(Mesh* mp) {
+  if (mp->nspec_outer == 0 && mp->nspec_inner == 0) {
+    mp->nspec_outer = mp->phase_valid[0];
+    mp->nspec_inner = mp->phase_valid[1];
+  }
+}
+// reads and clears the kernel error word; false (and a stored error) if set
+bool check_kernel_error(Mesh* mp);
+// dispatch on Mesh::stiffness_variant
+inline void run_stiffness(Mesh* mp, const StiffnessArgs& a, bool att, bool store_strain, cudaStream_t s) {
+  if (mp->stiffness_variant == 1 && mp->d_kerr)
+    launch_stiffness_pipelined(a, att, store_strain, mp->d_kerr, s);
+  else
+    launch_stiffness(a, att, store_strain, s, variant_blocks_per_sm(mp->stiffness_variant));
+}
 void launch_pressure_seismograms(Mesh* mp, int slot);
+// one fused forward elastic step of sf3d_iterate_time (predictor fused with the
+// previous corrector unless first_step); returns the number of launches
+int enqueue_step(Mesh* mp, float dt, float dt2, float dtsq2, bool first_step, cudaEvent_t* ev);
+void launch_stacey(Mesh* mp, const float* veloc, float* accel, cudaStream_t s);
+void launch_set_it(Mesh* mp, int it, cudaStream_t s);
+void launch_mass_corrector(Mesh* mp, float dt2, cudaStream_t s);
+StiffnessArgs stiffness_args(Mesh* mp, Fields& F, int iphase, float deltat, bool att, bool strain, bool backward);
 
 }  // namespace sf3d

@@ -242,8 +242,7 @@ void prepare_constants_device_(long* Mesh_pointer, int* h_NGLLX, int* NSPEC_AB, 
                                int* SAVE_SEISMOGRAMS_ACCELERATION, int* SAVE_SEISMOGRAMS_PRESSURE,
                                int* h_NB_RUNS_ACOUSTIC_GPU, int* FAULT_SIMULATION,
                                int* UNDO_ATTENUATION_AND_OR_PML, int* PML_CONDITIONS) {
-  (void)num_interfaces_ext_mesh; (void)max_nibool_interfaces_ext_mesh; (void)h_nibool_interfaces_ext_mesh;
-  (void)h_ibool_interfaces_ext_mesh; (void)h_ispec_is_inner; (void)USE_MESH_COLORING_GPU_f;
+  (void)h_ispec_is_inner; (void)USE_MESH_COLORING_GPU_f;
   (void)nspec_elastic; (void)ispec_is_elastic;
   (void)FAULT_SIMULATION; (void)UNDO_ATTENUATION_AND_OR_PML; (void)nu_source;
   if (!Mesh_pointer) { set_error(SF3D_ERR_ARG, "Mesh_pointer is NULL"); return; }
@@ -289,6 +288,9 @@ void prepare_constants_device_(long* Mesh_pointer, int* h_NGLLX, int* NSPEC_AB, 
     ok = copy_in((void**)&mp->d_irregular, irr.data(), sizeof(int) * nspec, s);
   }
   if (ok) ok = upload_padded_int_minus1(&mp->d_ibool, h_ibool, nspec, s);
+  if (ok && num_interfaces_ext_mesh && *num_interfaces_ext_mesh > 0)
+    ok = prepare_interfaces(mp, *num_interfaces_ext_mesh, *max_nibool_interfaces_ext_mesh,
+                            h_nibool_interfaces_ext_mesh, h_ibool_interfaces_ext_mesh);
   realw* hm[9] = {h_xix, h_xiy, h_xiz, h_etax, h_etay, h_etaz, h_gammax, h_gammay, h_gammaz};
   for (int q = 0; ok && q < 9; ++q) ok = upload_padded(&mp->d_metric[q], hm[q], mp->nspec_irregular, s);
   if (ok) {
@@ -296,6 +298,11 @@ void prepare_constants_device_(long* Mesh_pointer, int* h_NGLLX, int* NSPEC_AB, 
     memcpy(gll, h_hprime_xx, sizeof(float) * 25);
     memcpy(gll + 25, h_hprimewgll_xx, sizeof(float) * 25);
     memcpy(gll + 50, h_wgllwgll_xy, sizeof(float) * 25);
+    memcpy(mp->h_hprime, h_hprime_xx, sizeof(float) * 25);
+    memcpy(mp->h_hprimewgll, h_hprimewgll_xx, sizeof(float) * 25);
+    memcpy(mp->h_wxy, h_wgllwgll_xy, sizeof(float) * 25);
+    memcpy(mp->h_wxz, h_wgllwgll_xz, sizeof(float) * 25);
+    memcpy(mp->h_wyz, h_wgllwgll_yz, sizeof(float) * 25);
     memcpy(gll + 75, h_wgllwgll_xz, sizeof(float) * 25);
     memcpy(gll + 100, h_wgllwgll_yz, sizeof(float) * 25);
     ok = copy_in((void**)&mp->d_gll, gll, sizeof(gll), s);
@@ -395,6 +402,7 @@ void prepare_constants_device_(long* Mesh_pointer, int* h_NGLLX, int* NSPEC_AB, 
   if (ok) ok = alloc_zero((void**)&mp->d_it, sizeof(int) * 4);
   if (ok) ok = alloc_zero((void**)&mp->d_done, sizeof(unsigned int) * 4);
   if (ok) ok = alloc_zero((void**)&mp->d_scratch, sizeof(float) * 4096);
+  if (ok) ok = alloc_zero((void**)&mp->d_kerr, sizeof(int) * 4);
   if (!ok) {
     long tmp = (long)mp;
     prepare_cleanup_device_(&tmp, nullptr, nullptr, nullptr);
@@ -460,6 +468,12 @@ void prepare_fields_elastic_device_(long* Mesh_pointer, realw* rmassx, realw* rm
       // entries past nspec_outer/nspec_inner are unused padding; only range-check set ones
       if (ph[q] >= nspec) ok = set_error(SF3D_ERR_ARG, "phase_ispec_inner_elastic out of range");
     }
+    // the element counts used later may not reach into padding
+    for (int c = 0; c < 2; ++c) {
+      int n = 0;
+      while (n < mp->num_phase_ispec && ph[(size_t)c * mp->num_phase_ispec + n] >= 0) ++n;
+      mp->phase_valid[c] = n;
+    }
     if (ok) ok = copy_in((void**)&mp->d_phase_ispec, ph.data(), sizeof(int) * ph.size(), s);
   }
   mp->compute_and_store_strain = *COMPUTE_AND_STORE_STRAIN;
@@ -508,9 +522,12 @@ void prepare_cleanup_device_(long* Mesh_pointer, int* ACOUSTIC_SIMULATION, int* 
   cudaFree(mp->d_phase_ispec_ac); cudaFree(mp->d_fs_ispec); cudaFree(mp->d_fs_pt); cudaFree(mp->d_cp_ispec);
   cudaFree(mp->d_cp_pt); cudaFree(mp->d_cp_normal); cudaFree(mp->d_cp_jw); cudaFree(mp->d_seismo_p);
   cudaFree(mp->d_rec_is_acoustic);
-  cudaFree(mp->d_it); cudaFree(mp->d_stamps); cudaFree(mp->d_done); cudaFree(mp->d_scratch); cudaFree(mp->d_stage);
+  free_grad(mp);
+  free_interfaces(mp);
+  cudaFree(mp->d_it); cudaFree(mp->d_done); cudaFree(mp->d_scratch); cudaFree(mp->d_kerr); cudaFree(mp->d_stage);
   if (mp->ev0) cudaEventDestroy(mp->ev0);
   if (mp->ev1) cudaEventDestroy(mp->ev1);
+  for (cudaEvent_t e : mp->tev) cudaEventDestroy(e);
   if (mp->stream) cudaStreamDestroy(mp->stream);
   delete mp;
   *Mesh_pointer = 0;
@@ -608,7 +625,7 @@ void* sf3d_device_ptr(long* Mesh_pointer, const char* name) {
 int sf3d_synchronize(long* Mesh_pointer) {
   Mesh* mp = get_mesh(Mesh_pointer);
   if (!mp) return SF3D_ERR_STATE;
-  cuda_ok(cudaStreamSynchronize(mp->stream), "cudaStreamSynchronize");
+  if (cuda_ok(cudaStreamSynchronize(mp->stream), "cudaStreamSynchronize")) check_kernel_error(mp);
   return sf3d_last_error(nullptr, 0);
 }
 

@@ -12,6 +12,7 @@
 #include <math.h>
 #include <string.h>
 
+#include <utility>
 #include <vector>
 
 #include "sf3d_internal.h"
@@ -212,25 +213,27 @@ __global__ void set_it_kernel(int* d_it, int v) { *d_it = v; }
 // max |u| over the field (check_stability.f90:408), NaN-propagating
 __global__ void maxabs_kernel(const float* __restrict__ x, long n, float* __restrict__ out) {
   float m = 0.f;
+  bool nan = false;
   for (long i = (long)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (long)gridDim.x * blockDim.x) {
-    float v = fabsf(x[i]);
-    if (!(v <= m)) m = v;  // keeps NaN
+    const float v = fabsf(x[i]);
+    if (v != v)
+      nan = true;
+    else
+      m = fmaxf(m, v);
   }
 #pragma unroll
-  for (int o = 16; o > 0; o >>= 1) {
-    float w = __shfl_down_sync(0xffffffffu, m, o);
-    if (!(w <= m)) m = w;
-  }
+  for (int o = 16; o > 0; o >>= 1) m = fmaxf(m, __shfl_down_sync(0xffffffffu, m, o));
+  nan = __any_sync(0xffffffffu, nan);
   if ((threadIdx.x & 31) == 0) {
     unsigned int* ui = reinterpret_cast<unsigned int*>(out);
-    if (m != m)
-      atomicExch(ui + 1, 1u);
-    else
-      atomicMax(ui, __float_as_uint(m));  // non-negative floats order like their bits
+    if (nan) atomicExch(ui + 1, 1u);
+    atomicMax(ui, __float_as_uint(m));  // non-negative floats order like their bits
   }
 }
 
 Fields* pick(Mesh* mp, int fwd_or_adj) { return fwd_or_adj == 3 ? &mp->b : &mp->f; }
+
+}  // namespace
 
 StiffnessArgs stiffness_args(Mesh* mp, Fields& F, int iphase, float deltat, bool att, bool strain, bool backward) {
   StiffnessArgs a;
@@ -262,7 +265,99 @@ StiffnessArgs stiffness_args(Mesh* mp, Fields& F, int iphase, float deltat, bool
   return a;
 }
 
-}  // namespace
+
+// Reads and clears the kernel error word (set by a bounded wait that timed out).
+bool check_kernel_error(Mesh* mp) {
+  if (!mp->d_kerr) return true;
+  int h = 0;
+  if (!copy_sync(&h, mp->d_kerr, sizeof(int), cudaMemcpyDeviceToHost, mp->stream)) return false;
+  if (h != 0) {
+    cudaMemsetAsync(mp->d_kerr, 0, sizeof(int), mp->stream);
+    set_error(SF3D_ERR_CUDA, "stiffness pipeline: a bulk-copy wait timed out; the step result is invalid");
+    return false;
+  }
+  return true;
+}
+
+// One fused forward step on the compute stream; the predictor of this step is
+// fused with the corrector of the previous one unless first_step.
+// ev (optional): events recorded on the compute stream around the stiffness
+// launches of the step.
+int enqueue_step(Mesh* mp, float dt, float dt2, float dtsq2, bool first_step, cudaEvent_t* ev) {
+  Fields& F = mp->f;
+  cudaStream_t s = mp->stream;
+  int launches = 0;
+  if (first_step) {
+    const long n = 3L * mp->nglob;
+    predictor_kernel<<<nblk(n, 256), 256, 0, s>>>(F.displ, F.veloc, F.accel, n, dt, dt2, dtsq2);
+  } else {
+    corrector_predictor_kernel<<<nblk(3L * mp->nglob, 256), 256, 0, s>>>(F.displ, F.veloc, F.accel, mp->d_rmassx,
+                                                                    mp->d_rmassy, mp->d_rmassz, mp->nglob, dt, dt2,
+                                                                    dtsq2);
+  }
+  ++launches;
+  if (mp->stacey && mp->num_abs_faces > 0) {
+    const long n = (long)mp->num_abs_faces * NGLL2;
+    stacey_kernel<<<nblk(n, 128), 128, 0, s>>>(mp->num_abs_faces, mp->d_abs_ispec, mp->d_abs_pt, mp->d_abs_normal,
+                                                mp->d_abs_jw, mp->d_ibool, mp->d_rho_vp, mp->d_rho_vs, F.veloc,
+                                                F.accel, nullptr, mp->d_ispec_is_acoustic);
+    ++launches;
+  }
+  if (mp->nsources > 0 && mp->d_stf_table) {
+    sources_kernel<<<mp->nsources, NGLL3_PAD, 0, s>>>(mp->nsources, mp->d_ispec_src, mp->d_sourcearrays, nullptr,
+                                                      mp->d_stf_table, mp->d_it, mp->stf_nstep, mp->d_ibool, F.accel,
+                                                      mp->d_ispec_is_acoustic);
+    ++launches;
+  }
+  const bool att = mp->attenuation != 0;
+  const bool strain = mp->compute_and_store_strain != 0;
+  if (ev) cudaEventRecord(ev[0], s);
+  for (int iphase = 1; iphase <= 2; ++iphase) {
+    StiffnessArgs a = stiffness_args(mp, F, iphase, dt, att, strain, false);
+    if (a.nelem <= 0) continue;
+    run_stiffness(mp, a, att, strain, s);
+    ++launches;
+  }
+  if (ev) cudaEventRecord(ev[1], s);
+  if (mp->nrec_local > 0 && mp->save_d) {
+    seismogram_kernel<<<mp->nrec_local, NGLL3_PAD, 0, s>>>(mp->nrec_local, mp->d_ispec_rec, mp->d_hxir, mp->d_hetar,
+                                                           mp->d_hgammar, mp->d_nu_rec, mp->d_ibool, F.displ,
+                                                           mp->d_seismo_d, mp->nlength_seismogram, 0, mp->d_it,
+                                                           mp->d_it, mp->d_done, 1);
+  } else {
+    advance_it_kernel<<<1, 1, 0, s>>>(mp->d_it);
+  }
+  ++launches;
+  return launches;
+}
+
+// Stacey traction of a velocity-like field into an acceleration-like buffer.
+void launch_stacey(Mesh* mp, const float* veloc, float* accel, cudaStream_t s) {
+  if (!mp->stacey || mp->num_abs_faces == 0) return;
+  const long n = (long)mp->num_abs_faces * NGLL2;
+  stacey_kernel<<<nblk(n, 128), 128, 0, s>>>(mp->num_abs_faces, mp->d_abs_ispec, mp->d_abs_pt, mp->d_abs_normal,
+                                              mp->d_abs_jw, mp->d_ibool, mp->d_rho_vp, mp->d_rho_vs, veloc, accel,
+                                              nullptr, mp->d_ispec_is_acoustic);
+}
+
+void launch_set_it(Mesh* mp, int it, cudaStream_t s) { set_it_kernel<<<1, 1, 0, s>>>(mp->d_it, it); }
+
+void launch_mass_corrector(Mesh* mp, float dt2, cudaStream_t s) {
+  mass_corrector_kernel<<<nblk(3L * mp->nglob, 256), 256, 0, s>>>(mp->f.veloc, mp->f.accel, mp->d_rmassx,
+                                                                  mp->d_rmassy, mp->d_rmassz, mp->nglob, dt2);
+}
+
+bool device_maxabs(Mesh* mp, const float* x, long n, float* out) {
+  if (!cuda_ok(cudaMemsetAsync(mp->d_scratch, 0, sizeof(float) * 2, mp->stream), "cudaMemsetAsync")) return false;
+  maxabs_kernel<<<4 * 152, 256, 0, mp->stream>>>(x, n, mp->d_scratch);
+  float h[2];
+  if (!copy_sync(h, mp->d_scratch, sizeof(h), cudaMemcpyDeviceToHost, mp->stream)) return false;
+  unsigned nanflag;
+  memcpy(&nanflag, &h[1], 4);
+  *out = nanflag ? NAN : h[0];
+  return true;
+}
+
 }  // namespace sf3d
 
 using namespace sf3d;
@@ -292,7 +387,7 @@ void compute_forces_viscoelastic_cuda_(long* Mesh_pointer, int* iphase, realw* d
   mp->nspec_outer = *nspec_outer_elastic;
   mp->nspec_inner = *nspec_inner_elastic;
   const int nel = *iphase == 1 ? mp->nspec_outer : mp->nspec_inner;
-  if (nel < 0 || nel > mp->nspec || (nel > 0 && mp->num_phase_ispec < nel)) {
+  if (nel < 0 || nel > mp->phase_valid[*iphase - 1]) {
     set_error(SF3D_ERR_ARG, "nspec_outer/inner_elastic exceeds the phase element lists");
     return;
   }
@@ -300,11 +395,11 @@ void compute_forces_viscoelastic_cuda_(long* Mesh_pointer, int* iphase, realw* d
   const bool strain = *COMPUTE_AND_STORE_STRAIN && mp->compute_and_store_strain;
   if (fa == 1 || fa == 0) {
     StiffnessArgs a = stiffness_args(mp, mp->f, *iphase, *deltat, att, strain, false);
-    launch_stiffness(a, att, strain, mp->stream);
+    run_stiffness(mp, a, att, strain, mp->stream);
   }
   if ((fa == 3 || fa == 0) && mp->b.displ) {
     StiffnessArgs a = stiffness_args(mp, mp->b, *iphase, *deltat, att, strain, true);
-    launch_stiffness(a, att && mp->b.R[0] != nullptr, strain && mp->b.eps[0] != nullptr, mp->stream);
+    run_stiffness(mp, a, att && mp->b.R[0] != nullptr, strain && mp->b.eps[0] != nullptr, mp->stream);
   }
   cuda_ok(cudaGetLastError(), "stiffness_kernel");
 }
@@ -469,64 +564,6 @@ int sf3d_set_stf_table(long* Mesh_pointer, const double* h_stf, int nsources, in
   return SF3D_OK;
 }
 
-__global__ void stamp_kernel(unsigned long long* stamps, const int* d_it, int which, int nmax) {
-  unsigned long long t;
-  asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t));
-  const int it = *d_it;
-  if (it >= 1 && it <= nmax) stamps[2 * (it - 1) + which] = t;
-}
-
-// One fused forward step on the compute stream; the predictor of this step is
-// fused with the corrector of the previous one unless first_step.
-static int enqueue_step(Mesh* mp, float dt, float dt2, float dtsq2, bool first_step, unsigned long long* stamps,
-                        int nmax) {
-  Fields& F = mp->f;
-  cudaStream_t s = mp->stream;
-  int launches = 0;
-  if (first_step) {
-    const long n = 3L * mp->nglob;
-    predictor_kernel<<<nblk(n, 256), 256, 0, s>>>(F.displ, F.veloc, F.accel, n, dt, dt2, dtsq2);
-  } else {
-    corrector_predictor_kernel<<<nblk(3L * mp->nglob, 256), 256, 0, s>>>(F.displ, F.veloc, F.accel, mp->d_rmassx,
-                                                                    mp->d_rmassy, mp->d_rmassz, mp->nglob, dt, dt2,
-                                                                    dtsq2);
-  }
-  ++launches;
-  if (mp->stacey && mp->num_abs_faces > 0) {
-    const long n = (long)mp->num_abs_faces * NGLL2;
-    stacey_kernel<<<nblk(n, 128), 128, 0, s>>>(mp->num_abs_faces, mp->d_abs_ispec, mp->d_abs_pt, mp->d_abs_normal,
-                                                mp->d_abs_jw, mp->d_ibool, mp->d_rho_vp, mp->d_rho_vs, F.veloc,
-                                                F.accel, nullptr, mp->d_ispec_is_acoustic);
-    ++launches;
-  }
-  if (mp->nsources > 0 && mp->d_stf_table) {
-    sources_kernel<<<mp->nsources, NGLL3_PAD, 0, s>>>(mp->nsources, mp->d_ispec_src, mp->d_sourcearrays, nullptr,
-                                                      mp->d_stf_table, mp->d_it, mp->stf_nstep, mp->d_ibool, F.accel,
-                                                      mp->d_ispec_is_acoustic);
-    ++launches;
-  }
-  const bool att = mp->attenuation != 0;
-  const bool strain = mp->compute_and_store_strain != 0;
-  for (int iphase = 1; iphase <= 2; ++iphase) {
-    StiffnessArgs a = stiffness_args(mp, F, iphase, dt, att, strain, false);
-    if (a.nelem <= 0) continue;
-    if (stamps && iphase == 2) stamp_kernel<<<1, 1, 0, s>>>(stamps, mp->d_it, 0, nmax);
-    launch_stiffness(a, att, strain, s);
-    if (stamps && iphase == 2) stamp_kernel<<<1, 1, 0, s>>>(stamps, mp->d_it, 1, nmax);
-    ++launches;
-  }
-  if (mp->nrec_local > 0 && mp->save_d) {
-    seismogram_kernel<<<mp->nrec_local, NGLL3_PAD, 0, s>>>(mp->nrec_local, mp->d_ispec_rec, mp->d_hxir, mp->d_hetar,
-                                                           mp->d_hgammar, mp->d_nu_rec, mp->d_ibool, F.displ,
-                                                           mp->d_seismo_d, mp->nlength_seismogram, 0, mp->d_it,
-                                                           mp->d_it, mp->d_done, 1);
-  } else {
-    advance_it_kernel<<<1, 1, 0, s>>>(mp->d_it);
-  }
-  ++launches;
-  return launches;
-}
-
 int sf3d_iterate_time(long* Mesh_pointer, int it_begin, int it_end, realw deltat, int steps_per_graph, int flags) {
   Mesh* mp = get_mesh(Mesh_pointer);
   if (!mp) return SF3D_ERR_STATE;
@@ -537,32 +574,37 @@ int sf3d_iterate_time(long* Mesh_pointer, int it_begin, int it_end, realw deltat
     return SF3D_ERR_STATE;
   }
   if (mp->num_phase_ispec <= 0) { set_error(SF3D_ERR_STATE, "phase element lists not prepared"); return SF3D_ERR_STATE; }
-  if (mp->nspec_outer == 0 && mp->nspec_inner == 0) mp->nspec_inner = mp->num_phase_ispec;
+  default_phase_counts(mp);
   const float dt = deltat, dt2 = deltat / 2.f, dtsq2 = deltat * deltat / 2.f;
   const bool timing = (flags & 1) != 0;
   const int nsteps = it_end - it_begin + 1;
   if (timing) {
-    cudaFree(mp->d_stamps);
-    mp->d_stamps = nullptr;
-    if (!alloc_zero((void**)&mp->d_stamps, sizeof(unsigned long long) * 2 * (size_t)it_end)) return SF3D_ERR_CUDA;
+    while (mp->tev.size() < 2 * (size_t)nsteps) {
+      cudaEvent_t e;
+      SF3D_CUDA_RET(cudaEventCreate(&e), SF3D_ERR_CUDA);
+      mp->tev.push_back(e);
+    }
   }
   cudaStream_t s = mp->stream;
   set_it_kernel<<<1, 1, 0, s>>>(mp->d_it, it_begin);
   SF3D_CUDA_RET(cudaMemsetAsync(mp->d_done, 0, sizeof(unsigned int), s), SF3D_ERR_CUDA);
   SF3D_CUDA_RET(cudaEventRecord(mp->ev0, s), SF3D_ERR_CUDA);
-  int launches = 0;
+  int launches = 0, done = 0;
   auto step = [&](bool first) {
-    launches += enqueue_step(mp, dt, dt2, dtsq2, first, timing ? mp->d_stamps : nullptr, it_end);
+    launches += enqueue_step(mp, dt, dt2, dtsq2, first, timing ? &mp->tev[2 * (size_t)done] : nullptr);
+    ++done;
   };
   step(true);
   int remaining = nsteps - 1;
-  const int K = steps_per_graph > 0 ? steps_per_graph : 0;
+  // timing mode brackets every stiffness launch with its own events, so it
+  // launches the steps one by one instead of through a graph
+  const int K = (steps_per_graph > 0 && !timing) ? steps_per_graph : 0;
   if (K > 0 && remaining >= K) {
     cudaGraph_t graph = nullptr;
     cudaGraphExec_t exec = nullptr;
     int per_block = 0;
     SF3D_CUDA_RET(cudaStreamBeginCapture(s, cudaStreamCaptureModeThreadLocal), SF3D_ERR_CUDA);
-    for (int q = 0; q < K; ++q) per_block += enqueue_step(mp, dt, dt2, dtsq2, false, timing ? mp->d_stamps : nullptr, it_end);
+    for (int q = 0; q < K; ++q) per_block += enqueue_step(mp, dt, dt2, dtsq2, false, nullptr);
     SF3D_CUDA_RET(cudaStreamEndCapture(s, &graph), SF3D_ERR_CUDA);
     SF3D_CUDA_RET(cudaGraphInstantiate(&exec, graph, 0), SF3D_ERR_CUDA);
     while (remaining >= K) {
@@ -585,16 +627,83 @@ int sf3d_iterate_time(long* Mesh_pointer, int it_begin, int it_end, realw deltat
   mp->last_stiff_launches = 0;
   mp->last_stiff_ms = 0.f;
   if (timing) {
-    std::vector<unsigned long long> st(2 * (size_t)it_end);
-    if (!copy_sync(st.data(), mp->d_stamps, sizeof(unsigned long long) * st.size(), cudaMemcpyDeviceToHost, mp->stream)) return SF3D_ERR_CUDA;
-    double ns = 0;
-    for (int it = it_begin; it <= it_end; ++it) {
-      const unsigned long long a = st[2 * (it - 1)], b = st[2 * (it - 1) + 1];
-      if (b > a) { ns += (double)(b - a); ++mp->last_stiff_launches; }
+    double ms = 0;
+    for (int q = 0; q < nsteps; ++q) {
+      float d = 0.f;
+      if (cudaEventElapsedTime(&d, mp->tev[2 * q], mp->tev[2 * q + 1]) == cudaSuccess && d > 0.f) {
+        ms += d;
+        ++mp->last_stiff_launches;
+      }
     }
-    mp->last_stiff_ms = (float)(ns * 1e-6);
+    mp->last_stiff_ms = (float)ms;
   }
+  if (!check_kernel_error(mp)) return SF3D_ERR_CUDA;
   return sf3d_last_error(nullptr, 0);
+}
+
+int sf3d_set_stiffness_variant(long* Mesh_pointer, int variant) {
+  Mesh* mp = get_mesh(Mesh_pointer);
+  if (!mp) return SF3D_ERR_STATE;
+  if (variant < 0 || variant >= kNumStiffnessVariants) {
+    set_error(SF3D_ERR_ARG, "unknown stiffness variant");
+    return SF3D_ERR_ARG;
+  }
+  mp->stiffness_variant = variant;
+  return SF3D_OK;
+}
+
+int sf3d_autotune_stiffness(long* Mesh_pointer, int reps, float* ms_per_variant, int* best_variant) {
+  Mesh* mp = get_mesh(Mesh_pointer);
+  if (!mp) return SF3D_ERR_STATE;
+  if (!mp->f.displ || mp->num_phase_ispec <= 0) {
+    set_error(SF3D_ERR_STATE, "sf3d_autotune_stiffness: fields and phase lists not prepared");
+    return SF3D_ERR_STATE;
+  }
+  if (reps < 1) reps = 1;
+  default_phase_counts(mp);
+  // timing the kernels on a wavefield at rest leaves every array unchanged
+  // (zero strain keeps zero memory variables and adds zero force)
+  const bool att = mp->attenuation != 0;
+  std::vector<std::pair<const float*, long>> check = {{mp->f.displ, 3L * mp->nglob}, {mp->f.veloc, 3L * mp->nglob}};
+  if (att)
+    for (int c = 0; c < 6; ++c)
+      if (mp->f.R[c]) check.push_back({mp->f.R[c], (long)mp->nspec * NSLS * NGLL3_PAD});
+  for (auto& q : check) {
+    float m = 0.f;
+    if (!device_maxabs(mp, q.first, q.second, &m)) return SF3D_ERR_CUDA;
+    if (!(m == 0.f)) {
+      set_error(SF3D_ERR_STATE, "sf3d_autotune_stiffness must run on a wavefield at rest (before the first step)");
+      return SF3D_ERR_STATE;
+    }
+  }
+  const bool strain = mp->compute_and_store_strain != 0;
+  const int keep = mp->stiffness_variant;
+  auto pass = [&]() {
+    for (int iphase = 1; iphase <= 2; ++iphase) {
+      StiffnessArgs a = stiffness_args(mp, mp->f, iphase, 0.f, att, strain, false);
+      if (a.nelem > 0) run_stiffness(mp, a, att, strain, mp->stream);
+    }
+  };
+  int best = -1;
+  float best_ms = 0.f;
+  for (int v = 0; v < kNumStiffnessVariants; ++v) {
+    mp->stiffness_variant = v;
+    pass();
+    SF3D_CUDA_RET(cudaEventRecord(mp->ev0, mp->stream), SF3D_ERR_CUDA);
+    for (int r = 0; r < reps; ++r) pass();
+    SF3D_CUDA_RET(cudaEventRecord(mp->ev1, mp->stream), SF3D_ERR_CUDA);
+    SF3D_CUDA_RET(cudaEventSynchronize(mp->ev1), SF3D_ERR_CUDA);
+    if (!cuda_ok(cudaGetLastError(), "sf3d_autotune_stiffness")) { mp->stiffness_variant = keep; return SF3D_ERR_CUDA; }
+    if (!check_kernel_error(mp)) { mp->stiffness_variant = keep; return SF3D_ERR_CUDA; }
+    float ms = 0.f;
+    cudaEventElapsedTime(&ms, mp->ev0, mp->ev1);
+    ms /= (float)reps;
+    if (ms_per_variant) ms_per_variant[v] = ms;
+    if (best < 0 || ms < best_ms) { best = v; best_ms = ms; }
+  }
+  mp->stiffness_variant = best;
+  if (best_variant) *best_variant = best;
+  return SF3D_OK;
 }
 
 int sf3d_last_timing(long* Mesh_pointer, float* stiffness_ms, int* stiffness_launches, float* total_ms,
@@ -627,6 +736,7 @@ int sf3d_check_stability(long* Mesh_pointer, realw threshold, realw* max_norm) {
   float h[2];
   SF3D_CUDA_RET(cudaMemcpyAsync(h, mp->d_scratch, sizeof(h), cudaMemcpyDeviceToHost, mp->stream), SF3D_ERR_CUDA);
   SF3D_CUDA_RET(cudaStreamSynchronize(mp->stream), SF3D_ERR_CUDA);
+  if (!check_kernel_error(mp)) return SF3D_ERR_CUDA;
   unsigned nanflag;
   memcpy(&nanflag, &h[1], 4);
   if (max_norm) *max_norm = nanflag ? NAN : h[0];

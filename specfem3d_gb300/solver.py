@@ -52,6 +52,9 @@ class GPUSolver:
     # ------------------------------------------------------------------ setup
     def _prepare_constants(self, db, save_forward):
         A = abi.Args()
+        # MPI interfaces of a slice: ibool_interfaces (max_nibool, num_interfaces), 1-based
+        self.num_interfaces = int(db.get("num_interfaces", 0))
+        self.max_nibool = int(db.get("max_nibool_interfaces", 0))
         nspec, nirr = self.nspec, int(db["nspec_irregular"])
         nrec = self.nrec
         nu = np.tile(np.eye(3).reshape(-1, order="F"), max(nrec, 1))
@@ -62,7 +65,8 @@ class GPUSolver:
             self.mp, A.i(5), A.i(nspec), A.i(self.nglob), A.i(nirr), A.ai(db["irregular_element_number"]),
             *(A.af(db[n]) for n in ("xix", "xiy", "xiz", "etax", "etay", "etaz", "gammax", "gammay", "gammaz")),
             A.f(db["xix_regular"]), A.f(db["jacobian_regular"]), A.ai(db["ibool"]),
-            A.i(0), A.i(0), A.ai(None), A.ai(None),
+            A.i(self.num_interfaces), A.i(self.max_nibool), A.ai(db.get("nibool_interfaces")),
+            A.ai(db.get("ibool_interfaces")),
             A.af(db["hprime_xx"]), A.af(db["hprimewgll_xx"]), A.af(db["wgllwgll_xy"]), A.af(db["wgllwgll_xz"]),
             A.af(db["wgllwgll_yz"]),
             A.i(int(db.get("stacey", 1))), A.ai(db["abs_boundary_ispec"]), A.ai(db["abs_boundary_ijk"]),
@@ -83,10 +87,15 @@ class GPUSolver:
     def _prepare_fields(self, db):
         A = abi.Args()
         nspec = self.nspec
+        # phase_ispec_inner_elastic: outer elements (touching an MPI interface) in
+        # column 1, inner elements in column 2 (1-based)
         solid = np.nonzero(self.isac == 0)[0] + 1
-        self.nspec_elastic = len(solid)
-        phase = np.zeros((max(len(solid), 1), 2), np.int32)
-        phase[:len(solid), 1] = solid
+        outer = np.asarray(db.get("phase_outer", np.zeros(0, np.int32)), np.int32)
+        inner = np.setdiff1d(solid, outer).astype(np.int32)
+        self.nspec_outer, self.nspec_elastic = len(outer), len(inner)
+        phase = np.zeros((max(len(outer), len(inner), 1), 2), np.int32)
+        phase[:len(outer), 0] = outer
+        phase[:len(inner), 1] = inner
         att = self.attenuation
         strain = int(att or self.simulation_type == 3)
         zsls = np.zeros(N_SLS * NGLL3 * nspec, np.float32) if att else None
@@ -148,6 +157,14 @@ class GPUSolver:
 
     def step(self):
         """One time step through the per-call entry points, in the reference's order."""
+        self.step_predict()
+        self.step_forces(1)
+        self.step_forces(2)
+        self.step_finish()
+
+    # the pieces of a step, for drivers that exchange MPI interface buffers
+    # between the outer (iphase 1) and inner (iphase 2) element passes
+    def step_predict(self):
         L, A, it = self.L, abi.Args(), self.it
         one = A.i(1)
         L.update_displacement_cuda_(self.mp, A.f(self.deltat), A.f(self.deltatover2), A.f(self.deltatsqover2), one)
@@ -155,15 +172,40 @@ class GPUSolver:
             L.update_displacement_ac_cuda_(self.mp, A.f(self.deltat), A.f(self.deltatover2),
                                            A.f(self.deltatsqover2), one)
             self._acoustic_step(A, it)
-        for iphase in (1, 2):
-            L.compute_forces_viscoelastic_cuda_(self.mp, A.i(iphase), A.f(self.deltat), A.i(0),
-                                                A.i(self.nspec_elastic), A.i(self.strain), A.i(self.attenuation), one)
-            if iphase == 1:
-                L.compute_stacey_viscoelastic_cuda_(self.mp, A.i(1), A.af(None), one)
-                if self.coupled:
-                    L.compute_coupling_el_ac_cuda_(self.mp, A.i(1), A.i(self.ncoupling), one)
-                if self.nsources:
-                    L.compute_add_sources_el_cuda_(self.mp, A.ad(self._stf_now(it)), A.i(self.nsources))
+
+    def step_forces(self, iphase: int):
+        """compute_forces_viscoelastic_calling (compute_forces_viscoelastic_calling_routine.F90:107-160)."""
+        L, A, it = self.L, abi.Args(), self.it
+        one = A.i(1)
+        L.compute_forces_viscoelastic_cuda_(self.mp, A.i(iphase), A.f(self.deltat), A.i(self.nspec_outer),
+                                            A.i(self.nspec_elastic), A.i(self.strain), A.i(self.attenuation), one)
+        if iphase == 1:
+            L.compute_stacey_viscoelastic_cuda_(self.mp, A.i(1), A.af(None), one)
+            if self.coupled:
+                L.compute_coupling_el_ac_cuda_(self.mp, A.i(1), A.i(self.ncoupling), one)
+            if self.nsources:
+                L.compute_add_sources_el_cuda_(self.mp, A.ad(self._stf_now(it)), A.i(self.nsources))
+
+    def pack_interfaces(self) -> np.ndarray:
+        """transfer_boun_accel_from_device: accel at the interface points, (num_interfaces, max_nibool, 3)."""
+        buf = np.zeros((max(self.num_interfaces, 1), max(self.max_nibool, 1), 3), np.float32)
+        A = abi.Args()
+        self.L.transfer_boun_accel_from_device_(self.mp, buf.ctypes.data, A.i(1))
+        abi.check()
+        return buf
+
+    def assemble_interfaces(self, recv: np.ndarray):
+        """transfer_asmbl_accel_to_device: add the neighbours' contributions (same layout as pack)."""
+        A = abi.Args()
+        recv = np.ascontiguousarray(recv, np.float32)
+        self.L.transfer_asmbl_accel_to_device_(self.mp, recv.ctypes.data, A.i(self.num_interfaces),
+                                               A.i(self.max_nibool), A.ai(self.db.get("nibool_interfaces")),
+                                               A.ai(self.db.get("ibool_interfaces")), A.i(1))
+        abi.check()
+
+    def step_finish(self):
+        L, A, it = self.L, abi.Args(), self.it
+        one = A.i(1)
         L.kernel_3_a_cuda_(self.mp, A.f(self.deltatover2), A.f(0.0), A.i(0), one)
         if self.nrec:
             if not hasattr(self, "_seis_host"):
@@ -246,6 +288,11 @@ class GPUSolver:
                                                  A.i(1))
         self.L.sf3d_synchronize(self.mp)
         abi.check()
+
+    def set_stiffness_variant(self, variant: int):
+        """0: one CTA per element; 1: persistent bulk-copy pipelined kernel (default)."""
+        if self.L.sf3d_set_stiffness_variant(self.mp, int(variant)) != 0:
+            abi.check()
 
     def check_stability(self, threshold: float = 1e25):
         m = ctypes.c_float()

@@ -9,8 +9,9 @@ a different order, and recomputes J from the metric as the reference GPU does):
   differently ordered sums shows more in it);
 * accuracy against the FP64 oracle (the reference built with double
   CUSTOM_REAL): the device's FP32 error is at most 1.5x the FP32 CPU oracle's;
-* the fused graph-captured loop against the per-call ABI loop: <= 2e-5 (atomic
-  accumulation order differs from run to run);
+* the fused graph-captured loop against the per-call ABI loop: seismograms
+  <= 2e-5 (atomic accumulation order differs from run to run), and the same
+  FP64-relative bound;
 * the reference's golden seismograms: relative L2 <= 1e-3, correlation >= 0.999.
 """
 import os
@@ -63,11 +64,45 @@ def test_stiffness_pass_random_fields(gpulib, att):
     g.close()
 
 
+@pytest.mark.parametrize("att", [False, True])
+def test_stiffness_variants_agree(gpulib, att):
+    """All stiffness variants (one CTA per element at 4-7 CTAs/SM, the pipelined
+    persistent kernel) do the same arithmetic in the same order; the scatter-added acceleration differs
+    only by the order of the atomic additions, the memory variables and strains
+    at most by FMA contraction choices of the compiler."""
+    from specfem3d_gb300 import configs, meshgen
+    cfg = configs.small_layered(nx=9, ny=7, counts=(3, 3, 4), nstep=4, attenuation=att)
+    db = meshgen.build_database(cfg)
+    rng = np.random.default_rng(5)
+    n3 = 3 * db["nglob"]
+    d = rng.standard_normal(n3).astype(np.float32) * 1e-3
+    v = rng.standard_normal(n3).astype(np.float32) * 1e-2
+    out = []
+    for variant in range(5):
+        g = _solver(db, cfg)
+        g.set_stiffness_variant(variant)
+        g.set_fields(d, v, np.zeros(n3, np.float32))
+        g.forces_only()
+        g.forces_only()
+        acc = g.fields()[2]
+        mem = g.memory_variables() if att else None
+        out.append((acc, mem))
+        g.close()
+    for v in range(1, 5):
+        assert rel_l2(out[v][0], out[0][0]) < 1e-6, v
+        if att:
+            same = []
+            for a, b in zip(out[0][1][0] + out[0][1][1], out[v][1][0] + out[v][1][1]):
+                assert rel_l2(b, a) < 1e-6, v
+                same.append(float(np.mean(a == b)))
+            print(f"variant {v}: fraction of bit-identical memory-variable/strain values:", min(same))
+
+
 @pytest.fixture(scope="module")
-def cfg0_runs(gpulib):
+def homog_runs(gpulib):
     from specfem3d_gb300 import configs, meshgen
     from oracle import oracle as O
-    cfg = configs.cfg0(nstep=2000)
+    cfg = configs.homogeneous_block(nstep=2000)
     db = meshgen.build_database(cfg)
     sim = _oracle_sim(db, cfg)
     sim.step(cfg["nstep"])
@@ -89,22 +124,22 @@ def cfg0_runs(gpulib):
     return dict(cfg=cfg, db=db, so=so, sim=sim, sp=sp, fp=fp, sf=sf, ff=ff, so64=so64, sim64=sim64)
 
 
-def test_cfg0_seismograms_vs_oracle(cfg0_runs):
-    r = cfg0_runs
+def test_homogeneous_seismograms_vs_oracle(homog_runs):
+    r = homog_runs
     err = rel_l2(r["sp"], r["so"])
     assert err < 5e-5, err
     per_rec = [rel_l2(r["sp"][i], r["so"][i]) for i in range(len(r["so"]))]
     assert max(per_rec) < 1e-4
     ed = rel_l2(r["fp"][0], r["sim"].get("displ"))
     ev = rel_l2(r["fp"][1], r["sim"].get("veloc"))
-    print(f"cfg0 2000 steps: seismograms {err:.2e} (max receiver {max(per_rec):.2e}), displ {ed:.2e}, veloc {ev:.2e}")
+    print(f"homogeneous_block 2000 steps: seismograms {err:.2e} (max receiver {max(per_rec):.2e}), displ {ed:.2e}, veloc {ev:.2e}")
     assert ed < 3e-4 and ev < 3e-4
 
 
-def test_cfg0_accuracy_against_fp64_oracle(cfg0_runs):
+def test_homogeneous_accuracy_against_fp64_oracle(homog_runs):
     """The device's FP32 error against the FP64 oracle is no larger than the FP32
     CPU oracle's own (seismograms and final wavefields)."""
-    r = cfg0_runs
+    r = homog_runs
     e_gpu = rel_l2(r["sp"], r["so64"])
     e_cpu = rel_l2(r["so"], r["so64"])
     print(f"seismograms vs FP64: device {e_gpu:.2e}, FP32 oracle {e_cpu:.2e}")
@@ -117,11 +152,21 @@ def test_cfg0_accuracy_against_fp64_oracle(cfg0_runs):
         assert eg < 1.5 * ec + 1e-7, (name, eg, ec)
 
 
-def test_fused_loop_equals_per_call_abi(cfg0_runs):
-    r = cfg0_runs
+def test_fused_loop_equals_per_call_abi(homog_runs):
+    """The graph-captured fused loop and the per-call ABI loop give the same
+    seismograms, and the fused loop's FP32 error against the FP64 oracle is no
+    larger than the FP32 CPU oracle's (the wavefields left after the waves
+    exit are a tiny residual, so they are compared through that accuracy bound
+    rather than against each other)."""
+    r = homog_runs
     assert rel_l2(r["sf"], r["sp"]) < 2e-5
-    for a, b in zip(r["ff"], r["fp"]):
-        assert rel_l2(a, b) < 2e-4
+    e_cpu = rel_l2(r["so"], r["so64"])
+    assert rel_l2(r["sf"], r["so64"]) < 1.5 * e_cpu + 1e-7
+    for k, name in ((0, "displ"), (1, "veloc")):
+        eg = rel_l2(r["ff"][k], r["sim64"].get(name))
+        ec = rel_l2(r["sim"].get(name), r["sim64"].get(name))
+        print(f"fused {name} vs FP64: device {eg:.2e}, FP32 oracle {ec:.2e}")
+        assert eg < 1.5 * ec + 1e-7, (name, eg, ec)
 
 
 def test_attenuation_time_stepping_vs_oracle(gpulib):
@@ -144,7 +189,14 @@ def test_attenuation_time_stepping_vs_oracle(gpulib):
 
 @pytest.mark.parametrize("example,stacey", [("refex_stacey5sides", True), ("refex_no_absorbing", False)])
 def test_reference_golden_seismograms_on_gpu(gpulib, example, stacey):
-    """Full 5000-step reference example on the GPU against the reference's REF_SEIS."""
+    """Full 5000-step reference example on the GPU against the reference's REF_SEIS.
+
+    Stacey example: relative L2 <= 1e-3 and correlation >= 0.999 per trace.  No-absorbing
+    example: the FP32 and FP64 oracles themselves differ from that REF_SEIS by up to
+    6.2e-3 (correlation >= 0.99998), so the trace check uses the reference's own
+    tolerances (compare_seismogram_correlations.py TOL_ERR = 0.01, CI correlation
+    >= 0.999) and the GPU is additionally held to the FP64 oracle's traces
+    (tests/golden/make_oracle_fixture.py) at <= 2e-4 (FP32 after 5000 steps)."""
     from specfem3d_gb300 import configs, meshgen
     cfg = configs.refex(5000)
     cfg["stacey"] = stacey
@@ -154,10 +206,16 @@ def test_reference_golden_seismograms_on_gpu(gpulib, example, stacey):
     seis = g.seismograms()
     g.close()
     ref = np.load(os.path.join(ROOT, "tests", "golden", example + ".npz"))["displ"]
+    tol = 1e-3 if stacey else 1e-2
     for r in range(4):
         for c in range(3):
-            assert rel_l2(seis[r, c], ref[r, c]) < 1e-3, (r, c)
+            assert rel_l2(seis[r, c], ref[r, c]) < tol, (r, c)
             assert np.corrcoef(seis[r, c], ref[r, c])[0, 1] > 0.999
+    if not stacey:
+        o64 = np.load(os.path.join(ROOT, "tests", "golden", "refex_no_absorbing_oracle_f64.npz"))["displ"]
+        e = rel_l2(seis, o64)
+        print(f"no-absorbing example vs FP64 oracle: {e:.2e}")
+        assert e < 2e-4
 
 
 def test_stability_check_and_errors(gpulib):

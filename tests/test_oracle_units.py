@@ -53,7 +53,7 @@ def test_time_step_rule():
     assert abs(0.5 * dmin / 2800.0 - 0.114772588) < 1e-5
     assert configs.significant_dt(0.0734815) == 0.073
     assert configs.significant_dt(0.012847) == 0.0125
-    assert configs.cfg0()["dt"] == 0.0125
+    assert configs.homogeneous_block()["dt"] == 0.0125
 
 
 def test_attenuation_band_matches_reference_log():

@@ -12,12 +12,12 @@ FLOAT_KEYS = ["xix", "etay", "gammaz", "jacobian", "kappastore", "mustore", "rho
 
 def _cfgs():
     from specfem3d_gb300 import configs
-    return {"cfg0": configs.cfg0(nstep=20), "small_layered": configs.small_layered(nstep=20),
+    return {"homogeneous_block": configs.homogeneous_block(nstep=20), "small_layered": configs.small_layered(nstep=20),
             "small_noatt": configs.small_layered(nstep=20, attenuation=False, nx=3, ny=4, counts=(1, 2, 2)),
             "refex": configs.refex(20)}
 
 
-@pytest.mark.parametrize("name", ["cfg0", "small_layered", "small_noatt", "refex"])
+@pytest.mark.parametrize("name", ["homogeneous_block", "small_layered", "small_noatt", "refex"])
 def test_database_parity(name):
     from oracle import oracle as O
     from specfem3d_gb300 import meshgen
@@ -62,9 +62,9 @@ def test_ibool_invariants():
 
 def test_regular_mesh_split_follows_single_precision_rule():
     """The cube test of check_element_regularity runs on single-precision corner
-    coordinates, so rounding makes most cfg0 cubes 'irregular'; both sides agree."""
+    coordinates, so rounding makes most homogeneous_block cubes 'irregular'; both sides agree."""
     from specfem3d_gb300 import configs, meshgen
-    db = meshgen.build_database(configs.cfg0(nstep=5))
+    db = meshgen.build_database(configs.homogeneous_block(nstep=5))
     irr = db["irregular_element_number"]
     assert 0 < (irr == 0).sum() < len(irr)
     assert np.array_equal(irr[irr > 0], np.arange(1, (irr > 0).sum() + 1))
