@@ -377,6 +377,24 @@ int sf3d_gradient_get(long *Mesh_pointer, double *g_rho, double *g_kappa, double
 /* Free the gradient buffers (also freed by prepare_cleanup_device). */
 int sf3d_gradient_release(long *Mesh_pointer);
 
+/* Max |x| over the first n values of a device array of floats (NaN if any is
+ * NaN), computed on `stream` (NULL: the default stream) without allocating:
+ * the reduction's scratch is a fixed 256 KB device array inside the library.
+ * No reference counterpart (it is the reduction of sf3d_check_stability /
+ * check_stability.f90:408 for callers that must not allocate device memory).
+ * Limits and rules:
+ *   - 1 <= n <= 536854528 (one partial per 16384 values in the fixed scratch);
+ *     larger n returns SF3D_ERR_ARG with a message;
+ *   - nothing has to be zeroed beforehand: every scratch slot the call reads
+ *     is written earlier in the same call;
+ *   - the first call on a device looks up the scratch address
+ *     (cudaGetSymbolAddress) with that device current; make that first call
+ *     before any stream capture begins;
+ *   - calls that overlap in time on one device (other streams or host
+ *     threads) share the scratch and race: serialise them;
+ *   - returns after the result is on the host (synchronises `stream`). */
+int sf3d_field_maxabs_noalloc(const realw *d_field, long n, void *stream, realw *max_abs);
+
 /* Synchronise the compute stream and report the first stored status. */
 int sf3d_synchronize(long *Mesh_pointer);
 

@@ -83,6 +83,8 @@ def load() -> ctypes.CDLL:
     L.sf3d_gradient_get.argtypes = [P, P, P, P]
     L.sf3d_gradient_release.restype = ctypes.c_int
     L.sf3d_gradient_release.argtypes = [P]
+    L.sf3d_field_maxabs_noalloc.restype = ctypes.c_int
+    L.sf3d_field_maxabs_noalloc.argtypes = [P, ctypes.c_long, P, P]
     L.sf3d_synchronize.restype = ctypes.c_int
     L.sf3d_synchronize.argtypes = [P]
     L.sf3d_device_ptr.restype = P
