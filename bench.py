@@ -54,13 +54,13 @@ def _peaks():
 
 
 def _traffic():
-    """DRAM bytes per stiffness launch from the committed ncu summary, scaled to the
-    bench mesh by element count, or None."""
-    path = os.path.join(ROOT, "profiles", "stiffness_att_traffic.json")
+    """DRAM bytes per element of the stiffness kernel from the committed ncu summary
+    (line 'dram_bytes_per_element: N'), or None."""
+    import re
+    path = os.path.join(ROOT, "profiles", "stiffness_kernel_att_6ctas_layered_32x32x16.md")
     try:
-        with open(path) as f:
-            t = json.load(f)
-        return float(t["dram_bytes_per_element"])
+        m = re.search(r"dram_bytes_per_element:\s*([0-9.]+)", open(path).read())
+        return float(m.group(1)) if m else None
     except Exception:
         return None
 
@@ -161,6 +161,37 @@ def adjoint_leg(nshots: int):
             "workload": "64x64x32 hexes, 20x20x10 km, perturbed background, +3% vs blob true model"}
 
 
+def batch_leg(nshots: int, steps: int):
+    """Per-shot GLL-point updates/s of the batched-shots workload (64x64x32 hexes,
+    perturbed model, no attenuation): all shots advancing together with
+    shot-innermost fields against the plain single-shot path on the same mesh."""
+    from specfem3d_gb300 import configs, gradient as G, meshgen
+    from specfem3d_gb300.batch import BatchSolver
+    from specfem3d_gb300.solver import GPUSolver
+    cfg = configs.batched_shots(nstep=steps + 8, nshots=nshots)
+    db = meshgen.build_database(cfg)
+    nglob = int(db["nglob"])
+    b = BatchSolver(db, cfg, nlength=steps + 8)
+    tune = b.autotune(reps=3)
+    b.run(3, steps_per_graph=0)
+    ms_b = b.run(steps, steps_per_graph=50)
+    b.close()
+    plain = GPUSolver(db, G.shot_config(cfg, 0), nlength=steps + 8)
+    plain.run(3, steps_per_graph=50)
+    plain.run(steps, steps_per_graph=50)
+    ms_p = plain.last_timing()["total_ms"]
+    plain.close()
+    # shot-point updates per second: every shot's points advanced one step count once
+    rate_b = nglob * steps * nshots / (ms_b / 1000.0)
+    rate_p = nglob * steps / (ms_p / 1000.0)
+    return {"unit": "GLL-pt updates/s summed over shots", "shots": nshots, "steps": steps, "nglob": nglob,
+            "nspec": int(db["nspec"]), "batched": rate_b, "plain_single_shot": rate_p,
+            "speedup_per_shot": rate_b / rate_p, "batched_ms_per_step": ms_b / steps,
+            "plain_ms_per_step": ms_p / steps, "tiling": tune,
+            "workload": "64x64x32 hexes, 20x20x10 km, +-5% perturbed model, no attenuation, "
+                        f"{nshots} CMT shots, Ricker 2 Hz"}
+
+
 def run_reference(args, rank):
     if rank != 0:
         return 0
@@ -193,6 +224,9 @@ def main():
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--variant", type=int, default=-1,
                     help="stiffness kernel variant (sf3d_set_stiffness_variant); -1: autotune at rest")
+    ap.add_argument("--batch", type=int, default=0,
+                    help="also time this many shots of the batched-shots workload against the plain path (0: skip)")
+    ap.add_argument("--batch-steps", type=int, default=100)
     ap.add_argument("--adjoint", type=int, default=0,
                     help="also time the checkpointed misfit gradient over this many shots of the "
                          "8-shot 64x64x32 gradient workload (0: skip)")
@@ -217,7 +251,7 @@ def main():
         L.initialize_gpu_device_(A.i(lr), A.i(0))
     W, K = max(3, args.warmup), max(1, args.steps)
     Kr = max(3, min(K, args.roofline_steps))
-    nstep_total = W + K + Kr + args.e2e_steps + 2
+    nstep_total = W + K + 2 * Kr + args.e2e_steps + 2
     if args.small:
         cfg = configs.layered_viscoelastic(nstep=nstep_total, nx=32, ny=32, counts=(4, 6, 6))
         workload = "layered viscoelastic 32x32x16 block (reduced)"
@@ -255,18 +289,24 @@ def main():
         g.run(Kr, steps_per_graph=0, timing=True)
         tk = g.last_timing()
     abi.check()
-    total_ms = tm["total_ms"]
-    if dist:
-        import torch
-        t = torch.tensor([total_ms], dtype=torch.float64)
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        total_ms = float(t.item())
-    value = nglob * K * world / (total_ms / 1000.0)
+    from specfem3d_gb300.parallel_host import replica_throughput
+    # whole-job units over the slowest rank's time (replicas: equal work per rank)
+    value = replica_throughput(float(nglob) * K, tm["total_ms"])
+    total_ms = float(nglob) * K * world / value * 1000.0
     stiff_ms = tk["stiffness_ms"] / max(tk["stiffness_launches"], 1)
     bytes_launch = 33000.0 * nspec + 48.0 * nglob
     peak, peak_kind = _peaks()
     achieved = bytes_launch / (stiff_ms / 1000.0) / 1e9
     traffic_pe = _traffic()
+    # 16-bit geometric factors and moduli (per-element scales): stiffness launches
+    # timed the same way; the layered model is represented exactly
+    g.set_geometry_precision(16)
+    g.run(Kr, steps_per_graph=0, timing=True)
+    th = g.last_timing()
+    g.set_geometry_precision(32)
+    abi.check()
+    half_ms = th["stiffness_ms"] / max(th["stiffness_launches"], 1)
+    half_bytes = (33000.0 - 0.5 * (4500.0 + 1000.0)) * nspec + 48.0 * nglob
     rc, maxu = g.check_stability(1e25)
     # ---------------- e2e: per-call C-ABI path, host buffers ----------------
     A = abi.Args()
@@ -277,7 +317,7 @@ def main():
     L.sf3d_synchronize(g.mp)
     t_e2e = time.perf_counter() - t0
     abi.check()
-    e2e_value = nglob * Ke * world / t_e2e
+    e2e_value = replica_throughput(float(nglob) * Ke, t_e2e * 1000.0)
     h2d = 4 * g.nsources
     d2h = 4 * 3 * g.nrec
     g.close()
@@ -292,11 +332,20 @@ def main():
         "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
                      "peak_kind": peak_kind,
                      "traffic": (traffic_pe * nspec if traffic_pe else None),
+                     "traffic_note": ("ncu dram read+write bytes per element of a 16,384-element capture "
+                                      "(profiles/stiffness_kernel_att_6ctas_layered_32x32x16.md) x elements; "
+                                      "the field gathers of that capture stayed in L2"),
                      "kernel": ("stiffness_pipe_kernel<att>" if args.variant == 1 else
                                 f"stiffness_kernel<att, {[4, 0, 5, 6, 7][args.variant]} CTAs/SM>"),
                      "autotune": autotune,
                      "algorithmic_bytes_per_launch": bytes_launch,
                      "mean_launch_ms": stiff_ms, "timed_launches": tk["stiffness_launches"]},
+        "geometry16": {"mean_launch_ms": half_ms, "algorithmic_bytes_per_launch": half_bytes,
+                       "achieved_gbs": half_bytes / (half_ms / 1000.0) / 1e9,
+                       "frac": half_bytes / (half_ms / 1000.0) / 1e9 / peak,
+                       "speedup_vs_fp32_geometry": stiff_ms / half_ms,
+                       "note": "metric and kappa/mu rows in FP16 with per-element (offset, scale); exact "
+                               "for this layered model (rows constant per element)"},
         "e2e": {"value": e2e_value, "unit": UNIT, "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h,
                 "steps": Ke, "path": "per-call FC_FUNC_ entry points"},
         "gpu_launches": tm["total_launches"],
@@ -305,6 +354,8 @@ def main():
         "setup": {"database_s": t_db, "upload_s": t_up},
         "stable": rc == 0,
     }
+    if args.batch > 0:
+        line["batched"] = batch_leg(args.batch, args.batch_steps)
     if args.adjoint > 0:
         line["adjoint"] = adjoint_leg(args.adjoint)
     if rank == 0 and not args.no_cpu:

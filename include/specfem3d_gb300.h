@@ -310,6 +310,13 @@ int sf3d_last_timing(long *Mesh_pointer, float *stiffness_ms, int *stiffness_lau
  * configuration). */
 int sf3d_set_stiffness_variant(long *Mesh_pointer, int variant);
 
+/* Storage of the stiffness kernel's geometric factors and moduli: 32 (FP32,
+ * default) or 16 (FP16 with a per-element (offset, scale) per array; exact for
+ * rows constant over an element, otherwise error <= (max-min)*2^-12 of the
+ * element's range).  Fields and arithmetic stay FP32.  No reference
+ * counterpart (the reference stores CUSTOM_REAL only). */
+int sf3d_set_geometry_precision(long *Mesh_pointer, int bits);
+
 /* Time every stiffness variant over `reps` full passes and keep the fastest.
  * Must run on a wavefield at rest (after prepare_fields_elastic_device, before
  * the first step): zero fields make the passes leave every array unchanged;
@@ -394,6 +401,40 @@ int sf3d_gradient_release(long *Mesh_pointer);
  *     threads) share the scratch and race: serialise them;
  *   - returns after the result is on the host (synchronises `stream`). */
 int sf3d_field_maxabs_noalloc(const realw *d_field, long n, void *stream, realw *max_abs);
+
+/* ------------------------------------------------------------------------
+ * Many shots on one prepared mesh (elastic, no attenuation).  The reference
+ * runs shots as independent simulations (NUMBER_OF_SIMULTANEOUS_RUNS,
+ * parallel.f90:2171-2260); here the shots' wavefields are stacked
+ * shot-innermost and advance together, one stiffness pass per step reading
+ * the mesh once for a tile of shots.  No reference counterpart as calls.
+ * Receivers are the mesh's (prepare_constants_device), shared by all shots. */
+/* Per-shot sources: ispec_selected_source (nshots, 1-based), sourcearrays in the
+ * layout of prepare_constants_device (nshots,3,5,5,5), stf (nshots, nstep) FP64;
+ * seismogram buffer of nlength samples; *device_bytes receives the footprint. */
+int sf3d_batch_prepare(long *Mesh_pointer, int nshots, const int *ispec_selected_source,
+                       const realw *sourcearrays, const double *stf, int nstep, int nlength,
+                       double *device_bytes);
+/* Tiling of the batched stiffness kernel: shots per CTA (1, 2, 4, 8; divides
+ * nshots) x elements per CTA (1, 2, 4) x shots per thread (1, or 4 with 4 or 8
+ * shots per CTA: float4 rows and vector atomics). */
+int sf3d_batch_set_tiling(long *Mesh_pointer, int shots_per_block, int elements_per_block,
+                          int shots_per_thread);
+/* Time every valid tiling over `reps` stiffness passes on wavefields at rest and
+ * keep the fastest; ms_table (24 floats, [shots per thread 1,4] x [shots per CTA
+ * 1,2,4,8] x [elements 1,2,4], -1 where invalid) and the outputs may be NULL. */
+int sf3d_batch_autotune(long *Mesh_pointer, int reps, float *ms_table, int *best_shots_per_block,
+                        int *best_elements_per_block, int *best_shots_per_thread);
+/* Steps it_begin..it_end of all shots, graph-captured in blocks of steps_per_graph. */
+int sf3d_batch_iterate(long *Mesh_pointer, int it_begin, int it_end, realw deltat, int steps_per_graph);
+/* Device time (CUDA events on the compute stream) and launches of the last sf3d_batch_iterate. */
+int sf3d_batch_timing(long *Mesh_pointer, float *total_ms, int *launches);
+/* Displacement seismograms, layout (3, nrec_local, nshots, nlength). */
+int sf3d_batch_get_seismograms(long *Mesh_pointer, realw *h_seismograms);
+/* Stacked displacement, layout (nshots, 3, NGLOB) Fortran order (shot fastest). */
+int sf3d_batch_get_displ(long *Mesh_pointer, realw *h_displ);
+/* Free the batch (also freed by prepare_cleanup_device). */
+int sf3d_batch_release(long *Mesh_pointer);
 
 /* Synchronise the compute stream and report the first stored status. */
 int sf3d_synchronize(long *Mesh_pointer);

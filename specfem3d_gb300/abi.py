@@ -70,6 +70,8 @@ def load() -> ctypes.CDLL:
     L.sf3d_last_timing.argtypes = [P, P, P, P, P]
     L.sf3d_set_stiffness_variant.restype = ctypes.c_int
     L.sf3d_set_stiffness_variant.argtypes = [P, ctypes.c_int]
+    L.sf3d_set_geometry_precision.restype = ctypes.c_int
+    L.sf3d_set_geometry_precision.argtypes = [P, ctypes.c_int]
     L.sf3d_autotune_stiffness.restype = ctypes.c_int
     L.sf3d_autotune_stiffness.argtypes = [P, ctypes.c_int, P, P]
     for name in ("sf3d_gradient_forward", "sf3d_gradient_backward"):
@@ -85,6 +87,22 @@ def load() -> ctypes.CDLL:
     L.sf3d_gradient_release.argtypes = [P]
     L.sf3d_field_maxabs_noalloc.restype = ctypes.c_int
     L.sf3d_field_maxabs_noalloc.argtypes = [P, ctypes.c_long, P, P]
+    L.sf3d_batch_prepare.restype = ctypes.c_int
+    L.sf3d_batch_prepare.argtypes = [P, ctypes.c_int, P, P, P, ctypes.c_int, ctypes.c_int, P]
+    L.sf3d_batch_set_tiling.restype = ctypes.c_int
+    L.sf3d_batch_set_tiling.argtypes = [P, ctypes.c_int, ctypes.c_int, ctypes.c_int]
+    L.sf3d_batch_autotune.restype = ctypes.c_int
+    L.sf3d_batch_autotune.argtypes = [P, ctypes.c_int, P, P, P, P]
+    L.sf3d_batch_iterate.restype = ctypes.c_int
+    L.sf3d_batch_iterate.argtypes = [P, ctypes.c_int, ctypes.c_int, ctypes.c_float, ctypes.c_int]
+    for name in ("sf3d_batch_timing",):
+        getattr(L, name).restype = ctypes.c_int
+        getattr(L, name).argtypes = [P, P, P]
+    for name in ("sf3d_batch_get_seismograms", "sf3d_batch_get_displ"):
+        getattr(L, name).restype = ctypes.c_int
+        getattr(L, name).argtypes = [P, P]
+    L.sf3d_batch_release.restype = ctypes.c_int
+    L.sf3d_batch_release.argtypes = [P]
     L.sf3d_synchronize.restype = ctypes.c_int
     L.sf3d_synchronize.argtypes = [P]
     L.sf3d_device_ptr.restype = P

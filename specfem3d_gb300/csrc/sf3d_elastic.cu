@@ -21,7 +21,7 @@ namespace sf3d {
 
 namespace {
 
-template <bool ATT, bool STRAIN, int MINB>
+template <bool ATT, bool STRAIN, int MINB, bool HALF = false>
 __global__ void __launch_bounds__(NGLL3_PAD, MINB) stiffness_kernel(const StiffnessArgs a) {
   __shared__ float s_gll[NGLL3];
   __shared__ float s_u[3][NGLL3_PAD];
@@ -53,12 +53,27 @@ __global__ void __launch_bounds__(NGLL3_PAD, MINB) stiffness_kernel(const Stiffn
   for (int s = 0; s < NSLS; ++s) fc[s] = fck[s] = 0.f;
   if (active) {
     iglob = __ldg(a.ibool + eo);
-    kap = __ldg(a.kappav + eo);
-    mu = __ldg(a.muv + eo);
-    if (ir >= 0) {
-      const long mo = (long)ir * NGLL3_PAD + t;
+    if (HALF) {
+      // 16-bit storage with a per-element (offset, scale): value = offset + scale * h
+      const float2 ks = __ldg(a.kso + e), ms = __ldg(a.muso + e);
+      kap = fmaf(ks.y, __half2float(a.kh[eo]), ks.x);
+      mu = fmaf(ms.y, __half2float(a.muh[eo]), ms.x);
+      if (ir >= 0) {
+        const long mo = (long)ir * NGLL3_PAD + t;
 #pragma unroll
-      for (int q = 0; q < 9; ++q) m[q] = __ldg(a.m[q] + mo);
+        for (int q = 0; q < 9; ++q) {
+          const float2 so = __ldg(a.mso + (long)q * a.nirr + ir);
+          m[q] = fmaf(so.y, __half2float(a.mh[q][mo]), so.x);
+        }
+      }
+    } else {
+      kap = __ldg(a.kappav + eo);
+      mu = __ldg(a.muv + eo);
+      if (ir >= 0) {
+        const long mo = (long)ir * NGLL3_PAD + t;
+#pragma unroll
+        for (int q = 0; q < 9; ++q) m[q] = __ldg(a.m[q] + mo);
+      }
     }
     if (ATT) {
       const long so = (long)e * (NSLS * NGLL3_PAD) + t;
@@ -252,29 +267,38 @@ __global__ void __launch_bounds__(NGLL3_PAD, MINB) stiffness_kernel(const Stiffn
   }
 }
 
-template <int MINB>
+template <int MINB, bool HALF>
 void launch_minb(const StiffnessArgs& a, bool att, bool store_strain, cudaStream_t s) {
   dim3 grid(a.nelem), block(NGLL3_PAD);
   if (att)
-    stiffness_kernel<true, true, MINB><<<grid, block, 0, s>>>(a);
+    stiffness_kernel<true, true, MINB, HALF><<<grid, block, 0, s>>>(a);
   else if (store_strain)
-    stiffness_kernel<false, true, MINB><<<grid, block, 0, s>>>(a);
+    stiffness_kernel<false, true, MINB, HALF><<<grid, block, 0, s>>>(a);
   else
-    stiffness_kernel<false, false, MINB><<<grid, block, 0, s>>>(a);
+    stiffness_kernel<false, false, MINB, HALF><<<grid, block, 0, s>>>(a);
 }
 
 }  // namespace
 
 // blocks_per_sm: the register budget the kernel is compiled for (4..7 CTAs of
 // 128 threads per SM; more CTAs keep more elements' loads in flight, fewer
-// let the compiler keep every load of an element in registers).
-void launch_stiffness(const StiffnessArgs& a, bool att, bool store_strain, cudaStream_t s, int blocks_per_sm) {
+// let the compiler keep every load of an element in registers).  The 16-bit
+// geometry builds exist for 6 and 7 CTAs/SM.
+void launch_stiffness(const StiffnessArgs& a, bool att, bool store_strain, cudaStream_t s, int blocks_per_sm,
+                      bool half_geometry) {
   if (a.nelem <= 0) return;
+  if (half_geometry) {
+    if (blocks_per_sm == 7)
+      launch_minb<7, true>(a, att, store_strain, s);
+    else
+      launch_minb<6, true>(a, att, store_strain, s);
+    return;
+  }
   switch (blocks_per_sm) {
-    case 5: launch_minb<5>(a, att, store_strain, s); break;
-    case 6: launch_minb<6>(a, att, store_strain, s); break;
-    case 7: launch_minb<7>(a, att, store_strain, s); break;
-    default: launch_minb<4>(a, att, store_strain, s); break;
+    case 5: launch_minb<5, false>(a, att, store_strain, s); break;
+    case 6: launch_minb<6, false>(a, att, store_strain, s); break;
+    case 7: launch_minb<7, false>(a, att, store_strain, s); break;
+    default: launch_minb<4, false>(a, att, store_strain, s); break;
   }
 }
 

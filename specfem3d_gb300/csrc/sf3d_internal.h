@@ -11,6 +11,7 @@
 //     host transfers of the Fortran arrays are plain copies.
 #pragma once
 
+#include <cuda_fp16.h>
 #include <cuda_runtime.h>
 #include <stdint.h>
 
@@ -69,6 +70,25 @@ struct GradState {
   double res_scale = 1.0;      // power of two applied to the residual (undone in sf3d_gradient_get)
   float u_scale = 1.f;         // power of two applied to the forward field in the strain products
   size_t bytes = 0;
+};
+
+// Many shots on one mesh (sf3d_batch_*): wavefields stacked shot-innermost,
+// index (3 * iglob + component) * nshots + shot.
+struct BatchState {
+  int nshots = 0, nstep = 0, nlength = 0;
+  int shots_per_block = 8, elements_per_block = 1;
+  int shots_per_thread = 1;     // 4: vector kernel (shots_per_block 4 or 8)
+  float* displ = nullptr;
+  float* veloc = nullptr;
+  float* accel = nullptr;
+  int* d_ispec_src = nullptr;   // [nshots] 0-based element of each shot's source
+  float* d_sa = nullptr;        // [nshots][128][3] source arrays
+  float* d_stf = nullptr;       // [nstep][nshots]
+  float* d_seismo = nullptr;    // [nlength][nshots][nrec_local][3]
+  int* d_it = nullptr;          // device step counter (1-based)
+  size_t bytes = 0;
+  float last_ms = 0.f;
+  int last_launches = 0;
 };
 
 struct Mesh {
@@ -178,6 +198,7 @@ struct Mesh {
   float* d_scratch = nullptr;             // reduction scratch
   int* d_kerr = nullptr;                  // kernel error word (bounded waits that timed out)
   GradState* grad = nullptr;              // checkpointed adjoint gradient (optional)
+  BatchState* batch = nullptr;            // batched shots (optional)
 
   // MPI interfaces of this slice (inter-slice assembly of accel)
   int num_interfaces = 0, max_nibool_interfaces = 0;
@@ -191,6 +212,14 @@ struct Mesh {
   cudaStream_t copy_stream = nullptr;
   cudaEvent_t ev_pack = nullptr;          // packing done on the compute stream
   int stiffness_variant = 3;              // see variant_blocks_per_sm; 1: persistent bulk-copy pipeline
+  // 16-bit geometry and moduli with per-element affine scales (stiffness kernel only)
+  int geom_half = 0;
+  __half* d_metric_h[9] = {};
+  float2* d_metric_so = nullptr;          // [9][nspec_irr]
+  __half* d_kappa_h = nullptr;
+  __half* d_mu_h = nullptr;
+  float2* d_kappa_so = nullptr;           // [nspec]
+  float2* d_mu_so = nullptr;
 
   cudaStream_t stream = nullptr;
   cudaEvent_t ev0 = nullptr, ev1 = nullptr;
@@ -247,14 +276,25 @@ struct StiffnessArgs {
   const float* fc;
   const float* fck;
   float alpha[NSLS], beta[NSLS], gamma[NSLS];
+  // 16-bit geometry (sf3d_set_geometry_precision): value = offset + scale * half
+  const __half* mh[9];          // [nspec_irr][128]
+  const float2* mso;            // [9][nspec_irr] (offset, scale)
+  const __half* kh;             // [nspec][128]
+  const __half* muh;
+  const float2* kso;            // [nspec]
+  const float2* muso;
+  int nirr;                     // rows of each 16-bit metric array
 };
 
-void launch_stiffness(const StiffnessArgs& a, bool att, bool store_strain, cudaStream_t s, int blocks_per_sm);
+void launch_stiffness(const StiffnessArgs& a, bool att, bool store_strain, cudaStream_t s, int blocks_per_sm,
+                      bool half_geometry = false);
 void launch_stiffness_pipelined(const StiffnessArgs& a, bool att, bool store_strain, int* err, cudaStream_t s);
 // stiffness kernel variants (sf3d_set_stiffness_variant / sf3d_autotune_stiffness)
 constexpr int kNumStiffnessVariants = 5;
 inline int variant_blocks_per_sm(int v) { return v == 0 ? 4 : (v == 2 ? 5 : (v == 3 ? 6 : (v == 4 ? 7 : 0))); }
 void free_grad(Mesh* mp);
+void free_batch(Mesh* mp);
+void free_half_geometry(Mesh* mp);
 // max |x| over n values on the compute stream (NaN if any value is NaN); synchronises
 bool device_maxabs(Mesh* mp, const float* x, long n, float* out);
 // inter-slice assembly buffers (sf3d_assemble.cu)
@@ -271,10 +311,22 @@ inline void default_phase_counts(Mesh* mp) {
 bool check_kernel_error(Mesh* mp);
 // dispatch on Mesh::stiffness_variant
 inline void run_stiffness(Mesh* mp, const StiffnessArgs& a, bool att, bool store_strain, cudaStream_t s) {
-  if (mp->stiffness_variant == 1 && mp->d_kerr)
+  if (mp->geom_half) {
+    // 16-bit geometry: the one-CTA-per-element kernel at 6 or 7 CTAs/SM
+    StiffnessArgs h = a;
+    for (int q = 0; q < 9; ++q) h.mh[q] = mp->d_metric_h[q];
+    h.mso = mp->d_metric_so;
+    h.kh = mp->d_kappa_h;
+    h.muh = mp->d_mu_h;
+    h.kso = mp->d_kappa_so;
+    h.muso = mp->d_mu_so;
+    h.nirr = mp->nspec_irregular;
+    launch_stiffness(h, att, store_strain, s, mp->stiffness_variant == 4 ? 7 : 6, true);
+  } else if (mp->stiffness_variant == 1 && mp->d_kerr) {
     launch_stiffness_pipelined(a, att, store_strain, mp->d_kerr, s);
-  else
+  } else {
     launch_stiffness(a, att, store_strain, s, variant_blocks_per_sm(mp->stiffness_variant));
+  }
 }
 void launch_pressure_seismograms(Mesh* mp, int slot);
 // one fused forward elastic step of sf3d_iterate_time (predictor fused with the

@@ -523,6 +523,8 @@ void prepare_cleanup_device_(long* Mesh_pointer, int* ACOUSTIC_SIMULATION, int* 
   cudaFree(mp->d_cp_pt); cudaFree(mp->d_cp_normal); cudaFree(mp->d_cp_jw); cudaFree(mp->d_seismo_p);
   cudaFree(mp->d_rec_is_acoustic);
   free_grad(mp);
+  free_batch(mp);
+  free_half_geometry(mp);
   free_interfaces(mp);
   cudaFree(mp->d_it); cudaFree(mp->d_done); cudaFree(mp->d_scratch); cudaFree(mp->d_kerr); cudaFree(mp->d_stage);
   if (mp->ev0) cudaEventDestroy(mp->ev0);

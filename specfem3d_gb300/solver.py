@@ -294,6 +294,11 @@ class GPUSolver:
         if self.L.sf3d_set_stiffness_variant(self.mp, int(variant)) != 0:
             abi.check()
 
+    def set_geometry_precision(self, bits: int):
+        """32: FP32 geometry and moduli; 16: FP16 with per-element (offset, scale)."""
+        if self.L.sf3d_set_geometry_precision(self.mp, int(bits)) != 0:
+            abi.check()
+
     def check_stability(self, threshold: float = 1e25):
         m = ctypes.c_float()
         rc = self.L.sf3d_check_stability(self.mp, float(threshold), ctypes.addressof(m))
