@@ -271,7 +271,7 @@ def main():
         autotune = None
     else:
         # fields are at rest: time every stiffness variant and keep the fastest
-        ms = (ctypes.c_float * 5)()
+        ms = (ctypes.c_float * 8)()
         best = ctypes.c_int()
         if L.sf3d_autotune_stiffness(g.mp, 3, ms, ctypes.addressof(best)) != 0:
             abi.check()
@@ -321,6 +321,15 @@ def main():
     h2d = 4 * g.nsources
     d2h = 4 * 3 * g.nrec
     g.close()
+    # atomic-free assembly by mesh colouring (8 parity colours of the block), timed the
+    # same way, to choose between red.global atomics and colouring by measurement
+    gc = solver.GPUSolver(db, cfg, nlength=1, colors=meshgen.block_colors(cfg))
+    gc.run(W, steps_per_graph=args.graph)
+    gc.run(Kr, steps_per_graph=0, timing=True)
+    tc = gc.last_timing()
+    gc.close()
+    abi.check()
+    color_ms = tc["stiffness_ms"] / max(tc["stiffness_launches"], 1)
     del db
     line = {
         "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": K, "warmup": W,
@@ -336,7 +345,8 @@ def main():
                                       "(profiles/stiffness_kernel_att_6ctas_layered_32x32x16.md) x elements; "
                                       "the field gathers of that capture stayed in L2"),
                      "kernel": ("stiffness_pipe_kernel<att>" if args.variant == 1 else
-                                f"stiffness_kernel<att, {[4, 0, 5, 6, 7][args.variant]} CTAs/SM>"),
+                                f"stiffness_kernel<att, {[4, 0, 5, 6, 7, 6, 7, 8][args.variant]} CTAs/SM"
+                                + (", cp.async-staged memory variables>" if args.variant >= 5 else ">")),
                      "autotune": autotune,
                      "algorithmic_bytes_per_launch": bytes_launch,
                      "mean_launch_ms": stiff_ms, "timed_launches": tk["stiffness_launches"]},
@@ -346,6 +356,9 @@ def main():
                        "speedup_vs_fp32_geometry": stiff_ms / half_ms,
                        "note": "metric and kappa/mu rows in FP16 with per-element (offset, scale); exact "
                                "for this layered model (rows constant per element)"},
+        "assembly": {"atomic_stiffness_ms": stiff_ms, "colored_stiffness_ms": color_ms,
+                     "chosen": "atomic" if stiff_ms <= color_ms else "colored",
+                     "note": "colored: 8 launches per step (one per colour), plain read-modify-write scatter"},
         "e2e": {"value": e2e_value, "unit": UNIT, "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h,
                 "steps": Ke, "path": "per-call FC_FUNC_ entry points"},
         "gpu_launches": tm["total_launches"],

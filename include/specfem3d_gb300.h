@@ -304,7 +304,10 @@ int sf3d_last_timing(long *Mesh_pointer, float *stiffness_ms, int *stiffness_lau
  * arithmetic in the same order:
  *   0, 2, 3, 4: one 128-thread CTA per element, compiled for 4, 5, 6, 7
  *               resident CTAs per SM (register budget 128, 96, 80, 72);
- *   1:          persistent CTAs fed by a three-stage bulk-copy (TMA) pipeline.
+ *   1:          persistent CTAs fed by a three-stage bulk-copy (TMA) pipeline;
+ *   5, 6, 7:    one CTA per element with the memory variables, strains and
+ *               attenuation factors staged in shared memory by cp.async, for
+ *               6, 7, 8 CTAs per SM (register budget 80, 72, 64).
  * Default 3 (the fastest on GB300 for the layered viscoelastic workload).
  * No reference counterpart (the reference compiles one Kernel_2 per
  * configuration). */
@@ -320,7 +323,7 @@ int sf3d_set_geometry_precision(long *Mesh_pointer, int bits);
 /* Time every stiffness variant over `reps` full passes and keep the fastest.
  * Must run on a wavefield at rest (after prepare_fields_elastic_device, before
  * the first step): zero fields make the passes leave every array unchanged;
- * returns SF3D_ERR_STATE otherwise.  ms_per_variant (5 floats) and
+ * returns SF3D_ERR_STATE otherwise.  ms_per_variant (8 floats) and
  * best_variant may be NULL.  No reference counterpart. */
 int sf3d_autotune_stiffness(long *Mesh_pointer, int reps, float *ms_per_variant, int *best_variant);
 

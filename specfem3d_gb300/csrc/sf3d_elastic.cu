@@ -21,8 +21,19 @@ namespace sf3d {
 
 namespace {
 
-template <bool ATT, bool STRAIN, int MINB, bool HALF = false>
+__device__ __forceinline__ void cp_async16(void* smem, const void* gmem) {
+  asm volatile("cp.async.cg.shared.global [%0], [%1], 16;" ::"r"(static_cast<unsigned>(__cvta_generic_to_shared(smem))),
+               "l"(gmem)
+               : "memory");
+}
+
+// STAGE (attenuation only): the 30 memory-variable / strain / factor rows of the
+// element (15 KB) are copied into shared memory with cp.async instead of being
+// held in registers from the start of the kernel to the end, so the kernel fits
+// a smaller register budget (more resident CTAs per SM).
+template <bool ATT, bool STRAIN, int MINB, bool HALF = false, bool STAGE = false, bool ATOMIC = true>
 __global__ void __launch_bounds__(NGLL3_PAD, MINB) stiffness_kernel(const StiffnessArgs a) {
+  __shared__ __align__(16) float s_att[(ATT && STAGE) ? 30 : 1][NGLL3_PAD];
   __shared__ float s_gll[NGLL3];
   __shared__ float s_u[3][NGLL3_PAD];
   __shared__ float s_v[ATT ? 3 : 1][NGLL3_PAD];
@@ -51,6 +62,21 @@ __global__ void __launch_bounds__(NGLL3_PAD, MINB) stiffness_kernel(const Stiffn
   }
 #pragma unroll
   for (int s = 0; s < NSLS; ++s) fc[s] = fck[s] = 0.f;
+  if (ATT && STAGE) {
+    // rows: R[c][s] -> 3c+s (0..17), epsilondev[c] -> 18+c, factor_common[s] -> 24+s,
+    // factor_common_kappa[s] -> 27+s; 32 chunks of 16 B per row
+    const long se = (long)e * (NSLS * NGLL3_PAD), ee = (long)e * NGLL3_PAD;
+    for (int q = t; q < 30 * 32; q += NGLL3_PAD) {
+      const int row = q >> 5, col = (q & 31) * 4;
+      const float* src;
+      if (row < 18) src = a.R[row / 3] + se + (row % 3) * NGLL3_PAD;
+      else if (row < 24) src = a.eps[row - 18] + ee;
+      else if (row < 27) src = a.fc + se + (row - 24) * NGLL3_PAD;
+      else src = a.fck + se + (row - 27) * NGLL3_PAD;
+      cp_async16(&s_att[row][col], src + col);
+    }
+    asm volatile("cp.async.commit_group;" ::: "memory");
+  }
   if (active) {
     iglob = __ldg(a.ibool + eo);
     if (HALF) {
@@ -75,7 +101,7 @@ __global__ void __launch_bounds__(NGLL3_PAD, MINB) stiffness_kernel(const Stiffn
         for (int q = 0; q < 9; ++q) m[q] = __ldg(a.m[q] + mo);
       }
     }
-    if (ATT) {
+    if (ATT && !STAGE) {
       const long so = (long)e * (NSLS * NGLL3_PAD) + t;
 #pragma unroll
       for (int c = 0; c < 6; ++c)
@@ -99,6 +125,7 @@ __global__ void __launch_bounds__(NGLL3_PAD, MINB) stiffness_kernel(const Stiffn
     }
   }
   if (t < NGLL3) s_gll[t] = __ldg(a.gll + t);
+  if (ATT && STAGE) asm volatile("cp.async.wait_all;" ::: "memory");
   s_u[0][t] = ux;
   s_u[1][t] = uy;
   s_u[2][t] = uz;
@@ -193,7 +220,8 @@ __global__ void __launch_bounds__(NGLL3_PAD, MINB) stiffness_kernel(const Stiffn
     if (ATT) {
       float sR[6];
 #pragma unroll
-      for (int c = 0; c < 6; ++c) sR[c] = R[c][0] + R[c][1] + R[c][2];
+      for (int c = 0; c < 6; ++c)
+        sR[c] = STAGE ? s_att[3 * c][t] + s_att[3 * c + 1][t] + s_att[3 * c + 2][t] : R[c][0] + R[c][1] + R[c][2];
       sig_xx = sig_xx - sR[0] - sR[5];
       sig_yy = sig_yy - sR[1] - sR[5];
       sig_zz = sig_zz + sR[0] + sR[1] - sR[5];
@@ -241,21 +269,36 @@ __global__ void __launch_bounds__(NGLL3_PAD, MINB) stiffness_kernel(const Stiffn
     const float ax = fac1 * n1x + fac2 * n2x + fac3 * n3x;
     const float ay = fac1 * n1y + fac2 * n2y + fac3 * n3y;
     const float az = fac1 * n1z + fac2 * n2z + fac3 * n3z;
-    atomicAdd(a.accel + 3L * iglob, -ax);
-    atomicAdd(a.accel + 3L * iglob + 1, -ay);
-    atomicAdd(a.accel + 3L * iglob + 2, -az);
+    if (ATOMIC) {
+      atomicAdd(a.accel + 3L * iglob, -ax);
+      atomicAdd(a.accel + 3L * iglob + 1, -ay);
+      atomicAdd(a.accel + 3L * iglob + 2, -az);
+    } else {
+      // one colour: no other element of this launch touches iglob
+      a.accel[3L * iglob] -= ax;
+      a.accel[3L * iglob + 1] -= ay;
+      a.accel[3L * iglob + 2] -= az;
+    }
 
     if (ATT) {
       const long so = (long)e * (NSLS * NGLL3_PAD) + t;
       const float fkap = kap, fmu = mu;
+      if (STAGE) {
+#pragma unroll
+        for (int c = 0; c < 6; ++c) eold[c] = s_att[18 + c][t];
+      }
 #pragma unroll
       for (int s = 0; s < NSLS; ++s) {
         const float al = a.alpha[s], be = a.beta[s], ga = a.gamma[s];
-        const float fk = fkap * fck[s];
-        a.R[5][so + s * NGLL3_PAD] = al * R[5][s] + fk * (be * eold[5] + ga * epsl[5]);
-        const float fm = fmu * fc[s];
+        const float fk = fkap * (STAGE ? s_att[27 + s][t] : fck[s]);
+        const float r5 = STAGE ? s_att[15 + s][t] : R[5][s];
+        a.R[5][so + s * NGLL3_PAD] = al * r5 + fk * (be * eold[5] + ga * epsl[5]);
+        const float fm = fmu * (STAGE ? s_att[24 + s][t] : fc[s]);
 #pragma unroll
-        for (int c = 0; c < 5; ++c) a.R[c][so + s * NGLL3_PAD] = al * R[c][s] + fm * (be * eold[c] + ga * epsl[c]);
+        for (int c = 0; c < 5; ++c) {
+          const float rc = STAGE ? s_att[3 * c + s][t] : R[c][s];
+          a.R[c][so + s * NGLL3_PAD] = al * rc + fm * (be * eold[c] + ga * epsl[c]);
+        }
       }
     }
     if (STRAIN) {
@@ -267,11 +310,11 @@ __global__ void __launch_bounds__(NGLL3_PAD, MINB) stiffness_kernel(const Stiffn
   }
 }
 
-template <int MINB, bool HALF>
+template <int MINB, bool HALF, bool STAGE = false>
 void launch_minb(const StiffnessArgs& a, bool att, bool store_strain, cudaStream_t s) {
   dim3 grid(a.nelem), block(NGLL3_PAD);
   if (att)
-    stiffness_kernel<true, true, MINB, HALF><<<grid, block, 0, s>>>(a);
+    stiffness_kernel<true, true, MINB, HALF, STAGE><<<grid, block, 0, s>>>(a);
   else if (store_strain)
     stiffness_kernel<false, true, MINB, HALF><<<grid, block, 0, s>>>(a);
   else
@@ -285,8 +328,19 @@ void launch_minb(const StiffnessArgs& a, bool att, bool store_strain, cudaStream
 // let the compiler keep every load of an element in registers).  The 16-bit
 // geometry builds exist for 6 and 7 CTAs/SM.
 void launch_stiffness(const StiffnessArgs& a, bool att, bool store_strain, cudaStream_t s, int blocks_per_sm,
-                      bool half_geometry) {
+                      bool half_geometry, bool staged) {
   if (a.nelem <= 0) return;
+  if (staged) {
+    // cp.async-staged memory variables (attenuation); without attenuation the
+    // same register budgets of the plain build
+    if (blocks_per_sm == 8)
+      launch_minb<8, false, true>(a, att, store_strain, s);
+    else if (blocks_per_sm == 7)
+      launch_minb<7, false, true>(a, att, store_strain, s);
+    else
+      launch_minb<6, false, true>(a, att, store_strain, s);
+    return;
+  }
   if (half_geometry) {
     if (blocks_per_sm == 7)
       launch_minb<7, true>(a, att, store_strain, s);
@@ -300,6 +354,17 @@ void launch_stiffness(const StiffnessArgs& a, bool att, bool store_strain, cudaS
     case 7: launch_minb<7, false>(a, att, store_strain, s); break;
     default: launch_minb<4, false>(a, att, store_strain, s); break;
   }
+}
+
+void launch_stiffness_colored(const StiffnessArgs& a, bool att, bool store_strain, cudaStream_t s) {
+  if (a.nelem <= 0) return;
+  dim3 grid(a.nelem), block(NGLL3_PAD);
+  if (att)
+    stiffness_kernel<true, true, 6, false, false, false><<<grid, block, 0, s>>>(a);
+  else if (store_strain)
+    stiffness_kernel<false, true, 6, false, false, false><<<grid, block, 0, s>>>(a);
+  else
+    stiffness_kernel<false, false, 6, false, false, false><<<grid, block, 0, s>>>(a);
 }
 
 }  // namespace sf3d

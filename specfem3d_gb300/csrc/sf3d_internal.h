@@ -114,6 +114,11 @@ struct Mesh {
   // phases: [2][num_phase_ispec] 0-based element lists
   int num_phase_ispec = 0;
   int phase_valid[2] = {0, 0};           // leading in-range entries of each phase column
+  // mesh colouring (USE_MESH_COLORING_GPU): phase lists ordered by colour, no two
+  // elements of a colour share a point, so a colour's scatter needs no atomics
+  int use_mesh_coloring = 0;
+  int num_colors_outer = 0, num_colors_inner = 0;
+  std::vector<int> elem_colors;          // elements per colour, outer colours first
   int nspec_outer = 0, nspec_inner = 0;
   int* d_phase_ispec = nullptr;
 
@@ -284,14 +289,21 @@ struct StiffnessArgs {
   const float2* kso;            // [nspec]
   const float2* muso;
   int nirr;                     // rows of each 16-bit metric array
+  int nonatomic;                // 1: the elements of this launch share no point (one colour)
 };
 
 void launch_stiffness(const StiffnessArgs& a, bool att, bool store_strain, cudaStream_t s, int blocks_per_sm,
-                      bool half_geometry = false);
+                      bool half_geometry = false, bool staged = false);
 void launch_stiffness_pipelined(const StiffnessArgs& a, bool att, bool store_strain, int* err, cudaStream_t s);
 // stiffness kernel variants (sf3d_set_stiffness_variant / sf3d_autotune_stiffness)
-constexpr int kNumStiffnessVariants = 5;
-inline int variant_blocks_per_sm(int v) { return v == 0 ? 4 : (v == 2 ? 5 : (v == 3 ? 6 : (v == 4 ? 7 : 0))); }
+//   0, 2, 3, 4: one CTA per element at 4, 5, 6, 7 CTAs/SM; 1: persistent bulk-copy pipeline;
+//   5, 6, 7: one CTA per element with cp.async-staged memory variables at 6, 7, 8 CTAs/SM
+constexpr int kNumStiffnessVariants = 8;
+inline int variant_blocks_per_sm(int v) {
+  const int t[kNumStiffnessVariants] = {4, 0, 5, 6, 7, 6, 7, 8};
+  return (v >= 0 && v < kNumStiffnessVariants) ? t[v] : 4;
+}
+inline bool variant_staged(int v) { return v >= 5; }
 void free_grad(Mesh* mp);
 void free_batch(Mesh* mp);
 void free_half_geometry(Mesh* mp);
@@ -310,7 +322,29 @@ inline void default_phase_counts(Mesh* mp) {
 // reads and clears the kernel error word; false (and a stored error) if set
 bool check_kernel_error(Mesh* mp);
 // dispatch on Mesh::stiffness_variant
+void launch_stiffness_colored(const StiffnessArgs& a, bool att, bool store_strain, cudaStream_t s);
+inline void run_stiffness(Mesh* mp, const StiffnessArgs& a, bool att, bool store_strain, cudaStream_t s);
+// iphase's elements colour by colour with plain read-modify-write assembly
+inline bool run_stiffness_by_color(Mesh* mp, const StiffnessArgs& a, int iphase, bool att, bool store_strain,
+                                   cudaStream_t s) {
+  if (!mp->use_mesh_coloring || mp->elem_colors.empty() || !a.phase) return false;
+  const int c0 = iphase == 1 ? 0 : mp->num_colors_outer;
+  const int c1 = iphase == 1 ? mp->num_colors_outer : mp->num_colors_outer + mp->num_colors_inner;
+  int off = 0;
+  for (int c = c0; c < c1 && off < a.nelem; ++c) {
+    StiffnessArgs b = a;
+    b.phase = a.phase + off;
+    b.nelem = mp->elem_colors[c] < a.nelem - off ? mp->elem_colors[c] : a.nelem - off;
+    launch_stiffness_colored(b, att, store_strain, s);
+    off += mp->elem_colors[c];
+  }
+  return true;
+}
 inline void run_stiffness(Mesh* mp, const StiffnessArgs& a, bool att, bool store_strain, cudaStream_t s) {
+  if (mp->use_mesh_coloring && !mp->geom_half && a.phase && mp->d_phase_ispec) {
+    const int iphase = a.phase == mp->d_phase_ispec ? 1 : 2;
+    if (run_stiffness_by_color(mp, a, iphase, att, store_strain, s)) return;
+  }
   if (mp->geom_half) {
     // 16-bit geometry: the one-CTA-per-element kernel at 6 or 7 CTAs/SM
     StiffnessArgs h = a;
@@ -325,7 +359,8 @@ inline void run_stiffness(Mesh* mp, const StiffnessArgs& a, bool att, bool store
   } else if (mp->stiffness_variant == 1 && mp->d_kerr) {
     launch_stiffness_pipelined(a, att, store_strain, mp->d_kerr, s);
   } else {
-    launch_stiffness(a, att, store_strain, s, variant_blocks_per_sm(mp->stiffness_variant));
+    launch_stiffness(a, att, store_strain, s, variant_blocks_per_sm(mp->stiffness_variant), false,
+                     variant_staged(mp->stiffness_variant));
   }
 }
 void launch_pressure_seismograms(Mesh* mp, int slot);

@@ -242,7 +242,7 @@ void prepare_constants_device_(long* Mesh_pointer, int* h_NGLLX, int* NSPEC_AB, 
                                int* SAVE_SEISMOGRAMS_ACCELERATION, int* SAVE_SEISMOGRAMS_PRESSURE,
                                int* h_NB_RUNS_ACOUSTIC_GPU, int* FAULT_SIMULATION,
                                int* UNDO_ATTENUATION_AND_OR_PML, int* PML_CONDITIONS) {
-  (void)h_ispec_is_inner; (void)USE_MESH_COLORING_GPU_f;
+  (void)h_ispec_is_inner;
   (void)nspec_elastic; (void)ispec_is_elastic;
   (void)FAULT_SIMULATION; (void)UNDO_ATTENUATION_AND_OR_PML; (void)nu_source;
   if (!Mesh_pointer) { set_error(SF3D_ERR_ARG, "Mesh_pointer is NULL"); return; }
@@ -258,6 +258,7 @@ void prepare_constants_device_(long* Mesh_pointer, int* h_NGLLX, int* NSPEC_AB, 
     return;
   }
   Mesh* mp = new Mesh();
+  mp->use_mesh_coloring = USE_MESH_COLORING_GPU_f ? *USE_MESH_COLORING_GPU_f : 0;
   const long nspec = *NSPEC_AB;
   mp->nspec = (int)nspec;
   mp->nglob = *NGLOB_AB;
@@ -433,7 +434,6 @@ void prepare_fields_elastic_device_(long* Mesh_pointer, realw* rmassx, realw* rm
                                     realw* c56store, realw* c66store) {
   (void)b_absorb_field; (void)b_reclen_field; (void)R_size; (void)rmass_ocean_load; (void)free_surface_normal;
   (void)free_surface_ispec; (void)free_surface_ijk; (void)num_free_surface_faces; (void)ACOUSTIC_SIMULATION;
-  (void)num_colors_outer_elastic; (void)num_colors_inner_elastic; (void)num_elem_colors_elastic;
   (void)c11store; (void)c12store; (void)c13store; (void)c14store; (void)c15store; (void)c16store;
   (void)c22store; (void)c23store; (void)c24store; (void)c25store; (void)c26store; (void)c33store;
   (void)c34store; (void)c35store; (void)c36store; (void)c44store; (void)c45store; (void)c46store;
@@ -475,6 +475,28 @@ void prepare_fields_elastic_device_(long* Mesh_pointer, realw* rmassx, realw* rm
       mp->phase_valid[c] = n;
     }
     if (ok) ok = copy_in((void**)&mp->d_phase_ispec, ph.data(), sizeof(int) * ph.size(), s);
+  }
+  // colours: num_elem_colors_elastic(num_colors_outer + num_colors_inner), the
+  // phase lists ordered colour by colour (outer colours for phase 1, inner for phase 2)
+  if (ok && mp->use_mesh_coloring) {
+    const int nco = num_colors_outer_elastic ? *num_colors_outer_elastic : 0;
+    const int nci = num_colors_inner_elastic ? *num_colors_inner_elastic : 0;
+    if (nco < 0 || nci < 0 || (nco + nci > 0 && !num_elem_colors_elastic)) {
+      ok = set_error(SF3D_ERR_ARG, "invalid mesh colouring arguments");
+    } else {
+      long so = 0, si = 0;
+      for (int c = 0; c < nco + nci; ++c) {
+        if (num_elem_colors_elastic[c] < 0) ok = set_error(SF3D_ERR_ARG, "negative colour size");
+        (c < nco ? so : si) += num_elem_colors_elastic[c];
+      }
+      if (ok && (so > mp->phase_valid[0] || si > mp->phase_valid[1]))
+        ok = set_error(SF3D_ERR_ARG, "colour sizes exceed the phase element lists");
+      if (ok) {
+        mp->num_colors_outer = nco;
+        mp->num_colors_inner = nci;
+        mp->elem_colors.assign(num_elem_colors_elastic, num_elem_colors_elastic + nco + nci);
+      }
+    }
   }
   mp->compute_and_store_strain = *COMPUTE_AND_STORE_STRAIN;
   mp->attenuation = *ATTENUATION;

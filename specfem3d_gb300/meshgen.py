@@ -571,3 +571,29 @@ def stf_table(cfg: dict):
         t0 = float(cfg["t0"])
     t = (np.arange(nstep) * dt) - t0
     return np.stack([stf_value(k, t - ts, p) for k, p, ts in zip(kinds, params, tsh)]), t0
+
+
+def block_colors(cfg: dict) -> np.ndarray:
+    """Colour of every element of a block mesh such that no two elements of a colour
+    share a GLL point: the parity of the element indices along x, y, z (8 colours).
+    Plays the part of get_perm_color (generate_databases) for structured blocks."""
+    B = Block(cfg)
+    e = np.arange(B.nspec)
+    ex, ey, ez = B.elem_xyz(e)
+    return ((ex % 2) + 2 * (ey % 2) + 4 * (ez % 2)).astype(np.int32)
+
+
+def greedy_colors(ibool: np.ndarray, nspec: int, nglob: int) -> np.ndarray:
+    """First-fit colouring of elements through shared points (any mesh): element e
+    takes the lowest colour not used by an element sharing one of its points."""
+    ib = np.asarray(ibool).reshape(nspec, -1) - 1
+    used = np.zeros(nglob, np.uint64)          # bit c set: colour c already touches the point
+    col = np.zeros(nspec, np.int32)
+    for e in range(nspec):
+        m = np.bitwise_or.reduce(used[ib[e]])
+        c = 0
+        while (int(m) >> c) & 1:
+            c += 1
+        col[e] = c
+        used[ib[e]] |= np.uint64(1 << c)
+    return col

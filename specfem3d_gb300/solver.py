@@ -24,7 +24,11 @@ N_SLS = 3
 
 class GPUSolver:
     def __init__(self, db: dict, cfg: dict, nlength: int | None = None, simulation_type: int = 1,
-                 save_forward: bool = False, record=("displ",)):
+                 save_forward: bool = False, record=("displ",), colors=None):
+        """colors: optional colour per element (no two elements of a colour share a
+        point, e.g. meshgen.block_colors); the phase lists are then ordered colour by
+        colour and USE_MESH_COLORING_GPU is set, so assembly runs without atomics."""
+        self.colors = None if colors is None else np.asarray(colors, np.int32)
         self.L = abi.load()
         self.db, self.cfg = db, cfg
         self.nspec, self.nglob = int(db["nspec"]), int(db["nglob"])
@@ -74,7 +78,8 @@ class GPUSolver:
             A.i(int(db["num_abs_boundary_faces"]) if db.get("stacey", 1) else 0),
             A.ai(np.ones(nspec, np.int32)), A.i(self.nsources), A.i(self.nsources), A.af(db["sourcearrays"]),
             A.ai(np.zeros(max(self.nsources, 1), np.int32)), A.ai(db["ispec_selected_source"]),
-            A.ai(db["ispec_selected_rec"]), A.i(nrec), A.i(nrec), A.i(self.simulation_type), A.i(0),
+            A.ai(db["ispec_selected_rec"]), A.i(nrec), A.i(nrec), A.i(self.simulation_type),
+            A.i(int(self.colors is not None)),
             A.i(int(self.isac.sum())), A.i(int(nspec - self.isac.sum())), A.ai(self.isac), A.ai(1 - self.isac),
             A.i(0), A.i(int(save_forward)), A.af(hx), A.af(he), A.af(hg), A.ad(nu), A.ad(nu),
             A.ai(np.zeros(max(nrec, 1), np.int32)), A.i(self.nlength),
@@ -92,6 +97,19 @@ class GPUSolver:
         solid = np.nonzero(self.isac == 0)[0] + 1
         outer = np.asarray(db.get("phase_outer", np.zeros(0, np.int32)), np.int32)
         inner = np.setdiff1d(solid, outer).astype(np.int32)
+        ncol_out = ncol_in = 0
+        elem_colors = None
+        if self.colors is not None:
+            # get_perm_color order: outer elements colour by colour, then inner ones
+            counts = []
+            for lst in (outer, inner):
+                c = self.colors[lst - 1]
+                order = np.argsort(c, kind="stable")
+                lst[:] = lst[order]
+                u, n = np.unique(c, return_counts=True)
+                counts.append(n.astype(np.int32))
+            ncol_out, ncol_in = len(counts[0]), len(counts[1])
+            elem_colors = np.concatenate(counts).astype(np.int32)
         self.nspec_outer, self.nspec_elastic = len(outer), len(inner)
         phase = np.zeros((max(len(outer), len(inner), 1), 2), np.int32)
         phase[:len(outer), 0] = outer
@@ -109,7 +127,8 @@ class GPUSolver:
             A.af(zsls), A.af(zeps), A.af(db.get("factor_common_kappa") if att else None),
             A.af(db.get("alphaval", np.zeros(3))), A.af(db.get("betaval", np.zeros(3))),
             A.af(db.get("gammaval", np.zeros(3))), A.i(0), A.af(None), A.i(0), A.af(None), A.ai(None), A.ai(None),
-            A.i(0), A.i(0), A.i(0), A.i(0), A.ai(None), A.i(0), *(A.af(None) for _ in range(21)),
+            A.i(0), A.i(0), A.i(ncol_out), A.i(ncol_in), A.ai(elem_colors), A.i(0),
+            *(A.af(None) for _ in range(21)),
         ]
         self.L.prepare_fields_elastic_device_(*args)
         abi.check()

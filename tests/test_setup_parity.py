@@ -100,3 +100,19 @@ def test_perturbation_model_bounds():
     solid = vs > 0
     assert np.all(np.abs(vp[solid] / 3000.0 - 1) <= 0.0500001)
     assert np.all(vp[~solid] == 1500.0)
+
+
+@pytest.mark.parametrize("kind", ["block", "greedy"])
+def test_element_colouring_is_conflict_free(kind):
+    """No two elements of one colour share a GLL point (the condition for the
+    atomic-free assembly of USE_MESH_COLORING_GPU)."""
+    from specfem3d_gb300 import configs, meshgen
+    cfg = configs.small_layered(nx=6, ny=5, counts=(2, 2, 3), nstep=4)
+    db = meshgen.build_database(cfg)
+    n = db["nspec"]
+    col = meshgen.block_colors(cfg) if kind == "block" else meshgen.greedy_colors(db["ibool"], n, db["nglob"])
+    ib = db["ibool"].reshape(n, 125)
+    for c in np.unique(col):
+        pts = ib[col == c].reshape(-1)
+        assert len(np.unique(pts)) == len(pts), c
+    assert col.max() + 1 <= (8 if kind == "block" else 27)
