@@ -113,17 +113,20 @@ class ClockSampler:
         return {"sm_mhz": float(np.median(sm)), "sm_max_mhz": float(max(smax)), "reasons": sorted(reasons)}
 
 
-def cpu_baseline(steps: int, nthreads: int):
+WORKLOAD = "layered viscoelastic 20x20x10 km, 128x128x64 hexes, N_SLS=3, Stacey 5 faces"
+
+
+def cpu_baseline(steps: int, nthreads: int, warmup: int = 1):
     """Oracle (FP32, OpenMP) on a bounded sample with the bench physics: a 32x32x16
     block of the same layered viscoelastic model (irregular elements, Stacey)."""
     from oracle import oracle as O
     from specfem3d_gb300 import configs, meshgen
-    cfg = configs.layered_viscoelastic(nstep=steps + 2, nx=32, ny=32, counts=(4, 6, 6))
+    cfg = configs.layered_viscoelastic(nstep=steps + warmup + 2, nx=32, ny=32, counts=(4, 6, 6))
     cfg["x1"] = 20000.0 * 32 / 128
     cfg["y1"] = 20000.0 * 32 / 128
     db = meshgen.build_database(cfg)
     sim = O.make_sim(db, cfg, "f32", nthreads=nthreads)
-    sim.step(1)
+    sim.step(max(1, warmup))
     t = time.perf_counter()
     sim.step(steps)
     dt = time.perf_counter() - t
@@ -197,13 +200,16 @@ def run_reference(args, rank):
         return 0
     nthreads = os.cpu_count() or 1
     steps = max(1, args.steps)
-    val, info = cpu_baseline(steps, nthreads)
+    val, info = cpu_baseline(steps, nthreads, warmup=max(1, args.warmup))
     sample = (f"CPU oracle (C restatement of the reference CPU solver, not the reference binary) on a "
-              f"32x32x16-element block with the bench physics ({info['nglob']} points), {steps} steps")
+              f"32x32x16-element block with the bench physics ({info['nglob']} points), {steps} steps "
+              f"after {max(1, args.warmup)} warm-up steps; the reference's Fortran solver cannot be built "
+              f"(no Fortran compiler or MPI)")
     line = {"metric": METRIC, "value": val, "unit": UNIT, "n_gpus": args.gpus, "steps": steps,
             "warmup": args.warmup, "ms_per_step": 1000 * info["seconds"] / steps, "higher_is_better": True,
             "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
-            "config": {"workload": "layered viscoelastic block, CPU sample", "sample_elements": info["nspec"]},
+            "config": {"workload": WORKLOAD, "cpu_sample_elements": info["nspec"],
+                       "cpu_sample_points": info["nglob"]},
             "impl": "reference",
             "cpu_baseline": {"value": val, "unit": UNIT, "cores": nthreads, "kind": "port", "sample": sample},
             "e2e": {"value": val, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
@@ -257,7 +263,7 @@ def main():
         workload = "layered viscoelastic 32x32x16 block (reduced)"
     else:
         cfg = configs.layered_viscoelastic(nstep=nstep_total)
-        workload = "layered viscoelastic 20x20x10 km, 128x128x64 hexes, N_SLS=3, Stacey 5 faces"
+        workload = WORKLOAD
     t0 = time.perf_counter()
     db = meshgen.build_database(cfg)
     t_db = time.perf_counter() - t0

@@ -21,16 +21,16 @@ namespace sf3d {
 
 namespace {
 
-__device__ __forceinline__ void cp_async16(void* smem, const void* gmem) {
-  asm volatile("cp.async.cg.shared.global [%0], [%1], 16;" ::"r"(static_cast<unsigned>(__cvta_generic_to_shared(smem))),
+__device__ __forceinline__ void cp_async4(void* smem, const void* gmem) {
+  asm volatile("cp.async.ca.shared.global [%0], [%1], 4;" ::"r"(static_cast<unsigned>(__cvta_generic_to_shared(smem))),
                "l"(gmem)
                : "memory");
 }
 
-// STAGE (attenuation only): the 30 memory-variable / strain / factor rows of the
-// element (15 KB) are copied into shared memory with cp.async instead of being
-// held in registers from the start of the kernel to the end, so the kernel fits
-// a smaller register budget (more resident CTAs per SM).
+// STAGE (attenuation only): the 30 memory-variable / strain / factor values of
+// each point (15 KB per element) are copied into shared memory with cp.async
+// instead of being held in registers from the start of the kernel to the end,
+// so the kernel fits a smaller register budget (more resident CTAs per SM).
 template <bool ATT, bool STRAIN, int MINB, bool HALF = false, bool STAGE = false, bool ATOMIC = true>
 __global__ void __launch_bounds__(NGLL3_PAD, MINB) stiffness_kernel(const StiffnessArgs a) {
   __shared__ __align__(16) float s_att[(ATT && STAGE) ? 30 : 1][NGLL3_PAD];
@@ -62,18 +62,20 @@ __global__ void __launch_bounds__(NGLL3_PAD, MINB) stiffness_kernel(const Stiffn
   }
 #pragma unroll
   for (int s = 0; s < NSLS; ++s) fc[s] = fck[s] = 0.f;
-  if (ATT && STAGE) {
+  if (ATT && STAGE && active) {
     // rows: R[c][s] -> 3c+s (0..17), epsilondev[c] -> 18+c, factor_common[s] -> 24+s,
-    // factor_common_kappa[s] -> 27+s; 32 chunks of 16 B per row
-    const long se = (long)e * (NSLS * NGLL3_PAD), ee = (long)e * NGLL3_PAD;
-    for (int q = t; q < 30 * 32; q += NGLL3_PAD) {
-      const int row = q >> 5, col = (q & 31) * 4;
+    // factor_common_kappa[s] -> 27+s.  Each thread copies (4-byte cp.async) and later
+    // reads only its own point's column, so no barrier is needed, and the copies
+    // stay in flight through the first contraction set.
+    const long se = (long)e * (NSLS * NGLL3_PAD) + t, ee = (long)e * NGLL3_PAD + t;
+#pragma unroll
+    for (int row = 0; row < 30; ++row) {
       const float* src;
       if (row < 18) src = a.R[row / 3] + se + (row % 3) * NGLL3_PAD;
       else if (row < 24) src = a.eps[row - 18] + ee;
       else if (row < 27) src = a.fc + se + (row - 24) * NGLL3_PAD;
       else src = a.fck + se + (row - 27) * NGLL3_PAD;
-      cp_async16(&s_att[row][col], src + col);
+      cp_async4(&s_att[row][t], src);
     }
     asm volatile("cp.async.commit_group;" ::: "memory");
   }
@@ -125,7 +127,6 @@ __global__ void __launch_bounds__(NGLL3_PAD, MINB) stiffness_kernel(const Stiffn
     }
   }
   if (t < NGLL3) s_gll[t] = __ldg(a.gll + t);
-  if (ATT && STAGE) asm volatile("cp.async.wait_all;" ::: "memory");
   s_u[0][t] = ux;
   s_u[1][t] = uy;
   s_u[2][t] = uz;
@@ -217,6 +218,7 @@ __global__ void __launch_bounds__(NGLL3_PAD, MINB) stiffness_kernel(const Stiffn
     float sig_xy = mu * (dxy + dyx);
     float sig_xz = mu * (dzx + dxz);
     float sig_yz = mu * (dzy + dyz);
+    if (ATT && STAGE) asm volatile("cp.async.wait_all;" ::: "memory");
     if (ATT) {
       float sR[6];
 #pragma unroll

@@ -84,17 +84,29 @@ __global__ void adj_p_kernel(const float* __restrict__ vh, const float* __restri
   bp[i] = 0.f;
 }
 
-// kp = -K p and bp = -B p: uth = uh - kp, vth = vh - bp; back through the predictor
+// kp = -K p and bp = -B p: uth = uh - kp, vth = vh - bp; back through the
+// predictor; then p of the previous step, -M^-1 (ah + dt/2 vh), from the new
+// adjoints (the residual enters uh only, so p does not depend on it), and the
+// K p / B p accumulators cleared for that step
 __global__ void adj_update_kernel(float* __restrict__ uh, float* __restrict__ vh, float* __restrict__ ah,
-                                  const float* __restrict__ kp, const float* __restrict__ bp, long n, float dt,
-                                  float dt2, float dtsq2) {
+                                  float* __restrict__ kp, float* __restrict__ bp, float* __restrict__ p,
+                                  const float* __restrict__ rmx, const float* __restrict__ rmy,
+                                  const float* __restrict__ rmz, long nglob, float dt, float dt2, float dtsq2) {
   const long i = (long)blockIdx.x * blockDim.x + threadIdx.x;
-  if (i >= n) return;
+  if (i >= 3 * nglob) return;
   const float ut = uh[i] - kp[i];
   const float vt = vh[i] - bp[i];
+  const float vn = dt * ut + vt;
+  const float an = dtsq2 * ut + dt2 * vt;
   uh[i] = ut;
-  vh[i] = dt * ut + vt;
-  ah[i] = dtsq2 * ut + dt2 * vt;
+  vh[i] = vn;
+  ah[i] = an;
+  const long g = i / 3;
+  const int c = (int)(i - 3 * g);
+  const float rm = c == 0 ? __ldg(rmx + g) : (c == 1 ? __ldg(rmy + g) : __ldg(rmz + g));
+  p[i] = -rm * (an + dt2 * vn);
+  kp[i] = 0.f;
+  bp[i] = 0.f;
 }
 
 struct GradArgs {
@@ -264,8 +276,8 @@ void adjoint_step(Mesh* mp, int n, const float* u, const float* araw, float dt, 
     adj_residual_kernel<<<mp->nrec_local, NGLL3_PAD, 0, s>>>(mp->nrec_local, mp->d_ispec_rec, mp->d_hxir,
                                                              mp->d_hetar, mp->d_hgammar, mp->d_nu_rec, mp->d_ibool,
                                                              G->residual, n, G->adj_u);
-  adj_p_kernel<<<nblk(n3, 256), 256, 0, s>>>(G->adj_v, G->adj_a, mp->d_rmassx, mp->d_rmassy, mp->d_rmassz,
-                                             mp->nglob, dt2, G->p, G->kp, G->bp);
+  // p, kp, bp of this step were produced by the previous transposed step (or the
+  // start of the sweep)
   launch_stacey(mp, G->p, G->bp, s);
   Fields tmp;
   tmp.displ = G->p;
@@ -298,7 +310,8 @@ void adjoint_step(Mesh* mp, int n, const float* u, const float* araw, float dt, 
     ga.g_mu = G->g_mu;
     grad_accum_kernel<<<a.nelem, NGLL3_PAD, 0, s>>>(ga);
   }
-  adj_update_kernel<<<nblk(n3, 256), 256, 0, s>>>(G->adj_u, G->adj_v, G->adj_a, G->kp, G->bp, n3, dt, dt2, dtsq2);
+  adj_update_kernel<<<nblk(n3, 256), 256, 0, s>>>(G->adj_u, G->adj_v, G->adj_a, G->kp, G->bp, G->p, mp->d_rmassx,
+                                                  mp->d_rmassy, mp->d_rmassz, mp->nglob, dt, dt2, dtsq2);
 }
 
 }  // namespace
@@ -444,6 +457,9 @@ int sf3d_gradient_backward(long* Mesh_pointer, realw deltat) {
   SF3D_CUDA_RET(cudaMemsetAsync(G->g_mu, 0, sizeof(double) * npt, s), SF3D_ERR_CUDA);
   SF3D_CUDA_RET(cudaMemsetAsync(mp->d_done, 0, sizeof(unsigned int), s), SF3D_ERR_CUDA);
   SF3D_CUDA_RET(cudaEventRecord(mp->ev0, s), SF3D_ERR_CUDA);
+  // p of the last step from the zero adjoint state (p = 0, accumulators cleared)
+  adj_p_kernel<<<nblk((long)n3, 256), 256, 0, s>>>(G->adj_v, G->adj_a, mp->d_rmassx, mp->d_rmassy, mp->d_rmassz,
+                                                   mp->nglob, dt2, G->p, G->kp, G->bp);
   const int nseg = G->nckpt + 1;
   for (int j = nseg - 1; j >= 0; --j) {
     const int n0 = j * G->every;
