@@ -164,14 +164,14 @@ def adjoint_leg(nshots: int):
             "workload": "64x64x32 hexes, 20x20x10 km, perturbed background, +3% vs blob true model"}
 
 
-def batch_leg(nshots: int, steps: int):
+def batch_leg(nshots: int, steps: int, nx: int = 64):
     """Per-shot GLL-point updates/s of the batched-shots workload (64x64x32 hexes,
     perturbed model, no attenuation): all shots advancing together with
     shot-innermost fields against the plain single-shot path on the same mesh."""
     from specfem3d_gb300 import configs, gradient as G, meshgen
     from specfem3d_gb300.batch import BatchSolver
     from specfem3d_gb300.solver import GPUSolver
-    cfg = configs.batched_shots(nstep=steps + 8, nshots=nshots)
+    cfg = configs.batched_shots(nstep=steps + 8, nshots=nshots, nx=nx)
     db = meshgen.build_database(cfg)
     nglob = int(db["nglob"])
     b = BatchSolver(db, cfg, nlength=steps + 8)
@@ -191,8 +191,34 @@ def batch_leg(nshots: int, steps: int):
             "nspec": int(db["nspec"]), "batched": rate_b, "plain_single_shot": rate_p,
             "speedup_per_shot": rate_b / rate_p, "batched_ms_per_step": ms_b / steps,
             "plain_ms_per_step": ms_p / steps, "tiling": tune,
-            "workload": "64x64x32 hexes, 20x20x10 km, +-5% perturbed model, no attenuation, "
+            "workload": f"{nx}x{nx}x{nx // 2} hexes, 20x20x10 km, +-5% perturbed model, no attenuation, "
                         f"{nshots} CMT shots, Ricker 2 Hz"}
+
+
+def coupled_leg(steps: int):
+    """GLL-point updates/s of the coupled fluid-solid workload (96x96x48 hexes, top sixth
+    water over a perturbed solid, pressure source, 256 hydrophones) through the per-call
+    entry points in the reference's order (acoustic and elastic predictors, fluid
+    stiffness, Sommerfeld faces, both coupling terms, sources, correctors, pressure
+    seismograms), wall clock with the device synchronised on both sides."""
+    from specfem3d_gb300 import configs, meshgen
+    from specfem3d_gb300.solver import GPUSolver
+    cfg = configs.coupled_fluid_solid(nstep=steps + 5)
+    db = meshgen.build_database(cfg)
+    g = GPUSolver(db, cfg)
+    g.run_per_call(3)
+    g.L.sf3d_synchronize(g.mp)
+    t0 = time.perf_counter()
+    g.run_per_call(steps)
+    g.L.sf3d_synchronize(g.mp)
+    dt = time.perf_counter() - t0
+    ok = bool(np.isfinite(g.seismograms()).all())
+    nglob = int(db["nglob"])
+    g.close()
+    return {"unit": UNIT, "value": nglob * steps / dt, "ms_per_step": 1000 * dt / steps, "steps": steps,
+            "nglob": nglob, "nspec": int(db["nspec"]), "fluid_elements": int(db["ispec_is_acoustic"].sum()),
+            "finite": ok, "path": "per-call FC_FUNC_ entry points, host stf per step, pressure traces",
+            "workload": "coupled fluid/solid 96x96x48 hexes, 20x20x10 km"}
 
 
 def run_reference(args, rank):
@@ -233,6 +259,8 @@ def main():
     ap.add_argument("--batch", type=int, default=0,
                     help="also time this many shots of the batched-shots workload against the plain path (0: skip)")
     ap.add_argument("--batch-steps", type=int, default=100)
+    ap.add_argument("--batch-nx", type=int, default=64, help="elements along x and y of the batched mesh")
+    ap.add_argument("--coupled", type=int, default=0, help="also time this many steps of the coupled workload")
     ap.add_argument("--adjoint", type=int, default=0,
                     help="also time the checkpointed misfit gradient over this many shots of the "
                          "8-shot 64x64x32 gradient workload (0: skip)")
@@ -374,7 +402,9 @@ def main():
         "stable": rc == 0,
     }
     if args.batch > 0:
-        line["batched"] = batch_leg(args.batch, args.batch_steps)
+        line["batched"] = batch_leg(args.batch, args.batch_steps, args.batch_nx)
+    if args.coupled > 0:
+        line["coupled"] = coupled_leg(args.coupled)
     if args.adjoint > 0:
         line["adjoint"] = adjoint_leg(args.adjoint)
     if rank == 0 and not args.no_cpu:

@@ -280,17 +280,20 @@ int sf3d_get_kernels_f64(long *Mesh_pointer, double *h_rho_kl, double *h_mu_kl, 
  * the device copy is rounded to FP32 like the per-step stf of the reference. */
 int sf3d_set_stf_table(long *Mesh_pointer, const double *h_stf, int nsources, int nstep);
 
-/* Run time steps it_begin..it_end (1-based, inclusive) of the forward elastic
- * scheme entirely on the device: fused corrector+predictor, Stacey, sources,
- * stiffness, displacement seismograms (trace slot (it-1) mod nlength_seismogram).
- * Steps are captured in CUDA graphs of
+/* Run time steps it_begin..it_end (1-based, inclusive) of the forward scheme
+ * entirely on the device: fused corrector+predictor, Stacey, sources,
+ * stiffness, displacement seismograms (trace slot (it-1) mod nlength_seismogram);
+ * with a fluid domain (prepare_fields_acoustic_device) also the fluid step,
+ * both coupling terms and the pressure traces, in the order of
+ * iterate_time.F90.  Steps are captured in CUDA graphs of
  * steps_per_graph steps (0 = no graphs).  Leaves the fields as the per-call
  * ABI leaves them after the same steps.  flags bit 0: record the device time
  * of every stiffness launch (read back with sf3d_last_timing). */
 int sf3d_iterate_time(long *Mesh_pointer, int it_begin, int it_end, realw deltat, int steps_per_graph,
                       int flags);
 
-/* Copy the device trace buffer (3, nrec_local, nlength) to the host. */
+/* Copy the device trace buffer (3, nrec_local, nlength) to the host (pressure
+ * runs: pressure in component 0, as compute_seismograms_cuda returns it). */
 int sf3d_get_seismograms(long *Mesh_pointer, realw *h_seismograms);
 
 /* Device time of the stiffness kernel launches of the last sf3d_iterate_time

@@ -198,22 +198,24 @@ def small_layered(nx=6, ny=5, counts=(2, 2, 3), nstep=200, attenuation=True, see
     return finish(cfg)
 
 
-def batched_shots(nstep: int = 3000, nshots: int = 32, seed: int = 2026) -> dict:
+def batched_shots(nstep: int = 3000, nshots: int = 32, seed: int = 2026, nx: int = 64) -> dict:
+    """nx x nx x nx/2 elements on the 20x20x10 km block (64 in the benchmark
+    definition; smaller nx for profiling), shots and receivers unchanged."""
     rng = np.random.default_rng(seed)
-    zlev = list(np.linspace(-10000.0, 0.0, 33))
+    zlev = list(np.linspace(-10000.0, 0.0, nx // 2 + 1))
     g = np.linspace(1000.0, 19000.0, 5)
     shots = []
     for _ in range(nshots):
         shots.append(dict(type="cmt", x=float(rng.uniform(1000, 19000)), y=float(rng.uniform(1000, 19000)),
                           z=-float(rng.uniform(2000, 8000)), M=random_moment_tensor(rng), stf="ricker", f0=2.0))
-    cfg = dict(nx=64, ny=64, x0=0.0, x1=20000.0, y0=0.0, y1=20000.0, zlev=zlev, elem_layer=None,
+    cfg = dict(nx=nx, ny=nx, x0=0.0, x1=20000.0, y0=0.0, y1=20000.0, zlev=zlev, elem_layer=None,
                layers=[dict(rho=2400.0, vp=3000.0, vs=1700.0)], dt=None, nstep=nstep,
                perturbation=dict(corr_len=1000.0, seed=2027),
                sources=shots[:1], shots=shots,
                receivers=[(float(x), float(y), 0.0) for y in g for x in g], vmax_factor=1.05)
     cfg = finish(cfg)
     # CFL with the +-5 % perturbation bound on vp
-    cfg["dt"] = significant_dt(COURANT_SUGGESTED * GLL_MIN_SPACING * (20000.0 / 64) / (3000.0 * 1.05))
+    cfg["dt"] = significant_dt(COURANT_SUGGESTED * GLL_MIN_SPACING * (20000.0 / nx) / (3000.0 * 1.05))
     return cfg
 
 

@@ -159,16 +159,27 @@ __global__ void free_surface_kernel(int nfaces, const int* __restrict__ fs_ispec
 
 // chi_dd -= sourcearray(1) stf / kappa for sources in fluid elements
 // (compute_add_sources_acoustic.f90:100-126)
+// stf from the per-call array, or from the whole-run table at the device step
+// counter (stf_table != nullptr)
 __global__ void sources_acoustic_kernel(int nsrc, const int* __restrict__ ispec_src, const int* __restrict__ is_acoustic,
                                         const float* __restrict__ sa, const float* __restrict__ stf,
                                         const int* __restrict__ ibool, const float* __restrict__ kappav,
-                                        float* __restrict__ pot_dd) {
+                                        float* __restrict__ pot_dd, const float* __restrict__ stf_table,
+                                        const int* __restrict__ d_it, int stf_nstep) {
   const int is = blockIdx.x, p = threadIdx.x;
   if (is >= nsrc || p >= NGLL3) return;
   const int e = ispec_src[is];
   if (e < 0 || !is_acoustic[e]) return;
+  float f;
+  if (stf_table) {
+    const int it = *d_it;
+    if (it < 1 || it > stf_nstep) return;
+    f = stf_table[(long)(it - 1) * nsrc + is];
+  } else {
+    f = stf[is];
+  }
   const long q = (long)e * NGLL3_PAD + p;
-  atomicAdd(pot_dd + ibool[q], -(sa[((long)is * NGLL3_PAD + p) * 3] * stf[is] / kappav[q]));
+  atomicAdd(pot_dd + ibool[q], -(sa[((long)is * NGLL3_PAD + p) * 3] * f / kappav[q]));
 }
 
 __global__ void predictor_scalar_kernel(float* __restrict__ d, float* __restrict__ v, float* __restrict__ a, long n,
@@ -198,7 +209,8 @@ __global__ void pressure_seismogram_kernel(int nrec, const int* __restrict__ isp
                                            const int* __restrict__ rec_is_acoustic, const float* __restrict__ hx,
                                            const float* __restrict__ he, const float* __restrict__ hg,
                                            const int* __restrict__ ibool, const float* __restrict__ pot_dd,
-                                           float* __restrict__ seismo_p, int slot) {
+                                           float* __restrict__ seismo_p, int slot, const int* __restrict__ d_it,
+                                           int nlength) {
   __shared__ float red[4];
   const int r = blockIdx.x, t = threadIdx.x;
   float s = 0.f;
@@ -211,14 +223,104 @@ __global__ void pressure_seismogram_kernel(int nrec, const int* __restrict__ isp
   for (int o = 16; o > 0; o >>= 1) s += __shfl_down_sync(0xffffffffu, s, o);
   if ((t & 31) == 0) red[t >> 5] = s;
   __syncthreads();
-  if (t == 0 && r < nrec) seismo_p[r + (long)nrec * slot] = red[0] + red[1] + red[2] + red[3];
+  if (t == 0 && r < nrec) {
+    const int sl = d_it ? (*d_it - 1) % nlength : slot;
+    seismo_p[r + (long)nrec * sl] = red[0] + red[1] + red[2] + red[3];
+  }
 }
 
 void launch_pressure_seismograms(Mesh* mp, int slot) {
   if (!mp->d_seismo_p || mp->nrec_local == 0 || !mp->d_potential_dot_dot) return;
   pressure_seismogram_kernel<<<mp->nrec_local, NGLL3_PAD, 0, mp->stream>>>(
       mp->nrec_local, mp->d_ispec_rec, mp->d_rec_is_acoustic, mp->d_hxir, mp->d_hetar, mp->d_hgammar, mp->d_ibool,
-      mp->d_potential_dot_dot, mp->d_seismo_p, slot);
+      mp->d_potential_dot_dot, mp->d_seismo_p, slot, nullptr, 1);
+}
+
+// The fluid part of one fused step (compute_forces_acoustic_forward_calling,
+// compute_forces_acoustic_calling_routine.f90:54-343, with the acoustic
+// predictor of update_displacement_scheme.f90 in front): predictor, free
+// surface, stiffness of both phases, Sommerfeld faces, coupling with the
+// solid displacement, sources from the whole-run stf table at the device step
+// counter, mass + corrector, free surface.  Returns the number of launches.
+int enqueue_acoustic_step(Mesh* mp, float dt, float dt2, float dtsq2) {
+  cudaStream_t s = mp->stream;
+  int launches = 0;
+  const long n = mp->nglob;
+  predictor_scalar_kernel<<<nblk(n, 256), 256, 0, s>>>(mp->d_potential, mp->d_potential_dot, mp->d_potential_dot_dot,
+                                                        n, dt, dt2, dtsq2);
+  ++launches;
+  const long nfs = (long)mp->num_free_surface_faces * NGLL2;
+  if (nfs > 0) {
+    free_surface_kernel<<<nblk(nfs, 128), 128, 0, s>>>(mp->num_free_surface_faces, mp->d_fs_ispec, mp->d_fs_pt,
+                                                        mp->d_ispec_is_acoustic, mp->d_ibool, mp->d_potential,
+                                                        mp->d_potential_dot, mp->d_potential_dot_dot);
+    ++launches;
+  }
+  if (mp->nspec_outer_ac == 0 && mp->nspec_inner_ac == 0) {
+    mp->nspec_outer_ac = mp->phase_valid_ac[0];
+    mp->nspec_inner_ac = mp->phase_valid_ac[1];
+  }
+  for (int iphase = 1; iphase <= 2; ++iphase) {
+    const int nel = iphase == 1 ? mp->nspec_outer_ac : mp->nspec_inner_ac;
+    if (nel <= 0) continue;
+    const int* ph = mp->d_phase_ispec_ac + (long)(iphase - 1) * mp->num_phase_ispec_ac;
+    acoustic_stiffness_kernel<<<nel, NGLL3_PAD, 0, s>>>(
+        nel, ph, mp->d_ibool, mp->d_irregular, mp->d_metric[0], mp->d_metric[1], mp->d_metric[2], mp->d_metric[3],
+        mp->d_metric[4], mp->d_metric[5], mp->d_metric[6], mp->d_metric[7], mp->d_metric[8], mp->d_rhostore,
+        mp->d_gll, mp->xix_regular, mp->jacobian_regular, mp->d_potential, mp->d_potential_dot_dot);
+    ++launches;
+  }
+  if (mp->stacey && mp->num_abs_faces > 0) {
+    const long nf = (long)mp->num_abs_faces * NGLL2;
+    stacey_acoustic_kernel<<<nblk(nf, 128), 128, 0, s>>>(mp->num_abs_faces, mp->d_abs_ispec, mp->d_abs_pt,
+                                                          mp->d_abs_jw, mp->d_ispec_is_acoustic, mp->d_ibool,
+                                                          mp->d_rhostore, mp->d_kappav, mp->d_potential_dot,
+                                                          mp->d_potential_dot_dot);
+    ++launches;
+  }
+  if (mp->num_coupling_faces > 0) {
+    const long nc = (long)mp->num_coupling_faces * NGLL2;
+    coupling_ac_el_kernel<<<nblk(nc, 128), 128, 0, s>>>(mp->num_coupling_faces, mp->d_cp_ispec, mp->d_cp_pt,
+                                                         mp->d_cp_normal, mp->d_cp_jw, mp->d_ibool, mp->f.displ, 1.f,
+                                                         mp->d_potential_dot_dot);
+    ++launches;
+  }
+  if (mp->nsources > 0 && mp->d_stf_table) {
+    sources_acoustic_kernel<<<mp->nsources, NGLL3_PAD, 0, s>>>(mp->nsources, mp->d_ispec_src, mp->d_ispec_is_acoustic,
+                                                                mp->d_sourcearrays, nullptr, mp->d_ibool,
+                                                                mp->d_kappav, mp->d_potential_dot_dot,
+                                                                mp->d_stf_table, mp->d_it, mp->stf_nstep);
+    ++launches;
+  }
+  mass_corrector_scalar_kernel<<<nblk(n, 256), 256, 0, s>>>(mp->d_potential_dot, mp->d_potential_dot_dot,
+                                                            mp->d_rmass_acoustic, n, dt2);
+  ++launches;
+  if (nfs > 0) {
+    free_surface_kernel<<<nblk(nfs, 128), 128, 0, s>>>(mp->num_free_surface_faces, mp->d_fs_ispec, mp->d_fs_pt,
+                                                        mp->d_ispec_is_acoustic, mp->d_ibool, mp->d_potential,
+                                                        mp->d_potential_dot, mp->d_potential_dot_dot);
+    ++launches;
+  }
+  return launches;
+}
+
+// the solid side of the coupling (compute_coupling_viscoelastic_ac.f90:28-140) and
+// the pressure traces at the device step counter
+int enqueue_coupling_el_ac(Mesh* mp) {
+  if (mp->num_coupling_faces == 0) return 0;
+  const long nc = (long)mp->num_coupling_faces * NGLL2;
+  coupling_el_ac_kernel<<<nblk(nc, 128), 128, 0, mp->stream>>>(mp->num_coupling_faces, mp->d_cp_ispec, mp->d_cp_pt,
+                                                                mp->d_cp_normal, mp->d_cp_jw, mp->d_ibool,
+                                                                mp->d_potential_dot_dot, 1.f, mp->f.accel);
+  return 1;
+}
+
+int enqueue_pressure_seismograms(Mesh* mp) {
+  if (!mp->d_seismo_p || mp->nrec_local == 0 || !mp->d_potential_dot_dot || !mp->save_p) return 0;
+  pressure_seismogram_kernel<<<mp->nrec_local, NGLL3_PAD, 0, mp->stream>>>(
+      mp->nrec_local, mp->d_ispec_rec, mp->d_rec_is_acoustic, mp->d_hxir, mp->d_hetar, mp->d_hgammar, mp->d_ibool,
+      mp->d_potential_dot_dot, mp->d_seismo_p, 0, mp->d_it, mp->nlength_seismogram);
+  return 1;
 }
 
 }  // namespace sf3d
@@ -417,7 +519,7 @@ void compute_add_sources_ac_cuda_(long* Mesh_pointer, int* NSOURCESf, double* h_
   sources_acoustic_kernel<<<mp->nsources, NGLL3_PAD, 0, mp->stream>>>(mp->nsources, mp->d_ispec_src,
                                                                       mp->d_ispec_is_acoustic, mp->d_sourcearrays,
                                                                       mp->d_stf_step, mp->d_ibool, mp->d_kappav,
-                                                                      mp->d_potential_dot_dot);
+                                                                      mp->d_potential_dot_dot, nullptr, nullptr, 0);
   SF3D_CUDA(cudaStreamSynchronize(mp->stream));
   cuda_ok(cudaGetLastError(), "sources_acoustic_kernel");
 }

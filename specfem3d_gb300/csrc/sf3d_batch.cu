@@ -48,7 +48,12 @@ __global__ void __launch_bounds__(NGLL3_PAD * SB, 8 / SB) batch_stiffness_kernel
   __shared__ float s_buf[9 * NGLL3_PAD * SB];  // displacement (3 comps), then J sigma grad(xi) (9)
   const int tid = threadIdx.x;
   const int sl = tid % SB, p = tid / SB;
-  const int shot = blockIdx.y * SB + sl;
+  // shot tiles vary fastest over consecutive CTAs: the tiles of one element run
+  // together and read the same 128-byte lines of the stacked fields from L2
+  const int ntiles = a.nshots / SB;
+  const int tile = blockIdx.x % ntiles;
+  const int egroup = blockIdx.x / ntiles;
+  const int shot = tile * SB + sl;
   const bool active = p < NGLL3;
   const int k = p / NGLL2, j = (p / NGLLX) % NGLLX, i = p % NGLLX;
   const long S = a.nshots;
@@ -56,7 +61,7 @@ __global__ void __launch_bounds__(NGLL3_PAD * SB, 8 / SB) batch_stiffness_kernel
   auto U = [&](int c, int pt) -> float& { return s_buf[(c * NGLL3_PAD + pt) * SB + sl]; };
 #pragma unroll 1
   for (int eb = 0; eb < EB; ++eb) {
-    const int slot = blockIdx.x * EB + eb;
+    const int slot = egroup * EB + eb;
     if (slot >= a.nelem) break;
     const int e = a.phase ? __ldg(a.phase + slot) : slot;
     const int ir = __ldg(a.irregular + e);
@@ -318,14 +323,17 @@ __global__ void __launch_bounds__(NGLL3_PAD * GB, 4 / GB) batch_stiffness4_kerne
   const int tid = threadIdx.x;
   const int gi = tid % GB, p = tid / GB;
   const long S = a.nshots;
-  const long shot0 = 4L * (blockIdx.y * GB + gi);
+  const int ntiles = a.nshots / (4 * GB);
+  const int tile = blockIdx.x % ntiles;
+  const int egroup = blockIdx.x / ntiles;
+  const long shot0 = 4L * (tile * GB + gi);
   const bool active = p < NGLL3;
   const int k = p / NGLL2, j = (p / NGLLX) % NGLLX, i = p % NGLLX;
   for (int q = tid; q < NGLL3; q += NGLL3_PAD * GB) s_gll[q] = __ldg(a.gll + q);
   float4(*B)[NGLL3_PAD] = s_buf[gi];
 #pragma unroll 1
   for (int eb = 0; eb < EB; ++eb) {
-    const int slot = blockIdx.x * EB + eb;
+    const int slot = egroup * EB + eb;
     if (slot >= a.nelem) break;
     const int e = a.phase ? __ldg(a.phase + slot) : slot;
     const int ir = __ldg(a.irregular + e);
@@ -463,8 +471,8 @@ __global__ void __launch_bounds__(NGLL3_PAD * GB, 4 / GB) batch_stiffness4_kerne
 
 template <int GB, int EB>
 void launch_tile4(const BatchStiffArgs& a, cudaStream_t s) {
-  dim3 grid((unsigned)((a.nelem + EB - 1) / EB), (unsigned)(a.nshots / (4 * GB)));
-  batch_stiffness4_kernel<GB, EB><<<grid, NGLL3_PAD * GB, 0, s>>>(a);
+  const long nblocks = (long)((a.nelem + EB - 1) / EB) * (a.nshots / (4 * GB));
+  batch_stiffness4_kernel<GB, EB><<<(unsigned)nblocks, NGLL3_PAD * GB, 0, s>>>(a);
 }
 
 template <int GB>
@@ -479,8 +487,8 @@ void launch_gb4(const BatchStiffArgs& a, int eb, cudaStream_t s) {
 
 template <int SB, int EB>
 void launch_tile(const BatchStiffArgs& a, cudaStream_t s) {
-  dim3 grid((unsigned)((a.nelem + EB - 1) / EB), (unsigned)(a.nshots / SB));
-  batch_stiffness_kernel<SB, EB><<<grid, NGLL3_PAD * SB, 0, s>>>(a);
+  const long nblocks = (long)((a.nelem + EB - 1) / EB) * (a.nshots / SB);
+  batch_stiffness_kernel<SB, EB><<<(unsigned)nblocks, NGLL3_PAD * SB, 0, s>>>(a);
 }
 
 template <int SB>

@@ -364,6 +364,10 @@ inline void run_stiffness(Mesh* mp, const StiffnessArgs& a, bool att, bool store
   }
 }
 void launch_pressure_seismograms(Mesh* mp, int slot);
+// fused-loop pieces of a coupled fluid/solid step (sf3d_acoustic.cu)
+int enqueue_acoustic_step(Mesh* mp, float dt, float dt2, float dtsq2);
+int enqueue_coupling_el_ac(Mesh* mp);
+int enqueue_pressure_seismograms(Mesh* mp);
 // one fused forward elastic step of sf3d_iterate_time (predictor fused with the
 // previous corrector unless first_step); returns the number of launches
 int enqueue_step(Mesh* mp, float dt, float dt2, float dtsq2, bool first_step, cudaEvent_t* ev);

@@ -5,10 +5,11 @@
 // update_displacement_cuda.cu, compute_forces_viscoelastic_cuda.cu,
 // compute_stacey_viscoelastic_cuda.cu, compute_add_sources_viscoelastic_cuda.cu
 // and write_seismograms_cuda.cu.  sf3d_iterate_time replaces the Fortran
-// time loop (iterate_time.F90:219-330) for the forward elastic case: it fuses
-// the corrector of step n-1 with the predictor of step n into one streaming
-// pass, reads the step index from device memory, and captures blocks of steps
-// into CUDA graphs so a step costs four graph nodes and no host round trip.
+// time loop (iterate_time.F90:219-330) for forward runs (elastic, viscoelastic,
+// and coupled fluid/solid meshes): it fuses the corrector of step n-1 with the
+// predictor of step n into one streaming pass, reads the step index from device
+// memory, and captures blocks of steps into CUDA graphs, so a step costs a few
+// graph nodes and no host round trip.
 #include <math.h>
 #include <string.h>
 
@@ -296,6 +297,8 @@ int enqueue_step(Mesh* mp, float dt, float dt2, float dtsq2, bool first_step, cu
                                                                     dtsq2);
   }
   ++launches;
+  // fluid domain: its whole step (it reads the solid displacement just predicted)
+  if (mp->has_acoustic) launches += enqueue_acoustic_step(mp, dt, dt2, dtsq2);
   if (mp->stacey && mp->num_abs_faces > 0) {
     const long n = (long)mp->num_abs_faces * NGLL2;
     stacey_kernel<<<nblk(n, 128), 128, 0, s>>>(mp->num_abs_faces, mp->d_abs_ispec, mp->d_abs_pt, mp->d_abs_normal,
@@ -303,6 +306,7 @@ int enqueue_step(Mesh* mp, float dt, float dt2, float dtsq2, bool first_step, cu
                                                 F.accel, nullptr, mp->d_ispec_is_acoustic);
     ++launches;
   }
+  if (mp->has_acoustic) launches += enqueue_coupling_el_ac(mp);
   if (mp->nsources > 0 && mp->d_stf_table) {
     sources_kernel<<<mp->nsources, NGLL3_PAD, 0, s>>>(mp->nsources, mp->d_ispec_src, mp->d_sourcearrays, nullptr,
                                                       mp->d_stf_table, mp->d_it, mp->stf_nstep, mp->d_ibool, F.accel,
@@ -319,6 +323,7 @@ int enqueue_step(Mesh* mp, float dt, float dt2, float dtsq2, bool first_step, cu
     ++launches;
   }
   if (ev) cudaEventRecord(ev[1], s);
+  if (mp->has_acoustic) launches += enqueue_pressure_seismograms(mp);
   if (mp->nrec_local > 0 && mp->save_d) {
     seismogram_kernel<<<mp->nrec_local, NGLL3_PAD, 0, s>>>(mp->nrec_local, mp->d_ispec_rec, mp->d_hxir, mp->d_hetar,
                                                            mp->d_hgammar, mp->d_nu_rec, mp->d_ibool, F.displ,
@@ -720,7 +725,21 @@ int sf3d_last_timing(long* Mesh_pointer, float* stiffness_ms, int* stiffness_lau
 int sf3d_get_seismograms(long* Mesh_pointer, realw* h) {
   Mesh* mp = get_mesh(Mesh_pointer);
   if (!mp) return SF3D_ERR_STATE;
-  if (!mp->d_seismo_d || mp->nrec_local == 0) return SF3D_OK;
+  if (mp->nrec_local == 0) return SF3D_OK;
+  if (!mp->save_d && mp->save_p && mp->d_seismo_p) {
+    // pressure runs: pressure in component 0, as compute_seismograms_cuda returns it
+    const size_t n = (size_t)mp->nrec_local * mp->nlength_seismogram;
+    std::vector<float> p(n);
+    if (!copy_sync(p.data(), mp->d_seismo_p, sizeof(float) * n, cudaMemcpyDeviceToHost, mp->stream))
+      return SF3D_ERR_CUDA;
+    for (size_t q = 0; q < n; ++q) {
+      h[3 * q] = p[q];
+      h[3 * q + 1] = 0.f;
+      h[3 * q + 2] = 0.f;
+    }
+    return SF3D_OK;
+  }
+  if (!mp->d_seismo_d) return SF3D_OK;
   const size_t bytes = sizeof(float) * 3 * (size_t)mp->nrec_local * mp->nlength_seismogram;
   SF3D_CUDA_RET(cudaMemcpyAsync(h, mp->d_seismo_d, bytes, cudaMemcpyDeviceToHost, mp->stream), SF3D_ERR_CUDA);
   SF3D_CUDA_RET(cudaStreamSynchronize(mp->stream), SF3D_ERR_CUDA);

@@ -236,6 +236,7 @@ class GPUSolver:
         self.it += 1
 
     def run_per_call(self, nsteps: int):
+        self._last_path = "per_call"
         for _ in range(nsteps):
             self.step()
         abi.check()
@@ -243,6 +244,7 @@ class GPUSolver:
     # ------------------------------------------------- whole step blocks (fused)
     def run(self, nsteps: int, steps_per_graph: int = 50, timing: bool = False):
         """nsteps time steps on the device (fused predictor/corrector, graph-captured)."""
+        self._last_path = "device"
         rc = self.L.sf3d_iterate_time(self.mp, self.it, self.it + nsteps - 1, float(self.deltat),
                                       int(steps_per_graph), int(bool(timing)))
         if rc != 0:
@@ -259,7 +261,7 @@ class GPUSolver:
     def seismograms(self) -> np.ndarray:
         """(nrec, 3, nlength) displacement traces (pressure runs: the per-call
         path's host array, pressure in component 0)."""
-        if "pressure" in self.record:
+        if "pressure" in self.record and getattr(self, "_last_path", "") == "per_call":
             return self._seis_host.reshape(self.nlength, self.nrec, 3).transpose(1, 2, 0).copy()
         out = np.zeros(3 * self.nrec * self.nlength, np.float32)
         if self.nrec:

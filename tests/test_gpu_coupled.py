@@ -32,3 +32,23 @@ def test_coupled_fluid_solid_vs_oracle(gpulib):
     print(f"coupled 300 steps: pressure {e_p:.2e}, potential {e_chi:.2e}, solid displacement {e_u:.2e}")
     assert np.abs(ref[:, 0]).max() > 0 and np.abs(sim.get("displ")).max() > 0
     assert e_p < 5e-5 and e_chi < 5e-5 and e_u < 1e-4
+
+
+def test_coupled_fused_loop_equals_per_call(gpulib):
+    """sf3d_iterate_time with the fluid domain fused into the graph-captured step
+    gives the per-call path's hydrophone traces and fields (<= 1e-5: atomics
+    reorder sums)."""
+    from specfem3d_gb300 import configs, meshgen, solver
+    cfg = configs.small_coupled(nstep=300)
+    db = meshgen.build_database(cfg)
+    g = solver.GPUSolver(db, cfg)
+    g.run_per_call(cfg["nstep"])
+    s1, p1, d1 = g.seismograms(), g.potentials()[0], g.fields()[0]
+    g.close()
+    g = solver.GPUSolver(db, cfg)
+    g.run(cfg["nstep"], steps_per_graph=50)
+    s2, p2, d2 = g.seismograms(), g.potentials()[0], g.fields()[0]
+    g.close()
+    assert np.abs(s1[:, 0]).max() > 0
+    assert rel_l2(s2[:, 0], s1[:, 0]) < 1e-5
+    assert rel_l2(p2, p1) < 1e-5 and rel_l2(d2, d1) < 1e-5
