@@ -310,7 +310,9 @@ int sf3d_last_timing(long *Mesh_pointer, float *stiffness_ms, int *stiffness_lau
  *   1:          persistent CTAs fed by a three-stage bulk-copy (TMA) pipeline;
  *   5, 6, 7:    one CTA per element with the memory variables, strains and
  *               attenuation factors staged in shared memory by cp.async, for
- *               6, 7, 8 CTAs per SM (register budget 80, 72, 64).
+ *               6, 7, 8 CTAs per SM (register budget 80, 72, 64);
+ *   8, 9:       one CTA per element, evict-first cache hints on the element
+ *               streams (read and written once per launch), 6 and 7 CTAs/SM.
  * Default 3 (the fastest on GB300 for the layered viscoelastic workload).
  * No reference counterpart (the reference compiles one Kernel_2 per
  * configuration). */
@@ -326,7 +328,7 @@ int sf3d_set_geometry_precision(long *Mesh_pointer, int bits);
 /* Time every stiffness variant over `reps` full passes and keep the fastest.
  * Must run on a wavefield at rest (after prepare_fields_elastic_device, before
  * the first step): zero fields make the passes leave every array unchanged;
- * returns SF3D_ERR_STATE otherwise.  ms_per_variant (8 floats) and
+ * returns SF3D_ERR_STATE otherwise.  ms_per_variant (10 floats) and
  * best_variant may be NULL.  No reference counterpart. */
 int sf3d_autotune_stiffness(long *Mesh_pointer, int reps, float *ms_per_variant, int *best_variant);
 
@@ -385,6 +387,9 @@ int sf3d_gradient_forward(long *Mesh_pointer, realw deltat);
 int sf3d_gradient_set_residual(long *Mesh_pointer, const realw *residual);
 /* Reverse sweep: recompute each segment, apply the transposed steps, accumulate. */
 int sf3d_gradient_backward(long *Mesh_pointer, realw deltat);
+/* 1 (default): the transposed stiffness K p and the gradient terms of an element
+ * in one kernel; 0: the stiffness kernel on p, then a separate gradient kernel. */
+int sf3d_gradient_set_fused(long *Mesh_pointer, int fused);
 /* dJ/drho, dJ/dkappa, dJ/dmu per GLL point, layout (5,5,5,NSPEC); any may be NULL. */
 int sf3d_gradient_get(long *Mesh_pointer, double *g_rho, double *g_kappa, double *g_mu);
 /* Free the gradient buffers (also freed by prepare_cleanup_device). */

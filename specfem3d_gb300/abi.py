@@ -83,6 +83,8 @@ def load() -> ctypes.CDLL:
     L.sf3d_gradient_set_residual.argtypes = [P, P]
     L.sf3d_gradient_get.restype = ctypes.c_int
     L.sf3d_gradient_get.argtypes = [P, P, P, P]
+    L.sf3d_gradient_set_fused.restype = ctypes.c_int
+    L.sf3d_gradient_set_fused.argtypes = [P, ctypes.c_int]
     L.sf3d_gradient_release.restype = ctypes.c_int
     L.sf3d_gradient_release.argtypes = [P]
     L.sf3d_field_maxabs_noalloc.restype = ctypes.c_int

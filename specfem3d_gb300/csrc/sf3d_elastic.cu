@@ -31,7 +31,32 @@ __device__ __forceinline__ void cp_async4(void* smem, const void* gmem) {
 // each point (15 KB per element) are copied into shared memory with cp.async
 // instead of being held in registers from the start of the kernel to the end,
 // so the kernel fits a smaller register budget (more resident CTAs per SM).
-template <bool ATT, bool STRAIN, int MINB, bool HALF = false, bool STAGE = false, bool ATOMIC = true>
+// Element streams are read and written exactly once per launch: with STREAM
+// they carry evict-first hints (ld.global.cs / st.global.cs) so that L2 keeps
+// the gathered displacement / velocity and the scattered acceleration, which
+// neighbouring elements reuse.
+template <bool STREAM>
+__device__ __forceinline__ float ld_elem(const float* p) {
+  return STREAM ? __ldcs(p) : __ldg(p);
+}
+template <bool STREAM>
+__device__ __forceinline__ int ld_elem(const int* p) {
+  return STREAM ? __ldcs(p) : __ldg(p);
+}
+template <bool STREAM>
+__device__ __forceinline__ float ld_state(const float* p) {
+  return STREAM ? __ldcs(p) : *p;
+}
+template <bool STREAM>
+__device__ __forceinline__ void st_state(float* p, float v) {
+  if (STREAM)
+    __stcs(p, v);
+  else
+    *p = v;
+}
+
+template <bool ATT, bool STRAIN, int MINB, bool HALF = false, bool STAGE = false, bool ATOMIC = true,
+          bool STREAM = false>
 __global__ void __launch_bounds__(NGLL3_PAD, MINB) stiffness_kernel(const StiffnessArgs a) {
   __shared__ __align__(16) float s_att[(ATT && STAGE) ? 30 : 1][NGLL3_PAD];
   __shared__ float s_gll[NGLL3];
@@ -80,7 +105,7 @@ __global__ void __launch_bounds__(NGLL3_PAD, MINB) stiffness_kernel(const Stiffn
     asm volatile("cp.async.commit_group;" ::: "memory");
   }
   if (active) {
-    iglob = __ldg(a.ibool + eo);
+    iglob = ld_elem<STREAM>(a.ibool + eo);
     if (HALF) {
       // 16-bit storage with a per-element (offset, scale): value = offset + scale * h
       const float2 ks = __ldg(a.kso + e), ms = __ldg(a.muso + e);
@@ -95,12 +120,12 @@ __global__ void __launch_bounds__(NGLL3_PAD, MINB) stiffness_kernel(const Stiffn
         }
       }
     } else {
-      kap = __ldg(a.kappav + eo);
-      mu = __ldg(a.muv + eo);
+      kap = ld_elem<STREAM>(a.kappav + eo);
+      mu = ld_elem<STREAM>(a.muv + eo);
       if (ir >= 0) {
         const long mo = (long)ir * NGLL3_PAD + t;
 #pragma unroll
-        for (int q = 0; q < 9; ++q) m[q] = __ldg(a.m[q] + mo);
+        for (int q = 0; q < 9; ++q) m[q] = ld_elem<STREAM>(a.m[q] + mo);
       }
     }
     if (ATT && !STAGE) {
@@ -108,13 +133,13 @@ __global__ void __launch_bounds__(NGLL3_PAD, MINB) stiffness_kernel(const Stiffn
 #pragma unroll
       for (int c = 0; c < 6; ++c)
 #pragma unroll
-        for (int s = 0; s < NSLS; ++s) R[c][s] = a.R[c][so + s * NGLL3_PAD];
+        for (int s = 0; s < NSLS; ++s) R[c][s] = ld_state<STREAM>(a.R[c] + so + s * NGLL3_PAD);
 #pragma unroll
-      for (int c = 0; c < 6; ++c) eold[c] = a.eps[c][eo];
+      for (int c = 0; c < 6; ++c) eold[c] = ld_state<STREAM>(a.eps[c] + eo);
 #pragma unroll
       for (int s = 0; s < NSLS; ++s) {
-        fc[s] = __ldg(a.fc + so + s * NGLL3_PAD);
-        fck[s] = __ldg(a.fck + so + s * NGLL3_PAD);
+        fc[s] = ld_elem<STREAM>(a.fc + so + s * NGLL3_PAD);
+        fck[s] = ld_elem<STREAM>(a.fck + so + s * NGLL3_PAD);
       }
     }
     ux = a.displ[3L * iglob];
@@ -294,33 +319,33 @@ __global__ void __launch_bounds__(NGLL3_PAD, MINB) stiffness_kernel(const Stiffn
         const float al = a.alpha[s], be = a.beta[s], ga = a.gamma[s];
         const float fk = fkap * (STAGE ? s_att[27 + s][t] : fck[s]);
         const float r5 = STAGE ? s_att[15 + s][t] : R[5][s];
-        a.R[5][so + s * NGLL3_PAD] = al * r5 + fk * (be * eold[5] + ga * epsl[5]);
+        st_state<STREAM>(a.R[5] + so + s * NGLL3_PAD, al * r5 + fk * (be * eold[5] + ga * epsl[5]));
         const float fm = fmu * (STAGE ? s_att[24 + s][t] : fc[s]);
 #pragma unroll
         for (int c = 0; c < 5; ++c) {
           const float rc = STAGE ? s_att[3 * c + s][t] : R[c][s];
-          a.R[c][so + s * NGLL3_PAD] = al * rc + fm * (be * eold[c] + ga * epsl[c]);
+          st_state<STREAM>(a.R[c] + so + s * NGLL3_PAD, al * rc + fm * (be * eold[c] + ga * epsl[c]));
         }
       }
     }
     if (STRAIN) {
-      if (ATT) a.eps[5][eo] = epsl[5];
+      if (ATT) st_state<STREAM>(a.eps[5] + eo, epsl[5]);
 #pragma unroll
       for (int c = 0; c < 5; ++c)
-        if (a.eps[c]) a.eps[c][eo] = epsl[c];
+        if (a.eps[c]) st_state<STREAM>(a.eps[c] + eo, epsl[c]);
     }
   }
 }
 
-template <int MINB, bool HALF, bool STAGE = false>
+template <int MINB, bool HALF, bool STAGE = false, bool STREAM = false>
 void launch_minb(const StiffnessArgs& a, bool att, bool store_strain, cudaStream_t s) {
   dim3 grid(a.nelem), block(NGLL3_PAD);
   if (att)
-    stiffness_kernel<true, true, MINB, HALF, STAGE><<<grid, block, 0, s>>>(a);
+    stiffness_kernel<true, true, MINB, HALF, STAGE, true, STREAM><<<grid, block, 0, s>>>(a);
   else if (store_strain)
-    stiffness_kernel<false, true, MINB, HALF><<<grid, block, 0, s>>>(a);
+    stiffness_kernel<false, true, MINB, HALF, false, true, STREAM><<<grid, block, 0, s>>>(a);
   else
-    stiffness_kernel<false, false, MINB, HALF><<<grid, block, 0, s>>>(a);
+    stiffness_kernel<false, false, MINB, HALF, false, true, STREAM><<<grid, block, 0, s>>>(a);
 }
 
 }  // namespace
@@ -330,8 +355,15 @@ void launch_minb(const StiffnessArgs& a, bool att, bool store_strain, cudaStream
 // let the compiler keep every load of an element in registers).  The 16-bit
 // geometry builds exist for 6 and 7 CTAs/SM.
 void launch_stiffness(const StiffnessArgs& a, bool att, bool store_strain, cudaStream_t s, int blocks_per_sm,
-                      bool half_geometry, bool staged) {
+                      bool half_geometry, bool staged, bool streaming) {
   if (a.nelem <= 0) return;
+  if (streaming) {
+    if (blocks_per_sm == 7)
+      launch_minb<7, false, false, true>(a, att, store_strain, s);
+    else
+      launch_minb<6, false, false, true>(a, att, store_strain, s);
+    return;
+  }
   if (staged) {
     // cp.async-staged memory variables (attenuation); without attenuation the
     // same register budgets of the plain build

@@ -128,6 +128,9 @@ struct GradArgs {
   double* g_rho;
   double* g_kappa;
   double* g_mu;
+  const float* kappav; // fused form: moduli and the K p accumulator
+  const float* muv;
+  float* kp;
 };
 
 // Gradient of the 3x3 displacement derivative of a field staged in shared memory.
@@ -221,6 +224,135 @@ __global__ void __launch_bounds__(NGLL3_PAD) grad_accum_kernel(const GradArgs a)
   a.g_rho[eo] += wj * (double)pa;
 }
 
+// Fused form of one element's part of the transposed step: K p (the elastic
+// stiffness applied to p, arithmetic of stiffness_kernel<ATT=0>) scatter-added
+// into kp, and the gradient contributions of grad_accum_kernel, from one gather
+// of p and one set of p derivatives.
+__global__ void __launch_bounds__(NGLL3_PAD, 5) adj_stiffness_grad_kernel(const GradArgs a) {
+  __shared__ float s_gll[NGLL3];
+  __shared__ float s_p[3][NGLL3_PAD];
+  __shared__ float s_u[3][NGLL3_PAD];
+  __shared__ float s_t[9][NGLL3_PAD];
+  const int t = threadIdx.x;
+  const int e = a.phase ? __ldg(a.phase + blockIdx.x) : (int)blockIdx.x;
+  const bool active = t < NGLL3;
+  const int k = t / NGLL2, j = (t / NGLLX) % NGLLX, i = t % NGLLX;
+  const long eo = (long)e * NGLL3_PAD + t;
+  float pa = 0.f, kap = 0.f, mu = 0.f;
+  int g = 0;
+  if (active) {
+    s_gll[t] = __ldg(a.gll + t);
+    g = __ldg(a.ibool + eo);
+    kap = __ldg(a.kappav + eo);
+    mu = __ldg(a.muv + eo);
+#pragma unroll
+    for (int c = 0; c < 3; ++c) {
+      s_p[c][t] = a.p[3L * g + c];
+      s_u[c][t] = a.u[3L * g + c] * a.uscale;
+    }
+    pa = s_p[0][t] * (a.araw[3L * g] * a.uscale * __ldg(a.rmx + g)) +
+         s_p[1][t] * (a.araw[3L * g + 1] * a.uscale * __ldg(a.rmy + g)) +
+         s_p[2][t] * (a.araw[3L * g + 2] * a.uscale * __ldg(a.rmz + g));
+  }
+  __syncthreads();
+  const int ir = __ldg(a.irregular + e);
+  if (active) {
+    float tp[3][3], tu[3][3];
+    local_grad(s_p, s_gll, i, j, k, tp);
+    local_grad(s_u, s_gll, i, j, k, tu);
+    float dp[3][3], du[3][3], jac, m[9];
+#pragma unroll
+    for (int q = 0; q < 9; ++q) m[q] = 0.f;
+    if (ir >= 0) {
+      const long mo = (long)ir * NGLL3_PAD + t;
+#pragma unroll
+      for (int q = 0; q < 9; ++q) m[q] = __ldg(a.m[q] + mo);
+#pragma unroll
+      for (int c = 0; c < 3; ++c)
+#pragma unroll
+        for (int x = 0; x < 3; ++x) {
+          dp[c][x] = m[x] * tp[c][0] + m[3 + x] * tp[c][1] + m[6 + x] * tp[c][2];
+          du[c][x] = m[x] * tu[c][0] + m[3 + x] * tu[c][1] + m[6 + x] * tu[c][2];
+        }
+      jac = 1.f / (m[0] * (m[4] * m[8] - m[5] * m[7]) - m[1] * (m[3] * m[8] - m[5] * m[6]) +
+                   m[2] * (m[3] * m[7] - m[4] * m[6]));
+    } else {
+#pragma unroll
+      for (int c = 0; c < 3; ++c)
+#pragma unroll
+        for (int x = 0; x < 3; ++x) {
+          dp[c][x] = a.xix_regular * tp[c][x];
+          du[c][x] = a.xix_regular * tu[c][x];
+        }
+      jac = a.jacobian_regular;
+    }
+    // gradient contributions
+    const float trp = dp[0][0] + dp[1][1] + dp[2][2];
+    const float tru = du[0][0] + du[1][1] + du[2][2];
+    float dd = 0.f;
+#pragma unroll
+    for (int x = 0; x < 3; ++x) dd += (dp[x][x] - trp * (1.f / 3.f)) * (du[x][x] - tru * (1.f / 3.f));
+    const float exy_p = 0.5f * (dp[0][1] + dp[1][0]), exz_p = 0.5f * (dp[0][2] + dp[2][0]),
+                eyz_p = 0.5f * (dp[1][2] + dp[2][1]);
+    const float exy_u = 0.5f * (du[0][1] + du[1][0]), exz_u = 0.5f * (du[0][2] + du[2][0]),
+                eyz_u = 0.5f * (du[1][2] + du[2][1]);
+    dd += 2.f * (exy_p * exy_u + exz_p * exz_u + eyz_p * eyz_u);
+    const double wj = (double)(a.w[i] * a.w[j] * a.w[k]) * (double)jac;
+    a.g_kappa[eo] += wj * (double)trp * (double)tru;
+    a.g_mu[eo] += wj * 2.0 * (double)dd;
+    a.g_rho[eo] += wj * (double)pa;
+    // stress of p (stiffness_kernel<ATT=0> arithmetic)
+    const float dxx = dp[0][0], dxy = dp[0][1], dxz = dp[0][2];
+    const float dyx = dp[1][0], dyy = dp[1][1], dyz = dp[1][2];
+    const float dzx = dp[2][0], dzy = dp[2][1], dzz = dp[2][2];
+    const float l2m = kap + (4.f / 3.f) * mu;
+    const float lam = l2m - 2.f * mu;
+    const float sxx = l2m * dxx + lam * (dyy + dzz);
+    const float syy = l2m * dyy + lam * (dxx + dzz);
+    const float szz = l2m * dzz + lam * (dxx + dyy);
+    const float sxy = mu * (dxy + dyx);
+    const float sxz = mu * (dzx + dxz);
+    const float syz = mu * (dzy + dyz);
+    if (ir >= 0) {
+      const float xix = m[0], xiy = m[1], xiz = m[2], etax = m[3], etay = m[4], etaz = m[5];
+      const float gammax = m[6], gammay = m[7], gammaz = m[8];
+      s_t[0][t] = jac * (sxx * xix + sxy * xiy + sxz * xiz);
+      s_t[1][t] = jac * (sxy * xix + syy * xiy + syz * xiz);
+      s_t[2][t] = jac * (sxz * xix + syz * xiy + szz * xiz);
+      s_t[3][t] = jac * (sxx * etax + sxy * etay + sxz * etaz);
+      s_t[4][t] = jac * (sxy * etax + syy * etay + syz * etaz);
+      s_t[5][t] = jac * (sxz * etax + syz * etay + szz * etaz);
+      s_t[6][t] = jac * (sxx * gammax + sxy * gammay + sxz * gammaz);
+      s_t[7][t] = jac * (sxy * gammax + syy * gammay + syz * gammaz);
+      s_t[8][t] = jac * (sxz * gammax + syz * gammay + szz * gammaz);
+    } else {
+      const float js = a.jacobian_regular * a.xix_regular;
+      s_t[0][t] = js * sxx; s_t[1][t] = js * sxy; s_t[2][t] = js * sxz;
+      s_t[3][t] = js * sxy; s_t[4][t] = js * syy; s_t[5][t] = js * syz;
+      s_t[6][t] = js * sxz; s_t[7][t] = js * syz; s_t[8][t] = js * szz;
+    }
+  }
+  __syncthreads();
+  if (active) {
+    const float* hpw = s_gll + NGLL2;
+    float n1x = 0.f, n2x = 0.f, n3x = 0.f, n1y = 0.f, n2y = 0.f, n3y = 0.f, n1z = 0.f, n2z = 0.f, n3z = 0.f;
+#pragma unroll
+    for (int l = 0; l < NGLLX; ++l) {
+      const float f1 = hpw[l + NGLLX * i], f2 = hpw[l + NGLLX * j], f3 = hpw[l + NGLLX * k];
+      const int p1 = l + NGLLX * j + NGLL2 * k, p2 = i + NGLLX * l + NGLL2 * k, p3 = i + NGLLX * j + NGLL2 * l;
+      n1x = fmaf(s_t[0][p1], f1, n1x); n1y = fmaf(s_t[1][p1], f1, n1y); n1z = fmaf(s_t[2][p1], f1, n1z);
+      n2x = fmaf(s_t[3][p2], f2, n2x); n2y = fmaf(s_t[4][p2], f2, n2y); n2z = fmaf(s_t[5][p2], f2, n2z);
+      n3x = fmaf(s_t[6][p3], f3, n3x); n3y = fmaf(s_t[7][p3], f3, n3y); n3z = fmaf(s_t[8][p3], f3, n3z);
+    }
+    const float fac1 = s_gll[4 * NGLL2 + j + NGLLX * k];
+    const float fac2 = s_gll[3 * NGLL2 + i + NGLLX * k];
+    const float fac3 = s_gll[2 * NGLL2 + i + NGLLX * j];
+    atomicAdd(a.kp + 3L * g, -(fac1 * n1x + fac2 * n2x + fac3 * n3x));
+    atomicAdd(a.kp + 3L * g + 1, -(fac1 * n1y + fac2 * n2y + fac3 * n3y));
+    atomicAdd(a.kp + 3L * g + 2, -(fac1 * n1z + fac2 * n2z + fac3 * n3z));
+  }
+}
+
 bool alloc_f(float** d, size_t n) { return alloc_zero((void**)d, sizeof(float) * n); }
 
 }  // namespace
@@ -286,7 +418,7 @@ void adjoint_step(Mesh* mp, int n, const float* u, const float* araw, float dt, 
   for (int iphase = 1; iphase <= 2; ++iphase) {
     StiffnessArgs a = stiffness_args(mp, tmp, iphase, dt, false, false, false);
     if (a.nelem <= 0) continue;
-    run_stiffness(mp, a, false, false, s);
+    if (!G->fused) run_stiffness(mp, a, false, false, s);
     GradArgs ga;
     memset(&ga, 0, sizeof(ga));
     ga.nelem = a.nelem;
@@ -308,7 +440,13 @@ void adjoint_step(Mesh* mp, int n, const float* u, const float* araw, float dt, 
     ga.g_rho = G->g_rho;
     ga.g_kappa = G->g_kappa;
     ga.g_mu = G->g_mu;
-    grad_accum_kernel<<<a.nelem, NGLL3_PAD, 0, s>>>(ga);
+    ga.kappav = mp->d_kappav;
+    ga.muv = mp->d_muv;
+    ga.kp = G->kp;
+    if (G->fused)
+      adj_stiffness_grad_kernel<<<a.nelem, NGLL3_PAD, 0, s>>>(ga);
+    else
+      grad_accum_kernel<<<a.nelem, NGLL3_PAD, 0, s>>>(ga);
   }
   adj_update_kernel<<<nblk(n3, 256), 256, 0, s>>>(G->adj_u, G->adj_v, G->adj_a, G->kp, G->bp, G->p, mp->d_rmassx,
                                                   mp->d_rmassy, mp->d_rmassz, mp->nglob, dt, dt2, dtsq2);
@@ -484,6 +622,14 @@ int sf3d_gradient_backward(long* Mesh_pointer, realw deltat) {
   cudaEventElapsedTime(&mp->last_total_ms, mp->ev0, mp->ev1);
   if (!check_kernel_error(mp)) return SF3D_ERR_CUDA;
   return sf3d_last_error(nullptr, 0);
+}
+
+int sf3d_gradient_set_fused(long* Mesh_pointer, int fused) {
+  Mesh* mp = get_mesh(Mesh_pointer);
+  if (!mp) return SF3D_ERR_STATE;
+  if (!mp->grad) { set_error(SF3D_ERR_STATE, "sf3d_gradient_setup not called"); return SF3D_ERR_STATE; }
+  mp->grad->fused = fused ? 1 : 0;
+  return SF3D_OK;
 }
 
 int sf3d_gradient_get(long* Mesh_pointer, double* g_rho, double* g_kappa, double* g_mu) {

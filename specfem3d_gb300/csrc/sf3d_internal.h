@@ -69,6 +69,7 @@ struct GradState {
   float wgll[NGLLX] = {};
   double res_scale = 1.0;      // power of two applied to the residual (undone in sf3d_gradient_get)
   float u_scale = 1.f;         // power of two applied to the forward field in the strain products
+  int fused = 1;               // 1: K p and the gradient terms in one kernel per element
   size_t bytes = 0;
 };
 
@@ -293,17 +294,19 @@ struct StiffnessArgs {
 };
 
 void launch_stiffness(const StiffnessArgs& a, bool att, bool store_strain, cudaStream_t s, int blocks_per_sm,
-                      bool half_geometry = false, bool staged = false);
+                      bool half_geometry = false, bool staged = false, bool streaming = false);
 void launch_stiffness_pipelined(const StiffnessArgs& a, bool att, bool store_strain, int* err, cudaStream_t s);
 // stiffness kernel variants (sf3d_set_stiffness_variant / sf3d_autotune_stiffness)
 //   0, 2, 3, 4: one CTA per element at 4, 5, 6, 7 CTAs/SM; 1: persistent bulk-copy pipeline;
-//   5, 6, 7: one CTA per element with cp.async-staged memory variables at 6, 7, 8 CTAs/SM
-constexpr int kNumStiffnessVariants = 8;
+//   5, 6, 7: one CTA per element with cp.async-staged memory variables at 6, 7, 8 CTAs/SM;
+//   8, 9: one CTA per element, evict-first hints on the element streams, 6 and 7 CTAs/SM
+constexpr int kNumStiffnessVariants = 10;
 inline int variant_blocks_per_sm(int v) {
-  const int t[kNumStiffnessVariants] = {4, 0, 5, 6, 7, 6, 7, 8};
+  const int t[kNumStiffnessVariants] = {4, 0, 5, 6, 7, 6, 7, 8, 6, 7};
   return (v >= 0 && v < kNumStiffnessVariants) ? t[v] : 4;
 }
-inline bool variant_staged(int v) { return v >= 5; }
+inline bool variant_staged(int v) { return v >= 5 && v <= 7; }
+inline bool variant_streaming(int v) { return v >= 8; }
 void free_grad(Mesh* mp);
 void free_batch(Mesh* mp);
 void free_half_geometry(Mesh* mp);
@@ -360,7 +363,7 @@ inline void run_stiffness(Mesh* mp, const StiffnessArgs& a, bool att, bool store
     launch_stiffness_pipelined(a, att, store_strain, mp->d_kerr, s);
   } else {
     launch_stiffness(a, att, store_strain, s, variant_blocks_per_sm(mp->stiffness_variant), false,
-                     variant_staged(mp->stiffness_variant));
+                     variant_staged(mp->stiffness_variant), variant_streaming(mp->stiffness_variant));
   }
 }
 void launch_pressure_seismograms(Mesh* mp, int slot);

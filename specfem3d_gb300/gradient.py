@@ -115,7 +115,7 @@ class MisfitGradient:
     """One shot: forward from rest with checkpoints every ``checkpoint_every``
     steps, then the adjoint sweep for a given residual."""
 
-    def __init__(self, db: dict, cfg: dict, checkpoint_every: int = 200):
+    def __init__(self, db: dict, cfg: dict, checkpoint_every: int = 200, fused: bool = True):
         cfg = dict(cfg)
         cfg["record"] = ("displ",)
         self.cfg, self.db = cfg, db
@@ -127,6 +127,8 @@ class MisfitGradient:
         if rc != 0:
             abi.check()
         self.device_bytes = nbytes.value
+        if self.L.sf3d_gradient_set_fused(self.solver.mp, int(bool(fused))) != 0:
+            abi.check()
 
     @property
     def dt(self) -> float:
@@ -174,7 +176,7 @@ def shot_config(cfg: dict, shot: int) -> dict:
     return c
 
 
-def misfit_gradient(db_of_shot, cfg: dict, observed, checkpoint_every: int = 200):
+def misfit_gradient(db_of_shot, cfg: dict, observed, checkpoint_every: int = 200, fused: bool = True):
     """Sum over shots of the misfit and its gradient.  ``db_of_shot(i)`` returns the
     database of shot i (same mesh and model, shot i's source); ``observed[i]`` its
     observed traces (nrec, 3, nstep)."""
@@ -182,7 +184,7 @@ def misfit_gradient(db_of_shot, cfg: dict, observed, checkpoint_every: int = 200
     grad = None
     timing = []
     for i, obs in enumerate(observed):
-        mg = MisfitGradient(db_of_shot(i), shot_config(cfg, i), checkpoint_every)
+        mg = MisfitGradient(db_of_shot(i), shot_config(cfg, i), checkpoint_every, fused)
         seis = mg.forward()
         J, res = misfit(seis, obs, mg.dt)
         g = mg.gradient(res)

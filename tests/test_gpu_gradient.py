@@ -91,3 +91,15 @@ def test_autograd_wrapper(problem):
     for t, k in zip(z, ("rho", "kappa", "mu")):
         # two device runs: atomics reorder the FP32 sums
         assert rel_l2(t.grad.numpy(), grad[k] * problem.stores[k]) < 1e-4
+
+
+def test_fused_and_separate_adjoint_kernels_agree(problem):
+    """K p and the gradient terms in one kernel per element (default) give the
+    gradient of the stiffness kernel followed by the separate gradient kernel."""
+    from specfem3d_gb300 import gradient as G
+    _, g1, t1 = G.misfit_gradient(lambda i: G.shot_database(problem.db, problem.cfg, i), problem.cfg,
+                                  problem.observed, problem.every, fused=True)
+    _, g2, t2 = G.misfit_gradient(lambda i: G.shot_database(problem.db, problem.cfg, i), problem.cfg,
+                                  problem.observed, problem.every, fused=False)
+    for k in ("rho", "kappa", "mu"):
+        assert rel_l2(g1[k], g2[k]) < 5e-5, k
