@@ -305,7 +305,7 @@ def main():
         autotune = None
     else:
         # fields are at rest: time every stiffness variant and keep the fastest
-        ms = (ctypes.c_float * 10)()
+        ms = (ctypes.c_float * 12)()
         best = ctypes.c_int()
         if L.sf3d_autotune_stiffness(g.mp, 3, ms, ctypes.addressof(best)) != 0:
             abi.check()
@@ -379,9 +379,11 @@ def main():
                                       "(profiles/stiffness_kernel_att_6ctas_layered_32x32x16.md) x elements; "
                                       "the field gathers of that capture stayed in L2"),
                      "kernel": ("stiffness_pipe_kernel<att>" if args.variant == 1 else
-                                f"stiffness_kernel<att, {[4, 0, 5, 6, 7, 6, 7, 8, 6, 7][args.variant]} CTAs/SM"
+                                f"stiffness_{'split_' if args.variant >= 10 else ''}kernel<att, "
+                                f"{[4, 0, 5, 6, 7, 6, 7, 8, 6, 7, 3, 4][args.variant]} CTAs/SM"
                                 + (", cp.async-staged memory variables>" if 5 <= args.variant <= 7 else
-                                   ", evict-first element streams>" if args.variant >= 8 else ">")),
+                                   ", evict-first element streams>" if args.variant in (8, 9) else
+                                   ", 3 threads per point>" if args.variant >= 10 else ">")),
                      "autotune": autotune,
                      "algorithmic_bytes_per_launch": bytes_launch,
                      "mean_launch_ms": stiff_ms, "timed_launches": tk["stiffness_launches"]},

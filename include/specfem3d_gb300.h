@@ -312,7 +312,9 @@ int sf3d_last_timing(long *Mesh_pointer, float *stiffness_ms, int *stiffness_lau
  *               attenuation factors staged in shared memory by cp.async, for
  *               6, 7, 8 CTAs per SM (register budget 80, 72, 64);
  *   8, 9:       one CTA per element, evict-first cache hints on the element
- *               streams (read and written once per launch), 6 and 7 CTAs/SM.
+ *               streams (read and written once per launch), 6 and 7 CTAs/SM;
+ *   10, 11:     three threads per GLL point (one per displacement component),
+ *               384-thread CTAs, 3 and 4 CTAs/SM.
  * Default 3 (the fastest on GB300 for the layered viscoelastic workload).
  * No reference counterpart (the reference compiles one Kernel_2 per
  * configuration). */
@@ -328,7 +330,7 @@ int sf3d_set_geometry_precision(long *Mesh_pointer, int bits);
 /* Time every stiffness variant over `reps` full passes and keep the fastest.
  * Must run on a wavefield at rest (after prepare_fields_elastic_device, before
  * the first step): zero fields make the passes leave every array unchanged;
- * returns SF3D_ERR_STATE otherwise.  ms_per_variant (10 floats) and
+ * returns SF3D_ERR_STATE otherwise.  ms_per_variant (12 floats) and
  * best_variant may be NULL.  No reference counterpart. */
 int sf3d_autotune_stiffness(long *Mesh_pointer, int reps, float *ms_per_variant, int *best_variant);
 

@@ -299,14 +299,17 @@ void launch_stiffness_pipelined(const StiffnessArgs& a, bool att, bool store_str
 // stiffness kernel variants (sf3d_set_stiffness_variant / sf3d_autotune_stiffness)
 //   0, 2, 3, 4: one CTA per element at 4, 5, 6, 7 CTAs/SM; 1: persistent bulk-copy pipeline;
 //   5, 6, 7: one CTA per element with cp.async-staged memory variables at 6, 7, 8 CTAs/SM;
-//   8, 9: one CTA per element, evict-first hints on the element streams, 6 and 7 CTAs/SM
-constexpr int kNumStiffnessVariants = 10;
+//   8, 9: one CTA per element, evict-first hints on the element streams, 6 and 7 CTAs/SM;
+//   10, 11: three threads per point (384-thread CTAs), 3 and 4 CTAs/SM
+constexpr int kNumStiffnessVariants = 12;
 inline int variant_blocks_per_sm(int v) {
-  const int t[kNumStiffnessVariants] = {4, 0, 5, 6, 7, 6, 7, 8, 6, 7};
+  const int t[kNumStiffnessVariants] = {4, 0, 5, 6, 7, 6, 7, 8, 6, 7, 3, 4};
   return (v >= 0 && v < kNumStiffnessVariants) ? t[v] : 4;
 }
 inline bool variant_staged(int v) { return v >= 5 && v <= 7; }
-inline bool variant_streaming(int v) { return v >= 8; }
+inline bool variant_streaming(int v) { return v == 8 || v == 9; }
+inline bool variant_split(int v) { return v >= 10; }
+void launch_stiffness_split(const StiffnessArgs& a, bool att, bool store_strain, cudaStream_t s, int blocks_per_sm);
 void free_grad(Mesh* mp);
 void free_batch(Mesh* mp);
 void free_half_geometry(Mesh* mp);
@@ -361,6 +364,8 @@ inline void run_stiffness(Mesh* mp, const StiffnessArgs& a, bool att, bool store
     launch_stiffness(h, att, store_strain, s, mp->stiffness_variant == 4 ? 7 : 6, true);
   } else if (mp->stiffness_variant == 1 && mp->d_kerr) {
     launch_stiffness_pipelined(a, att, store_strain, mp->d_kerr, s);
+  } else if (variant_split(mp->stiffness_variant)) {
+    launch_stiffness_split(a, att, store_strain, s, variant_blocks_per_sm(mp->stiffness_variant));
   } else {
     launch_stiffness(a, att, store_strain, s, variant_blocks_per_sm(mp->stiffness_variant), false,
                      variant_staged(mp->stiffness_variant), variant_streaming(mp->stiffness_variant));
