@@ -150,7 +150,10 @@ void compute_add_sources_el_cuda_(long *Mesh_pointer, double *h_stf_pre_compute,
 void compute_add_sources_el_s3_cuda_(long *Mesh_pointer, double *h_stf_pre_compute, int *h_NSOURCES);
 
 /* kernel_3_a_cuda (update_displacement_cuda.cu:287-380): a *= rmass{x,y,z};
- * v += dt/2 a (fused mass + corrector without ocean load). */
+ * v += dt/2 a (fused mass + corrector without ocean load).  The pass is
+ * deferred and fused with the next update_displacement_cuda of the same field
+ * (one streaming pass instead of two); every other entry point applies it
+ * first, so callers observe the reference's fields. */
 void kernel_3_a_cuda_(long *Mesh_pointer, realw *deltatover2_F, realw *b_deltatover2_F,
                       int *APPROXIMATE_OCEAN_LOAD, int *FORWARD_OR_ADJOINT);
 

@@ -1,7 +1,7 @@
 """ctypes front end of the CPU oracle (TEST INFRASTRUCTURE ONLY).
 
 Only ``tests/``, ``__graft_entry__.smoke()`` and ``bench.py``'s CPU-baseline leg
-may import this module; it is the checker, never the product.  It builds
+may import this module; it is test infrastructure, never the product.  It builds
 ``liboracle_f32.so`` / ``liboracle_f64.so`` from ``sem_oracle.c`` and restates
 the reference's database generation for a regular layered block:
 

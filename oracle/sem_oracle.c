@@ -1,8 +1,8 @@
 /*
  * CPU oracle for the SPECFEM3D Cartesian spectral-element time step.
  *
- * TEST INFRASTRUCTURE ONLY: the checker for the GB300 CUDA path.  See
- * sem_oracle.h for the layout conventions.  Every routine below restates the
+ * TEST INFRASTRUCTURE ONLY: the reference against which the GB300 CUDA path is
+ * tested.  sem_oracle.h gives the layout conventions.  Every routine below restates the
  * reference's CPU algorithm; the citation is the reference file:line it follows
  * (paths relative to the SPECFEM3D source tree).
  */

@@ -1,8 +1,8 @@
 /*
  * CPU oracle for the SPECFEM3D Cartesian spectral-element time step.
  *
- * TEST INFRASTRUCTURE ONLY.  This library is the checker for the GB300 CUDA
- * path: only tests/, __graft_entry__.smoke() and bench.py's CPU-baseline leg
+ * TEST INFRASTRUCTURE ONLY.  The GB300 CUDA path is tested against this
+ * library: only tests/, __graft_entry__.smoke() and bench.py's CPU-baseline leg
  * may load it.  The product library never links or calls it.
  *
  * It restates, in plain C, the reference solver's CPU algorithms (file:line

@@ -228,6 +228,9 @@ struct Mesh {
   float2* d_mu_so = nullptr;
 
   cudaStream_t stream = nullptr;
+  // deferred mass + corrector of the forward [0] and backward [1] field, and its dt/2
+  int pend_corrector[2] = {0, 0};
+  float pend_dt2[2] = {0.f, 0.f};
   cudaEvent_t ev0 = nullptr, ev1 = nullptr;
   std::vector<cudaEvent_t> tev;           // timing mode: start/end event per stiffness step
   float last_stiff_ms = 0.f, last_total_ms = 0.f;
@@ -238,12 +241,21 @@ struct Mesh {
   size_t stage_bytes = 0;
 };
 
-inline Mesh* get_mesh(long* p) {
+// Applies deferred mass/corrector passes (kernel_3_a_cuda leaves its work for the
+// next update_displacement_cuda, which fuses it with the predictor).
+void flush_correctors(Mesh* mp);
+
+// Every entry point fetches its Mesh here; by default any deferred corrector is
+// applied first, so entry points that read or write veloc / accel see the state
+// the reference would leave.
+inline Mesh* get_mesh(long* p, bool flush = true) {
   if (!p || *p == 0) {
     set_error(SF3D_ERR_STATE, "Mesh_pointer is not prepared");
     return nullptr;
   }
-  return reinterpret_cast<Mesh*>(*p);
+  Mesh* mp = reinterpret_cast<Mesh*>(*p);
+  if (flush && (mp->pend_corrector[0] || mp->pend_corrector[1])) flush_correctors(mp);
+  return mp;
 }
 
 // element-major upload of a (5,5,5,n) host array into [n][128]

@@ -363,6 +363,19 @@ bool device_maxabs(Mesh* mp, const float* x, long n, float* out) {
   return true;
 }
 
+void flush_correctors(Mesh* mp) {
+  for (int idx = 0; idx < 2; ++idx) {
+    if (!mp->pend_corrector[idx]) continue;
+    mp->pend_corrector[idx] = 0;
+    Fields* F = idx == 0 ? &mp->f : &mp->b;
+    if (!F->veloc) continue;
+    mass_corrector_kernel<<<nblk(3L * mp->nglob, 256), 256, 0, mp->stream>>>(F->veloc, F->accel, mp->d_rmassx,
+                                                                            mp->d_rmassy, mp->d_rmassz, mp->nglob,
+                                                                            mp->pend_dt2[idx]);
+    cuda_ok(cudaGetLastError(), "mass_corrector_kernel");
+  }
+}
+
 }  // namespace sf3d
 
 using namespace sf3d;
@@ -371,11 +384,22 @@ extern "C" {
 
 void update_displacement_cuda_(long* Mesh_pointer, realw* deltat_F, realw* deltatover2_F, realw* deltatsqover2_F,
                                int* FORWARD_OR_ADJOINT) {
-  Mesh* mp = get_mesh(Mesh_pointer);
+  Mesh* mp = get_mesh(Mesh_pointer, false);
   if (!mp) return;
-  Fields* F = pick(mp, *FORWARD_OR_ADJOINT == 1 ? 1 : 3);
+  const int idx = *FORWARD_OR_ADJOINT == 1 ? 0 : 1;
+  Fields* F = pick(mp, idx == 0 ? 1 : 3);
   if (!F->displ) { set_error(SF3D_ERR_STATE, "update_displacement_cuda: field not allocated"); return; }
   const long n = 3L * mp->nglob;
+  if (mp->pend_corrector[idx] && mp->pend_dt2[idx] == *deltatover2_F) {
+    // the deferred corrector of the previous step fused with this predictor
+    mp->pend_corrector[idx] = 0;
+    corrector_predictor_kernel<<<nblk(n, 256), 256, 0, mp->stream>>>(F->displ, F->veloc, F->accel, mp->d_rmassx,
+                                                                    mp->d_rmassy, mp->d_rmassz, mp->nglob,
+                                                                    *deltat_F, *deltatover2_F, *deltatsqover2_F);
+    cuda_ok(cudaGetLastError(), "corrector_predictor_kernel");
+    return;
+  }
+  if (mp->pend_corrector[idx]) flush_correctors(mp);
   predictor_kernel<<<nblk(n, 256), 256, 0, mp->stream>>>(F->displ, F->veloc, F->accel, n, *deltat_F,
                                                           *deltatover2_F, *deltatsqover2_F);
   cuda_ok(cudaGetLastError(), "predictor_kernel");
@@ -475,17 +499,20 @@ void compute_add_sources_el_s3_cuda_(long* Mesh_pointer, double* h_stf_pre_compu
   add_sources(Mesh_pointer, h_stf_pre_compute, h_NSOURCES, true);
 }
 
+// Deferred: the mass matrix and corrector run at the next update_displacement_cuda
+// of the same field (fused with its predictor), or before any other entry point
+// (get_mesh) -- the reference's call sequence sees the same fields.
 void kernel_3_a_cuda_(long* Mesh_pointer, realw* deltatover2_F, realw* b_deltatover2_F, int* APPROXIMATE_OCEAN_LOAD,
                       int* FORWARD_OR_ADJOINT) {
-  Mesh* mp = get_mesh(Mesh_pointer);
+  Mesh* mp = get_mesh(Mesh_pointer, false);
   if (!mp) return;
   if (*FORWARD_OR_ADJOINT != 1 && *FORWARD_OR_ADJOINT != 3) { set_error(SF3D_ERR_ARG, "invalid FORWARD_OR_ADJOINT"); return; }
   if (*APPROXIMATE_OCEAN_LOAD) { set_error(SF3D_ERR_ARG, "ocean load is not supported"); return; }
-  Fields* F = pick(mp, *FORWARD_OR_ADJOINT);
-  const float dt2 = *FORWARD_OR_ADJOINT == 1 ? *deltatover2_F : *b_deltatover2_F;
-  mass_corrector_kernel<<<nblk(3L * mp->nglob, 256), 256, 0, mp->stream>>>(F->veloc, F->accel, mp->d_rmassx, mp->d_rmassy,
-                                                                     mp->d_rmassz, mp->nglob, dt2);
-  cuda_ok(cudaGetLastError(), "mass_corrector_kernel");
+  const int idx = *FORWARD_OR_ADJOINT == 1 ? 0 : 1;
+  if (!pick(mp, *FORWARD_OR_ADJOINT)->veloc) { set_error(SF3D_ERR_STATE, "kernel_3_a_cuda: field not allocated"); return; }
+  if (mp->pend_corrector[idx]) flush_correctors(mp);
+  mp->pend_corrector[idx] = 1;
+  mp->pend_dt2[idx] = *FORWARD_OR_ADJOINT == 1 ? *deltatover2_F : *b_deltatover2_F;
 }
 
 void kernel_3_b_cuda_(long* Mesh_pointer, realw* deltatover2_F, realw* b_deltatover2_F, int* FORWARD_OR_ADJOINT) {
@@ -503,8 +530,10 @@ void compute_seismograms_cuda_(long* Mesh_pointer_f, realw* seismograms_d, realw
                                int* nlength_seismogramf, int* itf, int* it_endf, int* ACOUSTIC_SIMULATION,
                                int* ELASTIC_SIMULATION, int* USE_TRICK_FOR_BETTER_PRESSURE) {
   (void)seismograms_p; (void)ACOUSTIC_SIMULATION; (void)ELASTIC_SIMULATION;
-  Mesh* mp = get_mesh(Mesh_pointer_f);
+  Mesh* mp = get_mesh(Mesh_pointer_f, false);
   if (!mp) return;
+  // displacement and pressure traces do not depend on a deferred corrector
+  if ((mp->save_v || mp->save_a) && (mp->pend_corrector[0] || mp->pend_corrector[1])) flush_correctors(mp);
   if (mp->nrec_local == 0) return;
   const int cur = *seismo_currentf - 1;
   const int nlen = *nlength_seismogramf;
