@@ -54,12 +54,12 @@ def _peaks():
 
 
 def _traffic():
-    """DRAM bytes per element of the stiffness kernel from the committed ncu summary
-    (line 'dram_bytes_per_element: N'), or None."""
+    """DRAM bytes (read + write) of one stiffness launch of the full bench mesh, measured
+    with ncu (line 'dram_bytes_per_launch: N' of the committed summary), or None."""
     import re
-    path = os.path.join(ROOT, "profiles", "stiffness_kernel_att_6ctas_layered_32x32x16.md")
+    path = os.path.join(ROOT, "profiles", "stiffness_kernel_att_traffic_layered_128x128x64.md")
     try:
-        m = re.search(r"dram_bytes_per_element:\s*([0-9.]+)", open(path).read())
+        m = re.search(r"dram_bytes_per_launch:\s*([0-9.]+)", open(path).read())
         return float(m.group(1)) if m else None
     except Exception:
         return None
@@ -251,6 +251,7 @@ def main():
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--small", action="store_true", help="scaled-down mesh for quick checks")
     ap.add_argument("--graph", type=int, default=50, help="steps per captured CUDA graph")
+    ap.add_argument("--tile", type=int, default=0, help="process elements in tiles of tile^3 (0: mesh order)")
     ap.add_argument("--e2e-steps", type=int, default=50)
     ap.add_argument("--cpu-steps", type=int, default=40)
     ap.add_argument("--no-cpu", action="store_true")
@@ -297,7 +298,7 @@ def main():
     t_db = time.perf_counter() - t0
     nspec, nglob = db["nspec"], db["nglob"]
     t0 = time.perf_counter()
-    g = solver.GPUSolver(db, cfg, nlength=1)
+    g = solver.GPUSolver(db, cfg, nlength=1, tile=args.tile)
     t_up = time.perf_counter() - t0
     # ---------------- value: device-resident, graph-captured steps ----------------
     if args.variant >= 0:
@@ -374,10 +375,9 @@ def main():
                    "parallelism": "replicas" if world > 1 else "single GPU"},
         "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
                      "peak_kind": peak_kind,
-                     "traffic": (traffic_pe * nspec if traffic_pe else None),
-                     "traffic_note": ("ncu dram read+write bytes per element of a 16,384-element capture "
-                                      "(profiles/stiffness_kernel_att_6ctas_layered_32x32x16.md) x elements; "
-                                      "the field gathers of that capture stayed in L2"),
+                     "traffic": (traffic_pe if (traffic_pe and nspec == 1048576) else None),
+                     "traffic_note": ("ncu dram__bytes_read.sum + dram__bytes_write.sum of one stiffness launch "
+                                      "of this mesh (profiles/stiffness_kernel_att_traffic_layered_128x128x64.md)"),
                      "kernel": ("stiffness_pipe_kernel<att>" if args.variant == 1 else
                                 f"stiffness_{'split_' if args.variant >= 10 else ''}kernel<att, "
                                 f"{[4, 0, 5, 6, 7, 6, 7, 8, 6, 7, 3, 4][args.variant]} CTAs/SM"

@@ -24,11 +24,15 @@ N_SLS = 3
 
 class GPUSolver:
     def __init__(self, db: dict, cfg: dict, nlength: int | None = None, simulation_type: int = 1,
-                 save_forward: bool = False, record=("displ",), colors=None):
+                 save_forward: bool = False, record=("displ",), colors=None, tile: int = 0):
         """colors: optional colour per element (no two elements of a colour share a
         point, e.g. meshgen.block_colors); the phase lists are then ordered colour by
         colour and USE_MESH_COLORING_GPU is set, so assembly runs without atomics."""
         self.colors = None if colors is None else np.asarray(colors, np.int32)
+        # tile > 0: phase lists in tiles of tile^3 elements of a block mesh, so that
+        # elements sharing points are processed close in time (L2 reuse of the
+        # gathered wavefield)
+        self.tile = int(tile)
         self.L = abi.load()
         self.db, self.cfg = db, cfg
         self.nspec, self.nglob = int(db["nspec"]), int(db["nglob"])
@@ -97,6 +101,14 @@ class GPUSolver:
         solid = np.nonzero(self.isac == 0)[0] + 1
         outer = np.asarray(db.get("phase_outer", np.zeros(0, np.int32)), np.int32)
         inner = np.setdiff1d(solid, outer).astype(np.int32)
+        if self.tile > 0:
+            from .meshgen import Block
+            B = Block(self.cfg)
+            T = self.tile
+            for lst in (outer, inner):
+                ex, ey, ez = B.elem_xyz(lst - 1)
+                key = np.lexsort((ex % T, ey % T, ez % T, ex // T, ey // T, ez // T))
+                lst[:] = lst[key]
         ncol_out = ncol_in = 0
         elem_colors = None
         if self.colors is not None:
