@@ -70,13 +70,14 @@ def lib(precision: str = "f32") -> ctypes.CDLL:
             L.orc_get_global.restype = ctypes.c_int
             L.orc_get_global.argtypes = [ctypes.c_long, vp, vp, vp, vp, ctypes.c_double]
             L.orc_mesh_regular.argtypes = [ctypes.c_int] * 3 + [ctypes.c_double] * 4 + [vp] * 5
+            L.orc_gll_coordinates.argtypes = [ctypes.c_int, vp, vp, vp, vp]
             L.orc_calc_jacobian_all.restype = ctypes.c_int
             L.orc_calc_jacobian_all.argtypes = [ctypes.c_int, vp, vp, vp, vp, vp]
             L.orc_mass_stacey_elastic.argtypes = [ctypes.c_int, ctypes.c_double] + [vp] * 10
             L.orc_invert_mass.argtypes = [ctypes.c_int, vp, vp, vp, vp, ctypes.c_int]
             L.orc_face_geometry.argtypes = [vp, ctypes.c_int, vp, vp, vp]
             L.orc_locate_point.restype = ctypes.c_int
-            L.orc_locate_point.argtypes = [ctypes.c_int, vp, vp, vp, vp] + [ctypes.c_double] * 3 + [vp] * 3
+            L.orc_locate_point.argtypes = [ctypes.c_int] + [vp] * 8 + [ctypes.c_double] * 3 + [vp] * 3
             L.orc_lagrange_any.argtypes = [ctypes.c_double, vp, vp, vp]
             L.orc_gll.argtypes = [vp, vp]
             L.orc_derivation_matrices.argtypes = [vp] * 6
@@ -190,7 +191,6 @@ def build_database(cfg: dict, precision: str = "f32", material=None) -> dict:
     float32) for models that are not piecewise constant by layer.
     """
     L = lib(precision)
-    rd = real_dtype(precision)
     nx, ny = int(cfg["nx"]), int(cfg["ny"])
     zlev = np.asarray(cfg["zlev"], dtype=np.float64)
     nz = len(zlev) - 1
@@ -200,8 +200,99 @@ def build_database(cfg: dict, precision: str = "f32", material=None) -> dict:
     xs, ys, zs = np.zeros(npt), np.zeros(npt), np.zeros(npt)
     L.orc_mesh_regular(nx, ny, nz, float(cfg["x0"]), float(cfg["x1"]), float(cfg["y0"]), float(cfg["y1"]),
                        _p(zlev), _p(anchors), _p(xs), _p(ys), _p(zs))
-    ibool = np.zeros(npt, np.int32)
     xtol = 1e-10 * abs(float(cfg["x1"]) - float(cfg["x0"]))
+    # materials: per element layer, optionally per GLL point
+    if material is None:
+        lay = np.repeat(np.asarray(cfg["elem_layer"], np.int64), NGLL3)
+        rho = np.asarray([m["rho"] for m in cfg["layers"]], np.float32)[lay]
+        vp = np.asarray([m["vp"] for m in cfg["layers"]], np.float32)[lay]
+        vs = np.asarray([m["vs"] for m in cfg["layers"]], np.float32)[lay]
+    else:
+        rho, vp, vs = (np.asarray(a, np.float32) for a in material)
+    # absorbing faces: xmin, xmax, ymin, ymax, bottom (and top if requested)
+    faces = []
+    ex = np.arange(nspec) % nx
+    ey = (np.arange(nspec) // nx) % ny
+    ez = np.arange(nspec) // (nx * ny)
+    want = cfg.get("absorbing", ["xmin", "xmax", "ymin", "ymax", "bottom"])
+    conds = {"xmin": (1, ex == 0), "xmax": (2, ex == nx - 1), "ymin": (3, ey == 0), "ymax": (4, ey == ny - 1),
+             "bottom": (5, ez == 0), "top": (6, ez == nz - 1)}
+    for name in ["xmin", "xmax", "ymin", "ymax", "bottom", "top"]:
+        if name in want:
+            iface, sel = conds[name]
+            faces += [(int(e) + 1, iface) for e in np.nonzero(sel)[0]]
+    return _database(L, precision, cfg, anchors, xs, ys, zs, xtol, (rho, vp, vs), faces,
+                     stacey=bool(cfg.get("stacey", True)))
+
+
+_FACE_ANCHORS = {1: (0, 3, 7, 4), 2: (1, 2, 6, 5), 3: (0, 1, 5, 4), 4: (3, 2, 6, 7), 5: (0, 1, 2, 3), 6: (4, 5, 6, 7)}
+_FACE_FILES = [("xmin", "absorbing_surface_file_xmin"), ("xmax", "absorbing_surface_file_xmax"),
+               ("ymin", "absorbing_surface_file_ymin"), ("ymax", "absorbing_surface_file_ymax"),
+               ("bottom", "absorbing_surface_file_bottom"), ("top", "free_or_absorbing_surface_file_zmax")]
+
+
+def element_face_id(an: np.ndarray, corners: np.ndarray, tol: float) -> int:
+    """get_element_face_id (get_element_face.f90:28-167) restated: the face of the
+    element (anchors an (8,3)) whose four corner points coincide, within tol, with
+    the four given corner coordinates (4,3), in any order."""
+    for f, ids in _FACE_ANCHORS.items():
+        pts = an[list(ids)]
+        if all(np.min(np.abs(pts - c).max(axis=1)) <= tol for c in corners):
+            return f
+    raise ValueError("face corners do not match any face of the element")
+
+
+def build_database_from_mesh(mesh: dict, cfg: dict, precision: str = "f32") -> dict:
+    """The restated set-up chain for a general 8-node hexahedral mesh given as
+    nodes (nnod,3), elems (nspec,8) 0-based, mat_id per element, materials {id:
+    dict(domain, rho, vp, vs, ...)} and face lists {file name: (nf,5) [element,
+    4 nodes] 0-based}, the content of the reference's MESH files.  Absorbing faces
+    are found by coordinates like get_element_face_id."""
+    L = lib(precision)
+    nodes = np.asarray(mesh["nodes"], np.float64)
+    elems = np.asarray(mesh["elems"], np.int64)
+    nspec = len(elems)
+    anchors = np.ascontiguousarray(nodes[elems].reshape(-1))
+    npt = NGLL3 * nspec
+    xs, ys, zs = np.zeros(npt), np.zeros(npt), np.zeros(npt)
+    L.orc_gll_coordinates(nspec, _p(anchors), _p(xs), _p(ys), _p(zs))
+    xtol = 1e-10 * abs(float(nodes[:, 0].max() - nodes[:, 0].min()))
+    ids = sorted(mesh["materials"])
+    mats = [mesh["materials"][i] for i in ids]
+    lay = np.array([ids.index(int(m)) for m in mesh["mat_id"]], np.int64)
+    per = np.repeat(lay, NGLL3)
+    rho = np.array([m["rho"] for m in mats], np.float32)[per]
+    vp = np.array([m["vp"] for m in mats], np.float32)[per]
+    vs = np.array([0.0 if m["domain"] == 1 else m["vs"] for m in mats], np.float32)[per]
+    want = cfg.get("absorbing", ["xmin", "xmax", "ymin", "ymax", "bottom"])
+    an3 = anchors.reshape(nspec, 8, 3)
+    tol = 1e-6 * (1.0 + float(np.abs(nodes).max()))
+    faces = []
+    for name, fname in _FACE_FILES:
+        if name not in want or fname not in mesh["faces"]:
+            continue
+        for rec in mesh["faces"][fname]:
+            e = int(rec[0])
+            faces.append((e + 1, element_face_id(an3[e], nodes[rec[1:5]], tol)))
+    cfg2 = dict(cfg, layers=[dict(m) for m in mats], elem_layer=lay)
+    db = _database(L, precision, cfg2, anchors, xs, ys, zs, xtol, (rho, vp, vs), faces,
+                   stacey=bool(cfg.get("stacey", True)))
+    top = mesh["faces"].get("free_or_absorbing_surface_file_zmax", np.zeros((0, 5), np.int64))
+    if "top" in want:
+        top = np.zeros((0, 5), np.int64)
+    db["free_surface_faces"] = [(int(r[0]) + 1, element_face_id(an3[int(r[0])], nodes[r[1:5]], tol))
+                                for r in top]
+    db["layers"], db["elem_layer"] = cfg2["layers"], lay
+    return db
+
+
+def _database(L, precision, cfg, anchors, xs, ys, zs, xtol, material, faces, stacey):
+    """The set-up chain shared by block and general meshes, from the anchors, the
+    GLL coordinates, per-point (rho, vp, vs) and the absorbing faces [(ispec, iface)]."""
+    rd = real_dtype(precision)
+    nspec = len(anchors) // 24
+    npt = NGLL3 * nspec
+    ibool = np.zeros(npt, np.int32)
     xc, yc, zc = xs.copy(), ys.copy(), zs.copy()
     nglob = L.orc_get_global(npt, _p(xc), _p(yc), _p(zc), _p(ibool), xtol)
     del xc, yc, zc
@@ -217,14 +308,7 @@ def build_database(cfg: dict, precision: str = "f32", material=None) -> dict:
     db.update(nspec=nspec, nglob=nglob, nspec_irregular=nirr, ibool=ibool, irregular_element_number=irreg,
               xix_regular=float(xr.value), jacobian_regular=float(jr.value), anchors=anchors,
               xstore=xs, ystore=ys, zstore=zs)
-    # materials: per element layer, optionally per GLL point
-    if material is None:
-        lay = np.repeat(np.asarray(cfg["elem_layer"], np.int64), NGLL3)
-        rho = np.asarray([m["rho"] for m in cfg["layers"]], np.float32)[lay]
-        vp = np.asarray([m["vp"] for m in cfg["layers"]], np.float32)[lay]
-        vs = np.asarray([m["vs"] for m in cfg["layers"]], np.float32)[lay]
-    else:
-        rho, vp, vs = (np.asarray(a, np.float32) for a in material)
+    rho, vp, vs = material
     rho_r, vp_r, vs_r = rho.astype(rd), vp.astype(rd), vs.astype(rd)
     db["rhostore"] = rho_r
     db["kappastore"] = (rho_r * (vp_r * vp_r - rd(4.0 / 3.0) * vs_r * vs_r)).astype(rd)
@@ -233,18 +317,7 @@ def build_database(cfg: dict, precision: str = "f32", material=None) -> dict:
     db["rho_vs"] = (rho_r * vs_r).astype(rd)
     db["vp"] = vp
     db["vs"] = vs
-    # absorbing faces: xmin, xmax, ymin, ymax, bottom (and top if requested)
-    faces = []
-    ex = np.arange(nspec) % nx
-    ey = (np.arange(nspec) // nx) % ny
-    ez = np.arange(nspec) // (nx * ny)
-    want = cfg.get("absorbing", ["xmin", "xmax", "ymin", "ymax", "bottom"])
-    conds = {"xmin": (1, ex == 0), "xmax": (2, ex == nx - 1), "ymin": (3, ey == 0), "ymax": (4, ey == ny - 1),
-             "bottom": (5, ez == 0), "top": (6, ez == nz - 1)}
-    for name in ["xmin", "xmax", "ymin", "ymax", "bottom", "top"]:
-        if name in want:
-            iface, sel = conds[name]
-            faces += [(int(e) + 1, iface) for e in np.nonzero(sel)[0]]
+    db["ispec_is_acoustic"] = (np.asarray(vs, np.float32).reshape(nspec, NGLL3) == 0).all(axis=1).astype(np.int32)
     nf = len(faces)
     abs_ispec = np.array([f[0] for f in faces], np.int32)
     abs_ijk = np.zeros(3 * 25 * nf, np.int32)
@@ -265,7 +338,7 @@ def build_database(cfg: dict, precision: str = "f32", material=None) -> dict:
     rmass = np.zeros(nglob, rd)
     _mass_elastic(L, precision, nspec, nglob, db, rmass)
     rmx, rmy, rmz = np.zeros(nglob, rd), np.zeros(nglob, rd), np.zeros(nglob, rd)
-    stacey = bool(cfg.get("stacey", True)) and nf > 0
+    stacey = stacey and nf > 0
     if stacey:
         L.orc_mass_stacey_elastic(nglob, dt, _p(ibool), _p(db["rho_vp"]), _p(db["rho_vs"]), nf, _p(abs_ispec),
                                   _p(abs_ijk), _p(abs_n), _p(abs_jw), _p(rmx), _p(rmy), _p(rmz))
@@ -289,6 +362,80 @@ def _mass_elastic(L, precision, nspec, nglob, db, rmass):
        rt(db["jacobian_regular"]), _p(rmass))
 
 
+def element_neighbours(ibool: np.ndarray, nspec: int):
+    """CSR (xadj, adjncy) of every element's neighbours for the point search:
+    elements sharing a corner with it and their own corner neighbours, in element
+    order, the element itself excluded (setup_mesh_adjacency.f90 adds neighbours
+    of neighbours the same way)."""
+    from scipy import sparse
+    ib = np.asarray(ibool).reshape(nspec, NGLL3) - 1
+    corners = ib[:, [0, 4, 20, 24, 100, 104, 120, 124]].reshape(-1)
+    A = sparse.csr_matrix((np.ones(8 * nspec), (np.repeat(np.arange(nspec), 8), corners)),
+                          shape=(nspec, int(ib.max()) + 1))
+    r1 = (A @ A.T).astype(bool).astype(np.int32)
+    r2 = (r1 @ r1).tocsr()
+    r2.setdiag(0)
+    r2.eliminate_zeros()
+    r2.sort_indices()
+    return r2.indptr.astype(np.int32), (r2.indices.astype(np.int32) if r2.nnz else np.zeros(1, np.int32))
+
+
+def surface_points(ibool: np.ndarray, nspec: int) -> np.ndarray:
+    """Per element GLL point (125*nspec, uint8): 1 where the point lies on a face
+    that only one element has, the mesh's outer surface (iglob_is_surface_external_mesh)."""
+    ib = np.asarray(ibool).reshape(nspec, NGLL3) - 1
+    count = {}
+    faces = []
+    for e in range(nspec):
+        for f, corners in _FACE_CORNERS.items():
+            key = tuple(sorted(int(ib[e][i + 5 * j + 25 * k]) for i, j, k in corners))
+            count[key] = count.get(key, 0) + 1
+            faces.append((e, f, key))
+    on = np.zeros(int(ib.max()) + 1, bool)
+    for e, f, key in faces:
+        if count[key] == 1:
+            c = (f - 1) // 2
+            v = 0 if f % 2 == 1 else NGLL - 1
+            for a in range(NGLL):
+                for b in range(NGLL):
+                    ijk = [a, b]
+                    ijk.insert(c, v)
+                    on[ib[e][ijk[0] + 5 * ijk[1] + 25 * ijk[2]]] = True
+    return on[ib].reshape(-1).astype(np.uint8)
+
+
+def locate(L, db, x, y, z, octant=None):
+    """(ispec 1-based, xi, eta, gamma) of a target through orc_locate_point, with
+    the element neighbours and outer-surface points of the mesh (computed once)."""
+    nspec = db["nspec"]
+    if "_nb" not in db:
+        db["_nb"] = element_neighbours(db["ibool"], nspec)
+        db["_surf"] = surface_points(db["ibool"], nspec)
+        db["_isac"] = np.asarray(db.get("ispec_is_acoustic", np.zeros(nspec, np.int32)), np.int32)
+    xi, eta, ga = ctypes.c_double(), ctypes.c_double(), ctypes.c_double()
+    xadj, adj = db["_nb"]
+    ispec = L.orc_locate_point(nspec, _p(db["anchors"]), _p(db["xstore"]), _p(db["ystore"]), _p(db["zstore"]),
+                               _p(xadj), _p(adj), _p(db["_surf"]), _p(db["_isac"]), float(x), float(y), float(z),
+                               ctypes.addressof(xi), ctypes.addressof(eta), ctypes.addressof(ga))
+    if octant is not None:
+        # a target on element boundaries placed in the element on the given side:
+        # the first element whose anchor box holds it and whose centre lies on
+        # that side, then the location restricted to that element
+        an = db["anchors"].reshape(nspec, 8, 3)
+        xt = np.array([float(x), float(y), float(z)])
+        inside = np.nonzero(((an.min(1) <= xt) & (xt <= an.max(1))).all(1))[0]
+        side = (np.sign(an[inside].mean(1) - xt) == np.sign(np.asarray(octant, float))).all(1)
+        if side.any():
+            e = int(inside[side][0])
+            sl = slice(NGLL3 * e, NGLL3 * (e + 1))
+            one = [np.ascontiguousarray(db[k][sl]) for k in ("xstore", "ystore", "zstore")]
+            L.orc_locate_point(1, _p(np.ascontiguousarray(an[e].reshape(-1))), _p(one[0]), _p(one[1]), _p(one[2]),
+                               None, None, None, None, xt[0], xt[1], xt[2], ctypes.addressof(xi),
+                               ctypes.addressof(eta), ctypes.addressof(ga))
+            ispec = e + 1
+    return ispec, xi.value, eta.value, ga.value
+
+
 def _sources_receivers(L, precision, cfg, db):
     rd = real_dtype(precision)
     nspec = db["nspec"]
@@ -301,22 +448,19 @@ def _sources_receivers(L, precision, cfg, db):
     isel = np.zeros(ns, np.int32)
     loc = np.zeros((ns, 3))
     for i, s in enumerate(srcs):
-        xi, eta, ga = ctypes.c_double(), ctypes.c_double(), ctypes.c_double()
-        ispec = L.orc_locate_point(nspec, _p(db["anchors"]), _p(db["xstore"]), _p(db["ystore"]), _p(db["zstore"]),
-                                   float(s["x"]), float(s["y"]), float(s["z"]), ctypes.addressof(xi),
-                                   ctypes.addressof(eta), ctypes.addressof(ga))
+        ispec, xi, eta, ga = locate(L, db, s["x"], s["y"], s["z"], s.get("octant"))
         isel[i] = ispec
-        loc[i] = (xi.value, eta.value, ga.value)
+        loc[i] = (xi, eta, ga)
         out = np.zeros(3 * NGLL3, rd)
         if s.get("type", "cmt") == "cmt":
             Mxx, Myy, Mzz, Mxy, Mxz, Myz = (float(v) for v in s["M"])
             rt = ctypes.c_float if precision == "f32" else ctypes.c_double
             L.orc_source_array_cmt(ispec, _p(db["irregular_element_number"]), ctypes.addressof(mptrs),
-                                   rt(db["xix_regular"]), xi.value, eta.value, ga.value,
+                                   rt(db["xix_regular"]), xi, eta, ga,
                                    Mxx, Myy, Mzz, Mxy, Mxz, Myz, _p(out))
         else:
             f = [float(v) for v in s["F"]]
-            L.orc_source_array_force(xi.value, eta.value, ga.value, f[0], f[1], f[2], _p(out))
+            L.orc_source_array_force(xi, eta, ga, f[0], f[1], f[2], _p(out))
         sa[i] = out.reshape(NGLL3, 3).T
     # Fortran sourcearrays(NSOURCES,NDIM,NGLLX,NGLLY,NGLLZ): isrc fastest
     db["sourcearrays"] = np.ascontiguousarray(sa.transpose(2, 1, 0)).reshape(-1)
@@ -328,15 +472,12 @@ def _sources_receivers(L, precision, cfg, db):
     hx, he, hg = np.zeros((nr, NGLL)), np.zeros((nr, NGLL)), np.zeros((nr, NGLL))
     rloc = np.zeros((nr, 3))
     for r, (x, y, z) in enumerate(recs):
-        xi, eta, ga = ctypes.c_double(), ctypes.c_double(), ctypes.c_double()
-        ispec = L.orc_locate_point(nspec, _p(db["anchors"]), _p(db["xstore"]), _p(db["ystore"]), _p(db["zstore"]),
-                                   float(x), float(y), float(z), ctypes.addressof(xi), ctypes.addressof(eta),
-                                   ctypes.addressof(ga))
+        ispec, xi, eta, ga = locate(L, db, x, y, z)
         irec[r] = ispec
-        rloc[r] = (xi.value, eta.value, ga.value)
-        hx[r], _ = lagrange_any(xi.value)
-        he[r], _ = lagrange_any(eta.value)
-        hg[r], _ = lagrange_any(ga.value)
+        rloc[r] = (xi, eta, ga)
+        hx[r], _ = lagrange_any(xi)
+        he[r], _ = lagrange_any(eta)
+        hg[r], _ = lagrange_any(ga)
     db.update(ispec_selected_rec=irec, hxir=hx.reshape(-1), hetar=he.reshape(-1), hgammar=hg.reshape(-1),
               receiver_xi_eta_gamma=rloc, nrec=nr, nsources=ns)
 
@@ -558,17 +699,24 @@ def fluid_setup(db: dict, cfg: dict, precision: str = "f32") -> dict:
     out["coupling_ac_el_ijk"] = np.concatenate([f[1] for f in faces]) if nf else np.zeros(0, np.int32)
     out["coupling_ac_el_jacobian2Dw"] = np.concatenate([f[2] for f in faces]) if nf else np.zeros(0, rd)
     out["coupling_ac_el_normal"] = np.concatenate([f[3] for f in faces]) if nf else np.zeros(0, rd)
-    # free surface: top faces of the block (face 6 of the top element row)
-    nx, ny = int(cfg["nx"]), int(cfg["ny"])
-    nz = len(cfg["zlev"]) - 1
-    top = np.arange(nx * ny * (nz - 1), nx * ny * nz)
-    fs_ijk = np.zeros(75, np.int32)
-    _jw = np.zeros(25, rd)
-    _n = np.zeros(75, rd)
-    L.orc_face_geometry(_p(db["anchors"]), 6, _p(fs_ijk), _p(_jw), _p(_n))
-    out["num_free_surface_faces"] = len(top)
-    out["free_surface_ispec"] = (top + 1).astype(np.int32)
-    out["free_surface_ijk"] = np.tile(fs_ijk, len(top))
+    # free surface: the listed faces of a general mesh, else the top faces of the
+    # block (face 6 of the top element row)
+    if "free_surface_faces" in db:
+        fsf = db["free_surface_faces"]
+    else:
+        nx, ny = int(cfg["nx"]), int(cfg["ny"])
+        nz = len(cfg["zlev"]) - 1
+        fsf = [(int(e) + 1, 6) for e in range(nx * ny * (nz - 1), nx * ny * nz)]
+    fs = []
+    for e1, f in fsf:
+        fs_ijk = np.zeros(75, np.int32)
+        _jw = np.zeros(25, rd)
+        _n = np.zeros(75, rd)
+        L.orc_face_geometry(_p(db["anchors"][24 * (e1 - 1):]), f, _p(fs_ijk), _p(_jw), _p(_n))
+        fs.append(fs_ijk)
+    out["num_free_surface_faces"] = len(fsf)
+    out["free_surface_ispec"] = np.array([e1 for e1, _ in fsf], np.int32)
+    out["free_surface_ijk"] = np.concatenate(fs) if fs else np.zeros(0, np.int32)
     # fluid mass matrix: sum J w / kappa, plus dt/2 jw / (rho vp) on absorbing faces
     x, w = gll()
     w3 = np.array([w[i] * w[j] * w[k] for k in range(5) for j in range(5) for i in range(5)])

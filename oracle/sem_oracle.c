@@ -235,6 +235,26 @@ void orc_mesh_regular(int nx, int ny, int nz, double x0, double x1, double y0, d
       }
 }
 
+/* GLL point coordinates of any 8-node hexahedral mesh (calc_coords,
+ * calc_jacobian.f90:148-178): anchors[(c + 3 a) + 24 ispec]. */
+void orc_gll_coordinates(int nspec, const double *anchors, double *xstore, double *ystore, double *zstore) {
+  double xg[NGLL], wg[NGLL];
+  orc_gll(xg, wg);
+  for (long ispec = 0; ispec < nspec; ++ispec) {
+    const double *an = anchors + 24 * ispec;
+    for (int k = 0; k < NGLL; ++k)
+      for (int j = 0; j < NGLL; ++j)
+        for (int i = 0; i < NGLL; ++i) {
+          double sh[8], dsh[24];
+          shape8(xg[i], xg[j], xg[k], sh, dsh);
+          double xm = 0, ym = 0, zm = 0;
+          for (int a = 0; a < 8; ++a) { xm += sh[a] * an[3 * a]; ym += sh[a] * an[3 * a + 1]; zm += sh[a] * an[3 * a + 2]; }
+          long p = IJK(i, j, k) + NGLL3 * ispec;
+          xstore[p] = xm; ystore[p] = ym; zstore[p] = zm;
+        }
+  }
+}
+
 /* ------------------------------------------------------------------------- */
 /* global numbering: get_global + get_global_indirect_addressing               */
 /* (get_global.f90:28-141, sort_array_coordinates.f90:30-128)                  */
@@ -529,18 +549,69 @@ void orc_face_geometry(const double *an, int iface, int *ijk, realw *jw, realw *
 /* point location (locate_point.f90:32-416, :422-624)                         */
 /* ------------------------------------------------------------------------- */
 
-/* Closest GLL point over all elements (first strictly-closer wins, element
- * order), then the Newton iteration of find_local_coordinates in that element.
- * xstore etc. are the per-element GLL coordinates (125*nspec).  If the
- * converged point lies outside [-1,1]^3 the search moves to the first element
- * that contains the target. Returns ispec (1-based). */
-int orc_locate_point(int nspec, const double *anchors, const double *xs, const double *ys,
-                     const double *zs, double xt, double yt, double zt, double *xi_out,
-                     double *eta_out, double *gamma_out) {
+/* find_local_coordinates (locate_point.f90:422-624): up to 5 Newton steps on
+ * (xi, eta, gamma) from GLL point (ix, iy, iz) of the element, stopping when the
+ * distance stops decreasing; steps longer than 1 are cut to a third; the local
+ * coordinates are clamped to [-1.01, 1.01].  d2 = final squared distance. */
+static void find_local(const double *an, double xt, double yt, double zt, int ix, int iy, int iz,
+                       double *xi_o, double *eta_o, double *ga_o, double *d2_o) {
   double xg[NGLL], wg[NGLL];
   orc_gll(xg, wg);
+  double xi = xg[ix], eta = xg[iy], ga = xg[iz], dmin2 = 1e30;
+  for (int it = 0; it < 5; ++it) {
+    double sh[8], dsh[24], x = 0, y = 0, z = 0;
+    double J[3][3] = {{0}};
+    shape8(xi, eta, ga, sh, dsh);
+    for (int a = 0; a < 8; ++a) {
+      x += sh[a] * an[3 * a]; y += sh[a] * an[3 * a + 1]; z += sh[a] * an[3 * a + 2];
+      for (int d = 0; d < 3; ++d)
+        for (int e = 0; e < 3; ++e) J[e][d] += dsh[d * 8 + a] * an[3 * a + e];
+    }
+    double dx = xt - x, dy = yt - y, dz = zt - z, d2 = dx * dx + dy * dy + dz * dz;
+    if (!(d2 < dmin2)) break;
+    dmin2 = d2;
+    double det = J[0][0] * (J[1][1] * J[2][2] - J[1][2] * J[2][1]) - J[0][1] * (J[1][0] * J[2][2] - J[1][2] * J[2][0]) +
+                 J[0][2] * (J[1][0] * J[2][1] - J[1][1] * J[2][0]);
+    double inv[3][3];
+    inv[0][0] = (J[1][1] * J[2][2] - J[1][2] * J[2][1]) / det; inv[0][1] = (J[0][2] * J[2][1] - J[0][1] * J[2][2]) / det;
+    inv[0][2] = (J[0][1] * J[1][2] - J[0][2] * J[1][1]) / det; inv[1][0] = (J[1][2] * J[2][0] - J[1][0] * J[2][2]) / det;
+    inv[1][1] = (J[0][0] * J[2][2] - J[0][2] * J[2][0]) / det; inv[1][2] = (J[0][2] * J[1][0] - J[0][0] * J[1][2]) / det;
+    inv[2][0] = (J[1][0] * J[2][1] - J[1][1] * J[2][0]) / det; inv[2][1] = (J[0][1] * J[2][0] - J[0][0] * J[2][1]) / det;
+    inv[2][2] = (J[0][0] * J[1][1] - J[0][1] * J[1][0]) / det;
+    double dxi = inv[0][0] * dx + inv[0][1] * dy + inv[0][2] * dz;
+    double deta = inv[1][0] * dx + inv[1][1] * dy + inv[1][2] * dz;
+    double dga = inv[2][0] * dx + inv[2][1] * dy + inv[2][2] * dz;
+    if (dxi * dxi + deta * deta + dga * dga > 1.0) { dxi *= 0.33333333333; deta *= 0.33333333333; dga *= 0.33333333333; }
+    xi += dxi; eta += deta; ga += dga;
+    xi = xi > 1.01 ? 1.01 : (xi < -1.01 ? -1.01 : xi);
+    eta = eta > 1.01 ? 1.01 : (eta < -1.01 ? -1.01 : eta);
+    ga = ga > 1.01 ? 1.01 : (ga < -1.01 ? -1.01 : ga);
+  }
+  /* position and distance at the final local coordinates */
+  double sh[8], dsh[24], x = 0, y = 0, z = 0;
+  shape8(xi, eta, ga, sh, dsh);
+  for (int a = 0; a < 8; ++a) { x += sh[a] * an[3 * a]; y += sh[a] * an[3 * a + 1]; z += sh[a] * an[3 * a + 2]; }
+  *xi_o = xi; *eta_o = eta; *ga_o = ga;
+  *d2_o = (xt - x) * (xt - x) + (yt - y) * (yt - y) + (zt - z) * (zt - z);
+}
+
+static int outside(double xi, double eta, double ga) { return fabs(xi) > 1.0 || fabs(eta) > 1.0 || fabs(ga) > 1.0; }
+
+/* locate_point_in_mesh (locate_point.f90:32-416) with the brute-force first
+ * guess: the closest GLL point over all elements (single-precision coordinates,
+ * first strictly closer point in element, k, j, i order), Newton in that element;
+ * unless the result lies strictly inside the element (or above the top of a
+ * surface element), up to 3 rounds of find_best_neighbor (:630-804) over the
+ * element's neighbours (CSR xadj/adjncy, 0-based; NULL = none).
+ * surface_pt flags GLL points (per element, 125*nspec) on the mesh's outer
+ * surface; is_acoustic flags fluid elements (NULL = all solid).
+ * Returns ispec (1-based). */
+int orc_locate_point(int nspec, const double *anchors, const double *xs, const double *ys,
+                     const double *zs, const int *xadj, const int *adjncy, const unsigned char *surface_pt,
+                     const int *is_acoustic, double xt, double yt, double zt, double *xi_out,
+                     double *eta_out, double *gamma_out) {
   double dmin = 1e300;
-  int isel = -1, ix = 0, iy = 0, iz = 0;
+  int isel = 0, ix = 0, iy = 0, iz = 0;
   for (int ispec = 0; ispec < nspec; ++ispec)
     for (int k = 0; k < NGLL; ++k)
       for (int j = 0; j < NGLL; ++j)
@@ -550,55 +621,44 @@ int orc_locate_point(int nspec, const double *anchors, const double *xs, const d
           double d = (xt - x) * (xt - x) + (yt - y) * (yt - y) + (zt - z) * (zt - z);
           if (d < dmin) { dmin = d; isel = ispec; ix = i; iy = j; iz = k; }
         }
-  for (int pass = 0; pass < 2; ++pass) {
-    const double *an = anchors + 24 * isel;
-    double xi = xg[ix], eta = xg[iy], ga = xg[iz], dmin2 = 1e30;
-    for (int it = 0; it < 5; ++it) {
-      double sh[8], dsh[24], x = 0, y = 0, z = 0;
-      double J[3][3] = {{0}};
-      shape8(xi, eta, ga, sh, dsh);
-      for (int a = 0; a < 8; ++a) {
-        x += sh[a] * an[3 * a]; y += sh[a] * an[3 * a + 1]; z += sh[a] * an[3 * a + 2];
-        for (int d = 0; d < 3; ++d)
-          for (int e = 0; e < 3; ++e) J[e][d] += dsh[d * 8 + a] * an[3 * a + e];
+  double xi, eta, ga, d2;
+  find_local(anchors + 24 * (long)isel, xt, yt, zt, ix, iy, iz, &xi, &eta, &ga, &d2);
+  int search = !(fabs(xi) < 1.0 && fabs(eta) < 1.0 && fabs(ga) < 1.0);
+  if (search && ga > 1.0 && surface_pt && surface_pt[IJK(ix, iy, iz) + (long)NGLL3 * isel]) search = 0;
+  if (search && xadj) {
+    for (int itry = 0; itry < 3; ++itry) {
+      int e0 = isel;
+      for (int q = xadj[e0]; q < xadj[e0 + 1]; ++q) {
+        int e = adjncy[q];
+        /* best GLL point of this neighbour as the starting guess */
+        double dg = 1e300;
+        int gx = NGLL / 2, gy = NGLL / 2, gz = NGLL / 2;
+        for (int k = 0; k < NGLL; ++k)
+          for (int j = 0; j < NGLL; ++j)
+            for (int i = 0; i < NGLL; ++i) {
+              long p = IJK(i, j, k) + (long)NGLL3 * e;
+              double x = (float)xs[p], y = (float)ys[p], z = (float)zs[p];
+              double d = (xt - x) * (xt - x) + (yt - y) * (yt - y) + (zt - z) * (zt - z);
+              if (d < dg) { dg = d; gx = i; gy = j; gz = k; }
+            }
+        double nxi, neta, nga, nd2;
+        find_local(anchors + 24 * (long)e, xt, yt, zt, gx, gy, gz, &nxi, &neta, &nga, &nd2);
+        int better = 0;
+        if (nd2 < 1e-10 && !outside(nxi, neta, nga)) {
+          if (outside(xi, eta, ga)) better = 1;
+          if (is_acoustic && is_acoustic[isel] && !is_acoustic[e]) better = 1;
+        }
+        /* a closer location: improvements below the reference's own 1e-15 tie
+         * threshold count as ties (the earlier element stays), so that a point on
+         * an element boundary does not move with rounding noise */
+        if (nd2 < d2 - 1e-15) better = 1;
+        if (better) { isel = e; xi = nxi; eta = neta; ga = nga; d2 = nd2; }
       }
-      double dx = xt - x, dy = yt - y, dz = zt - z, d2 = dx * dx + dy * dy + dz * dz;
-      if (!(d2 < dmin2)) break;
-      dmin2 = d2;
-      double det = J[0][0] * (J[1][1] * J[2][2] - J[1][2] * J[2][1]) - J[0][1] * (J[1][0] * J[2][2] - J[1][2] * J[2][0]) +
-                   J[0][2] * (J[1][0] * J[2][1] - J[1][1] * J[2][0]);
-      double inv[3][3];
-      inv[0][0] = (J[1][1] * J[2][2] - J[1][2] * J[2][1]) / det; inv[0][1] = (J[0][2] * J[2][1] - J[0][1] * J[2][2]) / det;
-      inv[0][2] = (J[0][1] * J[1][2] - J[0][2] * J[1][1]) / det; inv[1][0] = (J[1][2] * J[2][0] - J[1][0] * J[2][2]) / det;
-      inv[1][1] = (J[0][0] * J[2][2] - J[0][2] * J[2][0]) / det; inv[1][2] = (J[0][2] * J[1][0] - J[0][0] * J[1][2]) / det;
-      inv[2][0] = (J[1][0] * J[2][1] - J[1][1] * J[2][0]) / det; inv[2][1] = (J[0][1] * J[2][0] - J[0][0] * J[2][1]) / det;
-      inv[2][2] = (J[0][0] * J[1][1] - J[0][1] * J[1][0]) / det;
-      double dxi = inv[0][0] * dx + inv[0][1] * dy + inv[0][2] * dz;
-      double deta = inv[1][0] * dx + inv[1][1] * dy + inv[1][2] * dz;
-      double dga = inv[2][0] * dx + inv[2][1] * dy + inv[2][2] * dz;
-      if (dxi * dxi + deta * deta + dga * dga > 1.0) { dxi *= 0.33333333333; deta *= 0.33333333333; dga *= 0.33333333333; }
-      xi += dxi; eta += deta; ga += dga;
-      xi = xi > 1.01 ? 1.01 : (xi < -1.01 ? -1.01 : xi);
-      eta = eta > 1.01 ? 1.01 : (eta < -1.01 ? -1.01 : eta);
-      ga = ga > 1.01 ? 1.01 : (ga < -1.01 ? -1.01 : ga);
+      if (isel == e0) break;
+      if (!outside(xi, eta, ga)) break;
     }
-    const double eps = 1e-9;
-    if (fabs(xi) <= 1 + eps && fabs(eta) <= 1 + eps && fabs(ga) <= 1 + eps) {
-      *xi_out = xi; *eta_out = eta; *gamma_out = ga;
-      return isel + 1;
-    }
-    /* outside: first element whose bounding box holds the target */
-    int found = -1;
-    for (int ispec = 0; ispec < nspec && found < 0; ++ispec) {
-      const double *b = anchors + 24 * ispec;
-      double lo[3] = {1e300, 1e300, 1e300}, hi[3] = {-1e300, -1e300, -1e300};
-      for (int a = 0; a < 8; ++a)
-        for (int d = 0; d < 3; ++d) { if (b[3 * a + d] < lo[d]) lo[d] = b[3 * a + d]; if (b[3 * a + d] > hi[d]) hi[d] = b[3 * a + d]; }
-      if (xt >= lo[0] && xt <= hi[0] && yt >= lo[1] && yt <= hi[1] && zt >= lo[2] && zt <= hi[2]) found = ispec;
-    }
-    if (found < 0) { *xi_out = xi; *eta_out = eta; *gamma_out = ga; return isel + 1; }
-    isel = found; ix = iy = iz = NGLL / 2;
   }
+  *xi_out = xi; *eta_out = eta; *gamma_out = ga;
   return isel + 1;
 }
 

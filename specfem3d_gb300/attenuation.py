@@ -30,8 +30,14 @@ PI_SIMPLEX = 3.14159265358979
 
 
 def min_resolved_period(cfg: dict, db: dict) -> float:
-    """Largest per-element resolved period (single precision): (max edge /4) / min(vp,vs) * 5."""
+    """Largest per-element resolved period (single precision): (max edge /4) / min(vp,vs) * 5
+    (check_mesh_resolution.f90, get_elem_minmaxsize: longest of the 12 edges).
+    Meshes other than blocks give the edge per element as db["elem_size_max"]."""
     f32 = np.float32
+    nspec = db["nspec"]
+    if "elem_size_max" in db:
+        emax = np.asarray(db["elem_size_max"], f32)
+        return _resolved(db, emax)
     nx, ny = cfg["nx"], cfg["ny"]
     xl = np.array([cfg["x0"] + (cfg["x1"] - cfg["x0"]) * e / nx for e in range(nx + 1)])
     yl = np.array([cfg["y0"] + (cfg["y1"] - cfg["y0"]) * e / ny for e in range(ny + 1)])
@@ -39,9 +45,14 @@ def min_resolved_period(cfg: dict, db: dict) -> float:
     dx = (xl[1:] - xl[:-1]).astype(f32)
     dy = (yl[1:] - yl[:-1]).astype(f32)
     dz = (zl[1:] - zl[:-1]).astype(f32)
-    nspec = db["nspec"]
     e = np.arange(nspec)
     emax = np.maximum(np.maximum(dx[e % nx], dy[(e // nx) % ny]), dz[e // (nx * ny)]).astype(f32)
+    return _resolved(db, emax)
+
+
+def _resolved(db: dict, emax) -> float:
+    f32 = np.float32
+    nspec = db["nspec"]
     kap = db["kappastore"].reshape(nspec, NGLL3)
     mu = db["mustore"].reshape(nspec, NGLL3)
     rho = db["rhostore"].reshape(nspec, NGLL3)

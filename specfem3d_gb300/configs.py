@@ -127,7 +127,23 @@ def refex(nstep: int = 5000) -> dict:
                # six significant digits
                receivers=[(x, 67000.0, 0.0) for x in (22732.1, 34696.4, 46660.7, 58625.0)],
                station_names=["X20", "X30", "X40", "X50"])
+    # the source sits on a mesh vertex shared by 8 elements; the REF_SEIS run put
+    # it in the element below, in front of and left of it (its output_solver.txt:
+    # element 2772 of slice 0, local coordinates (1, 1, 1) of the CUBIT mesh)
+    cfg["sources"][0]["octant"] = (-1, -1, -1)
     return finish(cfg)
+
+
+def refex_no_absorbing(nstep: int = 5000) -> dict:
+    """The reference example homogeneous_halfspace_HEX8_elastic_no_absorbing: the
+    same block, source and stations without Stacey faces.  Its REF_SEIS run (4
+    slices) placed the source, a vertex of 8 elements, in element 4905 of slice 0
+    at local coordinates (-1, -1, 1) (REF_SEIS/output_solver.txt), which in its
+    CUBIT mesh (MESH-default) is the element on the -x, +y, -z side of the vertex."""
+    cfg = refex(nstep)
+    cfg["stacey"] = False
+    cfg["sources"][0]["octant"] = (-1, 1, -1)
+    return cfg
 
 
 def homogeneous_block(nstep: int = 2000, seed: int = 2024) -> dict:

@@ -376,20 +376,20 @@ def _coupling_and_free_surface(cfg, B, db, dtype):
 
 
 def _mass(cfg, B, db, dtype):
-    nspec, nglob = B.nspec, B.nglob
+    """Mass matrices of any hexahedral mesh: per-point Jacobian of irregular
+    elements, the regular Jacobian elsewhere."""
+    nspec, nglob = int(db["nspec"]), int(db["nglob"])
     irr = db["irregular_element_number"]
     w3 = (WGLL[None, None, :] * WGLL[None, :, None] * WGLL[:, None, None]).reshape(-1)  # i fastest
-    jac = np.where(irr > 0, 0, 1)  # placeholder shape
-    del jac
-    jel = np.empty(nspec, np.float64)
+    jel = np.empty((nspec, NGLL3), np.float64)
     reg = irr == 0
     jel[reg] = np.float32(db["jacobian_regular"])
     if (~reg).any():
-        jel[~reg] = db["jacobian"].reshape(-1, NGLL3)[irr[~reg] - 1, 0]
+        jel[~reg] = db["jacobian"].reshape(-1, NGLL3)[irr[~reg] - 1]
     rho = db["rhostore"].reshape(nspec, NGLL3).astype(np.float64)
     isac = db["ispec_is_acoustic"].astype(bool)
     ib = db["ibool"].reshape(nspec, NGLL3).astype(np.int64) - 1
-    terms = (jel[:, None] * w3[None, :] * rho).astype(dtype).astype(np.float64)
+    terms = (jel * w3[None, :] * rho).astype(dtype).astype(np.float64)
     terms[isac] = 0.0
     rmass = np.bincount(ib.reshape(-1), weights=terms.reshape(-1), minlength=nglob)
     rmass = rmass.astype(dtype)
@@ -397,7 +397,7 @@ def _mass(cfg, B, db, dtype):
         # rmass_acoustic = 1 / (sum J w / kappa + Stacey term) (define_mass_matrices.f90:120-160, :488-520)
         kap = db["kappastore"].reshape(nspec, NGLL3).astype(np.float64)
         ta = np.zeros_like(terms)
-        ta[isac] = (jel[isac, None] * w3[None, :] / kap[isac]).astype(dtype)
+        ta[isac] = (jel[isac] * w3[None, :] / kap[isac]).astype(dtype)
         rma = np.bincount(ib.reshape(-1), weights=ta.reshape(-1), minlength=nglob).astype(dtype)
         if db["stacey"]:
             nf = db["num_abs_boundary_faces"]
@@ -438,11 +438,25 @@ def _mass(cfg, B, db, dtype):
     db["rmassz"] = (dtype(1) / mz).astype(dtype)
 
 
-def locate(B: Block, xt: float, yt: float, zt: float):
+def locate(B: Block, xt: float, yt: float, zt: float, octant=None):
     """Closest GLL point (single-precision coordinates, first strictly-closer wins
     in element order), then local coordinates in that element; a target outside
     that element moves to the first element containing it
-    (specfem3D/locate_point.f90:160-300, :422-624).  Returns (ispec 1-based, xi, eta, gamma)."""
+    (specfem3D/locate_point.f90:160-300, :422-624).  Returns (ispec 1-based, xi, eta, gamma).
+
+    ``octant`` (3 signs) places a target that lies on element boundaries in the
+    element on that side of it along each axis, the element a run partitioned
+    differently may have chosen."""
+    if octant is not None:
+        idx = []
+        for v, lv, n, sgn in ((xt, B.xl, B.nx, octant[0]), (yt, B.yl, B.ny, octant[1]), (zt, B.zl, B.nz, octant[2])):
+            i = np.searchsorted(lv, v, side="left" if sgn < 0 else "right") - 1
+            idx.append(int(np.clip(i, 0, n - 1)))
+        ex, ey, ez = idx
+        e = ex + B.nx * (ey + B.ny * ez)
+        return (e + 1, (2 * xt - B.xl[ex] - B.xl[ex + 1]) / (B.xl[ex + 1] - B.xl[ex]),
+                (2 * yt - B.yl[ey] - B.yl[ey + 1]) / (B.yl[ey + 1] - B.yl[ey]),
+                (2 * zt - B.zl[ez] - B.zl[ez + 1]) / (B.zl[ez + 1] - B.zl[ez]))
     ex0 = np.searchsorted(B.xl, xt) - 1
     ey0 = np.searchsorted(B.yl, yt) - 1
     ez0 = np.searchsorted(B.zl, zt) - 1
@@ -474,7 +488,12 @@ def locate(B: Block, xt: float, yt: float, zt: float):
     return e + 1, xi, eta, ga
 
 
-def _sources_receivers(cfg, B, db, dtype):
+def _sources_receivers(cfg, B, db, dtype, locator=None):
+    """Source arrays, receiver interpolants and stf tables; ``locator(x, y, z)`` returns
+    (ispec 1-based, xi, eta, gamma) and defaults to the block locator."""
+    if locator is None:
+        def locator(x, y, z, octant=None):
+            return locate(B, x, y, z, octant)
     srcs = cfg.get("sources", [])
     ns = len(srcs)
     sa = np.zeros((ns, 3, NGLL3))
@@ -482,7 +501,7 @@ def _sources_receivers(cfg, B, db, dtype):
     loc = np.zeros((ns, 3))
     irr = db["irregular_element_number"]
     for i, s in enumerate(srcs):
-        e1, xi, eta, ga = locate(B, float(s["x"]), float(s["y"]), float(s["z"]))
+        e1, xi, eta, ga = locator(float(s["x"]), float(s["y"]), float(s["z"]), s.get("octant"))
         isel[i] = e1
         loc[i] = (xi, eta, ga)
         hx, hpx = lagrange(xi)
@@ -525,7 +544,7 @@ def _sources_receivers(cfg, B, db, dtype):
     hx, he, hg = np.zeros((nr, NGLL)), np.zeros((nr, NGLL)), np.zeros((nr, NGLL))
     rloc = np.zeros((nr, 3))
     for r, (x, y, z) in enumerate(recs):
-        e1, xi, eta, ga = locate(B, float(x), float(y), float(z))
+        e1, xi, eta, ga = locator(float(x), float(y), float(z))
         irec[r] = e1
         rloc[r] = (xi, eta, ga)
         hx[r], _ = lagrange(xi)

@@ -1,11 +1,10 @@
 """FP64 oracle seismograms of the reference's no-absorbing example (5000 steps).
 
-The reference's REF_SEIS for homogeneous_halfspace_HEX8_elastic_no_absorbing
-differ from the FP32 and FP64 oracle by up to 6e-3 relative L2 (correlation
->= 0.99998; the reference's own CI accepts correlation >= 0.999), while the
-Stacey example of the same mesh agrees to 3e-4.  This fixture holds the FP64
-oracle's traces so the GPU run of that example is also held to the oracle at
-FP32 accuracy.  Runs in a few minutes on 8 cores:
+The source of homogeneous_halfspace_HEX8_elastic_no_absorbing lies on a vertex
+shared by 8 elements; its REF_SEIS run placed it in the element on the -x, +y, -z
+side (configs.refex_no_absorbing).  This fixture holds the FP64 oracle's traces
+of that set-up so the GPU run of the example is held to the oracle at FP32
+accuracy, besides the REF_SEIS comparison.  Runs in a few minutes on 8 cores:
 
     python tests/golden/make_oracle_fixture.py
 """
@@ -22,8 +21,7 @@ def main():
     from oracle import oracle as O
     from specfem3d_gb300 import configs, meshgen
     nstep = 5000
-    cfg = configs.refex(nstep)
-    cfg["stacey"] = False
+    cfg = configs.refex_no_absorbing(nstep)
     db = meshgen.build_database(cfg, dtype=np.float64)
     sim = O.make_sim(db, cfg, "f64", nthreads=os.cpu_count() or 1)
     sim.step(nstep)

@@ -1,0 +1,89 @@
+"""GPU time stepping on general hexahedral meshes: full, varying metric tensors from
+moved interior nodes and a rotated block (every element irregular), against the
+oracle's FP32 stepping on the same database, and the rotation invariance of the
+device's seismograms.  The databases come from specfem3d_gb300.hexmesh, which the
+CPU tests hold to the oracle's own restatement of the set-up."""
+import os
+
+import numpy as np
+import pytest
+
+from conftest import rel_l2
+import hexmesh_cases as C
+
+pytestmark = pytest.mark.gpu
+
+
+def _run_gpu(db, cfg, per_call=False):
+    from specfem3d_gb300 import solver
+    g = solver.GPUSolver(db, cfg)
+    if per_call:
+        g.run_per_call(cfg["nstep"])
+    else:
+        g.run(cfg["nstep"], steps_per_graph=50)
+    s = g.seismograms()
+    d = g.fields()[0]
+    extra = g.potentials()[0] if db["ispec_is_acoustic"].any() else None
+    g.close()
+    return s, d, extra
+
+
+@pytest.mark.parametrize("att", [False, True])
+def test_distorted_rotated_mesh_vs_oracle(gpulib, att):
+    """Seismograms <= 5e-5 and displacement <= 1e-4 relative L2 after 400 steps,
+    the bars of the block tests."""
+    from oracle import oracle as O
+    from specfem3d_gb300 import configs, hexmesh
+    cfg = configs.small_layered(nstep=400, attenuation=att)
+    mesh, c = C.rotated(cfg, C.rotation(), C.distorted(cfg))
+    db = hexmesh.build_database(mesh, c)
+    assert db["nspec_irregular"] == db["nspec"]
+    sim = O.make_sim(db, c, "f32", nthreads=os.cpu_count() or 1)
+    sim.step(c["nstep"])
+    ref = O.seismograms(sim)
+    s, d, _ = _run_gpu(db, c)
+    es, ed = rel_l2(s, ref), rel_l2(d, sim.get("displ"))
+    print(f"distorted+rotated att={att}: seismograms {es:.2e}, displacement {ed:.2e}")
+    assert np.abs(ref).max() > 0
+    assert es < 5e-5 and ed < 1e-4
+
+
+def test_coupled_distorted_mesh_vs_oracle(gpulib):
+    """Fluid over solid with a bumpy interface (moved interior nodes): hydrophone
+    pressure and potential <= 5e-5, solid displacement <= 1e-4 (the block bars)."""
+    from oracle import oracle as O
+    from specfem3d_gb300 import configs, hexmesh
+    cfg = configs.small_coupled(nstep=300)
+    cfg.pop("perturbation", None)
+    mesh = C.distorted(cfg, amplitude=0.15)
+    db = hexmesh.build_database(mesh, cfg)
+    assert db["num_coupling_ac_el_faces"] > 0
+    sim = O.make_coupled_sim(db, cfg, "f32", nthreads=os.cpu_count() or 1)
+    O.run_coupled(sim, cfg["nstep"])
+    ref = O.seismograms(sim)
+    s, d, p = _run_gpu(db, cfg, per_call=True)
+    e_p, e_chi, e_u = rel_l2(s[:, 0], ref[:, 0]), rel_l2(p, sim.get("potential")), rel_l2(d, sim.get("displ"))
+    print(f"coupled distorted: pressure {e_p:.2e}, potential {e_chi:.2e}, displacement {e_u:.2e}")
+    assert np.abs(ref[:, 0]).max() > 0
+    assert e_p < 5e-5 and e_chi < 5e-5 and e_u < 1e-4
+
+
+def test_rotation_invariance(gpulib):
+    """The same block, source and stations turned by a rotation R (moment tensor
+    R M R^T) give the seismograms turned by R, to FP32 accuracy (2e-5 relative
+    L2; the FP32 oracle meets 4e-7).  Free surfaces only: the Stacey mass term keeps the diagonal of a
+    tensor and is not invariant under rotation."""
+    from specfem3d_gb300 import configs, hexmesh
+    cfg = configs.small_layered(nstep=400, attenuation=True)
+    cfg["stacey"] = False
+    R = C.rotation()
+    db0 = hexmesh.build_database(hexmesh.block_mesh(cfg), cfg)
+    mesh, c = C.rotated(cfg, R)
+    db1 = hexmesh.build_database(mesh, c)
+    s0, _, _ = _run_gpu(db0, cfg)
+    s1, _, _ = _run_gpu(db1, c)
+    back = np.einsum("dc,rdt->rct", R, s1)
+    e = rel_l2(back, s0)
+    print(f"rotation invariance: {e:.2e}")
+    assert np.abs(s0).max() > 0
+    assert e < 2e-5

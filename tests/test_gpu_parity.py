@@ -189,29 +189,28 @@ def test_attenuation_time_stepping_vs_oracle(gpulib):
     g.close()
 
 
-@pytest.mark.parametrize("example,stacey", [("refex_stacey5sides", True), ("refex_no_absorbing", False)])
-def test_reference_golden_seismograms_on_gpu(gpulib, example, stacey):
-    """Full 5000-step reference example on the GPU against the reference's REF_SEIS.
-
-    Stacey example: relative L2 <= 1e-3 and correlation >= 0.999 per trace.  No-absorbing
-    example: the FP32 and FP64 oracles themselves differ from that REF_SEIS by up to
-    6.2e-3 (correlation >= 0.99998), so the trace check uses the reference's own
-    tolerances (compare_seismogram_correlations.py TOL_ERR = 0.01, CI correlation
-    >= 0.999) and the GPU is additionally held to the FP64 oracle's traces
+@pytest.mark.parametrize("example", ["refex_stacey5sides", "refex_no_absorbing"])
+def test_reference_golden_seismograms_on_gpu(gpulib, example):
+    """Full 5000-step reference examples on the GPU against the reference's REF_SEIS:
+    relative L2 <= 1e-3 and correlation >= 0.999 per trace.  The source of both
+    examples is a vertex of 8 elements; each configuration places it in the element
+    its REF_SEIS run chose (logged in that run's output_solver.txt).  The
+    no-absorbing run is also held to the FP64 oracle's traces
     (tests/golden/make_oracle_fixture.py) at <= 2e-4 (FP32 after 5000 steps)."""
     from specfem3d_gb300 import configs, meshgen
-    cfg = configs.refex(5000)
-    cfg["stacey"] = stacey
+    stacey = example == "refex_stacey5sides"
+    cfg = configs.refex(5000) if stacey else configs.refex_no_absorbing(5000)
     db = meshgen.build_database(cfg)
     g = _solver(db, cfg)
     g.run(cfg["nstep"], steps_per_graph=100)
     seis = g.seismograms()
     g.close()
     ref = np.load(os.path.join(ROOT, "tests", "golden", example + ".npz"))["displ"]
-    tol = 1e-3 if stacey else 1e-2
+    errs = [rel_l2(seis[r, c], ref[r, c]) for r in range(4) for c in range(3)]
+    print(f"{example}: all traces {rel_l2(seis, ref):.2e}, worst trace {max(errs):.2e}")
     for r in range(4):
         for c in range(3):
-            assert rel_l2(seis[r, c], ref[r, c]) < tol, (r, c)
+            assert rel_l2(seis[r, c], ref[r, c]) < 1e-3, (r, c)
             assert np.corrcoef(seis[r, c], ref[r, c])[0, 1] > 0.999
     if not stacey:
         o64 = np.load(os.path.join(ROOT, "tests", "golden", "refex_no_absorbing_oracle_f64.npz"))["displ"]
