@@ -299,6 +299,14 @@ int sf3d_iterate_time(long *Mesh_pointer, int it_begin, int it_end, realw deltat
  * runs: pressure in component 0, as compute_seismograms_cuda returns it). */
 int sf3d_get_seismograms(long *Mesh_pointer, realw *h_seismograms);
 
+/* One kind of the device seismogram buffers, (NDIM, nrec_local, nlength):
+ * kind 0 displacement, 1 velocity, 2 acceleration (the kinds enabled by
+ * SAVE_SEISMOGRAMS_* at prepare time), 3 pressure (component 1, the others 0).
+ * Receivers in fluid elements hold (1/rho) grad of chi, chi_dot, chi_dot_dot
+ * (compute_seismograms.f90:127-144).  Library-only: the Fortran solver gets
+ * these arrays from compute_seismograms_cuda. */
+int sf3d_get_seismograms_kind(long *Mesh_pointer, int kind, realw *h_seismograms);
+
 /* Device time of the stiffness kernel launches of the last sf3d_iterate_time
  * call with flags bit 0 set, in ms (a pair of CUDA events recorded on the
  * compute stream around each step's stiffness launches), their count, and the

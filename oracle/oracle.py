@@ -347,7 +347,7 @@ def _database(L, precision, cfg, anchors, xs, ys, zs, xtol, material, faces, sta
     db.update(derivation_matrices(precision))
     # sources and receivers
     _sources_receivers(L, precision, cfg, db)
-    db["stf"], db["t0"] = source_time_functions(cfg)
+    db["stf"], db["t0"] = source_time_functions(cfg, db.get("source_in_fluid"))
     db["attenuation"] = int(bool(cfg.get("attenuation", False)))
     if db["attenuation"]:
         db.update(attenuation_setup(db, cfg, precision))
@@ -447,12 +447,22 @@ def _sources_receivers(L, precision, cfg, db):
     sa = np.zeros((ns, 3, NGLL3), rd)  # (isrc, c, ijk) -> stored (NSOURCES,3,5,5,5) column-major
     isel = np.zeros(ns, np.int32)
     loc = np.zeros((ns, 3))
+    src_fluid = []
     for i, s in enumerate(srcs):
         ispec, xi, eta, ga = locate(L, db, s["x"], s["y"], s["z"], s.get("octant"))
         isel[i] = ispec
         loc[i] = (xi, eta, ga)
         out = np.zeros(3 * NGLL3, rd)
-        if s.get("type", "cmt") == "cmt":
+        fluid = bool(np.asarray(db["ispec_is_acoustic"])[ispec - 1]) if "ispec_is_acoustic" in db else False
+        src_fluid.append(fluid)
+        if s.get("type", "cmt") == "cmt" and fluid:
+            # setup_sources_receivers.f90:1187-1212: scalar moment M0 (Dahlen &
+            # Tromp 5.91) scaled to the equivalent explosion, on all components
+            Mxx, Myy, Mzz, Mxy, Mxz, Myz = (float(v) for v in s["M"])
+            m0 = np.sqrt(0.5 * (Mxx * Mxx + Myy * Myy + Mzz * Mzz + 2.0 * (Myz * Myz + Mxz * Mxz + Mxy * Mxy)))
+            fac = float(m0 * np.sqrt(2.0 / 3.0))
+            L.orc_source_array_force(xi, eta, ga, fac, fac, fac, _p(out))
+        elif s.get("type", "cmt") == "cmt":
             Mxx, Myy, Mzz, Mxy, Mxz, Myz = (float(v) for v in s["M"])
             rt = ctypes.c_float if precision == "f32" else ctypes.c_double
             L.orc_source_array_cmt(ispec, _p(db["irregular_element_number"]), ctypes.addressof(mptrs),
@@ -466,6 +476,7 @@ def _sources_receivers(L, precision, cfg, db):
     db["sourcearrays"] = np.ascontiguousarray(sa.transpose(2, 1, 0)).reshape(-1)
     db["ispec_selected_source"] = isel
     db["source_xi_eta_gamma"] = loc
+    db["source_in_fluid"] = np.asarray(src_fluid, bool)
     recs = cfg.get("receivers", [])
     nr = len(recs)
     irec = np.zeros(nr, np.int32)
@@ -482,14 +493,23 @@ def _sources_receivers(L, precision, cfg, db):
               receiver_xi_eta_gamma=rloc, nrec=nr, nsources=ns)
 
 
-def source_time_functions(cfg: dict) -> np.ndarray:
+def source_time_functions(cfg: dict, in_fluid=None) -> np.ndarray:
     """(NSOURCES, NSTEP) FP64 table following setup_sources_receivers.f90:482-491
-    for t0 and get_stf_viscoelastic (compute_add_sources_viscoelastic.F90:837-932)."""
+    for t0 and get_stf_viscoelastic (compute_add_sources_viscoelastic.F90:837-932).
+    Sources in fluid elements: a moment tensor takes the Gaussian instead of the
+    Heaviside (get_stf_acoustic), and a Gaussian there sets t0 to at least
+    3 (hdur - tshift) (setup_sources_receivers.f90:495-514)."""
     srcs = cfg.get("sources", [])
     dt, nstep = float(cfg["dt"]), int(cfg["nstep"])
     if not srcs:
         return np.zeros((0, nstep)), 0.0
-    kinds = [s.get("stf", "ricker") for s in srcs]
+    fl = list(in_fluid) if in_fluid is not None else [False] * len(srcs)
+    kinds = []
+    for s, f in zip(srcs, fl):
+        k = s.get("stf", "ricker")
+        if f and s.get("type", "cmt") == "cmt" and k == "heaviside":
+            k = "gaussian"
+        kinds.append(k)
     params = [float(s["f0"]) if k == "ricker" else float(s["hdur"]) for s, k in zip(srcs, kinds)]
     tsh = np.array([float(s.get("tshift", 0.0)) for s in srcs])
     tsh = tsh - tsh.min() if len(srcs) > 1 else np.zeros(1)
@@ -497,6 +517,9 @@ def source_time_functions(cfg: dict) -> np.ndarray:
         t0 = -1.2 * min(ts - 1.0 / p for ts, p in zip(tsh, params))
     else:
         t0 = -2.0 * min(ts - p for ts, p in zip(tsh, params))
+    for f, k, ts, p in zip(fl, kinds, tsh, params):
+        if f and k == "gaussian" and -3.0 * (ts - p) > t0:
+            t0 = -3.0 * (ts - p)
     if "t0" in cfg:
         t0 = float(cfg["t0"])
     return np.stack([stf_table(k, p, ts, t0, dt, nstep) for k, p, ts in zip(kinds, params, tsh)]), t0

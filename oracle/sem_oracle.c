@@ -46,7 +46,7 @@ static const orc_field k_int_fields[] = {
   F(nspec), F(nglob), F(nspec_irregular), F(nsources), F(nrec), F(nstep), F(it),
   F(attenuation), F(stacey), F(compute_and_store_strain), F(simulation_type), F(nthreads),
   F(record_what), F(num_abs_boundary_faces), F(n_elastic), F(n_acoustic), F(num_coupling_faces),
-  F(num_free_surface_faces),
+  F(num_free_surface_faces), F(fluid_vector),
 };
 static const orc_field k_real_fields[] = {
   F(xix_regular), F(jacobian_regular), F(deltat), F(deltatover2), F(deltatsqover2),
@@ -1005,9 +1005,54 @@ void orc_add_sources(orc_sim *s, realw *accel, int it) {
 
 /* compute_seismograms + compute_interpolated_dva_viscoelast
  * (compute_seismograms.f90:29-265, compute_interpolated_dva.f90:28-110). */
+/* (1/rho) grad chi at the GLL points of one fluid element
+ * (compute_gradient_in_acoustic.f90:28-200), then interpolated at the receiver
+ * with its Lagrange weights (compute_interpolated_dva_acoust). */
+static void fluid_vector_seismogram(const orc_sim *s, const realw *chi, int r, int ispec, double u[3]) {
+  const int ir = s->irregular_element_number[ispec];
+  u[0] = u[1] = u[2] = 0.0;
+  for (int k = 0; k < NGLL; ++k)
+    for (int j = 0; j < NGLL; ++j)
+      for (int i = 0; i < NGLL; ++i) {
+        realw t1 = 0, t2 = 0, t3 = 0;
+        for (int l = 0; l < NGLL; ++l) {
+          t1 += chi[s->ibool[IJK(l, j, k) + (long)NGLL3 * ispec] - 1] * s->hprime_xx[i + NGLL * l];
+          t2 += chi[s->ibool[IJK(i, l, k) + (long)NGLL3 * ispec] - 1] * s->hprime_xx[j + NGLL * l];
+          t3 += chi[s->ibool[IJK(i, j, l) + (long)NGLL3 * ispec] - 1] * s->hprime_xx[k + NGLL * l];
+        }
+        const int p = IJK(i, j, k);
+        const realw rho_inv = (realw)1 / s->rhostore[p + (long)NGLL3 * ispec];
+        realw g[3];
+        if (ir) {
+          const long q = p + (long)NGLL3 * (ir - 1);
+          g[0] = rho_inv * (s->xix[q] * t1 + s->etax[q] * t2 + s->gammax[q] * t3);
+          g[1] = rho_inv * (s->xiy[q] * t1 + s->etay[q] * t2 + s->gammay[q] * t3);
+          g[2] = rho_inv * (s->xiz[q] * t1 + s->etaz[q] * t2 + s->gammaz[q] * t3);
+        } else {
+          g[0] = rho_inv * s->xix_regular * t1;
+          g[1] = rho_inv * s->xix_regular * t2;
+          g[2] = rho_inv * s->xix_regular * t3;
+        }
+        const double h = s->hxir[i + NGLL * r] * s->hetar[j + NGLL * r] * s->hgammar[k + NGLL * r];
+        for (int c = 0; c < 3; ++c) u[c] += h * (double)g[c];
+      }
+}
+
 void orc_seismograms(orc_sim *s, const realw *field, int it) {
   for (int r = 0; r < s->nrec; ++r) {
     int ispec = s->ispec_selected_rec[r] - 1;
+    if (s->rec_is_acoustic && s->rec_is_acoustic[r] && s->fluid_vector) {
+      const realw *chi = s->record_what == 2 ? s->potential_dot
+                         : (s->record_what == 3 ? s->potential_dot_dot : s->potential);
+      double u[3];
+      fluid_vector_seismogram(s, chi, r, ispec, u);
+      const double *nu = s->nu_rec ? s->nu_rec + 9 * r : NULL;
+      for (int c = 0; c < 3; ++c) {
+        double v = nu ? nu[c + 0] * u[0] + nu[c + 3] * u[1] + nu[c + 6] * u[2] : u[c];
+        s->seismograms[c + 3 * (r + (long)s->nrec * (it - 1))] = (double)(realw)v;
+      }
+      continue;
+    }
     if (s->rec_is_acoustic && s->rec_is_acoustic[r]) {
       /* pressure = - sum h chi_dot_dot (compute_interpolated_dva.f90:280-300) */
       double pd = 0.0;
@@ -1396,7 +1441,10 @@ void orc_step_coupled(orc_sim *s) {
     s->accel[3 * g + 2] *= s->rmassz[g];
   }
   for (long i = 0; i < n3; ++i) s->veloc[i] += s->deltatover2 * s->accel[i];
-  if (s->nrec > 0 && s->seismograms) orc_seismograms(s, s->displ, s->it);
+  if (s->nrec > 0 && s->seismograms) {
+    const realw *f = s->record_what == 2 ? s->veloc : (s->record_what == 3 ? s->accel : s->displ);
+    orc_seismograms(s, f, s->it);
+  }
   s->it++;
 }
 

@@ -93,6 +93,7 @@ typedef struct orc_sim {
   realw *coupling_normal, *coupling_jacobian2Dw;
   int num_free_surface_faces, *free_surface_ispec, *free_surface_ijk;
   int *rec_is_acoustic;                /* (nrec) records pressure when 1 */
+  int fluid_vector;                    /* 1: fluid receivers record (1/rho) grad of the potential */
 } orc_sim;
 
 #endif

@@ -146,6 +146,45 @@ def refex_no_absorbing(nstep: int = 5000) -> dict:
     return cfg
 
 
+# the 22 stations of EXAMPLES/applications/waterlayered_halfspace/DATA/STATIONS:
+# (name, x = longitude column, y = latitude column, burial)
+WATERLAYERED_STATIONS = [
+    ("X10", 10767.86, 67000.0, 100.0), ("X20", 22732.14, 67000.0, 100.0), ("X30", 34696.43, 67000.0, 100.0),
+    ("X40", 46660.71, 67000.0, 100.0), ("X50", 58625.00, 67000.0, 100.0), ("X55", 67000.00, 67000.0, 100.0),
+    ("X60", 75375.00, 67000.0, 100.0), ("X70", 87339.29, 67000.0, 100.0), ("X80", 99303.57, 67000.0, 100.0),
+    ("X90", 111269.86, 67000.0, 100.0), ("X1", 0.0, 67000.0, 100.0), ("X2", 67000.0, 67000.0, 25000.0),
+    ("X3", 134000.0, 67000.0, 100.0), ("X4", 67000.0, 67000.0, 3500.0), ("X5", 67000.0, 67000.0, 3000.2),
+    ("X6", 67000.0, 67000.0, 3000.1), ("X7", 67000.0, 67000.0, 2999.9), ("X8", 67000.0, 67000.0, 2999.8),
+    ("Y1", 58625.0, 67000.0, 2999.9), ("Y2", 58625.0, 67000.0, 3000.1), ("Y3", 46660.71, 67000.0, 2999.9),
+    ("Y4", 46660.71, 67000.0, 3000.1)]
+
+
+def waterlayered(nstep: int = 4500) -> dict:
+    """The reference example waterlayered_halfspace: a 45 x 45 x 20 element block
+    of 134 x 134 x 60 km (its MESH-default grid), the top element row water
+    (rho 1028, vp 1480) over a solid (3200, 7500, 4300) given as two materials
+    of equal properties as in its nummaterial_velocity_file; Stacey on the five
+    sides, free surface on top; the CMTSOLUTION explosion (Mrr = Mtt = Mpp =
+    1e23 dyne.cm, half duration 2 s) 1 km deep in the water at (66999.9, 67000);
+    the STATIONS list buried below the surface; dt 0.005 s.  The source lies in
+    a fluid element, so the reference takes a Gaussian time function and t0 = 6 s;
+    seismograms in fluid elements are (1/rho) grad of the potential."""
+    M0 = 1e23 * 1e-7
+    zlev = [float(z) for z in np.linspace(-60000.0, 0.0, 21)]
+    rows = [2] * 16 + [1] * 3 + [0]           # bottom-up: material 3, material 2, water
+    cfg = dict(nx=45, ny=45, x0=0.0, x1=134000.0, y0=0.0, y1=134000.0, zlev=zlev,
+               elem_layer=np.repeat(np.asarray(rows, np.int32), 45 * 45),
+               layers=[dict(rho=1028.0, vp=1480.0, vs=0.0), dict(rho=3200.0, vp=7500.0, vs=4300.0),
+                       dict(rho=3200.0, vp=7500.0, vs=4300.0)],
+               dt=0.005, nstep=nstep,
+               sources=[dict(type="cmt", x=66999.9, y=67000.0, z=-1000.0, M=[M0, M0, M0, 0.0, 0.0, 0.0],
+                             stf="heaviside", hdur=2.0)],
+               receivers=[(x, y, -b) for _, x, y, b in WATERLAYERED_STATIONS],
+               station_names=[n for n, _, _, _ in WATERLAYERED_STATIONS],
+               record=("displ", "veloc", "accel"))
+    return finish(cfg)
+
+
 def homogeneous_block(nstep: int = 2000, seed: int = 2024) -> dict:
     rng = np.random.default_rng(seed)
     g = np.linspace(1000.0, 9000.0, 5)

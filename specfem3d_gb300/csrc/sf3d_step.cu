@@ -151,6 +151,20 @@ __global__ void sources_kernel(int nsrc, const int* __restrict__ ispec_src, cons
   atomicAdd(accel + 3L * g + 2, s[2] * stf);
 }
 
+// Fluid receivers of vector seismograms: the field is (1/rho) grad of a potential
+// (chi, chi_dot, chi_dot_dot for displacement, velocity, acceleration) evaluated
+// at the element's GLL points (compute_gradient_in_acoustic.f90:28-200) before
+// the interpolation.  scalar == nullptr: no fluid receivers.
+struct AcousticSeismo {
+  const float* scalar = nullptr;
+  const int* rec_is_acoustic = nullptr;
+  const int* irregular = nullptr;
+  const float* m[9] = {};
+  const float* rhostore = nullptr;
+  const float* gll = nullptr;          // hprime first
+  float xix_regular = 0.f;
+};
+
 // Receiver interpolation (compute_interpolated_dva.f90:28-110,
 // kernels/compute_elastic_seismogram_kernel.cu): block = receiver; warp-shuffle
 // tree sum of h_xi h_eta h_gamma u over the 125 points, then rotation by nu.
@@ -161,11 +175,48 @@ __global__ void seismogram_kernel(int nrec, const int* __restrict__ ispec_rec, c
                                   const float* __restrict__ nu, const int* __restrict__ ibool,
                                   const float* __restrict__ field, float* __restrict__ seismo, int nlength,
                                   int slot, const int* __restrict__ d_it_slot, int* d_it, unsigned int* d_done,
-                                  int advance) {
+                                  int advance, AcousticSeismo ac) {
   __shared__ float red[3][4];
+  __shared__ float s_chi[NGLL3_PAD];
+  __shared__ float s_hp[NGLL2];
   const int r = blockIdx.x, t = threadIdx.x;
   float s0 = 0.f, s1 = 0.f, s2 = 0.f;
-  if (r < nrec && t < NGLL3) {
+  // block-uniform: the whole block takes one branch
+  const bool fluid = ac.scalar != nullptr && r < nrec && ac.rec_is_acoustic[r] != 0;
+  if (fluid) {
+    const int e = ispec_rec[r];
+    const long eo = (long)e * NGLL3_PAD + t;
+    if (t < NGLL3) s_chi[t] = ac.scalar[ibool[eo]];
+    if (t < NGLL2) s_hp[t] = ac.gll[t];
+    __syncthreads();
+    if (t < NGLL3) {
+      const int k = t / NGLL2, j = (t / NGLLX) % NGLLX, i = t % NGLLX;
+      float a = 0.f, b = 0.f, c = 0.f;
+#pragma unroll
+      for (int l = 0; l < NGLLX; ++l) {
+        a = fmaf(s_chi[l + NGLLX * j + NGLL2 * k], s_hp[i + NGLLX * l], a);
+        b = fmaf(s_chi[i + NGLLX * l + NGLL2 * k], s_hp[j + NGLLX * l], b);
+        c = fmaf(s_chi[i + NGLLX * j + NGLL2 * l], s_hp[k + NGLLX * l], c);
+      }
+      const float rho_inv = 1.f / ac.rhostore[eo];
+      const int ir = ac.irregular[e];
+      float gx, gy, gz;
+      if (ir >= 0) {
+        const long mo = (long)ir * NGLL3_PAD + t;
+        gx = ac.m[0][mo] * a + ac.m[3][mo] * b + ac.m[6][mo] * c;
+        gy = ac.m[1][mo] * a + ac.m[4][mo] * b + ac.m[7][mo] * c;
+        gz = ac.m[2][mo] * a + ac.m[5][mo] * b + ac.m[8][mo] * c;
+      } else {
+        gx = ac.xix_regular * a;
+        gy = ac.xix_regular * b;
+        gz = ac.xix_regular * c;
+      }
+      const float h = hx[5 * r + i] * he[5 * r + j] * hg[5 * r + k];
+      s0 = h * (rho_inv * gx);
+      s1 = h * (rho_inv * gy);
+      s2 = h * (rho_inv * gz);
+    }
+  } else if (r < nrec && t < NGLL3) {
     const int e = ispec_rec[r];
     const int k = t / NGLL2, j = (t / NGLLX) % NGLLX, i = t % NGLLX;
     const float h = hx[5 * r + i] * he[5 * r + j] * hg[5 * r + k];
@@ -209,6 +260,20 @@ __global__ void seismogram_kernel(int nrec, const int* __restrict__ ispec_rec, c
 }
 
 __global__ void advance_it_kernel(int* d_it) { *d_it += 1; }
+
+// fluid-receiver arguments for a potential field (nullptr: none)
+AcousticSeismo acoustic_seismo(const Mesh* mp, const float* potential) {
+  AcousticSeismo ac;
+  if (!mp->has_acoustic || !mp->d_rec_is_acoustic || !potential) return ac;
+  ac.scalar = potential;
+  ac.rec_is_acoustic = mp->d_rec_is_acoustic;
+  ac.irregular = mp->d_irregular;
+  for (int q = 0; q < 9; ++q) ac.m[q] = mp->d_metric[q];
+  ac.rhostore = mp->d_rhostore;
+  ac.gll = mp->d_gll;
+  ac.xix_regular = mp->xix_regular;
+  return ac;
+}
 __global__ void set_it_kernel(int* d_it, int v) { *d_it = v; }
 
 // max |u| over the field (check_stability.f90:408), NaN-propagating
@@ -328,7 +393,8 @@ int enqueue_step(Mesh* mp, float dt, float dt2, float dtsq2, bool first_step, cu
     seismogram_kernel<<<mp->nrec_local, NGLL3_PAD, 0, s>>>(mp->nrec_local, mp->d_ispec_rec, mp->d_hxir, mp->d_hetar,
                                                            mp->d_hgammar, mp->d_nu_rec, mp->d_ibool, F.displ,
                                                            mp->d_seismo_d, mp->nlength_seismogram, 0, mp->d_it,
-                                                           mp->d_it, mp->d_done, 1);
+                                                           mp->d_it, mp->d_done, 1,
+                                                           acoustic_seismo(mp, mp->d_potential));
   } else {
     advance_it_kernel<<<1, 1, 0, s>>>(mp->d_it);
   }
@@ -543,13 +609,16 @@ void compute_seismograms_cuda_(long* Mesh_pointer_f, realw* seismograms_d, realw
   }
   // kernel simulations record the reconstructed forward field
   Fields* F = mp->simulation_type == 3 ? &mp->b : &mp->f;
-  struct { int on; float* field; float* dst; } kinds[3] = {
-      {mp->save_d, F->displ, mp->d_seismo_d}, {mp->save_v, F->veloc, mp->d_seismo_v}, {mp->save_a, F->accel, mp->d_seismo_a}};
+  const bool fwd = mp->simulation_type != 3;
+  struct { int on; float* field; float* dst; const float* pot; } kinds[3] = {
+      {mp->save_d, F->displ, mp->d_seismo_d, fwd ? mp->d_potential : nullptr},
+      {mp->save_v, F->veloc, mp->d_seismo_v, fwd ? mp->d_potential_dot : nullptr},
+      {mp->save_a, F->accel, mp->d_seismo_a, fwd ? mp->d_potential_dot_dot : nullptr}};
   for (auto& kd : kinds) {
     if (!kd.on || !kd.field) continue;
     seismogram_kernel<<<mp->nrec_local, NGLL3_PAD, 0, mp->stream>>>(
         mp->nrec_local, mp->d_ispec_rec, mp->d_hxir, mp->d_hetar, mp->d_hgammar, mp->d_nu_rec, mp->d_ibool, kd.field,
-        kd.dst, nlen, cur, nullptr, nullptr, nullptr, 0);
+        kd.dst, nlen, cur, nullptr, nullptr, nullptr, 0, acoustic_seismo(mp, kd.pot));
   }
   if (mp->save_p) launch_pressure_seismograms(mp, cur);
   if (!cuda_ok(cudaGetLastError(), "seismogram_kernel")) return;
@@ -772,6 +841,39 @@ int sf3d_get_seismograms(long* Mesh_pointer, realw* h) {
   const size_t bytes = sizeof(float) * 3 * (size_t)mp->nrec_local * mp->nlength_seismogram;
   SF3D_CUDA_RET(cudaMemcpyAsync(h, mp->d_seismo_d, bytes, cudaMemcpyDeviceToHost, mp->stream), SF3D_ERR_CUDA);
   SF3D_CUDA_RET(cudaStreamSynchronize(mp->stream), SF3D_ERR_CUDA);
+  return SF3D_OK;
+}
+
+int sf3d_get_seismograms_kind(long* Mesh_pointer, int kind, realw* h) {
+  Mesh* mp = get_mesh(Mesh_pointer);
+  if (!mp) return SF3D_ERR_STATE;
+  if (kind < 0 || kind > 3) {
+    set_error(SF3D_ERR_ARG, "sf3d_get_seismograms_kind: kind must be 0..3");
+    return SF3D_ERR_ARG;
+  }
+  if (mp->nrec_local == 0) return SF3D_OK;
+  const size_t n = (size_t)mp->nrec_local * mp->nlength_seismogram;
+  if (kind == 3) {
+    if (!mp->d_seismo_p) {
+      set_error(SF3D_ERR_STATE, "pressure seismograms were not enabled");
+      return SF3D_ERR_STATE;
+    }
+    std::vector<float> p(n);
+    if (!copy_sync(p.data(), mp->d_seismo_p, sizeof(float) * n, cudaMemcpyDeviceToHost, mp->stream))
+      return SF3D_ERR_CUDA;
+    for (size_t q = 0; q < n; ++q) {
+      h[3 * q] = p[q];
+      h[3 * q + 1] = 0.f;
+      h[3 * q + 2] = 0.f;
+    }
+    return SF3D_OK;
+  }
+  const float* src = kind == 0 ? mp->d_seismo_d : (kind == 1 ? mp->d_seismo_v : mp->d_seismo_a);
+  if (!src) {
+    set_error(SF3D_ERR_STATE, "this seismogram kind was not enabled");
+    return SF3D_ERR_STATE;
+  }
+  if (!copy_sync(h, src, sizeof(float) * 3 * n, cudaMemcpyDeviceToHost, mp->stream)) return SF3D_ERR_CUDA;
   return SF3D_OK;
 }
 

@@ -499,6 +499,7 @@ def _sources_receivers(cfg, B, db, dtype, locator=None):
     sa = np.zeros((ns, 3, NGLL3))
     isel = np.zeros(ns, np.int32)
     loc = np.zeros((ns, 3))
+    src_fluid = np.zeros(ns, bool)
     irr = db["irregular_element_number"]
     for i, s in enumerate(srcs):
         e1, xi, eta, ga = locator(float(s["x"]), float(s["y"]), float(s["z"]), s.get("octant"))
@@ -508,7 +509,18 @@ def _sources_receivers(cfg, B, db, dtype, locator=None):
         he, hpe = lagrange(eta)
         hg, hpg = lagrange(ga)
         hl = (hg[:, None, None] * he[None, :, None] * hx[None, None, :]).reshape(-1)
-        if s.get("type", "cmt") == "cmt":
+        in_fluid = bool(np.asarray(db.get("ispec_is_acoustic", np.zeros(e1, np.int32)))[e1 - 1])
+        src_fluid[i] = in_fluid
+        if s.get("type", "cmt") == "cmt" and in_fluid:
+            # moment tensor in a fluid element: an explosion-equivalent pressure
+            # source of the scalar moment (setup_sources_receivers.f90:1187-1212):
+            # factor = sqrt(2/3) M0, M0 = sqrt(M:M / 2), interpolated on the element
+            Mxx, Myy, Mzz, Mxy, Mxz, Myz = (float(v) for v in s["M"])
+            m0 = math.sqrt(Mxx ** 2 + Myy ** 2 + Mzz ** 2 + 2.0 * (Myz ** 2 + Mxz ** 2 + Mxy ** 2)) / math.sqrt(2.0)
+            fac = m0 * math.sqrt(2.0) / math.sqrt(3.0)
+            for c in range(3):
+                sa[i, c] = fac * hl
+        elif s.get("type", "cmt") == "cmt":
             ir = irr[e1 - 1]
             if ir:
                 m = [db[n].reshape(-1, NGLL3)[ir - 1].astype(np.float64) for n in
@@ -552,7 +564,7 @@ def _sources_receivers(cfg, B, db, dtype, locator=None):
         hg[r], _ = lagrange(ga)
     db.update(ispec_selected_rec=irec, hxir=hx.reshape(-1), hetar=he.reshape(-1), hgammar=hg.reshape(-1),
               receiver_xi_eta_gamma=rloc, nrec=nr)
-    stf, t0 = stf_table(cfg)
+    stf, t0 = stf_table(cfg, src_fluid)
     db["stf"] = stf
     db["t0"] = t0
 
@@ -571,14 +583,20 @@ def stf_value(kind: str, t, p):
     return np.exp(-t * t / (hd * hd)) / (math.sqrt(math.pi) * hd)
 
 
-def stf_table(cfg: dict):
+def stf_table(cfg: dict, in_fluid=None):
     """(NSOURCES, NSTEP) FP64 stf at t = (it-1) dt - t0 - tshift
-    (compute_add_sources_viscoelastic.F90:80-100), t0 per setup_sources_receivers.f90:482-491."""
+    (compute_add_sources_viscoelastic.F90:80-100), t0 per setup_sources_receivers.f90:482-491.
+    Moment-tensor sources in fluid elements (in_fluid) use a Gaussian instead of
+    the Heaviside (get_stf_acoustic, compute_add_sources_acoustic.f90:693-821)
+    and move t0 to at least 3 (hdur - tshift) (setup_sources_receivers.f90:495-514)."""
     srcs = cfg.get("sources", [])
     dt, nstep = float(cfg["dt"]), int(cfg["nstep"])
     if not srcs:
         return np.zeros((0, nstep)), 0.0
+    fluid = [bool(in_fluid[i]) if in_fluid is not None else False for i in range(len(srcs))]
     kinds = [s.get("stf", "ricker") for s in srcs]
+    kinds = ["gaussian" if f and k == "heaviside" and s.get("type", "cmt") == "cmt" else k
+             for s, k, f in zip(srcs, kinds, fluid)]
     params = [float(s["f0"]) if k == "ricker" else float(s["hdur"]) for s, k in zip(srcs, kinds)]
     tsh = np.array([float(s.get("tshift", 0.0)) for s in srcs])
     tsh = tsh - tsh.min() if len(srcs) > 1 else np.zeros(1)
@@ -586,6 +604,9 @@ def stf_table(cfg: dict):
         t0 = -1.2 * min(ts - 1.0 / p for ts, p in zip(tsh, params))
     else:
         t0 = -2.0 * min(ts - p for ts, p in zip(tsh, params))
+    for f, k, ts, p in zip(fluid, kinds, tsh, params):
+        if f and k == "gaussian":
+            t0 = max(t0, -3.0 * (ts - p))
     if "t0" in cfg:
         t0 = float(cfg["t0"])
     t = (np.arange(nstep) * dt) - t0

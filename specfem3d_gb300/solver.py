@@ -270,9 +270,19 @@ class GPUSolver:
         return dict(stiffness_ms=sm.value, stiffness_launches=sl.value, total_ms=tm.value, total_launches=tl.value)
 
     # ----------------------------------------------------------------- outputs
-    def seismograms(self) -> np.ndarray:
+    def seismograms(self, kind: str = None) -> np.ndarray:
         """(nrec, 3, nlength) displacement traces (pressure runs: the per-call
-        path's host array, pressure in component 0)."""
+        path's host array, pressure in component 0).  kind "displ", "veloc",
+        "accel" or "pressure" reads that device buffer (enabled through
+        ``record``); fluid receivers hold (1/rho) grad of the potential's
+        matching time derivative."""
+        if kind is not None:
+            code = {"displ": 0, "veloc": 1, "accel": 2, "pressure": 3}[kind]
+            out = np.zeros(3 * self.nrec * self.nlength, np.float32)
+            if self.nrec:
+                self.L.sf3d_get_seismograms_kind(self.mp, code, out.ctypes.data)
+                abi.check()
+            return out.reshape(self.nlength, self.nrec, 3).transpose(1, 2, 0)
         if "pressure" in self.record and getattr(self, "_last_path", "") == "per_call":
             return self._seis_host.reshape(self.nlength, self.nrec, 3).transpose(1, 2, 0).copy()
         out = np.zeros(3 * self.nrec * self.nlength, np.float32)

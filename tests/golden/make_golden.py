@@ -2,9 +2,9 @@
 
 Run in a checkout where the SPECFEM3D reference tree is available (its path is
 the first argument, default /root/reference).  It reads the ASCII
-traces (.semd) committed under the reference's example REF_SEIS directories and writes
-float32 arrays (station, component, sample) plus the time axis to
-tests/golden/*.npz.  The fixtures are used by the oracle and GPU parity tests,
+traces (.semd, .semv, .sema) committed under the reference's example REF_SEIS
+directories and writes float32 arrays (station, component, sample) plus the time
+axis to tests/golden/*.npz.  The fixtures are used by the oracle and GPU parity tests,
 which never read the reference tree at run time.
 """
 import os
@@ -29,6 +29,30 @@ def read(root, example, ext):
     return np.asarray(traces, np.float32), np.asarray(t, np.float64)
 
 
+def read_waterlayered(root):
+    """waterlayered_halfspace REF_SEIS: vertical (HXZ) traces; displacement (the
+    nine X10..X90 stations it has) and velocity (all 22 stations).  Its
+    acceleration traces are left out to keep the fixture small."""
+    d = os.path.join(root, EX, "waterlayered_halfspace", "REF_SEIS")
+    sys.path.insert(0, os.path.dirname(os.path.dirname(os.path.dirname(os.path.abspath(__file__)))))
+    from specfem3d_gb300.configs import WATERLAYERED_STATIONS
+    names = [n for n, _, _, _ in WATERLAYERED_STATIONS]
+    out, t = {}, None
+    for ext, key in (("semd", "displ"), ("semv", "veloc")):
+        rows, have = [], []
+        for n in names:
+            f = os.path.join(d, f"DB.{n}.HXZ.{ext}")
+            if os.path.exists(f):
+                a = np.loadtxt(f)
+                t = a[:, 0]
+                rows.append(a[:, 1])
+                have.append(n)
+        out[key] = np.asarray(rows, np.float32)
+        out[key + "_stations"] = np.array(have)
+    out["t"] = np.asarray(t, np.float64)
+    return out
+
+
 def main():
     root = sys.argv[1] if len(sys.argv) > 1 else "/root/reference"
     out = os.path.dirname(os.path.abspath(__file__))
@@ -36,6 +60,7 @@ def main():
     np.savez_compressed(os.path.join(out, "refex_stacey5sides.npz"), displ=d, t=t, stations=np.array(STATIONS))
     nd, t2 = read(root, "homogeneous_halfspace_HEX8_elastic_no_absorbing", "semd")
     np.savez_compressed(os.path.join(out, "refex_no_absorbing.npz"), displ=nd, t=t2, stations=np.array(STATIONS))
+    np.savez_compressed(os.path.join(out, "waterlayered.npz"), **read_waterlayered(root))
 
 
 if __name__ == "__main__":

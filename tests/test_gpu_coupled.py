@@ -53,3 +53,63 @@ def test_coupled_fused_loop_equals_per_call(gpulib):
     assert np.abs(s1[:, 0]).max() > 0
     assert rel_l2(s2[:, 0], s1[:, 0]) < 5e-5
     assert rel_l2(p2, p1) < 5e-5 and rel_l2(d2, d1) < 5e-5
+
+
+def test_fluid_receiver_vector_seismograms_vs_oracle(gpulib):
+    """Receivers in fluid elements record (1/rho) grad of chi, chi_dot and
+    chi_dot_dot as displacement, velocity and acceleration (the reference's
+    compute_gradient_in_acoustic path), solid receivers their fields: per-call
+    GPU traces against the oracle's, 300 steps, <= 5e-5 relative L2 per kind."""
+    from oracle import oracle as O
+    from specfem3d_gb300 import configs, meshgen, solver
+    cfg = configs.small_coupled(nstep=300)
+    cfg["record"] = ("displ", "veloc", "accel")
+    zf = cfg["zlev"][len(cfg["zlev"]) - 3]
+    cfg["receivers"] = cfg["receivers"] + [(cfg["x1"] * 0.45, cfg["y1"] * 0.55, zf - 120.0)]   # one in the solid
+    db = meshgen.build_database(cfg)
+    isac = db["ispec_is_acoustic"].astype(bool)
+    in_fluid = isac[db["ispec_selected_rec"] - 1]
+    assert in_fluid[:3].all() and not in_fluid[3]
+    g = solver.GPUSolver(db, cfg)
+    g.run_per_call(cfg["nstep"])
+    got = {k: g.seismograms(k) for k in ("displ", "veloc", "accel")}
+    g.close()
+    for code, k in ((1, "displ"), (2, "veloc"), (3, "accel")):
+        sim = O.make_coupled_sim(db, cfg, "f32", nthreads=os.cpu_count() or 1)
+        sim.seti("fluid_vector", 1)
+        sim.seti("record_what", code)
+        O.run_coupled(sim, cfg["nstep"])
+        ref = O.seismograms(sim)
+        e = rel_l2(got[k], ref)
+        ef = rel_l2(got[k][:3], ref[:3])
+        print(f"{k}: all receivers {e:.2e}, fluid receivers {ef:.2e}")
+        assert np.abs(ref[:3]).max() > 0 and np.abs(ref[3]).max() > 0
+        assert e < 5e-5 and ef < 5e-5
+
+
+def test_waterlayered_reference_golden_seismograms(gpulib):
+    """The reference example waterlayered_halfspace (4500 steps, 40500 elements,
+    explosion in the water) against its REF_SEIS vertical traces: displacement at
+    the 9 X10..X90 stations (in the water, 100 m deep) and velocity at all 22
+    (water, solid, and 0.1-0.2 m either side of the sea floor)."""
+    from conftest import ROOT
+    from specfem3d_gb300 import configs, meshgen, solver
+    cfg = configs.waterlayered(4500)
+    db = meshgen.build_database(cfg)
+    g = solver.GPUSolver(db, cfg)
+    g.run_per_call(cfg["nstep"])
+    got = {k: g.seismograms(k) for k in ("displ", "veloc")}
+    g.close()
+    ref = np.load(os.path.join(ROOT, "tests", "golden", "waterlayered.npz"))
+    names = list(cfg["station_names"])
+    worst = {}
+    for k in ("displ", "veloc"):
+        for n, tr in zip(ref[k + "_stations"], ref[k]):
+            r = names.index(str(n))
+            e = rel_l2(got[k][r, 2], tr)
+            c = np.corrcoef(got[k][r, 2], tr)[0, 1]
+            worst[(k, str(n))] = (e, c)
+    for (k, n), (e, c) in sorted(worst.items(), key=lambda t: -t[1][0])[:8]:
+        print(f"waterlayered {k} {n}: rel L2 {e:.2e}, correlation {c:.6f}")
+    for (k, n), (e, c) in worst.items():
+        assert e < 1e-2 and c > 0.9999, (k, n, e, c)
