@@ -91,7 +91,9 @@ def test_waterlayered_reference_golden_seismograms(gpulib):
     """The reference example waterlayered_halfspace (4500 steps, 40500 elements,
     explosion in the water) against its REF_SEIS vertical traces: displacement at
     the 9 X10..X90 stations (in the water, 100 m deep) and velocity at all 22
-    (water, solid, and 0.1-0.2 m either side of the sea floor)."""
+    (water, solid, and 0.1-0.2 m either side of the sea floor).  Per trace:
+    relative L2 <= 1e-3 and correlation >= 0.99999 (measured: <= 2.5e-4, the
+    worst at the stations 0.1 m above the sea floor)."""
     from conftest import ROOT
     from specfem3d_gb300 import configs, meshgen, solver
     cfg = configs.waterlayered(4500)
@@ -112,4 +114,4 @@ def test_waterlayered_reference_golden_seismograms(gpulib):
     for (k, n), (e, c) in sorted(worst.items(), key=lambda t: -t[1][0])[:8]:
         print(f"waterlayered {k} {n}: rel L2 {e:.2e}, correlation {c:.6f}")
     for (k, n), (e, c) in worst.items():
-        assert e < 1e-2 and c > 0.9999, (k, n, e, c)
+        assert e < 1e-3 and c > 0.99999, (k, n, e, c)
