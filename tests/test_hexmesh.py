@@ -185,3 +185,36 @@ def test_reference_cubit_mesh_files():
         h = [db[k].reshape(-1, 5)[r] for k in ("hxir", "hetar", "hgammar")]
         w = (h[2][:, None, None] * h[1][None, :, None] * h[0][None, None, :]).reshape(-1)
         assert np.allclose(w @ xyz[e], [x, y, z], atol=1e-6 * 134000.0)
+
+
+@pytest.mark.skipif(not os.path.isdir(REF_EXAMPLES), reason="reference tree not present")
+def test_reference_cubit_waterlayered_mesh():
+    """waterlayered_halfspace's own CUBIT mesh, Par_file, CMTSOLUTION and STATIONS
+    read and set up by the general path give the database of the block
+    configuration the GPU golden test runs (configs.waterlayered): same point count,
+    coupling, absorbing and free-surface faces, masses, source time function, and
+    the same fluid/solid side for every station."""
+    from specfem3d_gb300 import configs, hexmesh, meshgen
+    d = os.path.join(REF_EXAMPLES, "waterlayered_halfspace")
+    mesh = hexmesh.read_external_mesh(os.path.join(d, "MESH-default"))
+    assert mesh["elems"].shape == (40500, 8) and len(mesh["materials"]) == 3
+    par = hexmesh.read_par_file(os.path.join(d, "DATA", "Par_file"))
+    assert par["NSTEP"] == 4500 and par["DT"] == 0.005 and par["STACEY_ABSORBING_CONDITIONS"]
+    src = hexmesh.read_cmtsolution(os.path.join(d, "DATA", "CMTSOLUTION"))
+    src["stf"] = "heaviside"
+    st = hexmesh.read_stations(os.path.join(d, "DATA", "STATIONS"))
+    ref_cfg = configs.waterlayered(20)
+    assert [s[0] for s in st] == ref_cfg["station_names"]
+    cfg = dict(dt=par["DT"], nstep=20, stacey=True, sources=[src], receivers=[(x, y, z) for _, _, x, y, z in st])
+    assert np.allclose(cfg["receivers"], ref_cfg["receivers"])
+    a = hexmesh.build_database(mesh, cfg)
+    b = meshgen.build_database(ref_cfg)
+    for k in ("nglob", "num_coupling_ac_el_faces", "num_abs_boundary_faces", "num_free_surface_faces"):
+        assert a[k] == b[k], k
+    for k in ("rmass", "rmass_acoustic", "rmassx", "rmassy", "rmassz"):
+        assert abs(a[k].astype(np.float64).sum() / b[k].astype(np.float64).sum() - 1) < 1e-6, k
+    assert a["t0"] == b["t0"] == 6.0 and np.allclose(a["stf"], b["stf"])
+    fa, fb = a["ispec_is_acoustic"].astype(bool), b["ispec_is_acoustic"].astype(bool)
+    assert fa.sum() == fb.sum() == 2025
+    assert np.array_equal(fa[a["ispec_selected_rec"] - 1], fb[b["ispec_selected_rec"] - 1])
+    assert fa[a["ispec_selected_source"][0] - 1]
