@@ -146,6 +146,23 @@ def refex_no_absorbing(nstep: int = 5000) -> dict:
     return cfg
 
 
+def attenuation_benchmark(nstep: int = 1300) -> dict:
+    """The reference benchmark EXAMPLES/benchmarks/attenuation/viscoelastic: an
+    80 x 80 x 80 regular mesh of 37.5 m cubes spanning [-1500, 1500]^3 m
+    (Mesh_Par_file, interfaces.dat), rho 2000, vp 3297.849, vs 2222.536,
+    Q_kappa 10, Q_mu 20 with N_SLS = 3 around f0_REFERENCE 18 Hz; free surfaces,
+    no Stacey; a vertical unit point force with an 18 Hz Ricker at (10, 10, 10)
+    and one station at (510, 510, 510) (USE_SOURCES_RECEIVERS_Z); dt 5e-4."""
+    lev = [float(v) for v in np.linspace(-1500.0, 1500.0, 81)]
+    cfg = dict(nx=80, ny=80, x0=-1500.0, x1=1500.0, y0=-1500.0, y1=1500.0, zlev=lev,
+               elem_layer=np.zeros(80 ** 3, np.int32),
+               layers=[dict(rho=2000.0, vp=3297.849, vs=2222.536, Qkappa=10.0, Qmu=20.0)],
+               dt=0.0005, nstep=nstep, stacey=False, absorbing=[], attenuation=True,
+               sources=[dict(type="force", x=10.0, y=10.0, z=10.0, F=[0.0, 0.0, 1.0], stf="ricker", f0=18.0)],
+               receivers=[(510.0, 510.0, 510.0)], station_names=["CE.1"])
+    return finish(cfg)
+
+
 # the 22 stations of EXAMPLES/applications/waterlayered_halfspace/DATA/STATIONS:
 # (name, x = longitude column, y = latitude column, burial)
 WATERLAYERED_STATIONS = [

@@ -53,6 +53,18 @@ def read_waterlayered(root):
     return out
 
 
+def read_attenuation_benchmark(root):
+    """EXAMPLES/benchmarks/attenuation/viscoelastic REF_SEIS: station CE.1,
+    displacement FXX, FXY, FXZ."""
+    d = os.path.join(root, "EXAMPLES/benchmarks/attenuation/viscoelastic/REF_SEIS")
+    comps, t = [], None
+    for c in "XYZ":
+        a = np.loadtxt(os.path.join(d, f"CE.1.FX{c}.semd"))
+        t = a[:, 0]
+        comps.append(a[:, 1])
+    return dict(displ=np.asarray([comps], np.float32), t=np.asarray(t, np.float64), stations=np.array(["CE.1"]))
+
+
 def main():
     root = sys.argv[1] if len(sys.argv) > 1 else "/root/reference"
     out = os.path.dirname(os.path.abspath(__file__))
@@ -61,6 +73,7 @@ def main():
     nd, t2 = read(root, "homogeneous_halfspace_HEX8_elastic_no_absorbing", "semd")
     np.savez_compressed(os.path.join(out, "refex_no_absorbing.npz"), displ=nd, t=t2, stations=np.array(STATIONS))
     np.savez_compressed(os.path.join(out, "waterlayered.npz"), **read_waterlayered(root))
+    np.savez_compressed(os.path.join(out, "attenuation_benchmark.npz"), **read_attenuation_benchmark(root))
 
 
 if __name__ == "__main__":

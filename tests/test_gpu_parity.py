@@ -219,6 +219,32 @@ def test_reference_golden_seismograms_on_gpu(gpulib, example):
         assert e < 2e-4
 
 
+def test_attenuation_benchmark_golden_seismograms(gpulib):
+    """The reference's viscoelastic attenuation benchmark (80^3 regular elements,
+    Q_kappa 10, Q_mu 20, N_SLS = 3, 1300 steps) against its REF_SEIS displacement:
+    relative L2 <= 1e-3 and correlation >= 0.99999 per component with signal
+    (the horizontal components of a vertical force on the diagonal are equal).
+    The same run without attenuation differs from REF_SEIS by far more, so the
+    match pins the memory-variable path itself."""
+    from specfem3d_gb300 import configs, meshgen
+    ref = np.load(os.path.join(ROOT, "tests", "golden", "attenuation_benchmark.npz"))["displ"]
+    out = {}
+    for att in (True, False):
+        cfg = configs.attenuation_benchmark(1300)
+        cfg["attenuation"] = att
+        db = meshgen.build_database(cfg)
+        g = _solver(db, cfg)
+        g.run(cfg["nstep"], steps_per_graph=100)
+        out[att] = g.seismograms()
+        g.close()
+    for c in range(3):
+        e, e0 = rel_l2(out[True][0, c], ref[0, c]), rel_l2(out[False][0, c], ref[0, c])
+        cc = np.corrcoef(out[True][0, c], ref[0, c])[0, 1]
+        print(f"attenuation benchmark component {'XYZ'[c]}: rel L2 {e:.2e} (elastic run {e0:.2e}), corr {cc:.7f}")
+        assert e < 1e-3 and cc > 0.99999
+        assert e0 > 20 * e
+
+
 def test_stability_check_and_errors(gpulib):
     from specfem3d_gb300 import abi, configs, meshgen
     cfg = configs.small_layered(nstep=4, attenuation=False)
