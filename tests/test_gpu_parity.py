@@ -222,8 +222,8 @@ def test_reference_golden_seismograms_on_gpu(gpulib, example):
 def test_attenuation_benchmark_golden_seismograms(gpulib):
     """The reference's viscoelastic attenuation benchmark (80^3 regular elements,
     Q_kappa 10, Q_mu 20, N_SLS = 3, 1300 steps) against its REF_SEIS displacement:
-    relative L2 <= 1e-3 and correlation >= 0.99999 per component with signal
-    (the horizontal components of a vertical force on the diagonal are equal).
+    relative L2 <= 1e-5 per component (measured 1.0e-6: FP32 rounding level),
+    correlation >= 0.99999.
     The same run without attenuation differs from REF_SEIS by far more, so the
     match pins the memory-variable path itself."""
     from specfem3d_gb300 import configs, meshgen
@@ -241,8 +241,8 @@ def test_attenuation_benchmark_golden_seismograms(gpulib):
         e, e0 = rel_l2(out[True][0, c], ref[0, c]), rel_l2(out[False][0, c], ref[0, c])
         cc = np.corrcoef(out[True][0, c], ref[0, c])[0, 1]
         print(f"attenuation benchmark component {'XYZ'[c]}: rel L2 {e:.2e} (elastic run {e0:.2e}), corr {cc:.7f}")
-        assert e < 1e-3 and cc > 0.99999
-        assert e0 > 20 * e
+        assert e < 1e-5 and cc > 0.99999
+        assert e0 > 1e3 * e
 
 
 def test_stability_check_and_errors(gpulib):
