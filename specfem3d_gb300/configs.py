@@ -163,6 +163,27 @@ def attenuation_benchmark(nstep: int = 1300) -> dict:
     return finish(cfg)
 
 
+def analytic_elastic(nstep: int = 14000) -> dict:
+    """The reference benchmark EXAMPLES/benchmarks/analytic_examples/analytic_solution_elastic:
+    16 x 16 x 16 regular elements of 2 km spanning [-16, 16]^3 km, rho 2300,
+    vp 2800, vs 1500; Stacey on all six faces (STACEY_INSTEAD_OF_FREE_SURFACE);
+    the CMTSOLUTION double couple Mrp = 1e23 dyne.cm (Heaviside, half duration
+    2 s) at the origin (USE_SOURCES_RECEIVERS_Z), a vertex of 8 elements, which
+    its REF_SEIS run placed at local (1, 1, 1) of its element 512, the element on
+    the -x, -y, -z side; six stations; dt 1e-3."""
+    s = 1e-7
+    M = [0.0, 0.0, 0.0, 0.0, 1e23 * s, 0.0]          # Mxz = Mrp
+    lev = [float(v) for v in np.linspace(-16000.0, 16000.0, 17)]
+    stations = [("Z1", 3000.0, 1000.0, 4000.0), ("Z2", 1000.0, 3000.0, 4000.0), ("Z3", 6000.0, 1000.0, 4000.0),
+                ("Z4", 1000.0, 6000.0, 4000.0), ("Z5", 6000.0, 1000.0, 2000.0), ("Z6", 1000.0, 6000.0, 2000.0)]
+    cfg = dict(nx=16, ny=16, x0=-16000.0, x1=16000.0, y0=-16000.0, y1=16000.0, zlev=lev,
+               elem_layer=np.zeros(16 ** 3, np.int32), layers=[dict(rho=2300.0, vp=2800.0, vs=1500.0)],
+               dt=0.001, nstep=nstep, stacey=True, absorbing=["xmin", "xmax", "ymin", "ymax", "bottom", "top"],
+               sources=[dict(type="cmt", x=0.0, y=0.0, z=0.0, M=M, stf="heaviside", hdur=2.0, octant=(-1, -1, -1))],
+               receivers=[(x, y, z) for _, x, y, z in stations], station_names=[n for n, _, _, _ in stations])
+    return finish(cfg)
+
+
 # the 22 stations of EXAMPLES/applications/waterlayered_halfspace/DATA/STATIONS:
 # (name, x = longitude column, y = latitude column, burial)
 WATERLAYERED_STATIONS = [

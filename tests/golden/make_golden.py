@@ -65,6 +65,28 @@ def read_attenuation_benchmark(root):
     return dict(displ=np.asarray([comps], np.float32), t=np.asarray(t, np.float64), stations=np.array(["CE.1"]))
 
 
+def read_analytic_elastic(root):
+    """EXAMPLES/benchmarks/analytic_examples/analytic_solution_elastic: REF_SEIS
+    (the reference's run) and REF_ANALYTIC (Aki & Richards 4.32-4.33) for
+    stations Z1..Z6, displacement FXX, FXY, FXZ; every 10th of the 14000
+    samples (the signal has a 2 s half duration; dt is 1 ms) to keep the
+    fixture small."""
+    base = os.path.join(root, "EXAMPLES/benchmarks/analytic_examples/analytic_solution_elastic")
+    out = {}
+    for sub, key in (("REF_SEIS", "displ"), ("REF_ANALYTIC", "analytic")):
+        tr, t = [], None
+        for n in ["Z1", "Z2", "Z3", "Z4", "Z5", "Z6"]:
+            comps = []
+            for c in "XYZ":
+                a = np.loadtxt(os.path.join(base, sub, f"DB.{n}.FX{c}.semd"))
+                t = a[::10, 0]
+                comps.append(a[::10, 1])
+            tr.append(comps)
+        out[key] = np.asarray(tr, np.float32)
+        out["t_" + key] = np.asarray(t, np.float64)
+    return out
+
+
 def main():
     root = sys.argv[1] if len(sys.argv) > 1 else "/root/reference"
     out = os.path.dirname(os.path.abspath(__file__))
@@ -74,6 +96,7 @@ def main():
     np.savez_compressed(os.path.join(out, "refex_no_absorbing.npz"), displ=nd, t=t2, stations=np.array(STATIONS))
     np.savez_compressed(os.path.join(out, "waterlayered.npz"), **read_waterlayered(root))
     np.savez_compressed(os.path.join(out, "attenuation_benchmark.npz"), **read_attenuation_benchmark(root))
+    np.savez_compressed(os.path.join(out, "analytic_elastic.npz"), **read_analytic_elastic(root))
 
 
 if __name__ == "__main__":
