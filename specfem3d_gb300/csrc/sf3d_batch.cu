@@ -469,6 +469,130 @@ __global__ void __launch_bounds__(NGLL3_PAD * GB, 4 / GB) batch_stiffness4_kerne
   }
 }
 
+// Meshes whose elements are all regular (cubes: xix = etay = gammaz = xix_regular,
+// no metric arrays): the float4 kernel without the metric path.  The stress of
+// a regular element is symmetric, so J sigma grad(xi) needs 6 shared rows, not 9,
+// and the transposed contraction runs one displacement component at a time (12
+// live accumulators instead of 36).  Fewer registers give more resident CTAs,
+// which is what this shared-memory-latency-bound kernel is short of.
+template <int EB, int MINB>
+__global__ void __launch_bounds__(NGLL3_PAD, MINB) batch_stiffness4_regular_kernel(const BatchStiffArgs a) {
+  __shared__ float s_gll[NGLL3];
+  __shared__ float4 B[6][NGLL3_PAD];   // displacement (rows 0-2), then sxx syy szz sxy sxz syz
+  const int p = threadIdx.x;
+  const long S = a.nshots;
+  const int ntiles = a.nshots / 4;
+  const int tile = blockIdx.x % ntiles;
+  const int egroup = blockIdx.x / ntiles;
+  const long shot0 = 4L * tile;
+  const bool active = p < NGLL3;
+  const int k = p / NGLL2, j = (p / NGLLX) % NGLLX, i = p % NGLLX;
+  if (p < NGLL3) s_gll[p] = __ldg(a.gll + p);
+  const float xr = a.xix_regular;
+  const float js = a.jacobian_regular * xr;
+  // row of sigma[d][c] in B
+  constexpr int sym[3][3] = {{0, 3, 4}, {3, 1, 5}, {4, 5, 2}};
+#pragma unroll 1
+  for (int eb = 0; eb < EB; ++eb) {
+    const int slot = egroup * EB + eb;
+    if (slot >= a.nelem) break;
+    const int e = a.phase ? __ldg(a.phase + slot) : slot;
+    const long eo = (long)e * NGLL3_PAD + p;
+    long g = 0;
+    float kap = 0.f, mu = 0.f;
+    if (active) {
+      g = __ldg(a.ibool + eo);
+      kap = __ldg(a.kappav + eo);
+      mu = __ldg(a.muv + eo);
+#pragma unroll
+      for (int c = 0; c < 3; ++c) B[c][p] = *reinterpret_cast<const float4*>(a.displ + (3 * g + c) * S + shot0);
+    }
+    __syncthreads();
+    float T[3][3][4];
+#pragma unroll
+    for (int c = 0; c < 3; ++c)
+#pragma unroll
+      for (int d = 0; d < 3; ++d)
+#pragma unroll
+        for (int w = 0; w < 4; ++w) T[c][d][w] = 0.f;
+    if (active) {
+#pragma unroll
+      for (int l = 0; l < NGLLX; ++l) {
+        const float h[3] = {s_gll[i + NGLLX * l], s_gll[j + NGLLX * l], s_gll[k + NGLLX * l]};
+        const int pp[3] = {l + NGLLX * j + NGLL2 * k, i + NGLLX * l + NGLL2 * k, i + NGLLX * j + NGLL2 * l};
+#pragma unroll
+        for (int c = 0; c < 3; ++c)
+#pragma unroll
+          for (int d = 0; d < 3; ++d) {
+            const float4 v = B[c][pp[d]];
+            T[c][d][0] = fmaf(v.x, h[d], T[c][d][0]);
+            T[c][d][1] = fmaf(v.y, h[d], T[c][d][1]);
+            T[c][d][2] = fmaf(v.z, h[d], T[c][d][2]);
+            T[c][d][3] = fmaf(v.w, h[d], T[c][d][3]);
+          }
+      }
+    }
+    __syncthreads();  // displacement reads done before the stress overwrites rows 0-2
+    if (active) {
+      const float l2m = kap + (4.f / 3.f) * mu;
+      const float lam = l2m - 2.f * mu;
+      float sg[6][4];
+#pragma unroll
+      for (int w = 0; w < 4; ++w) {
+        const float d00 = xr * T[0][0][w], d11 = xr * T[1][1][w], d22 = xr * T[2][2][w];
+        sg[0][w] = js * (l2m * d00 + lam * (d11 + d22));
+        sg[1][w] = js * (l2m * d11 + lam * (d00 + d22));
+        sg[2][w] = js * (l2m * d22 + lam * (d00 + d11));
+        sg[3][w] = js * (mu * (xr * T[0][1][w] + xr * T[1][0][w]));
+        sg[4][w] = js * (mu * (xr * T[2][0][w] + xr * T[0][2][w]));
+        sg[5][w] = js * (mu * (xr * T[2][1][w] + xr * T[1][2][w]));
+      }
+#pragma unroll
+      for (int q = 0; q < 6; ++q) B[q][p] = make_float4(sg[q][0], sg[q][1], sg[q][2], sg[q][3]);
+    }
+    __syncthreads();
+    if (active) {
+      const float* hpw = s_gll + NGLL2;
+      const float fac[3] = {s_gll[4 * NGLL2 + j + NGLLX * k], s_gll[3 * NGLL2 + i + NGLLX * k],
+                            s_gll[2 * NGLL2 + i + NGLLX * j]};
+#pragma unroll
+      for (int c = 0; c < 3; ++c) {
+        float N[3][4];
+#pragma unroll
+        for (int d = 0; d < 3; ++d)
+#pragma unroll
+          for (int w = 0; w < 4; ++w) N[d][w] = 0.f;
+#pragma unroll
+        for (int l = 0; l < NGLLX; ++l) {
+          const float f[3] = {hpw[l + NGLLX * i], hpw[l + NGLLX * j], hpw[l + NGLLX * k]};
+          const int pp[3] = {l + NGLLX * j + NGLL2 * k, i + NGLLX * l + NGLL2 * k, i + NGLLX * j + NGLL2 * l};
+#pragma unroll
+          for (int d = 0; d < 3; ++d) {
+            const float4 v = B[sym[d][c]][pp[d]];
+            N[d][0] = fmaf(v.x, f[d], N[d][0]);
+            N[d][1] = fmaf(v.y, f[d], N[d][1]);
+            N[d][2] = fmaf(v.z, f[d], N[d][2]);
+            N[d][3] = fmaf(v.w, f[d], N[d][3]);
+          }
+        }
+        float4 r;
+        r.x = -(fac[0] * N[0][0] + fac[1] * N[1][0] + fac[2] * N[2][0]);
+        r.y = -(fac[0] * N[0][1] + fac[1] * N[1][1] + fac[2] * N[2][1]);
+        r.z = -(fac[0] * N[0][2] + fac[1] * N[1][2] + fac[2] * N[2][2]);
+        r.w = -(fac[0] * N[0][3] + fac[1] * N[1][3] + fac[2] * N[2][3]);
+        atomicAdd(reinterpret_cast<float4*>(a.accel + (3 * g + c) * S + shot0), r);
+      }
+    }
+    __syncthreads();  // stress reads done before the next element's displacement
+  }
+}
+
+template <int EB>
+void launch_tile4_regular(const BatchStiffArgs& a, cudaStream_t s) {
+  const long nblocks = (long)((a.nelem + EB - 1) / EB) * (a.nshots / 4);
+  batch_stiffness4_regular_kernel<EB, 7><<<(unsigned)nblocks, NGLL3_PAD, 0, s>>>(a);
+}
+
 template <int GB, int EB>
 void launch_tile4(const BatchStiffArgs& a, cudaStream_t s) {
   const long nblocks = (long)((a.nelem + EB - 1) / EB) * (a.nshots / (4 * GB));
@@ -520,10 +644,19 @@ void launch_batch_stiffness(Mesh* mp, int iphase, cudaStream_t s) {
   a.displ = B->displ;
   a.accel = B->accel;
   if (B->shots_per_thread == 4) {
-    if (B->shots_per_block == 8)
+    if (B->shots_per_block == 8) {
       launch_gb4<2>(a, B->elements_per_block, s);
-    else
+    } else if (mp->nspec_irregular == 0) {
+      // every element regular: the metric-free float4 kernel
+      if (B->elements_per_block == 4)
+        launch_tile4_regular<4>(a, s);
+      else if (B->elements_per_block == 2)
+        launch_tile4_regular<2>(a, s);
+      else
+        launch_tile4_regular<1>(a, s);
+    } else {
       launch_gb4<1>(a, B->elements_per_block, s);
+    }
     return;
   }
   switch (B->shots_per_block) {
