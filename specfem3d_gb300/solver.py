@@ -51,6 +51,7 @@ class GPUSolver:
         self.record = tuple(cfg.get("record", record))
         self.isac = np.asarray(db.get("ispec_is_acoustic", np.zeros(self.nspec, np.int32)), np.int32)
         self.coupled = bool(self.isac.any())
+        self.absorb_record = None
         self._prepare_constants(db, save_forward)
         self._prepare_fields(db)
         if self.coupled:
@@ -211,7 +212,11 @@ class GPUSolver:
         L.compute_forces_viscoelastic_cuda_(self.mp, A.i(iphase), A.f(self.deltat), A.i(self.nspec_outer),
                                             A.i(self.nspec_elastic), A.i(self.strain), A.i(self.attenuation), one)
         if iphase == 1:
-            L.compute_stacey_viscoelastic_cuda_(self.mp, A.i(1), A.af(None), one)
+            # SAVE_FORWARD runs hand a (nstep, 3*25*nfaces) float32 array here to
+            # receive the boundary record; otherwise b_absorb_field is NULL
+            rec = self.absorb_record
+            buf = A.af(rec[it - 1]) if rec is not None else None
+            L.compute_stacey_viscoelastic_cuda_(self.mp, A.i(1), buf, one)
             if self.coupled:
                 L.compute_coupling_el_ac_cuda_(self.mp, A.i(1), A.i(self.ncoupling), one)
             if self.nsources:
