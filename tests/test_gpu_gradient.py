@@ -110,9 +110,10 @@ def test_gradient_matches_reference_style_kernels(problem):
     same shot: SIMULATION_TYPE = 3 through the reference's entry points (forward
     with SAVE_FORWARD and the Stacey record, then adjoint + time-reversed
     reconstruction + kernel accumulation; specfem3d_gb300.adjoint).  Both give
-    rho / mu / kappa kernel densities; they differ by the time discretisation of
-    the continuous adjoint, so the bar is agreement to a few percent (relative L2)
-    with correlation >= 0.999."""
+    rho / mu / kappa kernel densities.  With the reference's timing (adjoint sample
+    NSTEP - it + 1, backward field replaced after the first step) its accumulation
+    is the discrete adjoint of the Newmark step, so the two agree to FP32 rounding:
+    <= 1e-4 relative L2 (measured 1.7e-6 to 2.5e-6)."""
     from specfem3d_gb300 import adjoint as ADJ, gradient as G
     cfg, db = problem.cfg, problem.db
     c0 = G.shot_config(cfg, 0)
@@ -132,4 +133,4 @@ def test_gradient_matches_reference_style_kernels(problem):
         cc = np.corrcoef(ours[k].ravel(), ref[k].ravel())[0, 1]
         print(f"{k}: discrete adjoint vs SIMULATION_TYPE=3 kernels: rel L2 {e:.3e}, correlation {cc:.6f}")
         assert np.abs(ref[k]).max() > 0
-        assert e < 0.1 and cc > 0.99
+        assert e < 1e-4 and cc > 0.99999
