@@ -146,4 +146,8 @@ def setup(cfg: dict, db: dict) -> dict:
     al, be, ga = memory_values(tau_f, cfg["dt"])
     return dict(factor_common=np.ascontiguousarray(fcm), factor_common_kappa=np.ascontiguousarray(fck),
                 mustore=(db["mustore"] * smu).astype(f32), kappastore=(db["kappastore"] * skap).astype(f32),
+                # relaxed moduli and the unrelaxed scaling, as the databases keep
+                # them (mustore / kappastore, attenuation.bin scale_factor(_kappa))
+                mustore_relaxed=db["mustore"], kappastore_relaxed=db["kappastore"],
+                scale_factor=smu.astype(f32), scale_factor_kappa=skap.astype(f32),
                 alphaval=al, betaval=be, gammaval=ga, tau_sigma=tau_f, f_c_source=f_c, attenuation=1)

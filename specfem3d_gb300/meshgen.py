@@ -117,6 +117,13 @@ class Block:
         return x, y, z
 
 
+def element_coordinates(cfg: dict) -> np.ndarray:
+    """(nspec, 125, 3) coordinates of every element's GLL points of a block configuration."""
+    B = Block(cfg)
+    x, y, z = B.gll_coords(np.arange(B.nspec))
+    return np.stack([x, y, z], axis=-1)
+
+
 def _ibool_block(B: Block) -> np.ndarray:
     """First-appearance global numbering of the block's GLL points (1-based).
 
@@ -399,6 +406,7 @@ def _mass(cfg, B, db, dtype):
         ta = np.zeros_like(terms)
         ta[isac] = (jel[isac] * w3[None, :] / kap[isac]).astype(dtype)
         rma = np.bincount(ib.reshape(-1), weights=ta.reshape(-1), minlength=nglob).astype(dtype)
+        db["rmass_acoustic_volume"] = rma.copy()          # the database's rmass_acoustic
         if db["stacey"]:
             nf = db["num_abs_boundary_faces"]
             isp = db["abs_boundary_ispec"] - 1
@@ -408,8 +416,10 @@ def _mass(cfg, B, db, dtype):
             sel = isac[isp]
             sn = dtype(0.5 * float(cfg["dt"])) / db["rho_vp"][q[sel]]
             add = db["abs_boundary_jacobian2Dw"].reshape(nf, 25)[sel] * sn
-            rma = rma + np.bincount(db["ibool"][q[sel]].reshape(-1).astype(np.int64) - 1,
-                                    weights=add.astype(np.float64).reshape(-1), minlength=nglob).astype(dtype)
+            st = np.bincount(db["ibool"][q[sel]].reshape(-1).astype(np.int64) - 1,
+                             weights=add.astype(np.float64).reshape(-1), minlength=nglob).astype(dtype)
+            db["rmassz_acoustic"] = st                          # the database's Stacey term
+            rma = rma + st
         rma[rma <= 0] = 1
         db["rmass_acoustic"] = (dtype(1) / rma).astype(dtype)
     mx = rmass.copy(); my = rmass.copy(); mz = rmass.copy()
@@ -429,6 +439,9 @@ def _mass(cfg, B, db, dtype):
         for c, m in enumerate((mx, my, mz)):
             t = rvp * vn * n[..., c] + rvs * (dt2 - vn * n[..., c])
             add = np.bincount(g[el].reshape(-1), weights=(t * jw)[el].astype(np.float64).reshape(-1), minlength=nglob)
+            # the database keeps the Stacey terms apart (rmassx/y/z of
+            # save_arrays_solver.F90:228-231); the solver adds rmass before inverting
+            db["rmass" + "xyz"[c] + "_stacey"] = add.astype(dtype)
             m += add.astype(dtype)
     for m in (mx, my, mz):
         m[m <= 0] = 1
