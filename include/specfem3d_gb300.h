@@ -271,6 +271,22 @@ void compute_kernels_elastic_cuda_(long *Mesh_pointer, realw *deltat_f);
 void transfer_kernels_el_to_host_(long *Mesh_pointer, realw *h_rho_kl, realw *h_mu_kl,
                                   realw *h_kappa_kl, realw *h_cijkl_kl, int *NSPEC_AB);
 
+/* ---- Gaussian smoothing of kernels (xsmooth_sem GPU mode) ----------------
+ * Replace prepare_smooth_gpu / compute_smooth_gpu / get_smooth_gpu
+ * (src/gpu/smooth_cuda.cu:40-248).  *Container receives a handle; the
+ * coordinates are per element GLL point (5,5,5,nspec); sigma_h2 = 2 sigma_h^2,
+ * sigma_h3 = the horizontal search radius (smooth_sem.F90:524-559), nker <= 8.
+ * compute_smooth_gpu adds the contributions of one slice (call it for this
+ * slice and each neighbour); data_other is (5,5,5,nspec_other,nker).
+ * get_smooth_gpu normalises, copies (5,5,5,nspec_me,nker) back and releases
+ * the handle. */
+void prepare_smooth_gpu_(long *Container, realw *xstore_me, realw *ystore_me, realw *zstore_me,
+                         realw *sigma_h2, realw *sigma_v2, realw *sigma_h3, realw *sigma_v3, int *nspec_me,
+                         int *nker);
+void compute_smooth_gpu_(long *smooth_pointer, realw *data_other, realw *integ_factor, realw *xstore_other,
+                         realw *ystore_other, realw *zstore_other, const int *nspec_other_f);
+void get_smooth_gpu_(long *smooth_pointer, realw *data_smooth);
+
 /* FP64 sensitivity kernels (5,5,5,NSPEC) straight from the device accumulators
  * (no reference counterpart: the reference accumulates in single precision). */
 int sf3d_get_kernels_f64(long *Mesh_pointer, double *h_rho_kl, double *h_mu_kl, double *h_kappa_kl);

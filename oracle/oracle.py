@@ -807,3 +807,48 @@ def make_coupled_sim(db: dict, cfg: dict, precision: str = "f32", nthreads: int 
 
 def run_coupled(sim: OracleSim, nsteps: int) -> None:
     sim.L.orc_run_coupled(sim.h, int(nsteps))
+
+
+# ----------------------------------------------------------------------------
+# Gaussian smoothing of kernels (kernels/process_smooth.cu:30-194 and
+# normalize_data, smooth_sem.F90:524-559 for the constants)
+# ----------------------------------------------------------------------------
+
+def smooth_restated(xyz_me: np.ndarray, xyz_other: np.ndarray, data_other: np.ndarray, integ_other: np.ndarray,
+                    sigma_h2: float, sigma_v2: float, sigma_h3: float, sigma_v3: float) -> np.ndarray:
+    """Smoothed kernels (nker, nspec_me*125) in FP64 from per-element coordinates
+    xyz_me (nspec_me, 125, 3), xyz_other (nspec_other, 125, 3), kernel values
+    data_other (nker, nspec_other*125) and J w weights integ_other (nspec_other*125).
+    Element o of the other slice takes part for target element e when its centre
+    (mean of its first and last GLL point, single precision) lies within sigma_h3
+    horizontally and sigma_v3 vertically of GLL point (o mod 125) of e; each pair
+    of points weighs exp(-dh/sigma_h2 - dv/sigma_v2) (0 below exp(-86)) times J w."""
+    f32 = np.float32
+    xo = np.asarray(xyz_other, f32)
+    centre = ((xo[:, 0, :] + xo[:, NGLL3 - 1, :]) * f32(0.5)).astype(np.float64)
+    no = len(xo)
+    dat = np.asarray(data_other, np.float64).reshape(-1, no, NGLL3)
+    integ = np.asarray(integ_other, np.float64).reshape(no, NGLL3)
+    xo64 = xo.astype(np.float64)
+    hcrit, vcrit = float(f32(sigma_h3) * f32(sigma_h3)), float(f32(sigma_v3) * f32(sigma_v3))
+    h2inv, v2inv = 1.0 / float(f32(sigma_h2)), 1.0 / float(f32(sigma_v2))
+    me = np.asarray(xyz_me, f32).astype(np.float64)
+    out = np.zeros((dat.shape[0], len(me), NGLL3))
+    pidx = np.arange(no) % NGLL3
+    for e in range(len(me)):
+        p = me[e][pidx]                                     # the testing point of each candidate
+        dh = (p[:, 0] - centre[:, 0]) ** 2 + (p[:, 1] - centre[:, 1]) ** 2
+        dv = (p[:, 2] - centre[:, 2]) ** 2
+        inc = np.nonzero(~((dh > hcrit) | (dv > vcrit)))[0]
+        if not len(inc):
+            continue
+        q = xo64[inc].reshape(-1, 3)                        # (n_inc*125, 3)
+        ddh = (me[e][:, None, 0] - q[None, :, 0]) ** 2 + (me[e][:, None, 1] - q[None, :, 1]) ** 2
+        ddv = (me[e][:, None, 2] - q[None, :, 2]) ** 2
+        val = -ddh * h2inv - ddv * v2inv
+        g = np.where(val < -86.0, 0.0, np.exp(np.maximum(val, -86.0)))
+        coef = g * integ[inc].reshape(-1)[None, :]
+        norm = coef.sum(axis=1)
+        norm = np.where(norm < 1e-24, 1.0, norm)
+        out[:, e, :] = np.einsum("pq,kq->kp", coef, dat[:, inc, :].reshape(dat.shape[0], -1)) / norm[None, :]
+    return out.reshape(dat.shape[0], -1)
