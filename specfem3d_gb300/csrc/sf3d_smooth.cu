@@ -9,7 +9,8 @@
 // an element of the other slice takes part when its centre (the mean of its first
 // and last GLL points) lies within sigma_h3 horizontally and sigma_v3 vertically
 // of the target element's GLL point number (element index mod 125); exponents
-// below -86 give 0.  The reference scans every element of the other slice and
+// below -86 give 0.  The sums are kept in FP64 across elements (the reference
+// keeps them in FP32).  The reference scans every element of the other slice and
 // evaluates the weights once per kernel; here the other slice's elements are
 // binned on a uniform grid of cells (sigma_h3 x sigma_h3 x sigma_v3) so each
 // target element scans only the cells its search box touches, and the weights of
@@ -30,8 +31,8 @@ struct SmoothState {
   float* x_me = nullptr;
   float* y_me = nullptr;
   float* z_me = nullptr;
-  float* data_smooth = nullptr;     // (nker, 125 * nspec_me)
-  float* normalisation = nullptr;   // (125 * nspec_me)
+  double* data_smooth = nullptr;    // (nker, 125 * nspec_me)
+  double* normalisation = nullptr;  // (125 * nspec_me)
   float sigma_h2_inv = 0.f, sigma_v2_inv = 0.f;
   float h_criterion = 0.f, v_criterion = 0.f;   // sigma_h3^2, sigma_v3^2
   float sigma_h3 = 0.f, sigma_v3 = 0.f;
@@ -53,8 +54,8 @@ struct SmoothArgs {
   float ox, oy, oz, csh, csv;      // grid origin and cell sizes
   float sigma_h3, sigma_v3;
   float sigma_h2_inv, sigma_v2_inv, h_criterion, v_criterion;
-  float* data_smooth;
-  float* normalisation;
+  double* data_smooth;
+  double* normalisation;
 };
 
 __device__ __forceinline__ float block_reduce(float v, bool take_max, float* scratch) {
@@ -101,10 +102,12 @@ __global__ void __launch_bounds__(NGLL3_PAD) smooth_kernel(const SmoothArgs a) {
   const int cx0 = cell_lo(xmin - a.sigma_h3, a.ox, a.csh, a.ncx), cx1 = cell_lo(xmax + a.sigma_h3, a.ox, a.csh, a.ncx);
   const int cy0 = cell_lo(ymin - a.sigma_h3, a.oy, a.csh, a.ncy), cy1 = cell_lo(ymax + a.sigma_h3, a.oy, a.csh, a.ncy);
   const int cz0 = cell_lo(zmin - a.sigma_v3, a.oz, a.csv, a.ncz), cz1 = cell_lo(zmax + a.sigma_v3, a.oz, a.csv, a.ncz);
-  float acc[kMaxKernels];
+  // per element FP32 partial sums folded into FP64 totals: the totals gather
+  // thousands of terms, which in FP32 alone would lose ~1e-5
+  double acc[kMaxKernels];
 #pragma unroll
-  for (int k = 0; k < kMaxKernels; ++k) acc[k] = 0.f;
-  float norm = 0.f;
+  for (int k = 0; k < kMaxKernels; ++k) acc[k] = 0.0;
+  double norm = 0.0;
   const long no = (long)a.nspec_other * NGLL3;
   for (int cz = cz0; cz <= cz1; ++cz)
     for (int cy = cy0; cy <= cy1; ++cy)
@@ -150,16 +153,24 @@ __global__ void __launch_bounds__(NGLL3_PAD) smooth_kernel(const SmoothArgs a) {
             }
             __syncthreads();
             if (active) {
+              float pe[kMaxKernels];
+#pragma unroll
+              for (int k = 0; k < kMaxKernels; ++k) pe[k] = 0.f;
+              float ne = 0.f;
               for (int j = 0; j < NGLL3; ++j) {
                 const float dx = x - s_ox[j], dy = y - s_oy[j], dz = z - s_oz[j];
                 const float val = -(dx * dx + dy * dy) * a.sigma_h2_inv - dz * dz * a.sigma_v2_inv;
                 const float g = val < -86.0f ? 0.0f : expf(val);
                 const float coef = g * s_oi[j];
-                norm += coef;
+                ne += coef;
 #pragma unroll
                 for (int k = 0; k < kMaxKernels; ++k)
-                  if (k < a.nker) acc[k] = fmaf(s_dyn[k * NGLL3 + j], coef, acc[k]);
+                  if (k < a.nker) pe[k] = fmaf(s_dyn[k * NGLL3 + j], coef, pe[k]);
               }
+              norm += (double)ne;
+#pragma unroll
+              for (int k = 0; k < kMaxKernels; ++k)
+                if (k < a.nker) acc[k] += (double)pe[k];
             }
             __syncthreads();
           }
@@ -174,12 +185,13 @@ __global__ void __launch_bounds__(NGLL3_PAD) smooth_kernel(const SmoothArgs a) {
   }
 }
 
-__global__ void normalize_kernel(float* data, const float* norm, long n, int nker) {
+// normalize_data (process_smooth.cu): value / sum of weights, rounded to FP32
+__global__ void normalize_kernel(const double* data, const double* norm, float* out, long n, int nker) {
   const long i = (long)blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= n) return;
-  float w = norm[i];
-  if (w < 1.e-24f) w = 1.0f;
-  for (int k = 0; k < nker; ++k) data[k * n + i] /= w;
+  double w = norm[i];
+  if (w < 1.e-24) w = 1.0;
+  for (int k = 0; k < nker; ++k) out[k * n + i] = (float)(data[k * n + i] / w);
 }
 
 SmoothState* get_smooth(long* p) {
@@ -221,8 +233,8 @@ void prepare_smooth_gpu_(long* Container, realw* xstore_me, realw* ystore_me, re
   const size_t n = (size_t)NGLL3 * sp->nspec_me;
   bool ok = alloc_zero((void**)&sp->x_me, sizeof(float) * n) && alloc_zero((void**)&sp->y_me, sizeof(float) * n) &&
             alloc_zero((void**)&sp->z_me, sizeof(float) * n) &&
-            alloc_zero((void**)&sp->data_smooth, sizeof(float) * n * sp->nker) &&
-            alloc_zero((void**)&sp->normalisation, sizeof(float) * n);
+            alloc_zero((void**)&sp->data_smooth, sizeof(double) * n * sp->nker) &&
+            alloc_zero((void**)&sp->normalisation, sizeof(double) * n);
   ok = ok && cudaMemcpy(sp->x_me, xstore_me, sizeof(float) * n, cudaMemcpyHostToDevice) == cudaSuccess &&
        cudaMemcpy(sp->y_me, ystore_me, sizeof(float) * n, cudaMemcpyHostToDevice) == cudaSuccess &&
        cudaMemcpy(sp->z_me, zstore_me, sizeof(float) * n, cudaMemcpyHostToDevice) == cudaSuccess;
@@ -315,9 +327,15 @@ void get_smooth_gpu_(long* smooth_pointer, realw* data_smooth) {
   SmoothState* sp = get_smooth(smooth_pointer);
   if (!sp) return;
   const long n = (long)NGLL3 * sp->nspec_me;
-  normalize_kernel<<<(unsigned)((n + 255) / 256), 256>>>(sp->data_smooth, sp->normalisation, n, sp->nker);
-  if (cuda_ok(cudaGetLastError(), "normalize_kernel"))
-    SF3D_CUDA(cudaMemcpy(data_smooth, sp->data_smooth, sizeof(float) * n * sp->nker, cudaMemcpyDeviceToHost));
+  float* d_out = nullptr;
+  if (alloc_zero((void**)&d_out, sizeof(float) * n * sp->nker)) {
+    normalize_kernel<<<(unsigned)((n + 255) / 256), 256>>>(sp->data_smooth, sp->normalisation, d_out, n, sp->nker);
+    if (cuda_ok(cudaGetLastError(), "normalize_kernel"))
+      SF3D_CUDA(cudaMemcpy(data_smooth, d_out, sizeof(float) * n * sp->nker, cudaMemcpyDeviceToHost));
+    cudaFree(d_out);
+  } else {
+    set_error(SF3D_ERR_CUDA, "get_smooth_gpu: device allocation failed");
+  }
   cudaFree(sp->x_me); cudaFree(sp->y_me); cudaFree(sp->z_me); cudaFree(sp->data_smooth); cudaFree(sp->normalisation);
   delete sp;
   *smooth_pointer = 0;
