@@ -1,6 +1,6 @@
 """Gaussian smoothing of kernels on the device (prepare/compute/get_smooth_gpu)
-against the oracle's FP64 restatement of process_smooth: relative L2 <= 5e-6
-(FP32 weights and per-element partial sums, FP64 totals), on a layered block and
+against the oracle's FP64 restatement of process_smooth: relative L2 <= 1e-6
+(FP32 weights and per-element partial sums, FP64 totals; measured 2.3e-7), on a layered block and
 on a block with moved interior nodes; a constant field stays constant to 1e-6
 relative."""
 import numpy as np
@@ -41,6 +41,6 @@ def test_smoothing_vs_oracle(gpulib, which):
     e = rel_l2(got, ref)
     print(f"smoothing ({which}) vs FP64 restatement: {e:.2e}; roughness reduced "
           f"{np.std(np.diff(kern[0])) / np.std(np.diff(got[0])):.1f}x")
-    assert e < 5e-6
+    assert e < 1e-6
     const = S.smooth(db, xyz, np.full((1, n), 2.5, np.float32), sh, sv)
     assert np.abs(const - 2.5).max() < 2.5e-6
