@@ -525,6 +525,11 @@ def source_time_functions(cfg: dict, in_fluid=None) -> np.ndarray:
     return np.stack([stf_table(k, p, ts, t0, dt, nstep) for k, p, ts in zip(kinds, params, tsh)]), t0
 
 
+ANISO_NAMES = ["c11store", "c12store", "c13store", "c14store", "c15store", "c16store", "c22store", "c23store",
+               "c24store", "c25store", "c26store", "c33store", "c34store", "c35store", "c36store", "c44store",
+               "c45store", "c46store", "c55store", "c56store", "c66store"]
+
+
 def make_sim(db: dict, cfg: dict, precision: str = "f32", nthreads: int = 1) -> OracleSim:
     """Oracle forward simulation set up from database arrays (either the ones
     from :func:`build_database` or the product's generator, same names)."""
@@ -545,6 +550,8 @@ def make_sim(db: dict, cfg: dict, precision: str = "f32", nthreads: int = 1) -> 
         s.set(n, np.asarray(db[n], rd))
     for n in ["hxir", "hetar", "hgammar"]:
         s.set(n, np.asarray(db[n], np.float64))
+    if int(db.get("anisotropy", 0)):
+        s.set("cstore", np.ascontiguousarray(np.stack([np.asarray(db[n], rd) for n in ANISO_NAMES], axis=1)))
     s.setr("xix_regular", db["xix_regular"])
     s.setr("jacobian_regular", db["jacobian_regular"])
     s.seti("num_abs_boundary_faces", int(db["num_abs_boundary_faces"]) if db.get("stacey", 1) else 0)

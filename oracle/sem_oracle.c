@@ -40,7 +40,7 @@ static const orc_field k_ptr_fields[] = {
   F(source_adjoint), F(hxir_adj), F(hetar_adj), F(hgammar_adj), F(elastic_list), F(acoustic_list),
   F(ispec_is_acoustic), F(potential), F(potential_dot), F(potential_dot_dot), F(rmass_acoustic),
   F(coupling_ispec), F(coupling_ijk), F(coupling_normal), F(coupling_jacobian2Dw), F(free_surface_ispec),
-  F(free_surface_ijk), F(rec_is_acoustic),
+  F(free_surface_ijk), F(rec_is_acoustic), F(cstore),
 };
 static const orc_field k_int_fields[] = {
   F(nspec), F(nglob), F(nspec_irregular), F(nsources), F(nrec), F(nstep), F(it),
@@ -874,6 +874,19 @@ static void element_forces(const orc_sim *s, int ispec, const realw *displ, cons
     realw syy = l2m * duydyl + lambdal * (duxdxl + duzdzl);
     realw szz = l2m * duzdzl + lambdal * (duxdxl + duydyl);
     realw sxy = mul * dxy_yx, sxz = mul * dzx_xz, syz = mul * dzy_yz;
+    if (s->cstore) {
+      /* ANISOTROPY (compute_forces_viscoelastic.F90:578-611): c11..c66 at cstore[21 q + n] */
+      const realw *c = s->cstore + 21 * q;
+      realw c11 = c[0], c12 = c[1], c13 = c[2], c14 = c[3], c15 = c[4], c16 = c[5], c22 = c[6], c23 = c[7];
+      realw c24 = c[8], c25 = c[9], c26 = c[10], c33 = c[11], c34 = c[12], c35 = c[13], c36 = c[14], c44 = c[15];
+      realw c45 = c[16], c46 = c[17], c55 = c[18], c56 = c[19], c66 = c[20];
+      sxx = c11 * duxdxl + c16 * dxy_yx + c12 * duydyl + c15 * dzx_xz + c14 * dzy_yz + c13 * duzdzl;
+      syy = c12 * duxdxl + c26 * dxy_yx + c22 * duydyl + c25 * dzx_xz + c24 * dzy_yz + c23 * duzdzl;
+      szz = c13 * duxdxl + c36 * dxy_yx + c23 * duydyl + c35 * dzx_xz + c34 * dzy_yz + c33 * duzdzl;
+      sxy = c16 * duxdxl + c66 * dxy_yx + c26 * duydyl + c56 * dzx_xz + c46 * dzy_yz + c36 * duzdzl;
+      sxz = c15 * duxdxl + c56 * dxy_yx + c25 * duydyl + c55 * dzx_xz + c45 * dzy_yz + c35 * duzdzl;
+      syz = c14 * duxdxl + c46 * dxy_yx + c24 * duydyl + c45 * dzx_xz + c44 * dzy_yz + c34 * duzdzl;
+    }
     if (att) {
       realw Rxx = 0, Ryy = 0, Rtr = 0, Rxy = 0, Rxz = 0, Ryz = 0;
       for (int sl = 0; sl < N_SLS; ++sl) {

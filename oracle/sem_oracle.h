@@ -94,6 +94,7 @@ typedef struct orc_sim {
   int num_free_surface_faces, *free_surface_ispec, *free_surface_ijk;
   int *rec_is_acoustic;                /* (nrec) records pressure when 1 */
   int fluid_vector;                    /* 1: fluid receivers record (1/rho) grad of the potential */
+  realw *cstore;                       /* ANISOTROPY: (21, 125*nspec) c11..c66 per point, or NULL */
 } orc_sim;
 
 #endif

@@ -734,6 +734,10 @@ int sf3d_batch_prepare(long* Mesh_pointer, int nshots, const int* ispec_selected
                        const realw* sourcearrays, const double* stf, int nstep, int nlength, double* device_bytes) {
   Mesh* mp = get_mesh(Mesh_pointer);
   if (!mp) return SF3D_ERR_STATE;
+  if (mp->anisotropy) {
+    set_error(SF3D_ERR_ARG, "sf3d_batch_prepare: the batched kernels are isotropic");
+    return SF3D_ERR_ARG;
+  }
   if (!mp->f.displ || mp->num_phase_ispec <= 0) {
     set_error(SF3D_ERR_STATE, "sf3d_batch_prepare: prepare_fields_elastic_device not called");
     return SF3D_ERR_STATE;

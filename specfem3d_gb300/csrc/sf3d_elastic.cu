@@ -56,7 +56,7 @@ __device__ __forceinline__ void st_state(float* p, float v) {
 }
 
 template <bool ATT, bool STRAIN, int MINB, bool HALF = false, bool STAGE = false, bool ATOMIC = true,
-          bool STREAM = false>
+          bool STREAM = false, bool ANISO = false>
 __global__ void __launch_bounds__(NGLL3_PAD, MINB) stiffness_kernel(const StiffnessArgs a) {
   __shared__ __align__(16) float s_att[(ATT && STAGE) ? 30 : 1][NGLL3_PAD];
   __shared__ float s_gll[NGLL3];
@@ -235,14 +235,34 @@ __global__ void __launch_bounds__(NGLL3_PAD, MINB) stiffness_kernel(const Stiffn
       epsl[4] = 0.5f * (szy + syz);
       if (a.eps_trace_over_3) a.eps_trace_over_3[eo] = templ;
     }
-    const float l2m = kap + (4.f / 3.f) * mu;
-    const float lam = l2m - 2.f * mu;
-    float sig_xx = l2m * dxx + lam * (dyy + dzz);
-    float sig_yy = l2m * dyy + lam * (dxx + dzz);
-    float sig_zz = l2m * dzz + lam * (dxx + dyy);
-    float sig_xy = mu * (dxy + dyx);
-    float sig_xz = mu * (dzx + dxz);
-    float sig_yz = mu * (dzy + dyz);
+    float sig_xx, sig_yy, sig_zz, sig_xy, sig_xz, sig_yz;
+    if (ANISO) {
+      // sigma = C eps in the reference's Voigt arrangement
+      // (compute_forces_viscoelastic.F90:578-611); the memory variables below
+      // still take mu and kappa, as the reference does
+      float c[21];
+#pragma unroll
+      for (int q = 0; q < 21; ++q) c[q] = ld_elem<STREAM>(a.c[q] + eo);
+      const float c11 = c[0], c12 = c[1], c13 = c[2], c14 = c[3], c15 = c[4], c16 = c[5], c22 = c[6];
+      const float c23 = c[7], c24 = c[8], c25 = c[9], c26 = c[10], c33 = c[11], c34 = c[12], c35 = c[13];
+      const float c36 = c[14], c44 = c[15], c45 = c[16], c46 = c[17], c55 = c[18], c56 = c[19], c66 = c[20];
+      const float exy = dxy + dyx, exz = dzx + dxz, eyz = dzy + dyz;
+      sig_xx = c11 * dxx + c16 * exy + c12 * dyy + c15 * exz + c14 * eyz + c13 * dzz;
+      sig_yy = c12 * dxx + c26 * exy + c22 * dyy + c25 * exz + c24 * eyz + c23 * dzz;
+      sig_zz = c13 * dxx + c36 * exy + c23 * dyy + c35 * exz + c34 * eyz + c33 * dzz;
+      sig_xy = c16 * dxx + c66 * exy + c26 * dyy + c56 * exz + c46 * eyz + c36 * dzz;
+      sig_xz = c15 * dxx + c56 * exy + c25 * dyy + c55 * exz + c45 * eyz + c35 * dzz;
+      sig_yz = c14 * dxx + c46 * exy + c24 * dyy + c45 * exz + c44 * eyz + c34 * dzz;
+    } else {
+      const float l2m = kap + (4.f / 3.f) * mu;
+      const float lam = l2m - 2.f * mu;
+      sig_xx = l2m * dxx + lam * (dyy + dzz);
+      sig_yy = l2m * dyy + lam * (dxx + dzz);
+      sig_zz = l2m * dzz + lam * (dxx + dyy);
+      sig_xy = mu * (dxy + dyx);
+      sig_xz = mu * (dzx + dxz);
+      sig_yz = mu * (dzy + dyz);
+    }
     if (ATT && STAGE) asm volatile("cp.async.wait_all;" ::: "memory");
     if (ATT) {
       float sR[6];
@@ -388,6 +408,17 @@ void launch_stiffness(const StiffnessArgs& a, bool att, bool store_strain, cudaS
     case 7: launch_minb<7, false>(a, att, store_strain, s); break;
     default: launch_minb<4, false>(a, att, store_strain, s); break;
   }
+}
+
+void launch_stiffness_aniso(const StiffnessArgs& a, bool att, bool store_strain, cudaStream_t s) {
+  if (a.nelem <= 0) return;
+  dim3 grid(a.nelem), block(NGLL3_PAD);
+  if (att)
+    stiffness_kernel<true, true, 4, false, false, true, false, true><<<grid, block, 0, s>>>(a);
+  else if (store_strain)
+    stiffness_kernel<false, true, 4, false, false, true, false, true><<<grid, block, 0, s>>>(a);
+  else
+    stiffness_kernel<false, false, 4, false, false, true, false, true><<<grid, block, 0, s>>>(a);
 }
 
 void launch_stiffness_colored(const StiffnessArgs& a, bool att, bool store_strain, cudaStream_t s) {

@@ -75,6 +75,10 @@ int sf3d_set_geometry_precision(long* Mesh_pointer, int bits) {
     set_error(SF3D_ERR_ARG, "sf3d_set_geometry_precision: bits must be 16 or 32");
     return SF3D_ERR_ARG;
   }
+  if (bits == 16 && mp->anisotropy) {
+    set_error(SF3D_ERR_ARG, "sf3d_set_geometry_precision: 16-bit storage is for isotropic moduli");
+    return SF3D_ERR_ARG;
+  }
   if (!mp->d_kappav || !mp->d_muv) {
     set_error(SF3D_ERR_STATE, "sf3d_set_geometry_precision: prepare_fields_elastic_device not called");
     return SF3D_ERR_STATE;

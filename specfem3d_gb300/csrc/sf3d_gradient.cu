@@ -463,6 +463,10 @@ int sf3d_gradient_setup(long* Mesh_pointer, int nstep, int checkpoint_every, dou
   Mesh* mp = get_mesh(Mesh_pointer);
   if (!mp) return SF3D_ERR_STATE;
   if (!mp->f.displ) { set_error(SF3D_ERR_STATE, "prepare_fields_elastic_device not called"); return SF3D_ERR_STATE; }
+  if (mp->anisotropy) {
+    set_error(SF3D_ERR_ARG, "sf3d_gradient: the gradient is for isotropic rho, kappa, mu");
+    return SF3D_ERR_ARG;
+  }
   if (mp->attenuation) {
     set_error(SF3D_ERR_ARG, "sf3d_gradient: attenuation is not supported (elastic misfit gradient only)");
     return SF3D_ERR_ARG;

@@ -106,6 +106,8 @@ struct Mesh {
   float* d_muv = nullptr;                // [nspec][128]
   float* d_rho_vp = nullptr;             // [nspec][128]
   float* d_rho_vs = nullptr;             // [nspec][128]
+  int anisotropy = 0;
+  float* d_cstore[21] = {};              // ANISOTROPY c11..c66, each [nspec][128]
   float* d_rmassx = nullptr;             // [nglob]
   float* d_rmassy = nullptr;
   float* d_rmassz = nullptr;
@@ -303,6 +305,9 @@ struct StiffnessArgs {
   const float2* muso;
   int nirr;                     // rows of each 16-bit metric array
   int nonatomic;                // 1: the elements of this launch share no point (one colour)
+  // ANISOTROPY: c11 c12 c13 c14 c15 c16 c22 c23 c24 c25 c26 c33 c34 c35 c36 c44
+  // c45 c46 c55 c56 c66, each [nspec][128]; nullptr for isotropic meshes
+  const float* c[21];
 };
 
 void launch_stiffness(const StiffnessArgs& a, bool att, bool store_strain, cudaStream_t s, int blocks_per_sm,
@@ -342,6 +347,7 @@ bool check_kernel_error(Mesh* mp);
 // dispatch on Mesh::stiffness_variant
 void launch_stiffness_colored(const StiffnessArgs& a, bool att, bool store_strain, cudaStream_t s);
 inline void run_stiffness(Mesh* mp, const StiffnessArgs& a, bool att, bool store_strain, cudaStream_t s);
+void launch_stiffness_aniso(const StiffnessArgs& a, bool att, bool store_strain, cudaStream_t s);
 // iphase's elements colour by colour with plain read-modify-write assembly
 inline bool run_stiffness_by_color(Mesh* mp, const StiffnessArgs& a, int iphase, bool att, bool store_strain,
                                    cudaStream_t s) {
@@ -359,6 +365,12 @@ inline bool run_stiffness_by_color(Mesh* mp, const StiffnessArgs& a, int iphase,
   return true;
 }
 inline void run_stiffness(Mesh* mp, const StiffnessArgs& a, bool att, bool store_strain, cudaStream_t s) {
+  if (a.c[0]) {
+    // anisotropic stress: its own build of the one-CTA-per-element kernel
+    // (atomic assembly, which is correct with or without a colouring)
+    launch_stiffness_aniso(a, att, store_strain, s);
+    return;
+  }
   if (mp->use_mesh_coloring && !mp->geom_half && a.phase && mp->d_phase_ispec) {
     const int iphase = a.phase == mp->d_phase_ispec ? 1 : 2;
     if (run_stiffness_by_color(mp, a, iphase, att, store_strain, s)) return;

@@ -434,13 +434,8 @@ void prepare_fields_elastic_device_(long* Mesh_pointer, realw* rmassx, realw* rm
                                     realw* c56store, realw* c66store) {
   (void)b_absorb_field; (void)b_reclen_field; (void)R_size; (void)rmass_ocean_load; (void)free_surface_normal;
   (void)free_surface_ispec; (void)free_surface_ijk; (void)num_free_surface_faces; (void)ACOUSTIC_SIMULATION;
-  (void)c11store; (void)c12store; (void)c13store; (void)c14store; (void)c15store; (void)c16store;
-  (void)c22store; (void)c23store; (void)c24store; (void)c25store; (void)c26store; (void)c33store;
-  (void)c34store; (void)c35store; (void)c36store; (void)c44store; (void)c45store; (void)c46store;
-  (void)c55store; (void)c56store; (void)c66store;
   Mesh* mp = get_mesh(Mesh_pointer);
   if (!mp) return;
-  if (ANISOTROPY && *ANISOTROPY) { set_error(SF3D_ERR_ARG, "anisotropic stiffness is not supported"); return; }
   if (APPROXIMATE_OCEAN_LOAD && *APPROXIMATE_OCEAN_LOAD) { set_error(SF3D_ERR_ARG, "ocean load is not supported"); return; }
   if (NOISE_TOMOGRAPHY && *NOISE_TOMOGRAPHY) { set_error(SF3D_ERR_ARG, "noise tomography is not supported"); return; }
   const long nspec = mp->nspec, nglob = mp->nglob;
@@ -455,6 +450,17 @@ void prepare_fields_elastic_device_(long* Mesh_pointer, realw* rmassx, realw* rm
   if (mp->d_kappav) { cudaFree(mp->d_kappav); mp->d_kappav = nullptr; }
   ok = ok && upload_padded(&mp->d_kappav, h_kappav, nspec, s);
   ok = ok && upload_padded(&mp->d_muv, h_muv, nspec, s);
+  mp->anisotropy = (ANISOTROPY && *ANISOTROPY) ? 1 : 0;
+  if (ok && mp->anisotropy) {
+    // c11..c66 (5,5,5,NSPEC) each, padded to 128 per element like kappav
+    realw* hc[21] = {c11store, c12store, c13store, c14store, c15store, c16store, c22store,
+                     c23store, c24store, c25store, c26store, c33store, c34store, c35store,
+                     c36store, c44store, c45store, c46store, c55store, c56store, c66store};
+    for (int q = 0; q < 21 && ok; ++q) {
+      if (!hc[q]) ok = set_error(SF3D_ERR_ARG, "ANISOTROPY needs all 21 c_ij arrays");
+      else ok = upload_padded(&mp->d_cstore[q], hc[q], nspec, s);
+    }
+  }
   if (mp->stacey && mp->num_abs_faces > 0) {
     ok = ok && upload_padded(&mp->d_rho_vp, rho_vp, nspec, s);
     ok = ok && upload_padded(&mp->d_rho_vs, rho_vs, nspec, s);
@@ -532,6 +538,7 @@ void prepare_cleanup_device_(long* Mesh_pointer, int* ACOUSTIC_SIMULATION, int* 
   cudaFree(mp->d_abs_ispec); cudaFree(mp->d_abs_pt); cudaFree(mp->d_abs_normal); cudaFree(mp->d_abs_jw);
   cudaFree(mp->d_sourcearrays); cudaFree(mp->d_ispec_src); cudaFree(mp->d_stf_step); cudaFree(mp->d_stf_table);
   cudaFree(mp->d_ispec_rec); cudaFree(mp->d_hxir); cudaFree(mp->d_hetar); cudaFree(mp->d_hgammar);
+  for (int q = 0; q < 21; ++q) cudaFree(mp->d_cstore[q]);
   cudaFree(mp->d_nu_rec); cudaFree(mp->d_seismo_d); cudaFree(mp->d_seismo_v); cudaFree(mp->d_seismo_a);
   cudaFree(mp->d_factor_common); cudaFree(mp->d_factor_common_kappa);
   free_fields(mp->f);

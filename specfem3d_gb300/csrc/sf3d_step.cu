@@ -327,6 +327,8 @@ StiffnessArgs stiffness_args(Mesh* mp, Fields& F, int iphase, float deltat, bool
     a.beta[s] = backward ? mp->b_betaval[s] : mp->betaval[s];
     a.gamma[s] = backward ? mp->b_gammaval[s] : mp->gammaval[s];
   }
+  if (mp->anisotropy)
+    for (int q = 0; q < 21; ++q) a.c[q] = mp->d_cstore[q];
   (void)att; (void)strain;
   return a;
 }

@@ -74,3 +74,72 @@ def perturbed_material(cfg: dict, corr_len: float = 1000.0, seed: int = 7):
     vp = np.where(solid, vp * (1 + pert), vp)
     vs = np.where(solid, vs * (1 + pert), vs)
     return rho.astype(np.float32), vp.astype(np.float32), vs.astype(np.float32)
+
+
+# ----------------------------------------------------------------------------- anisotropy
+_VOIGT = [(0, 0), (1, 1), (2, 2), (1, 2), (0, 2), (0, 1)]      # 1..6 = xx yy zz yz xz xy
+ANISO_NAMES = ["c11store", "c12store", "c13store", "c14store", "c15store", "c16store", "c22store", "c23store",
+               "c24store", "c25store", "c26store", "c33store", "c34store", "c35store", "c36store", "c44store",
+               "c45store", "c46store", "c55store", "c56store", "c66store"]
+_UPPER = [(a, b) for a in range(6) for b in range(a, 6)]       # c11 c12 .. c16 c22 .. c66
+
+
+def tilted_ti(rho, vp, vs, eps: float = 0.05, gamma: float = 0.04, delta: float = 0.02,
+              tilt_deg: float = 30.0, azimuth_deg: float = 20.0) -> np.ndarray:
+    """(n, 6, 6) Voigt stiffness of a tilted transversely isotropic medium: the
+    hexagonal tensor of Thomsen's parameters about a symmetry axis tilted from
+    vertical by tilt_deg in the vertical plane at azimuth_deg (C33 = rho vp^2,
+    C44 = rho vs^2, C11 = C33 (1 + 2 eps), C66 = C44 (1 + 2 gamma),
+    C13 = sqrt((C33 - C44)(C33 (1 + 2 delta) - C44)) - C44)."""
+    rho, vp, vs = (np.asarray(v, np.float64).reshape(-1) for v in (rho, vp, vs))
+    c33, c44 = rho * vp * vp, rho * vs * vs
+    c11, c66 = c33 * (1 + 2 * eps), c44 * (1 + 2 * gamma)
+    c13 = np.sqrt(np.maximum((c33 - c44) * (c33 * (1 + 2 * delta) - c44), 0.0)) - c44
+    C = np.zeros((len(rho), 6, 6))
+    C[:, 0, 0] = C[:, 1, 1] = c11
+    C[:, 2, 2] = c33
+    C[:, 0, 1] = C[:, 1, 0] = c11 - 2 * c66
+    C[:, 0, 2] = C[:, 2, 0] = C[:, 1, 2] = C[:, 2, 1] = c13
+    C[:, 3, 3] = C[:, 4, 4] = c44
+    C[:, 5, 5] = c66
+    t, a = np.radians(tilt_deg), np.radians(azimuth_deg)
+    Ry = np.array([[np.cos(t), 0, np.sin(t)], [0, 1, 0], [-np.sin(t), 0, np.cos(t)]])
+    Rz = np.array([[np.cos(a), -np.sin(a), 0], [np.sin(a), np.cos(a), 0], [0, 0, 1]])
+    R = Rz @ Ry
+    # Voigt -> 4th order tensor, rotate, back
+    T = np.zeros((len(rho), 3, 3, 3, 3))
+    for I, (i, j) in enumerate(_VOIGT):
+        for J, (k, l) in enumerate(_VOIGT):
+            for (p, q) in {(i, j), (j, i)}:
+                for (r, s) in {(k, l), (l, k)}:
+                    T[:, p, q, r, s] = C[:, I, J]
+    T = np.einsum("ip,jq,kr,ls,npqrs->nijkl", R, R, R, R, T, optimize=True)
+    out = np.zeros_like(C)
+    for I, (i, j) in enumerate(_VOIGT):
+        for J, (k, l) in enumerate(_VOIGT):
+            out[:, I, J] = T[:, i, j, k, l]
+    return out
+
+
+def make_anisotropic(db: dict, voigt: np.ndarray) -> dict:
+    """Copy of db with ANISOTROPY on: the 21 c_ij per GLL point from (npt, 6, 6)
+    Voigt matrices (c11 c12 ... c66, upper triangle row by row)."""
+    out = dict(db)
+    v = np.asarray(voigt, np.float64)
+    for name, (a, b) in zip(ANISO_NAMES, _UPPER):
+        out[name] = v[:, a, b].astype(np.float32)
+    out["anisotropy"] = 1
+    return out
+
+
+def isotropic_voigt(kappa, mu) -> np.ndarray:
+    """(n, 6, 6) Voigt matrices of isotropic media (lambda + 2 mu, lambda, mu)."""
+    k, m = (np.asarray(v, np.float64).reshape(-1) for v in (kappa, mu))
+    lam = k - 2.0 * m / 3.0
+    C = np.zeros((len(k), 6, 6))
+    for i in range(3):
+        for j in range(3):
+            C[:, i, j] = lam
+        C[:, i, i] = lam + 2 * m
+        C[:, 3 + i, 3 + i] = m
+    return C

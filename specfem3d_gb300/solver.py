@@ -22,6 +22,12 @@ NGLL3 = 125
 N_SLS = 3
 
 
+# the 21 anisotropic moduli per GLL point, in the order prepare_fields_elastic_device takes them
+ANISO_NAMES = ["c11store", "c12store", "c13store", "c14store", "c15store", "c16store", "c22store", "c23store",
+               "c24store", "c25store", "c26store", "c33store", "c34store", "c35store", "c36store", "c44store",
+               "c45store", "c46store", "c55store", "c56store", "c66store"]
+
+
 class GPUSolver:
     def __init__(self, db: dict, cfg: dict, nlength: int | None = None, simulation_type: int = 1,
                  save_forward: bool = False, record=("displ",), colors=None, tile: int = 0):
@@ -129,6 +135,7 @@ class GPUSolver:
         phase[:len(inner), 1] = inner
         att = self.attenuation
         strain = int(att or self.simulation_type == 3)
+        aniso = int(db.get("anisotropy", 0))
         zsls = np.zeros(N_SLS * NGLL3 * nspec, np.float32) if att else None
         zeps = np.zeros(NGLL3 * nspec, np.float32) if strain else None
         args = [
@@ -140,8 +147,8 @@ class GPUSolver:
             A.af(zsls), A.af(zeps), A.af(db.get("factor_common_kappa") if att else None),
             A.af(db.get("alphaval", np.zeros(3))), A.af(db.get("betaval", np.zeros(3))),
             A.af(db.get("gammaval", np.zeros(3))), A.i(0), A.af(None), A.i(0), A.af(None), A.ai(None), A.ai(None),
-            A.i(0), A.i(0), A.i(ncol_out), A.i(ncol_in), A.ai(elem_colors), A.i(0),
-            *(A.af(None) for _ in range(21)),
+            A.i(0), A.i(0), A.i(ncol_out), A.i(ncol_in), A.ai(elem_colors), A.i(aniso),
+            *(A.af(db[n] if aniso else None) for n in ANISO_NAMES),
         ]
         self.L.prepare_fields_elastic_device_(*args)
         abi.check()

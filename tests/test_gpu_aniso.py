@@ -1,0 +1,65 @@
+"""Anisotropic stiffness (ANISOTROPY: 21 c_ij per GLL point) on the device.
+
+* c_ij of the isotropic medium (lambda + 2 mu, lambda, mu) reproduce the
+  isotropic path: seismograms within 1e-5 relative L2 after 400 steps (the two
+  stress formulas round differently);
+* a tilted transversely isotropic medium (Thomsen eps 0.05, gamma 0.04,
+  delta 0.02, axis tilted 30 degrees): device against the oracle's FP32 step,
+  seismograms <= 5e-5 and displacement <= 1e-4 relative L2, with and without
+  attenuation (the memory variables keep using mu and kappa, as the reference's)."""
+import os
+
+import numpy as np
+import pytest
+
+from conftest import rel_l2
+
+pytestmark = pytest.mark.gpu
+
+
+def _run(db, cfg):
+    from specfem3d_gb300.solver import GPUSolver
+    g = GPUSolver(db, cfg)
+    g.run(cfg["nstep"], steps_per_graph=50)
+    s, d = g.seismograms(), g.fields()[0]
+    g.close()
+    return s, d
+
+
+@pytest.mark.parametrize("att", [False, True])
+def test_isotropic_cij_equal_isotropic_path(gpulib, att):
+    from specfem3d_gb300 import configs, meshgen, models as M
+    cfg = configs.small_layered(nstep=400, attenuation=att)
+    db = meshgen.build_database(cfg)
+    # with attenuation the c_ij take the unrelaxed moduli the isotropic path uses
+    # (the reference scales mustore / kappastore, not the c_ij)
+    k, m = db["kappastore"], db["mustore"]
+    dba = M.make_anisotropic(db, M.isotropic_voigt(k, m))
+    s0, _ = _run(db, cfg)
+    s1, _ = _run(dba, cfg)
+    e = rel_l2(s1, s0)
+    print(f"isotropic c_ij vs isotropic path (att={att}): {e:.2e}")
+    assert np.abs(s0).max() > 0
+    assert e < 1e-5
+
+
+@pytest.mark.parametrize("att", [False, True])
+def test_tilted_ti_vs_oracle(gpulib, att):
+    from oracle import oracle as O
+    from specfem3d_gb300 import configs, meshgen, models as M
+    cfg = configs.small_layered(nstep=400, attenuation=att)
+    db = meshgen.build_database(cfg)
+    rho = db["rhostore"].astype(np.float64)
+    C = M.tilted_ti(rho, db["rho_vp"] / rho, db["rho_vs"] / rho)
+    dba = M.make_anisotropic(db, C)
+    sim = O.make_sim(dba, cfg, "f32", nthreads=os.cpu_count() or 1)
+    sim.step(cfg["nstep"])
+    ref = O.seismograms(sim)
+    s, d = _run(dba, cfg)
+    s_iso, _ = _run(db, cfg)
+    es, ed = rel_l2(s, ref), rel_l2(d, sim.get("displ"))
+    print(f"tilted TI (att={att}): seismograms {es:.2e}, displacement {ed:.2e}; "
+          f"differs from the isotropic run by {rel_l2(s, s_iso):.2e}")
+    assert np.abs(ref).max() > 0
+    assert rel_l2(s, s_iso) > 1e-2
+    assert es < 5e-5 and ed < 1e-4
