@@ -1,11 +1,12 @@
 """Anisotropic stiffness (ANISOTROPY: 21 c_ij per GLL point) on the device.
 
 * c_ij of the isotropic medium (lambda + 2 mu, lambda, mu) reproduce the
-  isotropic path: seismograms within 1e-5 relative L2 after 400 steps (the two
-  stress formulas round differently);
+  isotropic path: seismograms within 2e-6 relative L2 after 400 steps (the two
+  stress formulas round differently; measured 3.5e-7);
 * a tilted transversely isotropic medium (Thomsen eps 0.05, gamma 0.04,
   delta 0.02, axis tilted 30 degrees): device against the oracle's FP32 step,
-  seismograms <= 5e-5 and displacement <= 1e-4 relative L2, with and without
+  seismograms <= 5e-6 and displacement <= 1e-5 relative L2 (measured 3.3e-7 and
+  7.8e-7), with and without
   attenuation (the memory variables keep using mu and kappa, as the reference's)."""
 import os
 
@@ -40,7 +41,7 @@ def test_isotropic_cij_equal_isotropic_path(gpulib, att):
     e = rel_l2(s1, s0)
     print(f"isotropic c_ij vs isotropic path (att={att}): {e:.2e}")
     assert np.abs(s0).max() > 0
-    assert e < 1e-5
+    assert e < 2e-6
 
 
 @pytest.mark.parametrize("att", [False, True])
@@ -62,4 +63,4 @@ def test_tilted_ti_vs_oracle(gpulib, att):
           f"differs from the isotropic run by {rel_l2(s, s_iso):.2e}")
     assert np.abs(ref).max() > 0
     assert rel_l2(s, s_iso) > 1e-2
-    assert es < 5e-5 and ed < 1e-4
+    assert es < 5e-6 and ed < 1e-5
