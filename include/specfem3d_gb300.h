@@ -271,6 +271,20 @@ void compute_kernels_elastic_cuda_(long *Mesh_pointer, realw *deltat_f);
 void transfer_kernels_el_to_host_(long *Mesh_pointer, realw *h_rho_kl, realw *h_mu_kl,
                                   realw *h_kappa_kl, realw *h_cijkl_kl, int *NSPEC_AB);
 
+/* APPROXIMATE_HESS_KL (compute_kernels_cuda.cu:350-470): accumulate the
+ * elastic Hessian kernels hess_kl += dt a_adj . b_a, hess_rho_kl += dt
+ * b_v . b_v, hess_kappa_kl and hess_mu_kl from the backward strain
+ * (compute_kernels.f90:513-545); acoustic Hessian kernels are not supported. */
+void compute_kernels_hess_cuda_(long *Mesh_pointer, realw *deltat_f, int *ELASTIC_SIMULATION,
+                                int *ACOUSTIC_SIMULATION);
+void transfer_kernels_hess_el_tohost_(long *Mesh_pointer, realw *h_hess_kl, realw *h_hess_rho_kl,
+                                      realw *h_hess_kappa_kl, realw *h_hess_mu_kl, int *NSPEC_AB);
+
+/* FP64 accumulators of ANISOTROPIC_KL ((21,5,5,5,NSPEC), the strain products of
+ * compute_strain_product) and APPROXIMATE_HESS_KL ((5,5,5,NSPEC) x 4: hess,
+ * hess_rho, hess_kappa, hess_mu); either pointer may be NULL.  Library-only. */
+int sf3d_get_extra_kernels_f64(long *Mesh_pointer, double *h_cijkl_kl, double *h_hess);
+
 /* ---- Gaussian smoothing of kernels (xsmooth_sem GPU mode) ----------------
  * Replace prepare_smooth_gpu / compute_smooth_gpu / get_smooth_gpu
  * (src/gpu/smooth_cuda.cu:40-248).  *Container receives a handle; the

@@ -66,6 +66,8 @@ def load() -> ctypes.CDLL:
     L.sf3d_iterate_time.argtypes = [P, ctypes.c_int, ctypes.c_int, ctypes.c_float, ctypes.c_int, ctypes.c_int]
     L.sf3d_get_seismograms.restype = ctypes.c_int
     L.sf3d_get_seismograms.argtypes = [P, P]
+    L.sf3d_get_extra_kernels_f64.restype = ctypes.c_int
+    L.sf3d_get_extra_kernels_f64.argtypes = [P, P, P]
     L.sf3d_get_seismograms_kind.restype = ctypes.c_int
     L.sf3d_get_seismograms_kind.argtypes = [P, ctypes.c_int, P]
     L.sf3d_last_timing.restype = ctypes.c_int

@@ -110,6 +110,64 @@ __global__ void kernels_accum_kernel(long nspec, const int* __restrict__ ibool, 
   kappa_kl[eo] += dt * (9.0 * (double)tr[eo] * (double)btr[eo]);
 }
 
+// ANISOTROPIC_KL: the 21 strain products of compute_strain_product
+// (compute_kernels.f90:566-618; kernels/compute_kernels_ani_cudakernel.cu), FP64
+__global__ void kernels_aniso_kernel(long nspec, const Ptrs10 E, const float* __restrict__ tr,
+                                     const float* __restrict__ btr, double dt, double* __restrict__ cijkl) {
+  const long e = blockIdx.x;
+  const int t = threadIdx.x;
+  if (e >= nspec || t >= NGLL3) return;
+  const long eo = e * NGLL3_PAD + t;
+  // Voigt strains: 11, 22, 33, 23, 13, 12 from the deviatoric parts and the trace
+  double a[6], b[6];
+  const double ta = tr[eo], tb = btr[eo];
+  a[0] = E.p[0][eo] + ta; a[1] = E.p[1][eo] + ta; a[2] = -(a[0] + a[1]) + 3.0 * ta;
+  a[3] = E.p[4][eo]; a[4] = E.p[3][eo]; a[5] = E.p[2][eo];
+  b[0] = E.p[5][eo] + tb; b[1] = E.p[6][eo] + tb; b[2] = -(b[0] + b[1]) + 3.0 * tb;
+  b[3] = E.p[9][eo]; b[4] = E.p[8][eo]; b[5] = E.p[7][eo];
+  double* out = cijkl + eo * 21;
+  int p = 0;
+#pragma unroll
+  for (int i = 0; i < 6; ++i)
+#pragma unroll
+    for (int j = i; j < 6; ++j) {
+      double v = a[i] * b[j];
+      if (j > i) {
+        v += a[j] * b[i];
+        if (j > 2 && i < 3) v *= 2.0;
+      }
+      if (i > 2) v *= 4.0;
+      out[p] += dt * v;
+      ++p;
+    }
+}
+
+// APPROXIMATE_HESS_KL (compute_kernels.f90:513-545;
+// kernels/compute_kernels_hess_el_cudakernel.cu), FP64
+__global__ void kernels_hess_kernel(long nspec, const int* __restrict__ ibool, const int* __restrict__ is_acoustic,
+                                    const float* __restrict__ accel, const float* __restrict__ b_accel,
+                                    const float* __restrict__ b_veloc, const Ptrs10 E, const float* __restrict__ btr,
+                                    double dt, double* __restrict__ h0, double* __restrict__ h_rho,
+                                    double* __restrict__ h_kappa, double* __restrict__ h_mu) {
+  const long e = blockIdx.x;
+  const int t = threadIdx.x;
+  if (e >= nspec || t >= NGLL3) return;
+  if (is_acoustic && is_acoustic[e]) return;
+  const long eo = e * NGLL3_PAD + t;
+  const long g = ibool[eo];
+  double aa = 0.0, vv = 0.0;
+#pragma unroll
+  for (int c = 0; c < 3; ++c) {
+    aa += (double)accel[3 * g + c] * b_accel[3 * g + c];
+    vv += (double)b_veloc[3 * g + c] * b_veloc[3 * g + c];
+  }
+  h0[eo] += dt * aa;
+  h_rho[eo] += dt * vv;
+  const double b0 = E.p[5][eo], b1 = E.p[6][eo], b2 = E.p[7][eo], b3 = E.p[8][eo], b4 = E.p[9][eo];
+  h_mu[eo] += dt * (b0 * b0 + b1 * b1 + (b0 + b1) * (b0 + b1) + 2.0 * (b2 * b2 + b3 * b3 + b4 * b4));
+  h_kappa[eo] += dt * (9.0 * (double)btr[eo] * (double)btr[eo]);
+}
+
 __global__ void kl_to_float_kernel(float* __restrict__ dst, const double* __restrict__ src, long nspec) {
   long idx = (long)blockIdx.x * blockDim.x + threadIdx.x;
   if (idx >= nspec * NGLL3) return;
@@ -148,14 +206,16 @@ void prepare_fields_elastic_adj_dev_(long* Mesh_pointer, int* size_f, realw* eps
   (void)b_epsilondev_yy; (void)b_epsilondev_xy; (void)b_epsilondev_xz; (void)b_epsilondev_yz;
   Mesh* mp = get_mesh(Mesh_pointer);
   if (!mp) return;
-  if (ANISOTROPIC_KL && *ANISOTROPIC_KL) { set_error(SF3D_ERR_ARG, "anisotropic kernels are not supported"); return; }
-  if (APPROXIMATE_HESS_KL && *APPROXIMATE_HESS_KL) { set_error(SF3D_ERR_ARG, "Hessian kernels are not supported"); return; }
+  mp->anisotropic_kl = (ANISOTROPIC_KL && *ANISOTROPIC_KL) ? 1 : 0;
+  mp->hess_kl = (APPROXIMATE_HESS_KL && *APPROXIMATE_HESS_KL) ? 1 : 0;
   if (!size_f || *size_f != 3 * mp->nglob) { set_error(SF3D_ERR_ARG, "size_f must be NDIM*NGLOB_AB"); return; }
   bool ok = alloc_field_set(mp, mp->f) && alloc_field_set(mp, mp->b);
   const size_t nk = NGLL3_PAD * (size_t)mp->nspec;
   ok = ok && alloc_zero((void**)&mp->d_rho_kl, sizeof(double) * nk);
   ok = ok && alloc_zero((void**)&mp->d_mu_kl, sizeof(double) * nk);
   ok = ok && alloc_zero((void**)&mp->d_kappa_kl, sizeof(double) * nk);
+  if (mp->anisotropic_kl) ok = ok && alloc_zero((void**)&mp->d_cijkl_kl, sizeof(double) * 21 * nk);
+  for (int q = 0; q < 4 && mp->hess_kl; ++q) ok = ok && alloc_zero((void**)&mp->d_hess_kl[q], sizeof(double) * nk);
   if (ok && mp->attenuation) {
     realw* hr[6] = {b_R_xx, b_R_yy, b_R_xy, b_R_xz, b_R_yz, b_R_trace};
     for (int c = 0; c < 6 && ok; ++c) ok = upload_sls_padded(&mp->b.R[c], hr[c], mp->nspec, mp->stream);
@@ -238,6 +298,11 @@ void compute_kernels_elastic_cuda_(long* Mesh_pointer, realw* deltat_f) {
   kernels_accum_kernel<<<mp->nspec, NGLL3_PAD, 0, mp->stream>>>(
       mp->nspec, mp->d_ibool, mp->f.accel, mp->b.displ, E, mp->f.eps_trace_over_3, mp->b.eps_trace_over_3,
       (double)*deltat_f, mp->d_rho_kl, mp->d_mu_kl, mp->d_kappa_kl);
+  if (mp->anisotropic_kl)
+    // with ANISOTROPIC_KL the reference accumulates cijkl_kl in place of mu/kappa;
+    // both are kept here (mu_kl, kappa_kl stay available)
+    kernels_aniso_kernel<<<mp->nspec, NGLL3_PAD, 0, mp->stream>>>(
+        mp->nspec, E, mp->f.eps_trace_over_3, mp->b.eps_trace_over_3, (double)*deltat_f, mp->d_cijkl_kl);
   SF3D_CUDA(cudaStreamSynchronize(mp->stream));
   cuda_ok(cudaGetLastError(), "kernels_accum_kernel");
 }
@@ -257,6 +322,76 @@ void transfer_kernels_el_to_host_(long* Mesh_pointer, realw* h_rho_kl, realw* h_
     SF3D_CUDA(cudaMemcpyAsync(h[q], mp->d_stage, sizeof(float) * n, cudaMemcpyDeviceToHost, mp->stream));
     SF3D_CUDA(cudaStreamSynchronize(mp->stream));
   }
+  if (mp->anisotropic_kl && h_cijkl_kl) {
+    // cijkl_kl(21,5,5,5,NSPEC)
+    std::vector<double> tmp(21 * NGLL3_PAD * (size_t)mp->nspec);
+    if (!copy_sync(tmp.data(), mp->d_cijkl_kl, sizeof(double) * tmp.size(), cudaMemcpyDeviceToHost, mp->stream)) return;
+    for (long e = 0; e < mp->nspec; ++e)
+      for (int p = 0; p < NGLL3; ++p)
+        for (int c = 0; c < 21; ++c)
+          h_cijkl_kl[c + 21 * (p + NGLL3 * e)] = (float)tmp[c + 21 * (p + (size_t)NGLL3_PAD * e)];
+  }
+}
+
+void compute_kernels_hess_cuda_(long* Mesh_pointer, realw* deltat_f, int* ELASTIC_SIMULATION,
+                                int* ACOUSTIC_SIMULATION) {
+  Mesh* mp = get_mesh(Mesh_pointer);
+  if (!mp) return;
+  if (!mp->hess_kl || !mp->d_hess_kl[0]) { set_error(SF3D_ERR_STATE, "APPROXIMATE_HESS_KL was not prepared"); return; }
+  if (ACOUSTIC_SIMULATION && *ACOUSTIC_SIMULATION && mp->has_acoustic) {
+    set_error(SF3D_ERR_ARG, "acoustic Hessian kernels are not supported");
+    return;
+  }
+  if (ELASTIC_SIMULATION && !*ELASTIC_SIMULATION) return;
+  const Ptrs10 E = {{mp->f.eps[0], mp->f.eps[1], mp->f.eps[2], mp->f.eps[3], mp->f.eps[4],
+                     mp->b.eps[0], mp->b.eps[1], mp->b.eps[2], mp->b.eps[3], mp->b.eps[4]}};
+  kernels_hess_kernel<<<mp->nspec, NGLL3_PAD, 0, mp->stream>>>(
+      mp->nspec, mp->d_ibool, mp->d_ispec_is_acoustic, mp->f.accel, mp->b.accel, mp->b.veloc, E,
+      mp->b.eps_trace_over_3, (double)*deltat_f, mp->d_hess_kl[0], mp->d_hess_kl[1], mp->d_hess_kl[2],
+      mp->d_hess_kl[3]);
+  cuda_ok(cudaGetLastError(), "kernels_hess_kernel");
+}
+
+void transfer_kernels_hess_el_tohost_(long* Mesh_pointer, realw* h_hess_kl, realw* h_hess_rho_kl,
+                                      realw* h_hess_kappa_kl, realw* h_hess_mu_kl, int* NSPEC_AB) {
+  Mesh* mp = get_mesh(Mesh_pointer);
+  if (!mp) return;
+  if (*NSPEC_AB != mp->nspec || !mp->d_hess_kl[0]) { set_error(SF3D_ERR_ARG, "Hessian kernels not allocated / NSPEC mismatch"); return; }
+  const long n = (long)mp->nspec * NGLL3;
+  if (!ensure_stage(mp, sizeof(float) * n)) return;
+  realw* h[4] = {h_hess_kl, h_hess_rho_kl, h_hess_kappa_kl, h_hess_mu_kl};
+  for (int q = 0; q < 4; ++q) {
+    kl_to_float_kernel<<<nblk(n, 256), 256, 0, mp->stream>>>(mp->d_stage, mp->d_hess_kl[q], mp->nspec);
+    SF3D_CUDA(cudaMemcpyAsync(h[q], mp->d_stage, sizeof(float) * n, cudaMemcpyDeviceToHost, mp->stream));
+    SF3D_CUDA(cudaStreamSynchronize(mp->stream));
+  }
+}
+
+// FP64 anisotropic (21 per point) and Hessian (4 per point) accumulators, either may be NULL
+int sf3d_get_extra_kernels_f64(long* Mesh_pointer, double* h_cijkl_kl, double* h_hess) {
+  Mesh* mp = get_mesh(Mesh_pointer);
+  if (!mp) return SF3D_ERR_STATE;
+  const size_t np = NGLL3_PAD * (size_t)mp->nspec;
+  if (h_cijkl_kl) {
+    if (!mp->d_cijkl_kl) { set_error(SF3D_ERR_STATE, "ANISOTROPIC_KL was not prepared"); return SF3D_ERR_STATE; }
+    std::vector<double> tmp(21 * np);
+    if (!copy_sync(tmp.data(), mp->d_cijkl_kl, sizeof(double) * tmp.size(), cudaMemcpyDeviceToHost, mp->stream))
+      return SF3D_ERR_CUDA;
+    for (long e = 0; e < mp->nspec; ++e)
+      for (int p = 0; p < NGLL3; ++p)
+        for (int c = 0; c < 21; ++c) h_cijkl_kl[c + 21 * (p + NGLL3 * e)] = tmp[c + 21 * (p + (size_t)NGLL3_PAD * e)];
+  }
+  if (h_hess) {
+    if (!mp->d_hess_kl[0]) { set_error(SF3D_ERR_STATE, "APPROXIMATE_HESS_KL was not prepared"); return SF3D_ERR_STATE; }
+    std::vector<double> tmp(np);
+    for (int q = 0; q < 4; ++q) {
+      if (!copy_sync(tmp.data(), mp->d_hess_kl[q], sizeof(double) * np, cudaMemcpyDeviceToHost, mp->stream))
+        return SF3D_ERR_CUDA;
+      for (long e = 0; e < mp->nspec; ++e)
+        for (int p = 0; p < NGLL3; ++p) h_hess[(size_t)q * NGLL3 * mp->nspec + p + NGLL3 * e] = tmp[p + (size_t)NGLL3_PAD * e];
+    }
+  }
+  return SF3D_OK;
 }
 
 // FP64 kernels straight from the device accumulators, (5,5,5,NSPEC) each

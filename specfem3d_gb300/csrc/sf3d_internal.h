@@ -170,6 +170,9 @@ struct Mesh {
   double* d_rho_kl = nullptr;
   double* d_mu_kl = nullptr;
   double* d_kappa_kl = nullptr;
+  int anisotropic_kl = 0, hess_kl = 0;
+  double* d_cijkl_kl = nullptr;          // ANISOTROPIC_KL: [nspec][128][21]
+  double* d_hess_kl[4] = {};             // APPROXIMATE_HESS_KL: hess, hess_rho, hess_kappa, hess_mu
   int nadj_rec_local = 0;
   int ntstep_between_read_adjsrc = 0;
   int* d_ispec_adj = nullptr;             // [nadj_rec_local] 0-based

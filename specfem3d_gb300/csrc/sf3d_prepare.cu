@@ -543,7 +543,8 @@ void prepare_cleanup_device_(long* Mesh_pointer, int* ACOUSTIC_SIMULATION, int* 
   cudaFree(mp->d_factor_common); cudaFree(mp->d_factor_common_kappa);
   free_fields(mp->f);
   free_fields(mp->b);
-  cudaFree(mp->d_rho_kl); cudaFree(mp->d_mu_kl); cudaFree(mp->d_kappa_kl);
+  cudaFree(mp->d_rho_kl); cudaFree(mp->d_mu_kl); cudaFree(mp->d_kappa_kl); cudaFree(mp->d_cijkl_kl);
+  for (int q = 0; q < 4; ++q) cudaFree(mp->d_hess_kl[q]);
   cudaFree(mp->d_ispec_adj); cudaFree(mp->d_hxir_adj); cudaFree(mp->d_hetar_adj); cudaFree(mp->d_hgammar_adj);
   cudaFree(mp->d_source_adjoint);
   cudaFree(mp->d_ispec_is_acoustic); cudaFree(mp->d_rhostore); cudaFree(mp->d_potential);

@@ -345,3 +345,81 @@ def test_analytic_elastic_golden_seismograms(gpulib):
             assert e < 1e-3 and cc > 0.9999, (r, c, e, cc)
     print(f"analytic benchmark vs REF_SEIS: worst trace {max(errs):.2e}; vs the analytic solution "
           f"{rel_l2(seis, ana):.2e} (REF_SEIS itself {rel_l2(ref, ana):.2e})")
+
+
+def test_anisotropic_and_hessian_kernel_accumulation(gpulib):
+    """ANISOTROPIC_KL (21 strain products, compute_kernels.f90:566-618) and
+    APPROXIMATE_HESS_KL (hess, hess_rho, hess_kappa, hess_mu, :513-545) against the
+    formulas evaluated in FP64 on the oracle's strains of both fields."""
+    from specfem3d_gb300 import abi, configs, meshgen
+    from oracle import oracle as O
+    cfg = configs.small_layered(nstep=4, attenuation=False)
+    db = meshgen.build_database(cfg)
+    g = _solver(db, cfg, simulation_type=3)
+    L, A = g.L, abi.Args()
+    n3 = 3 * db["nglob"]
+    L.prepare_fields_elastic_adj_dev_(g.mp, A.i(n3), *([A.af(None)] * 7), A.i(1), *([A.af(None)] * 10), A.i(1),
+                                      A.i(1))
+    abi.check()
+    rng = np.random.default_rng(8)
+    f = rng.standard_normal(n3).astype(np.float32)
+    b = rng.standard_normal(n3).astype(np.float32)
+    bv = rng.standard_normal(n3).astype(np.float32)
+    ba = rng.standard_normal(n3).astype(np.float32)
+    g.set_fields(f, f * 0.5, f * 0.1)
+    L.transfer_b_fields_to_device_(A.i(n3), A.af(b), A.af(bv), A.af(ba), g.mp)
+    L.compute_strain_cuda_(g.mp, A.i(1))
+    L.compute_strain_cuda_(g.mp, A.i(3))
+    dt = np.float32(cfg["dt"])
+    L.compute_kernels_elastic_cuda_(g.mp, A.f(dt))
+    L.compute_kernels_hess_cuda_(g.mp, A.f(dt), A.i(1), A.i(0))
+    abi.check()
+    nspec = db["nspec"]
+    nk = 125 * nspec
+    cij = np.zeros(21 * nk)
+    hess = np.zeros(4 * nk)
+    assert L.sf3d_get_extra_kernels_f64(g.mp, cij.ctypes.data, hess.ctypes.data) == 0
+    h32 = [np.zeros(nk, np.float32) for _ in range(4)]
+    L.transfer_kernels_hess_el_tohost_(g.mp, *(h.ctypes.data for h in h32), A.i(nspec))
+    abi.check()
+    for q in range(4):
+        assert np.allclose(h32[q], hess[q * nk:(q + 1) * nk].astype(np.float32))
+    g.close()
+    sim = O.make_sim(db, cfg, "f64")
+    sim.seti("compute_and_store_strain", 1)
+    names = ["epsilondev_xx", "epsilondev_yy", "epsilondev_xy", "epsilondev_xz", "epsilondev_yz"]
+    strains = {}
+    for tag, fld in (("adj", f), ("b", b)):
+        for nm in names + ["epsilon_trace_over_3"]:
+            sim.set(nm, np.zeros(nk))
+        sim.get("displ")[:] = fld.astype(np.float64)
+        sim.forces()
+        strains[tag] = [sim.get(nm).copy() for nm in names] + [sim.get("epsilon_trace_over_3").copy()]
+
+    def voigt(s):
+        e11, e22 = s[0] + s[5], s[1] + s[5]
+        return [e11, e22, -(e11 + e22) + 3 * s[5], s[4], s[3], s[2]]
+
+    ea, eb = voigt(strains["adj"]), voigt(strains["b"])
+    ref = []
+    for i in range(6):
+        for j in range(i, 6):
+            v = ea[i] * eb[j]
+            if j > i:
+                v = v + ea[j] * eb[i]
+                if j > 2 and i < 3:
+                    v = v * 2
+            if i > 2:
+                v = v * 4
+            ref.append(float(dt) * v)
+    ref = np.stack(ref, axis=1).reshape(-1)
+    assert rel_l2(cij, ref) < 1e-5
+    ib = db["ibool"] - 1
+    acc = (f * np.float32(0.1)).astype(np.float64).reshape(-1, 3)[ib]
+    e = strains["b"]
+    href = [float(dt) * (acc * ba.astype(np.float64).reshape(-1, 3)[ib]).sum(1),
+            float(dt) * (bv.astype(np.float64).reshape(-1, 3)[ib] ** 2).sum(1),
+            float(dt) * 9 * e[5] * e[5],
+            float(dt) * (e[0] * e[0] + e[1] * e[1] + (e[0] + e[1]) ** 2 + 2 * (e[2] ** 2 + e[3] ** 2 + e[4] ** 2))]
+    for q in range(4):
+        assert rel_l2(hess[q * nk:(q + 1) * nk], href[q]) < 1e-5, q
