@@ -221,6 +221,60 @@ def coupled_leg(steps: int):
             "workload": "coupled fluid/solid 96x96x48 hexes, 20x20x10 km"}
 
 
+def aniso_leg(db: dict, cfg: dict, steps: int):
+    """Stiffness launch time of the main workload with ANISOTROPY on (tilted TI per
+    layer: 21 c_ij per GLL point on top of the attenuation arrays), CUDA events
+    around every stiffness launch, against the HBM roofline with the extra
+    21 x 4 B x 125 = 10,500 B per element."""
+    from specfem3d_gb300 import models as M, solver
+    lay = np.asarray(cfg["elem_layer"], np.int64)
+    L = cfg["layers"]
+    C = M.tilted_ti([m["rho"] for m in L], [m["vp"] for m in L], [m["vs"] for m in L])
+    d = dict(db)
+    for name, (a, b) in zip(M.ANISO_NAMES, M._UPPER):
+        d[name] = np.repeat(C[lay, a, b].astype(np.float32), 125)
+    d["anisotropy"] = 1
+    g = solver.GPUSolver(d, cfg, nlength=1)
+    g.run(3, steps_per_graph=0)
+    g.run(steps, steps_per_graph=0, timing=True)
+    t = g.last_timing()
+    g.close()
+    ms = t["stiffness_ms"] / max(t["stiffness_launches"], 1)
+    nspec, nglob = int(db["nspec"]), int(db["nglob"])
+    alg = (33000.0 + 10500.0) * nspec + 48.0 * nglob
+    peak, kind = _peaks()
+    return {"mean_launch_ms": ms, "algorithmic_bytes_per_launch": alg, "achieved_gbs": alg / (ms / 1000.0) / 1e9,
+            "frac": alg / (ms / 1000.0) / 1e9 / peak, "peak_kind": kind, "timed_launches": t["stiffness_launches"],
+            "kernel": "stiffness_kernel<att, aniso, 4 CTAs/SM>",
+            "workload": "main workload with a tilted transversely isotropic medium per layer"}
+
+
+def smooth_leg(nx: int = 64, sigma: float = 312.5):
+    """Gaussian smoothing of three kernels over a 64x64x32-element block (312.5 m
+    cubes, sigma_h = sigma_v = one element): wall time of prepare / compute / get
+    (host binning and copies included) and the point pairs it evaluates."""
+    from specfem3d_gb300 import configs, meshgen, smooth as S
+    from specfem3d_gb300.hexmesh import element_size_max
+    cfg = configs.small_adjoint(nstep=10, nshots=1, n=nx)
+    db = meshgen.build_database(cfg)
+    xyz = meshgen.element_coordinates(cfg)
+    n = int(db["nspec"]) * 125
+    kern = np.random.default_rng(1).standard_normal((3, n)).astype(np.float32)
+    S.smooth(db, xyz, kern, sigma, sigma)      # warm-up (module load, first launch)
+    t0 = time.perf_counter()
+    out = S.smooth(db, xyz, kern, sigma, sigma)
+    dt = time.perf_counter() - t0
+    # element pairs taking part (the inclusion rule on element centres, close to the
+    # per-point rule): 125 x 125 point pairs each, one exp and ~12 flops per pair
+    h2, v2, h3, v3 = S.smoothing_parameters(sigma, sigma, float(element_size_max(xyz).max()))
+    h = float(cfg["x1"]) / nx
+    rh, rv = int(np.ceil(float(h3) / h)), int(np.ceil(float(v3) / h))
+    pairs_el = int(db["nspec"]) * (2 * rh + 1) ** 2 * (2 * rv + 1)
+    return {"wall_s": dt, "nspec": int(db["nspec"]), "kernels": 3, "search_radius_m": float(h3),
+            "approx_point_pairs": pairs_el * 125 * 125, "approx_pairs_per_s": pairs_el * 125 * 125 / dt,
+            "finite": bool(np.isfinite(out).all())}
+
+
 def run_reference(args, rank):
     if rank != 0:
         return 0
@@ -262,6 +316,9 @@ def main():
     ap.add_argument("--batch-steps", type=int, default=100)
     ap.add_argument("--batch-nx", type=int, default=64, help="elements along x and y of the batched mesh")
     ap.add_argument("--coupled", type=int, default=0, help="also time this many steps of the coupled workload")
+    ap.add_argument("--aniso", type=int, default=0,
+                    help="also time this many steps of the main workload with anisotropic stiffness (0: skip)")
+    ap.add_argument("--smooth", action="store_true", help="also time the Gaussian smoothing of three kernels")
     ap.add_argument("--adjoint", type=int, default=0,
                     help="also time the checkpointed misfit gradient over this many shots of the "
                          "8-shot 64x64x32 gradient workload (0: skip)")
@@ -365,6 +422,7 @@ def main():
     gc.close()
     abi.check()
     color_ms = tc["stiffness_ms"] / max(tc["stiffness_launches"], 1)
+    aniso = aniso_leg(db, cfg, args.aniso) if args.aniso > 0 else None
     del db
     line = {
         "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": K, "warmup": W,
@@ -410,6 +468,10 @@ def main():
         line["coupled"] = coupled_leg(args.coupled)
     if args.adjoint > 0:
         line["adjoint"] = adjoint_leg(args.adjoint)
+    if aniso is not None:
+        line["anisotropic"] = aniso
+    if args.smooth:
+        line["smoothing"] = smooth_leg()
     if rank == 0 and not args.no_cpu:
         cv, info = cpu_baseline(args.cpu_steps, os.cpu_count() or 1)
         line["cpu_baseline"] = {"value": cv, "unit": UNIT, "cores": os.cpu_count() or 1, "kind": "port",
