@@ -236,16 +236,21 @@ def aniso_leg(db: dict, cfg: dict, steps: int):
     d["anisotropy"] = 1
     g = solver.GPUSolver(d, cfg, nlength=1)
     g.run(3, steps_per_graph=0)
-    g.run(steps, steps_per_graph=0, timing=True)
-    t = g.last_timing()
+    per = {}
+    for variant, bps in ((0, 4), (2, 5), (3, 6)):        # 4, 5, 6 resident CTAs per SM
+        g.set_stiffness_variant(variant)
+        g.run(steps, steps_per_graph=0, timing=True)
+        t = g.last_timing()
+        per[bps] = t["stiffness_ms"] / max(t["stiffness_launches"], 1)
     g.close()
-    ms = t["stiffness_ms"] / max(t["stiffness_launches"], 1)
+    best = min(per, key=per.get)
+    ms = per[best]
     nspec, nglob = int(db["nspec"]), int(db["nglob"])
     alg = (33000.0 + 10500.0) * nspec + 48.0 * nglob
     peak, kind = _peaks()
     return {"mean_launch_ms": ms, "algorithmic_bytes_per_launch": alg, "achieved_gbs": alg / (ms / 1000.0) / 1e9,
             "frac": alg / (ms / 1000.0) / 1e9 / peak, "peak_kind": kind, "timed_launches": t["stiffness_launches"],
-            "kernel": "stiffness_kernel<att, aniso, 4 CTAs/SM>",
+            "ms_by_ctas_per_sm": per, "kernel": f"stiffness_kernel<att, aniso, {best} CTAs/SM>",
             "workload": "main workload with a tilted transversely isotropic medium per layer"}
 
 

@@ -410,15 +410,26 @@ void launch_stiffness(const StiffnessArgs& a, bool att, bool store_strain, cudaS
   }
 }
 
-void launch_stiffness_aniso(const StiffnessArgs& a, bool att, bool store_strain, cudaStream_t s) {
-  if (a.nelem <= 0) return;
+template <int MINB>
+void launch_aniso_minb(const StiffnessArgs& a, bool att, bool store_strain, cudaStream_t s) {
   dim3 grid(a.nelem), block(NGLL3_PAD);
   if (att)
-    stiffness_kernel<true, true, 4, false, false, true, false, true><<<grid, block, 0, s>>>(a);
+    stiffness_kernel<true, true, MINB, false, false, true, false, true><<<grid, block, 0, s>>>(a);
   else if (store_strain)
-    stiffness_kernel<false, true, 4, false, false, true, false, true><<<grid, block, 0, s>>>(a);
+    stiffness_kernel<false, true, MINB, false, false, true, false, true><<<grid, block, 0, s>>>(a);
   else
-    stiffness_kernel<false, false, 4, false, false, true, false, true><<<grid, block, 0, s>>>(a);
+    stiffness_kernel<false, false, MINB, false, false, true, false, true><<<grid, block, 0, s>>>(a);
+}
+
+// blocks_per_sm: 4, 5 or 6 resident CTAs (the register budget of the 21 extra moduli)
+void launch_stiffness_aniso(const StiffnessArgs& a, bool att, bool store_strain, cudaStream_t s, int blocks_per_sm) {
+  if (a.nelem <= 0) return;
+  if (blocks_per_sm >= 6)
+    launch_aniso_minb<6>(a, att, store_strain, s);
+  else if (blocks_per_sm == 5)
+    launch_aniso_minb<5>(a, att, store_strain, s);
+  else
+    launch_aniso_minb<4>(a, att, store_strain, s);
 }
 
 void launch_stiffness_colored(const StiffnessArgs& a, bool att, bool store_strain, cudaStream_t s) {

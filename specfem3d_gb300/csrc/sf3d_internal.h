@@ -350,7 +350,7 @@ bool check_kernel_error(Mesh* mp);
 // dispatch on Mesh::stiffness_variant
 void launch_stiffness_colored(const StiffnessArgs& a, bool att, bool store_strain, cudaStream_t s);
 inline void run_stiffness(Mesh* mp, const StiffnessArgs& a, bool att, bool store_strain, cudaStream_t s);
-void launch_stiffness_aniso(const StiffnessArgs& a, bool att, bool store_strain, cudaStream_t s);
+void launch_stiffness_aniso(const StiffnessArgs& a, bool att, bool store_strain, cudaStream_t s, int blocks_per_sm);
 // iphase's elements colour by colour with plain read-modify-write assembly
 inline bool run_stiffness_by_color(Mesh* mp, const StiffnessArgs& a, int iphase, bool att, bool store_strain,
                                    cudaStream_t s) {
@@ -371,7 +371,8 @@ inline void run_stiffness(Mesh* mp, const StiffnessArgs& a, bool att, bool store
   if (a.c[0]) {
     // anisotropic stress: its own build of the one-CTA-per-element kernel
     // (atomic assembly, which is correct with or without a colouring)
-    launch_stiffness_aniso(a, att, store_strain, s);
+    const int bps = variant_blocks_per_sm(mp->stiffness_variant);
+    launch_stiffness_aniso(a, att, store_strain, s, bps > 0 ? bps : 4);
     return;
   }
   if (mp->use_mesh_coloring && !mp->geom_half && a.phase && mp->d_phase_ispec) {
