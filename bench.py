@@ -237,7 +237,7 @@ def aniso_leg(db: dict, cfg: dict, steps: int):
     g = solver.GPUSolver(d, cfg, nlength=1)
     g.run(3, steps_per_graph=0)
     per = {}
-    for variant, bps in ((0, 4), (2, 5), (3, 6)):        # 4, 5, 6 resident CTAs per SM
+    for variant, bps in ((2, 4), (3, 5), (4, 6)):        # anisotropic builds: 4, 5, 6 CTAs per SM
         g.set_stiffness_variant(variant)
         g.run(steps, steps_per_graph=0, timing=True)
         t = g.last_timing()

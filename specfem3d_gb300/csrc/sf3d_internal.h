@@ -371,8 +371,10 @@ inline void run_stiffness(Mesh* mp, const StiffnessArgs& a, bool att, bool store
   if (a.c[0]) {
     // anisotropic stress: its own build of the one-CTA-per-element kernel
     // (atomic assembly, which is correct with or without a colouring)
-    const int bps = variant_blocks_per_sm(mp->stiffness_variant);
-    launch_stiffness_aniso(a, att, store_strain, s, bps > 0 ? bps : 4);
+    // the 21 extra moduli take registers: one CTA/SM fewer than the isotropic
+    // build of the same variant (the default, 6, becomes the measured best, 5)
+    const int bps = variant_blocks_per_sm(mp->stiffness_variant) - 1;
+    launch_stiffness_aniso(a, att, store_strain, s, bps < 4 ? 4 : bps);
     return;
   }
   if (mp->use_mesh_coloring && !mp->geom_half && a.phase && mp->d_phase_ispec) {
