@@ -36,6 +36,7 @@ typedef float realw;
 #define SF3D_ERR_CUDA 2     /* CUDA runtime error */
 #define SF3D_ERR_STATE 3    /* call out of order / handle not prepared */
 #define SF3D_ERR_UNSTABLE 4 /* wavefield blew up (NaN/Inf or above threshold) */
+#define SF3D_ERR_UNSUPPORTED 5 /* entry point of a feature this library does not provide */
 
 int sf3d_last_error(char *msg, int msg_len);  /* returns last status, copies message */
 void sf3d_clear_error(void);
@@ -489,6 +490,140 @@ int sf3d_batch_get_seismograms(long *Mesh_pointer, realw *h_seismograms);
 int sf3d_batch_get_displ(long *Mesh_pointer, realw *h_displ);
 /* Free the batch (also freed by prepare_cleanup_device). */
 int sf3d_batch_release(long *Mesh_pointer);
+
+/* Host-side checks, norms and memory reports (check_fields_cuda.cu). The *_gpu checks and
+ * get_max_accel reduce the device field; the others reduce the host array passed in. */
+void check_error_vectors_(int *sizef, realw *vector1, realw *vector2);
+void check_max_norm_vector_(int *size, realw *vector1, int *announceID);
+void check_max_norm_displ_(int *size, realw *displ, int *announceID);
+void check_max_norm_b_displ_(int *size, realw *b_displ, int *announceID);
+void check_max_norm_b_accel_(int *size, realw *b_accel, int *announceID);
+void check_max_norm_displ_gpu_(int *size, realw *displ, long *Mesh_pointer, int *announceID);
+void check_max_norm_b_displ_gpu_(int *size, realw *b_displ, long *Mesh_pointer, int *announceID);
+void check_max_norm_b_accel_gpu_(int *size, realw *b_accel, long *Mesh_pointer, int *announceID);
+void check_max_norm_b_veloc_gpu_(int *size, realw *b_veloc, long *Mesh_pointer, int *announceID);
+void get_max_accel_(int *itf, int *sizef, long *Mesh_pointer);
+void get_norm_elastic_from_device_(realw *norm, long *Mesh_pointer, int *type);
+void get_norm_acoustic_from_device_(realw *norm, long *Mesh_pointer, int *sim_type);
+void get_free_device_memory_(realw *free_mb, realw *used, realw *total);
+void output_free_device_memory_(int *myrank);
+void make_displ_rand_(long *Mesh_pointer, realw *h_displ);
+void pause_for_debug_(void);
+void register_host_array_(int *size, realw *h_array);
+void unregister_host_array_(realw *h_array);
+
+/* Field transfers (transfer_fields_cuda.cu), host arrays in the reference's layout. */
+void transfer_b_accel_from_device_(int *size, realw *b_accel, long *Mesh_pointer);
+void transfer_b_accel_to_device_(int *size, realw *b_accel, long *Mesh_pointer);
+void transfer_b_veloc_from_device_(int *size, realw *b_veloc, long *Mesh_pointer);
+void transfer_b_veloc_to_device_(int *size, realw *b_veloc, long *Mesh_pointer);
+void transfer_potential_ac_from_device_(int *size, realw *potential_acoustic, long *Mesh_pointer);
+void transfer_dot_dot_from_device_(int *size, realw *potential_dot_dot_acoustic, long *Mesh_pointer);
+void transfer_dot_dot_to_device_(int *size, realw *potential_dot_dot_acoustic, long *Mesh_pointer);
+void transfer_b_strain_to_device_(long *Mesh_pointer, realw *b_epsilondev_xx, realw *b_epsilondev_yy,
+                                  realw *b_epsilondev_xy, realw *b_epsilondev_xz, realw *b_epsilondev_yz,
+                                  realw *b_epsilondev_trace, int *size_epsilondev);
+void transfer_b_rmemory_to_device_(long *Mesh_pointer, realw *b_R_xx, realw *b_R_yy, realw *b_R_xy,
+                                   realw *b_R_xz, realw *b_R_yz, realw *b_R_trace, int *size_R);
+void transfer_compute_kernel_answers_from_device_(long *Mesh_pointer, realw *rho_kl, int *size_rho,
+                                                  realw *mu_kl, int *size_mu, realw *kappa_kl,
+                                                  int *size_kappa);
+void transfer_compute_kernel_fields_from_device_(long *Mesh_pointer, realw *accel, int *size_accel,
+                                                 realw *b_displ, int *size_b_displ, realw *epsilondev_xx,
+                                                 realw *epsilondev_yy, realw *epsilondev_xy,
+                                                 realw *epsilondev_xz, realw *epsilondev_yz,
+                                                 int *size_epsilondev, realw *b_epsilondev_xx,
+                                                 realw *b_epsilondev_yy, realw *b_epsilondev_xy,
+                                                 realw *b_epsilondev_xz, realw *b_epsilondev_yz,
+                                                 int *size_b_epsilondev, realw *rho_kl, int *size_rho,
+                                                 realw *mu_kl, int *size_mu, realw *kappa_kl,
+                                                 int *size_kappa, realw *epsilon_trace_over_3,
+                                                 realw *b_epsilon_trace_over_3,
+                                                 int *size_epsilon_trace_over_3);
+void transfer_boun_pot_from_device_(long *Mesh_pointer, realw *send_potential_dot_dot_buffer,
+                                    const int *FORWARD_OR_ADJOINT);
+void transfer_asmbl_pot_to_device_(long *Mesh_pointer, realw *buffer_recv_scalar_ext_mesh,
+                                   const int *FORWARD_OR_ADJOINT);
+
+/* Stacey passes of the undo-attenuation scheme (compute_stacey_viscoelastic_cuda.cu,
+ * compute_stacey_acoustic_cuda.cu): the same boundary term without a boundary record. */
+void compute_stacey_viscoelastic_undoatt_cuda_(long *Mesh_pointer, int *iphasef, int *FORWARD_OR_ADJOINT_f);
+void compute_stacey_acoustic_undoatt_cuda_(long *Mesh_pointer, int *iphasef, int *FORWARD_OR_ADJOINT_f);
+
+/* Not provided: each records SF3D_ERR_UNSUPPORTED through sf3d_last_error (acoustic
+ * adjoint, noise tomography, C-PML, gravity, ocean load, faults); prepare_fields_gravity_device
+ * with GRAVITY = 0 and prepare_fault_device without Kelvin-Voigt damping are accepted no-ops. */
+void add_source_main_rec_noise_cu_(long *Mesh_pointer, int *it_f, int *irec_main_noise_f,
+                                   int *islice_selected_rec);
+void add_sources_ac_sim_2_or_3_cuda_(long *Mesh_pointer, realw *h_source_adjoint, int *nrec,
+                                     int *nadj_rec_local, int *NTSTEP_BETWEEN_READ_ADJSRC, int *it);
+void compute_add_sources_ac_s3_cuda_(long *Mesh_pointer, int *NSOURCESf, double *h_stf_pre_compute,
+                                     int *run_number_of_the_source);
+void compute_coupling_ocean_cuda_(long *Mesh_pointer, int *FORWARD_OR_ADJOINT);
+void compute_kernels_acoustic_cuda_(long *Mesh_pointer, realw *deltat_f);
+void compute_kernels_strgth_noise_cu_(long *Mesh_pointer, realw *h_noise_surface_movie, realw *deltat);
+void fault_solver_gpu_(long *Mesh_pointer, long *Fault_pointer, realw *dt, int *it);
+void initialize_fault_data_gpu_(long *Fault_solver, int *fault_index, int *iglob, int *num_of_records,
+                                int *ndat, int *NT_RECORD_LENGTH);
+void initialize_fault_solver_gpu_(long *Fault_solver, int *num_of_faults, realw *v_healing, realw *v_rupt,
+                                  int *RATE_AND_STATE);
+void noise_read_add_surface_movie_cu_(long *Mesh_pointer, realw *h_noise_surface_movie,
+                                      int *NOISE_TOMOGRAPHYf);
+void pml_impose_boundary_condition_elastic_cuda_(long *Mesh_pointer);
+void prepare_fault_device_(long *Mesh_pointer, int *KELVIN_VOIGT_DAMPING, realw *Kelvin_Voigt_eta);
+void prepare_fields_acoustic_adj_dev_(long *Mesh_pointer, int *APPROXIMATE_HESS_KL);
+void prepare_fields_elastic_pml_(long *Mesh_pointer, int *NSPEC_CPML, int *is_CPML, int *CPML_to_spec,
+                                 int *spec_to_CPML, realw *pml_convolution_coef_alpha,
+                                 realw *pml_convolution_coef_beta, realw *pml_convolution_coef_abar,
+                                 realw *pml_convolution_coef_strain, realw *h_wgll_cube, realw *rhostore);
+void prepare_fields_gravity_device_(long *Mesh_pointer, int *GRAVITY, realw *minus_deriv_gravity,
+                                    realw *minus_g, realw *h_wgll_cube, realw *rhostore);
+void prepare_fields_noise_device_(long *Mesh_pointer, int *NSPEC_AB, int *NGLOB_AB, int *free_surface_ispec,
+                                  int *free_surface_ijk, int *num_free_surface_faces, int *NOISE_TOMOGRAPHY,
+                                  int *NSTEP, realw *noise_sourcearray, realw *normal_x_noise,
+                                  realw *normal_y_noise, realw *normal_z_noise, realw *mask_noise,
+                                  realw *free_surface_jacobian2Dw);
+void transfer_b_dot_dot_from_device_(int *size, realw *b_potential_dot_dot_acoustic, long *Mesh_pointer);
+void transfer_b_fields_ac_from_device_(int *size, realw *b_potential_acoustic,
+                                       realw *b_potential_dot_acoustic, realw *b_potential_dot_dot_acoustic,
+                                       long *Mesh_pointer);
+void transfer_b_fields_ac_to_device_(int *size, realw *b_potential_acoustic,
+                                     realw *b_potential_dot_acoustic, realw *b_potential_dot_dot_acoustic,
+                                     long *Mesh_pointer);
+void transfer_b_potential_ac_from_device_(int *size, realw *b_potential_acoustic, long *Mesh_pointer);
+void transfer_b_potential_ac_to_device_(int *size, realw *b_potential_acoustic, long *Mesh_pointer);
+void transfer_b_potential_dot_dot_ac_from_device_(int *size, realw *b_potential_dot_dot_acoustic,
+                                                  long *Mesh_pointer);
+void transfer_b_potential_dot_dot_ac_to_device_(int *size, realw *b_potential_dot_dot_acoustic,
+                                                long *Mesh_pointer);
+void transfer_datat_to_host_(long *Fault_pointer, int *fault_index, realw *h_dataT, int *it_in);
+void transfer_fault_data_to_device_(long *Fault_pointer, int *fault_index, int *NSPEC_FLT, int *NGLOB_FLT,
+                                    realw *D, realw *T0, realw *T, realw *B, realw *R, realw *V0, realw *Z,
+                                    realw *invM1, realw *invM2, int *ibulk1, int *ibulk2,
+                                    int *allow_opening);
+void transfer_fault_data_to_host_(long *Fault_pointer, int *fault_index, int *NSPEC_FLT, int *NGLOB_FLT,
+                                  realw *D, realw *V, realw *T);
+void transfer_kernels_ac_to_host_(long *Mesh_pointer, realw *h_rho_ac_kl, realw *h_kappa_ac_kl,
+                                  int *NSPEC_AB);
+void transfer_kernels_hess_ac_tohost_(long *Mesh_pointer, realw *h_hess_ac_kl, realw *h_hess_rho_ac_kl,
+                                      realw *h_hess_kappa_ac_kl, int *NSPEC_AB);
+void transfer_kernels_noise_to_host_(long *Mesh_pointer, realw *h_sigma_kl, int *NSPEC_AB);
+void transfer_pml_displ_from_device_(int *size, realw *PML_displ_old, realw *PML_displ_new,
+                                     long *Mesh_pointer);
+void transfer_pml_displ_to_device_(int *size, realw *PML_displ_old, realw *PML_displ_new,
+                                   long *Mesh_pointer);
+void transfer_rsf_data_todevice_(long *Fault_pointer, int *fault_index, int *NGLOB_FLT, realw *Fload,
+                                 realw *V0, realw *f0, realw *V_init, realw *a, realw *b, realw *L,
+                                 realw *theta, realw *T, realw *C, realw *fw, realw *Vw, int *StateLaw);
+void transfer_rsf_data_tohost_(long *Fault_pointer, int *fault_index, int *NGLOB_FLT, realw *V0, realw *f0,
+                               realw *V_init, realw *a, realw *b, realw *L, realw *theta, realw *T,
+                               realw *C, realw *fw, realw *Vw);
+void transfer_sigma_from_device_(int *size, realw *sigma_kl, long *Mesh_pointer);
+void transfer_surface_to_host_(long *Mesh_pointer, realw *h_noise_surface_movie);
+void transfer_swf_data_todevice_(long *Fault_pointer, int *fault_index, int *NGLOB_FLT, realw *Dc,
+                                 realw *mus, realw *mud, realw *T, realw *C, realw *theta);
+void transfer_swf_data_tohost_(long *Fault_pointer, int *fault_index, int *NGLOB_FLT, realw *Dc, realw *mus,
+                               realw *mud, realw *T, realw *C, realw *theta);
 
 /* Synchronise the compute stream and report the first stored status. */
 int sf3d_synchronize(long *Mesh_pointer);

@@ -5,6 +5,8 @@ import json
 import os
 import re
 
+import numpy as np
+
 import pytest
 
 from conftest import ROOT
@@ -81,3 +83,58 @@ def test_null_handle_is_an_error(gpulib):
     L.kernel_3_a_cuda_(ctypes.addressof(mesh), A.f(0.1), A.f(0.0), A.i(0), A.i(1))
     with pytest.raises(abi.SF3DError, match="not prepared"):
         abi.check()
+
+
+def test_every_reference_entry_point_is_declared_and_exported(gpulib):
+    """The library links into the reference program in place of its GPU layer:
+    each of the entry points of the reference's stub file is declared in the
+    header and exported by the library."""
+    from specfem3d_gb300 import abi
+    ref = json.load(open(FIXTURE))
+    ours = abi.header_signatures()
+    missing = [n for n in ref if n + "_" not in ours]
+    assert not missing, missing
+    for n in ref:
+        assert hasattr(gpulib, n + "_"), n
+    assert len(ref) == 124
+
+
+@pytest.mark.parametrize("name,nargs", [("fault_solver_gpu_", 4), ("compute_kernels_acoustic_cuda_", 2),
+                                        ("pml_impose_boundary_condition_elastic_cuda_", 1),
+                                        ("noise_read_add_surface_movie_cu_", 3)])
+def test_unsupported_feature_is_an_error_status(gpulib, name, nargs):
+    """Entry points of features the library does not provide return with
+    SF3D_ERR_UNSUPPORTED (5) recorded and touch no argument."""
+    from specfem3d_gb300 import abi
+    gpulib.sf3d_clear_error()
+    getattr(gpulib, name)(*([None] * nargs))
+    buf = ctypes.create_string_buffer(512)
+    assert gpulib.sf3d_last_error(buf, 512) == 5
+    assert b"not supported" in buf.value
+    gpulib.sf3d_clear_error()
+    abi.check()
+
+
+def test_gravity_off_and_no_damping_are_accepted(gpulib):
+    from specfem3d_gb300 import abi
+    A = abi.Args()
+    gpulib.sf3d_clear_error()
+    gpulib.prepare_fields_gravity_device_(None, A.i(0), None, None, None, None)
+    gpulib.prepare_fault_device_(None, A.i(0), None)
+    abi.check()
+    gpulib.prepare_fields_gravity_device_(None, A.i(1), None, None, None, None)
+    with pytest.raises(abi.SF3DError, match="gravity"):
+        abi.check()
+
+
+def test_host_vector_checks(gpulib, capfd):
+    """check_error_vectors / check_max_norm_vector (check_fields_cuda.cu) reduce host
+    arrays and print the result; no CUDA call."""
+    from specfem3d_gb300 import abi
+    A = abi.Args()
+    a = np.array([1.0, -3.0, 2.0], np.float32)
+    b = np.array([1.0, -1.0, 2.5], np.float32)
+    gpulib.check_error_vectors_(A.i(3), A.af(a), A.af(b))
+    gpulib.check_max_norm_vector_(A.i(3), A.af(a), A.i(7))
+    out = capfd.readouterr().out
+    assert "2.000000e+00" in out and "7: maximum norm of vector = 3.000000e+00" in out
