@@ -24,6 +24,7 @@ import numpy as np
 
 from . import abi
 from .meshgen import NGLL3, WGLL
+from .solver import N_SLS
 from .solver import GPUSolver
 
 
@@ -53,24 +54,17 @@ def kernel_run(db: dict, cfg: dict, adjoint_source: np.ndarray, final_fields, ab
         raise ValueError("kernel_run: the time-reversed reconstruction is for meshes without attenuation")
     nstep = int(cfg["nstep"])
     g = GPUSolver(db, cfg, nlength=nstep, simulation_type=3)
-    L, A = g.L, abi.Args()
+    L = g.L
     n3 = 3 * g.nglob
-    # prepare_fields_elastic_adj_dev: backward fields and kernel accumulators
-    L.prepare_fields_elastic_adj_dev_(g.mp, A.i(n3), *([A.af(None)] * 7), A.i(1), *([A.af(None)] * 10),
-                                      A.i(0), A.i(0))
-    abi.check()
+    _prepare_adjoint(g, db, nstep)
     nrec = g.nrec
-    # prepare_sim2_or_3_const_device: every receiver of this slice carries an adjoint source
-    L.prepare_sim2_or_3_const_device_(g.mp, A.i(nrec), A.i(nstep), A.af(db["hxir"]), A.af(db["hetar"]),
-                                      A.af(db["hgammar"]), A.i(nrec), A.ai(np.zeros(nrec, np.int32)),
-                                      A.ai(db["ispec_selected_rec"]))
-    abi.check()
     # source_adjoint(NDIM, nadj_rec_local, NTSTEP_BETWEEN_READ_ADJSRC), one block of nstep samples
     src = np.ascontiguousarray(np.asarray(adjoint_source, np.float32).transpose(2, 0, 1))
     stf = np.asarray(db["stf"], np.float64).reshape(g.nsources, -1)
     dt = np.float32(cfg["dt"])
     dt2, dtsq2 = np.float32(dt / np.float32(2)), np.float32(dt * dt / np.float32(2))
     bdt, bdt2 = np.float32(-dt), np.float32(-dt / np.float32(2))
+    A = abi.Args()
     one, three, zero = A.i(1), A.i(3), A.i(0)
     d_fin, v_fin, a_fin = (np.ascontiguousarray(f, np.float32) for f in final_fields)
     for it in range(1, nstep + 1):
@@ -102,12 +96,145 @@ def kernel_run(db: dict, cfg: dict, adjoint_source: np.ndarray, final_fields, ab
             L.transfer_b_fields_to_device_(B.i(n3), B.af(d_fin), B.af(v_fin), B.af(a_fin), g.mp)
         L.compute_kernels_elastic_cuda_(g.mp, B.f(dt))
     abi.check()
+    return _kernels_f64(g)
+
+
+def _prepare_adjoint(g: GPUSolver, db: dict, nstep: int):
+    """prepare_fields_elastic_adj_dev (backward fields, kernel accumulators and, with
+    attenuation, the backward memory variables with the forward-time coefficients
+    of an undo-attenuation run) and prepare_sim2_or_3_const_device (every receiver
+    of this slice carries an adjoint source)."""
+    L, A = g.L, abi.Args()
+    n3 = 3 * g.nglob
+    att = g.attenuation
+    nsls = N_SLS * NGLL3 * g.nspec
+    zsls = np.zeros(nsls, np.float32) if att else None
+    zeps = np.zeros(NGLL3 * g.nspec, np.float32) if att else None
+    coef = [A.af(db.get(n) if att else None) for n in ("alphaval", "betaval", "gammaval")]
+    L.prepare_fields_elastic_adj_dev_(g.mp, A.i(n3), *([A.af(None)] * 7), A.i(nsls if att else 1),
+                                      *(A.af(zsls) for _ in range(6)), A.af(zeps), *coef, A.i(0), A.i(0))
+    abi.check()
+    nrec = g.nrec
+    L.prepare_sim2_or_3_const_device_(g.mp, A.i(nrec), A.i(nstep), A.af(db["hxir"]), A.af(db["hetar"]),
+                                      A.af(db["hgammar"]), A.i(nrec), A.ai(np.zeros(nrec, np.int32)),
+                                      A.ai(db["ispec_selected_rec"]))
+    abi.check()
+
+
+def _kernels_f64(g: GPUSolver) -> dict:
     n = g.nspec
     out = {k: np.zeros(n * NGLL3) for k in ("rho", "mu", "kappa")}
-    L.sf3d_get_kernels_f64(g.mp, out["rho"].ctypes.data, out["mu"].ctypes.data, out["kappa"].ctypes.data)
+    g.L.sf3d_get_kernels_f64(g.mp, out["rho"].ctypes.data, out["mu"].ctypes.data, out["kappa"].ctypes.data)
     abi.check()
     g.close()
     return {k: v.reshape(n, NGLL3) for k, v in out.items()}
+
+
+# ------------------------------------------------------------------ undo attenuation
+def undo_attenuation_forward(db: dict, cfg: dict, nt_dump: int):
+    """SIMULATION_TYPE = 1 with SAVE_FORWARD and UNDO_ATTENUATION_AND_OR_PML
+    (iterate_time_undoatt.F90:280-395): before each subset of nt_dump steps the
+    wavefield and, with attenuation, the memory variables are saved
+    (save_forward_arrays_undoatt: displ, veloc, accel, R_xx..R_yz, R_trace).
+    Returns (seismograms (nrec, 3, nstep), snapshots); snapshot s holds the state
+    after s * nt_dump steps."""
+    cfg = dict(cfg)
+    cfg["record"] = ("displ",)
+    nstep = int(cfg["nstep"])
+    nsub = -(-nstep // int(nt_dump))
+    g = GPUSolver(db, cfg, nlength=nstep, save_forward=True, undo_attenuation=True)
+    snaps = []
+    for s in range(nsub):
+        d, v, a = g.fields()
+        R = g.memory_variables()[0] if g.attenuation else None
+        snaps.append({"displ": d, "veloc": v, "accel": a, "R": R})
+        g.run_per_call(min(int(nt_dump), nstep - s * int(nt_dump)))
+    seis = g.seismograms()
+    g.close()
+    return seis, snaps
+
+
+def undo_attenuation_kernel_run(db: dict, cfg: dict, adjoint_source: np.ndarray, snapshots, nt_dump: int,
+                                history=None):
+    """SIMULATION_TYPE = 3 under UNDO_ATTENUATION_AND_OR_PML
+    (iterate_time_undoatt.F90:396-570), for meshes with or without attenuation.
+    Subsets are visited from the last forward one to the first: the snapshot is
+    restored (read_forward_arrays_undoatt: transfer_b_fields_to_device,
+    transfer_b_rmemory_to_device) and its strain recomputed
+    (compute_strain_cuda, FORWARD_OR_ADJOINT = 3); the backward field is stepped
+    forward in time over the subset (b_deltat = +DT, Stacey from b_veloc through
+    compute_stacey_viscoelastic_undoatt_cuda, the sources at the forward time
+    of compute_add_sources_viscoelastic.F90:743-809) and each b_displ buffered
+    (transfer_b_displ_from_device); then the adjoint field advances through the
+    subset while b_displ is restored from the buffer in reverse order
+    (transfer_b_displ_to_device) and the kernels accumulate (the strain of the
+    restored b_displ is recomputed inside compute_kernels_elastic_cuda).
+    history: optional list that receives the recomputed b_displ of every forward
+    step, keyed by the forward step number.  Returns the raw FP64 accumulators
+    rho_kl, mu_kl, kappa_kl, each (nspec, 125)."""
+    nstep, nt = int(cfg["nstep"]), int(nt_dump)
+    nsub = len(snapshots)
+    if nsub != -(-nstep // nt):
+        raise ValueError("undo_attenuation_kernel_run: one snapshot per subset of nt_dump steps is needed")
+    g = GPUSolver(db, cfg, nlength=nstep, simulation_type=3, undo_attenuation=True)
+    L = g.L
+    n3 = 3 * g.nglob
+    _prepare_adjoint(g, db, nstep)
+    nrec = g.nrec
+    src = np.ascontiguousarray(np.asarray(adjoint_source, np.float32).transpose(2, 0, 1))
+    stf = np.asarray(db["stf"], np.float64).reshape(g.nsources, -1)
+    dt = np.float32(cfg["dt"])
+    dt2, dtsq2 = np.float32(dt / np.float32(2)), np.float32(dt * dt / np.float32(2))
+    att = g.attenuation
+    nsls = N_SLS * NGLL3 * g.nspec
+    it = 0
+    for iteration_on_subset in range(1, nsub + 1):
+        B = abi.Args()
+        one, three = B.i(1), B.i(3)
+        snap = snapshots[nsub - iteration_on_subset]
+        L.transfer_b_fields_to_device_(B.i(n3), *(B.af(snap[k]) for k in ("displ", "veloc", "accel")), g.mp)
+        if att:
+            L.transfer_b_rmemory_to_device_(g.mp, *(B.af(r) for r in snap["R"]), B.i(nsls))
+        L.compute_strain_cuda_(g.mp, three)
+        abi.check()
+        it_subset_end = nstep - (nsub - 1) * nt if iteration_on_subset == 1 else nt
+        first = (nsub - iteration_on_subset) * nt  # forward steps before this subset
+        buf = np.zeros((it_subset_end, n3), np.float32)
+        for k in range(1, it_subset_end + 1):
+            S = abi.Args()
+            L.update_displacement_cuda_(g.mp, S.f(dt), S.f(dt2), S.f(dtsq2), three)
+            for iphase in (1, 2):
+                L.compute_forces_viscoelastic_cuda_(g.mp, S.i(iphase), S.f(dt), S.i(g.nspec_outer),
+                                                    S.i(g.nspec_elastic), one, S.i(att), three)
+                if iphase == 1:
+                    L.compute_stacey_viscoelastic_undoatt_cuda_(g.mp, one, three)
+                    if g.nsources:
+                        # it_tmp = NSTEP - first - k + 1: the stf sample of forward step first + k
+                        L.compute_add_sources_el_s3_cuda_(g.mp, S.ad(np.ascontiguousarray(stf[:, first + k - 1])),
+                                                          S.i(g.nsources))
+            L.kernel_3_a_cuda_(g.mp, S.f(dt2), S.f(dt2), S.i(0), three)
+            L.transfer_b_displ_from_device_(S.i(n3), buf[k - 1].ctypes.data, g.mp)
+            if history is not None:
+                history.append((first + k, buf[k - 1].copy()))
+        abi.check()
+        # compute_strain_att: strain of the current adjoint field
+        L.compute_strain_cuda_(g.mp, one)
+        for k in range(1, it_subset_end + 1):
+            S = abi.Args()
+            it += 1
+            L.transfer_b_displ_to_device_(S.i(n3), S.af(buf[it_subset_end - k]), g.mp)
+            L.update_displacement_cuda_(g.mp, S.f(dt), S.f(dt2), S.f(dtsq2), one)
+            for iphase in (1, 2):
+                L.compute_forces_viscoelastic_cuda_(g.mp, S.i(iphase), S.f(dt), S.i(g.nspec_outer),
+                                                    S.i(g.nspec_elastic), one, S.i(att), one)
+                if iphase == 1:
+                    L.compute_stacey_viscoelastic_cuda_(g.mp, one, None, one)
+                    if it < nstep:
+                        L.add_sources_el_sim_type_2_or_3_(g.mp, S.af(src), S.i(nrec), S.i(nrec), S.i(nstep), S.i(it))
+            L.kernel_3_a_cuda_(g.mp, S.f(dt2), S.f(dt2), S.i(0), one)
+            L.compute_kernels_elastic_cuda_(g.mp, S.f(dt))
+        abi.check()
+    return _kernels_f64(g)
 
 
 def scaled_kernels(db: dict, kl: dict) -> dict:

@@ -45,7 +45,8 @@ __global__ void adjoint_sources_kernel(int nadj, const int* __restrict__ ispec, 
 __global__ void element_strain_kernel(const int* __restrict__ ibool, const int* __restrict__ irregular,
                                       const Ptrs10 m, const float* __restrict__ gll,
                                       float xix_regular, const float* __restrict__ displ, float* eps0, float* eps1,
-                                      float* eps2, float* eps3, float* eps4, float* trace_over_3) {
+                                      float* eps2, float* eps3, float* eps4, float* trace_over_3,
+                                      float* trace) {
   __shared__ float s_u[3][NGLL3_PAD];
   __shared__ float s_hp[NGLL2];
   const int e = blockIdx.x, t = threadIdx.x;
@@ -81,8 +82,10 @@ __global__ void element_strain_kernel(const int* __restrict__ ibool, const int* 
       d[c][2] = xix_regular * t3;
     }
   }
-  const float templ = (1.f / 3.f) * (d[0][0] + d[1][1] + d[2][2]);
+  const float tr = d[0][0] + d[1][1] + d[2][2];
+  const float templ = (1.f / 3.f) * tr;
   trace_over_3[eo] = templ;
+  if (trace) trace[eo] = tr;  // epsilondev_trace of the memory-variable update
   eps0[eo] = d[0][0] - templ;
   eps1[eo] = d[1][1] - templ;
   eps2[eo] = 0.5f * (d[0][1] + d[1][0]);
@@ -276,23 +279,38 @@ void add_sources_el_sim_type_2_or_3_(long* Mesh_pointer, realw* h_source_adjoint
   cuda_ok(cudaGetLastError(), "adjoint_sources_kernel");
 }
 
-void compute_strain_cuda_(long* Mesh_pointer, int* FORWARD_OR_ADJOINT) {
-  Mesh* mp = get_mesh(Mesh_pointer);
-  if (!mp) return;
-  Fields& F = (*FORWARD_OR_ADJOINT == 3) ? mp->b : mp->f;
-  if (!F.displ || !F.eps[0] || !F.eps_trace_over_3) { set_error(SF3D_ERR_STATE, "strain arrays not allocated"); return; }
+namespace {
+// strain of a field from its displacement (compute_strain_cuda.cu,
+// kernels/compute_element_strain_cudakernel.cu)
+bool field_strain(Mesh* mp, Fields& F) {
+  if (!F.displ || !F.eps[0] || !F.eps_trace_over_3) { set_error(SF3D_ERR_STATE, "strain arrays not allocated"); return false; }
   Ptrs10 m = {};
   for (int q = 0; q < 9; ++q) m.p[q] = mp->d_metric[q];
   element_strain_kernel<<<mp->nspec, NGLL3_PAD, 0, mp->stream>>>(mp->d_ibool, mp->d_irregular, m, mp->d_gll,
                                                                  mp->xix_regular, F.displ, F.eps[0], F.eps[1],
-                                                                 F.eps[2], F.eps[3], F.eps[4], F.eps_trace_over_3);
-  cuda_ok(cudaGetLastError(), "element_strain_kernel");
+                                                                 F.eps[2], F.eps[3], F.eps[4], F.eps_trace_over_3,
+                                                                 F.eps[5]);
+  return cuda_ok(cudaGetLastError(), "element_strain_kernel");
+}
+}  // namespace
+
+void compute_strain_cuda_(long* Mesh_pointer, int* FORWARD_OR_ADJOINT) {
+  Mesh* mp = get_mesh(Mesh_pointer);
+  if (!mp) return;
+  if (!FORWARD_OR_ADJOINT || (*FORWARD_OR_ADJOINT != 1 && *FORWARD_OR_ADJOINT != 3)) {
+    set_error(SF3D_ERR_ARG, "compute_strain_cuda: FORWARD_OR_ADJOINT must be 1 or 3");
+    return;
+  }
+  field_strain(mp, (*FORWARD_OR_ADJOINT == 3) ? mp->b : mp->f);
 }
 
 void compute_kernels_elastic_cuda_(long* Mesh_pointer, realw* deltat_f) {
   Mesh* mp = get_mesh(Mesh_pointer);
   if (!mp) return;
   if (!mp->d_rho_kl || !mp->b.displ) { set_error(SF3D_ERR_STATE, "prepare_fields_elastic_adj_dev not called"); return; }
+  // undo attenuation: b_displ was restored from the recomputed history; its
+  // strain is recomputed here
+  if (mp->undo_attenuation && !field_strain(mp, mp->b)) return;
   const Ptrs10 E = {{mp->f.eps[0], mp->f.eps[1], mp->f.eps[2], mp->f.eps[3], mp->f.eps[4],
                      mp->b.eps[0], mp->b.eps[1], mp->b.eps[2], mp->b.eps[3], mp->b.eps[4]}};
   kernels_accum_kernel<<<mp->nspec, NGLL3_PAD, 0, mp->stream>>>(

@@ -158,6 +158,10 @@ struct Mesh {
   // attenuation
   int attenuation = 0;
   int compute_and_store_strain = 0;
+  // UNDO_ATTENUATION_AND_OR_PML: the backward field is recomputed forward in time
+  // from snapshots and its strain is recomputed from b_displ before each kernel
+  // accumulation (compute_kernels_cuda.cu:57)
+  int undo_attenuation = 0;
   float alphaval[NSLS] = {}, betaval[NSLS] = {}, gammaval[NSLS] = {};
   float b_alphaval[NSLS] = {}, b_betaval[NSLS] = {}, b_gammaval[NSLS] = {};
   float* d_factor_common = nullptr;      // [nspec][3][128]

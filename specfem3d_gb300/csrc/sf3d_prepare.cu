@@ -244,7 +244,7 @@ void prepare_constants_device_(long* Mesh_pointer, int* h_NGLLX, int* NSPEC_AB, 
                                int* UNDO_ATTENUATION_AND_OR_PML, int* PML_CONDITIONS) {
   (void)h_ispec_is_inner;
   (void)nspec_elastic; (void)ispec_is_elastic;
-  (void)FAULT_SIMULATION; (void)UNDO_ATTENUATION_AND_OR_PML; (void)nu_source;
+  (void)FAULT_SIMULATION; (void)nu_source;
   if (!Mesh_pointer) { set_error(SF3D_ERR_ARG, "Mesh_pointer is NULL"); return; }
   *Mesh_pointer = 0;
   if (*h_NGLLX != NGLLX) { set_error(SF3D_ERR_ARG, "NGLLX must be 5"); return; }
@@ -266,6 +266,7 @@ void prepare_constants_device_(long* Mesh_pointer, int* h_NGLLX, int* NSPEC_AB, 
   mp->xix_regular = *xix_regular;
   mp->jacobian_regular = *jacobian_regular;
   mp->simulation_type = *SIMULATION_TYPE;
+  mp->undo_attenuation = (UNDO_ATTENUATION_AND_OR_PML && *UNDO_ATTENUATION_AND_OR_PML) ? 1 : 0;
   mp->save_forward = SAVE_FORWARD ? *SAVE_FORWARD : 0;
   bool ok = cuda_ok(cudaStreamCreateWithFlags(&mp->stream, cudaStreamNonBlocking), "cudaStreamCreate") &&
             cuda_ok(cudaEventCreate(&mp->ev0), "event") && cuda_ok(cudaEventCreate(&mp->ev1), "event");

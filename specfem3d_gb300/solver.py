@@ -30,10 +30,13 @@ ANISO_NAMES = ["c11store", "c12store", "c13store", "c14store", "c15store", "c16s
 
 class GPUSolver:
     def __init__(self, db: dict, cfg: dict, nlength: int | None = None, simulation_type: int = 1,
-                 save_forward: bool = False, record=("displ",), colors=None, tile: int = 0):
+                 save_forward: bool = False, record=("displ",), colors=None, tile: int = 0,
+                 undo_attenuation: bool = False):
         """colors: optional colour per element (no two elements of a colour share a
         point, e.g. meshgen.block_colors); the phase lists are then ordered colour by
-        colour and USE_MESH_COLORING_GPU is set, so assembly runs without atomics."""
+        colour and USE_MESH_COLORING_GPU is set, so assembly runs without atomics.
+        undo_attenuation: UNDO_ATTENUATION_AND_OR_PML of prepare_constants_device (the
+        kernel accumulation then recomputes the backward strain from b_displ)."""
         self.colors = None if colors is None else np.asarray(colors, np.int32)
         # tile > 0: phase lists in tiles of tile^3 elements of a block mesh, so that
         # elements sharing points are processed close in time (L2 reuse of the
@@ -58,6 +61,7 @@ class GPUSolver:
         self.isac = np.asarray(db.get("ispec_is_acoustic", np.zeros(self.nspec, np.int32)), np.int32)
         self.coupled = bool(self.isac.any())
         self.absorb_record = None
+        self.undo_attenuation = bool(undo_attenuation)
         self._prepare_constants(db, save_forward)
         self._prepare_fields(db)
         if self.coupled:
@@ -95,7 +99,7 @@ class GPUSolver:
             A.i(0), A.i(int(save_forward)), A.af(hx), A.af(he), A.af(hg), A.ad(nu), A.ad(nu),
             A.ai(np.zeros(max(nrec, 1), np.int32)), A.i(self.nlength),
             A.i(int("displ" in self.record)), A.i(int("veloc" in self.record)), A.i(int("accel" in self.record)),
-            A.i(int("pressure" in self.record)), A.i(1), A.i(0), A.i(0), A.i(0),
+            A.i(int("pressure" in self.record)), A.i(1), A.i(0), A.i(int(self.undo_attenuation)), A.i(0),
         ]
         self.L.prepare_constants_device_(*args)
         abi.check()
