@@ -255,7 +255,7 @@ def aniso_leg(db: dict, cfg: dict, steps: int):
 
 
 def smooth_leg(nx: int = 64, sigma: float = 312.5):
-    """Gaussian smoothing of three kernels over a 64x64x32-element block (312.5 m
+    """Gaussian smoothing of three kernels over an nx x nx x nx/2-element block (312.5 m
     cubes, sigma_h = sigma_v = one element): wall time of prepare / compute / get
     (host binning and copies included) and the point pairs it evaluates."""
     from specfem3d_gb300 import configs, meshgen, smooth as S
@@ -324,6 +324,7 @@ def main():
     ap.add_argument("--aniso", type=int, default=0,
                     help="also time this many steps of the main workload with anisotropic stiffness (0: skip)")
     ap.add_argument("--smooth", action="store_true", help="also time the Gaussian smoothing of three kernels")
+    ap.add_argument("--smooth-nx", type=int, default=64, help="elements along x and y of the smoothing block")
     ap.add_argument("--adjoint", type=int, default=0,
                     help="also time the checkpointed misfit gradient over this many shots of the "
                          "8-shot 64x64x32 gradient workload (0: skip)")
@@ -476,7 +477,7 @@ def main():
     if aniso is not None:
         line["anisotropic"] = aniso
     if args.smooth:
-        line["smoothing"] = smooth_leg()
+        line["smoothing"] = smooth_leg(args.smooth_nx)
     if rank == 0 and not args.no_cpu:
         cv, info = cpu_baseline(args.cpu_steps, os.cpu_count() or 1)
         line["cpu_baseline"] = {"value": cv, "unit": UNIT, "cores": os.cpu_count() or 1, "kind": "port",
