@@ -550,39 +550,19 @@ void transfer_asmbl_pot_to_device_(long *Mesh_pointer, realw *buffer_recv_scalar
 void compute_stacey_viscoelastic_undoatt_cuda_(long *Mesh_pointer, int *iphasef, int *FORWARD_OR_ADJOINT_f);
 void compute_stacey_acoustic_undoatt_cuda_(long *Mesh_pointer, int *iphasef, int *FORWARD_OR_ADJOINT_f);
 
-/* Not provided: each records SF3D_ERR_UNSUPPORTED through sf3d_last_error (acoustic
- * adjoint, noise tomography, C-PML, gravity, ocean load, faults); prepare_fields_gravity_device
- * with GRAVITY = 0 and prepare_fault_device without Kelvin-Voigt damping are accepted no-ops. */
-void add_source_main_rec_noise_cu_(long *Mesh_pointer, int *it_f, int *irec_main_noise_f,
-                                   int *islice_selected_rec);
+/* SIMULATION_TYPE = 3 in fluid elements (prepare_mesh_constants_cuda.cu,
+ * compute_add_sources_acoustic_cuda.cu, compute_kernels_cuda.cu, transfer_fields_cuda.cu):
+ * backward potentials (FORWARD_OR_ADJOINT = 3 on every acoustic entry point, Stacey
+ * record b_absorb_potential(NGLL2, nfaces) stored by SAVE_FORWARD runs and replayed),
+ * adjoint sources of receivers in fluid elements, and the rho / kappa kernels
+ * rho_ac_kl += dt grad(chi_adj).grad(b_chi), kappa_ac_kl += dt chi_adj b_chi_dd
+ * (FP64 accumulators; APPROXIMATE_HESS_KL is not provided in fluid elements). */
 void add_sources_ac_sim_2_or_3_cuda_(long *Mesh_pointer, realw *h_source_adjoint, int *nrec,
                                      int *nadj_rec_local, int *NTSTEP_BETWEEN_READ_ADJSRC, int *it);
 void compute_add_sources_ac_s3_cuda_(long *Mesh_pointer, int *NSOURCESf, double *h_stf_pre_compute,
                                      int *run_number_of_the_source);
-void compute_coupling_ocean_cuda_(long *Mesh_pointer, int *FORWARD_OR_ADJOINT);
 void compute_kernels_acoustic_cuda_(long *Mesh_pointer, realw *deltat_f);
-void compute_kernels_strgth_noise_cu_(long *Mesh_pointer, realw *h_noise_surface_movie, realw *deltat);
-void fault_solver_gpu_(long *Mesh_pointer, long *Fault_pointer, realw *dt, int *it);
-void initialize_fault_data_gpu_(long *Fault_solver, int *fault_index, int *iglob, int *num_of_records,
-                                int *ndat, int *NT_RECORD_LENGTH);
-void initialize_fault_solver_gpu_(long *Fault_solver, int *num_of_faults, realw *v_healing, realw *v_rupt,
-                                  int *RATE_AND_STATE);
-void noise_read_add_surface_movie_cu_(long *Mesh_pointer, realw *h_noise_surface_movie,
-                                      int *NOISE_TOMOGRAPHYf);
-void pml_impose_boundary_condition_elastic_cuda_(long *Mesh_pointer);
-void prepare_fault_device_(long *Mesh_pointer, int *KELVIN_VOIGT_DAMPING, realw *Kelvin_Voigt_eta);
 void prepare_fields_acoustic_adj_dev_(long *Mesh_pointer, int *APPROXIMATE_HESS_KL);
-void prepare_fields_elastic_pml_(long *Mesh_pointer, int *NSPEC_CPML, int *is_CPML, int *CPML_to_spec,
-                                 int *spec_to_CPML, realw *pml_convolution_coef_alpha,
-                                 realw *pml_convolution_coef_beta, realw *pml_convolution_coef_abar,
-                                 realw *pml_convolution_coef_strain, realw *h_wgll_cube, realw *rhostore);
-void prepare_fields_gravity_device_(long *Mesh_pointer, int *GRAVITY, realw *minus_deriv_gravity,
-                                    realw *minus_g, realw *h_wgll_cube, realw *rhostore);
-void prepare_fields_noise_device_(long *Mesh_pointer, int *NSPEC_AB, int *NGLOB_AB, int *free_surface_ispec,
-                                  int *free_surface_ijk, int *num_free_surface_faces, int *NOISE_TOMOGRAPHY,
-                                  int *NSTEP, realw *noise_sourcearray, realw *normal_x_noise,
-                                  realw *normal_y_noise, realw *normal_z_noise, realw *mask_noise,
-                                  realw *free_surface_jacobian2Dw);
 void transfer_b_dot_dot_from_device_(int *size, realw *b_potential_dot_dot_acoustic, long *Mesh_pointer);
 void transfer_b_fields_ac_from_device_(int *size, realw *b_potential_acoustic,
                                        realw *b_potential_dot_acoustic, realw *b_potential_dot_dot_acoustic,
@@ -596,6 +576,39 @@ void transfer_b_potential_dot_dot_ac_from_device_(int *size, realw *b_potential_
                                                   long *Mesh_pointer);
 void transfer_b_potential_dot_dot_ac_to_device_(int *size, realw *b_potential_dot_dot_acoustic,
                                                 long *Mesh_pointer);
+void transfer_kernels_ac_to_host_(long *Mesh_pointer, realw *h_rho_ac_kl, realw *h_kappa_ac_kl,
+                                  int *NSPEC_AB);
+/* FP64 acoustic accumulators, (5,5,5,NSPEC) each (library extension). */
+int sf3d_get_kernels_ac_f64(long *Mesh_pointer, double *h_rho_ac_kl, double *h_kappa_ac_kl);
+
+/* Not provided: each records SF3D_ERR_UNSUPPORTED through sf3d_last_error (acoustic
+ * Hessian kernels, noise tomography, C-PML, gravity, ocean load, faults);
+ * prepare_fields_gravity_device with GRAVITY = 0 and prepare_fault_device without
+ * Kelvin-Voigt damping are accepted no-ops. */
+void add_source_main_rec_noise_cu_(long *Mesh_pointer, int *it_f, int *irec_main_noise_f,
+                                   int *islice_selected_rec);
+void compute_coupling_ocean_cuda_(long *Mesh_pointer, int *FORWARD_OR_ADJOINT);
+void compute_kernels_strgth_noise_cu_(long *Mesh_pointer, realw *h_noise_surface_movie, realw *deltat);
+void fault_solver_gpu_(long *Mesh_pointer, long *Fault_pointer, realw *dt, int *it);
+void initialize_fault_data_gpu_(long *Fault_solver, int *fault_index, int *iglob, int *num_of_records,
+                                int *ndat, int *NT_RECORD_LENGTH);
+void initialize_fault_solver_gpu_(long *Fault_solver, int *num_of_faults, realw *v_healing, realw *v_rupt,
+                                  int *RATE_AND_STATE);
+void noise_read_add_surface_movie_cu_(long *Mesh_pointer, realw *h_noise_surface_movie,
+                                      int *NOISE_TOMOGRAPHYf);
+void pml_impose_boundary_condition_elastic_cuda_(long *Mesh_pointer);
+void prepare_fault_device_(long *Mesh_pointer, int *KELVIN_VOIGT_DAMPING, realw *Kelvin_Voigt_eta);
+void prepare_fields_elastic_pml_(long *Mesh_pointer, int *NSPEC_CPML, int *is_CPML, int *CPML_to_spec,
+                                 int *spec_to_CPML, realw *pml_convolution_coef_alpha,
+                                 realw *pml_convolution_coef_beta, realw *pml_convolution_coef_abar,
+                                 realw *pml_convolution_coef_strain, realw *h_wgll_cube, realw *rhostore);
+void prepare_fields_gravity_device_(long *Mesh_pointer, int *GRAVITY, realw *minus_deriv_gravity,
+                                    realw *minus_g, realw *h_wgll_cube, realw *rhostore);
+void prepare_fields_noise_device_(long *Mesh_pointer, int *NSPEC_AB, int *NGLOB_AB, int *free_surface_ispec,
+                                  int *free_surface_ijk, int *num_free_surface_faces, int *NOISE_TOMOGRAPHY,
+                                  int *NSTEP, realw *noise_sourcearray, realw *normal_x_noise,
+                                  realw *normal_y_noise, realw *normal_z_noise, realw *mask_noise,
+                                  realw *free_surface_jacobian2Dw);
 void transfer_datat_to_host_(long *Fault_pointer, int *fault_index, realw *h_dataT, int *it_in);
 void transfer_fault_data_to_device_(long *Fault_pointer, int *fault_index, int *NSPEC_FLT, int *NGLOB_FLT,
                                     realw *D, realw *T0, realw *T, realw *B, realw *R, realw *V0, realw *Z,
@@ -603,8 +616,6 @@ void transfer_fault_data_to_device_(long *Fault_pointer, int *fault_index, int *
                                     int *allow_opening);
 void transfer_fault_data_to_host_(long *Fault_pointer, int *fault_index, int *NSPEC_FLT, int *NGLOB_FLT,
                                   realw *D, realw *V, realw *T);
-void transfer_kernels_ac_to_host_(long *Mesh_pointer, realw *h_rho_ac_kl, realw *h_kappa_ac_kl,
-                                  int *NSPEC_AB);
 void transfer_kernels_hess_ac_tohost_(long *Mesh_pointer, realw *h_hess_ac_kl, realw *h_hess_rho_ac_kl,
                                       realw *h_hess_kappa_ac_kl, int *NSPEC_AB);
 void transfer_kernels_noise_to_host_(long *Mesh_pointer, realw *h_sigma_kl, int *NSPEC_AB);

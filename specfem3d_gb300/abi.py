@@ -117,6 +117,8 @@ def load() -> ctypes.CDLL:
     L.sf3d_check_stability.argtypes = [P, ctypes.c_float, P]
     L.sf3d_get_kernels_f64.restype = ctypes.c_int
     L.sf3d_get_kernels_f64.argtypes = [P, P, P, P]
+    L.sf3d_get_kernels_ac_f64.restype = ctypes.c_int
+    L.sf3d_get_kernels_ac_f64.argtypes = [P, P, P]
     _LIB = L
     return L
 

@@ -99,6 +99,120 @@ def kernel_run(db: dict, cfg: dict, adjoint_source: np.ndarray, final_fields, ab
     return _kernels_f64(g)
 
 
+def forward_with_boundary_record_coupled(db: dict, cfg: dict):
+    """SIMULATION_TYPE = 1 with SAVE_FORWARD on a fluid-solid mesh: (seismograms,
+    final elastic (displ, veloc, accel), final potentials (chi, chi_dot, chi_dot_dot),
+    elastic boundary record (nstep, 75 nfaces), acoustic boundary record
+    b_absorb_potential (nstep, 25 nfaces)); records are None without Stacey faces."""
+    cfg = dict(cfg)
+    nstep = int(cfg["nstep"])
+    g = GPUSolver(db, cfg, nlength=nstep, save_forward=True)
+    nf = int(db["num_abs_boundary_faces"]) if int(db.get("stacey", 0)) else 0
+    g.absorb_record = np.zeros((nstep, 75 * nf), np.float32) if nf else None
+    g.absorb_record_ac = np.zeros((nstep, 25 * nf), np.float32) if nf else None
+    g.run_per_call(nstep)
+    out = (g.seismograms(), g.fields(), g.potentials(), g.absorb_record, g.absorb_record_ac)
+    g.close()
+    return out
+
+
+def kernel_run_coupled(db: dict, cfg: dict, adjoint_source: np.ndarray, final_el, final_ac, rec_el, rec_ac,
+                       history=None):
+    """The SIMULATION_TYPE = 3 run on a fluid-solid mesh (iterate_time.F90:219-330):
+    per step the adjoint potentials and displacement (compute_forces_acoustic_
+    forward_calling, then compute_forces_viscoelastic_calling: Stacey, coupling with
+    the adjoint sign, adjoint sources of the receivers of each domain), then the
+    backward potentials and displacement with b_deltat = -DT (the two boundary
+    records replayed in reverse, coupling on the b_ fields, the sources at
+    (NSTEP - it) DT - t0), both backward fields replaced by the saved final state
+    after the first step, and the elastic and acoustic kernels accumulated.
+    history: optional list receiving, after each step, a dict with the adjoint
+    potential and its second derivative (chi, chi_dd) and the backward ones
+    (b_chi, b_chi_dd).
+    Returns the raw FP64 accumulators rho, mu, kappa (solid) and rho_ac, kappa_ac
+    (fluid), each (nspec, 125)."""
+    if int(db.get("attenuation", 0)):
+        raise ValueError("kernel_run_coupled: the time-reversed reconstruction is for meshes without attenuation")
+    nstep = int(cfg["nstep"])
+    g = GPUSolver(db, cfg, nlength=nstep, simulation_type=3)
+    L = g.L
+    n3, n1 = 3 * g.nglob, g.nglob
+    _prepare_adjoint(g, db, nstep)
+    A = abi.Args()
+    L.prepare_fields_acoustic_adj_dev_(g.mp, A.i(0))
+    abi.check()
+    nrec = g.nrec
+    src = np.ascontiguousarray(np.asarray(adjoint_source, np.float32).transpose(2, 0, 1))
+    stf = np.asarray(db["stf"], np.float64).reshape(g.nsources, -1)
+    dt = np.float32(cfg["dt"])
+    dt2, dtsq2 = np.float32(dt / np.float32(2)), np.float32(dt * dt / np.float32(2))
+    bdt, bdt2 = np.float32(-dt), np.float32(-dt / np.float32(2))
+    fin_el = [np.ascontiguousarray(f, np.float32) for f in final_el]
+    fin_ac = [np.ascontiguousarray(f, np.float32) for f in final_ac]
+    nac = g.nspec_acoustic
+    for it in range(1, nstep + 1):
+        B = abi.Args()
+        one, three, zero = B.i(1), B.i(3), B.i(0)
+        L.update_displacement_cuda_(g.mp, B.f(dt), B.f(dt2), B.f(dtsq2), one)
+        L.update_displacement_ac_cuda_(g.mp, B.f(dt), B.f(dt2), B.f(dtsq2), one)
+        L.update_displacement_cuda_(g.mp, B.f(bdt), B.f(bdt2), B.f(dtsq2), three)
+        L.update_displacement_ac_cuda_(g.mp, B.f(bdt), B.f(bdt2), B.f(dtsq2), three)
+        for fa, d, d2 in ((one, dt, dt2), (three, bdt, bdt2)):
+            backward = fa is three
+            # acoustic domain (compute_forces_acoustic_forward/backward_calling)
+            L.acoustic_enforce_free_surf_cuda_(g.mp, zero, fa)
+            for iphase in (1, 2):
+                L.compute_forces_acoustic_cuda_(g.mp, B.i(iphase), zero, B.i(nac), fa)
+                if iphase == 1:
+                    rec = B.af(rec_ac[nstep - it]) if (backward and rec_ac is not None) else None
+                    L.compute_stacey_acoustic_cuda_(g.mp, one, rec, fa)
+                    L.compute_coupling_ac_el_cuda_(g.mp, one, B.i(g.ncoupling), fa)
+                    if backward:
+                        if g.nsources:
+                            L.compute_add_sources_ac_s3_cuda_(g.mp, B.i(g.nsources),
+                                                              B.ad(np.ascontiguousarray(stf[:, nstep - it])), one)
+                    elif it < nstep:
+                        L.add_sources_ac_sim_2_or_3_cuda_(g.mp, B.af(src), B.i(nrec), B.i(nrec), B.i(nstep), B.i(it))
+            L.kernel_3_acoustic_cuda_(g.mp, B.f(dt2), B.f(bdt2), fa)
+            L.acoustic_enforce_free_surf_cuda_(g.mp, zero, fa)
+            # elastic domain (compute_forces_viscoelastic_calling / _backward_calling)
+            for iphase in (1, 2):
+                L.compute_forces_viscoelastic_cuda_(g.mp, B.i(iphase), B.f(d), B.i(g.nspec_outer),
+                                                    B.i(g.nspec_elastic), one, zero, fa)
+                if iphase == 1:
+                    rec = B.af(rec_el[nstep - it]) if (backward and rec_el is not None) else None
+                    L.compute_stacey_viscoelastic_cuda_(g.mp, one, rec, fa)
+                    L.compute_coupling_el_ac_cuda_(g.mp, one, B.i(g.ncoupling), fa)
+                    if backward:
+                        if g.nsources:
+                            L.compute_add_sources_el_s3_cuda_(g.mp, B.ad(np.ascontiguousarray(stf[:, nstep - it])),
+                                                              B.i(g.nsources))
+                    elif it < nstep:
+                        L.add_sources_el_sim_type_2_or_3_(g.mp, B.af(src), B.i(nrec), B.i(nrec), B.i(nstep), B.i(it))
+            L.kernel_3_a_cuda_(g.mp, B.f(dt2), B.f(bdt2), zero, fa)
+        if it == 1:
+            # read_forward_arrays: both backward fields start from the saved final state
+            L.transfer_b_fields_to_device_(B.i(n3), *(B.af(f) for f in fin_el), g.mp)
+            L.transfer_b_fields_ac_to_device_(B.i(n1), *(B.af(f) for f in fin_ac), g.mp)
+        L.compute_kernels_elastic_cuda_(g.mp, B.f(dt))
+        L.compute_kernels_acoustic_cuda_(g.mp, B.f(dt))
+        if history is not None:
+            h = {k: np.zeros(n1, np.float32) for k in ("chi", "chi_dd", "b_chi", "b_chi_dd")}
+            L.transfer_fields_ac_from_device_(B.i(n1), h["chi"].ctypes.data, None, h["chi_dd"].ctypes.data, g.mp)
+            L.transfer_b_fields_ac_from_device_(B.i(n1), h["b_chi"].ctypes.data, None, h["b_chi_dd"].ctypes.data,
+                                                g.mp)
+            h["it"] = it
+            history.append(h)
+    abi.check()
+    n = g.nspec
+    ac = {k: np.zeros(n * NGLL3) for k in ("rho_ac", "kappa_ac")}
+    if L.sf3d_get_kernels_ac_f64(g.mp, ac["rho_ac"].ctypes.data, ac["kappa_ac"].ctypes.data) != 0:
+        abi.check()
+    out = _kernels_f64(g)
+    out.update({k: v.reshape(n, NGLL3) for k, v in ac.items()})
+    return out
+
+
 def _prepare_adjoint(g: GPUSolver, db: dict, nstep: int):
     """prepare_fields_elastic_adj_dev (backward fields, kernel accumulators and, with
     attenuation, the backward memory variables with the forward-time coefficients

@@ -11,9 +11,9 @@
 // * acoustic MPI interface pack / assembly (transfer_boun_pot_from_device,
 //   transfer_asmbl_pot_to_device);
 // * Stacey of a recomputed backward field (*_undoatt_cuda);
-// * features this library does not provide (acoustic adjoint runs, noise
-//   tomography, faults, C-PML, gravity, ocean load): the call records an error
-//   status (sf3d_last_error) and does nothing else.
+// * features this library does not provide (acoustic Hessian kernels, noise
+//   tomography, faults, C-PML, gravity, ocean load): the call records
+//   SF3D_ERR_UNSUPPORTED (sf3d_last_error) and does nothing else.
 #include <stdarg.h>
 #include <stdio.h>
 #include <stdlib.h>
@@ -188,10 +188,10 @@ void get_norm_elastic_from_device_(realw* norm, long* Mesh_pointer, int* type) {
 void get_norm_acoustic_from_device_(realw* norm, long* Mesh_pointer, int* sim_type) {
   Mesh* mp = get_mesh(Mesh_pointer);
   if (!mp) return;
-  if (sim_type && *sim_type == 3) { unsupported("the backward acoustic field"); return; }
+  const float* d = (sim_type && *sim_type == 3) ? mp->d_b_potential_dot_dot : mp->d_potential_dot_dot;
   float m = 0.f;
-  if (!mp->d_potential_dot_dot) { set_error(SF3D_ERR_STATE, "acoustic fields not prepared"); return; }
-  if (!device_maxabs(mp, mp->d_potential_dot_dot, (long)mp->nglob, &m)) return;
+  if (!d) { set_error(SF3D_ERR_STATE, "acoustic fields not prepared"); return; }
+  if (!device_maxabs(mp, d, (long)mp->nglob, &m)) return;
   *norm = m;
 }
 void get_free_device_memory_(realw* free_mb, realw* used_mb, realw* total_mb) {
@@ -338,12 +338,12 @@ void transfer_boun_pot_from_device_(long* Mesh_pointer, realw* send_potential_do
                                     const int* FORWARD_OR_ADJOINT) {
   Mesh* mp = get_mesh(Mesh_pointer);
   if (!mp) return;
-  if (FORWARD_OR_ADJOINT && *FORWARD_OR_ADJOINT == 3) { unsupported("the backward acoustic field"); return; }
+  float* pdd = (FORWARD_OR_ADJOINT && *FORWARD_OR_ADJOINT == 3) ? mp->d_b_potential_dot_dot : mp->d_potential_dot_dot;
   const long n = (long)mp->num_interfaces * mp->max_nibool_interfaces;
   if (n == 0) return;
-  if (!mp->d_potential_dot_dot) { set_error(SF3D_ERR_STATE, "acoustic fields not prepared"); return; }
+  if (!pdd) { set_error(SF3D_ERR_STATE, "acoustic fields not prepared"); return; }
   if (!ensure_stage(mp, sizeof(float) * n)) return;
-  pack_scalar_kernel<<<nblk(n, 128), 128, 0, mp->stream>>>(mp->d_potential_dot_dot, mp->d_stage, mp->num_interfaces,
+  pack_scalar_kernel<<<nblk(n, 128), 128, 0, mp->stream>>>(pdd, mp->d_stage, mp->num_interfaces,
                                                            mp->max_nibool_interfaces, mp->d_nibool_interfaces,
                                                            mp->d_ibool_interfaces);
   if (!cuda_ok(cudaGetLastError(), "pack_scalar_kernel")) return;
@@ -353,13 +353,13 @@ void transfer_asmbl_pot_to_device_(long* Mesh_pointer, realw* buffer_recv_scalar
                                    const int* FORWARD_OR_ADJOINT) {
   Mesh* mp = get_mesh(Mesh_pointer);
   if (!mp) return;
-  if (FORWARD_OR_ADJOINT && *FORWARD_OR_ADJOINT == 3) { unsupported("the backward acoustic field"); return; }
+  float* pdd = (FORWARD_OR_ADJOINT && *FORWARD_OR_ADJOINT == 3) ? mp->d_b_potential_dot_dot : mp->d_potential_dot_dot;
   const long n = (long)mp->num_interfaces * mp->max_nibool_interfaces;
   if (n == 0) return;
-  if (!mp->d_potential_dot_dot) { set_error(SF3D_ERR_STATE, "acoustic fields not prepared"); return; }
+  if (!pdd) { set_error(SF3D_ERR_STATE, "acoustic fields not prepared"); return; }
   if (!ensure_stage(mp, sizeof(float) * n)) return;
   if (!copy_sync(mp->d_stage, buffer_recv_scalar_ext_mesh, sizeof(float) * n, cudaMemcpyHostToDevice, mp->stream)) return;
-  add_scalar_kernel<<<nblk(n, 128), 128, 0, mp->stream>>>(mp->d_potential_dot_dot, mp->d_stage, mp->num_interfaces,
+  add_scalar_kernel<<<nblk(n, 128), 128, 0, mp->stream>>>(pdd, mp->d_stage, mp->num_interfaces,
                                                           mp->max_nibool_interfaces, mp->d_nibool_interfaces,
                                                           mp->d_ibool_interfaces);
   cuda_ok(cudaGetLastError(), "add_scalar_kernel");
@@ -371,58 +371,15 @@ void compute_stacey_viscoelastic_undoatt_cuda_(long* Mesh_pointer, int* iphasef,
   compute_stacey_viscoelastic_cuda_(Mesh_pointer, iphasef, nullptr, FORWARD_OR_ADJOINT_f);
 }
 void compute_stacey_acoustic_undoatt_cuda_(long* Mesh_pointer, int* iphasef, int* FORWARD_OR_ADJOINT_f) {
-  if (FORWARD_OR_ADJOINT_f && *FORWARD_OR_ADJOINT_f != 1) { unsupported("the backward acoustic field"); return; }
   compute_stacey_acoustic_cuda_(Mesh_pointer, iphasef, nullptr, FORWARD_OR_ADJOINT_f);
 }
 
 // ---------------------------------------------------------------- not provided
-// acoustic adjoint (SIMULATION_TYPE = 3 in fluid elements)
-void prepare_fields_acoustic_adj_dev_(long* Mesh_pointer, int* APPROXIMATE_HESS_KL) {
-  (void)Mesh_pointer; (void)APPROXIMATE_HESS_KL;
-  unsupported("the acoustic adjoint simulation (prepare_fields_acoustic_adj_dev)");
-}
-void add_sources_ac_sim_2_or_3_cuda_(long* Mesh_pointer, realw* h_source_adjoint, int* nrec, int* nadj_rec_local,
-                                     int* NTSTEP_BETWEEN_READ_ADJSRC, int* it) {
-  (void)Mesh_pointer; (void)h_source_adjoint; (void)nrec; (void)nadj_rec_local; (void)NTSTEP_BETWEEN_READ_ADJSRC;
-  (void)it;
-  unsupported("acoustic adjoint sources (add_sources_ac_sim_2_or_3_cuda)");
-}
-void compute_add_sources_ac_s3_cuda_(long* Mesh_pointer, int* NSOURCESf, double* h_stf_pre_compute,
-                                     int* run_number_of_the_source) {
-  (void)Mesh_pointer; (void)NSOURCESf; (void)h_stf_pre_compute; (void)run_number_of_the_source;
-  unsupported("backward acoustic sources (compute_add_sources_ac_s3_cuda)");
-}
-void compute_kernels_acoustic_cuda_(long* Mesh_pointer, realw* deltat_f) {
-  (void)Mesh_pointer; (void)deltat_f;
-  unsupported("acoustic sensitivity kernels (compute_kernels_acoustic_cuda)");
-}
-void transfer_kernels_ac_to_host_(long* Mesh_pointer, realw* h_rho_ac_kl, realw* h_kappa_ac_kl, int* NSPEC_AB) {
-  (void)Mesh_pointer; (void)h_rho_ac_kl; (void)h_kappa_ac_kl; (void)NSPEC_AB;
-  unsupported("acoustic sensitivity kernels (transfer_kernels_ac_to_host)");
-}
+// acoustic Hessian kernels (APPROXIMATE_HESS_KL in fluid elements)
 void transfer_kernels_hess_ac_tohost_(long* Mesh_pointer, realw* h_hess_ac_kl, realw* h_hess_rho_ac_kl,
                                       realw* h_hess_kappa_ac_kl, int* NSPEC_AB) {
   (void)Mesh_pointer; (void)h_hess_ac_kl; (void)h_hess_rho_ac_kl; (void)h_hess_kappa_ac_kl; (void)NSPEC_AB;
   unsupported("acoustic Hessian kernels (transfer_kernels_hess_ac_tohost)");
-}
-#define SF3D_NO_B_ACOUSTIC(name)                                                   \
-  void name(int* size, realw* a, long* Mesh_pointer) {                             \
-    (void)size; (void)a; (void)Mesh_pointer;                                       \
-    unsupported("the backward acoustic field (" #name ")");                        \
-  }
-SF3D_NO_B_ACOUSTIC(transfer_b_potential_ac_from_device_)
-SF3D_NO_B_ACOUSTIC(transfer_b_potential_ac_to_device_)
-SF3D_NO_B_ACOUSTIC(transfer_b_potential_dot_dot_ac_from_device_)
-SF3D_NO_B_ACOUSTIC(transfer_b_potential_dot_dot_ac_to_device_)
-SF3D_NO_B_ACOUSTIC(transfer_b_dot_dot_from_device_)
-#undef SF3D_NO_B_ACOUSTIC
-void transfer_b_fields_ac_from_device_(int* size, realw* p, realw* pd, realw* pdd, long* Mesh_pointer) {
-  (void)size; (void)p; (void)pd; (void)pdd; (void)Mesh_pointer;
-  unsupported("the backward acoustic field (transfer_b_fields_ac_from_device)");
-}
-void transfer_b_fields_ac_to_device_(int* size, realw* p, realw* pd, realw* pdd, long* Mesh_pointer) {
-  (void)size; (void)p; (void)pd; (void)pdd; (void)Mesh_pointer;
-  unsupported("the backward acoustic field (transfer_b_fields_ac_to_device)");
 }
 
 // noise tomography

@@ -18,6 +18,29 @@ namespace {
 
 inline unsigned nblk(long n, int b) { return (unsigned)((n + b - 1) / b); }
 
+struct Metric9 {
+  const float* p[9];
+};
+
+// FORWARD_OR_ADJOINT 1: the forward (adjoint, in a kernel run) potentials;
+// 3: the backward / reconstructed potentials of SIMULATION_TYPE = 3
+struct AcField {
+  float* p;
+  float* pd;
+  float* pdd;
+};
+
+bool ac_field(Mesh* mp, const int* fa, AcField* F) {
+  if (!fa || (*fa != 1 && *fa != 3)) return set_error(SF3D_ERR_ARG, "FORWARD_OR_ADJOINT must be 1 or 3 for acoustic fields");
+  if (*fa == 1) {
+    *F = {mp->d_potential, mp->d_potential_dot, mp->d_potential_dot_dot};
+    return true;
+  }
+  if (!mp->d_b_potential) return set_error(SF3D_ERR_STATE, "prepare_fields_acoustic_adj_dev not called");
+  *F = {mp->d_b_potential, mp->d_b_potential_dot, mp->d_b_potential_dot_dot};
+  return true;
+}
+
 // chi_dot_dot -= w . hprimewgll^T ( J/rho grad(xi) . grad chi )
 // (compute_forces_acoustic.F90:130-340); one 128-thread CTA per element.
 __global__ void __launch_bounds__(NGLL3_PAD, 8)
@@ -102,7 +125,7 @@ __global__ void stacey_acoustic_kernel(int nfaces, const int* __restrict__ abs_i
                                        const float* __restrict__ jw, const int* __restrict__ is_acoustic,
                                        const int* __restrict__ ibool, const float* __restrict__ rhostore,
                                        const float* __restrict__ kappav, const float* __restrict__ pot_dot,
-                                       float* __restrict__ pot_dd) {
+                                       float* __restrict__ pot_dd, float* __restrict__ record) {
   long idx = (long)blockIdx.x * blockDim.x + threadIdx.x;
   if (idx >= (long)nfaces * NGLL2) return;
   const int e = abs_ispec[idx / NGLL2];
@@ -111,7 +134,82 @@ __global__ void stacey_acoustic_kernel(int nfaces, const int* __restrict__ abs_i
   const int g = ibool[q];
   const float rhol = rhostore[q];
   const float cpl = sqrtf(kappav[q] / rhol);
-  atomicAdd(pot_dd + g, -(pot_dot[g] * jw[idx] / cpl / rhol));
+  const float absorbl = pot_dot[g] / rhol * jw[idx] / cpl;
+  atomicAdd(pot_dd + g, -absorbl);
+  // SAVE_FORWARD: b_absorb_potential(NGLL2, nfaces) of this step
+  if (record) record[idx] = absorbl;
+}
+
+// replay of the boundary record on the backward potentials
+// (kernels/compute_stacey_acoustic_kernel.cu, SIMULATION_TYPE = 3)
+__global__ void stacey_acoustic_replay_kernel(int nfaces, const int* __restrict__ abs_ispec,
+                                              const int* __restrict__ abs_pt, const int* __restrict__ is_acoustic,
+                                              const int* __restrict__ ibool, const float* __restrict__ record,
+                                              float* __restrict__ pot_dd) {
+  long idx = (long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (idx >= (long)nfaces * NGLL2) return;
+  const int e = abs_ispec[idx / NGLL2];
+  if (!is_acoustic[e]) return;
+  atomicAdd(pot_dd + ibool[(long)e * NGLL3_PAD + abs_pt[idx]], -record[idx]);
+}
+
+// acoustic kernels (compute_kernels.f90:257-330, kernels/compute_kernels_acoustic_kernel.cu):
+// rho_ac_kl += dt grad(chi_adj) . grad(b_chi), kappa_ac_kl += dt chi_adj b_chi_dd;
+// the 1/rho of the reference's gradient routine is undone there by rho, so the
+// plain gradients are used; FP64 accumulators
+__global__ void __launch_bounds__(NGLL3_PAD)
+    kernels_acoustic_kernel(long nspec, const int* __restrict__ is_acoustic, const int* __restrict__ ibool,
+                            const int* __restrict__ irregular, Metric9 m, const float* __restrict__ gll,
+                            float xix_regular, const float* __restrict__ pot, const float* __restrict__ b_pot,
+                            const float* __restrict__ b_pot_dd, double dt, double* __restrict__ rho_kl,
+                            double* __restrict__ kappa_kl) {
+  __shared__ float s_a[NGLL3_PAD];
+  __shared__ float s_b[NGLL3_PAD];
+  __shared__ float s_hp[NGLL2];
+  const long e = blockIdx.x;
+  const int t = threadIdx.x;
+  if (e >= nspec || !is_acoustic[e]) return;
+  const bool active = t < NGLL3;
+  const long eo = e * NGLL3_PAD + t;
+  const int g = active ? ibool[eo] : 0;
+  if (t < NGLL2) s_hp[t] = gll[t];
+  s_a[t] = active ? pot[g] : 0.f;
+  s_b[t] = active ? b_pot[g] : 0.f;
+  __syncthreads();
+  if (!active) return;
+  const int k = t / NGLL2, j = (t / NGLLX) % NGLLX, i = t % NGLLX;
+  float da[3] = {0.f, 0.f, 0.f}, db[3] = {0.f, 0.f, 0.f};
+#pragma unroll
+  for (int l = 0; l < NGLLX; ++l) {
+    const float h1 = s_hp[i + NGLLX * l], h2 = s_hp[j + NGLLX * l], h3 = s_hp[k + NGLLX * l];
+    da[0] = fmaf(s_a[l + NGLLX * j + NGLL2 * k], h1, da[0]);
+    da[1] = fmaf(s_a[i + NGLLX * l + NGLL2 * k], h2, da[1]);
+    da[2] = fmaf(s_a[i + NGLLX * j + NGLL2 * l], h3, da[2]);
+    db[0] = fmaf(s_b[l + NGLLX * j + NGLL2 * k], h1, db[0]);
+    db[1] = fmaf(s_b[i + NGLLX * l + NGLL2 * k], h2, db[1]);
+    db[2] = fmaf(s_b[i + NGLLX * j + NGLL2 * l], h3, db[2]);
+  }
+  float ga[3], gb[3];
+  const int ir = irregular[e];
+  if (ir >= 0) {
+    const long mo = (long)ir * NGLL3_PAD + t;
+    float mm[9];
+#pragma unroll
+    for (int q = 0; q < 9; ++q) mm[q] = m.p[q][mo];
+#pragma unroll
+    for (int c = 0; c < 3; ++c) {
+      ga[c] = mm[c] * da[0] + mm[3 + c] * da[1] + mm[6 + c] * da[2];
+      gb[c] = mm[c] * db[0] + mm[3 + c] * db[1] + mm[6 + c] * db[2];
+    }
+  } else {
+#pragma unroll
+    for (int c = 0; c < 3; ++c) {
+      ga[c] = xix_regular * da[c];
+      gb[c] = xix_regular * db[c];
+    }
+  }
+  rho_kl[eo] += dt * ((double)ga[0] * gb[0] + (double)ga[1] * gb[1] + (double)ga[2] * gb[2]);
+  kappa_kl[eo] += dt * ((double)pot[g] * b_pot_dd[g]);
 }
 
 // chi_dd += jw (u . n)   (compute_coupling_acoustic_el.f90:70-150)
@@ -275,7 +373,7 @@ int enqueue_acoustic_step(Mesh* mp, float dt, float dt2, float dtsq2) {
     stacey_acoustic_kernel<<<nblk(nf, 128), 128, 0, s>>>(mp->num_abs_faces, mp->d_abs_ispec, mp->d_abs_pt,
                                                           mp->d_abs_jw, mp->d_ispec_is_acoustic, mp->d_ibool,
                                                           mp->d_rhostore, mp->d_kappav, mp->d_potential_dot,
-                                                          mp->d_potential_dot_dot);
+                                                          mp->d_potential_dot_dot, nullptr);
     ++launches;
   }
   if (mp->num_coupling_faces > 0) {
@@ -409,7 +507,8 @@ void compute_forces_acoustic_cuda_(long* Mesh_pointer, int* iphase, int* nspec_o
   Mesh* mp = get_mesh(Mesh_pointer);
   if (!mp) return;
   if (!mp->has_acoustic) { set_error(SF3D_ERR_STATE, "prepare_fields_acoustic_device not called"); return; }
-  if (*FORWARD_OR_ADJOINT_f != 1) { set_error(SF3D_ERR_ARG, "acoustic adjoint fields are not supported"); return; }
+  AcField F;
+  if (!ac_field(mp, FORWARD_OR_ADJOINT_f, &F)) return;
   mp->nspec_outer_ac = *nspec_outer_acoustic;
   mp->nspec_inner_ac = *nspec_inner_acoustic;
   const int nel = *iphase == 1 ? mp->nspec_outer_ac : mp->nspec_inner_ac;
@@ -423,58 +522,81 @@ void compute_forces_acoustic_cuda_(long* Mesh_pointer, int* iphase, int* nspec_o
   acoustic_stiffness_kernel<<<nel, NGLL3_PAD, 0, mp->stream>>>(
       nel, ph, mp->d_ibool, mp->d_irregular, mp->d_metric[0], mp->d_metric[1], mp->d_metric[2], mp->d_metric[3],
       mp->d_metric[4], mp->d_metric[5], mp->d_metric[6], mp->d_metric[7], mp->d_metric[8], mp->d_rhostore, mp->d_gll,
-      mp->xix_regular, mp->jacobian_regular, mp->d_potential, mp->d_potential_dot_dot);
+      mp->xix_regular, mp->jacobian_regular, F.p, F.pdd);
   cuda_ok(cudaGetLastError(), "acoustic_stiffness_kernel");
 }
 
 void acoustic_enforce_free_surf_cuda_(long* Mesh_pointer, int* ABSORB_INSTEAD_OF_FREE_SURFACE,
                                       int* FORWARD_OR_ADJOINT) {
-  (void)FORWARD_OR_ADJOINT;
   Mesh* mp = get_mesh(Mesh_pointer);
   if (!mp || !mp->has_acoustic) return;
+  AcField F;
+  if (!ac_field(mp, FORWARD_OR_ADJOINT, &F)) return;
   if (*ABSORB_INSTEAD_OF_FREE_SURFACE || mp->num_free_surface_faces == 0) return;
   const long n = (long)mp->num_free_surface_faces * NGLL2;
   free_surface_kernel<<<nblk(n, 128), 128, 0, mp->stream>>>(mp->num_free_surface_faces, mp->d_fs_ispec, mp->d_fs_pt,
-                                                             mp->d_ispec_is_acoustic, mp->d_ibool, mp->d_potential,
-                                                             mp->d_potential_dot, mp->d_potential_dot_dot);
+                                                             mp->d_ispec_is_acoustic, mp->d_ibool, F.p, F.pd, F.pdd);
   cuda_ok(cudaGetLastError(), "free_surface_kernel");
 }
 
 void update_displacement_ac_cuda_(long* Mesh_pointer, realw* deltat_F, realw* deltatover2_F, realw* deltatsqover2_F,
                                   int* FORWARD_OR_ADJOINT) {
-  (void)FORWARD_OR_ADJOINT;
   Mesh* mp = get_mesh(Mesh_pointer);
   if (!mp || !mp->has_acoustic) return;
+  AcField F;
+  if (!ac_field(mp, FORWARD_OR_ADJOINT, &F)) return;
   const long n = mp->nglob;
-  predictor_scalar_kernel<<<nblk(n, 256), 256, 0, mp->stream>>>(mp->d_potential, mp->d_potential_dot,
-                                                                mp->d_potential_dot_dot, n, *deltat_F, *deltatover2_F,
+  predictor_scalar_kernel<<<nblk(n, 256), 256, 0, mp->stream>>>(F.p, F.pd, F.pdd, n, *deltat_F, *deltatover2_F,
                                                                 *deltatsqover2_F);
   cuda_ok(cudaGetLastError(), "predictor_scalar_kernel");
 }
 
 void kernel_3_acoustic_cuda_(long* Mesh_pointer, realw* deltatover2_F, realw* b_deltatover2_F,
                              int* FORWARD_OR_ADJOINT_f) {
-  (void)b_deltatover2_F; (void)FORWARD_OR_ADJOINT_f;
   Mesh* mp = get_mesh(Mesh_pointer);
   if (!mp || !mp->has_acoustic) return;
+  AcField F;
+  if (!ac_field(mp, FORWARD_OR_ADJOINT_f, &F)) return;
+  const float dt2 = *FORWARD_OR_ADJOINT_f == 3 ? *b_deltatover2_F : *deltatover2_F;
   const long n = mp->nglob;
-  mass_corrector_scalar_kernel<<<nblk(n, 256), 256, 0, mp->stream>>>(mp->d_potential_dot, mp->d_potential_dot_dot,
-                                                                     mp->d_rmass_acoustic, n, *deltatover2_F);
+  mass_corrector_scalar_kernel<<<nblk(n, 256), 256, 0, mp->stream>>>(F.pd, F.pdd, mp->d_rmass_acoustic, n, dt2);
   cuda_ok(cudaGetLastError(), "mass_corrector_scalar_kernel");
 }
 
 void compute_stacey_acoustic_cuda_(long* Mesh_pointer, int* iphasef, realw* h_b_absorb_potential,
                                    int* FORWARD_OR_ADJOINT_f) {
-  (void)h_b_absorb_potential; (void)FORWARD_OR_ADJOINT_f;
   Mesh* mp = get_mesh(Mesh_pointer);
   if (!mp || !mp->has_acoustic) return;
+  AcField F;
+  if (!ac_field(mp, FORWARD_OR_ADJOINT_f, &F)) return;
   if (*iphasef != 1 || !mp->stacey || mp->num_abs_faces == 0) return;
   const long n = (long)mp->num_abs_faces * NGLL2;
+  const bool backward = *FORWARD_OR_ADJOINT_f == 3;
+  if (backward && h_b_absorb_potential && mp->simulation_type == 3) {
+    // replay of b_absorb_potential stored by the SAVE_FORWARD run
+    if (!ensure_stage(mp, sizeof(float) * n)) return;
+    SF3D_CUDA(cudaMemcpyAsync(mp->d_stage, h_b_absorb_potential, sizeof(float) * n, cudaMemcpyHostToDevice,
+                              mp->stream));
+    stacey_acoustic_replay_kernel<<<nblk(n, 128), 128, 0, mp->stream>>>(mp->num_abs_faces, mp->d_abs_ispec,
+                                                                         mp->d_abs_pt, mp->d_ispec_is_acoustic,
+                                                                         mp->d_ibool, mp->d_stage, F.pdd);
+    cuda_ok(cudaGetLastError(), "stacey_acoustic_replay_kernel");
+    return;
+  }
+  // forward, adjoint, or a recomputed backward field (undo attenuation)
+  const bool store = !backward && mp->save_forward && mp->simulation_type == 1 && h_b_absorb_potential;
+  if (store && !ensure_stage(mp, sizeof(float) * n)) return;
+  if (store) SF3D_CUDA(cudaMemsetAsync(mp->d_stage, 0, sizeof(float) * n, mp->stream));
   stacey_acoustic_kernel<<<nblk(n, 128), 128, 0, mp->stream>>>(mp->num_abs_faces, mp->d_abs_ispec, mp->d_abs_pt,
                                                                 mp->d_abs_jw, mp->d_ispec_is_acoustic, mp->d_ibool,
-                                                                mp->d_rhostore, mp->d_kappav, mp->d_potential_dot,
-                                                                mp->d_potential_dot_dot);
-  cuda_ok(cudaGetLastError(), "stacey_acoustic_kernel");
+                                                                mp->d_rhostore, mp->d_kappav, F.pd, F.pdd,
+                                                                store ? mp->d_stage : nullptr);
+  if (!cuda_ok(cudaGetLastError(), "stacey_acoustic_kernel")) return;
+  if (store) {
+    SF3D_CUDA(cudaMemcpyAsync(h_b_absorb_potential, mp->d_stage, sizeof(float) * n, cudaMemcpyDeviceToHost,
+                              mp->stream));
+    SF3D_CUDA(cudaStreamSynchronize(mp->stream));
+  }
 }
 
 void compute_coupling_ac_el_cuda_(long* Mesh_pointer, int* iphasef, int* num_coupling_ac_el_facesf,
@@ -483,11 +605,15 @@ void compute_coupling_ac_el_cuda_(long* Mesh_pointer, int* iphasef, int* num_cou
   if (!mp || !mp->has_acoustic) return;
   if (*iphasef != 1 || mp->num_coupling_faces == 0) return;
   if (*num_coupling_ac_el_facesf != mp->num_coupling_faces) { set_error(SF3D_ERR_ARG, "coupling face count mismatch"); return; }
+  AcField F;
+  if (!ac_field(mp, FORWARD_OR_ADJOINT, &F)) return;
+  const float* displ = *FORWARD_OR_ADJOINT == 3 ? mp->b.displ : mp->f.displ;
+  if (!displ) { set_error(SF3D_ERR_STATE, "backward elastic field not allocated"); return; }
   const float sign = (mp->simulation_type != 1 && *FORWARD_OR_ADJOINT == 1) ? -1.f : 1.f;
   const long n = (long)mp->num_coupling_faces * NGLL2;
   coupling_ac_el_kernel<<<nblk(n, 128), 128, 0, mp->stream>>>(mp->num_coupling_faces, mp->d_cp_ispec, mp->d_cp_pt,
-                                                               mp->d_cp_normal, mp->d_cp_jw, mp->d_ibool, mp->f.displ,
-                                                               sign, mp->d_potential_dot_dot);
+                                                               mp->d_cp_normal, mp->d_cp_jw, mp->d_ibool, displ,
+                                                               sign, F.pdd);
   cuda_ok(cudaGetLastError(), "coupling_ac_el_kernel");
 }
 
@@ -497,11 +623,15 @@ void compute_coupling_el_ac_cuda_(long* Mesh_pointer, int* iphasef, int* num_cou
   if (!mp || !mp->has_acoustic) return;
   if (*iphasef != 1 || mp->num_coupling_faces == 0) return;
   if (*num_coupling_ac_el_facesf != mp->num_coupling_faces) { set_error(SF3D_ERR_ARG, "coupling face count mismatch"); return; }
+  AcField F;
+  if (!ac_field(mp, FORWARD_OR_ADJOINT, &F)) return;
+  float* accel = *FORWARD_OR_ADJOINT == 3 ? mp->b.accel : mp->f.accel;
+  if (!accel) { set_error(SF3D_ERR_STATE, "backward elastic field not allocated"); return; }
   const float sign = (mp->simulation_type != 1 && *FORWARD_OR_ADJOINT == 1) ? -1.f : 1.f;
   const long n = (long)mp->num_coupling_faces * NGLL2;
   coupling_el_ac_kernel<<<nblk(n, 128), 128, 0, mp->stream>>>(mp->num_coupling_faces, mp->d_cp_ispec, mp->d_cp_pt,
-                                                               mp->d_cp_normal, mp->d_cp_jw, mp->d_ibool,
-                                                               mp->d_potential_dot_dot, sign, mp->f.accel);
+                                                               mp->d_cp_normal, mp->d_cp_jw, mp->d_ibool, F.pdd, sign,
+                                                               accel);
   cuda_ok(cudaGetLastError(), "coupling_el_ac_kernel");
 }
 
@@ -524,12 +654,15 @@ void compute_add_sources_ac_cuda_(long* Mesh_pointer, int* NSOURCESf, double* h_
   cuda_ok(cudaGetLastError(), "sources_acoustic_kernel");
 }
 
-static void xfer_ac(int* size, realw* a, realw* b, realw* c, long* Mesh_pointer, bool to_device) {
+static void xfer_ac(int* size, realw* a, realw* b, realw* c, long* Mesh_pointer, bool to_device,
+                    int fa = 1) {
   Mesh* mp = get_mesh(Mesh_pointer);
   if (!mp) return;
   if (!mp->has_acoustic) { set_error(SF3D_ERR_STATE, "acoustic fields not allocated"); return; }
-  if (*size != mp->nglob) { set_error(SF3D_ERR_ARG, "acoustic transfer size must be NGLOB_AB"); return; }
-  float* d[3] = {mp->d_potential, mp->d_potential_dot, mp->d_potential_dot_dot};
+  if (!size || *size != mp->nglob) { set_error(SF3D_ERR_ARG, "acoustic transfer size must be NGLOB_AB"); return; }
+  AcField F;
+  if (!ac_field(mp, &fa, &F)) return;
+  float* d[3] = {F.p, F.pd, F.pdd};
   realw* h[3] = {a, b, c};
   for (int q = 0; q < 3; ++q) {
     if (!h[q]) continue;
@@ -549,6 +682,122 @@ void transfer_fields_ac_to_device_(int* size, realw* potential_acoustic, realw* 
 void transfer_fields_ac_from_device_(int* size, realw* potential_acoustic, realw* potential_dot_acoustic,
                                      realw* potential_dot_dot_acoustic, long* Mesh_pointer) {
   xfer_ac(size, potential_acoustic, potential_dot_acoustic, potential_dot_dot_acoustic, Mesh_pointer, false);
+}
+
+
+// ---------------------------------------------------------------- SIMULATION_TYPE = 3 in fluid elements
+// prepare_fields_acoustic_adj_dev (prepare_mesh_constants_cuda.cu): backward
+// potentials and the rho / kappa kernel accumulators
+void prepare_fields_acoustic_adj_dev_(long* Mesh_pointer, int* APPROXIMATE_HESS_KL) {
+  Mesh* mp = get_mesh(Mesh_pointer);
+  if (!mp) return;
+  if (!mp->has_acoustic) { set_error(SF3D_ERR_STATE, "prepare_fields_acoustic_device not called"); return; }
+  if (APPROXIMATE_HESS_KL && *APPROXIMATE_HESS_KL) {
+    set_error(SF3D_ERR_UNSUPPORTED, "acoustic Hessian kernels (APPROXIMATE_HESS_KL in fluid elements) are not supported by this library");
+    return;
+  }
+  const long nglob = mp->nglob, nk = (long)NGLL3_PAD * mp->nspec;
+  if (mp->d_b_potential) return;
+  alloc_zero((void**)&mp->d_b_potential, sizeof(float) * nglob) &&
+      alloc_zero((void**)&mp->d_b_potential_dot, sizeof(float) * nglob) &&
+      alloc_zero((void**)&mp->d_b_potential_dot_dot, sizeof(float) * nglob) &&
+      alloc_zero((void**)&mp->d_rho_ac_kl, sizeof(double) * nk) &&
+      alloc_zero((void**)&mp->d_kappa_ac_kl, sizeof(double) * nk);
+}
+
+// compute_add_sources_ac_s3_cuda (compute_add_sources_acoustic_cuda.cu): the
+// sources on the backward potentials, stf at the caller's time
+void compute_add_sources_ac_s3_cuda_(long* Mesh_pointer, int* NSOURCESf, double* h_stf_pre_compute,
+                                     int* run_number_of_the_source) {
+  (void)run_number_of_the_source;
+  Mesh* mp = get_mesh(Mesh_pointer);
+  if (!mp || !mp->has_acoustic) return;
+  if (!mp->d_b_potential) { set_error(SF3D_ERR_STATE, "prepare_fields_acoustic_adj_dev not called"); return; }
+  if (mp->nsources_local == 0 || mp->nsources == 0) return;
+  if (*NSOURCESf != mp->nsources) { set_error(SF3D_ERR_ARG, "NSOURCES mismatch"); return; }
+  std::vector<float> stf(mp->nsources);
+  for (int i = 0; i < mp->nsources; ++i) stf[i] = (float)h_stf_pre_compute[i];
+  SF3D_CUDA(cudaMemcpyAsync(mp->d_stf_step, stf.data(), sizeof(float) * mp->nsources, cudaMemcpyHostToDevice,
+                            mp->stream));
+  sources_acoustic_kernel<<<mp->nsources, NGLL3_PAD, 0, mp->stream>>>(mp->nsources, mp->d_ispec_src,
+                                                                      mp->d_ispec_is_acoustic, mp->d_sourcearrays,
+                                                                      mp->d_stf_step, mp->d_ibool, mp->d_kappav,
+                                                                      mp->d_b_potential_dot_dot, nullptr, nullptr, 0);
+  SF3D_CUDA(cudaStreamSynchronize(mp->stream));
+  cuda_ok(cudaGetLastError(), "sources_acoustic_kernel(b)");
+}
+
+// compute_kernels_acoustic_cuda (compute_kernels_cuda.cu)
+void compute_kernels_acoustic_cuda_(long* Mesh_pointer, realw* deltat_f) {
+  Mesh* mp = get_mesh(Mesh_pointer);
+  if (!mp) return;
+  if (!mp->d_rho_ac_kl) { set_error(SF3D_ERR_STATE, "prepare_fields_acoustic_adj_dev not called"); return; }
+  Metric9 m;
+  for (int q = 0; q < 9; ++q) m.p[q] = mp->d_metric[q];
+  kernels_acoustic_kernel<<<mp->nspec, NGLL3_PAD, 0, mp->stream>>>(
+      mp->nspec, mp->d_ispec_is_acoustic, mp->d_ibool, mp->d_irregular, m, mp->d_gll, mp->xix_regular,
+      mp->d_potential, mp->d_b_potential, mp->d_b_potential_dot_dot, (double)*deltat_f, mp->d_rho_ac_kl,
+      mp->d_kappa_ac_kl);
+  cuda_ok(cudaGetLastError(), "kernels_acoustic_kernel");
+}
+
+static bool ac_kernels_to_host(Mesh* mp, double* h_rho, double* h_kappa, float* f_rho, float* f_kappa) {
+  if (!mp->d_rho_ac_kl) return set_error(SF3D_ERR_STATE, "acoustic kernels not allocated");
+  const size_t nk = (size_t)NGLL3_PAD * mp->nspec;
+  std::vector<double> tmp(nk);
+  const double* d[2] = {mp->d_rho_ac_kl, mp->d_kappa_ac_kl};
+  double* hd[2] = {h_rho, h_kappa};
+  float* hf[2] = {f_rho, f_kappa};
+  for (int q = 0; q < 2; ++q) {
+    if (!copy_sync(tmp.data(), d[q], sizeof(double) * nk, cudaMemcpyDeviceToHost, mp->stream)) return false;
+    for (long e = 0; e < mp->nspec; ++e)
+      for (int p = 0; p < NGLL3; ++p) {
+        const double v = tmp[(size_t)NGLL3_PAD * e + p];
+        if (hd[q]) hd[q][(size_t)NGLL3 * e + p] = v;
+        if (hf[q]) hf[q][(size_t)NGLL3 * e + p] = (float)v;
+      }
+  }
+  return true;
+}
+
+// transfer_kernels_ac_to_host (transfer_fields_cuda.cu): rho_ac_kl, kappa_ac_kl (5,5,5,NSPEC)
+void transfer_kernels_ac_to_host_(long* Mesh_pointer, realw* h_rho_ac_kl, realw* h_kappa_ac_kl, int* NSPEC_AB) {
+  Mesh* mp = get_mesh(Mesh_pointer);
+  if (!mp) return;
+  if (!NSPEC_AB || *NSPEC_AB != mp->nspec) { set_error(SF3D_ERR_ARG, "NSPEC_AB mismatch"); return; }
+  ac_kernels_to_host(mp, nullptr, nullptr, h_rho_ac_kl, h_kappa_ac_kl);
+}
+
+// FP64 read-back of the acoustic accumulators (library extension)
+int sf3d_get_kernels_ac_f64(long* Mesh_pointer, double* h_rho_ac_kl, double* h_kappa_ac_kl) {
+  Mesh* mp = get_mesh(Mesh_pointer);
+  if (!mp) return SF3D_ERR_STATE;
+  return ac_kernels_to_host(mp, h_rho_ac_kl, h_kappa_ac_kl, nullptr, nullptr) ? SF3D_OK : SF3D_ERR_STATE;
+}
+
+// single-field transfers of the backward potentials (transfer_fields_cuda.cu)
+void transfer_b_fields_ac_to_device_(int* size, realw* b_potential_acoustic, realw* b_potential_dot_acoustic,
+                                     realw* b_potential_dot_dot_acoustic, long* Mesh_pointer) {
+  xfer_ac(size, b_potential_acoustic, b_potential_dot_acoustic, b_potential_dot_dot_acoustic, Mesh_pointer, true, 3);
+}
+void transfer_b_fields_ac_from_device_(int* size, realw* b_potential_acoustic, realw* b_potential_dot_acoustic,
+                                       realw* b_potential_dot_dot_acoustic, long* Mesh_pointer) {
+  xfer_ac(size, b_potential_acoustic, b_potential_dot_acoustic, b_potential_dot_dot_acoustic, Mesh_pointer, false, 3);
+}
+void transfer_b_potential_ac_from_device_(int* size, realw* b_potential_acoustic, long* Mesh_pointer) {
+  xfer_ac(size, b_potential_acoustic, nullptr, nullptr, Mesh_pointer, false, 3);
+}
+void transfer_b_potential_ac_to_device_(int* size, realw* b_potential_acoustic, long* Mesh_pointer) {
+  xfer_ac(size, b_potential_acoustic, nullptr, nullptr, Mesh_pointer, true, 3);
+}
+void transfer_b_potential_dot_dot_ac_from_device_(int* size, realw* b_potential_dot_dot_acoustic, long* Mesh_pointer) {
+  xfer_ac(size, nullptr, nullptr, b_potential_dot_dot_acoustic, Mesh_pointer, false, 3);
+}
+void transfer_b_potential_dot_dot_ac_to_device_(int* size, realw* b_potential_dot_dot_acoustic, long* Mesh_pointer) {
+  xfer_ac(size, nullptr, nullptr, b_potential_dot_dot_acoustic, Mesh_pointer, true, 3);
+}
+void transfer_b_dot_dot_from_device_(int* size, realw* b_potential_dot_dot_acoustic, long* Mesh_pointer) {
+  xfer_ac(size, nullptr, nullptr, b_potential_dot_dot_acoustic, Mesh_pointer, false, 3);
 }
 
 }  // extern "C"

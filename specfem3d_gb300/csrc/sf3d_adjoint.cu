@@ -27,9 +27,10 @@ inline unsigned nblk(long n, int b) { return (unsigned)((n + b - 1) / b); }
 __global__ void adjoint_sources_kernel(int nadj, const int* __restrict__ ispec, const float* __restrict__ hx,
                                        const float* __restrict__ he, const float* __restrict__ hg,
                                        const float* __restrict__ src, int it_index, const int* __restrict__ ibool,
-                                       float* __restrict__ accel) {
+                                       const int* __restrict__ is_acoustic, float* __restrict__ accel) {
   const int r = blockIdx.x, t = threadIdx.x;
   if (r >= nadj || t >= NGLL3) return;
+  if (is_acoustic && is_acoustic[ispec[r]]) return;  // elastic receivers only
   const int k = t / NGLL2, j = (t / NGLLX) % NGLLX, i = t % NGLLX;
   const float h = hx[5 * r + i] * he[5 * r + j] * hg[5 * r + k];
   const int g = ibool[(long)ispec[r] * NGLL3_PAD + t];
@@ -37,6 +38,19 @@ __global__ void adjoint_sources_kernel(int nadj, const int* __restrict__ ispec, 
   atomicAdd(accel + 3L * g, s[0] * h);
   atomicAdd(accel + 3L * g + 1, s[1] * h);
   atomicAdd(accel + 3L * g + 2, s[2] * h);
+}
+
+// adjoint sources of receivers in fluid elements: the first component into
+// potential_dot_dot (kernels/add_sources_ac_SIM_TYPE_2_OR_3_kernel.cu:31-85)
+__global__ void adjoint_sources_ac_kernel(int nadj, const int* __restrict__ ispec, const float* __restrict__ hx,
+                                          const float* __restrict__ he, const float* __restrict__ hg,
+                                          const float* __restrict__ src, int it_index, const int* __restrict__ ibool,
+                                          const int* __restrict__ is_acoustic, float* __restrict__ pot_dd) {
+  const int r = blockIdx.x, t = threadIdx.x;
+  if (r >= nadj || t >= NGLL3 || !is_acoustic[ispec[r]]) return;
+  const int k = t / NGLL2, j = (t / NGLLX) % NGLLX, i = t % NGLLX;
+  const float h = hx[5 * r + i] * he[5 * r + j] * hg[5 * r + k];
+  atomicAdd(pot_dd + ibool[(long)ispec[r] * NGLL3_PAD + t], src[3L * (r + (long)nadj * it_index)] * h);
 }
 
 // deviatoric strain and trace/3 of a displacement field per element
@@ -274,9 +288,32 @@ void add_sources_el_sim_type_2_or_3_(long* Mesh_pointer, realw* h_source_adjoint
                               cudaMemcpyHostToDevice, mp->stream));
   adjoint_sources_kernel<<<mp->nadj_rec_local, NGLL3_PAD, 0, mp->stream>>>(
       mp->nadj_rec_local, mp->d_ispec_adj, mp->d_hxir_adj, mp->d_hetar_adj, mp->d_hgammar_adj, mp->d_source_adjoint,
-      it_index, mp->d_ibool, mp->f.accel);
+      it_index, mp->d_ibool, mp->d_ispec_is_acoustic, mp->f.accel);
   SF3D_CUDA(cudaStreamSynchronize(mp->stream));
   cuda_ok(cudaGetLastError(), "adjoint_sources_kernel");
+}
+
+// add_sources_ac_sim_2_or_3_cuda (compute_add_sources_acoustic_cuda.cu): the same
+// time-reversed block of adjoint traces, receivers in fluid elements
+void add_sources_ac_sim_2_or_3_cuda_(long* Mesh_pointer, realw* h_source_adjoint, int* nrec, int* nadj_rec_local,
+                                     int* NTSTEP_BETWEEN_READ_ADJSRC, int* it) {
+  (void)nrec;
+  Mesh* mp = get_mesh(Mesh_pointer);
+  if (!mp) return;
+  if (!mp->d_potential_dot_dot) { set_error(SF3D_ERR_STATE, "acoustic fields not prepared"); return; }
+  if (*nadj_rec_local != mp->nadj_rec_local) { set_error(SF3D_ERR_ARG, "nadj_rec_local not equal"); return; }
+  if (mp->nadj_rec_local == 0) return;
+  const int nt = *NTSTEP_BETWEEN_READ_ADJSRC;
+  if (nt != mp->ntstep_between_read_adjsrc || nt <= 0) { set_error(SF3D_ERR_ARG, "NTSTEP_BETWEEN_READ_ADJSRC mismatch"); return; }
+  const int it_index = nt - (*it - 1) % nt - 1;
+  if ((*it - 1) % nt == 0)
+    SF3D_CUDA(cudaMemcpyAsync(mp->d_source_adjoint, h_source_adjoint, sizeof(float) * 3 * (size_t)mp->nadj_rec_local * nt,
+                              cudaMemcpyHostToDevice, mp->stream));
+  adjoint_sources_ac_kernel<<<mp->nadj_rec_local, NGLL3_PAD, 0, mp->stream>>>(
+      mp->nadj_rec_local, mp->d_ispec_adj, mp->d_hxir_adj, mp->d_hetar_adj, mp->d_hgammar_adj, mp->d_source_adjoint,
+      it_index, mp->d_ibool, mp->d_ispec_is_acoustic, mp->d_potential_dot_dot);
+  SF3D_CUDA(cudaStreamSynchronize(mp->stream));
+  cuda_ok(cudaGetLastError(), "adjoint_sources_ac_kernel");
 }
 
 namespace {

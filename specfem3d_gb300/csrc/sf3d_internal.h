@@ -192,6 +192,13 @@ struct Mesh {
   float* d_potential = nullptr;
   float* d_potential_dot = nullptr;
   float* d_potential_dot_dot = nullptr;
+  // SIMULATION_TYPE = 3 in fluid elements: backward potentials and the FP64
+  // rho / kappa kernel accumulators [nspec][128] (prepare_fields_acoustic_adj_dev)
+  float* d_b_potential = nullptr;
+  float* d_b_potential_dot = nullptr;
+  float* d_b_potential_dot_dot = nullptr;
+  double* d_rho_ac_kl = nullptr;
+  double* d_kappa_ac_kl = nullptr;
   float* d_rmass_acoustic = nullptr;
   int num_phase_ispec_ac = 0, nspec_outer_ac = 0, nspec_inner_ac = 0;
   int phase_valid_ac[2] = {0, 0};

@@ -114,10 +114,11 @@ __global__ void stacey_kernel(int nfaces, const int* __restrict__ abs_ispec, con
 // (kernels/compute_stacey_elastic_kernel.cu:111-147).
 __global__ void stacey_replay_kernel(int nfaces, const int* __restrict__ abs_ispec, const int* __restrict__ abs_pt,
                                      const int* __restrict__ ibool, const float* __restrict__ record,
-                                     float* __restrict__ accel) {
+                                     const int* __restrict__ is_acoustic, float* __restrict__ accel) {
   long idx = (long)blockIdx.x * blockDim.x + threadIdx.x;
   if (idx >= (long)nfaces * NGLL2) return;
   const int f = (int)(idx / NGLL2);
+  if (is_acoustic && is_acoustic[abs_ispec[f]]) return;  // faces of fluid elements carry no elastic record
   const int g = ibool[(long)abs_ispec[f] * NGLL3_PAD + abs_pt[idx]];
   atomicAdd(accel + 3L * g, -record[3 * idx]);
   atomicAdd(accel + 3L * g + 1, -record[3 * idx + 1]);
@@ -510,6 +511,8 @@ void compute_stacey_viscoelastic_cuda_(long* Mesh_pointer, int* iphasef, realw* 
   const long n = (long)mp->num_abs_faces * NGLL2;
   const bool store = (fa == 1) && mp->save_forward && mp->simulation_type == 1 && b_absorb_field;
   if (store && !ensure_stage(mp, sizeof(float) * 3 * n)) return;
+  // faces of fluid elements are skipped by the kernel: their record entries are zero
+  if (store) SF3D_CUDA(cudaMemsetAsync(mp->d_stage, 0, sizeof(float) * 3 * n, mp->stream));
   if (fa == 1 || fa == 0) {
     stacey_kernel<<<nblk(n, 128), 128, 0, mp->stream>>>(mp->num_abs_faces, mp->d_abs_ispec, mp->d_abs_pt,
                                                         mp->d_abs_normal, mp->d_abs_jw, mp->d_ibool, mp->d_rho_vp,
@@ -529,7 +532,8 @@ void compute_stacey_viscoelastic_cuda_(long* Mesh_pointer, int* iphasef, realw* 
       SF3D_CUDA(cudaMemcpyAsync(mp->d_stage, b_absorb_field, sizeof(float) * 3 * n, cudaMemcpyHostToDevice,
                                 mp->stream));
       stacey_replay_kernel<<<nblk(n, 128), 128, 0, mp->stream>>>(mp->num_abs_faces, mp->d_abs_ispec, mp->d_abs_pt,
-                                                                 mp->d_ibool, mp->d_stage, mp->b.accel);
+                                                                 mp->d_ibool, mp->d_stage, mp->d_ispec_is_acoustic,
+                                                                 mp->b.accel);
     } else {
       // recomputed (checkpointed) backward field: same traction from b_veloc
       stacey_kernel<<<nblk(n, 128), 128, 0, mp->stream>>>(mp->num_abs_faces, mp->d_abs_ispec, mp->d_abs_pt,

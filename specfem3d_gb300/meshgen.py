@@ -244,7 +244,8 @@ def build_database(cfg: dict, material=None, dtype=np.float32) -> dict:
         vp = np.repeat(np.asarray([m["vp"] for m in L], np.float32)[lay], NGLL3)
         vs = np.repeat(np.asarray([m["vs"] for m in L], np.float32)[lay], NGLL3)
     else:
-        rho, vp, vs = (np.asarray(a, np.float32) for a in material)
+        # the database's precision (an FP64 database keeps FP64 material values)
+        rho, vp, vs = (np.asarray(a, dtype) for a in material)
     r, p, s = rho.astype(dtype), vp.astype(dtype), vs.astype(dtype)
     # fluid elements: zero shear velocity (generate_databases/get_model.F90 sets
     # ispec_is_acoustic for vs == 0)

@@ -61,6 +61,7 @@ class GPUSolver:
         self.isac = np.asarray(db.get("ispec_is_acoustic", np.zeros(self.nspec, np.int32)), np.int32)
         self.coupled = bool(self.isac.any())
         self.absorb_record = None
+        self.absorb_record_ac = None
         self.undo_attenuation = bool(undo_attenuation)
         self._prepare_constants(db, save_forward)
         self._prepare_fields(db)
@@ -191,7 +192,11 @@ class GPUSolver:
         for iphase in (1, 2):
             L.compute_forces_acoustic_cuda_(self.mp, A.i(iphase), A.i(0), A.i(self.nspec_acoustic), one)
             if iphase == 1:
-                L.compute_stacey_acoustic_cuda_(self.mp, A.i(1), A.af(None), one)
+                # SAVE_FORWARD runs hand a (nstep, 25*nfaces) float32 array here to
+                # receive b_absorb_potential; otherwise NULL
+                rec = self.absorb_record_ac
+                L.compute_stacey_acoustic_cuda_(self.mp, A.i(1), A.af(rec[it - 1]) if rec is not None else None,
+                                                one)
                 L.compute_coupling_ac_el_cuda_(self.mp, A.i(1), A.i(self.ncoupling), one)
                 if self.nsources:
                     L.compute_add_sources_ac_cuda_(self.mp, A.i(self.nsources), A.ad(self._stf_now(it)), A.i(1))

@@ -146,8 +146,8 @@ def test_acoustic_interfaces_and_potential_transfers(gpulib):
         np.add.at(want, ibif[:nib[i], i] - 1, recv[i, :nib[i]])
     L.transfer_dot_dot_from_device_(A.i(nglob), back.ctypes.data, g.mp)
     assert np.allclose(back, want, rtol=0, atol=1e-6)
-    # the backward acoustic field is not provided
+    # the backward potentials exist only after prepare_fields_acoustic_adj_dev
     L.transfer_boun_pot_from_device_(g.mp, send.ctypes.data, A.i(3))
-    with pytest.raises(abi.SF3DError, match="not supported"):
+    with pytest.raises(abi.SF3DError, match="not prepared"):
         abi.check()
     g.close()
