@@ -578,6 +578,9 @@ void transfer_b_potential_dot_dot_ac_to_device_(int *size, realw *b_potential_do
                                                 long *Mesh_pointer);
 void transfer_kernels_ac_to_host_(long *Mesh_pointer, realw *h_rho_ac_kl, realw *h_kappa_ac_kl,
                                   int *NSPEC_AB);
+/* Fluid kernel pairing: 0 (default) the reference's chi_adj; 1 chi_adj_dd, whose
+ * kernels are the discrete derivative of the misfit (same host scaling). */
+int sf3d_set_acoustic_kernel_pairing(long *Mesh_pointer, int discrete);
 /* FP64 acoustic accumulators, (5,5,5,NSPEC) each (library extension). */
 int sf3d_get_kernels_ac_f64(long *Mesh_pointer, double *h_rho_ac_kl, double *h_kappa_ac_kl);
 

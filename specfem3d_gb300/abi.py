@@ -119,6 +119,8 @@ def load() -> ctypes.CDLL:
     L.sf3d_get_kernels_f64.argtypes = [P, P, P, P]
     L.sf3d_get_kernels_ac_f64.restype = ctypes.c_int
     L.sf3d_get_kernels_ac_f64.argtypes = [P, P, P]
+    L.sf3d_set_acoustic_kernel_pairing.restype = ctypes.c_int
+    L.sf3d_set_acoustic_kernel_pairing.argtypes = [P, ctypes.c_int]
     _LIB = L
     return L
 

@@ -117,7 +117,7 @@ def forward_with_boundary_record_coupled(db: dict, cfg: dict):
 
 
 def kernel_run_coupled(db: dict, cfg: dict, adjoint_source: np.ndarray, final_el, final_ac, rec_el, rec_ac,
-                       history=None):
+                       history=None, discrete_fluid_kernels: bool = False):
     """The SIMULATION_TYPE = 3 run on a fluid-solid mesh (iterate_time.F90:219-330):
     per step the adjoint potentials and displacement (compute_forces_acoustic_
     forward_calling, then compute_forces_viscoelastic_calling: Stacey, coupling with
@@ -126,6 +126,8 @@ def kernel_run_coupled(db: dict, cfg: dict, adjoint_source: np.ndarray, final_el
     records replayed in reverse, coupling on the b_ fields, the sources at
     (NSTEP - it) DT - t0), both backward fields replaced by the saved final state
     after the first step, and the elastic and acoustic kernels accumulated.
+    discrete_fluid_kernels: pair chi_adj_dd instead of chi_adj in the fluid kernels
+    (sf3d_set_acoustic_kernel_pairing), which gives the discrete derivative.
     history: optional list receiving, after each step, a dict with the adjoint
     potential and its second derivative (chi, chi_dd) and the backward ones
     (b_chi, b_chi_dd).
@@ -141,6 +143,8 @@ def kernel_run_coupled(db: dict, cfg: dict, adjoint_source: np.ndarray, final_el
     A = abi.Args()
     L.prepare_fields_acoustic_adj_dev_(g.mp, A.i(0))
     abi.check()
+    if L.sf3d_set_acoustic_kernel_pairing(g.mp, int(bool(discrete_fluid_kernels))) != 0:
+        abi.check()
     nrec = g.nrec
     src = np.ascontiguousarray(np.asarray(adjoint_source, np.float32).transpose(2, 0, 1))
     stf = np.asarray(db["stf"], np.float64).reshape(g.nsources, -1)

@@ -154,9 +154,10 @@ __global__ void stacey_acoustic_replay_kernel(int nfaces, const int* __restrict_
 }
 
 // acoustic kernels (compute_kernels.f90:257-330, kernels/compute_kernels_acoustic_kernel.cu):
-// rho_ac_kl += dt grad(chi_adj) . grad(b_chi), kappa_ac_kl += dt chi_adj b_chi_dd;
-// the 1/rho of the reference's gradient routine is undone there by rho, so the
-// plain gradients are used; FP64 accumulators
+// rho_ac_kl += dt grad(a) . grad(b_chi), kappa_ac_kl += dt a b_chi_dd with a = chi_adj
+// (the reference) or a = chi_adj_dd (the discrete derivative of the misfit; the
+// caller passes that array as pot); the 1/rho of the reference's gradient routine
+// is undone there by rho, so the plain gradients are used; FP64 accumulators
 __global__ void __launch_bounds__(NGLL3_PAD)
     kernels_acoustic_kernel(long nspec, const int* __restrict__ is_acoustic, const int* __restrict__ ibool,
                             const int* __restrict__ irregular, Metric9 m, const float* __restrict__ gll,
@@ -209,7 +210,7 @@ __global__ void __launch_bounds__(NGLL3_PAD)
     }
   }
   rho_kl[eo] += dt * ((double)ga[0] * gb[0] + (double)ga[1] * gb[1] + (double)ga[2] * gb[2]);
-  kappa_kl[eo] += dt * ((double)pot[g] * b_pot_dd[g]);
+  kappa_kl[eo] += dt * ((double)s_a[t] * b_pot_dd[g]);
 }
 
 // chi_dd += jw (u . n)   (compute_coupling_acoustic_el.f90:70-150)
@@ -736,7 +737,8 @@ void compute_kernels_acoustic_cuda_(long* Mesh_pointer, realw* deltat_f) {
   for (int q = 0; q < 9; ++q) m.p[q] = mp->d_metric[q];
   kernels_acoustic_kernel<<<mp->nspec, NGLL3_PAD, 0, mp->stream>>>(
       mp->nspec, mp->d_ispec_is_acoustic, mp->d_ibool, mp->d_irregular, m, mp->d_gll, mp->xix_regular,
-      mp->d_potential, mp->d_b_potential, mp->d_b_potential_dot_dot, (double)*deltat_f, mp->d_rho_ac_kl,
+      mp->ac_kernel_discrete ? mp->d_potential_dot_dot : mp->d_potential, mp->d_b_potential,
+      mp->d_b_potential_dot_dot, (double)*deltat_f, mp->d_rho_ac_kl,
       mp->d_kappa_ac_kl);
   cuda_ok(cudaGetLastError(), "kernels_acoustic_kernel");
 }
@@ -766,6 +768,21 @@ void transfer_kernels_ac_to_host_(long* Mesh_pointer, realw* h_rho_ac_kl, realw*
   if (!mp) return;
   if (!NSPEC_AB || *NSPEC_AB != mp->nspec) { set_error(SF3D_ERR_ARG, "NSPEC_AB mismatch"); return; }
   ac_kernels_to_host(mp, nullptr, nullptr, h_rho_ac_kl, h_kappa_ac_kl);
+}
+
+// Fluid kernel pairing (library extension): 0 (default) the reference's formula
+// with the adjoint potential chi_adj; 1 the adjoint chi_adj_dd, which gives the
+// discrete derivative of the misfit (the reference's adjoint potential of the
+// fluid is the second time integral of the discrete adjoint variable)
+int sf3d_set_acoustic_kernel_pairing(long* Mesh_pointer, int discrete) {
+  Mesh* mp = get_mesh(Mesh_pointer);
+  if (!mp) return SF3D_ERR_STATE;
+  if (discrete != 0 && discrete != 1) {
+    set_error(SF3D_ERR_ARG, "sf3d_set_acoustic_kernel_pairing: 0 or 1");
+    return SF3D_ERR_ARG;
+  }
+  mp->ac_kernel_discrete = discrete;
+  return SF3D_OK;
 }
 
 // FP64 read-back of the acoustic accumulators (library extension)

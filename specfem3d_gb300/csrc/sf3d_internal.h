@@ -199,6 +199,9 @@ struct Mesh {
   float* d_b_potential_dot_dot = nullptr;
   double* d_rho_ac_kl = nullptr;
   double* d_kappa_ac_kl = nullptr;
+  // 1: fluid kernels pair the adjoint chi_dd (the discrete adjoint variable of the
+  // fluid) instead of chi (the reference's formula); sf3d_set_acoustic_kernel_pairing
+  int ac_kernel_discrete = 0;
   float* d_rmass_acoustic = nullptr;
   int num_phase_ispec_ac = 0, nspec_outer_ac = 0, nspec_inner_ac = 0;
   int phase_valid_ac[2] = {0, 0};

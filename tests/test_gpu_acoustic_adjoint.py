@@ -72,7 +72,7 @@ def _volume(db):
     return jac * w3[None, :]
 
 
-def _run(stacey, fluid_source):
+def _run(stacey, fluid_source, discrete=False):
     from specfem3d_gb300 import adjoint as ADJ
     from specfem3d_gb300.solver import GPUSolver
     cfg, mat = _setup()
@@ -89,7 +89,8 @@ def _run(stacey, fluid_source):
         H[s] = g.potentials()[0]
     g.close()
     hist = []
-    kl = ADJ.kernel_run_coupled(db, cfg, seis.astype(np.float64), fin_el, fin_ac, rec_el, rec_ac, history=hist)
+    kl = ADJ.kernel_run_coupled(db, cfg, seis.astype(np.float64), fin_el, fin_ac, rec_el, rec_ac, history=hist,
+                                discrete_fluid_kernels=discrete)
     return cfg, mat, db, seis, H, hist, kl
 
 
@@ -104,6 +105,12 @@ def run_plain(gpulib):
     """No absorbing faces (the Stacey coefficients rho vp, rho vs depend on the model
     and the volume kernels leave that out), the moment tensor only."""
     return _run(False, False)
+
+
+@pytest.fixture(scope="module")
+def run_discrete(gpulib):
+    """As run_plain, with the fluid kernels pairing chi_adj_dd (sf3d_set_acoustic_kernel_pairing)."""
+    return _run(False, False, discrete=True)
 
 
 def _gradient(db, f):
@@ -211,4 +218,30 @@ def test_fluid_kappa_derivative_is_the_second_derivative_pairing(run_plain):
     e = abs(pred - fd) / abs(fd)
     print(f"fluid kappa: finite difference {fd:.6e}, chi_adj_dd pairing {pred:.6e} (relative {e:.2e}), "
           f"reference formula {ref_formula:.6e}")
+    assert abs(fd) > 0 and e < 1e-3
+
+
+@pytest.mark.parametrize("param", ["kappa", "rho"])
+def test_discrete_fluid_kernels_match_finite_differences(run_discrete, param):
+    """With the chi_adj_dd pairing the library's fluid kernels, scaled as the
+    reference scales its own (K = kl / kappa, kl / rho), give the derivative of the
+    misfit along smooth relative perturbations of the fluid's kappa (rho fixed) or
+    rho (kappa fixed): central differences of the FP64 oracle, eps = 3e-5."""
+    from specfem3d_gb300 import gradient as G
+    cfg, mat, db, seis, H, hist, kl = run_discrete
+    n = int(db["nspec"])
+    fluid = np.repeat(np.asarray(db["ispec_is_acoustic"]) > 0, 125).reshape(n, 125)
+    rho, vp, vs = mat
+    store = np.asarray(db["kappastore" if param == "kappa" else "rhostore"], np.float64).reshape(n, 125)
+    K = kl[param + "_ac"] / store
+    d = G.smooth_direction(cfg, 11 if param == "kappa" else 22, corr_len=600.0).reshape(n, 125) * fluid
+    js = []
+    for sgn in (1.0, -1.0):
+        f = (1.0 + sgn * EPS * d).reshape(-1)
+        m = (rho, vp * np.sqrt(f), vs) if param == "kappa" else (rho * f, vp / np.sqrt(f), vs)
+        js.append(_misfit64(cfg, m))
+    fd = (js[0] - js[1]) / (2 * EPS)
+    pred = float(np.sum(K * d * _volume(db)))
+    e = abs(pred - fd) / abs(fd)
+    print(f"discrete fluid {param}: finite difference {fd:.6e}, kernels {pred:.6e}, relative {e:.2e}")
     assert abs(fd) > 0 and e < 1e-3
