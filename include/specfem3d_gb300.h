@@ -556,7 +556,10 @@ void compute_stacey_acoustic_undoatt_cuda_(long *Mesh_pointer, int *iphasef, int
  * record b_absorb_potential(NGLL2, nfaces) stored by SAVE_FORWARD runs and replayed),
  * adjoint sources of receivers in fluid elements, and the rho / kappa kernels
  * rho_ac_kl += dt grad(chi_adj).grad(b_chi), kappa_ac_kl += dt chi_adj b_chi_dd
- * (FP64 accumulators; APPROXIMATE_HESS_KL is not provided in fluid elements). */
+ * (FP64 accumulators); with APPROXIMATE_HESS_KL, compute_kernels_hess_cuda with
+ * ACOUSTIC_SIMULATION also accumulates hess_ac_kl, hess_rho_ac_kl, hess_kappa_ac_kl. */
+void transfer_kernels_hess_ac_tohost_(long *Mesh_pointer, realw *h_hess_ac_kl, realw *h_hess_rho_ac_kl,
+                                      realw *h_hess_kappa_ac_kl, int *NSPEC_AB);
 void add_sources_ac_sim_2_or_3_cuda_(long *Mesh_pointer, realw *h_source_adjoint, int *nrec,
                                      int *nadj_rec_local, int *NTSTEP_BETWEEN_READ_ADJSRC, int *it);
 void compute_add_sources_ac_s3_cuda_(long *Mesh_pointer, int *NSOURCESf, double *h_stf_pre_compute,
@@ -584,8 +587,8 @@ int sf3d_set_acoustic_kernel_pairing(long *Mesh_pointer, int discrete);
 /* FP64 acoustic accumulators, (5,5,5,NSPEC) each (library extension). */
 int sf3d_get_kernels_ac_f64(long *Mesh_pointer, double *h_rho_ac_kl, double *h_kappa_ac_kl);
 
-/* Not provided: each records SF3D_ERR_UNSUPPORTED through sf3d_last_error (acoustic
- * Hessian kernels, noise tomography, C-PML, gravity, ocean load, faults);
+/* Not provided: each records SF3D_ERR_UNSUPPORTED through sf3d_last_error (noise
+ * tomography, C-PML, gravity, ocean load, faults);
  * prepare_fields_gravity_device with GRAVITY = 0 and prepare_fault_device without
  * Kelvin-Voigt damping are accepted no-ops. */
 void add_source_main_rec_noise_cu_(long *Mesh_pointer, int *it_f, int *irec_main_noise_f,
@@ -619,8 +622,6 @@ void transfer_fault_data_to_device_(long *Fault_pointer, int *fault_index, int *
                                     int *allow_opening);
 void transfer_fault_data_to_host_(long *Fault_pointer, int *fault_index, int *NSPEC_FLT, int *NGLOB_FLT,
                                   realw *D, realw *V, realw *T);
-void transfer_kernels_hess_ac_tohost_(long *Mesh_pointer, realw *h_hess_ac_kl, realw *h_hess_rho_ac_kl,
-                                      realw *h_hess_kappa_ac_kl, int *NSPEC_AB);
 void transfer_kernels_noise_to_host_(long *Mesh_pointer, realw *h_sigma_kl, int *NSPEC_AB);
 void transfer_pml_displ_from_device_(int *size, realw *PML_displ_old, realw *PML_displ_new,
                                      long *Mesh_pointer);

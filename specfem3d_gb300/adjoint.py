@@ -117,7 +117,7 @@ def forward_with_boundary_record_coupled(db: dict, cfg: dict):
 
 
 def kernel_run_coupled(db: dict, cfg: dict, adjoint_source: np.ndarray, final_el, final_ac, rec_el, rec_ac,
-                       history=None, discrete_fluid_kernels: bool = False):
+                       history=None, discrete_fluid_kernels: bool = False, hessian: bool = False):
     """The SIMULATION_TYPE = 3 run on a fluid-solid mesh (iterate_time.F90:219-330):
     per step the adjoint potentials and displacement (compute_forces_acoustic_
     forward_calling, then compute_forces_viscoelastic_calling: Stacey, coupling with
@@ -130,7 +130,9 @@ def kernel_run_coupled(db: dict, cfg: dict, adjoint_source: np.ndarray, final_el
     (sf3d_set_acoustic_kernel_pairing), which gives the discrete derivative.
     history: optional list receiving, after each step, a dict with the adjoint
     potential and its second derivative (chi, chi_dd) and the backward ones
-    (b_chi, b_chi_dd).
+    (b_chi, b_chi_dot, b_chi_dd).  hessian: APPROXIMATE_HESS_KL in the fluid
+    (hess_ac, hess_rho_ac, hess_kappa_ac in the result, FP32 as
+    transfer_kernels_hess_ac_tohost returns them).
     Returns the raw FP64 accumulators rho, mu, kappa (solid) and rho_ac, kappa_ac
     (fluid), each (nspec, 125)."""
     if int(db.get("attenuation", 0)):
@@ -141,7 +143,7 @@ def kernel_run_coupled(db: dict, cfg: dict, adjoint_source: np.ndarray, final_el
     n3, n1 = 3 * g.nglob, g.nglob
     _prepare_adjoint(g, db, nstep)
     A = abi.Args()
-    L.prepare_fields_acoustic_adj_dev_(g.mp, A.i(0))
+    L.prepare_fields_acoustic_adj_dev_(g.mp, A.i(int(bool(hessian))))
     abi.check()
     if L.sf3d_set_acoustic_kernel_pairing(g.mp, int(bool(discrete_fluid_kernels))) != 0:
         abi.check()
@@ -200,11 +202,14 @@ def kernel_run_coupled(db: dict, cfg: dict, adjoint_source: np.ndarray, final_el
             L.transfer_b_fields_ac_to_device_(B.i(n1), *(B.af(f) for f in fin_ac), g.mp)
         L.compute_kernels_elastic_cuda_(g.mp, B.f(dt))
         L.compute_kernels_acoustic_cuda_(g.mp, B.f(dt))
+        if hessian:
+            # APPROXIMATE_HESS_KL in the fluid only (ELASTIC_SIMULATION = 0 here)
+            L.compute_kernels_hess_cuda_(g.mp, B.f(dt), zero, one)
         if history is not None:
-            h = {k: np.zeros(n1, np.float32) for k in ("chi", "chi_dd", "b_chi", "b_chi_dd")}
+            h = {k: np.zeros(n1, np.float32) for k in ("chi", "chi_dd", "b_chi", "b_chi_dot", "b_chi_dd")}
             L.transfer_fields_ac_from_device_(B.i(n1), h["chi"].ctypes.data, None, h["chi_dd"].ctypes.data, g.mp)
-            L.transfer_b_fields_ac_from_device_(B.i(n1), h["b_chi"].ctypes.data, None, h["b_chi_dd"].ctypes.data,
-                                                g.mp)
+            L.transfer_b_fields_ac_from_device_(B.i(n1), h["b_chi"].ctypes.data, h["b_chi_dot"].ctypes.data,
+                                                h["b_chi_dd"].ctypes.data, g.mp)
             h["it"] = it
             history.append(h)
     abi.check()
@@ -212,6 +217,11 @@ def kernel_run_coupled(db: dict, cfg: dict, adjoint_source: np.ndarray, final_el
     ac = {k: np.zeros(n * NGLL3) for k in ("rho_ac", "kappa_ac")}
     if L.sf3d_get_kernels_ac_f64(g.mp, ac["rho_ac"].ctypes.data, ac["kappa_ac"].ctypes.data) != 0:
         abi.check()
+    if hessian:
+        hs = [np.zeros(n * NGLL3, np.float32) for _ in range(3)]
+        L.transfer_kernels_hess_ac_tohost_(g.mp, *(x.ctypes.data for x in hs), B.i(n))
+        abi.check()
+        ac.update({k: x.reshape(n, NGLL3) for k, x in zip(("hess_ac", "hess_rho_ac", "hess_kappa_ac"), hs)})
     out = _kernels_f64(g)
     out.update({k: v.reshape(n, NGLL3) for k, v in ac.items()})
     return out

@@ -11,8 +11,8 @@
 // * acoustic MPI interface pack / assembly (transfer_boun_pot_from_device,
 //   transfer_asmbl_pot_to_device);
 // * Stacey of a recomputed backward field (*_undoatt_cuda);
-// * features this library does not provide (acoustic Hessian kernels, noise
-//   tomography, faults, C-PML, gravity, ocean load): the call records
+// * features this library does not provide (noise tomography, faults, C-PML,
+//   gravity, ocean load): the call records
 //   SF3D_ERR_UNSUPPORTED (sf3d_last_error) and does nothing else.
 #include <stdarg.h>
 #include <stdio.h>
@@ -375,13 +375,6 @@ void compute_stacey_acoustic_undoatt_cuda_(long* Mesh_pointer, int* iphasef, int
 }
 
 // ---------------------------------------------------------------- not provided
-// acoustic Hessian kernels (APPROXIMATE_HESS_KL in fluid elements)
-void transfer_kernels_hess_ac_tohost_(long* Mesh_pointer, realw* h_hess_ac_kl, realw* h_hess_rho_ac_kl,
-                                      realw* h_hess_kappa_ac_kl, int* NSPEC_AB) {
-  (void)Mesh_pointer; (void)h_hess_ac_kl; (void)h_hess_rho_ac_kl; (void)h_hess_kappa_ac_kl; (void)NSPEC_AB;
-  unsupported("acoustic Hessian kernels (transfer_kernels_hess_ac_tohost)");
-}
-
 // noise tomography
 void prepare_fields_noise_device_(long* Mesh_pointer, int* NSPEC_AB, int* NGLOB_AB, int* free_surface_ispec,
                                   int* free_surface_ijk, int* num_free_surface_faces, int* NOISE_TOMOGRAPHY,

@@ -301,6 +301,63 @@ __global__ void mass_corrector_scalar_kernel(float* __restrict__ v, float* __res
   v[i] += dt2 * ai;
 }
 
+// acoustic Hessian kernels (compute_kernels.f90:459-510,
+// kernels/compute_kernels_hess_ac_cudakernel.cu), gradients with the reference's
+// 1/rho (g = grad / rho): hess_ac_kl += dt g(chi_adj_dd).g(b_chi_dd),
+// hess_rho_ac_kl += dt rho |g(b_chi_dot)|^2, hess_kappa_ac_kl += dt b_chi_dot^2 / kappa;
+// FP64 accumulators
+__global__ void __launch_bounds__(NGLL3_PAD)
+    kernels_hess_acoustic_kernel(long nspec, const int* __restrict__ is_acoustic, const int* __restrict__ ibool,
+                                 const int* __restrict__ irregular, Metric9 m, const float* __restrict__ gll,
+                                 float xix_regular, const float* __restrict__ rhostore,
+                                 const float* __restrict__ kappav, const float* __restrict__ pot_dd,
+                                 const float* __restrict__ b_pot_dot, const float* __restrict__ b_pot_dd, double dt,
+                                 double* __restrict__ hess, double* __restrict__ hess_rho,
+                                 double* __restrict__ hess_kappa) {
+  __shared__ float s_f[3][NGLL3_PAD];
+  __shared__ float s_hp[NGLL2];
+  const long e = blockIdx.x;
+  const int t = threadIdx.x;
+  if (e >= nspec || !is_acoustic[e]) return;
+  const bool active = t < NGLL3;
+  const long eo = e * NGLL3_PAD + t;
+  const int g = active ? ibool[eo] : 0;
+  if (t < NGLL2) s_hp[t] = gll[t];
+  s_f[0][t] = active ? pot_dd[g] : 0.f;
+  s_f[1][t] = active ? b_pot_dd[g] : 0.f;
+  s_f[2][t] = active ? b_pot_dot[g] : 0.f;
+  __syncthreads();
+  if (!active) return;
+  const int k = t / NGLL2, j = (t / NGLLX) % NGLLX, i = t % NGLLX;
+  const int ir = irregular[e];
+  const float rinv = 1.f / rhostore[eo];
+  float gr[3][3];
+#pragma unroll
+  for (int f = 0; f < 3; ++f) {
+    float d0 = 0.f, d1 = 0.f, d2 = 0.f;
+#pragma unroll
+    for (int l = 0; l < NGLLX; ++l) {
+      d0 = fmaf(s_f[f][l + NGLLX * j + NGLL2 * k], s_hp[i + NGLLX * l], d0);
+      d1 = fmaf(s_f[f][i + NGLLX * l + NGLL2 * k], s_hp[j + NGLLX * l], d1);
+      d2 = fmaf(s_f[f][i + NGLLX * j + NGLL2 * l], s_hp[k + NGLLX * l], d2);
+    }
+    if (ir >= 0) {
+      const long mo = (long)ir * NGLL3_PAD + t;
+#pragma unroll
+      for (int c = 0; c < 3; ++c) gr[f][c] = rinv * (m.p[c][mo] * d0 + m.p[3 + c][mo] * d1 + m.p[6 + c][mo] * d2);
+    } else {
+      gr[f][0] = rinv * xix_regular * d0;
+      gr[f][1] = rinv * xix_regular * d1;
+      gr[f][2] = rinv * xix_regular * d2;
+    }
+  }
+  const double rho = (double)rhostore[eo];
+  hess[eo] += dt * ((double)gr[0][0] * gr[1][0] + (double)gr[0][1] * gr[1][1] + (double)gr[0][2] * gr[1][2]);
+  hess_rho[eo] += dt * rho * ((double)gr[2][0] * gr[2][0] + (double)gr[2][1] * gr[2][1] + (double)gr[2][2] * gr[2][2]);
+  const double bv = (double)s_f[2][t];
+  hess_kappa[eo] += dt * bv * bv / (double)kappav[eo];
+}
+
 }  // namespace
 
 // pressure seismograms (compute_interpolated_dva.f90:280-300): p = - sum h chi_dd
@@ -420,6 +477,17 @@ int enqueue_pressure_seismograms(Mesh* mp) {
       mp->nrec_local, mp->d_ispec_rec, mp->d_rec_is_acoustic, mp->d_hxir, mp->d_hetar, mp->d_hgammar, mp->d_ibool,
       mp->d_potential_dot_dot, mp->d_seismo_p, 0, mp->d_it, mp->nlength_seismogram);
   return 1;
+}
+
+bool launch_hess_acoustic(Mesh* mp, double dt) {
+  if (!mp->d_hess_ac_kl[0]) return set_error(SF3D_ERR_STATE, "APPROXIMATE_HESS_KL was not prepared in fluid elements");
+  Metric9 m;
+  for (int q = 0; q < 9; ++q) m.p[q] = mp->d_metric[q];
+  kernels_hess_acoustic_kernel<<<mp->nspec, NGLL3_PAD, 0, mp->stream>>>(
+      mp->nspec, mp->d_ispec_is_acoustic, mp->d_ibool, mp->d_irregular, m, mp->d_gll, mp->xix_regular,
+      mp->d_rhostore, mp->d_kappav, mp->d_potential_dot_dot, mp->d_b_potential_dot, mp->d_b_potential_dot_dot, dt,
+      mp->d_hess_ac_kl[0], mp->d_hess_ac_kl[1], mp->d_hess_ac_kl[2]);
+  return cuda_ok(cudaGetLastError(), "kernels_hess_acoustic_kernel");
 }
 
 }  // namespace sf3d
@@ -693,17 +761,32 @@ void prepare_fields_acoustic_adj_dev_(long* Mesh_pointer, int* APPROXIMATE_HESS_
   Mesh* mp = get_mesh(Mesh_pointer);
   if (!mp) return;
   if (!mp->has_acoustic) { set_error(SF3D_ERR_STATE, "prepare_fields_acoustic_device not called"); return; }
-  if (APPROXIMATE_HESS_KL && *APPROXIMATE_HESS_KL) {
-    set_error(SF3D_ERR_UNSUPPORTED, "acoustic Hessian kernels (APPROXIMATE_HESS_KL in fluid elements) are not supported by this library");
-    return;
-  }
   const long nglob = mp->nglob, nk = (long)NGLL3_PAD * mp->nspec;
   if (mp->d_b_potential) return;
-  alloc_zero((void**)&mp->d_b_potential, sizeof(float) * nglob) &&
-      alloc_zero((void**)&mp->d_b_potential_dot, sizeof(float) * nglob) &&
-      alloc_zero((void**)&mp->d_b_potential_dot_dot, sizeof(float) * nglob) &&
-      alloc_zero((void**)&mp->d_rho_ac_kl, sizeof(double) * nk) &&
-      alloc_zero((void**)&mp->d_kappa_ac_kl, sizeof(double) * nk);
+  bool ok = alloc_zero((void**)&mp->d_b_potential, sizeof(float) * nglob) &&
+            alloc_zero((void**)&mp->d_b_potential_dot, sizeof(float) * nglob) &&
+            alloc_zero((void**)&mp->d_b_potential_dot_dot, sizeof(float) * nglob) &&
+            alloc_zero((void**)&mp->d_rho_ac_kl, sizeof(double) * nk) &&
+            alloc_zero((void**)&mp->d_kappa_ac_kl, sizeof(double) * nk);
+  for (int q = 0; q < 3 && ok && APPROXIMATE_HESS_KL && *APPROXIMATE_HESS_KL; ++q)
+    ok = alloc_zero((void**)&mp->d_hess_ac_kl[q], sizeof(double) * nk);
+}
+
+// transfer_kernels_hess_ac_tohost (transfer_fields_cuda.cu): (5,5,5,NSPEC) each, FP32
+void transfer_kernels_hess_ac_tohost_(long* Mesh_pointer, realw* h_hess_ac_kl, realw* h_hess_rho_ac_kl,
+                                      realw* h_hess_kappa_ac_kl, int* NSPEC_AB) {
+  Mesh* mp = get_mesh(Mesh_pointer);
+  if (!mp) return;
+  if (!NSPEC_AB || *NSPEC_AB != mp->nspec) { set_error(SF3D_ERR_ARG, "NSPEC_AB mismatch"); return; }
+  if (!mp->d_hess_ac_kl[0]) { set_error(SF3D_ERR_STATE, "APPROXIMATE_HESS_KL was not prepared in fluid elements"); return; }
+  const size_t nk = (size_t)NGLL3_PAD * mp->nspec;
+  std::vector<double> tmp(nk);
+  realw* h[3] = {h_hess_ac_kl, h_hess_rho_ac_kl, h_hess_kappa_ac_kl};
+  for (int q = 0; q < 3; ++q) {
+    if (!copy_sync(tmp.data(), mp->d_hess_ac_kl[q], sizeof(double) * nk, cudaMemcpyDeviceToHost, mp->stream)) return;
+    for (long e = 0; e < mp->nspec; ++e)
+      for (int p = 0; p < NGLL3; ++p) h[q][(size_t)NGLL3 * e + p] = (float)tmp[(size_t)NGLL3_PAD * e + p];
+  }
 }
 
 // compute_add_sources_ac_s3_cuda (compute_add_sources_acoustic_cuda.cu): the

@@ -392,12 +392,11 @@ void compute_kernels_hess_cuda_(long* Mesh_pointer, realw* deltat_f, int* ELASTI
                                 int* ACOUSTIC_SIMULATION) {
   Mesh* mp = get_mesh(Mesh_pointer);
   if (!mp) return;
-  if (!mp->hess_kl || !mp->d_hess_kl[0]) { set_error(SF3D_ERR_STATE, "APPROXIMATE_HESS_KL was not prepared"); return; }
-  if (ACOUSTIC_SIMULATION && *ACOUSTIC_SIMULATION && mp->has_acoustic) {
-    set_error(SF3D_ERR_ARG, "acoustic Hessian kernels are not supported");
+  if (ACOUSTIC_SIMULATION && *ACOUSTIC_SIMULATION && mp->has_acoustic &&
+      !launch_hess_acoustic(mp, (double)*deltat_f))
     return;
-  }
   if (ELASTIC_SIMULATION && !*ELASTIC_SIMULATION) return;
+  if (!mp->hess_kl || !mp->d_hess_kl[0]) { set_error(SF3D_ERR_STATE, "APPROXIMATE_HESS_KL was not prepared"); return; }
   const Ptrs10 E = {{mp->f.eps[0], mp->f.eps[1], mp->f.eps[2], mp->f.eps[3], mp->f.eps[4],
                      mp->b.eps[0], mp->b.eps[1], mp->b.eps[2], mp->b.eps[3], mp->b.eps[4]}};
   kernels_hess_kernel<<<mp->nspec, NGLL3_PAD, 0, mp->stream>>>(

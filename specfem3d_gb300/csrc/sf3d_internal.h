@@ -30,6 +30,9 @@ namespace sf3d {
 
 // Records the first error; returns false on failure so callers can bail out.
 bool set_error(int code, const std::string& msg);
+// acoustic Hessian kernels of one step (sf3d_acoustic.cu)
+struct Mesh;
+bool launch_hess_acoustic(Mesh* mp, double dt);
 bool cuda_ok(cudaError_t e, const char* what);
 #define SF3D_CUDA(call)                           \
   do {                                            \
@@ -202,6 +205,8 @@ struct Mesh {
   // 1: fluid kernels pair the adjoint chi_dd (the discrete adjoint variable of the
   // fluid) instead of chi (the reference's formula); sf3d_set_acoustic_kernel_pairing
   int ac_kernel_discrete = 0;
+  // APPROXIMATE_HESS_KL in fluid elements: hess_ac_kl, hess_rho_ac_kl, hess_kappa_ac_kl
+  double* d_hess_ac_kl[3] = {nullptr, nullptr, nullptr};
   float* d_rmass_acoustic = nullptr;
   int num_phase_ispec_ac = 0, nspec_outer_ac = 0, nspec_inner_ac = 0;
   int phase_valid_ac[2] = {0, 0};

@@ -552,6 +552,7 @@ void prepare_cleanup_device_(long* Mesh_pointer, int* ACOUSTIC_SIMULATION, int* 
   cudaFree(mp->d_potential_dot); cudaFree(mp->d_potential_dot_dot); cudaFree(mp->d_rmass_acoustic);
   cudaFree(mp->d_b_potential); cudaFree(mp->d_b_potential_dot); cudaFree(mp->d_b_potential_dot_dot);
   cudaFree(mp->d_rho_ac_kl); cudaFree(mp->d_kappa_ac_kl);
+  for (int q = 0; q < 3; ++q) cudaFree(mp->d_hess_ac_kl[q]);
   cudaFree(mp->d_phase_ispec_ac); cudaFree(mp->d_fs_ispec); cudaFree(mp->d_fs_pt); cudaFree(mp->d_cp_ispec);
   cudaFree(mp->d_cp_pt); cudaFree(mp->d_cp_normal); cudaFree(mp->d_cp_jw); cudaFree(mp->d_seismo_p);
   cudaFree(mp->d_rec_is_acoustic);

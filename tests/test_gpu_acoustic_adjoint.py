@@ -72,7 +72,7 @@ def _volume(db):
     return jac * w3[None, :]
 
 
-def _run(stacey, fluid_source, discrete=False):
+def _run(stacey, fluid_source, discrete=False, hessian=False):
     from specfem3d_gb300 import adjoint as ADJ
     from specfem3d_gb300.solver import GPUSolver
     cfg, mat = _setup()
@@ -90,14 +90,14 @@ def _run(stacey, fluid_source, discrete=False):
     g.close()
     hist = []
     kl = ADJ.kernel_run_coupled(db, cfg, seis.astype(np.float64), fin_el, fin_ac, rec_el, rec_ac, history=hist,
-                                discrete_fluid_kernels=discrete)
+                                discrete_fluid_kernels=discrete, hessian=hessian)
     return cfg, mat, db, seis, H, hist, kl
 
 
 @pytest.fixture(scope="module")
 def run_stacey(gpulib):
     """Stacey faces on the sides and bottom, a source in each domain."""
-    return _run(True, True)
+    return _run(True, True, hessian=True)
 
 
 @pytest.fixture(scope="module")
@@ -245,3 +245,28 @@ def test_discrete_fluid_kernels_match_finite_differences(run_discrete, param):
     e = abs(pred - fd) / abs(fd)
     print(f"discrete fluid {param}: finite difference {fd:.6e}, kernels {pred:.6e}, relative {e:.2e}")
     assert abs(fd) > 0 and e < 1e-3
+
+
+def test_fluid_hessian_kernels_equal_the_reference_accumulation(run_stacey):
+    """hess_ac_kl, hess_rho_ac_kl, hess_kappa_ac_kl (compute_kernels.f90:459-510:
+    gradients carry 1/rho) against the host restatement from the fields of every
+    step; the device returns them in FP32 like transfer_kernels_hess_ac_tohost."""
+    cfg, mat, db, seis, H, hist, kl = run_stacey
+    n, dt = int(db["nspec"]), float(cfg["dt"])
+    fluid = np.repeat(np.asarray(db["ispec_is_acoustic"]) > 0, 125).reshape(n, 125)
+    ib = np.asarray(db["ibool"]).reshape(n, 125) - 1
+    rho = np.asarray(db["rhostore"], np.float64).reshape(n, 125)
+    kap = np.asarray(db["kappastore"], np.float64).reshape(n, 125)
+    hs, hr, hk = (np.zeros((n, 125)) for _ in range(3))
+    for h in hist:
+        ga, gb, gv = (_gradient(db, h[k]) / rho for k in ("chi_dd", "b_chi_dd", "b_chi_dot"))
+        hs += dt * np.sum(ga * gb, axis=0)
+        hr += dt * rho * np.sum(gv * gv, axis=0)
+        hk += dt * h["b_chi_dot"].astype(np.float64)[ib] ** 2 / kap
+    errs = {}
+    for name, ref in (("hess_ac", hs), ("hess_rho_ac", hr), ("hess_kappa_ac", hk)):
+        errs[name] = np.linalg.norm((kl[name] - ref)[fluid]) / np.linalg.norm(ref[fluid])
+        assert np.abs(ref[fluid]).max() > 0
+        assert not kl[name][~fluid].any()
+    print("fluid Hessian kernels vs host restatement: " + ", ".join(f"{k} {v:.2e}" for k, v in errs.items()))
+    assert all(v < 1e-5 for v in errs.values())
