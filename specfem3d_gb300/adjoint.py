@@ -137,6 +137,8 @@ def kernel_run_coupled(db: dict, cfg: dict, adjoint_source: np.ndarray, final_el
     (fluid), each (nspec, 125)."""
     if int(db.get("attenuation", 0)):
         raise ValueError("kernel_run_coupled: the time-reversed reconstruction is for meshes without attenuation")
+    if not np.asarray(db.get("ispec_is_acoustic", [0])).any():
+        raise ValueError("kernel_run_coupled: the mesh has no fluid elements (use kernel_run)")
     nstep = int(cfg["nstep"])
     g = GPUSolver(db, cfg, nlength=nstep, simulation_type=3)
     L = g.L

@@ -762,13 +762,15 @@ void prepare_fields_acoustic_adj_dev_(long* Mesh_pointer, int* APPROXIMATE_HESS_
   if (!mp) return;
   if (!mp->has_acoustic) { set_error(SF3D_ERR_STATE, "prepare_fields_acoustic_device not called"); return; }
   const long nglob = mp->nglob, nk = (long)NGLL3_PAD * mp->nspec;
-  if (mp->d_b_potential) return;
-  bool ok = alloc_zero((void**)&mp->d_b_potential, sizeof(float) * nglob) &&
-            alloc_zero((void**)&mp->d_b_potential_dot, sizeof(float) * nglob) &&
-            alloc_zero((void**)&mp->d_b_potential_dot_dot, sizeof(float) * nglob) &&
-            alloc_zero((void**)&mp->d_rho_ac_kl, sizeof(double) * nk) &&
-            alloc_zero((void**)&mp->d_kappa_ac_kl, sizeof(double) * nk);
-  for (int q = 0; q < 3 && ok && APPROXIMATE_HESS_KL && *APPROXIMATE_HESS_KL; ++q)
+  bool ok = true;
+  if (!mp->d_b_potential)
+    ok = alloc_zero((void**)&mp->d_b_potential, sizeof(float) * nglob) &&
+         alloc_zero((void**)&mp->d_b_potential_dot, sizeof(float) * nglob) &&
+         alloc_zero((void**)&mp->d_b_potential_dot_dot, sizeof(float) * nglob) &&
+         alloc_zero((void**)&mp->d_rho_ac_kl, sizeof(double) * nk) &&
+         alloc_zero((void**)&mp->d_kappa_ac_kl, sizeof(double) * nk);
+  // a repeated call may add the Hessian accumulators
+  for (int q = 0; q < 3 && ok && APPROXIMATE_HESS_KL && *APPROXIMATE_HESS_KL && !mp->d_hess_ac_kl[q]; ++q)
     ok = alloc_zero((void**)&mp->d_hess_ac_kl[q], sizeof(double) * nk);
 }
 
