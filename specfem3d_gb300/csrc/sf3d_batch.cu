@@ -859,6 +859,7 @@ int sf3d_batch_autotune(long* Mesh_pointer, int reps, float* ms_table, int* best
 }
 
 int sf3d_batch_iterate(long* Mesh_pointer, int it_begin, int it_end, realw deltat, int steps_per_graph) {
+  NvtxRange nvtx_range("sf3d_batch_iterate");
   Mesh* mp = get_mesh(Mesh_pointer);
   if (!mp) return SF3D_ERR_STATE;
   if (!batch_ready(mp)) return SF3D_ERR_STATE;

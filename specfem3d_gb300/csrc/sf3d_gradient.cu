@@ -514,6 +514,7 @@ int sf3d_gradient_setup(long* Mesh_pointer, int nstep, int checkpoint_every, dou
 }
 
 int sf3d_gradient_forward(long* Mesh_pointer, realw deltat) {
+  NvtxRange nvtx_range("sf3d_gradient_forward");
   Mesh* mp = get_mesh(Mesh_pointer);
   if (!mp) return SF3D_ERR_STATE;
   if (!grad_ready(mp)) return SF3D_ERR_STATE;
@@ -583,6 +584,7 @@ int sf3d_gradient_set_residual(long* Mesh_pointer, const realw* residual) {
 }
 
 int sf3d_gradient_backward(long* Mesh_pointer, realw deltat) {
+  NvtxRange nvtx_range("sf3d_gradient_backward");
   Mesh* mp = get_mesh(Mesh_pointer);
   if (!mp) return SF3D_ERR_STATE;
   if (!grad_ready(mp)) return SF3D_ERR_STATE;

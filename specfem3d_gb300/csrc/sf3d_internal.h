@@ -11,6 +11,7 @@
 //     host transfers of the Fortran arrays are plain copies.
 #pragma once
 
+#include <nvtx3/nvToolsExt.h>
 #include <cuda_fp16.h>
 #include <cuda_runtime.h>
 #include <stdint.h>
@@ -30,6 +31,15 @@ namespace sf3d {
 
 // Records the first error; returns false on failure so callers can bail out.
 bool set_error(int code, const std::string& msg);
+
+// NVTX range over one library call (header-only NVTX v3: inactive unless a
+// profiler is attached), so timelines show the step blocks, sweeps and passes
+struct NvtxRange {
+  explicit NvtxRange(const char* name) { nvtxRangePushA(name); }
+  ~NvtxRange() { nvtxRangePop(); }
+  NvtxRange(const NvtxRange&) = delete;
+  NvtxRange& operator=(const NvtxRange&) = delete;
+};
 // acoustic Hessian kernels of one step (sf3d_acoustic.cu)
 struct Mesh;
 bool launch_hess_acoustic(Mesh* mp, double dt);

@@ -249,6 +249,7 @@ void prepare_smooth_gpu_(long* Container, realw* xstore_me, realw* ystore_me, re
 
 void compute_smooth_gpu_(long* smooth_pointer, realw* data_other, realw* integ_factor, realw* xstore_other,
                          realw* ystore_other, realw* zstore_other, const int* nspec_other_f) {
+  NvtxRange nvtx_range("compute_smooth_gpu");
   SmoothState* sp = get_smooth(smooth_pointer);
   if (!sp) return;
   const int nso = *nspec_other_f;

@@ -674,6 +674,7 @@ int sf3d_set_stf_table(long* Mesh_pointer, const double* h_stf, int nsources, in
 }
 
 int sf3d_iterate_time(long* Mesh_pointer, int it_begin, int it_end, realw deltat, int steps_per_graph, int flags) {
+  NvtxRange nvtx_range("sf3d_iterate_time");
   Mesh* mp = get_mesh(Mesh_pointer);
   if (!mp) return SF3D_ERR_STATE;
   if (!mp->f.displ) { set_error(SF3D_ERR_STATE, "prepare_fields_elastic_device not called"); return SF3D_ERR_STATE; }
