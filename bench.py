@@ -116,21 +116,73 @@ class ClockSampler:
 WORKLOAD = "layered viscoelastic 20x20x10 km, 128x128x64 hexes, N_SLS=3, Stacey 5 faces"
 
 
-def cpu_baseline(steps: int, nthreads: int, warmup: int = 1):
-    """Oracle (FP32, OpenMP) on a bounded sample with the bench physics: a 32x32x16
-    block of the same layered viscoelastic model (irregular elements, Stacey)."""
+def cpu_baseline(steps: int, nthreads: int, warmup: int = 1, db=None, cfg=None):
+    """CPU oracle (FP32 C restatement of the reference CPU solver, OpenMP over nthreads)
+    on the bench workload itself: the full 128x128x64-element layered viscoelastic mesh,
+    `warmup` untimed steps then `steps` timed ones.  db/cfg: an already built database
+    of that workload (built here when absent)."""
     from oracle import oracle as O
     from specfem3d_gb300 import configs, meshgen
-    cfg = configs.layered_viscoelastic(nstep=steps + warmup + 2, nx=32, ny=32, counts=(4, 6, 6))
-    cfg["x1"] = 20000.0 * 32 / 128
-    cfg["y1"] = 20000.0 * 32 / 128
-    db = meshgen.build_database(cfg)
+    if db is None:
+        cfg = configs.layered_viscoelastic(nstep=steps + warmup + 2)
+        db = meshgen.build_database(cfg)
     sim = O.make_sim(db, cfg, "f32", nthreads=nthreads)
     sim.step(max(1, warmup))
     t = time.perf_counter()
     sim.step(steps)
     dt = time.perf_counter() - t
+    del sim
     return db["nglob"] * steps / dt, dict(nspec=db["nspec"], nglob=db["nglob"], steps=steps, seconds=dt)
+
+
+def _per_trace_rel_l2(a, ref):
+    """rel-L2 of every receiver's trace (3 components x samples), float64."""
+    a = np.asarray(a, np.float64).reshape(a.shape[0], -1)
+    r = np.asarray(ref, np.float64).reshape(ref.shape[0], -1)
+    nr = np.linalg.norm(r, axis=1)
+    e = np.linalg.norm(a - r, axis=1) / np.maximum(nr, 1e-300)
+    return e, nr
+
+
+def l2_error_leg(steps: int = 500, nx: int = 32, formats=("fp32", "fp16", "bf16", "packed-fp16")):
+    """Per-seismogram relative L2 error of the device run against the FP64 oracle (the
+    reference's algorithm with double-precision CUSTOM_REAL) on the bench physics at a
+    size the FP64 oracle finishes in seconds: the layered viscoelastic 20x20x10 km block
+    at nx x nx x nx/2 elements (4/6/6 element rows per layer), N_SLS = 3, Stacey, the
+    same source at 8 km depth and the 400 surface receivers, `steps` steps.  One device
+    run per geometry storage format."""
+    from oracle import oracle as O
+    from specfem3d_gb300 import configs, meshgen
+    from specfem3d_gb300.solver import GPUSolver
+    cfg = configs.layered_viscoelastic(nstep=steps, nx=nx, ny=nx, counts=(nx // 8, 3 * nx // 16, 3 * nx // 16))
+    db = meshgen.build_database(cfg)
+    t0 = time.perf_counter()
+    sim = O.make_sim(db, cfg, "f64", nthreads=os.cpu_count() or 1)
+    sim.step(steps)
+    ref = O.seismograms(sim)
+    t_oracle = time.perf_counter() - t0
+    del sim
+    out = {"workload": f"layered viscoelastic 20x20x10 km, {nx}x{nx}x{nx // 2} hexes, N_SLS=3, Stacey 5 faces, "
+                       f"{int(db['nrec'])} surface receivers",
+           "nstep": steps, "t_end_s": float(cfg["dt"]) * steps, "oracle": "FP64 C restatement",
+           "oracle_s": t_oracle, "metric": "rel-L2 per receiver trace (3 components x samples), float64"}
+    for fmt in formats:
+        g = GPUSolver(db, cfg)
+        try:
+            g.set_geometry_format(fmt)
+        except Exception as exc:  # a format this build does not offer
+            out[fmt] = {"unavailable": str(exc)[:200]}
+            g.close()
+            continue
+        g.run(steps, steps_per_graph=50)
+        seis = g.seismograms()
+        g.close()
+        e, nr = _per_trace_rel_l2(seis, ref)
+        strong = nr >= 1e-2 * nr.max()
+        out[fmt] = {"median": float(np.median(e)), "p95": float(np.percentile(e, 95)), "max": float(e.max()),
+                    "max_strong_traces": float(e[strong].max()), "all_traces": float(
+                        np.linalg.norm(np.asarray(seis, np.float64) - ref) / np.linalg.norm(ref))}
+    return out
 
 
 def adjoint_leg(nshots: int):
@@ -286,15 +338,14 @@ def run_reference(args, rank):
     nthreads = os.cpu_count() or 1
     steps = max(1, args.steps)
     val, info = cpu_baseline(steps, nthreads, warmup=max(1, args.warmup))
-    sample = (f"CPU oracle (C restatement of the reference CPU solver, not the reference binary) on a "
-              f"32x32x16-element block with the bench physics ({info['nglob']} points), {steps} steps "
-              f"after {max(1, args.warmup)} warm-up steps; the reference's Fortran solver cannot be built "
-              f"(no Fortran compiler or MPI)")
+    sample = (f"CPU oracle (C restatement of the reference CPU solver, not the reference binary; FP32, OpenMP "
+              f"over {nthreads} threads) on the full bench mesh ({info['nspec']} elements, {info['nglob']} points), "
+              f"{steps} steps after {max(1, args.warmup)} warm-up steps; the reference's Fortran solver cannot be "
+              f"built (no Fortran compiler or MPI)")
     line = {"metric": METRIC, "value": val, "unit": UNIT, "n_gpus": args.gpus, "steps": steps,
             "warmup": args.warmup, "ms_per_step": 1000 * info["seconds"] / steps, "higher_is_better": True,
             "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
-            "config": {"workload": WORKLOAD, "cpu_sample_elements": info["nspec"],
-                       "cpu_sample_points": info["nglob"]},
+            "config": {"workload": WORKLOAD, "nspec": info["nspec"], "nglob": info["nglob"]},
             "impl": "reference",
             "cpu_baseline": {"value": val, "unit": UNIT, "cores": nthreads, "kind": "port", "sample": sample},
             "e2e": {"value": val, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
@@ -312,20 +363,22 @@ def main():
     ap.add_argument("--graph", type=int, default=50, help="steps per captured CUDA graph")
     ap.add_argument("--tile", type=int, default=0, help="process elements in tiles of tile^3 (0: mesh order)")
     ap.add_argument("--e2e-steps", type=int, default=50)
-    ap.add_argument("--cpu-steps", type=int, default=40)
+    ap.add_argument("--cpu-steps", type=int, default=10, help="timed CPU-oracle steps on the full bench mesh")
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--variant", type=int, default=-1,
                     help="stiffness kernel variant (sf3d_set_stiffness_variant); -1: autotune at rest")
-    ap.add_argument("--batch", type=int, default=0,
+    ap.add_argument("--batch", type=int, default=32,
                     help="also time this many shots of the batched-shots workload against the plain path (0: skip)")
     ap.add_argument("--batch-steps", type=int, default=100)
     ap.add_argument("--batch-nx", type=int, default=64, help="elements along x and y of the batched mesh")
-    ap.add_argument("--coupled", type=int, default=0, help="also time this many steps of the coupled workload")
+    ap.add_argument("--coupled", type=int, default=100, help="also time this many steps of the coupled workload")
     ap.add_argument("--aniso", type=int, default=0,
                     help="also time this many steps of the main workload with anisotropic stiffness (0: skip)")
     ap.add_argument("--smooth", action="store_true", help="also time the Gaussian smoothing of three kernels")
     ap.add_argument("--smooth-nx", type=int, default=64, help="elements along x and y of the smoothing block")
-    ap.add_argument("--adjoint", type=int, default=0,
+    ap.add_argument("--l2-steps", type=int, default=500,
+                    help="steps of the seismogram-error run against the FP64 oracle (0: skip)")
+    ap.add_argument("--adjoint", type=int, default=8,
                     help="also time the checkpointed misfit gradient over this many shots of the "
                          "8-shot 64x64x32 gradient workload (0: skip)")
     ap.add_argument("--roofline-steps", type=int, default=20,
@@ -429,6 +482,10 @@ def main():
     abi.check()
     color_ms = tc["stiffness_ms"] / max(tc["stiffness_launches"], 1)
     aniso = aniso_leg(db, cfg, args.aniso) if args.aniso > 0 else None
+    cpu = None
+    if rank == 0 and not args.no_cpu and args.cpu_steps > 0:
+        # the CPU oracle on this very mesh (same database, same physics)
+        cpu = cpu_baseline(args.cpu_steps, os.cpu_count() or 1, warmup=1, db=db, cfg=cfg)
     del db
     line = {
         "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": K, "warmup": W,
@@ -440,8 +497,9 @@ def main():
         "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
                      "peak_kind": peak_kind,
                      "traffic": (traffic_pe if (traffic_pe and nspec == 1048576) else None),
+                     "traffic_kind": "constant from a committed ncu profile, not measured in this run",
                      "traffic_note": ("ncu dram__bytes_read.sum + dram__bytes_write.sum of one stiffness launch "
-                                      "of this mesh (profiles/stiffness_kernel_att_traffic_layered_128x128x64.md)"),
+                                      "of this mesh, read from profiles/stiffness_kernel_att_traffic_layered_128x128x64.md"),
                      "kernel": ("stiffness_pipe_kernel<att>" if args.variant == 1 else
                                 f"stiffness_{'split_' if args.variant >= 10 else ''}kernel<att, "
                                 f"{[4, 0, 5, 6, 7, 6, 7, 8, 6, 7, 3, 4][args.variant]} CTAs/SM"
@@ -478,12 +536,14 @@ def main():
         line["anisotropic"] = aniso
     if args.smooth:
         line["smoothing"] = smooth_leg(args.smooth_nx)
-    if rank == 0 and not args.no_cpu:
-        cv, info = cpu_baseline(args.cpu_steps, os.cpu_count() or 1)
+    if args.l2_steps > 0:
+        line["l2_error"] = l2_error_leg(args.l2_steps)
+    if cpu is not None:
+        cv, info = cpu
         line["cpu_baseline"] = {"value": cv, "unit": UNIT, "cores": os.cpu_count() or 1, "kind": "port",
-                                "sample": f"CPU oracle, 32x32x16-element block with the bench physics "
-                                          f"({info['nglob']} points), {info['steps']} steps, "
-                                          f"{info['seconds']:.1f} s"}
+                                "sample": f"CPU oracle (FP32 C restatement, OpenMP) on the bench mesh itself "
+                                          f"({info['nspec']} elements, {info['nglob']} points), {info['steps']} "
+                                          f"steps after 1 warm-up step, {info['seconds']:.1f} s"}
     if rank == 0:
         print(json.dumps(line), flush=True)
     if dist:

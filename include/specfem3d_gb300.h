@@ -454,6 +454,9 @@ int sf3d_gradient_release(long *Mesh_pointer);
  *     before any stream capture begins;
  *   - calls that overlap in time on one device (other streams or host
  *     threads) share the scratch and race: serialise them;
+ *   - a non-null `stream` must belong to the current device (SF3D_ERR_ARG
+ *     otherwise); a process that resets the device (cudaDeviceReset) must
+ *     not call this entry point afterwards (the cached address is gone);
  *   - returns after the result is on the host (synchronises `stream`). */
 int sf3d_field_maxabs_noalloc(const realw *d_field, long n, void *stream, realw *max_abs);
 

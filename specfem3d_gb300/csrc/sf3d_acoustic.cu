@@ -30,13 +30,19 @@ struct AcField {
   float* pdd;
 };
 
+// every array prepare_fields_acoustic_adj_dev allocates is present
+inline bool ac_adj_ready(const Mesh* mp) {
+  return mp->d_b_potential && mp->d_b_potential_dot && mp->d_b_potential_dot_dot && mp->d_rho_ac_kl &&
+         mp->d_kappa_ac_kl;
+}
+
 bool ac_field(Mesh* mp, const int* fa, AcField* F) {
   if (!fa || (*fa != 1 && *fa != 3)) return set_error(SF3D_ERR_ARG, "FORWARD_OR_ADJOINT must be 1 or 3 for acoustic fields");
   if (*fa == 1) {
     *F = {mp->d_potential, mp->d_potential_dot, mp->d_potential_dot_dot};
     return true;
   }
-  if (!mp->d_b_potential) return set_error(SF3D_ERR_STATE, "prepare_fields_acoustic_adj_dev not called");
+  if (!ac_adj_ready(mp)) return set_error(SF3D_ERR_STATE, "prepare_fields_acoustic_adj_dev not called");
   *F = {mp->d_b_potential, mp->d_b_potential_dot, mp->d_b_potential_dot_dot};
   return true;
 }
@@ -762,13 +768,15 @@ void prepare_fields_acoustic_adj_dev_(long* Mesh_pointer, int* APPROXIMATE_HESS_
   if (!mp) return;
   if (!mp->has_acoustic) { set_error(SF3D_ERR_STATE, "prepare_fields_acoustic_device not called"); return; }
   const long nglob = mp->nglob, nk = (long)NGLL3_PAD * mp->nspec;
+  // each array is allocated where it is still missing, so a repeated call after a
+  // failed allocation completes the set instead of leaving later pointers null
   bool ok = true;
-  if (!mp->d_b_potential)
-    ok = alloc_zero((void**)&mp->d_b_potential, sizeof(float) * nglob) &&
-         alloc_zero((void**)&mp->d_b_potential_dot, sizeof(float) * nglob) &&
-         alloc_zero((void**)&mp->d_b_potential_dot_dot, sizeof(float) * nglob) &&
-         alloc_zero((void**)&mp->d_rho_ac_kl, sizeof(double) * nk) &&
-         alloc_zero((void**)&mp->d_kappa_ac_kl, sizeof(double) * nk);
+  float** pot[3] = {&mp->d_b_potential, &mp->d_b_potential_dot, &mp->d_b_potential_dot_dot};
+  for (int q = 0; q < 3 && ok; ++q)
+    if (!*pot[q]) ok = alloc_zero((void**)pot[q], sizeof(float) * nglob);
+  double** kl[2] = {&mp->d_rho_ac_kl, &mp->d_kappa_ac_kl};
+  for (int q = 0; q < 2 && ok; ++q)
+    if (!*kl[q]) ok = alloc_zero((void**)kl[q], sizeof(double) * nk);
   // a repeated call may add the Hessian accumulators
   for (int q = 0; q < 3 && ok && APPROXIMATE_HESS_KL && *APPROXIMATE_HESS_KL && !mp->d_hess_ac_kl[q]; ++q)
     ok = alloc_zero((void**)&mp->d_hess_ac_kl[q], sizeof(double) * nk);
@@ -798,7 +806,7 @@ void compute_add_sources_ac_s3_cuda_(long* Mesh_pointer, int* NSOURCESf, double*
   (void)run_number_of_the_source;
   Mesh* mp = get_mesh(Mesh_pointer);
   if (!mp || !mp->has_acoustic) return;
-  if (!mp->d_b_potential) { set_error(SF3D_ERR_STATE, "prepare_fields_acoustic_adj_dev not called"); return; }
+  if (!ac_adj_ready(mp)) { set_error(SF3D_ERR_STATE, "prepare_fields_acoustic_adj_dev not called"); return; }
   if (mp->nsources_local == 0 || mp->nsources == 0) return;
   if (*NSOURCESf != mp->nsources) { set_error(SF3D_ERR_ARG, "NSOURCES mismatch"); return; }
   std::vector<float> stf(mp->nsources);
@@ -817,7 +825,7 @@ void compute_add_sources_ac_s3_cuda_(long* Mesh_pointer, int* NSOURCESf, double*
 void compute_kernels_acoustic_cuda_(long* Mesh_pointer, realw* deltat_f) {
   Mesh* mp = get_mesh(Mesh_pointer);
   if (!mp) return;
-  if (!mp->d_rho_ac_kl) { set_error(SF3D_ERR_STATE, "prepare_fields_acoustic_adj_dev not called"); return; }
+  if (!ac_adj_ready(mp)) { set_error(SF3D_ERR_STATE, "prepare_fields_acoustic_adj_dev not called"); return; }
   Metric9 m;
   for (int q = 0; q < 9; ++q) m.p[q] = mp->d_metric[q];
   kernels_acoustic_kernel<<<mp->nspec, NGLL3_PAD, 0, mp->stream>>>(
@@ -829,7 +837,7 @@ void compute_kernels_acoustic_cuda_(long* Mesh_pointer, realw* deltat_f) {
 }
 
 static bool ac_kernels_to_host(Mesh* mp, double* h_rho, double* h_kappa, float* f_rho, float* f_kappa) {
-  if (!mp->d_rho_ac_kl) return set_error(SF3D_ERR_STATE, "acoustic kernels not allocated");
+  if (!mp->d_rho_ac_kl || !mp->d_kappa_ac_kl) return set_error(SF3D_ERR_STATE, "acoustic kernels not allocated");
   const size_t nk = (size_t)NGLL3_PAD * mp->nspec;
   std::vector<double> tmp(nk);
   const double* d[2] = {mp->d_rho_ac_kl, mp->d_kappa_ac_kl};

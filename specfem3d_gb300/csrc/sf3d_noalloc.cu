@@ -8,9 +8,13 @@
 // the last two slots.  Every slot that is read was written earlier in the same
 // call, so nothing has to start at zero.  The device address of the array is
 // looked up with cudaGetSymbolAddress on the first call on each device (with
-// that device current) and cached; no call allocates or frees memory.  Two
-// calls that overlap in time on the same device (different streams or host
-// threads) share the array and race; callers serialise them.
+// that device current) and cached; no call allocates or frees memory.  The
+// cached address belongs to the device's primary context: a caller that resets
+// the device (cudaDeviceReset) between calls unloads the module and must not
+// call this entry point again in that process.  A non-null stream must belong
+// to the current device (checked).  Two calls that overlap in time on the same
+// device (different streams or host threads) share the array and race; callers
+// serialise them.
 #include <math.h>
 #include <mutex>
 #include <string.h>
@@ -140,9 +144,20 @@ int sf3d_field_maxabs_noalloc(const realw* d_field, long n, void* stream, realw*
               "per 16384 values)");
     return SF3D_ERR_ARG;
   }
+  cudaStream_t s = static_cast<cudaStream_t>(stream);
+  if (s) {
+    // the scratch address is the current device's: a stream of another device
+    // would launch against it
+    int sdev = -1, cur = -1;
+    if (!cuda_ok(cudaStreamGetDevice(s, &sdev), "cudaStreamGetDevice") || !cuda_ok(cudaGetDevice(&cur), "cudaGetDevice"))
+      return SF3D_ERR_CUDA;
+    if (sdev != cur) {
+      set_error(SF3D_ERR_ARG, "sf3d_field_maxabs_noalloc: the stream belongs to another device than the current one");
+      return SF3D_ERR_ARG;
+    }
+  }
   float* scratch = scratch_on_current_device();
   if (!scratch) return SF3D_ERR_CUDA;
-  cudaStream_t s = static_cast<cudaStream_t>(stream);
   const int nblocks = (int)((n + kNoAllocPerBlock - 1) / kNoAllocPerBlock);
   noalloc_partial_kernel<<<nblocks, kNoAllocThreads, 0, s>>>(d_field, n, scratch);
   noalloc_final_kernel<<<1, kNoAllocThreads, 0, s>>>(nblocks, scratch);

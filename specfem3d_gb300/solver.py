@@ -363,6 +363,14 @@ class GPUSolver:
         if self.L.sf3d_set_geometry_precision(self.mp, int(bits)) != 0:
             abi.check()
 
+    def set_geometry_format(self, fmt: str):
+        """Storage of the stiffness kernel's static per-element streams: "fp32", or
+        "fp16" (16-bit rows with a per-element (offset, scale))."""
+        bits = {"fp32": 32, "fp16": 16}.get(fmt)
+        if bits is None:
+            raise ValueError(f"geometry format {fmt!r} is not offered")
+        self.set_geometry_precision(bits)
+
     def check_stability(self, threshold: float = 1e25):
         m = ctypes.c_float()
         rc = self.L.sf3d_check_stability(self.mp, float(threshold), ctypes.addressof(m))

@@ -1,7 +1,7 @@
 """Extract the reference's golden seismograms into compact fixtures.
 
 Run in a checkout where the SPECFEM3D reference tree is available (its path is
-the first argument, default /root/reference).  It reads the ASCII
+the first argument, or the environment variable SPECFEM3D_REFERENCE).  It reads the ASCII
 traces (.semd, .semv, .sema) committed under the reference's example REF_SEIS
 directories and writes float32 arrays (station, component, sample) plus the time
 axis to tests/golden/*.npz.  The fixtures are used by the oracle and GPU parity tests,
@@ -88,7 +88,9 @@ def read_analytic_elastic(root):
 
 
 def main():
-    root = sys.argv[1] if len(sys.argv) > 1 else "/root/reference"
+    root = sys.argv[1] if len(sys.argv) > 1 else os.environ.get("SPECFEM3D_REFERENCE", "")
+    if not root or not os.path.isdir(root):
+        sys.exit("usage: %s <SPECFEM3D source tree> (or set SPECFEM3D_REFERENCE)" % sys.argv[0])
     out = os.path.dirname(os.path.abspath(__file__))
     d, t = read(root, "homogeneous_halfspace_HEX8_elastic_absorbing_Stacey_5sides", "semd")
     np.savez_compressed(os.path.join(out, "refex_stacey5sides.npz"), displ=d, t=t, stations=np.array(STATIONS))

@@ -2,7 +2,8 @@
 against the block builder and against the oracle's C restatement of
 xgenerate_databases + the solver's point location, on a structured block, a block
 with randomly moved interior nodes, a rotated block, and the reference's own CUBIT
-mesh files when the reference tree is present.
+mesh files when the reference tree is present (its root in the environment variable
+SPECFEM3D_REFERENCE).
 
 Bars: integer arrays (ibool, nglob, irregular numbering, face ijk, selected
 elements) bit-exact; metric terms and face geometry within 2 float32 ulps of the
@@ -17,7 +18,8 @@ import pytest
 from conftest import ROOT
 import hexmesh_cases as C
 
-REF_EXAMPLES = "/root/reference/EXAMPLES/applications"
+# root of a SPECFEM3D source tree (read-only); the two tests on its CUBIT meshes skip without it
+REF_EXAMPLES = os.path.join(os.environ.get("SPECFEM3D_REFERENCE", ""), "EXAMPLES", "applications")
 
 INT_KEYS = ["ibool", "irregular_element_number", "abs_boundary_ispec", "abs_boundary_ijk", "ispec_selected_source",
             "ispec_selected_rec", "coupling_ac_el_ispec", "coupling_ac_el_ijk", "free_surface_ispec",
@@ -155,7 +157,7 @@ def test_source_octant_choice_agrees_between_block_and_general_paths():
         assert np.abs(d["sourcearrays"] - a["sourcearrays"]).max() <= 1e-6 * np.abs(a["sourcearrays"]).max()
 
 
-@pytest.mark.skipif(not os.path.isdir(REF_EXAMPLES), reason="reference tree not present")
+@pytest.mark.skipif(not os.path.isdir(REF_EXAMPLES), reason="SPECFEM3D_REFERENCE does not name a reference tree")
 def test_reference_cubit_mesh_files():
     """The reference example's own MESH-default (a CUBIT mesh of the same block with
     its elements in another order and orientation): the database has the block's
@@ -187,7 +189,7 @@ def test_reference_cubit_mesh_files():
         assert np.allclose(w @ xyz[e], [x, y, z], atol=1e-6 * 134000.0)
 
 
-@pytest.mark.skipif(not os.path.isdir(REF_EXAMPLES), reason="reference tree not present")
+@pytest.mark.skipif(not os.path.isdir(REF_EXAMPLES), reason="SPECFEM3D_REFERENCE does not name a reference tree")
 def test_reference_cubit_waterlayered_mesh():
     """waterlayered_halfspace's own CUBIT mesh, Par_file, CMTSOLUTION and STATIONS
     read and set up by the general path give the database of the block

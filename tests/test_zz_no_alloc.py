@@ -56,3 +56,33 @@ def test_noalloc_maxabs_matches_check_stability(gpulib):
     with pytest.raises(abi.SF3DError, match="256 KB scratch"):
         abi.check()
     g.close()
+
+
+def test_noalloc_maxabs_many_blocks_and_at_the_limit(gpulib):
+    """Device buffers of 6,000,000 values (367 partials: the final pass strides over
+    more than 256 of them) and of exactly the documented maximum, 536,854,528 values
+    (2.1 GB, 32,767 partials); the maximum equals the buffer's true max |x|, twice in
+    a row, and a NaN in the last block of the large buffer is reported as NaN."""
+    torch = pytest.importorskip("torch")
+    from specfem3d_gb300 import abi
+    L = abi.load()
+    L.sf3d_field_maxabs_noalloc.restype = ctypes.c_int
+    L.sf3d_field_maxabs_noalloc.argtypes = [ctypes.c_void_p, ctypes.c_long, ctypes.c_void_p,
+                                            ctypes.POINTER(ctypes.c_float)]
+    torch.cuda.synchronize()
+    gen = torch.Generator(device="cuda").manual_seed(11)
+    for n, spot in ((6_000_000, 5_999_001), (536_854_528, 536_854_000)):
+        x = torch.randn(n, device="cuda", generator=gen)
+        x[spot] = -123.5                       # the maximum sits in the last partial
+        torch.cuda.synchronize()
+        ref = float(x.abs().max().item())
+        assert ref == 123.5
+        for _ in range(2):
+            rc, m = _noalloc(L, x.data_ptr(), n)
+            assert rc == 0 and m == ref
+        x[spot] = float("nan")
+        torch.cuda.synchronize()
+        rc, m = _noalloc(L, x.data_ptr(), n)
+        assert rc == 0 and np.isnan(m)
+        del x
+        torch.cuda.empty_cache()
