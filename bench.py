@@ -144,54 +144,61 @@ def _per_trace_rel_l2(a, ref):
     return e, nr
 
 
-def l2_error_leg(steps: int = 500, nx: int = 32, formats=("fp32", "fp16", "bf16", "packed-fp16")):
+def l2_error_leg(steps: int = 500, nx: int = 32, formats=("fp32", "fp16", "bf16", "packed-fp32")):
     """Per-seismogram relative L2 error of the device run against the FP64 oracle (the
-    reference's algorithm with double-precision CUSTOM_REAL) on the bench physics at a
-    size the FP64 oracle finishes in seconds: the layered viscoelastic 20x20x10 km block
-    at nx x nx x nx/2 elements (4/6/6 element rows per layer), N_SLS = 3, Stacey, the
-    same source at 8 km depth and the 400 surface receivers, `steps` steps.  One device
-    run per geometry storage format."""
+    reference's algorithm with double-precision CUSTOM_REAL, on a database built in
+    double precision) at a size the FP64 oracle finishes in seconds, for every
+    geometry storage format, on two models:
+    * "layered": the bench physics, 20x20x10 km at nx x nx x nx/2 elements (4/6/6
+      element rows per layer), N_SLS = 3, Stacey, the source at 8 km depth, the 400
+      surface receivers;
+    * "perturbed": the batched-shots model (+-5 % Gaussian-correlated vp/vs per GLL
+      point, no attenuation) at nx x nx x nx/2 elements, its first shot, 25 receivers."""
     from oracle import oracle as O
-    from specfem3d_gb300 import configs, meshgen
+    from specfem3d_gb300 import configs, gradient as G, meshgen
     from specfem3d_gb300.solver import GPUSolver
-    cfg = configs.layered_viscoelastic(nstep=steps, nx=nx, ny=nx, counts=(nx // 8, 3 * nx // 16, 3 * nx // 16))
-    db = meshgen.build_database(cfg)
-    t0 = time.perf_counter()
-    sim = O.make_sim(db, cfg, "f64", nthreads=os.cpu_count() or 1)
-    sim.step(steps)
-    ref = O.seismograms(sim)
-    t_oracle = time.perf_counter() - t0
-    del sim
-    out = {"workload": f"layered viscoelastic 20x20x10 km, {nx}x{nx}x{nx // 2} hexes, N_SLS=3, Stacey 5 faces, "
-                       f"{int(db['nrec'])} surface receivers",
-           "nstep": steps, "t_end_s": float(cfg["dt"]) * steps, "oracle": "FP64 C restatement",
-           "oracle_s": t_oracle, "metric": "rel-L2 per receiver trace (3 components x samples), float64"}
-    for fmt in formats:
-        g = GPUSolver(db, cfg)
-        try:
+    out = {"metric": "rel-L2 per receiver trace (3 components x samples), float64", "nstep": steps,
+           "oracle": "FP64 C restatement on an FP64 database"}
+    cases = {}
+    c = configs.layered_viscoelastic(nstep=steps, nx=nx, ny=nx, counts=(nx // 8, 3 * nx // 16, 3 * nx // 16))
+    cases["layered"] = (c, meshgen.build_database(c), meshgen.build_database(c, dtype=np.float64),
+                        f"layered viscoelastic 20x20x10 km, {nx}x{nx}x{nx // 2} hexes, N_SLS=3")
+    c = G.shot_config(configs.batched_shots(nstep=steps, nshots=1, nx=nx), 0)
+    mat = G.background_material(c)
+    cases["perturbed"] = (c, meshgen.build_database(c, material=mat),
+                          meshgen.build_database(c, material=mat, dtype=np.float64),
+                          f"+-5% perturbed block 20x20x10 km, {nx}x{nx}x{nx // 2} hexes, no attenuation")
+    for name, (cfg, db, db64, desc) in cases.items():
+        t0 = time.perf_counter()
+        sim = O.make_sim(db64, cfg, "f64", nthreads=os.cpu_count() or 1)
+        sim.step(steps)
+        ref = O.seismograms(sim)
+        del sim, db64
+        res = {"workload": desc, "receivers": int(db["nrec"]), "t_end_s": float(cfg["dt"]) * steps,
+               "oracle_s": time.perf_counter() - t0}
+        for fmt in formats:
+            g = GPUSolver(db, cfg)
             g.set_geometry_format(fmt)
-        except Exception as exc:  # a format this build does not offer
-            out[fmt] = {"unavailable": str(exc)[:200]}
+            rows = g.geometry_pack_info()[0]
+            g.run(steps, steps_per_graph=50)
+            seis = g.seismograms()
             g.close()
-            continue
-        g.run(steps, steps_per_graph=50)
-        seis = g.seismograms()
-        g.close()
-        e, nr = _per_trace_rel_l2(seis, ref)
-        strong = nr >= 1e-2 * nr.max()
-        out[fmt] = {"median": float(np.median(e)), "p95": float(np.percentile(e, 95)), "max": float(e.max()),
-                    "max_strong_traces": float(e[strong].max()), "all_traces": float(
-                        np.linalg.norm(np.asarray(seis, np.float64) - ref) / np.linalg.norm(ref))}
+            e, nr = _per_trace_rel_l2(seis, ref)
+            strong = nr >= 1e-2 * nr.max()
+            res[fmt] = {"median": float(np.median(e)), "p95": float(np.percentile(e, 95)), "max": float(e.max()),
+                        "max_strong_traces": float(e[strong].max()), "payload_rows": rows,
+                        "all_traces": float(np.linalg.norm(np.asarray(seis, np.float64) - ref) / np.linalg.norm(ref))}
+        out[name] = res
     return out
 
 
-def adjoint_leg(nshots: int):
+def adjoint_leg(nshots: int, nstep: int = 3000):
     """Seconds per shot of the checkpointed misfit gradient on the 64x64x32-element
     gradient workload (3000 steps, checkpoints every 200 steps): forward from rest,
     then the reverse sweep with recomputation; observed traces from the true model."""
     from specfem3d_gb300 import configs, gradient as G, meshgen
     from specfem3d_gb300.solver import GPUSolver
-    cfg = configs.adjoint_gradient(nshots=nshots)
+    cfg = configs.adjoint_gradient(nstep=nstep, nshots=nshots, checkpoint_every=min(200, nstep))
     db_true = meshgen.build_database(cfg, material=G.true_material(cfg))
     observed = []
     for i in range(nshots):
@@ -209,7 +216,32 @@ def adjoint_leg(nshots: int):
     wall = time.perf_counter() - t0
     fwd = sum(t[0] for t in timing) / 1000.0
     bwd = sum(t[1] for t in timing) / 1000.0
+    # directional derivative along one seeded smooth direction against central
+    # differences of the misfit from device FP32 forward runs (eps = 1e-3; FP32
+    # rounding noise limits this check to ~1e-2; the FP64-oracle check at 1e-3 runs
+    # in the test suite on a scaled-down copy of this workload)
+    n = int(db0["nspec"])
+    d = [G.smooth_direction(cfg, 101 + q, corr_len=1500.0) for q in range(3)]
+    stores = {k: db0[s].reshape(n, -1).astype(np.float64)
+              for k, s in (("rho", "rhostore"), ("kappa", "kappastore"), ("mu", "mustore"))}
+    gd = sum(float(np.sum(grad[k] * stores[k] * dq)) for k, dq in zip(("rho", "kappa", "mu"), d))
+
+    def misfit_of(sign, eps=1e-3):
+        dbp = G.perturbed_database(db0, cfg, *(sign * eps * dq for dq in d))
+        total = 0.0
+        for i in range(nshots):
+            c = G.shot_config(cfg, i)
+            c["record"] = ("displ",)
+            s = GPUSolver(G.shot_database(dbp, cfg, i), c, nlength=cfg["nstep"])
+            s.run(cfg["nstep"], steps_per_graph=50)
+            total += G.misfit(s.seismograms(), observed[i], float(s.deltat))[0]
+            s.close()
+        return total
+    fd = (misfit_of(1.0) - misfit_of(-1.0)) / 2e-3
     return {"unit": "s/shot", "s_per_shot": wall / nshots, "device_s_per_shot": (fwd + bwd) / nshots,
+            "fd_check": {"direction": "seeded smooth (dln rho, dln kappa, dln mu), 1.5 km correlation",
+                         "adjoint": gd, "central_difference_fp32_device": fd, "eps": 1e-3,
+                         "rel": abs(gd - fd) / abs(fd)},
             "forward_s_per_shot": fwd / nshots, "backward_s_per_shot": bwd / nshots, "shots": nshots,
             "nstep": cfg["nstep"], "checkpoint_every": cfg["checkpoint_every"], "nspec": db0["nspec"],
             "nglob": db0["nglob"], "misfit": J, "gradient_dtype": "f64 accumulation, f32 fields",
@@ -219,17 +251,22 @@ def adjoint_leg(nshots: int):
 def batch_leg(nshots: int, steps: int, nx: int = 64):
     """Per-shot GLL-point updates/s of the batched-shots workload (64x64x32 hexes,
     perturbed model, no attenuation): all shots advancing together with
-    shot-innermost fields against the plain single-shot path on the same mesh."""
+    shot-innermost fields (autotuned stiffness kernel; FP32 arrays, then packed FP16
+    moduli) against the plain single-shot path on the same mesh."""
     from specfem3d_gb300 import configs, gradient as G, meshgen
     from specfem3d_gb300.batch import BatchSolver
     from specfem3d_gb300.solver import GPUSolver
-    cfg = configs.batched_shots(nstep=steps + 8, nshots=nshots, nx=nx)
-    db = meshgen.build_database(cfg)
-    nglob = int(db["nglob"])
-    b = BatchSolver(db, cfg, nlength=steps + 8)
+    cfg = configs.batched_shots(nstep=2 * steps + 16, nshots=nshots, nx=nx)
+    db = meshgen.build_database(cfg, material=G.background_material(cfg))
+    nglob, nspec = int(db["nglob"]), int(db["nspec"])
+    b = BatchSolver(db, cfg, nlength=2 * steps + 16)
     tune = b.autotune(reps=3)
     b.run(3, steps_per_graph=0)
     ms_b = b.run(steps, steps_per_graph=50)
+    b.solver.set_geometry_format("fp16")
+    rows = b.solver.geometry_pack_info()[0]
+    b.run(3, steps_per_graph=0)
+    ms_h = b.run(steps, steps_per_graph=50)
     b.close()
     plain = GPUSolver(db, G.shot_config(cfg, 0), nlength=steps + 8)
     plain.run(3, steps_per_graph=50)
@@ -238,11 +275,23 @@ def batch_leg(nshots: int, steps: int, nx: int = 64):
     plain.close()
     # shot-point updates per second: every shot's points advanced one step count once
     rate_b = nglob * steps * nshots / (ms_b / 1000.0)
+    rate_h = nglob * steps * nshots / (ms_h / 1000.0)
     rate_p = nglob * steps / (ms_p / 1000.0)
+    peak, kind = _peaks()
+    # whole batched step, algorithmic bytes: per shot-point u v a read + written (72 B),
+    # the u gather (12 B), per point rmass (12 B); per element ibool + kappa/mu (FP32
+    # arrays 1,500 B; packed: ibool + record + FP16 rows)
+    static32 = 1500.0 * nspec
+    static16 = (500.0 + 160.0) * nspec + rows * 250.0
+    dyn = (84.0 * nshots + 12.0) * nglob
     return {"unit": "GLL-pt updates/s summed over shots", "shots": nshots, "steps": steps, "nglob": nglob,
-            "nspec": int(db["nspec"]), "batched": rate_b, "plain_single_shot": rate_p,
-            "speedup_per_shot": rate_b / rate_p, "batched_ms_per_step": ms_b / steps,
+            "nspec": nspec, "batched": rate_b, "batched_fp16_moduli": rate_h, "plain_single_shot": rate_p,
+            "speedup_per_shot": rate_b / rate_p, "speedup_per_shot_fp16_moduli": rate_h / rate_p,
+            "batched_ms_per_step": ms_b / steps, "batched_fp16_ms_per_step": ms_h / steps,
             "plain_ms_per_step": ms_p / steps, "tiling": tune,
+            "step_hbm_frac": (dyn + static32) / (ms_b / steps / 1000.0) / 1e9 / peak,
+            "step_hbm_frac_fp16_moduli": (dyn + static16) / (ms_h / steps / 1000.0) / 1e9 / peak,
+            "peak_gbs": peak, "peak_kind": kind,
             "workload": f"{nx}x{nx}x{nx // 2} hexes, 20x20x10 km, +-5% perturbed model, no attenuation, "
                         f"{nshots} CMT shots, Ricker 2 Hz"}
 
@@ -381,6 +430,7 @@ def main():
     ap.add_argument("--adjoint", type=int, default=8,
                     help="also time the checkpointed misfit gradient over this many shots of the "
                          "8-shot 64x64x32 gradient workload (0: skip)")
+    ap.add_argument("--adjoint-steps", type=int, default=3000, help="time steps of the gradient workload")
     ap.add_argument("--roofline-steps", type=int, default=20,
                     help="steps whose stiffness launches are bracketed by CUDA events")
     args = ap.parse_args()
@@ -402,7 +452,7 @@ def main():
         L.initialize_gpu_device_(A.i(lr), A.i(0))
     W, K = max(3, args.warmup), max(1, args.steps)
     Kr = max(3, min(K, args.roofline_steps))
-    nstep_total = W + K + 2 * Kr + args.e2e_steps + 2
+    nstep_total = W + 2 * K + 4 * Kr + args.e2e_steps + 4
     if args.small:
         cfg = configs.layered_viscoelastic(nstep=nstep_total, nx=32, ny=32, counts=(4, 6, 6))
         workload = "layered viscoelastic 32x32x16 block (reduced)"
@@ -449,15 +499,32 @@ def main():
     peak, peak_kind = _peaks()
     achieved = bytes_launch / (stiff_ms / 1000.0) / 1e9
     traffic_pe = _traffic()
-    # 16-bit geometric factors and moduli (per-element scales): stiffness launches
-    # timed the same way; the layered model is represented exactly
-    g.set_geometry_precision(16)
-    g.run(Kr, steps_per_graph=0, timing=True)
-    th = g.last_timing()
-    g.set_geometry_precision(32)
+    # packed static element streams (constant streams stored once per element,
+    # varying ones as FP16 / BF16 / FP32 rows): stiffness launches timed the same way
+    geometry = {}
+    for fmt in ("fp16", "bf16", "packed-fp32"):
+        g.set_geometry_format(fmt)
+        rows, pack_bytes = g.geometry_pack_info()
+        g.run(Kr, steps_per_graph=0, timing=True)
+        th = g.last_timing()
+        ms = th["stiffness_ms"] / max(th["stiffness_launches"], 1)
+        vb = 4 if fmt == "packed-fp32" else 2
+        # ibool + per-element record + payload rows + memory variables / strains R+W
+        alg = (500.0 + 160.0 + 24000.0) * nspec + rows * 125.0 * vb + 48.0 * nglob
+        geometry[fmt] = {"mean_launch_ms": ms, "payload_rows": rows, "pack_device_bytes": pack_bytes,
+                         "algorithmic_bytes_per_launch": alg, "achieved_gbs": alg / (ms / 1000.0) / 1e9,
+                         "frac": alg / (ms / 1000.0) / 1e9 / peak, "speedup_vs_fp32_arrays": stiff_ms / ms}
+    # whole steps with the lossless packing (same results as the FP32 arrays)
+    g.set_geometry_format("packed-fp32")
+    g.run(K, steps_per_graph=args.graph)
+    tp = g.last_timing()
+    geometry["packed-fp32"]["step_value"] = float(nglob) * K / (tp["total_ms"] / 1000.0)
+    geometry["packed-fp32"]["ms_per_step"] = tp["total_ms"] / K
+    g.set_geometry_format("fp32")
     abi.check()
-    half_ms = th["stiffness_ms"] / max(th["stiffness_launches"], 1)
-    half_bytes = (33000.0 - 0.5 * (4500.0 + 1000.0)) * nspec + 48.0 * nglob
+    geometry["fp32_arrays_mean_launch_ms"] = stiff_ms
+    geometry["note"] = ("streams constant over an element stored once (exact); the layered workload's "
+                        "box elements and per-layer materials leave no varying stream")
     rc, maxu = g.check_stability(1e25)
     # ---------------- e2e: per-call C-ABI path, host buffers ----------------
     A = abi.Args()
@@ -509,12 +576,7 @@ def main():
                      "autotune": autotune,
                      "algorithmic_bytes_per_launch": bytes_launch,
                      "mean_launch_ms": stiff_ms, "timed_launches": tk["stiffness_launches"]},
-        "geometry16": {"mean_launch_ms": half_ms, "algorithmic_bytes_per_launch": half_bytes,
-                       "achieved_gbs": half_bytes / (half_ms / 1000.0) / 1e9,
-                       "frac": half_bytes / (half_ms / 1000.0) / 1e9 / peak,
-                       "speedup_vs_fp32_geometry": stiff_ms / half_ms,
-                       "note": "metric and kappa/mu rows in FP16 with per-element (offset, scale); exact "
-                               "for this layered model (rows constant per element)"},
+        "geometry": geometry,
         "assembly": {"atomic_stiffness_ms": stiff_ms, "colored_stiffness_ms": color_ms,
                      "chosen": "atomic" if stiff_ms <= color_ms else "colored",
                      "note": "colored: 8 launches per step (one per colour), plain read-modify-write scatter"},
@@ -531,7 +593,7 @@ def main():
     if args.coupled > 0:
         line["coupled"] = coupled_leg(args.coupled)
     if args.adjoint > 0:
-        line["adjoint"] = adjoint_leg(args.adjoint)
+        line["adjoint"] = adjoint_leg(args.adjoint, args.adjoint_steps)
     if aniso is not None:
         line["anisotropic"] = aniso
     if args.smooth:

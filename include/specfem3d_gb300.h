@@ -362,12 +362,25 @@ int sf3d_last_timing(long *Mesh_pointer, float *stiffness_ms, int *stiffness_lau
  * configuration). */
 int sf3d_set_stiffness_variant(long *Mesh_pointer, int variant);
 
-/* Storage of the stiffness kernel's geometric factors and moduli: 32 (FP32,
- * default) or 16 (FP16 with a per-element (offset, scale) per array; exact for
- * rows constant over an element, otherwise error <= (max-min)*2^-12 of the
- * element's range).  Fields and arithmetic stay FP32.  No reference
- * counterpart (the reference stores CUSTOM_REAL only). */
+/* Storage of the stiffness kernel's static per-element streams (nine metric
+ * rows of irregular elements, kappa, mu and, with attenuation, factor_common
+ * and factor_common_kappa of the three solids), in packed form:
+ *   0: the FP32 arrays (default);
+ *   1: FP16, 2: BF16: a stream constant over an element is stored once, exactly,
+ *      in a 160-byte per-element record; a varying stream gets a 125-value row
+ *      value = offset + scale * h, offset/scale = (max +- min)/2 over the element,
+ *      h in [-1, 1] in FP16 (error <= scale * 2^-11) or BF16 (scale * 2^-8);
+ *   3: FP32 rows for the varying streams (lossless).
+ * Fields, memory variables and arithmetic stay FP32.  Isotropic meshes only.
+ * No reference counterpart (the reference stores CUSTOM_REAL arrays only). */
+int sf3d_set_geometry_format(long *Mesh_pointer, int format);
+
+/* 32: format 0; 16: format 1 of sf3d_set_geometry_format. */
 int sf3d_set_geometry_precision(long *Mesh_pointer, int bits);
+
+/* Payload rows and device bytes (records + rows) of the packed format in use
+ * (0, 0 for the FP32 arrays).  No reference counterpart. */
+int sf3d_geometry_pack_info(long *Mesh_pointer, long *payload_rows, long *device_bytes);
 
 /* Time every stiffness variant over `reps` full passes and keep the fastest.
  * Must run on a wavefield at rest (after prepare_fields_elastic_device, before
@@ -475,12 +488,16 @@ int sf3d_batch_prepare(long *Mesh_pointer, int nshots, const int *ispec_selected
                        double *device_bytes);
 /* Tiling of the batched stiffness kernel: shots per CTA (1, 2, 4, 8; divides
  * nshots) x elements per CTA (1, 2, 4) x shots per thread (1, or 4 with 4 or 8
- * shots per CTA: float4 rows and vector atomics). */
+ * shots per CTA: float4 rows and vector atomics); shots_per_thread 0 selects the
+ * register-blocked pencil kernel with shots_per_block 8, 16 or 32 shots per CTA
+ * (dividing nshots) and elements_per_block 1. */
 int sf3d_batch_set_tiling(long *Mesh_pointer, int shots_per_block, int elements_per_block,
                           int shots_per_thread);
 /* Time every valid tiling over `reps` stiffness passes on wavefields at rest and
- * keep the fastest; ms_table (24 floats, [shots per thread 1,4] x [shots per CTA
- * 1,2,4,8] x [elements 1,2,4], -1 where invalid) and the outputs may be NULL. */
+ * keep the fastest; ms_table (27 floats: 0-23 [shots per thread 1,4] x [shots per
+ * CTA 1,2,4,8] x [elements 1,2,4], 24-26 the pencil kernel with 8, 16, 32 shots
+ * per CTA; -1 where invalid) and the outputs may be NULL.  The pencil kernel is
+ * reported as shots_per_thread 0. */
 int sf3d_batch_autotune(long *Mesh_pointer, int reps, float *ms_table, int *best_shots_per_block,
                         int *best_elements_per_block, int *best_shots_per_thread);
 /* Steps it_begin..it_end of all shots, graph-captured in blocks of steps_per_graph. */

@@ -76,6 +76,10 @@ def load() -> ctypes.CDLL:
     L.sf3d_set_stiffness_variant.argtypes = [P, ctypes.c_int]
     L.sf3d_set_geometry_precision.restype = ctypes.c_int
     L.sf3d_set_geometry_precision.argtypes = [P, ctypes.c_int]
+    L.sf3d_set_geometry_format.restype = ctypes.c_int
+    L.sf3d_set_geometry_format.argtypes = [P, ctypes.c_int]
+    L.sf3d_geometry_pack_info.restype = ctypes.c_int
+    L.sf3d_geometry_pack_info.argtypes = [P, P, P]
     L.sf3d_autotune_stiffness.restype = ctypes.c_int
     L.sf3d_autotune_stiffness.argtypes = [P, ctypes.c_int, P, P]
     for name in ("sf3d_gradient_forward", "sf3d_gradient_backward"):

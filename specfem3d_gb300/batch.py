@@ -68,9 +68,10 @@ class BatchSolver:
             abi.check()
 
     def autotune(self, reps: int = 3) -> dict:
-        """Time every (shots per thread, shots per CTA, elements per CTA) tiling at rest
-        and keep the fastest."""
-        ms = (ctypes.c_float * 24)()
+        """Time every stiffness kernel and tiling at rest (per-point kernels: shots per
+        thread x shots per CTA x elements per CTA; pencil kernel: shots per CTA) and keep
+        the fastest; shots_per_thread 0 in the result is the pencil kernel."""
+        ms = (ctypes.c_float * 27)()
         sb, eb, spt = ctypes.c_int(), ctypes.c_int(), ctypes.c_int()
         if self.L.sf3d_batch_autotune(self.mp, int(reps), ms, ctypes.addressof(sb), ctypes.addressof(eb),
                                       ctypes.addressof(spt)) != 0:
@@ -82,8 +83,11 @@ class BatchSolver:
                     x = ms[(v * 4 + a) * 3 + b]
                     if x >= 0:
                         table[f"{t}x{s}x{e}"] = round(float(x), 4)
+        for q, lanes in enumerate((8, 16, 32)):
+            if ms[24 + q] >= 0:
+                table[f"pencil{lanes}"] = round(float(ms[24 + q]), 4)
         return {"shots_per_thread": spt.value, "shots_per_block": sb.value, "elements_per_block": eb.value,
-                "ms": table}
+                "kernel": "pencil" if spt.value == 0 else "per-point", "ms": table}
 
     def run(self, nsteps: int, steps_per_graph: int = 50) -> float:
         """nsteps steps of every shot; returns the device time in ms."""

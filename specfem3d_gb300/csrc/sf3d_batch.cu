@@ -10,9 +10,10 @@
 // The elastic arithmetic per shot is that of stiffness_kernel<ATT=0>
 // (compute_forces_viscoelastic.F90:250-860); the time scheme, Stacey faces,
 // sources and receivers are those of sf3d_step.cu applied per shot.  Each step
-// is six launches, captured in CUDA graphs in blocks of steps; the
-// (shots-per-block, elements-per-block) tiling is chosen by timing
-// (sf3d_batch_autotune).
+// is six launches, captured in CUDA graphs in blocks of steps; the stiffness
+// kernel (per-point kernels with their (shots-per-block, elements-per-block)
+// tilings, or the register-blocked pencil kernel of sf3d_batch_pencil.cu with
+// 8, 16 or 32 shots per CTA) is chosen by timing (sf3d_batch_autotune).
 #include <math.h>
 #include <string.h>
 
@@ -627,6 +628,30 @@ void launch_sb(const BatchStiffArgs& a, int eb, cudaStream_t s) {
 
 void launch_batch_stiffness(Mesh* mp, int iphase, cudaStream_t s) {
   BatchState* B = mp->batch;
+  if (B->pencil_lanes > 0) {
+    PencilArgs q;
+    memset(&q, 0, sizeof(q));
+    q.nelem = iphase == 1 ? mp->nspec_outer : mp->nspec_inner;
+    if (q.nelem <= 0) return;
+    q.nshots = B->nshots;
+    q.shot_offset = 0;
+    q.shot_tiles = B->nshots / B->pencil_lanes;
+    q.phase = mp->d_phase_ispec + (long)(iphase - 1) * mp->num_phase_ispec;
+    q.ibool = mp->d_ibool;
+    q.irregular = mp->d_irregular;
+    for (int c = 0; c < 9; ++c) q.m[c] = mp->d_metric[c];
+    q.kappav = mp->d_kappav;
+    q.muv = mp->d_muv;
+    q.pack = mp->d_pack;
+    q.pool = mp->d_pack_pool;
+    q.gll = mp->d_gll;
+    q.xix_regular = mp->xix_regular;
+    q.jacobian_regular = mp->jacobian_regular;
+    q.displ = B->displ;
+    q.accel = B->accel;
+    launch_batch_pencil(q, B->pencil_lanes, mp->geom_format, s);
+    return;
+  }
   BatchStiffArgs a;
   memset(&a, 0, sizeof(a));
   a.nelem = iphase == 1 ? mp->nspec_outer : mp->nspec_inner;
@@ -766,6 +791,7 @@ int sf3d_batch_prepare(long* Mesh_pointer, int nshots, const int* ispec_selected
   B->nlength = nlength;
   B->shots_per_block = nshots % 8 == 0 ? 8 : (nshots % 4 == 0 ? 4 : (nshots % 2 == 0 ? 2 : 1));
   B->shots_per_thread = nshots % 4 == 0 ? 4 : 1;
+  B->pencil_lanes = nshots % 16 == 0 ? 16 : (nshots % 8 == 0 ? 8 : 0);
   const size_t n = 3ull * mp->nglob * nshots;
   std::vector<float> sa((size_t)nshots * NGLL3_PAD * 3, 0.f), tab((size_t)nstep * nshots);
   for (int s = 0; s < nshots; ++s)
@@ -795,6 +821,16 @@ int sf3d_batch_set_tiling(long* Mesh_pointer, int shots_per_block, int elements_
   if (!mp) return SF3D_ERR_STATE;
   if (!mp->batch) { set_error(SF3D_ERR_STATE, "sf3d_batch_prepare not called"); return SF3D_ERR_STATE; }
   const int sb = shots_per_block, eb = elements_per_block, spt = shots_per_thread;
+  if (spt == 0) {
+    // register-blocked pencils: sb shots per CTA, one element per CTA
+    if ((sb != 8 && sb != 16 && sb != 32) || mp->batch->nshots % sb != 0 || eb != 1) {
+      set_error(SF3D_ERR_ARG, "sf3d_batch_set_tiling: the pencil kernel takes 8, 16 or 32 shots per CTA "
+                              "dividing nshots and one element per CTA");
+      return SF3D_ERR_ARG;
+    }
+    mp->batch->pencil_lanes = sb;
+    return SF3D_OK;
+  }
   const bool ok_sb = (sb == 1 || sb == 2 || sb == 4 || sb == 8) && mp->batch->nshots % sb == 0;
   const bool ok_spt = spt == 1 || (spt == 4 && (sb == 4 || sb == 8));
   if (!ok_sb || !ok_spt || (eb != 1 && eb != 2 && eb != 4)) {
@@ -802,6 +838,7 @@ int sf3d_batch_set_tiling(long* Mesh_pointer, int shots_per_block, int elements_
                             "elements_per_block in {1,2,4}, shots_per_thread 1 or 4 (4 with 4 or 8 shots per block)");
     return SF3D_ERR_ARG;
   }
+  mp->batch->pencil_lanes = 0;
   mp->batch->shots_per_block = sb;
   mp->batch->elements_per_block = eb;
   mp->batch->shots_per_thread = spt;
@@ -821,9 +858,27 @@ int sf3d_batch_autotune(long* Mesh_pointer, int reps, float* ms_table, int* best
     return SF3D_ERR_STATE;
   }
   if (reps < 1) reps = 1;
-  const int sbs[4] = {1, 2, 4, 8}, ebs[3] = {1, 2, 4}, spts[2] = {1, 4};
+  const int sbs[4] = {1, 2, 4, 8}, ebs[3] = {1, 2, 4}, spts[2] = {1, 4}, lanes[3] = {8, 16, 32};
   int bsb = -1, beb = -1, bspt = -1;
   float best = 0.f;
+  auto pass = [&]() {
+    for (int iphase = 1; iphase <= 2; ++iphase) launch_batch_stiffness(mp, iphase, mp->stream);
+  };
+  auto time_it = [&](float* ms) -> bool {
+    pass();
+    if (!cuda_ok(cudaEventRecord(mp->ev0, mp->stream), "cudaEventRecord")) return false;
+    for (int r = 0; r < reps; ++r) pass();
+    if (!cuda_ok(cudaEventRecord(mp->ev1, mp->stream), "cudaEventRecord") ||
+        !cuda_ok(cudaEventSynchronize(mp->ev1), "cudaEventSynchronize") ||
+        !cuda_ok(cudaGetLastError(), "sf3d_batch_autotune"))
+      return false;
+    cudaEventElapsedTime(ms, mp->ev0, mp->ev1);
+    *ms /= (float)reps;
+    return true;
+  };
+  // table entries 0-23: per-point kernels [shots per thread 1,4] x [shots per CTA
+  // 1,2,4,8] x [elements 1,2,4]; 24-26: pencil kernel with 8, 16, 32 shots per CTA
+  B->pencil_lanes = 0;
   for (int v = 0; v < 2; ++v)
     for (int a = 0; a < 4; ++a)
       for (int b = 0; b < 3; ++b) {
@@ -834,24 +889,31 @@ int sf3d_batch_autotune(long* Mesh_pointer, int reps, float* ms_table, int* best
         B->shots_per_block = sbs[a];
         B->elements_per_block = ebs[b];
         B->shots_per_thread = spts[v];
-        auto pass = [&]() {
-          for (int iphase = 1; iphase <= 2; ++iphase) launch_batch_stiffness(mp, iphase, mp->stream);
-        };
-        pass();
-        SF3D_CUDA_RET(cudaEventRecord(mp->ev0, mp->stream), SF3D_ERR_CUDA);
-        for (int r = 0; r < reps; ++r) pass();
-        SF3D_CUDA_RET(cudaEventRecord(mp->ev1, mp->stream), SF3D_ERR_CUDA);
-        SF3D_CUDA_RET(cudaEventSynchronize(mp->ev1), SF3D_ERR_CUDA);
-        if (!cuda_ok(cudaGetLastError(), "sf3d_batch_autotune")) return SF3D_ERR_CUDA;
         float ms = 0.f;
-        cudaEventElapsedTime(&ms, mp->ev0, mp->ev1);
-        ms /= (float)reps;
+        if (!time_it(&ms)) return SF3D_ERR_CUDA;
         if (ms_table) ms_table[idx] = ms;
         if (bsb < 0 || ms < best) { best = ms; bsb = sbs[a]; beb = ebs[b]; bspt = spts[v]; }
       }
-  B->shots_per_block = bsb;
-  B->elements_per_block = beb;
-  B->shots_per_thread = bspt;
+  int blanes = 0;
+  for (int q = 0; q < 3; ++q) {
+    if (ms_table) ms_table[24 + q] = -1.f;
+    if (B->nshots % lanes[q] != 0) continue;
+    B->pencil_lanes = lanes[q];
+    float ms = 0.f;
+    if (!time_it(&ms)) return SF3D_ERR_CUDA;
+    if (ms_table) ms_table[24 + q] = ms;
+    if (bsb < 0 || ms < best) { best = ms; blanes = lanes[q]; }
+  }
+  B->pencil_lanes = blanes;
+  if (blanes > 0) {
+    bsb = blanes;
+    beb = 1;
+    bspt = 0;
+  } else {
+    B->shots_per_block = bsb;
+    B->elements_per_block = beb;
+    B->shots_per_thread = bspt;
+  }
   if (best_shots_per_block) *best_shots_per_block = bsb;
   if (best_elements_per_block) *best_elements_per_block = beb;
   if (best_shots_per_thread) *best_shots_per_thread = bspt;

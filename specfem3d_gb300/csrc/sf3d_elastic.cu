@@ -55,7 +55,10 @@ __device__ __forceinline__ void st_state(float* p, float v) {
     *p = v;
 }
 
-template <bool ATT, bool STRAIN, int MINB, bool HALF = false, bool STAGE = false, bool ATOMIC = true,
+// GEOM: kGeomFP32 reads the FP32 element arrays; the packed formats read the
+// per-element records and payload rows of a.pack / a.pool instead (metric,
+// kappa, mu and, with attenuation, factor_common(_kappa)).
+template <bool ATT, bool STRAIN, int MINB, int GEOM = kGeomFP32, bool STAGE = false, bool ATOMIC = true,
           bool STREAM = false, bool ANISO = false>
 __global__ void __launch_bounds__(NGLL3_PAD, MINB) stiffness_kernel(const StiffnessArgs a) {
   __shared__ __align__(16) float s_att[(ATT && STAGE) ? 30 : 1][NGLL3_PAD];
@@ -106,17 +109,21 @@ __global__ void __launch_bounds__(NGLL3_PAD, MINB) stiffness_kernel(const Stiffn
   }
   if (active) {
     iglob = ld_elem<STREAM>(a.ibool + eo);
-    if (HALF) {
-      // 16-bit storage with a per-element (offset, scale): value = offset + scale * h
-      const float2 ks = __ldg(a.kso + e), ms = __ldg(a.muso + e);
-      kap = fmaf(ks.y, __half2float(a.kh[eo]), ks.x);
-      mu = fmaf(ms.y, __half2float(a.muh[eo]), ms.x);
+    if (GEOM != kGeomFP32) {
+      const ElemPack* pk = a.pack + e;
+      const unsigned vary = __ldg(&pk->vary);
+      const int base = __ldg(&pk->base);
+      kap = pack_value<GEOM>(pk, a.pool, vary, base, 9, t);
+      mu = pack_value<GEOM>(pk, a.pool, vary, base, 10, t);
       if (ir >= 0) {
-        const long mo = (long)ir * NGLL3_PAD + t;
 #pragma unroll
-        for (int q = 0; q < 9; ++q) {
-          const float2 so = __ldg(a.mso + (long)q * a.nirr + ir);
-          m[q] = fmaf(so.y, __half2float(a.mh[q][mo]), so.x);
+        for (int q = 0; q < 9; ++q) m[q] = pack_value<GEOM>(pk, a.pool, vary, base, q, t);
+      }
+      if (ATT && !STAGE) {
+#pragma unroll
+        for (int s = 0; s < NSLS; ++s) {
+          fc[s] = pack_value<GEOM>(pk, a.pool, vary, base, 11 + s, t);
+          fck[s] = pack_value<GEOM>(pk, a.pool, vary, base, 14 + s, t);
         }
       }
     } else {
@@ -136,10 +143,12 @@ __global__ void __launch_bounds__(NGLL3_PAD, MINB) stiffness_kernel(const Stiffn
         for (int s = 0; s < NSLS; ++s) R[c][s] = ld_state<STREAM>(a.R[c] + so + s * NGLL3_PAD);
 #pragma unroll
       for (int c = 0; c < 6; ++c) eold[c] = ld_state<STREAM>(a.eps[c] + eo);
+      if (GEOM == kGeomFP32) {
 #pragma unroll
-      for (int s = 0; s < NSLS; ++s) {
-        fc[s] = ld_elem<STREAM>(a.fc + so + s * NGLL3_PAD);
-        fck[s] = ld_elem<STREAM>(a.fck + so + s * NGLL3_PAD);
+        for (int s = 0; s < NSLS; ++s) {
+          fc[s] = ld_elem<STREAM>(a.fc + so + s * NGLL3_PAD);
+          fck[s] = ld_elem<STREAM>(a.fck + so + s * NGLL3_PAD);
+        }
       }
     }
     ux = a.displ[3L * iglob];
@@ -357,56 +366,66 @@ __global__ void __launch_bounds__(NGLL3_PAD, MINB) stiffness_kernel(const Stiffn
   }
 }
 
-template <int MINB, bool HALF, bool STAGE = false, bool STREAM = false>
+template <int MINB, int GEOM, bool STAGE = false, bool STREAM = false>
 void launch_minb(const StiffnessArgs& a, bool att, bool store_strain, cudaStream_t s) {
   dim3 grid(a.nelem), block(NGLL3_PAD);
   if (att)
-    stiffness_kernel<true, true, MINB, HALF, STAGE, true, STREAM><<<grid, block, 0, s>>>(a);
+    stiffness_kernel<true, true, MINB, GEOM, STAGE, true, STREAM><<<grid, block, 0, s>>>(a);
   else if (store_strain)
-    stiffness_kernel<false, true, MINB, HALF, false, true, STREAM><<<grid, block, 0, s>>>(a);
+    stiffness_kernel<false, true, MINB, GEOM, false, true, STREAM><<<grid, block, 0, s>>>(a);
   else
-    stiffness_kernel<false, false, MINB, HALF, false, true, STREAM><<<grid, block, 0, s>>>(a);
+    stiffness_kernel<false, false, MINB, GEOM, false, true, STREAM><<<grid, block, 0, s>>>(a);
+}
+
+template <int MINB>
+void launch_packed(const StiffnessArgs& a, bool att, bool store_strain, cudaStream_t s, int geom) {
+  if (geom == kGeomPackF16)
+    launch_minb<MINB, kGeomPackF16>(a, att, store_strain, s);
+  else if (geom == kGeomPackBF16)
+    launch_minb<MINB, kGeomPackBF16>(a, att, store_strain, s);
+  else
+    launch_minb<MINB, kGeomPackF32>(a, att, store_strain, s);
 }
 
 }  // namespace
 
 // blocks_per_sm: the register budget the kernel is compiled for (4..7 CTAs of
 // 128 threads per SM; more CTAs keep more elements' loads in flight, fewer
-// let the compiler keep every load of an element in registers).  The 16-bit
+// let the compiler keep every load of an element in registers).  The packed
 // geometry builds exist for 6 and 7 CTAs/SM.
 void launch_stiffness(const StiffnessArgs& a, bool att, bool store_strain, cudaStream_t s, int blocks_per_sm,
-                      bool half_geometry, bool staged, bool streaming) {
+                      int geom_format, bool staged, bool streaming) {
   if (a.nelem <= 0) return;
   if (streaming) {
     if (blocks_per_sm == 7)
-      launch_minb<7, false, false, true>(a, att, store_strain, s);
+      launch_minb<7, kGeomFP32, false, true>(a, att, store_strain, s);
     else
-      launch_minb<6, false, false, true>(a, att, store_strain, s);
+      launch_minb<6, kGeomFP32, false, true>(a, att, store_strain, s);
     return;
   }
   if (staged) {
     // cp.async-staged memory variables (attenuation); without attenuation the
     // same register budgets of the plain build
     if (blocks_per_sm == 8)
-      launch_minb<8, false, true>(a, att, store_strain, s);
+      launch_minb<8, kGeomFP32, true>(a, att, store_strain, s);
     else if (blocks_per_sm == 7)
-      launch_minb<7, false, true>(a, att, store_strain, s);
+      launch_minb<7, kGeomFP32, true>(a, att, store_strain, s);
     else
-      launch_minb<6, false, true>(a, att, store_strain, s);
+      launch_minb<6, kGeomFP32, true>(a, att, store_strain, s);
     return;
   }
-  if (half_geometry) {
+  if (geom_format != kGeomFP32) {
     if (blocks_per_sm == 7)
-      launch_minb<7, true>(a, att, store_strain, s);
+      launch_packed<7>(a, att, store_strain, s, geom_format);
     else
-      launch_minb<6, true>(a, att, store_strain, s);
+      launch_packed<6>(a, att, store_strain, s, geom_format);
     return;
   }
   switch (blocks_per_sm) {
-    case 5: launch_minb<5, false>(a, att, store_strain, s); break;
-    case 6: launch_minb<6, false>(a, att, store_strain, s); break;
-    case 7: launch_minb<7, false>(a, att, store_strain, s); break;
-    default: launch_minb<4, false>(a, att, store_strain, s); break;
+    case 5: launch_minb<5, kGeomFP32>(a, att, store_strain, s); break;
+    case 6: launch_minb<6, kGeomFP32>(a, att, store_strain, s); break;
+    case 7: launch_minb<7, kGeomFP32>(a, att, store_strain, s); break;
+    default: launch_minb<4, kGeomFP32>(a, att, store_strain, s); break;
   }
 }
 
@@ -414,11 +433,11 @@ template <int MINB>
 void launch_aniso_minb(const StiffnessArgs& a, bool att, bool store_strain, cudaStream_t s) {
   dim3 grid(a.nelem), block(NGLL3_PAD);
   if (att)
-    stiffness_kernel<true, true, MINB, false, false, true, false, true><<<grid, block, 0, s>>>(a);
+    stiffness_kernel<true, true, MINB, kGeomFP32, false, true, false, true><<<grid, block, 0, s>>>(a);
   else if (store_strain)
-    stiffness_kernel<false, true, MINB, false, false, true, false, true><<<grid, block, 0, s>>>(a);
+    stiffness_kernel<false, true, MINB, kGeomFP32, false, true, false, true><<<grid, block, 0, s>>>(a);
   else
-    stiffness_kernel<false, false, MINB, false, false, true, false, true><<<grid, block, 0, s>>>(a);
+    stiffness_kernel<false, false, MINB, kGeomFP32, false, true, false, true><<<grid, block, 0, s>>>(a);
 }
 
 // blocks_per_sm: 4, 5 or 6 resident CTAs (the register budget of the 21 extra moduli)
@@ -436,11 +455,11 @@ void launch_stiffness_colored(const StiffnessArgs& a, bool att, bool store_strai
   if (a.nelem <= 0) return;
   dim3 grid(a.nelem), block(NGLL3_PAD);
   if (att)
-    stiffness_kernel<true, true, 6, false, false, false><<<grid, block, 0, s>>>(a);
+    stiffness_kernel<true, true, 6, kGeomFP32, false, false><<<grid, block, 0, s>>>(a);
   else if (store_strain)
-    stiffness_kernel<false, true, 6, false, false, false><<<grid, block, 0, s>>>(a);
+    stiffness_kernel<false, true, 6, kGeomFP32, false, false><<<grid, block, 0, s>>>(a);
   else
-    stiffness_kernel<false, false, 6, false, false, false><<<grid, block, 0, s>>>(a);
+    stiffness_kernel<false, false, 6, kGeomFP32, false, false><<<grid, block, 0, s>>>(a);
 }
 
 }  // namespace sf3d

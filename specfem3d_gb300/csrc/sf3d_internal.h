@@ -12,6 +12,7 @@
 #pragma once
 
 #include <nvtx3/nvToolsExt.h>
+#include <cuda_bf16.h>
 #include <cuda_fp16.h>
 #include <cuda_runtime.h>
 #include <stdint.h>
@@ -53,6 +54,44 @@ bool cuda_ok(cudaError_t e, const char* what);
     if (!::sf3d::cuda_ok((call), #call)) return ret;  \
   } while (0)
 
+// Static per-element streams of the stiffness kernel in packed form.  Stream q:
+// 0-8 the metric (xix xiy xiz etax etay etaz gammax gammay gammaz; irregular
+// elements), 9 kappa, 10 mu, 11-13 factor_common, 14-16 factor_common_kappa.
+// value(q, p) = so[q].x                                  if bit q of vary is clear
+//             = so[q].x + so[q].y * pool[row(q)][p]      otherwise, with
+// row(q) = base + popcount(vary & ((1 << q) - 1)): only the streams that vary
+// inside the element carry a 128-value payload row.
+constexpr int kPackStreams = 17;
+enum GeomFormat { kGeomFP32 = 0, kGeomPackF16 = 1, kGeomPackBF16 = 2, kGeomPackF32 = 3 };
+struct __align__(16) ElemPack {
+  float2 so[kPackStreams];  // (offset, scale)
+  unsigned vary;            // bit q: stream q has a payload row
+  int base;                 // first payload row of this element
+  int pad[4];
+};
+static_assert(sizeof(ElemPack) == 160, "ElemPack is five 32-byte sectors");
+
+// payload value i of a packed pool in the format GEOM
+template <int GEOM>
+__device__ __forceinline__ float pool_value(const void* pool, long i) {
+  if (GEOM == kGeomPackF16)
+    return __half2float(__ushort_as_half(__ldg(static_cast<const unsigned short*>(pool) + i)));
+  if (GEOM == kGeomPackBF16)
+    return __bfloat162float(__ushort_as_bfloat16(__ldg(static_cast<const unsigned short*>(pool) + i)));
+  return __ldg(static_cast<const float*>(pool) + i);
+}
+
+// value of stream q at point t of the element whose record is pk (vary, base: its
+// varying-stream mask and first payload row, read once per element)
+template <int GEOM>
+__device__ __forceinline__ float pack_value(const ElemPack* pk, const void* pool, unsigned vary, int base, int q,
+                                            int t) {
+  const float2 so = __ldg(&pk->so[q]);
+  if (!((vary >> q) & 1u)) return so.x;
+  const long row = (long)base + __popc(vary & ((1u << q) - 1u));
+  return fmaf(so.y, pool_value<GEOM>(pool, row * NGLL3_PAD + t), so.x);
+}
+
 struct Fields {
   float* displ = nullptr;
   float* veloc = nullptr;
@@ -92,6 +131,7 @@ struct BatchState {
   int nshots = 0, nstep = 0, nlength = 0;
   int shots_per_block = 8, elements_per_block = 1;
   int shots_per_thread = 1;     // 4: vector kernel (shots_per_block 4 or 8)
+  int pencil_lanes = 0;         // > 0: register-blocked pencil kernel, shots per CTA (8, 16, 32)
   float* displ = nullptr;
   float* veloc = nullptr;
   float* accel = nullptr;
@@ -252,14 +292,12 @@ struct Mesh {
   cudaStream_t copy_stream = nullptr;
   cudaEvent_t ev_pack = nullptr;          // packing done on the compute stream
   int stiffness_variant = 3;              // see variant_blocks_per_sm; 1: persistent bulk-copy pipeline
-  // 16-bit geometry and moduli with per-element affine scales (stiffness kernel only)
-  int geom_half = 0;
-  __half* d_metric_h[9] = {};
-  float2* d_metric_so = nullptr;          // [9][nspec_irr]
-  __half* d_kappa_h = nullptr;
-  __half* d_mu_h = nullptr;
-  float2* d_kappa_so = nullptr;           // [nspec]
-  float2* d_mu_so = nullptr;
+  // packed static element streams of the stiffness kernel (sf3d_set_geometry_format):
+  // one ElemPack record per element, payload rows only for streams that vary
+  int geom_format = 0;                    // kGeomFP32 (plain arrays) ... kGeomPackF32
+  ElemPack* d_pack = nullptr;             // [nspec]
+  void* d_pack_pool = nullptr;            // [pack_rows][128] FP16 / BF16 / FP32 values
+  long pack_rows = 0;
 
   cudaStream_t stream = nullptr;
   // deferred mass + corrector of the forward [0] and backward [1] field, and its dt/2
@@ -328,14 +366,9 @@ struct StiffnessArgs {
   const float* fc;
   const float* fck;
   float alpha[NSLS], beta[NSLS], gamma[NSLS];
-  // 16-bit geometry (sf3d_set_geometry_precision): value = offset + scale * half
-  const __half* mh[9];          // [nspec_irr][128]
-  const float2* mso;            // [9][nspec_irr] (offset, scale)
-  const __half* kh;             // [nspec][128]
-  const __half* muh;
-  const float2* kso;            // [nspec]
-  const float2* muso;
-  int nirr;                     // rows of each 16-bit metric array
+  // packed static streams (sf3d_set_geometry_format); nullptr: the FP32 arrays above
+  const ElemPack* pack;         // [nspec]
+  const void* pool;             // payload rows
   int nonatomic;                // 1: the elements of this launch share no point (one colour)
   // ANISOTROPY: c11 c12 c13 c14 c15 c16 c22 c23 c24 c25 c26 c33 c34 c35 c36 c44
   // c45 c46 c55 c56 c66, each [nspec][128]; nullptr for isotropic meshes
@@ -343,7 +376,31 @@ struct StiffnessArgs {
 };
 
 void launch_stiffness(const StiffnessArgs& a, bool att, bool store_strain, cudaStream_t s, int blocks_per_sm,
-                      bool half_geometry = false, bool staged = false, bool streaming = false);
+                      int geom_format = kGeomFP32, bool staged = false, bool streaming = false);
+// batched-shots stiffness with register-blocked pencils (sf3d_batch_pencil.cu):
+// elements of a phase list x shots [shot_offset, shot_offset + shot_tiles * lanes)
+// of fields stacked shot-innermost with nshots shots per point
+struct PencilArgs {
+  int nelem;
+  int nshots;                   // stride of the stacked fields
+  int shot_offset;              // first shot of this launch
+  int shot_tiles;               // CTAs per element (shots of this launch / lanes)
+  const int* phase;
+  const int* ibool;
+  const int* irregular;
+  const float* m[9];
+  const float* kappav;
+  const float* muv;
+  const ElemPack* pack;         // packed static streams, or nullptr
+  const void* pool;
+  const float* gll;
+  float xix_regular;
+  float jacobian_regular;
+  const float* displ;
+  float* accel;
+};
+bool launch_batch_pencil(const PencilArgs& a, int lanes, int geom_format, cudaStream_t s);
+
 void launch_stiffness_pipelined(const StiffnessArgs& a, bool att, bool store_strain, int* err, cudaStream_t s);
 // stiffness kernel variants (sf3d_set_stiffness_variant / sf3d_autotune_stiffness)
 //   0, 2, 3, 4: one CTA per element at 4, 5, 6, 7 CTAs/SM; 1: persistent bulk-copy pipeline;
@@ -361,7 +418,7 @@ inline bool variant_split(int v) { return v >= 10; }
 void launch_stiffness_split(const StiffnessArgs& a, bool att, bool store_strain, cudaStream_t s, int blocks_per_sm);
 void free_grad(Mesh* mp);
 void free_batch(Mesh* mp);
-void free_half_geometry(Mesh* mp);
+void free_geometry_pack(Mesh* mp);
 // max |x| over n values on the compute stream (NaN if any value is NaN); synchronises
 bool device_maxabs(Mesh* mp, const float* x, long n, float* out);
 // inter-slice assembly buffers (sf3d_assemble.cu)
@@ -406,21 +463,16 @@ inline void run_stiffness(Mesh* mp, const StiffnessArgs& a, bool att, bool store
     launch_stiffness_aniso(a, att, store_strain, s, bps < 4 ? 4 : bps);
     return;
   }
-  if (mp->use_mesh_coloring && !mp->geom_half && a.phase && mp->d_phase_ispec) {
+  if (mp->use_mesh_coloring && !mp->geom_format && a.phase && mp->d_phase_ispec) {
     const int iphase = a.phase == mp->d_phase_ispec ? 1 : 2;
     if (run_stiffness_by_color(mp, a, iphase, att, store_strain, s)) return;
   }
-  if (mp->geom_half) {
-    // 16-bit geometry: the one-CTA-per-element kernel at 6 or 7 CTAs/SM
+  if (mp->geom_format) {
+    // packed static streams: the one-CTA-per-element kernel at 6 or 7 CTAs/SM
     StiffnessArgs h = a;
-    for (int q = 0; q < 9; ++q) h.mh[q] = mp->d_metric_h[q];
-    h.mso = mp->d_metric_so;
-    h.kh = mp->d_kappa_h;
-    h.muh = mp->d_mu_h;
-    h.kso = mp->d_kappa_so;
-    h.muso = mp->d_mu_so;
-    h.nirr = mp->nspec_irregular;
-    launch_stiffness(h, att, store_strain, s, mp->stiffness_variant == 4 ? 7 : 6, true);
+    h.pack = mp->d_pack;
+    h.pool = mp->d_pack_pool;
+    launch_stiffness(h, att, store_strain, s, mp->stiffness_variant == 4 ? 7 : 6, mp->geom_format);
   } else if (mp->stiffness_variant == 1 && mp->d_kerr) {
     launch_stiffness_pipelined(a, att, store_strain, mp->d_kerr, s);
   } else if (variant_split(mp->stiffness_variant)) {

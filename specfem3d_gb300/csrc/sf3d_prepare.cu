@@ -558,7 +558,7 @@ void prepare_cleanup_device_(long* Mesh_pointer, int* ACOUSTIC_SIMULATION, int* 
   cudaFree(mp->d_rec_is_acoustic);
   free_grad(mp);
   free_batch(mp);
-  free_half_geometry(mp);
+  free_geometry_pack(mp);
   free_interfaces(mp);
   cudaFree(mp->d_it); cudaFree(mp->d_done); cudaFree(mp->d_scratch); cudaFree(mp->d_kerr); cudaFree(mp->d_stage);
   if (mp->ev0) cudaEventDestroy(mp->ev0);

@@ -359,17 +359,28 @@ class GPUSolver:
             abi.check()
 
     def set_geometry_precision(self, bits: int):
-        """32: FP32 geometry and moduli; 16: FP16 with per-element (offset, scale)."""
+        """32: FP32 geometry and moduli; 16: the "fp16" packed format."""
         if self.L.sf3d_set_geometry_precision(self.mp, int(bits)) != 0:
             abi.check()
 
+    GEOMETRY_FORMATS = {"fp32": 0, "fp16": 1, "bf16": 2, "packed-fp32": 3}
+
     def set_geometry_format(self, fmt: str):
-        """Storage of the stiffness kernel's static per-element streams: "fp32", or
-        "fp16" (16-bit rows with a per-element (offset, scale))."""
-        bits = {"fp32": 32, "fp16": 16}.get(fmt)
-        if bits is None:
+        """Storage of the stiffness kernel's static element streams (sf3d_set_geometry_format):
+        "fp32" (plain arrays), "fp16" / "bf16" (streams constant over an element stored
+        once, varying ones as 16-bit rows with a per-element offset and scale), or
+        "packed-fp32" (the same packing with FP32 rows: lossless)."""
+        if fmt not in self.GEOMETRY_FORMATS:
             raise ValueError(f"geometry format {fmt!r} is not offered")
-        self.set_geometry_precision(bits)
+        if self.L.sf3d_set_geometry_format(self.mp, self.GEOMETRY_FORMATS[fmt]) != 0:
+            abi.check()
+
+    def geometry_pack_info(self):
+        """(payload rows, device bytes) of the packed format in use."""
+        r, b = ctypes.c_long(), ctypes.c_long()
+        if self.L.sf3d_geometry_pack_info(self.mp, ctypes.addressof(r), ctypes.addressof(b)) != 0:
+            abi.check()
+        return r.value, b.value
 
     def check_stability(self, threshold: float = 1e25):
         m = ctypes.c_float()
