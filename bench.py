@@ -433,7 +433,20 @@ def main():
     ap.add_argument("--adjoint-steps", type=int, default=3000, help="time steps of the gradient workload")
     ap.add_argument("--roofline-steps", type=int, default=20,
                     help="steps whose stiffness launches are bracketed by CUDA events")
+    ap.add_argument("--legs", default="main,batch,coupled,adjoint,l2",
+                    help="comma list of the parts to run: main (the headline workload and its e2e, roofline, "
+                         "geometry, CPU-oracle lines), batch, coupled, adjoint, l2; without main one JSON line "
+                         "holds the selected legs only (profiling)")
     args = ap.parse_args()
+    legs = set(x.strip() for x in args.legs.split(",") if x.strip())
+    if "batch" not in legs:
+        args.batch = 0
+    if "coupled" not in legs:
+        args.coupled = 0
+    if "adjoint" not in legs:
+        args.adjoint = 0
+    if "l2" not in legs:
+        args.l2_steps = 0
     rank = int(os.environ.get("RANK", "0"))
     world = int(os.environ.get("WORLD_SIZE", "1"))
     if args.impl == "reference":
@@ -443,6 +456,19 @@ def main():
     from specfem3d_gb300 import abi, build, configs, meshgen, solver
     build.build()
     L = abi.load()
+    if "main" not in legs:
+        out = {"legs": sorted(legs)}
+        if args.batch > 0:
+            out["batched"] = batch_leg(args.batch, args.batch_steps, args.batch_nx)
+        if args.coupled > 0:
+            out["coupled"] = coupled_leg(args.coupled)
+        if args.adjoint > 0:
+            out["adjoint"] = adjoint_leg(args.adjoint, args.adjoint_steps)
+        if args.l2_steps > 0:
+            out["l2_error"] = l2_error_leg(args.l2_steps)
+        if rank == 0:
+            print(json.dumps(out), flush=True)
+        return 0
     dist = None
     if world > 1:
         import torch.distributed as dist

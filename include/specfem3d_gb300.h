@@ -474,6 +474,30 @@ int sf3d_gradient_release(long *Mesh_pointer);
 int sf3d_field_maxabs_noalloc(const realw *d_field, long n, void *stream, realw *max_abs);
 
 /* ------------------------------------------------------------------------
+ * Misfit post-processing on the device (FP64).  No Mesh handle needed. */
+/* Adjoint sources of the reference's tools utils/adjoint_sources/
+ * {waveform,traveltime,amplitude}/create_adjsrc_*.f90 for all traces at once:
+ * kind 0 waveform (cosine-tapered window, adj = (syn - dat) tw), 1 cross-
+ * correlation traveltime (adj = -v tw / norm, v the centred time derivative of
+ * syn), 2 amplitude (adj = syn tw / norm).  Traces (nrec, 3, nstep) C order
+ * (component innermost of the first two, samples contiguous); window from
+ * ts, te with samples t0 + (j - 1) dt; component 0 keeps all components, 1-3
+ * only that one (ifile of the tools).  h_dat is used by kind 0 only.  norms
+ * (nrec, 3) = dt sum(tw signal^2).  Errors: window outside the trace; a
+ * waveform window shorter than 20 samples (the tool's taper divides by zero
+ * there). */
+int sf3d_adjoint_sources(int kind, int nrec, int nstep, double dt, double t0, double ts, double te,
+                         int component, const double *h_syn, const double *h_dat, double *h_adj,
+                         double *h_norms);
+/* Sum of nker event kernels of n values each (src/tomography/sum_kernels.f90:
+ * 215-315), each optionally multiplied by its source mask (USE_SOURCE_MASK;
+ * h_masks NULL: none), accumulated in FP64 on the device; h_total (n) FP64 and,
+ * if not NULL, h_total_f32 (n) rounded to CUSTOM_REAL; h_norms (nker) = sum(k^2)
+ * of each event kernel before masking (the tool prints its square root). */
+int sf3d_sum_kernels(int nker, long n, const realw *const *h_kernels, const realw *const *h_masks,
+                     double *h_total, realw *h_total_f32, double *h_norms);
+
+/* ------------------------------------------------------------------------
  * Many shots on one prepared mesh (elastic, no attenuation).  The reference
  * runs shots as independent simulations (NUMBER_OF_SIMULTANEOUS_RUNS,
  * parallel.f90:2171-2260); here the shots' wavefields are stacked

@@ -859,3 +859,72 @@ def smooth_restated(xyz_me: np.ndarray, xyz_other: np.ndarray, data_other: np.nd
         norm = np.where(norm < 1e-24, 1.0, norm)
         out[:, e, :] = np.einsum("pq,kq->kp", coef, dat[:, inc, :].reshape(dat.shape[0], -1)) / norm[None, :]
     return out.reshape(dat.shape[0], -1)
+
+
+# ------------------------------------------------------------------ misfit post-processing
+def adjoint_source(kind: int, syn, dat, dt: float, t0: float, ts: float, te: float, component: int = 0):
+    """Adjoint sources of utils/adjoint_sources/*/create_adjsrc_*.f90, one trace at a
+    time in sample order (the tools' real*8 loops): syn, dat (nrec, 3, nstep); kind 0
+    waveform (create_adjsrc_waveform.f90:222-287), 1 cross-correlation traveltime
+    (create_adjsrc_traveltime.f90:131-162), 2 amplitude (create_adjsrc_amplitude.f90:
+    130-157).  Returns (adj (nrec, 3, nstep), norms (nrec, 3))."""
+    syn = np.asarray(syn, np.float64)
+    dat = None if dat is None else np.asarray(dat, np.float64)
+    nrec, _, nstep = syn.shape
+    pi = 3.1415926                                    # the waveform tool's PI parameter
+    eps = 1.0e-17
+    istart = int((ts - t0) / dt) + 1
+    iend = int((te - t0) / dt) + 1
+    if istart < 1 or iend <= istart or iend > nstep:
+        raise ValueError("Error in ts, te")
+    tw = np.zeros(nstep + 1)                          # 1-based
+    if kind == 0:
+        taper = int(0.1 * (iend - istart))            # 10 percent taper length
+        for j in range(istart, iend + 1):
+            if j < istart + taper:
+                tw[j] = (1.0 - np.cos(pi * 2.0 * (j - istart) / (taper - 1))) / 2.0
+            elif j <= iend - taper:
+                tw[j] = 1.0
+            else:
+                tw[j] = (1.0 - np.cos(pi * 2.0 * (iend - j) / (taper - 1))) / 2.0
+    else:
+        for j in range(istart, iend + 1):
+            tw[j] = 1 - (2 * (float(j) - istart) / (iend - istart) - 1) ** 2
+    tw = tw[1:]
+    adj = np.zeros_like(syn)
+    norms = np.zeros((nrec, 3))
+    for r in range(nrec):
+        for c in range(3):
+            s = syn[r, c]
+            if kind == 0:
+                out = s - dat[r, c]
+            elif kind == 1:
+                out = np.zeros(nstep)
+                for it in range(1, nstep - 1):
+                    out[it] = (s[it + 1] - s[it - 1]) / (2 * dt)
+                out[0] = (s[1] - s[0]) / dt
+                out[nstep - 1] = (s[nstep - 1] - s[nstep - 2]) / dt
+            else:
+                out = s.copy()
+            norm = dt * np.sum(tw * out * out)
+            if component != 0 and component != c + 1:
+                norm = 0.0
+            if abs(norm) > eps:
+                adj[r, c] = out * tw if kind == 0 else (-out * tw / norm if kind == 1 else out * tw / norm)
+            norms[r, c] = norm
+    return adj, norms
+
+
+def sum_kernels(kernels, masks=None):
+    """Sum of event kernels (src/tomography/sum_kernels.f90:215-315) in FP64: each
+    kernel's norm sum(k*k) before masking (:267), masked by its source mask (:289),
+    accumulated (:293).  Returns (total, norms)."""
+    total = None
+    norms = []
+    for q, k in enumerate(kernels):
+        k = np.asarray(k, np.float64)
+        norms.append(float(np.sum(k * k)))
+        if masks is not None:
+            k = k * np.asarray(masks[q], np.float64)
+        total = k.copy() if total is None else total + k
+    return total, np.asarray(norms)

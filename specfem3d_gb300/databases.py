@@ -32,9 +32,12 @@ class RecordWriter:
 
     def __init__(self, path: str):
         self.f = open(path, "wb")
+        self.names = []     # the reference's variable names of the records written
 
-    def write(self, *items):
-        """One record holding the given scalars / arrays back to back."""
+    def write(self, *items, name: str = ""):
+        """One record holding the given scalars / arrays back to back (name: the
+        variable(s) the reference writes there)."""
+        self.names.append(name)
         data = b"".join(np.ascontiguousarray(a).tobytes(order="C") if isinstance(a, np.ndarray) else a
                         for a in items)
         n, off = len(data), 0
@@ -136,7 +139,8 @@ def write_external_mesh(path: str, db: dict, xyz_global: np.ndarray, stacey: boo
     """proc######_external_mesh.bin of one slice, in the record order of
     save_arrays_solver_mesh (save_arrays_solver.F90:100-405).  ``db`` is a
     database of this package (meshgen / hexmesh); with attenuation its relaxed
-    moduli are written (the unrelaxed scaling goes to attenuation.bin)."""
+    moduli are written (the unrelaxed scaling goes to attenuation.bin).  Returns the
+    reference's variable names of the records written, in order."""
     rt = np.float32 if real_bytes == 4 else np.float64
     nspec, nglob = int(db["nspec"]), int(db["nglob"])
     nirr = int(db["nspec_irregular"])
@@ -146,47 +150,47 @@ def write_external_mesh(path: str, db: dict, xyz_global: np.ndarray, stacey: boo
     R = lambda a: np.asarray(a, rt)                                  # noqa: E731
     I = lambda a: np.asarray(a, np.int32)                            # noqa: E731
     w = RecordWriter(path)
-    for v in (nspec, nglob, nirr):
-        w.write(I([v]))
-    w.write(I(db["ibool"]))
+    for v, n in ((nspec, "nspec"), (nglob, "nglob"), (nirr, "nspec_irregular")):
+        w.write(I([v]), name=n)
+    w.write(I(db["ibool"]), name="ibool")
     for d in range(3):
-        w.write(R(xyz_global[:, d]))
-    w.write(I(db["irregular_element_number"]))
-    w.write(R([db["xix_regular"]]))
-    w.write(R([db["jacobian_regular"]]))
+        w.write(R(xyz_global[:, d]), name="xyz"[d] + "store_unique")
+    w.write(I(db["irregular_element_number"]), name="irregular_element_number")
+    w.write(R([db["xix_regular"]]), name="xix_regular")
+    w.write(R([db["jacobian_regular"]]), name="jacobian_regular")
     for n in ("xix", "xiy", "xiz", "etax", "etay", "etaz", "gammax", "gammay", "gammaz", "jacobian"):
-        w.write(R(np.asarray(db[n])[:NGLL3 * nirr]))
-    w.write(R(db.get("kappastore_relaxed", db["kappastore"])))
-    w.write(R(db.get("mustore_relaxed", db["mustore"])))
-    w.write(_logical(isac))
-    w.write(_logical(~isac))
-    w.write(_logical(np.zeros(nspec, bool)))
-    w.write(I([9999]))
+        w.write(R(np.asarray(db[n])[:NGLL3 * nirr]), name=n + "store")
+    w.write(R(db.get("kappastore_relaxed", db["kappastore"])), name="kappastore")
+    w.write(R(db.get("mustore_relaxed", db["mustore"])), name="mustore")
+    w.write(_logical(isac), name="ispec_is_acoustic")
+    w.write(_logical(~isac), name="ispec_is_elastic")
+    w.write(_logical(np.zeros(nspec, bool)), name="ispec_is_poroelastic")
+    w.write(I([9999]), name="itest")
     if acoustic:
-        w.write(R(db["rmass_acoustic_volume"]))
-    w.write(R(db["rhostore"]))
+        w.write(R(db["rmass_acoustic_volume"]), name="rmass_acoustic")
+    w.write(R(db["rhostore"]), name="rhostore")
     if elastic:
-        w.write(R(db["rmass"]))
-        w.write(R(db["rho_vp"]))
-        w.write(R(db["rho_vs"]))
+        w.write(R(db["rmass"]), name="rmass")
+        w.write(R(db["rho_vp"]), name="rho_vp")
+        w.write(R(db["rho_vs"]), name="rho_vs")
     nf = int(db["num_abs_boundary_faces"])
-    w.write(I([nf]))
+    w.write(I([nf]), name="num_abs_boundary_faces")
     if nf:
-        w.write(I(db["abs_boundary_ispec"]))
-        w.write(I(db["abs_boundary_ijk"]))
-        w.write(R(db["abs_boundary_jacobian2Dw"]))
-        w.write(R(db["abs_boundary_normal"]))
+        w.write(I(db["abs_boundary_ispec"]), name="abs_boundary_ispec")
+        w.write(I(db["abs_boundary_ijk"]), name="abs_boundary_ijk")
+        w.write(R(db["abs_boundary_jacobian2Dw"]), name="abs_boundary_jacobian2Dw")
+        w.write(R(db["abs_boundary_normal"]), name="abs_boundary_normal")
         if stacey:
             if elastic:
                 for c in "xyz":
-                    w.write(R(db["rmass" + c + "_stacey"]))
+                    w.write(R(db["rmass" + c + "_stacey"]), name="rmass" + c)
             if acoustic:
-                w.write(R(db.get("rmassz_acoustic", np.zeros(nglob))))
-    w.write(I([9998]))
-    for _ in range(6):                       # nspec2D_xmin .. NSPEC2D_TOP: not kept here
-        w.write(I([0]))
+                w.write(R(db.get("rmassz_acoustic", np.zeros(nglob))), name="rmassz_acoustic")
+    w.write(I([9998]), name="itest")
+    for n in ("nspec2D_xmin", "nspec2D_xmax", "nspec2D_ymin", "nspec2D_ymax", "NSPEC2D_BOTTOM", "NSPEC2D_TOP"):
+        w.write(I([0]), name=n)              # the boundary element lists are not kept here
     nfs = int(db.get("num_free_surface_faces", 0))
-    w.write(I([nfs]))
+    w.write(I([nfs]), name="num_free_surface_faces")
     if nfs:
         from .hexmesh import face_geometry
         ijk = I(db["free_surface_ijk"]).reshape(nfs, 25, 3)
@@ -196,66 +200,67 @@ def write_external_mesh(path: str, db: dict, xyz_global: np.ndarray, stacey: boo
         corner = [0, 4, 24, 20, 100, 104, 124, 120]
         anchors = xyz_global[ib[ispec - 1][:, corner]]
         jw, nrm = face_geometry(anchors, iface)
-        w.write(ispec)
-        w.write(ijk.reshape(-1))
-        w.write(R(jw.reshape(-1)))
-        w.write(R(nrm.reshape(-1)))
+        w.write(ispec, name="free_surface_ispec")
+        w.write(ijk.reshape(-1), name="free_surface_ijk")
+        w.write(R(jw.reshape(-1)), name="free_surface_jacobian2Dw")
+        w.write(R(nrm.reshape(-1)), name="free_surface_normal")
     ncp = int(db.get("num_coupling_ac_el_faces", 0))
-    w.write(I([ncp]))
+    w.write(I([ncp]), name="num_coupling_ac_el_faces")
     if ncp:
-        w.write(I(db["coupling_ac_el_ispec"]))
-        w.write(I(db["coupling_ac_el_ijk"]))
-        w.write(R(db["coupling_ac_el_jacobian2Dw"]))
-        w.write(R(db["coupling_ac_el_normal"]))
-    w.write(I([0]))                          # num_coupling_ac_po_faces
-    w.write(I([0]))                          # num_coupling_el_po_faces
-    w.write(I([9997]))
+        w.write(I(db["coupling_ac_el_ispec"]), name="coupling_ac_el_ispec")
+        w.write(I(db["coupling_ac_el_ijk"]), name="coupling_ac_el_ijk")
+        w.write(R(db["coupling_ac_el_jacobian2Dw"]), name="coupling_ac_el_jacobian2Dw")
+        w.write(R(db["coupling_ac_el_normal"]), name="coupling_ac_el_normal")
+    w.write(I([0]), name="num_coupling_ac_po_faces")
+    w.write(I([0]), name="num_coupling_el_po_faces")
+    w.write(I([9997]), name="itest")
     nif = int(db.get("num_interfaces", 0))
     mxn = int(db.get("max_nibool_interfaces", 0)) if nif else 0
-    w.write(I([nif]))
-    w.write(I([mxn]))
+    w.write(I([nif]), name="num_interfaces_ext_mesh")
+    w.write(I([mxn]), name="max_nibool_interfaces_ext_mesh")
     if nif:
-        w.write(I(db.get("my_neighbors", db.get("neighbours", np.arange(nif)))))
-        w.write(I(db["nibool_interfaces"]))
-        w.write(I(db["ibool_interfaces"]))
-    w.write(I([9996]))
+        w.write(I(db.get("my_neighbors", db.get("neighbours", np.arange(nif)))), name="my_neighbors_ext_mesh")
+        w.write(I(db["nibool_interfaces"]), name="nibool_interfaces_ext_mesh")
+        w.write(I(db["ibool_interfaces"]), name="ibool_interfaces_ext_mesh_dummy")
+    w.write(I([9996]), name="itest")
     outer = I(db.get("phase_outer", np.zeros(0)))
     inner_flag = np.ones(nspec, bool)
     inner_flag[outer - 1] = False
-    w.write(_logical(inner_flag))
-    for flag, sel in ((acoustic, isac), (elastic, ~isac)):
+    w.write(_logical(inner_flag), name="ispec_is_inner")
+    for flag, sel, dom in ((acoustic, isac, "acoustic"), (elastic, ~isac, "elastic")):
         if not flag:
             continue
         members = np.nonzero(sel)[0] + 1
         out_l = members[~inner_flag[members - 1]]
         in_l = members[inner_flag[members - 1]]
-        w.write(I([len(in_l), len(out_l)]))
+        w.write(I([len(in_l), len(out_l)]), name=f"nspec_inner_{dom},nspec_outer_{dom}")
         nph = max(len(in_l), len(out_l))
-        w.write(I([nph]))
+        w.write(I([nph]), name="num_phase_ispec_" + dom)
         if nph:
             ph = np.zeros((nph, 2), np.int32)
             ph[:len(out_l), 0] = out_l
             ph[:len(in_l), 1] = in_l
-            w.write(ph.reshape(-1, order="F"))
+            w.write(ph.reshape(-1, order="F"), name="phase_ispec_inner_" + dom)
     if colors is not None:
         # USE_MESH_COLORING_GPU: colours of the outer, then the inner elements
         col = np.asarray(colors)
-        for flag, sel in ((acoustic, isac), (elastic, ~isac)):
+        for flag, sel, dom in ((acoustic, isac, "acoustic"), (elastic, ~isac, "elastic")):
             if not flag:
                 continue
             co = np.unique(col[sel & ~inner_flag], return_counts=True)[1]
             ci = np.unique(col[sel & inner_flag], return_counts=True)[1]
-            w.write(I([len(co), len(ci)]))
-            w.write(I(np.concatenate([co, ci])))
+            w.write(I([len(co), len(ci)]), name=f"num_colors_outer_{dom},num_colors_inner_{dom}")
+            w.write(I(np.concatenate([co, ci])), name="num_elem_colors_" + dom)
     nsurf, isurf, gsurf, xadj, adj = _surface_and_neighbours(db)
-    w.write(I([nsurf]))
-    w.write(_logical(isurf))
-    w.write(_logical(gsurf))
-    w.write(I([len(adj)]))
-    w.write(xadj)
-    w.write(adj)
-    w.write(I([9995]))
+    w.write(I([nsurf]), name="nfaces_surface")
+    w.write(_logical(isurf), name="ispec_is_surface_external_mesh")
+    w.write(_logical(gsurf), name="iglob_is_surface_external_mesh")
+    w.write(I([len(adj)]), name="num_neighbors_all")
+    w.write(xadj, name="neighbors_xadj")
+    w.write(adj, name="neighbors_adjncy")
+    w.write(I([9995]), name="itest")
     w.close()
+    return w.names
 
 
 def write_attenuation(path: str, db: dict, real_bytes: int = 4):

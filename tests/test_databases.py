@@ -167,3 +167,63 @@ def test_database_files_run_like_the_original(gpulib, tmp_path):
         g.close()
     assert np.abs(out[0]).max() > 0
     assert rel_l2(out[1], out[0]) < 1e-5
+
+
+def _reference_sequence(flags: dict):
+    """Variables save_arrays_solver_mesh writes under the given switches, in order
+    (tests/golden/reference_database_records.json, extracted from the reference's
+    save_arrays_solver.F90 by tests/golden/make_database_fixture.py)."""
+    import json
+    from conftest import ROOT
+    fx = json.load(open(os.path.join(ROOT, "tests", "golden", "reference_database_records.json")))
+    out = []
+    for rec in fx["records"]:
+        if all(flags.get(g, False) for g in rec["guards"]):
+            out.append(rec["name"])
+    return out
+
+
+@pytest.mark.parametrize("case", ["layered_stacey", "coupled", "partition_colored"])
+def test_record_sequence_follows_reference_writer(tmp_path, case):
+    """The records written are those of the reference's save_arrays_solver_mesh for
+    the same switches, in the same order and under the same variable names; the
+    reader consumes exactly that many records."""
+    from specfem3d_gb300 import configs, meshgen, databases as D
+    colors = None
+    if case == "layered_stacey":
+        cfg = configs.small_layered(nstep=20, attenuation=True)
+        db = meshgen.build_database(cfg)
+    elif case == "coupled":
+        cfg = configs.small_coupled(nstep=20)
+        db = meshgen.build_database(cfg)
+    else:
+        cfg = configs.small_layered(nstep=20, attenuation=False)
+        full = meshgen.build_database(cfg)
+        db = partition_block.split_x(full, cfg, 3)[1]
+        gl = np.asarray(db["global_points"]) - 1
+        for c in "xyz":
+            db["rmass" + c + "_stacey"] = full["rmass" + c + "_stacey"][gl]
+        db["num_free_surface_faces"] = 0
+        colors = np.arange(int(db["nspec"])) % 8
+    xyz_all = meshgen.element_coordinates(cfg)
+    if case == "partition_colored":
+        xyz = D.global_coordinates(full["ibool"], xyz_all, full["nglob"])[gl]
+    else:
+        xyz = D.global_coordinates(db["ibool"], xyz_all, db["nglob"])
+    p = os.path.join(str(tmp_path), "proc000000_external_mesh.bin")
+    names = D.write_external_mesh(p, db, xyz, colors=colors)
+    isac = np.asarray(db.get("ispec_is_acoustic", np.zeros(int(db["nspec"]))), bool)
+    nif = int(db.get("num_interfaces", 0))
+    flags = {
+        "ACOUSTIC_SIMULATION": bool(isac.any()), "ELASTIC_SIMULATION": bool((~isac).any()),
+        "num_abs_boundary_faces > 0": int(db["num_abs_boundary_faces"]) > 0,
+        "STACEY_ABSORBING_CONDITIONS .and. (.not. PML_CONDITIONS)": bool(db.get("stacey", 0)),
+        "num_free_surface_faces > 0": int(db.get("num_free_surface_faces", 0)) > 0,
+        "num_coupling_ac_el_faces > 0": int(db.get("num_coupling_ac_el_faces", 0)) > 0,
+        "num_interfaces_ext_mesh > 0": nif > 0,
+        "num_phase_ispec_acoustic > 0": bool(isac.any()), "num_phase_ispec_elastic > 0": bool((~isac).any()),
+        "USE_MESH_COLORING_GPU": colors is not None,
+    }
+    assert names == _reference_sequence(flags)
+    raw = D.read_external_mesh(p, stacey=bool(db.get("stacey", 0)), coloring=colors is not None)
+    assert raw["nspec"] == db["nspec"]
