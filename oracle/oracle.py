@@ -554,7 +554,9 @@ def make_sim(db: dict, cfg: dict, precision: str = "f32", nthreads: int = 1) -> 
         s.set("cstore", np.ascontiguousarray(np.stack([np.asarray(db[n], rd) for n in ANISO_NAMES], axis=1)))
     s.setr("xix_regular", db["xix_regular"])
     s.setr("jacobian_regular", db["jacobian_regular"])
-    s.seti("num_abs_boundary_faces", int(db["num_abs_boundary_faces"]) if db.get("stacey", 1) else 0)
+    # C-PML keeps the outer faces for its Dirichlet condition (no Stacey terms)
+    s.seti("num_abs_boundary_faces",
+           int(db["num_abs_boundary_faces"]) if (db.get("stacey", 1) or db.get("pml", 0)) else 0)
     s.seti("stacey", int(db.get("stacey", 1)))
     dt = float(cfg["dt"])
     dtr = rd(dt)
@@ -574,6 +576,8 @@ def make_sim(db: dict, cfg: dict, precision: str = "f32", nthreads: int = 1) -> 
         s.set("seismograms", np.zeros(3 * nr * nstep))
     for n in ["displ", "veloc", "accel"]:
         s.set(n, np.zeros(3 * nglob, rd))
+    if int(db.get("pml", 0)):
+        _set_pml(s, db, rd)
     att = int(db.get("attenuation", 0))
     s.seti("attenuation", att)
     s.seti("compute_and_store_strain", att)
@@ -586,6 +590,28 @@ def make_sim(db: dict, cfg: dict, precision: str = "f32", nthreads: int = 1) -> 
                   "epsilondev_trace"]:
             s.set(n, np.zeros(NGLL3 * nspec, rd))
     return s
+
+
+def _set_pml(s, db, rd):
+    """C-PML arrays of a database from specfem3d_gb300.pml.setup (layouts of
+    prepare_timerun_pml: coefficient index fastest, then GLL point, then CPML element)."""
+    from specfem3d_gb300.meshgen import WGLL
+    n = len(db["cpml_to_spec"])
+    nspec = int(db["nspec"])
+    s.seti("nspec_cpml", n)
+    s.set("is_cpml", np.asarray(db["is_cpml"], np.int32))
+    s.set("cpml_to_spec", np.asarray(db["cpml_to_spec"], np.int32))
+    s2c = np.zeros(nspec, np.int32)
+    s2c[np.asarray(db["cpml_to_spec"]) - 1] = np.arange(1, n + 1, dtype=np.int32)
+    s.set("spec_to_cpml", s2c)
+    for k in ("alpha", "beta", "abar", "strain"):
+        s.set("pml_coef_" + k, np.ascontiguousarray(np.asarray(db["pml_coef_" + k], rd)).reshape(-1))
+    w3 = (WGLL[None, None, :] * WGLL[None, :, None] * WGLL[:, None, None]).reshape(-1)
+    s.set("wgll_cube", w3.astype(rd))
+    s.set("rhostore", np.asarray(db["rhostore"], rd))
+    s.set("pml_displ_old", np.zeros(3 * 125 * n, rd))
+    s.set("pml_displ_new", np.zeros(3 * 125 * n, rd))
+    s.set("pml_rmem", np.zeros(48 * 125 * n, rd))
 
 
 def seismograms(sim: OracleSim) -> np.ndarray:

@@ -40,13 +40,15 @@ static const orc_field k_ptr_fields[] = {
   F(source_adjoint), F(hxir_adj), F(hetar_adj), F(hgammar_adj), F(elastic_list), F(acoustic_list),
   F(ispec_is_acoustic), F(potential), F(potential_dot), F(potential_dot_dot), F(rmass_acoustic),
   F(coupling_ispec), F(coupling_ijk), F(coupling_normal), F(coupling_jacobian2Dw), F(free_surface_ispec),
-  F(free_surface_ijk), F(rec_is_acoustic), F(cstore),
+  F(free_surface_ijk), F(rec_is_acoustic), F(cstore), F(is_cpml), F(cpml_to_spec), F(spec_to_cpml),
+  F(pml_coef_alpha), F(pml_coef_beta), F(pml_coef_abar), F(pml_coef_strain), F(wgll_cube), F(pml_displ_old),
+  F(pml_displ_new), F(pml_rmem),
 };
 static const orc_field k_int_fields[] = {
   F(nspec), F(nglob), F(nspec_irregular), F(nsources), F(nrec), F(nstep), F(it),
   F(attenuation), F(stacey), F(compute_and_store_strain), F(simulation_type), F(nthreads),
   F(record_what), F(num_abs_boundary_faces), F(n_elastic), F(n_acoustic), F(num_coupling_faces),
-  F(num_free_surface_faces), F(fluid_vector),
+  F(num_free_surface_faces), F(fluid_vector), F(nspec_cpml),
 };
 static const orc_field k_real_fields[] = {
   F(xix_regular), F(jacobian_regular), F(deltat), F(deltatover2), F(deltatsqover2),
@@ -754,6 +756,8 @@ static void newmark_predictor(long n3, realw *d, realw *v, realw *a, realw dt, r
 static void element_forces(const orc_sim *s, int ispec, const realw *displ, const realw *veloc,
                            realw *accel, realw deltat, realw *R[6], realw *eps[6],
                            realw *eps_trace_over_3, int is_backward) {
+  /* PML elements are computed by pml_element_forces (compute_forces_viscoelastic.F90:272-273) */
+  if (!is_backward && s->nspec_cpml > 0 && s->is_cpml && s->is_cpml[ispec]) return;
   const realw *hp = s->hprime_xx, *hpw = s->hprimewgll_xx;
   realw ux[NGLL3], uy[NGLL3], uz[NGLL3];
   realw t1x[NGLL3], t2x[NGLL3], t3x[NGLL3], t1y[NGLL3], t2y[NGLL3], t3y[NGLL3], t1z[NGLL3], t2z[NGLL3], t3z[NGLL3];
@@ -958,6 +962,237 @@ static void element_forces(const orc_sim *s, int ispec, const realw *displ, cons
   }
 }
 
+/* C-PML element (compute_forces_viscoelastic.F90:969-1400, compute_forces_viscoelastic_PML):
+ * gradients of u, PML_displ_old and PML_displ_new; the convolution memory variables
+ * and the non-symmetric stress (pml_compute_memory_variables.f90,
+ * pml_compute_memory_variables_elastic); the layer's acceleration term
+ * (pml_compute_accel_contribution.f90, pml_compute_accel_contribution_elastic); the
+ * dot products with the metric, the transposed contractions and the scatter of
+ * -(sum + acceleration term).  Memory variables rmem(48, 125, nspec_cpml): rows
+ * 3n+q the three convolutions of dux_dxl_x, duy_dxl_y, duz_dxl_z, dux_dyl_x,
+ * duy_dyl_y, duz_dyl_z, dux_dzl_x, duy_dzl_y, duz_dzl_z; rows 27-38 duz_dzl_y,
+ * duz_dyl_y, duy_dzl_z, duy_dyl_z, duz_dzl_x, duz_dxl_x, dux_dzl_z, dux_dxl_z,
+ * duy_dyl_x, duy_dxl_x, dux_dyl_y, dux_dxl_y; rows 39+3d+c the displacement. */
+static void grad_ref(const realw *hp, const realw *f /* [3][125] */, realw T[NGLL3][3][3]) {
+  for (int k = 0; k < NGLL; ++k)
+    for (int j = 0; j < NGLL; ++j)
+      for (int i = 0; i < NGLL; ++i) {
+        const int p = IJK(i, j, k);
+        for (int c = 0; c < 3; ++c) {
+          realw s1 = 0, s2 = 0, s3 = 0;
+          for (int l = 0; l < NGLL; ++l) {
+            s1 += f[c * NGLL3 + IJK(l, j, k)] * hp[i + NGLL * l];
+            s2 += f[c * NGLL3 + IJK(i, l, k)] * hp[j + NGLL * l];
+            s3 += f[c * NGLL3 + IJK(i, j, l)] * hp[k + NGLL * l];
+          }
+          T[p][c][0] = s1; T[p][c][1] = s2; T[p][c][2] = s3;
+        }
+      }
+}
+
+static void pml_element_forces(const orc_sim *s, int ispec, realw *accel, realw *eps[6]) {
+  const realw *hp = s->hprime_xx, *hpw = s->hprimewgll_xx;
+  const int ec = s->spec_to_cpml[ispec] - 1;
+  const int *ib = s->ibool + (long)NGLL3 * ispec;
+  static realw Tu[NGLL3][3][3], To[NGLL3][3][3], Tn[NGLL3][3][3];
+#pragma omp threadprivate(Tu, To, Tn)
+  realw fu[3 * NGLL3], fo[3 * NGLL3], fn[3 * NGLL3];
+  for (int p = 0; p < NGLL3; ++p) {
+    long g = ib[p] - 1;
+    for (int c = 0; c < 3; ++c) {
+      fu[c * NGLL3 + p] = s->displ[3 * g + c];
+      fo[c * NGLL3 + p] = s->pml_displ_old[c + 3 * (p + (long)NGLL3 * ec)];
+      fn[c * NGLL3 + p] = s->pml_displ_new[c + 3 * (p + (long)NGLL3 * ec)];
+    }
+  }
+  grad_ref(hp, fu, Tu);
+  grad_ref(hp, fo, To);
+  grad_ref(hp, fn, Tn);
+  const int ir = s->irregular_element_number[ispec];
+  const long mo = (long)NGLL3 * (ir - 1);
+  const realw xr = s->xix_regular;
+  realw t1x[NGLL3], t2x[NGLL3], t3x[NGLL3], t1y[NGLL3], t2y[NGLL3], t3y[NGLL3], t1z[NGLL3], t2z[NGLL3], t3z[NGLL3];
+  realw acc[NGLL3][3];
+  for (int p = 0; p < NGLL3; ++p) {
+    realw m[9], jacl;
+    if (ir) {
+      m[0] = s->xix[mo + p]; m[1] = s->xiy[mo + p]; m[2] = s->xiz[mo + p];
+      m[3] = s->etax[mo + p]; m[4] = s->etay[mo + p]; m[5] = s->etaz[mo + p];
+      m[6] = s->gammax[mo + p]; m[7] = s->gammay[mo + p]; m[8] = s->gammaz[mo + p];
+      jacl = s->jacobian[mo + p];
+    } else {
+      for (int q = 0; q < 9; ++q) m[q] = 0;
+      m[0] = m[4] = m[8] = xr;
+      jacl = s->jacobian_regular;
+    }
+    realw du[3][3], dold[3][3], dnew[3][3];
+    for (int c = 0; c < 3; ++c)
+      for (int x = 0; x < 3; ++x) {
+        if (ir) {
+          du[c][x] = m[x] * Tu[p][c][0] + m[3 + x] * Tu[p][c][1] + m[6 + x] * Tu[p][c][2];
+          dold[c][x] = m[x] * To[p][c][0] + m[3 + x] * To[p][c][1] + m[6 + x] * To[p][c][2];
+          dnew[c][x] = m[x] * Tn[p][c][0] + m[3 + x] * Tn[p][c][1] + m[6 + x] * Tn[p][c][2];
+        } else {
+          du[c][x] = xr * Tu[p][c][x];
+          dold[c][x] = xr * To[p][c][x];
+          dnew[c][x] = xr * Tn[p][c][x];
+        }
+      }
+    const long q = (long)NGLL3 * ispec + p;
+    if (s->compute_and_store_strain && eps[0]) {
+      realw templ = (realw)(1.0 / 3.0) * (du[0][0] + du[1][1] + du[2][2]);
+      eps[0][q] = du[0][0] - templ;
+      eps[1][q] = du[1][1] - templ;
+      eps[2][q] = (realw)0.5 * (du[0][1] + du[1][0]);
+      eps[3][q] = (realw)0.5 * (du[2][0] + du[0][2]);
+      eps[4][q] = (realw)0.5 * (du[2][1] + du[1][2]);
+    }
+    const long cp = p + (long)NGLL3 * ec;
+#define CA(r) s->pml_coef_alpha[(r) + 9 * cp]
+#define CB(r) s->pml_coef_beta[(r) + 9 * cp]
+#define RM(r) s->pml_rmem[(r) + 48 * cp]
+    /* sets of the three convolutions of the derivatives along x, y, z */
+    for (int x = 0; x < 3; ++x)
+      for (int c = 0; c < 3; ++c)
+        for (int qq = 0; qq < 3; ++qq) {
+          const int set = x == 0 ? (qq == 0 ? 6 : (qq == 1 ? 3 : -1)) : x == 1 ? (qq == 0 ? 0 : (qq == 1 ? 6 : -1))
+                                                                                : (qq == 0 ? 0 : (qq == 1 ? 3 : -1));
+          realw c0, c1, c2;
+          if (set >= 0) { c0 = CA(set); c1 = CA(set + 1); c2 = CA(set + 2); }
+          else { c0 = CB(3 * x); c1 = CB(3 * x + 1); c2 = CB(3 * x + 2); }
+          realw *r = &RM(3 * (3 * x + c) + qq);
+          *r = c0 * *r + dnew[c][x] * c1 + dold[c][x] * c2;
+        }
+    const int srow[12] = {0, 0, 0, 0, 3, 3, 3, 3, 6, 6, 6, 6};
+    const int sc[12] = {2, 2, 1, 1, 2, 2, 0, 0, 1, 1, 0, 0};
+    const int sx[12] = {2, 1, 2, 1, 2, 0, 2, 0, 1, 0, 1, 0};
+    for (int n = 0; n < 12; ++n) {
+      realw *r = &RM(27 + n);
+      *r = CA(srow[n]) * *r + dnew[sc[n]][sx[n]] * CA(srow[n] + 1) + dold[sc[n]][sx[n]] * CA(srow[n] + 2);
+    }
+    const realw *A = s->pml_coef_strain + 18 * cp;   /* A6 .. A23 */
+    realw duxdxl_x = A[0] * du[0][0] + A[1] * RM(0) + A[2] * RM(1) + A[3] * RM(2);
+    realw duxdyl_x = A[4] * du[0][1] + A[5] * RM(9) + A[6] * RM(10) + A[7] * RM(11);
+    realw duxdzl_x = A[8] * du[0][2] + A[9] * RM(18) + A[10] * RM(19) + A[11] * RM(20);
+    realw duzdzl_x = A[14] * du[2][2] + A[15] * RM(31);
+    realw duzdxl_x = A[14] * du[2][0] + A[15] * RM(32);
+    realw duydyl_x = A[16] * du[1][1] + A[17] * RM(35);
+    realw duydxl_x = A[16] * du[1][0] + A[17] * RM(36);
+    realw duydxl_y = A[0] * du[1][0] + A[1] * RM(3) + A[2] * RM(4) + A[3] * RM(5);
+    realw duydyl_y = A[4] * du[1][1] + A[5] * RM(12) + A[6] * RM(13) + A[7] * RM(14);
+    realw duydzl_y = A[8] * du[1][2] + A[9] * RM(21) + A[10] * RM(22) + A[11] * RM(23);
+    realw duzdzl_y = A[12] * du[2][2] + A[13] * RM(27);
+    realw duzdyl_y = A[12] * du[2][1] + A[13] * RM(28);
+    realw duxdyl_y = A[16] * du[0][1] + A[17] * RM(37);
+    realw duxdxl_y = A[16] * du[0][0] + A[17] * RM(38);
+    realw duzdxl_z = A[0] * du[2][0] + A[1] * RM(6) + A[2] * RM(7) + A[3] * RM(8);
+    realw duzdyl_z = A[4] * du[2][1] + A[5] * RM(15) + A[6] * RM(16) + A[7] * RM(17);
+    realw duzdzl_z = A[8] * du[2][2] + A[9] * RM(24) + A[10] * RM(25) + A[11] * RM(26);
+    realw duydzl_z = A[12] * du[1][2] + A[13] * RM(29);
+    realw duydyl_z = A[12] * du[1][1] + A[13] * RM(30);
+    realw duxdzl_z = A[14] * du[0][2] + A[15] * RM(33);
+    realw duxdxl_z = A[14] * du[0][0] + A[15] * RM(34);
+    realw kappal = s->kappastore[q], mul = s->mustore[q];
+    realw l2m = kappal + (realw)(4.0 / 3.0) * mul, lam = l2m - (realw)2 * mul;
+    realw sxx = l2m * duxdxl_x + lam * duydyl_x + lam * duzdzl_x;
+    realw syx = mul * duxdyl_x + mul * duydxl_x;
+    realw szx = mul * duzdxl_x + mul * duxdzl_x;
+    realw sxy = mul * duxdyl_y + mul * duydxl_y;
+    realw syy = lam * duxdxl_y + l2m * duydyl_y + lam * duzdzl_y;
+    realw szy = mul * duzdyl_y + mul * duydzl_y;
+    realw sxz = mul * duzdxl_z + mul * duxdzl_z;
+    realw syz = mul * duzdyl_z + mul * duydzl_z;
+    realw szz = lam * duxdxl_z + lam * duydyl_z + l2m * duzdzl_z;
+    /* displacement memory variables and the layer's acceleration term */
+    realw rd[3][3];
+    for (int d = 0; d < 3; ++d)
+      for (int c = 0; c < 3; ++c) {
+        realw *r = &RM(39 + 3 * d + c);
+        *r = CA(3 * d) * *r + fn[c * NGLL3 + p] * CA(3 * d + 1) + fo[c * NGLL3 + p] * CA(3 * d + 2);
+        rd[c][d] = *r;
+      }
+    const realw *Ab = s->pml_coef_abar + 5 * cp;
+    const realw wrj = s->wgll_cube[p] * s->rhostore[q] * jacl;
+    for (int c = 0; c < 3; ++c)
+      acc[p][c] = wrj * (Ab[0] * s->veloc[3 * (ib[p] - 1) + c] + Ab[1] * fu[c * NGLL3 + p] + Ab[2] * rd[c][0] +
+                         Ab[3] * rd[c][1] + Ab[4] * rd[c][2]);
+#undef CA
+#undef CB
+#undef RM
+    /* dot products with the metric rows, non-symmetric form */
+    t1x[p] = jacl * (sxx * m[0] + syx * m[1] + szx * m[2]);
+    t1y[p] = jacl * (sxy * m[0] + syy * m[1] + szy * m[2]);
+    t1z[p] = jacl * (sxz * m[0] + syz * m[1] + szz * m[2]);
+    t2x[p] = jacl * (sxx * m[3] + syx * m[4] + szx * m[5]);
+    t2y[p] = jacl * (sxy * m[3] + syy * m[4] + szy * m[5]);
+    t2z[p] = jacl * (sxz * m[3] + syz * m[4] + szz * m[5]);
+    t3x[p] = jacl * (sxx * m[6] + syx * m[7] + szx * m[8]);
+    t3y[p] = jacl * (sxy * m[6] + syy * m[7] + szy * m[8]);
+    t3z[p] = jacl * (sxz * m[6] + syz * m[7] + szz * m[8]);
+  }
+  for (int k = 0; k < NGLL; ++k)
+    for (int j = 0; j < NGLL; ++j)
+      for (int i = 0; i < NGLL; ++i) {
+        realw sx1 = 0, sx2 = 0, sx3 = 0, sy1 = 0, sy2 = 0, sy3 = 0, sz1 = 0, sz2 = 0, sz3 = 0;
+        for (int l = 0; l < NGLL; ++l) {
+          realw f1 = hpw[l + NGLL * i], f2 = hpw[l + NGLL * j], f3 = hpw[l + NGLL * k];
+          sx1 += t1x[IJK(l, j, k)] * f1; sy1 += t1y[IJK(l, j, k)] * f1; sz1 += t1z[IJK(l, j, k)] * f1;
+          sx2 += t2x[IJK(i, l, k)] * f2; sy2 += t2y[IJK(i, l, k)] * f2; sz2 += t2z[IJK(i, l, k)] * f2;
+          sx3 += t3x[IJK(i, j, l)] * f3; sy3 += t3y[IJK(i, j, l)] * f3; sz3 += t3z[IJK(i, j, l)] * f3;
+        }
+        realw fac1 = s->wgllwgll_yz[j + NGLL * k], fac2 = s->wgllwgll_xz[i + NGLL * k], fac3 = s->wgllwgll_xy[i + NGLL * j];
+        const int p = IJK(i, j, k);
+        long g = ib[p] - 1;
+        realw ax = fac1 * sx1 + fac2 * sx2 + fac3 * sx3 + acc[p][0];
+        realw ay = fac1 * sy1 + fac2 * sy2 + fac3 * sy3 + acc[p][1];
+        realw az = fac1 * sz1 + fac2 * sz2 + fac3 * sz3 + acc[p][2];
+#pragma omp atomic
+        accel[3 * g] -= ax;
+#pragma omp atomic
+        accel[3 * g + 1] -= ay;
+#pragma omp atomic
+        accel[3 * g + 2] -= az;
+      }
+}
+
+/* update_displ_elastic_PML (update_displacement_scheme.f90:417-455) */
+static void pml_store_displ(orc_sim *s, realw *out) {
+  const realw theta = (realw)0.125;
+  for (int ec = 0; ec < s->nspec_cpml; ++ec) {
+    const int ispec = s->cpml_to_spec[ec] - 1;
+    for (int p = 0; p < NGLL3; ++p) {
+      long g = s->ibool[(long)NGLL3 * ispec + p] - 1;
+      for (int c = 0; c < 3; ++c)
+        out[c + 3 * (p + (long)NGLL3 * ec)] = s->displ[3 * g + c] +
+                                              s->deltatover2 * ((realw)1 - (realw)2 * theta) * s->veloc[3 * g + c] +
+                                              s->deltatsqover2 * ((realw)1 - theta) * s->accel[3 * g + c];
+    }
+  }
+}
+
+/* pml_impose_boundary_condition_elastic (pml_compute_accel_contribution.f90 /
+ * pml_impose_boundary_condition_cuda_kernel.cu): u, v, a and the stored
+ * predictions zero on the outer faces of the layers */
+static void pml_boundary(orc_sim *s) {
+  for (int f = 0; f < s->num_abs_boundary_faces; ++f) {
+    const int ispec = s->abs_boundary_ispec[f] - 1;
+    if ((s->ispec_is_acoustic && s->ispec_is_acoustic[ispec]) || !s->is_cpml[ispec]) continue;
+    const int ec = s->spec_to_cpml[ispec] - 1;
+    for (int g = 0; g < NGLL2; ++g) {
+      const int *ijk = s->abs_boundary_ijk + 3 * (g + NGLL2 * f);
+      const int p = IJK(ijk[0] - 1, ijk[1] - 1, ijk[2] - 1);
+      long ig = s->ibool[p + (long)NGLL3 * ispec] - 1;
+      for (int c = 0; c < 3; ++c) {
+        s->displ[3 * ig + c] = 0;
+        s->veloc[3 * ig + c] = 0;
+        s->accel[3 * ig + c] = 0;
+        s->pml_displ_old[c + 3 * (p + (long)NGLL3 * ec)] = 0;
+        s->pml_displ_new[c + 3 * (p + (long)NGLL3 * ec)] = 0;
+      }
+    }
+  }
+}
+
 /* All elements' stiffness contribution (one phase covers the whole slice). */
 void orc_compute_forces_elastic(orc_sim *s, int backward) {
   realw *R[6] = {s->R_xx, s->R_yy, s->R_xy, s->R_xz, s->R_yz, s->R_trace};
@@ -977,6 +1212,12 @@ void orc_compute_forces_elastic(orc_sim *s, int backward) {
   for (int q = 0; q < n; ++q) {
     const int ispec = s->n_elastic < 0 ? q : s->elastic_list[q] - 1;
     element_forces(s, ispec, d, v, a, dt, R, E, tr3, backward);
+  }
+  if (!backward && s->nspec_cpml > 0) {
+#ifdef _OPENMP
+#pragma omp parallel for schedule(static)
+#endif
+    for (int ec = 0; ec < s->nspec_cpml; ++ec) pml_element_forces(s, s->cpml_to_spec[ec] - 1, a, E);
   }
 }
 
@@ -1102,10 +1343,14 @@ void orc_seismograms(orc_sim *s, const realw *field, int it) {
  * (stiffness of all elements), mass matrix, corrector, seismograms. */
 void orc_step(orc_sim *s) {
   long n3 = 3L * s->nglob;
+  const int pml = s->nspec_cpml > 0;
+  if (pml) pml_store_displ(s, s->pml_displ_old);
   newmark_predictor(n3, s->displ, s->veloc, s->accel, s->deltat, s->deltatover2, s->deltatsqover2);
+  if (pml) pml_store_displ(s, s->pml_displ_new);
   if (s->stacey && s->num_abs_boundary_faces > 0) orc_stacey_elastic(s, s->veloc, s->accel);
   if (s->nsources > 0 && s->stf) orc_add_sources(s, s->accel, s->it);
   orc_compute_forces_elastic(s, 0);
+  if (pml) pml_boundary(s);
   for (long g = 0; g < s->nglob; ++g) {
     s->accel[3 * g] *= s->rmassx[g];
     s->accel[3 * g + 1] *= s->rmassy[g];

@@ -95,6 +95,18 @@ typedef struct orc_sim {
   int *rec_is_acoustic;                /* (nrec) records pressure when 1 */
   int fluid_vector;                    /* 1: fluid receivers record (1/rho) grad of the potential */
   realw *cstore;                       /* ANISOTROPY: (21, 125*nspec) c11..c66 per point, or NULL */
+
+  /* C-PML layers, forward field (prepare_timerun_pml, compute_forces_viscoelastic_PML) */
+  int nspec_cpml;
+  int *is_cpml;                        /* (nspec) 0/1 */
+  int *cpml_to_spec;                   /* (nspec_cpml) 1-based */
+  int *spec_to_cpml;                   /* (nspec) 1-based, 0 outside the layers */
+  realw *pml_coef_alpha, *pml_coef_beta;   /* (9, 125, nspec_cpml) */
+  realw *pml_coef_abar;                /* (5, 125, nspec_cpml) */
+  realw *pml_coef_strain;              /* (18, 125, nspec_cpml) */
+  realw *wgll_cube;                    /* (125) */
+  realw *pml_displ_old, *pml_displ_new;    /* (3, 125, nspec_cpml) */
+  realw *pml_rmem;                     /* (48, 125, nspec_cpml) convolution memory variables */
 } orc_sim;
 
 #endif

@@ -11,7 +11,7 @@
 // * acoustic MPI interface pack / assembly (transfer_boun_pot_from_device,
 //   transfer_asmbl_pot_to_device);
 // * Stacey of a recomputed backward field (*_undoatt_cuda);
-// * features this library does not provide (noise tomography, faults, C-PML,
+// * features this library does not provide (noise tomography, faults,
 //   gravity, ocean load): the call records
 //   SF3D_ERR_UNSUPPORTED (sf3d_last_error) and does nothing else.
 #include <stdarg.h>
@@ -410,28 +410,7 @@ void transfer_surface_to_host_(long* Mesh_pointer, realw* h_noise_surface_movie)
   unsupported("noise tomography (transfer_surface_to_host)");
 }
 
-// C-PML, gravity, ocean load
-void prepare_fields_elastic_pml_(long* Mesh_pointer, int* NSPEC_CPML, int* is_CPML, int* CPML_to_spec,
-                                 int* spec_to_CPML, realw* pml_convolution_coef_alpha, realw* pml_convolution_coef_beta,
-                                 realw* pml_convolution_coef_abar, realw* pml_convolution_coef_strain,
-                                 realw* h_wgll_cube, realw* rhostore) {
-  (void)Mesh_pointer; (void)NSPEC_CPML; (void)is_CPML; (void)CPML_to_spec; (void)spec_to_CPML;
-  (void)pml_convolution_coef_alpha; (void)pml_convolution_coef_beta; (void)pml_convolution_coef_abar;
-  (void)pml_convolution_coef_strain; (void)h_wgll_cube; (void)rhostore;
-  unsupported("C-PML (prepare_fields_elastic_pml)");
-}
-void pml_impose_boundary_condition_elastic_cuda_(long* Mesh_pointer) {
-  (void)Mesh_pointer;
-  unsupported("C-PML (pml_impose_boundary_condition_elastic_cuda)");
-}
-void transfer_pml_displ_from_device_(int* size, realw* PML_displ_old, realw* PML_displ_new, long* Mesh_pointer) {
-  (void)size; (void)PML_displ_old; (void)PML_displ_new; (void)Mesh_pointer;
-  unsupported("C-PML (transfer_pml_displ_from_device)");
-}
-void transfer_pml_displ_to_device_(int* size, realw* PML_displ_old, realw* PML_displ_new, long* Mesh_pointer) {
-  (void)size; (void)PML_displ_old; (void)PML_displ_new; (void)Mesh_pointer;
-  unsupported("C-PML (transfer_pml_displ_to_device)");
-}
+// gravity, ocean load (C-PML: sf3d_pml.cu)
 void prepare_fields_gravity_device_(long* Mesh_pointer, int* GRAVITY, realw* minus_deriv_gravity, realw* minus_g,
                                     realw* h_wgll_cube, realw* rhostore) {
   (void)Mesh_pointer; (void)minus_deriv_gravity; (void)minus_g; (void)h_wgll_cube; (void)rhostore;

@@ -649,6 +649,8 @@ void launch_batch_stiffness(Mesh* mp, int iphase, cudaStream_t s) {
     q.jacobian_regular = mp->jacobian_regular;
     q.displ = B->displ;
     q.accel = B->accel;
+    memcpy(q.hp, mp->h_hprime, sizeof(q.hp));
+    memcpy(q.hpw, mp->h_hprimewgll, sizeof(q.hpw));
     launch_batch_pencil(q, B->pencil_lanes, mp->geom_format, s);
     return;
   }
@@ -767,8 +769,8 @@ int sf3d_batch_prepare(long* Mesh_pointer, int nshots, const int* ispec_selected
     set_error(SF3D_ERR_STATE, "sf3d_batch_prepare: prepare_fields_elastic_device not called");
     return SF3D_ERR_STATE;
   }
-  if (mp->attenuation || mp->has_acoustic) {
-    set_error(SF3D_ERR_ARG, "sf3d_batch_prepare: batched shots support elastic meshes without attenuation");
+  if (mp->attenuation || mp->has_acoustic || mp->pml) {
+    set_error(SF3D_ERR_ARG, "sf3d_batch_prepare: batched shots support elastic meshes without attenuation or C-PML");
     return SF3D_ERR_ARG;
   }
   if (nshots < 1 || nstep < 1 || nlength < 1 || !ispec_selected_source || !sourcearrays || !stf) {

@@ -76,8 +76,8 @@ __global__ void __launch_bounds__(kPencils * W, MINB) batch_pencil_kernel(const 
     for (int c = 0; c < 3; ++c) u[c][l] = a.displ[(3 * g + c) * S + shot];
   }
   __syncthreads();  // s_gll
-  const float* hp = s_gll;                  // hprime(i2,i1) = hp[i2 + 5 i1]
-  const float* hpw = s_gll + NGLL2;         // hprimewgll(i2,i1) = hpw[i2 + 5 i1]
+  const float* hp = a.hp;                   // hprime(i2,i1) = hp[i2 + 5 i1], parameter bank
+  const float* hpw = a.hpw;                 // hprimewgll(i2,i1) = hpw[i2 + 5 i1]
 #pragma unroll
   for (int c = 0; c < 3; ++c) {
 #pragma unroll

@@ -218,10 +218,12 @@ __global__ void __launch_bounds__(NGLL3_PAD) grad_accum_kernel(const GradArgs a)
   const float exy_u = 0.5f * (du[0][1] + du[1][0]), exz_u = 0.5f * (du[0][2] + du[2][0]),
               eyz_u = 0.5f * (du[1][2] + du[2][1]);
   dd += 2.f * (exy_p * exy_u + exz_p * exz_u + eyz_p * eyz_u);
-  const double wj = (double)(a.w[i] * a.w[j] * a.w[k]) * (double)jac;
-  a.g_kappa[eo] += wj * (double)trp * (double)tru;
-  a.g_mu[eo] += wj * 2.0 * (double)dd;
-  a.g_rho[eo] += wj * (double)pa;
+  // the step's products in FP32, their time integration in FP64 (GB300's FP64 pipe
+  // is narrow: 3 conversions + 3 adds per point instead of the whole product chain)
+  const float wj = (a.w[i] * a.w[j] * a.w[k]) * jac;
+  a.g_kappa[eo] += (double)(wj * trp * tru);
+  a.g_mu[eo] += (double)(wj * 2.f * dd);
+  a.g_rho[eo] += (double)(wj * pa);
 }
 
 // Fused form of one element's part of the transposed step: K p (the elastic
@@ -297,10 +299,11 @@ __global__ void __launch_bounds__(NGLL3_PAD, 5) adj_stiffness_grad_kernel(const 
     const float exy_u = 0.5f * (du[0][1] + du[1][0]), exz_u = 0.5f * (du[0][2] + du[2][0]),
                 eyz_u = 0.5f * (du[1][2] + du[2][1]);
     dd += 2.f * (exy_p * exy_u + exz_p * exz_u + eyz_p * eyz_u);
-    const double wj = (double)(a.w[i] * a.w[j] * a.w[k]) * (double)jac;
-    a.g_kappa[eo] += wj * (double)trp * (double)tru;
-    a.g_mu[eo] += wj * 2.0 * (double)dd;
-    a.g_rho[eo] += wj * (double)pa;
+    // products in FP32, time integration in FP64 (as grad_accum_kernel)
+    const float wj = (a.w[i] * a.w[j] * a.w[k]) * jac;
+    a.g_kappa[eo] += (double)(wj * trp * tru);
+    a.g_mu[eo] += (double)(wj * 2.f * dd);
+    a.g_rho[eo] += (double)(wj * pa);
     // stress of p (stiffness_kernel<ATT=0> arithmetic)
     const float dxx = dp[0][0], dxy = dp[0][1], dxz = dp[0][2];
     const float dyx = dp[1][0], dyy = dp[1][1], dyz = dp[1][2];
@@ -470,6 +473,10 @@ int sf3d_gradient_setup(long* Mesh_pointer, int nstep, int checkpoint_every, dou
   if (mp->attenuation) {
     set_error(SF3D_ERR_ARG, "sf3d_gradient: attenuation is not supported (elastic misfit gradient only)");
     return SF3D_ERR_ARG;
+  }
+  if (mp->pml) {
+    set_error(SF3D_ERR_UNSUPPORTED, "sf3d_gradient: C-PML layers are not supported in the adjoint sweep");
+    return SF3D_ERR_UNSUPPORTED;
   }
   if (mp->has_acoustic) {
     set_error(SF3D_ERR_ARG, "sf3d_gradient: acoustic elements are not supported");

@@ -299,6 +299,20 @@ struct Mesh {
   void* d_pack_pool = nullptr;            // [pack_rows][128] FP16 / BF16 / FP32 values
   long pack_rows = 0;
 
+  // C-PML layers (prepare_fields_elastic_pml): forward field only
+  int pml = 0, nspec_cpml = 0;
+  int* d_is_cpml = nullptr;               // [nspec] 0/1
+  int* d_spec_to_cpml = nullptr;          // [nspec] 0-based CPML index, -1 outside the layers
+  int* d_cpml_to_spec = nullptr;          // [nspec_cpml] 0-based
+  float* d_pml_coef = nullptr;            // [nspec_cpml][41][128]: alpha 9, beta 9, A-bar 5, strain 18
+  float* d_pml_rmem = nullptr;            // [nspec_cpml][48][128] convolution memory variables
+  float* d_pml_displ_old = nullptr;       // [nspec_cpml][3][128]
+  float* d_pml_displ_new = nullptr;
+  float* d_wgll_cube = nullptr;           // [128]
+  int* d_phase_nopml = nullptr;           // [2][num_phase_ispec] phase lists without the CPML elements
+  int* d_phase_pml = nullptr;             // [2][num_phase_ispec] the CPML elements of each phase
+  int phase_nopml_n[2] = {0, 0}, phase_pml_n[2] = {0, 0};
+
   cudaStream_t stream = nullptr;
   // deferred mass + corrector of the forward [0] and backward [1] field, and its dt/2
   int pend_corrector[2] = {0, 0};
@@ -398,6 +412,11 @@ struct PencilArgs {
   float jacobian_regular;
   const float* displ;
   float* accel;
+  // hprime and hprimewgll by value: the pencil loops index them with
+  // compile-time constants, so every FMA reads its coefficient from the
+  // kernel's parameter bank instead of shared memory
+  float hp[NGLL2];
+  float hpw[NGLL2];
 };
 bool launch_batch_pencil(const PencilArgs& a, int lanes, int geom_format, cudaStream_t s);
 
@@ -494,5 +513,13 @@ void launch_stacey(Mesh* mp, const float* veloc, float* accel, cudaStream_t s);
 void launch_set_it(Mesh* mp, int it, cudaStream_t s);
 void launch_mass_corrector(Mesh* mp, float dt2, cudaStream_t s);
 StiffnessArgs stiffness_args(Mesh* mp, Fields& F, int iphase, float deltat, bool att, bool strain, bool backward);
+// C-PML (sf3d_pml.cu): PML_displ_old / _new around the predictor of the forward
+// field (before: from the fields about to be predicted; after: from the predicted
+// ones), the CPML elements' stiffness of one phase, the Dirichlet condition on
+// the layers' outer faces
+void launch_pml_displ(Mesh* mp, bool after_predictor, float dt2, float dtsq2, cudaStream_t s);
+int launch_pml_stiffness(Mesh* mp, int iphase, bool strain, cudaStream_t s);
+void launch_pml_boundary(Mesh* mp, cudaStream_t s);
+void free_pml(Mesh* mp);
 
 }  // namespace sf3d

@@ -559,6 +559,7 @@ void prepare_cleanup_device_(long* Mesh_pointer, int* ACOUSTIC_SIMULATION, int* 
   free_grad(mp);
   free_batch(mp);
   free_geometry_pack(mp);
+  free_pml(mp);
   free_interfaces(mp);
   cudaFree(mp->d_it); cudaFree(mp->d_done); cudaFree(mp->d_scratch); cudaFree(mp->d_kerr); cudaFree(mp->d_stage);
   if (mp->ev0) cudaEventDestroy(mp->ev0);

@@ -307,6 +307,11 @@ StiffnessArgs stiffness_args(Mesh* mp, Fields& F, int iphase, float deltat, bool
   memset(&a, 0, sizeof(a));
   a.nelem = iphase == 1 ? mp->nspec_outer : mp->nspec_inner;
   a.phase = mp->d_phase_ispec ? mp->d_phase_ispec + (long)(iphase - 1) * mp->num_phase_ispec : nullptr;
+  if (mp->pml && !backward) {
+    // C-PML: the CPML elements of the phase run launch_pml_stiffness instead
+    a.nelem = mp->phase_nopml_n[iphase - 1];
+    a.phase = mp->d_phase_nopml + (long)(iphase - 1) * mp->num_phase_ispec;
+  }
   a.ibool = mp->d_ibool;
   a.irregular = mp->d_irregular;
   for (int q = 0; q < 9; ++q) a.m[q] = mp->d_metric[q];
@@ -356,7 +361,20 @@ int enqueue_step(Mesh* mp, float dt, float dt2, float dtsq2, bool first_step, cu
   Fields& F = mp->f;
   cudaStream_t s = mp->stream;
   int launches = 0;
-  if (first_step) {
+  if (mp->pml) {
+    // C-PML stores predictions of the field before and after the predictor, so
+    // the corrector of the previous step runs on its own
+    const long n = 3L * mp->nglob;
+    if (!first_step) {
+      mass_corrector_kernel<<<nblk(n, 256), 256, 0, s>>>(F.veloc, F.accel, mp->d_rmassx, mp->d_rmassy, mp->d_rmassz,
+                                                         mp->nglob, dt2);
+      ++launches;
+    }
+    launch_pml_displ(mp, false, dt2, dtsq2, s);
+    predictor_kernel<<<nblk(n, 256), 256, 0, s>>>(F.displ, F.veloc, F.accel, n, dt, dt2, dtsq2);
+    launch_pml_displ(mp, true, dt2, dtsq2, s);
+    launches += 2;
+  } else if (first_step) {
     const long n = 3L * mp->nglob;
     predictor_kernel<<<nblk(n, 256), 256, 0, s>>>(F.displ, F.veloc, F.accel, n, dt, dt2, dtsq2);
   } else {
@@ -388,6 +406,11 @@ int enqueue_step(Mesh* mp, float dt, float dt2, float dtsq2, bool first_step, cu
     StiffnessArgs a = stiffness_args(mp, F, iphase, dt, att, strain, false);
     if (a.nelem <= 0) continue;
     run_stiffness(mp, a, att, strain, s);
+    ++launches;
+  }
+  if (mp->pml) {
+    for (int iphase = 1; iphase <= 2; ++iphase) launches += launch_pml_stiffness(mp, iphase, strain, s);
+    launch_pml_boundary(mp, s);
     ++launches;
   }
   if (ev) cudaEventRecord(ev[1], s);
@@ -459,6 +482,17 @@ void update_displacement_cuda_(long* Mesh_pointer, realw* deltat_F, realw* delta
   Fields* F = pick(mp, idx == 0 ? 1 : 3);
   if (!F->displ) { set_error(SF3D_ERR_STATE, "update_displacement_cuda: field not allocated"); return; }
   const long n = 3L * mp->nglob;
+  if (mp->pml && idx == 0) {
+    // C-PML: PML_displ_old / _new around an unfused predictor
+    // (update_displacement_cuda.cu:95-160)
+    flush_correctors(mp);
+    launch_pml_displ(mp, false, *deltatover2_F, *deltatsqover2_F, mp->stream);
+    predictor_kernel<<<nblk(n, 256), 256, 0, mp->stream>>>(F->displ, F->veloc, F->accel, n, *deltat_F,
+                                                           *deltatover2_F, *deltatsqover2_F);
+    launch_pml_displ(mp, true, *deltatover2_F, *deltatsqover2_F, mp->stream);
+    cuda_ok(cudaGetLastError(), "predictor_kernel (C-PML)");
+    return;
+  }
   if (mp->pend_corrector[idx] && mp->pend_dt2[idx] == *deltatover2_F) {
     // the deferred corrector of the previous step fused with this predictor
     mp->pend_corrector[idx] = 0;
@@ -494,6 +528,7 @@ void compute_forces_viscoelastic_cuda_(long* Mesh_pointer, int* iphase, realw* d
   if (fa == 1 || fa == 0) {
     StiffnessArgs a = stiffness_args(mp, mp->f, *iphase, *deltat, att, strain, false);
     run_stiffness(mp, a, att, strain, mp->stream);
+    launch_pml_stiffness(mp, *iphase, strain, mp->stream);
   }
   if ((fa == 3 || fa == 0) && mp->b.displ) {
     StiffnessArgs a = stiffness_args(mp, mp->b, *iphase, *deltat, att, strain, true);

@@ -65,6 +65,9 @@ class GPUSolver:
         self.undo_attenuation = bool(undo_attenuation)
         self._prepare_constants(db, save_forward)
         self._prepare_fields(db)
+        self.pml = bool(db.get("pml", 0))
+        if self.pml:
+            self._prepare_pml(db)
         if self.coupled:
             self._prepare_acoustic(db)
         self.it = 1
@@ -91,7 +94,7 @@ class GPUSolver:
             A.af(db["wgllwgll_yz"]),
             A.i(int(db.get("stacey", 1))), A.ai(db["abs_boundary_ispec"]), A.ai(db["abs_boundary_ijk"]),
             A.af(db["abs_boundary_normal"]), A.af(db["abs_boundary_jacobian2Dw"]),
-            A.i(int(db["num_abs_boundary_faces"]) if db.get("stacey", 1) else 0),
+            A.i(int(db["num_abs_boundary_faces"]) if (db.get("stacey", 1) or db.get("pml", 0)) else 0),
             A.ai(np.ones(nspec, np.int32)), A.i(self.nsources), A.i(self.nsources), A.af(db["sourcearrays"]),
             A.ai(np.zeros(max(self.nsources, 1), np.int32)), A.ai(db["ispec_selected_source"]),
             A.ai(db["ispec_selected_rec"]), A.i(nrec), A.i(nrec), A.i(self.simulation_type),
@@ -104,6 +107,31 @@ class GPUSolver:
         ]
         self.L.prepare_constants_device_(*args)
         abi.check()
+
+    def _prepare_pml(self, db):
+        """prepare_fields_elastic_pml (prepare_gpu.f90): the C-PML layers of a database
+        from specfem3d_gb300.pml.setup."""
+        from .meshgen import WGLL
+        A = abi.Args()
+        n = len(db["cpml_to_spec"])
+        s2c = np.zeros(self.nspec, np.int32)
+        s2c[np.asarray(db["cpml_to_spec"]) - 1] = np.arange(1, n + 1, dtype=np.int32)
+        w3 = (WGLL[None, None, :] * WGLL[None, :, None] * WGLL[:, None, None]).reshape(-1).astype(np.float32)
+        self.nspec_cpml = n
+        self.L.prepare_fields_elastic_pml_(self.mp, A.i(n), A.ai(db["is_cpml"]), A.ai(db["cpml_to_spec"]),
+                                           A.ai(s2c), *(A.af(np.asarray(db["pml_coef_" + k]).reshape(-1))
+                                                        for k in ("alpha", "beta", "abar", "strain")),
+                                           A.af(w3), A.af(db["rhostore"]))
+        abi.check()
+
+    def pml_displ(self):
+        """(PML_displ_old, PML_displ_new), each (3, 125, nspec_cpml) Fortran order."""
+        A = abi.Args()
+        n = 3 * 125 * self.nspec_cpml
+        o, w = np.zeros(n, np.float32), np.zeros(n, np.float32)
+        self.L.transfer_pml_displ_from_device_(A.i(n), o.ctypes.data, w.ctypes.data, self.mp)
+        abi.check()
+        return o, w
 
     def _prepare_fields(self, db):
         A = abi.Args()
@@ -258,6 +286,10 @@ class GPUSolver:
     def step_finish(self):
         L, A, it = self.L, abi.Args(), self.it
         one = A.i(1)
+        if getattr(self, "pml", False):
+            # Dirichlet condition on the layers' outer faces, after the forces
+            # (compute_forces_viscoelastic_calling_routine.F90:361-365)
+            L.pml_impose_boundary_condition_elastic_cuda_(self.mp)
         L.kernel_3_a_cuda_(self.mp, A.f(self.deltatover2), A.f(0.0), A.i(0), one)
         if self.nrec:
             if not hasattr(self, "_seis_host"):
