@@ -100,7 +100,7 @@ def test_every_reference_entry_point_is_declared_and_exported(gpulib):
 
 
 @pytest.mark.parametrize("name,nargs", [("fault_solver_gpu_", 4), ("transfer_surface_to_host_", 2),
-                                        ("pml_impose_boundary_condition_elastic_cuda_", 1),
+                                        ("compute_coupling_ocean_cuda_", 2),
                                         ("noise_read_add_surface_movie_cu_", 3)])
 def test_unsupported_feature_is_an_error_status(gpulib, name, nargs):
     """Entry points of features the library does not provide return with
