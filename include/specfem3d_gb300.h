@@ -524,6 +524,12 @@ int sf3d_batch_set_tiling(long *Mesh_pointer, int shots_per_block, int elements_
  * reported as shots_per_thread 0. */
 int sf3d_batch_autotune(long *Mesh_pointer, int reps, float *ms_table, int *best_shots_per_block,
                         int *best_elements_per_block, int *best_shots_per_thread);
+/* 1: every kernel of a step covers all shots (default); 2: the two halves of the
+ * shots advance on two streams, the second half's corrector/predictor running
+ * while the first half's stiffness runs and the first half's next one while the
+ * second half's stiffness runs (needs the pencil kernel and nshots / 2 divisible
+ * by its shots per CTA).  Results do not depend on the choice. */
+int sf3d_batch_set_halves(long *Mesh_pointer, int halves);
 /* Steps it_begin..it_end of all shots, graph-captured in blocks of steps_per_graph. */
 int sf3d_batch_iterate(long *Mesh_pointer, int it_begin, int it_end, realw deltat, int steps_per_graph);
 /* Device time (CUDA events on the compute stream) and launches of the last sf3d_batch_iterate. */

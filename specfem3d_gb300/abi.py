@@ -101,6 +101,8 @@ def load() -> ctypes.CDLL:
     L.sf3d_batch_prepare.argtypes = [P, ctypes.c_int, P, P, P, ctypes.c_int, ctypes.c_int, P]
     L.sf3d_batch_set_tiling.restype = ctypes.c_int
     L.sf3d_batch_set_tiling.argtypes = [P, ctypes.c_int, ctypes.c_int, ctypes.c_int]
+    L.sf3d_batch_set_halves.restype = ctypes.c_int
+    L.sf3d_batch_set_halves.argtypes = [P, ctypes.c_int]
     L.sf3d_batch_autotune.restype = ctypes.c_int
     L.sf3d_batch_autotune.argtypes = [P, ctypes.c_int, P, P, P, P]
     L.sf3d_batch_iterate.restype = ctypes.c_int

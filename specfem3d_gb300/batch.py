@@ -67,6 +67,11 @@ class BatchSolver:
                                         int(shots_per_thread)) != 0:
             abi.check()
 
+    def set_halves(self, halves: int):
+        """1: all shots in every launch; 2: two shot halves overlapped on two streams."""
+        if self.L.sf3d_batch_set_halves(self.mp, int(halves)) != 0:
+            abi.check()
+
     def autotune(self, reps: int = 3) -> dict:
         """Time every stiffness kernel and tiling at rest (per-point kernels: shots per
         thread x shots per CTA x elements per CTA; pencil kernel: shots per CTA) and keep

@@ -196,14 +196,50 @@ __device__ __forceinline__ float rmass_of(long i, long S, const float* __restric
 __global__ void batch_corrector_predictor_kernel(float* __restrict__ d, float* __restrict__ v, float* __restrict__ a,
                                                  const float* __restrict__ rmx, const float* __restrict__ rmy,
                                                  const float* __restrict__ rmz, long n, long S, float dt, float dt2,
-                                                 float dtsq2) {
-  const long i = (long)blockIdx.x * blockDim.x + threadIdx.x;
-  if (i >= n) return;
+                                                 float dtsq2, int soff = 0, int scnt = 0) {
+  long i = (long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (scnt > 0) {
+    // shots [soff, soff + scnt) of every (point, component): n counts those values
+    if (i >= n) return;
+    i = (i / scnt) * S + soff + i % scnt;
+  } else if (i >= n) {
+    return;
+  }
   const float ac = a[i] * rmass_of(i, S, rmx, rmy, rmz);
   const float vh = v[i] + dt2 * ac;
   d[i] = d[i] + dt * vh + dtsq2 * ac;
   v[i] = vh + dt2 * ac;
   a[i] = 0.f;
+}
+
+// The same on four consecutive shots of one (point, component) per thread
+// (float4; S, soff and scnt multiples of 4): one mass lookup per vector.
+__global__ void batch_corrector_predictor4_kernel(float4* __restrict__ d, float4* __restrict__ v,
+                                                  float4* __restrict__ a, const float* __restrict__ rmx,
+                                                  const float* __restrict__ rmy, const float* __restrict__ rmz,
+                                                  long n4, int S4, int soff4, int scnt4, float dt, float dt2,
+                                                  float dtsq2) {
+  const long q = (long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (q >= n4) return;
+  const long gc = q / scnt4;                 // 3 * iglob + c
+  const long i = gc * S4 + soff4 + (q - gc * scnt4);
+  const long g = gc / 3;
+  const int c = (int)(gc - 3 * g);
+  const float rm = c == 0 ? __ldg(rmx + g) : (c == 1 ? __ldg(rmy + g) : __ldg(rmz + g));
+  const float4 a4 = a[i];
+  float4 v4 = v[i], d4 = d[i];
+#define SF3D_NEWMARK(x)                        \
+  {                                            \
+    const float ac = a4.x * rm;                \
+    const float vh = v4.x + dt2 * ac;          \
+    d4.x = d4.x + dt * vh + dtsq2 * ac;        \
+    v4.x = vh + dt2 * ac;                      \
+  }
+  SF3D_NEWMARK(x) SF3D_NEWMARK(y) SF3D_NEWMARK(z) SF3D_NEWMARK(w)
+#undef SF3D_NEWMARK
+  d[i] = d4;
+  v[i] = v4;
+  a[i] = make_float4(0.f, 0.f, 0.f, 0.f);
 }
 
 __global__ void batch_mass_corrector_kernel(float* __restrict__ v, float* __restrict__ a,
@@ -222,11 +258,11 @@ __global__ void batch_stacey_kernel(int nfaces, int S, const int* __restrict__ a
                                     const float* __restrict__ jw, const int* __restrict__ ibool,
                                     const float* __restrict__ rho_vp, const float* __restrict__ rho_vs,
                                     const float* __restrict__ veloc, float* __restrict__ accel,
-                                    const int* __restrict__ is_acoustic) {
+                                    const int* __restrict__ is_acoustic, int soff, int scnt) {
   const long idx = (long)blockIdx.x * blockDim.x + threadIdx.x;
-  if (idx >= (long)nfaces * NGLL2 * S) return;
-  const long fp = idx / S;
-  const int s = (int)(idx - fp * S);
+  if (idx >= (long)nfaces * NGLL2 * scnt) return;
+  const long fp = idx / scnt;
+  const int s = soff + (int)(idx - fp * scnt);
   const int f = (int)(fp / NGLL2);
   const int e = abs_ispec[f];
   if (is_acoustic[e]) return;
@@ -249,8 +285,8 @@ __global__ void batch_stacey_kernel(int nfaces, int S, const int* __restrict__ a
 __global__ void batch_sources_kernel(int S, const int* __restrict__ ispec_src, const float* __restrict__ sa,
                                      const float* __restrict__ stf, const int* __restrict__ d_it, int nstep,
                                      const int* __restrict__ ibool, float* __restrict__ accel,
-                                     const int* __restrict__ is_acoustic) {
-  const int s = blockIdx.x, p = threadIdx.x;
+                                     const int* __restrict__ is_acoustic, int soff) {
+  const int s = soff + blockIdx.x, p = threadIdx.x;
   if (s >= S || p >= NGLL3) return;
   const int e = ispec_src[s];
   if (e < 0 || is_acoustic[e]) return;
@@ -269,9 +305,10 @@ __global__ void batch_seismogram_kernel(int nrec, int S, const int* __restrict__
                                         const float* __restrict__ hx, const float* __restrict__ he,
                                         const float* __restrict__ hg, const float* __restrict__ nu,
                                         const int* __restrict__ ibool, const float* __restrict__ field,
-                                        float* __restrict__ seismo, int nlength, const int* __restrict__ d_it) {
+                                        float* __restrict__ seismo, int nlength, const int* __restrict__ d_it,
+                                        int soff) {
   __shared__ float red[3][4];
-  const int r = blockIdx.x, s = blockIdx.y, t = threadIdx.x;
+  const int r = blockIdx.x, s = soff + blockIdx.y, t = threadIdx.x;
   float s0 = 0.f, s1 = 0.f, s2 = 0.f;
   if (t < NGLL3) {
     const int e = ispec_rec[r];
@@ -308,7 +345,10 @@ __global__ void batch_seismogram_kernel(int nrec, int S, const int* __restrict__
 }
 
 __global__ void batch_advance_kernel(int* d_it) { *d_it += 1; }
-__global__ void batch_set_it_kernel(int* d_it, int v) { *d_it = v; }
+__global__ void batch_set_it_kernel(int* d_it, int v) {
+  d_it[0] = v;
+  d_it[1] = v;
+}
 
 bool alloc_f(float** d, size_t n) { return alloc_zero((void**)d, sizeof(float) * n); }
 
@@ -626,7 +666,7 @@ void launch_sb(const BatchStiffArgs& a, int eb, cudaStream_t s) {
     launch_tile<SB, 1>(a, s);
 }
 
-void launch_batch_stiffness(Mesh* mp, int iphase, cudaStream_t s) {
+void launch_batch_stiffness(Mesh* mp, int iphase, cudaStream_t s, int soff = 0, int scnt = 0) {
   BatchState* B = mp->batch;
   if (B->pencil_lanes > 0) {
     PencilArgs q;
@@ -634,8 +674,8 @@ void launch_batch_stiffness(Mesh* mp, int iphase, cudaStream_t s) {
     q.nelem = iphase == 1 ? mp->nspec_outer : mp->nspec_inner;
     if (q.nelem <= 0) return;
     q.nshots = B->nshots;
-    q.shot_offset = 0;
-    q.shot_tiles = B->nshots / B->pencil_lanes;
+    q.shot_offset = soff;
+    q.shot_tiles = (scnt > 0 ? scnt : B->nshots) / B->pencil_lanes;
     q.phase = mp->d_phase_ispec + (long)(iphase - 1) * mp->num_phase_ispec;
     q.ibool = mp->d_ibool;
     q.irregular = mp->d_irregular;
@@ -694,43 +734,115 @@ void launch_batch_stiffness(Mesh* mp, int iphase, cudaStream_t s) {
   }
 }
 
-// One batched step; the predictor is fused with the previous corrector unless first.
-int enqueue_batch_step(Mesh* mp, float dt, float dt2, float dtsq2, bool first) {
+// The kernels of one batched step for shots [soff, soff + scnt) on stream s (the
+// whole batch: soff 0, scnt nshots); d_it: the counter of those shots.  The
+// predictor is fused with the previous corrector unless first.
+int enqueue_batch_part(Mesh* mp, float dt, float dt2, float dtsq2, bool first, int soff, int scnt, int* d_it,
+                       cudaStream_t s, bool predictor) {
   BatchState* B = mp->batch;
-  cudaStream_t s = mp->stream;
   const long S = B->nshots;
-  const long n = 3L * mp->nglob * S;
+  const bool whole = soff == 0 && scnt == S;
   int launches = 0;
-  if (first)
-    batch_predictor_kernel<<<nblk(n, 256), 256, 0, s>>>(B->displ, B->veloc, B->accel, n, dt, dt2, dtsq2);
-  else
-    batch_corrector_predictor_kernel<<<nblk(n, 256), 256, 0, s>>>(B->displ, B->veloc, B->accel, mp->d_rmassx,
-                                                                  mp->d_rmassy, mp->d_rmassz, n, S, dt, dt2, dtsq2);
-  ++launches;
+  if (predictor) {
+    const long n = 3L * mp->nglob * scnt;
+    if (first) {
+      batch_predictor_kernel<<<nblk(3L * mp->nglob * S, 256), 256, 0, s>>>(B->displ, B->veloc, B->accel,
+                                                                          3L * mp->nglob * S, dt, dt2, dtsq2);
+    } else if (S % 4 == 0 && soff % 4 == 0 && scnt % 4 == 0) {
+      const long n4 = n / 4;
+      cudaLaunchConfig_t cfg = {};
+      cudaLaunchAttribute attr[1];
+      cfg.gridDim = dim3((unsigned)nblk(n4, 256));
+      cfg.blockDim = dim3(256);
+      cfg.stream = s;
+      if (B->halves == 2) {
+        attr[0].id = cudaLaunchAttributePriority;
+        attr[0].val.priority = B->prio_hi;
+        cfg.attrs = attr;
+        cfg.numAttrs = 1;
+      }
+      cudaLaunchKernelEx(&cfg, batch_corrector_predictor4_kernel, (float4*)B->displ, (float4*)B->veloc,
+                         (float4*)B->accel, (const float*)mp->d_rmassx, (const float*)mp->d_rmassy,
+                         (const float*)mp->d_rmassz, n4, (int)(S / 4), soff / 4, scnt / 4, dt, dt2, dtsq2);
+    } else {
+      batch_corrector_predictor_kernel<<<nblk(n, 256), 256, 0, s>>>(B->displ, B->veloc, B->accel, mp->d_rmassx,
+                                                                    mp->d_rmassy, mp->d_rmassz, n, S, dt, dt2, dtsq2,
+                                                                    whole ? 0 : soff, whole ? 0 : scnt);
+    }
+    ++launches;
+    return launches;
+  }
   if (mp->stacey && mp->num_abs_faces > 0) {
-    const long nf = (long)mp->num_abs_faces * NGLL2 * S;
+    const long nf = (long)mp->num_abs_faces * NGLL2 * scnt;
     batch_stacey_kernel<<<nblk(nf, 256), 256, 0, s>>>(mp->num_abs_faces, (int)S, mp->d_abs_ispec, mp->d_abs_pt,
                                                        mp->d_abs_normal, mp->d_abs_jw, mp->d_ibool, mp->d_rho_vp,
-                                                       mp->d_rho_vs, B->veloc, B->accel, mp->d_ispec_is_acoustic);
+                                                       mp->d_rho_vs, B->veloc, B->accel, mp->d_ispec_is_acoustic, soff,
+                                                       scnt);
     ++launches;
   }
-  batch_sources_kernel<<<(unsigned)S, NGLL3_PAD, 0, s>>>((int)S, B->d_ispec_src, B->d_sa, B->d_stf, B->d_it,
-                                                         B->nstep, mp->d_ibool, B->accel, mp->d_ispec_is_acoustic);
+  batch_sources_kernel<<<(unsigned)scnt, NGLL3_PAD, 0, s>>>((int)S, B->d_ispec_src, B->d_sa, B->d_stf, d_it,
+                                                            B->nstep, mp->d_ibool, B->accel, mp->d_ispec_is_acoustic,
+                                                            soff);
   ++launches;
   for (int iphase = 1; iphase <= 2; ++iphase) {
     if ((iphase == 1 ? mp->nspec_outer : mp->nspec_inner) <= 0) continue;
-    launch_batch_stiffness(mp, iphase, s);
+    launch_batch_stiffness(mp, iphase, s, soff, whole ? 0 : scnt);
     ++launches;
   }
   if (mp->nrec_local > 0) {
-    dim3 grid((unsigned)mp->nrec_local, (unsigned)S);
+    dim3 grid((unsigned)mp->nrec_local, (unsigned)scnt);
     batch_seismogram_kernel<<<grid, NGLL3_PAD, 0, s>>>(mp->nrec_local, (int)S, mp->d_ispec_rec, mp->d_hxir,
                                                       mp->d_hetar, mp->d_hgammar, mp->d_nu_rec, mp->d_ibool,
-                                                      B->displ, B->d_seismo, B->nlength, B->d_it);
+                                                      B->displ, B->d_seismo, B->nlength, d_it, soff);
     ++launches;
   }
-  batch_advance_kernel<<<1, 1, 0, s>>>(B->d_it);
+  batch_advance_kernel<<<1, 1, 0, s>>>(d_it);
   ++launches;
+  return launches;
+}
+
+// One batched step of every shot on the compute stream (the first step: the
+// predictor of every shot, then the rest of the step per counter).
+int enqueue_batch_step(Mesh* mp, float dt, float dt2, float dtsq2, bool first) {
+  BatchState* B = mp->batch;
+  cudaStream_t s = mp->stream;
+  const int S = B->nshots;
+  int launches = 0;
+  if (B->halves == 2 && first) {
+    launches += enqueue_batch_part(mp, dt, dt2, dtsq2, true, 0, S, B->d_it, s, true);
+    launches += enqueue_batch_part(mp, dt, dt2, dtsq2, false, 0, S / 2, B->d_it, s, false);
+    launches += enqueue_batch_part(mp, dt, dt2, dtsq2, false, S / 2, S / 2, B->d_it + 1, s, false);
+    return launches;
+  }
+  launches += enqueue_batch_part(mp, dt, dt2, dtsq2, first, 0, S, B->d_it, s, true);
+  launches += enqueue_batch_part(mp, dt, dt2, dtsq2, first, 0, S, B->d_it, s, false);
+  return launches;
+}
+
+// nsteps batched steps (not the first).  With two halves the shot halves run as
+// two independent chains, the first on the compute stream and the second on the
+// side stream, forked from and joined back into the compute stream around the
+// whole segment: with no edge between the chains, one half's corrector (launched
+// at the higher priority) is dispatched while the other half's stiffness runs.
+int enqueue_batch_steps(Mesh* mp, float dt, float dt2, float dtsq2, int nsteps) {
+  BatchState* B = mp->batch;
+  int launches = 0;
+  if (B->halves != 2) {
+    for (int q = 0; q < nsteps; ++q) launches += enqueue_batch_step(mp, dt, dt2, dtsq2, false);
+    return launches;
+  }
+  cudaStream_t s = mp->stream;
+  const int h = B->nshots / 2;
+  cudaEventRecord(B->ev_fork, s);
+  cudaStreamWaitEvent(B->side, B->ev_fork, 0);
+  for (int q = 0; q < nsteps; ++q) {
+    launches += enqueue_batch_part(mp, dt, dt2, dtsq2, false, 0, h, B->d_it, s, true);
+    launches += enqueue_batch_part(mp, dt, dt2, dtsq2, false, 0, h, B->d_it, s, false);
+    launches += enqueue_batch_part(mp, dt, dt2, dtsq2, false, h, h, B->d_it + 1, B->side, true);
+    launches += enqueue_batch_part(mp, dt, dt2, dtsq2, false, h, h, B->d_it + 1, B->side, false);
+  }
+  cudaEventRecord(B->ev_join, B->side);
+  cudaStreamWaitEvent(s, B->ev_join, 0);
   return launches;
 }
 
@@ -747,6 +859,9 @@ void free_batch(Mesh* mp) {
   if (!B) return;
   cudaFree(B->displ); cudaFree(B->veloc); cudaFree(B->accel);
   cudaFree(B->d_ispec_src); cudaFree(B->d_sa); cudaFree(B->d_stf); cudaFree(B->d_seismo); cudaFree(B->d_it);
+  if (B->side) cudaStreamDestroy(B->side);
+  if (B->ev_fork) cudaEventDestroy(B->ev_fork);
+  if (B->ev_join) cudaEventDestroy(B->ev_join);
   delete B;
   mp->batch = nullptr;
 }
@@ -805,7 +920,12 @@ int sf3d_batch_prepare(long* Mesh_pointer, int nshots, const int* ispec_selected
   bool ok = alloc_f(&B->displ, n) && alloc_f(&B->veloc, n) && alloc_f(&B->accel, n) &&
             alloc_zero((void**)&B->d_ispec_src, sizeof(int) * nshots) && alloc_f(&B->d_sa, sa.size()) &&
             alloc_f(&B->d_stf, tab.size()) && alloc_f(&B->d_seismo, nseis) &&
-            alloc_zero((void**)&B->d_it, sizeof(int));
+            alloc_zero((void**)&B->d_it, 2 * sizeof(int)) &&
+            cuda_ok(cudaStreamCreateWithFlags(&B->side, cudaStreamNonBlocking), "cudaStreamCreate") &&
+            cuda_ok(cudaEventCreateWithFlags(&B->ev_fork, cudaEventDisableTiming), "cudaEventCreate") &&
+            cuda_ok(cudaEventCreateWithFlags(&B->ev_join, cudaEventDisableTiming), "cudaEventCreate");
+  int prio_lo = 0;
+  ok = ok && cuda_ok(cudaDeviceGetStreamPriorityRange(&prio_lo, &B->prio_hi), "cudaDeviceGetStreamPriorityRange");
   ok = ok && copy_sync(B->d_ispec_src, isp.data(), sizeof(int) * nshots, cudaMemcpyHostToDevice, mp->stream) &&
        copy_sync(B->d_sa, sa.data(), sizeof(float) * sa.size(), cudaMemcpyHostToDevice, mp->stream) &&
        copy_sync(B->d_stf, tab.data(), sizeof(float) * tab.size(), cudaMemcpyHostToDevice, mp->stream);
@@ -831,6 +951,7 @@ int sf3d_batch_set_tiling(long* Mesh_pointer, int shots_per_block, int elements_
       return SF3D_ERR_ARG;
     }
     mp->batch->pencil_lanes = sb;
+    if (mp->batch->nshots % (2 * sb) != 0) mp->batch->halves = 1;
     return SF3D_OK;
   }
   const bool ok_sb = (sb == 1 || sb == 2 || sb == 4 || sb == 8) && mp->batch->nshots % sb == 0;
@@ -841,9 +962,28 @@ int sf3d_batch_set_tiling(long* Mesh_pointer, int shots_per_block, int elements_
     return SF3D_ERR_ARG;
   }
   mp->batch->pencil_lanes = 0;
+  mp->batch->halves = 1;
   mp->batch->shots_per_block = sb;
   mp->batch->elements_per_block = eb;
   mp->batch->shots_per_thread = spt;
+  return SF3D_OK;
+}
+
+int sf3d_batch_set_halves(long* Mesh_pointer, int halves) {
+  Mesh* mp = get_mesh(Mesh_pointer);
+  if (!mp) return SF3D_ERR_STATE;
+  if (!mp->batch) { set_error(SF3D_ERR_STATE, "sf3d_batch_prepare not called"); return SF3D_ERR_STATE; }
+  BatchState* B = mp->batch;
+  if (halves != 1 && halves != 2) {
+    set_error(SF3D_ERR_ARG, "sf3d_batch_set_halves: halves must be 1 or 2");
+    return SF3D_ERR_ARG;
+  }
+  if (halves == 2 && (B->pencil_lanes <= 0 || B->nshots % (2 * B->pencil_lanes) != 0)) {
+    set_error(SF3D_ERR_ARG, "sf3d_batch_set_halves: two halves need the pencil kernel and a half of the shots "
+                            "divisible by its shots per CTA");
+    return SF3D_ERR_ARG;
+  }
+  B->halves = halves;
   return SF3D_OK;
 }
 
@@ -907,6 +1047,7 @@ int sf3d_batch_autotune(long* Mesh_pointer, int reps, float* ms_table, int* best
     if (bsb < 0 || ms < best) { best = ms; blanes = lanes[q]; }
   }
   B->pencil_lanes = blanes;
+  if (blanes == 0 || B->nshots % (2 * blanes) != 0) B->halves = 1;
   if (blanes > 0) {
     bsb = blanes;
     beb = 1;
@@ -944,9 +1085,10 @@ int sf3d_batch_iterate(long* Mesh_pointer, int it_begin, int it_end, realw delta
     cudaGraphExec_t exec = nullptr;
     int per_block = 0;
     SF3D_CUDA_RET(cudaStreamBeginCapture(s, cudaStreamCaptureModeThreadLocal), SF3D_ERR_CUDA);
-    for (int q = 0; q < K; ++q) per_block += enqueue_batch_step(mp, dt, dt2, dtsq2, false);
+    per_block = enqueue_batch_steps(mp, dt, dt2, dtsq2, K);
     SF3D_CUDA_RET(cudaStreamEndCapture(s, &graph), SF3D_ERR_CUDA);
-    SF3D_CUDA_RET(cudaGraphInstantiate(&exec, graph, 0), SF3D_ERR_CUDA);
+    SF3D_CUDA_RET(cudaGraphInstantiateWithFlags(&exec, graph, cudaGraphInstantiateFlagUseNodePriority),
+                  SF3D_ERR_CUDA);
     while (remaining >= K) {
       if (!cuda_ok(cudaGraphLaunch(exec, s), "cudaGraphLaunch")) break;
       launches += per_block;
@@ -955,10 +1097,7 @@ int sf3d_batch_iterate(long* Mesh_pointer, int it_begin, int it_end, realw delta
     cudaGraphExecDestroy(exec);
     cudaGraphDestroy(graph);
   }
-  while (remaining > 0) {
-    launches += enqueue_batch_step(mp, dt, dt2, dtsq2, false);
-    --remaining;
-  }
+  if (remaining > 0) launches += enqueue_batch_steps(mp, dt, dt2, dtsq2, remaining);
   const long n = 3L * mp->nglob * B->nshots;
   batch_mass_corrector_kernel<<<nblk(n, 256), 256, 0, s>>>(B->veloc, B->accel, mp->d_rmassx, mp->d_rmassy,
                                                           mp->d_rmassz, n, B->nshots, dt2);

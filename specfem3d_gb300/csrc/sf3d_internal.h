@@ -139,10 +139,18 @@ struct BatchState {
   float* d_sa = nullptr;        // [nshots][128][3] source arrays
   float* d_stf = nullptr;       // [nstep][nshots]
   float* d_seismo = nullptr;    // [nlength][nshots][nrec_local][3]
-  int* d_it = nullptr;          // device step counter (1-based)
+  int* d_it = nullptr;          // device step counters (1-based), one per shot half
   size_t bytes = 0;
   float last_ms = 0.f;
   int last_launches = 0;
+  // 2: the two shot halves advance as two independent chains on two streams
+  // (shots never interact), the correctors launched at the higher priority so
+  // that one half's HBM-bound corrector runs beside the other half's stiffness
+  // (pencil kernel only)
+  int halves = 1;
+  int prio_hi = 0;              // greatest stream priority of the device
+  cudaStream_t side = nullptr;
+  cudaEvent_t ev_fork = nullptr, ev_join = nullptr;
 };
 
 struct Mesh {

@@ -71,6 +71,26 @@ def test_batched_shots_equal_plain_runs(plain_runs, tiling):
             assert rel_l2(seis[shot], O.seismograms(sim)) < 5e-5, shot
 
 
+@pytest.mark.parametrize("lanes", [8])
+def test_batched_two_halves_equal_plain_runs(plain_runs, lanes):
+    """The two shot halves on two streams (each half's corrector under the other
+    half's stiffness, graph-captured with event edges, and the remainder launched
+    directly) give every shot its plain run."""
+    from specfem3d_gb300.batch import BatchSolver
+    cfg, db, seis_ref, disp_ref = plain_runs
+    b = BatchSolver(db, cfg)
+    b.set_tiling(lanes, 1, 0)
+    b.set_halves(2)
+    b.run(cfg["nstep"] // 2, steps_per_graph=25)
+    b.run(cfg["nstep"] - cfg["nstep"] // 2, steps_per_graph=40)
+    seis = b.seismograms()
+    disp = b.displacement()
+    b.close()
+    for s in range(len(cfg["shots"])):
+        assert rel_l2(seis[s], seis_ref[s]) < 1e-5, s
+        assert rel_l2(disp[s], disp_ref[s]) < 1e-5, s
+
+
 def test_batched_pencil_32_shots_and_packed_moduli(gpulib):
     """32 shots: the pencil kernel with 32 shots per CTA equals the per-point float4
     kernel to the atomic-order level, and three shots equal their plain runs; packed
