@@ -123,11 +123,13 @@ __global__ void __launch_bounds__(kPencils * W, MINB) batch_pencil_kernel(const 
   __syncthreads();  // rows 3-8 complete; every read of rows 0-2 done
 
   // ---- strain, stress and J sigma grad(xi) at the z-line's points ---------------
-  // F[d][c] (contraction direction d, component c) goes to row 3d + c: rows 0-2 hold
-  // nothing live at these points any more, rows 3-8 were just read by this thread
+  // F[d][c] (contraction direction d, component c): d = 0, 1 go to row 3d + c (rows
+  // 0-2 hold nothing live at these points any more, rows 3-5 were just read by this
+  // thread); d = 2 stays in registers for the z-line's own transposed contraction
   const ElemPack* pk = GEOM != kGeomFP32 ? a.pack + e : nullptr;
   const unsigned vary = GEOM != kGeomFP32 ? __ldg(&pk->vary) : 0u;
   const int pbase = GEOM != kGeomFP32 ? __ldg(&pk->base) : 0;
+  float fz[3][NGLLX];
 #pragma unroll
   for (int o = 0; o < NGLLX; ++o) {
     const int p = zb + NGLL2 * o;
@@ -188,11 +190,15 @@ __global__ void __launch_bounds__(kPencils * W, MINB) batch_pencil_kernel(const 
       F[6] = js * sxz; F[7] = js * syz; F[8] = js * szz;
     }
 #pragma unroll
-    for (int q = 0; q < 9; ++q) ROW(q, p) = F[q];
+    for (int q = 0; q < 6; ++q) ROW(q, p) = F[q];
+#pragma unroll
+    for (int c = 0; c < 3; ++c) fz[c][o] = F[6 + c];
   }
   __syncthreads();
 
-  // ---- transposed contractions: x (rows 0-2), weighted partial sum into rows 0-2
+  // ---- transposed contractions along x (rows 0-2) and y (rows 3-5), each written
+  // in place along the thread's own line: the two passes touch disjoint rows, so
+  // no barrier separates them
   {
     const float fac1 = s_gll[4 * NGLL2 + pa + NGLLX * pb];  // wgllwgll_yz(j, k)
 #pragma unroll
@@ -208,11 +214,6 @@ __global__ void __launch_bounds__(kPencils * W, MINB) batch_pencil_kernel(const 
         ROW(c, xb + o) = fac1 * n;
       }
     }
-  }
-  __syncthreads();
-  // ---- y (rows 3-5), added to the partial sum ------------------------------------
-  {
-    const float fac2 = s_gll[3 * NGLL2 + pa + NGLLX * pb];  // wgllwgll_xz(i, k)
 #pragma unroll
     for (int c = 0; c < 3; ++c) {
       float v[NGLLX];
@@ -223,28 +224,27 @@ __global__ void __launch_bounds__(kPencils * W, MINB) batch_pencil_kernel(const 
         float n = 0.f;
 #pragma unroll
         for (int l = 0; l < NGLLX; ++l) n = fmaf(v[l], hpw[l + NGLLX * o], n);
-        float& r = ROW(c, yb + NGLLX * o);
-        r = fmaf(fac2, n, r);
+        ROW(3 + c, yb + NGLLX * o) = n;      // unweighted: fac2 applied in the sum below
       }
     }
   }
   __syncthreads();
-  // ---- z (rows 6-8), final sum and scatter-add -----------------------------------
+  // ---- z from registers, the weighted sum (fac1 nx + fac2 ny + fac3 nz, in that
+  // order and rounding) and the scatter-add ------------------------------------------
   {
     const float fac3 = s_gll[2 * NGLL2 + pa + NGLLX * pb];  // wgllwgll_xy(i, j)
 #pragma unroll
-    for (int c = 0; c < 3; ++c) {
-      float v[NGLLX];
+    for (int o = 0; o < NGLLX; ++o) {
+      const int p = zb + NGLL2 * o;
+      const float fac2 = s_gll[3 * NGLL2 + pa + NGLLX * o];  // wgllwgll_xz(i, k)
+      const long g = __ldg(a.ibool + eb + p);
 #pragma unroll
-      for (int l = 0; l < NGLLX; ++l) v[l] = ROW(6 + c, zb + NGLL2 * l);
-#pragma unroll
-      for (int o = 0; o < NGLLX; ++o) {
-        const int p = zb + NGLL2 * o;
-        const long g = __ldg(a.ibool + eb + p);
+      for (int c = 0; c < 3; ++c) {
         float n = 0.f;
 #pragma unroll
-        for (int l = 0; l < NGLLX; ++l) n = fmaf(v[l], hpw[l + NGLLX * o], n);
-        atomicAdd(a.accel + (3 * g + c) * S + shot, -(ROW(c, p) + fac3 * n));
+        for (int l = 0; l < NGLLX; ++l) n = fmaf(fz[c][l], hpw[l + NGLLX * o], n);
+        const float r = fmaf(fac2, ROW(3 + c, p), ROW(c, p));
+        atomicAdd(a.accel + (3 * g + c) * S + shot, -(r + fac3 * n));
       }
     }
   }
