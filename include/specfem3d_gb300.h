@@ -357,7 +357,12 @@ int sf3d_last_timing(long *Mesh_pointer, float *stiffness_ms, int *stiffness_lau
  *               streams (read and written once per launch), 6 and 7 CTAs/SM;
  *   10, 11:     three threads per GLL point (one per displacement component),
  *               384-thread CTAs, 3 and 4 CTAs/SM.
- * Default 3 (the fastest on GB300 for the layered viscoelastic workload).
+ * Under a packed geometry format (sf3d_set_geometry_format) the variant picks
+ * the packed build: 4 at 7 CTAs/SM; 5, 6, 7 with the memory variables and
+ * strains staged by cp.async and the factors read from the element record, at
+ * 8, 9, 10 CTAs/SM (register budget 64, 56, 48); any other at 6.
+ * Default 3 (the fastest on GB300 for the layered viscoelastic workload with
+ * the FP32 arrays).
  * No reference counterpart (the reference compiles one Kernel_2 per
  * configuration). */
 int sf3d_set_stiffness_variant(long *Mesh_pointer, int variant);

@@ -61,7 +61,7 @@ __device__ __forceinline__ void st_state(float* p, float v) {
 template <bool ATT, bool STRAIN, int MINB, int GEOM = kGeomFP32, bool STAGE = false, bool ATOMIC = true,
           bool STREAM = false, bool ANISO = false>
 __global__ void __launch_bounds__(NGLL3_PAD, MINB) stiffness_kernel(const StiffnessArgs a) {
-  __shared__ __align__(16) float s_att[(ATT && STAGE) ? 30 : 1][NGLL3_PAD];
+  __shared__ __align__(16) float s_att[(ATT && STAGE) ? (GEOM == kGeomFP32 ? 30 : 24) : 1][NGLL3_PAD];
   __shared__ float s_gll[NGLL3];
   __shared__ float s_u[3][NGLL3_PAD];
   __shared__ float s_v[ATT ? 3 : 1][NGLL3_PAD];
@@ -92,12 +92,13 @@ __global__ void __launch_bounds__(NGLL3_PAD, MINB) stiffness_kernel(const Stiffn
   for (int s = 0; s < NSLS; ++s) fc[s] = fck[s] = 0.f;
   if (ATT && STAGE && active) {
     // rows: R[c][s] -> 3c+s (0..17), epsilondev[c] -> 18+c, factor_common[s] -> 24+s,
-    // factor_common_kappa[s] -> 27+s.  Each thread copies (4-byte cp.async) and later
-    // reads only its own point's column, so no barrier is needed, and the copies
-    // stay in flight through the first contraction set.
+    // factor_common_kappa[s] -> 27+s (FP32 geometry only: the packed formats read
+    // the factors from the element record where they are used).  Each thread copies
+    // (4-byte cp.async) and later reads only its own point's column, so no barrier
+    // is needed, and the copies stay in flight through the first contraction set.
     const long se = (long)e * (NSLS * NGLL3_PAD) + t, ee = (long)e * NGLL3_PAD + t;
 #pragma unroll
-    for (int row = 0; row < 30; ++row) {
+    for (int row = 0; row < (GEOM == kGeomFP32 ? 30 : 24); ++row) {
       const float* src;
       if (row < 18) src = a.R[row / 3] + se + (row % 3) * NGLL3_PAD;
       else if (row < 24) src = a.eps[row - 18] + ee;
@@ -346,10 +347,24 @@ __global__ void __launch_bounds__(NGLL3_PAD, MINB) stiffness_kernel(const Stiffn
 #pragma unroll
       for (int s = 0; s < NSLS; ++s) {
         const float al = a.alpha[s], be = a.beta[s], ga = a.gamma[s];
-        const float fk = fkap * (STAGE ? s_att[27 + s][t] : fck[s]);
+        float fcs = 0.f, fcks = 0.f;
+        if (STAGE && GEOM != kGeomFP32) {
+          const ElemPack* pk = a.pack + e;
+          const unsigned vary = __ldg(&pk->vary);
+          const int base = __ldg(&pk->base);
+          fcs = pack_value<GEOM>(pk, a.pool, vary, base, 11 + s, t);
+          fcks = pack_value<GEOM>(pk, a.pool, vary, base, 14 + s, t);
+        } else if (STAGE) {
+          fcs = s_att[24 + s][t];
+          fcks = s_att[27 + s][t];
+        } else {
+          fcs = fc[s];
+          fcks = fck[s];
+        }
+        const float fk = fkap * fcks;
         const float r5 = STAGE ? s_att[15 + s][t] : R[5][s];
         st_state<STREAM>(a.R[5] + so + s * NGLL3_PAD, al * r5 + fk * (be * eold[5] + ga * epsl[5]));
-        const float fm = fmu * (STAGE ? s_att[24 + s][t] : fc[s]);
+        const float fm = fmu * fcs;
 #pragma unroll
         for (int c = 0; c < 5; ++c) {
           const float rc = STAGE ? s_att[3 * c + s][t] : R[c][s];
@@ -377,14 +392,14 @@ void launch_minb(const StiffnessArgs& a, bool att, bool store_strain, cudaStream
     stiffness_kernel<false, false, MINB, GEOM, false, true, STREAM><<<grid, block, 0, s>>>(a);
 }
 
-template <int MINB>
+template <int MINB, bool STAGE = false>
 void launch_packed(const StiffnessArgs& a, bool att, bool store_strain, cudaStream_t s, int geom) {
   if (geom == kGeomPackF16)
-    launch_minb<MINB, kGeomPackF16>(a, att, store_strain, s);
+    launch_minb<MINB, kGeomPackF16, STAGE>(a, att, store_strain, s);
   else if (geom == kGeomPackBF16)
-    launch_minb<MINB, kGeomPackBF16>(a, att, store_strain, s);
+    launch_minb<MINB, kGeomPackBF16, STAGE>(a, att, store_strain, s);
   else
-    launch_minb<MINB, kGeomPackF32>(a, att, store_strain, s);
+    launch_minb<MINB, kGeomPackF32, STAGE>(a, att, store_strain, s);
 }
 
 }  // namespace
@@ -392,10 +407,22 @@ void launch_packed(const StiffnessArgs& a, bool att, bool store_strain, cudaStre
 // blocks_per_sm: the register budget the kernel is compiled for (4..7 CTAs of
 // 128 threads per SM; more CTAs keep more elements' loads in flight, fewer
 // let the compiler keep every load of an element in registers).  The packed
-// geometry builds exist for 6 and 7 CTAs/SM.
+// geometry builds exist for 6 and 7 CTAs/SM, and with cp.async-staged memory
+// variables for 8, 9 and 10.
 void launch_stiffness(const StiffnessArgs& a, bool att, bool store_strain, cudaStream_t s, int blocks_per_sm,
                       int geom_format, bool staged, bool streaming) {
   if (a.nelem <= 0) return;
+  if (geom_format != kGeomFP32 && staged) {
+    // staged memory variables and record-resident constants leave 48-64
+    // registers a thread (no spills): 8, 9 or 10 CTAs/SM of 20.5 KB shared memory
+    if (blocks_per_sm >= 10)
+      launch_packed<10, true>(a, att, store_strain, s, geom_format);
+    else if (blocks_per_sm == 9)
+      launch_packed<9, true>(a, att, store_strain, s, geom_format);
+    else
+      launch_packed<8, true>(a, att, store_strain, s, geom_format);
+    return;
+  }
   if (streaming) {
     if (blocks_per_sm == 7)
       launch_minb<7, kGeomFP32, false, true>(a, att, store_strain, s);

@@ -434,6 +434,9 @@ void launch_stiffness_pipelined(const StiffnessArgs& a, bool att, bool store_str
 //   5, 6, 7: one CTA per element with cp.async-staged memory variables at 6, 7, 8 CTAs/SM;
 //   8, 9: one CTA per element, evict-first hints on the element streams, 6 and 7 CTAs/SM;
 //   10, 11: three threads per point (384-thread CTAs), 3 and 4 CTAs/SM
+// Under a packed geometry format (sf3d_set_geometry_format) 4 selects the packed
+// build at 7 CTAs/SM, 5, 6, 7 the packed builds with staged memory variables at
+// 8, 9, 10 CTAs/SM, and every other variant the packed build at 6.
 constexpr int kNumStiffnessVariants = 12;
 inline int variant_blocks_per_sm(int v) {
   const int t[kNumStiffnessVariants] = {4, 0, 5, 6, 7, 6, 7, 8, 6, 7, 3, 4};
@@ -496,10 +499,16 @@ inline void run_stiffness(Mesh* mp, const StiffnessArgs& a, bool att, bool store
   }
   if (mp->geom_format) {
     // packed static streams: the one-CTA-per-element kernel at 6 or 7 CTAs/SM
+    // (variant 4: 7), or with cp.async-staged memory variables at 8, 9 or 10
+    // (variants 5, 6, 7)
     StiffnessArgs h = a;
     h.pack = mp->d_pack;
     h.pool = mp->d_pack_pool;
-    launch_stiffness(h, att, store_strain, s, mp->stiffness_variant == 4 ? 7 : 6, mp->geom_format);
+    const int v = mp->stiffness_variant;
+    if (variant_staged(v))
+      launch_stiffness(h, att, store_strain, s, v + 3, mp->geom_format, true);
+    else
+      launch_stiffness(h, att, store_strain, s, v == 4 ? 7 : 6, mp->geom_format);
   } else if (mp->stiffness_variant == 1 && mp->d_kerr) {
     launch_stiffness_pipelined(a, att, store_strain, mp->d_kerr, s);
   } else if (variant_split(mp->stiffness_variant)) {

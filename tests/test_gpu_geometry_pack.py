@@ -46,7 +46,11 @@ def test_packed_formats_exact_on_layered_block(gpulib):
         assert rel_l2(out[fmt], out["fp32"]) < 1e-6, fmt
 
 
-def test_packed_formats_one_pass_on_full_metric_tensors(gpulib):
+@pytest.mark.parametrize("variant", [3, 4, 5, 6, 7])
+def test_packed_formats_one_pass_on_full_metric_tensors(gpulib, variant):
+    """variants 3 / 4: packed builds at 6 / 7 CTAs/SM; 5 / 6 / 7: packed builds with
+    cp.async-staged memory variables at 8 / 9 / 10 CTAs/SM (factors read from the
+    element record where they are used)."""
     from specfem3d_gb300 import configs, hexmesh
     from specfem3d_gb300.solver import GPUSolver
     cfg = configs.small_layered(nstep=4, attenuation=True)
@@ -60,6 +64,7 @@ def test_packed_formats_one_pass_on_full_metric_tensors(gpulib):
     res = {}
     for fmt in ("fp32",) + FORMATS:
         g = GPUSolver(db, c)
+        g.set_stiffness_variant(variant)
         g.set_geometry_format(fmt)
         if fmt != "fp32":
             assert g.geometry_pack_info()[0] == 9 * nspec, fmt
