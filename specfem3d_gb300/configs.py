@@ -146,6 +146,27 @@ def refex_no_absorbing(nstep: int = 5000) -> dict:
     return cfg
 
 
+def refex_cpml(nstep: int = 2400) -> dict:
+    """The reference example CPML_examples/homogeneous_halfspace_HEX8_elastic_absorbing_CPML_5sides:
+    the 36 x 36 x 16 block of the Stacey example with C-PML layers of three
+    elements on the four sides and the bottom (absorbing_cpml_file: 9036 CPML
+    elements, widths 11166.667 / 11166.667 / 11250 m), f0_FOR_PML 0.05555 Hz,
+    no Stacey; FORCESOLUTION: a point force of 1e10 N along (E, N, Z_UP) =
+    (1, -2, -1), normalised (setup_sources_receivers.f90:1132-1143), with a
+    0.128 Hz Ricker at (67, 67, -30) km, a mesh vertex, where a point force lands
+    on the vertex's one global point whichever element holds it; dt 0.11 s.
+    The layers themselves come from ``pml.setup(db, cfg, nel=3, f0=cfg["pml_f0"])``."""
+    cfg = refex(nstep)
+    cfg["dt"] = 0.11
+    f = np.array([1.0, -2.0, -1.0])
+    f = 1e10 * f / np.sqrt(np.sum(f * f))
+    cfg["sources"] = [dict(type="force", x=67000.0, y=67000.0, z=-30000.0, F=[float(v) for v in f],
+                           stf="ricker", f0=0.128)]
+    cfg["pml_f0"] = 0.05555
+    cfg["pml_elements"] = 3
+    return cfg
+
+
 def attenuation_benchmark(nstep: int = 1300) -> dict:
     """The reference benchmark EXAMPLES/benchmarks/attenuation/viscoelastic: an
     80 x 80 x 80 regular mesh of 37.5 m cubes spanning [-1500, 1500]^3 m

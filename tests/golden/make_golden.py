@@ -16,13 +16,13 @@ EX = "EXAMPLES/applications"
 STATIONS = ["X20", "X30", "X40", "X50"]
 
 
-def read(root, example, ext):
+def read(root, example, ext, band="BX"):
     d = os.path.join(root, EX, example, "REF_SEIS")
     traces, t = [], None
     for st in STATIONS:
         comps = []
         for c in "XYZ":
-            a = np.loadtxt(os.path.join(d, f"DB.{st}.BX{c}.{ext}"))
+            a = np.loadtxt(os.path.join(d, f"DB.{st}.{band}{c}.{ext}"))
             t = a[:, 0]
             comps.append(a[:, 1])
         traces.append(comps)
@@ -96,6 +96,9 @@ def main():
     np.savez_compressed(os.path.join(out, "refex_stacey5sides.npz"), displ=d, t=t, stations=np.array(STATIONS))
     nd, t2 = read(root, "homogeneous_halfspace_HEX8_elastic_no_absorbing", "semd")
     np.savez_compressed(os.path.join(out, "refex_no_absorbing.npz"), displ=nd, t=t2, stations=np.array(STATIONS))
+    # C-PML example (dt 0.11 s: band code M)
+    cd, t3 = read(root, "CPML_examples/homogeneous_halfspace_HEX8_elastic_absorbing_CPML_5sides", "semd", "MX")
+    np.savez_compressed(os.path.join(out, "refex_cpml5sides.npz"), displ=cd, t=t3, stations=np.array(STATIONS))
     np.savez_compressed(os.path.join(out, "waterlayered.npz"), **read_waterlayered(root))
     np.savez_compressed(os.path.join(out, "attenuation_benchmark.npz"), **read_attenuation_benchmark(root))
     np.savez_compressed(os.path.join(out, "analytic_elastic.npz"), **read_analytic_elastic(root))

@@ -11,6 +11,8 @@ pml_impose_boundary_condition_elastic_cuda, transfer_pml_displ_*): a block of
   times as wide and deep (no reflection within the window) the layered block's
   traces differ by <= 2 % (Stacey conditions on the same small block: about 3 %;
   measured 1.25 % and 2.9 % on the oracle);
+* the reference's own C-PML example (36x36x16 block, three-element layers on five
+  faces, 2400 steps) matches its REF_SEIS traces to 2.5e-6 relative L2;
 * meshes the device C-PML does not cover are rejected with an error status."""
 import os
 
@@ -73,6 +75,35 @@ def test_pml_absorbs(pml_db):
     print(f"against the wide block: C-PML {e_pml:.3e}, Stacey {e_st:.3e}")
     assert e_pml < 0.02
     assert e_pml < e_st
+
+
+@pytest.mark.parametrize("per_call", [False, True])
+def test_pml_reference_golden_seismograms(gpulib, per_call):
+    """The reference's C-PML example (CPML_examples/homogeneous_halfspace_HEX8_elastic_
+    absorbing_CPML_5sides: 36x36x16 block, three-element layers on five faces,
+    point force, 2400 steps of 0.11 s) on the device against its REF_SEIS:
+    relative L2 <= 2e-5 over all traces and <= 1e-4 per trace, correlation
+    >= 0.99999, through the fused loop and the per-call entry points (measured
+    2.5e-6 over all traces, worst trace 9.4e-6)."""
+    from specfem3d_gb300 import configs, meshgen, pml
+    from specfem3d_gb300.solver import GPUSolver
+    cfg = configs.refex_cpml(2400)
+    db = pml.setup(meshgen.build_database(cfg), cfg, nel=cfg["pml_elements"], f0=cfg["pml_f0"])
+    g = GPUSolver(db, cfg)
+    if per_call:
+        g.run_per_call(cfg["nstep"])
+    else:
+        g.run(cfg["nstep"], steps_per_graph=100)
+    seis = g.seismograms()
+    g.close()
+    ref = np.load(os.path.join(os.path.dirname(__file__), "golden", "refex_cpml5sides.npz"))["displ"]
+    errs = [rel_l2(seis[r, c], ref[r, c]) for r in range(4) for c in range(3)]
+    print(f"C-PML example: all traces {rel_l2(seis, ref):.2e}, worst trace {max(errs):.2e}")
+    assert rel_l2(seis, ref) < 2e-5
+    for r in range(4):
+        for c in range(3):
+            assert rel_l2(seis[r, c], ref[r, c]) < 1e-4, (r, c)
+            assert np.corrcoef(seis[r, c], ref[r, c])[0, 1] > 0.99999
 
 
 def test_pml_rejects_unsupported_meshes(gpulib):
