@@ -39,6 +39,20 @@ def test_adjoint_sources_match_oracle(gpulib, kind, component):
         assert not adj[:, ~keep].any()
 
 
+@pytest.mark.parametrize("case", ["P", "PSSP", "S", "SS"])
+def test_traveltime_adjoint_sources_match_reference_golden(gpulib, case):
+    """The reference's traveltime adjoint sources of the Liu & Tromp (2006) study
+    (REF_ADJ_SRC, tests/golden/liutromp2006_adjsrc.npz) from its REF_SEIS traces, on
+    the device: to the 7 significant digits the files carry."""
+    from test_postprocess_oracle import liutromp_case
+    from specfem3d_gb300 import postprocess as P
+    syn, dt, t0, ts, te, comp, ref = liutromp_case(case)
+    adj, norms = P.adjoint_sources("traveltime", syn, None, dt, t0, ts, te, component=comp)
+    a = adj[0, comp - 1]
+    assert np.linalg.norm(a - ref) / np.linalg.norm(ref) < 1e-6
+    assert norms[0, comp - 1] > 0
+
+
 def test_adjoint_sources_reject_bad_windows(gpulib):
     from specfem3d_gb300 import abi, postprocess as P
     syn, dat = _traces(nrec=2, nstep=100)
