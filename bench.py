@@ -333,6 +333,42 @@ def coupled_leg(steps: int):
             "workload": "coupled fluid/solid 96x96x48 hexes, 20x20x10 km"}
 
 
+def pml_leg(steps: int):
+    """The reference's C-PML example (36x36x16 block, layers of three elements on five
+    faces: 9036 of 20736 elements) through graph-captured device steps, against the
+    same block with Stacey faces instead; device time of sf3d_iterate_time, and the
+    per-step seismogram error against the reference's REF_SEIS over the full record
+    (tests/golden/refex_cpml5sides.npz, 2400 steps)."""
+    from specfem3d_gb300 import configs, meshgen, pml
+    from specfem3d_gb300.solver import GPUSolver
+    out = {"unit": UNIT, "steps": steps}
+    cfg = configs.refex_cpml(nstep=2400)
+    db = pml.setup(meshgen.build_database(cfg), cfg, nel=cfg["pml_elements"], f0=cfg["pml_f0"])
+    g = GPUSolver(db, cfg)
+    g.run(2400, steps_per_graph=100)
+    seis = g.seismograms()
+    g.close()
+    ref = np.load(os.path.join(ROOT, "tests", "golden", "refex_cpml5sides.npz"))["displ"]
+    out["rel_l2_vs_ref_seis"] = float(np.linalg.norm(seis.astype(np.float64) - ref) / np.linalg.norm(ref))
+    for name in ("cpml", "stacey"):
+        c = configs.refex_cpml(nstep=steps + 10)
+        d = meshgen.build_database(c)
+        if name == "cpml":
+            d = pml.setup(d, c, nel=c["pml_elements"], f0=c["pml_f0"])
+        g = GPUSolver(d, c)
+        g.run(5, steps_per_graph=0)
+        g.run(steps, steps_per_graph=50)
+        t = g.last_timing()
+        g.close()
+        out[name + "_ms_per_step"] = t["total_ms"] / steps
+        out[name + "_value"] = float(d["nglob"]) * steps / (t["total_ms"] / 1000.0)
+    out["cpml_over_stacey"] = out["cpml_ms_per_step"] / out["stacey_ms_per_step"]
+    out["nspec"], out["cpml_elements"] = int(db["nspec"]), int(np.count_nonzero(db["cpml_regions"]))
+    out["workload"] = ("CPML_examples/homogeneous_halfspace_HEX8_elastic_absorbing_CPML_5sides: 36x36x16 hexes, "
+                       "134x134x60 km, point force, dt 0.11 s")
+    return out
+
+
 def aniso_leg(db: dict, cfg: dict, steps: int):
     """Stiffness launch time of the main workload with ANISOTROPY on (tilted TI per
     layer: 21 c_ij per GLL point on top of the attenuation arrays), CUDA events
@@ -392,18 +428,25 @@ def smooth_leg(nx: int = 64, sigma: float = 312.5):
             "finite": bool(np.isfinite(out).all())}
 
 
+REFERENCE_MAX_STEPS = 40
+
+
 def run_reference(args, rank):
     if rank != 0:
         return 0
     nthreads = os.cpu_count() or 1
-    steps = max(1, args.steps)
-    val, info = cpu_baseline(steps, nthreads, warmup=max(1, args.warmup))
+    # about 1.3 s per step of the full mesh on 16 cores: at most 40 timed steps keep
+    # the arm within about a minute and a half whatever --steps asks
+    steps = max(1, min(args.steps, REFERENCE_MAX_STEPS))
+    warm = max(1, min(args.warmup, 3))
+    val, info = cpu_baseline(steps, nthreads, warmup=warm)
     sample = (f"CPU oracle (C restatement of the reference CPU solver, not the reference binary; FP32, OpenMP "
               f"over {nthreads} threads) on the full bench mesh ({info['nspec']} elements, {info['nglob']} points), "
-              f"{steps} steps after {max(1, args.warmup)} warm-up steps; the reference's Fortran solver cannot be "
-              f"built (no Fortran compiler or MPI)")
+              f"{steps} timed steps (of the {args.steps} requested) after {warm} warm-up steps; the reference's "
+              f"Fortran solver cannot be built (no Fortran compiler or MPI)")
     line = {"metric": METRIC, "value": val, "unit": UNIT, "n_gpus": args.gpus, "steps": steps,
-            "warmup": args.warmup, "ms_per_step": 1000 * info["seconds"] / steps, "higher_is_better": True,
+            "warmup": warm, "steps_requested": args.steps, "ms_per_step": 1000 * info["seconds"] / steps,
+            "higher_is_better": True,
             "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
             "config": {"workload": WORKLOAD, "nspec": info["nspec"], "nglob": info["nglob"]},
             "impl": "reference",
@@ -444,10 +487,11 @@ def main():
     ap.add_argument("--adjoint-steps", type=int, default=3000, help="time steps of the gradient workload")
     ap.add_argument("--roofline-steps", type=int, default=20,
                     help="steps whose stiffness launches are bracketed by CUDA events")
-    ap.add_argument("--legs", default="main,batch,coupled,adjoint,l2",
+    ap.add_argument("--pml-steps", type=int, default=200, help="timed steps of the C-PML example (0: skip)")
+    ap.add_argument("--legs", default="main,batch,coupled,adjoint,l2,pml",
                     help="comma list of the parts to run: main (the headline workload and its e2e, roofline, "
-                         "geometry, CPU-oracle lines), batch, coupled, adjoint, l2; without main one JSON line "
-                         "holds the selected legs only (profiling)")
+                         "geometry, CPU-oracle lines), batch, coupled, adjoint, l2, pml; without main one JSON "
+                         "line holds the selected legs only (profiling)")
     args = ap.parse_args()
     legs = set(x.strip() for x in args.legs.split(",") if x.strip())
     if "batch" not in legs:
@@ -458,6 +502,8 @@ def main():
         args.adjoint = 0
     if "l2" not in legs:
         args.l2_steps = 0
+    if "pml" not in legs:
+        args.pml_steps = 0
     rank = int(os.environ.get("RANK", "0"))
     world = int(os.environ.get("WORLD_SIZE", "1"))
     if args.impl == "reference":
@@ -477,6 +523,8 @@ def main():
             out["adjoint"] = adjoint_leg(args.adjoint, args.adjoint_steps)
         if args.l2_steps > 0:
             out["l2_error"] = l2_error_leg(args.l2_steps)
+        if args.pml_steps > 0:
+            out["pml"] = pml_leg(args.pml_steps)
         if rank == 0:
             print(json.dumps(out), flush=True)
         return 0
@@ -652,6 +700,8 @@ def main():
         line["smoothing"] = smooth_leg(args.smooth_nx)
     if args.l2_steps > 0:
         line["l2_error"] = l2_error_leg(args.l2_steps)
+    if args.pml_steps > 0:
+        line["pml"] = pml_leg(args.pml_steps)
     if cpu is not None:
         cv, info = cpu
         line["cpu_baseline"] = {"value": cv, "unit": UNIT, "cores": os.cpu_count() or 1, "kind": "port",

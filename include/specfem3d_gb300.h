@@ -642,8 +642,38 @@ int sf3d_set_acoustic_kernel_pairing(long *Mesh_pointer, int discrete);
 /* FP64 acoustic accumulators, (5,5,5,NSPEC) each (library extension). */
 int sf3d_get_kernels_ac_f64(long *Mesh_pointer, double *h_rho_ac_kl, double *h_kappa_ac_kl);
 
+/* ------------------------------------------------------------------------
+ * C-PML absorbing layers of elastic elements (forward runs).
+ * prepare_fields_elastic_pml (prepare_mesh_constants_cuda.cu:1176; called from
+ * prepare_gpu.f90:191): the CPML element lists (1-based CPML_to_spec /
+ * spec_to_CPML, is_CPML per element) and the recursive-convolution coefficients
+ * of pml_compute_memory_variables.f90 per CPML element and point
+ * (coef_alpha / _beta (9, NGLL3, NSPEC_CPML), coef_abar (5, ...),
+ * coef_strain (18, ...)); rhostore and wgll_cube for the PML mass terms.  The
+ * CPML elements' stiffness, memory variables and acceleration contribution
+ * (pml_compute_accel_contribution.f90, compute_forces_viscoelastic_PML) then
+ * run inside compute_forces_viscoelastic_cuda and sf3d_iterate_time, the
+ * PML_displ_old/_new stores around the predictor inside
+ * update_displacement_cuda.  Rejected with SF3D_ERR_UNSUPPORTED: attenuation,
+ * anisotropy, mesh colouring, SIMULATION_TYPE = 3.
+ * pml_impose_boundary_condition_elastic_cuda (pml_compute_accel_cuda.cu:245,
+ * called from pml_compute_accel_contribution.f90:695): displ, veloc and accel
+ * set to zero on the outer faces of the layers (the absorbing face lists of
+ * prepare_constants_device).
+ * transfer_pml_displ_from_device / _to_device (transfer_fields_cuda.cu:292,307):
+ * PML_displ_old / _new (3, NGLL3, NSPEC_CPML). */
+void pml_impose_boundary_condition_elastic_cuda_(long *Mesh_pointer);
+void prepare_fields_elastic_pml_(long *Mesh_pointer, int *NSPEC_CPML, int *is_CPML, int *CPML_to_spec,
+                                 int *spec_to_CPML, realw *pml_convolution_coef_alpha,
+                                 realw *pml_convolution_coef_beta, realw *pml_convolution_coef_abar,
+                                 realw *pml_convolution_coef_strain, realw *h_wgll_cube, realw *rhostore);
+void transfer_pml_displ_from_device_(int *size, realw *PML_displ_old, realw *PML_displ_new,
+                                     long *Mesh_pointer);
+void transfer_pml_displ_to_device_(int *size, realw *PML_displ_old, realw *PML_displ_new,
+                                   long *Mesh_pointer);
+
 /* Not provided: each records SF3D_ERR_UNSUPPORTED through sf3d_last_error (noise
- * tomography, C-PML, gravity, ocean load, faults);
+ * tomography, gravity, ocean load, faults);
  * prepare_fields_gravity_device with GRAVITY = 0 and prepare_fault_device without
  * Kelvin-Voigt damping are accepted no-ops. */
 void add_source_main_rec_noise_cu_(long *Mesh_pointer, int *it_f, int *irec_main_noise_f,
@@ -657,12 +687,7 @@ void initialize_fault_solver_gpu_(long *Fault_solver, int *num_of_faults, realw 
                                   int *RATE_AND_STATE);
 void noise_read_add_surface_movie_cu_(long *Mesh_pointer, realw *h_noise_surface_movie,
                                       int *NOISE_TOMOGRAPHYf);
-void pml_impose_boundary_condition_elastic_cuda_(long *Mesh_pointer);
 void prepare_fault_device_(long *Mesh_pointer, int *KELVIN_VOIGT_DAMPING, realw *Kelvin_Voigt_eta);
-void prepare_fields_elastic_pml_(long *Mesh_pointer, int *NSPEC_CPML, int *is_CPML, int *CPML_to_spec,
-                                 int *spec_to_CPML, realw *pml_convolution_coef_alpha,
-                                 realw *pml_convolution_coef_beta, realw *pml_convolution_coef_abar,
-                                 realw *pml_convolution_coef_strain, realw *h_wgll_cube, realw *rhostore);
 void prepare_fields_gravity_device_(long *Mesh_pointer, int *GRAVITY, realw *minus_deriv_gravity,
                                     realw *minus_g, realw *h_wgll_cube, realw *rhostore);
 void prepare_fields_noise_device_(long *Mesh_pointer, int *NSPEC_AB, int *NGLOB_AB, int *free_surface_ispec,
@@ -678,10 +703,6 @@ void transfer_fault_data_to_device_(long *Fault_pointer, int *fault_index, int *
 void transfer_fault_data_to_host_(long *Fault_pointer, int *fault_index, int *NSPEC_FLT, int *NGLOB_FLT,
                                   realw *D, realw *V, realw *T);
 void transfer_kernels_noise_to_host_(long *Mesh_pointer, realw *h_sigma_kl, int *NSPEC_AB);
-void transfer_pml_displ_from_device_(int *size, realw *PML_displ_old, realw *PML_displ_new,
-                                     long *Mesh_pointer);
-void transfer_pml_displ_to_device_(int *size, realw *PML_displ_old, realw *PML_displ_new,
-                                   long *Mesh_pointer);
 void transfer_rsf_data_todevice_(long *Fault_pointer, int *fault_index, int *NGLOB_FLT, realw *Fload,
                                  realw *V0, realw *f0, realw *V_init, realw *a, realw *b, realw *L,
                                  realw *theta, realw *T, realw *C, realw *fw, realw *Vw, int *StateLaw);
