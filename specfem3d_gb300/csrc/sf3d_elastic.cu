@@ -21,12 +21,6 @@ namespace sf3d {
 
 namespace {
 
-__device__ __forceinline__ void cp_async4(void* smem, const void* gmem) {
-  asm volatile("cp.async.ca.shared.global [%0], [%1], 4;" ::"r"(static_cast<unsigned>(__cvta_generic_to_shared(smem))),
-               "l"(gmem)
-               : "memory");
-}
-
 // STAGE (attenuation only): the 30 memory-variable / strain / factor values of
 // each point (15 KB per element) are copied into shared memory with cp.async
 // instead of being held in registers from the start of the kernel to the end,

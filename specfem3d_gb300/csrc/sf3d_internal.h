@@ -81,6 +81,14 @@ __device__ __forceinline__ float pool_value(const void* pool, long i) {
   return __ldg(static_cast<const float*>(pool) + i);
 }
 
+// 4-byte asynchronous global -> shared copy (cp.async; completes at
+// cp.async.wait_all of the issuing thread)
+__device__ __forceinline__ void cp_async4(void* smem, const void* gmem) {
+  asm volatile("cp.async.ca.shared.global [%0], [%1], 4;" ::"r"(static_cast<unsigned>(__cvta_generic_to_shared(smem))),
+               "l"(gmem)
+               : "memory");
+}
+
 // value of stream q at point t of the element whose record is pk (vary, base: its
 // varying-stream mask and first payload row, read once per element)
 template <int GEOM>
