@@ -293,6 +293,17 @@ def batch_leg(nshots: int, steps: int, nx: int = 64):
     static32 = 1500.0 * nspec
     static16 = (500.0 + 160.0) * nspec + rows * 250.0
     dyn = (84.0 * nshots + 12.0) * nglob
+    # FP32-SIMT ceiling of the batched stiffness: the minimal FMA count of the
+    # element algorithm, 663 flop per unique GLL point and shot, over the chosen
+    # tiling's pass time from the autotuner
+    key = (f"pencil{tune['shots_per_block']}" if tune["kernel"] == "pencil" else
+           f"{tune['shots_per_thread']}x{tune['shots_per_block']}x{tune['elements_per_block']}")
+    st_ms = tune["ms"].get(key)
+    simt = None
+    if st_ms:
+        tflops = 663.0 * nglob * nshots / (st_ms / 1000.0) / 1e12
+        simt = {"flop_per_pt": 663, "stiffness_ms": st_ms, "achieved_tflops": tflops, "peak_tflops": SIMT_TFLOPS,
+                "peak_kind": "nominal: 152 SMs x 128 FP32 lanes x 2 flop x 2.07 GHz", "frac": tflops / SIMT_TFLOPS}
     return {"unit": "GLL-pt updates/s summed over shots", "shots": nshots, "steps": steps, "nglob": nglob,
             "nspec": nspec, "batched": rate_b, "batched_fp16_moduli": rate_h, "plain_single_shot": rate_p,
             "speedup_per_shot": rate_b / rate_p, "speedup_per_shot_fp16_moduli": rate_h / rate_p,
@@ -302,7 +313,7 @@ def batch_leg(nshots: int, steps: int, nx: int = 64):
             "ms_per_step_two_halves": None if ms_two is None else ms_two / steps,
             "step_hbm_frac": (dyn + static32) / (ms_b / steps / 1000.0) / 1e9 / peak,
             "step_hbm_frac_fp16_moduli": (dyn + static16) / (ms_h / steps / 1000.0) / 1e9 / peak,
-            "peak_gbs": peak, "peak_kind": kind,
+            "peak_gbs": peak, "peak_kind": kind, "fp32_simt": simt,
             "workload": f"{nx}x{nx}x{nx // 2} hexes, 20x20x10 km, +-5% perturbed model, no attenuation, "
                         f"{nshots} CMT shots, Ricker 2 Hz"}
 
@@ -429,6 +440,7 @@ def smooth_leg(nx: int = 64, sigma: float = 312.5):
 
 
 REFERENCE_MAX_STEPS = 40
+SIMT_TFLOPS = 152 * 128 * 2 * 2.07e9 / 1e12
 
 
 def run_reference(args, rank):
