@@ -352,6 +352,9 @@ __global__ void batch_set_it_kernel(int* d_it, int v) {
 
 bool alloc_f(float** d, size_t n) { return alloc_zero((void**)d, sizeof(float) * n); }
 
+// the pencil kernel indexes the stacked fields with 32-bit unsigned offsets
+bool pencil_fits_index32(const Mesh* mp, long nshots) { return 3.0 * (double)mp->nglob * nshots < 4294967296.0; }
+
 // Four shots per thread: thread = (GLL point p, shot group gi of 4 consecutive
 // shots), gi fastest.  The four shots of a point are one 16-byte vector in the
 // stacked fields, in shared memory (float4 rows) and in the scatter
@@ -908,7 +911,7 @@ int sf3d_batch_prepare(long* Mesh_pointer, int nshots, const int* ispec_selected
   B->nlength = nlength;
   B->shots_per_block = nshots % 8 == 0 ? 8 : (nshots % 4 == 0 ? 4 : (nshots % 2 == 0 ? 2 : 1));
   B->shots_per_thread = nshots % 4 == 0 ? 4 : 1;
-  B->pencil_lanes = nshots % 16 == 0 ? 16 : (nshots % 8 == 0 ? 8 : 0);
+  B->pencil_lanes = !pencil_fits_index32(mp, nshots) ? 0 : (nshots % 16 == 0 ? 16 : (nshots % 8 == 0 ? 8 : 0));
   const size_t n = 3ull * mp->nglob * nshots;
   std::vector<float> sa((size_t)nshots * NGLL3_PAD * 3, 0.f), tab((size_t)nstep * nshots);
   for (int s = 0; s < nshots; ++s)
@@ -948,6 +951,11 @@ int sf3d_batch_set_tiling(long* Mesh_pointer, int shots_per_block, int elements_
     if ((sb != 8 && sb != 16 && sb != 32) || mp->batch->nshots % sb != 0 || eb != 1) {
       set_error(SF3D_ERR_ARG, "sf3d_batch_set_tiling: the pencil kernel takes 8, 16 or 32 shots per CTA "
                               "dividing nshots and one element per CTA");
+      return SF3D_ERR_ARG;
+    }
+    if (!pencil_fits_index32(mp, mp->batch->nshots)) {
+      set_error(SF3D_ERR_ARG, "sf3d_batch_set_tiling: the pencil kernel indexes the stacked fields in 32 bits "
+                              "(3 nglob nshots < 2^32); use a per-point tiling");
       return SF3D_ERR_ARG;
     }
     mp->batch->pencil_lanes = sb;
@@ -1039,7 +1047,7 @@ int sf3d_batch_autotune(long* Mesh_pointer, int reps, float* ms_table, int* best
   int blanes = 0;
   for (int q = 0; q < 3; ++q) {
     if (ms_table) ms_table[24 + q] = -1.f;
-    if (B->nshots % lanes[q] != 0) continue;
+    if (B->nshots % lanes[q] != 0 || !pencil_fits_index32(mp, B->nshots)) continue;
     B->pencil_lanes = lanes[q];
     float ms = 0.f;
     if (!time_it(&ms)) return SF3D_ERR_CUDA;

@@ -56,8 +56,10 @@ __global__ void __launch_bounds__(kPencils * W, MINB) batch_pencil_kernel(const 
   const int pa = pc % NGLLX, pb = pc / NGLLX;
   const int tile = blockIdx.x % a.shot_tiles;
   const int slot = blockIdx.x / a.shot_tiles;
-  const long S = a.nshots;
-  const long shot = a.shot_offset + (long)tile * W + w;
+  // stacked-field indices in 32 bits: the host allows this kernel only while
+  // 3 nglob nshots < 2^32 (pencil_fits_index32)
+  const unsigned S = a.nshots;
+  const unsigned shot = a.shot_offset + tile * W + w;
   const int e = a.phase ? __ldg(a.phase + slot) : slot;
   const int ir = __ldg(a.irregular + e);
   const long eb = (long)e * NGLL3_PAD;
@@ -71,9 +73,9 @@ __global__ void __launch_bounds__(kPencils * W, MINB) batch_pencil_kernel(const 
   float u[3][NGLLX];
 #pragma unroll
   for (int l = 0; l < NGLLX; ++l) {
-    const long g = __ldg(a.ibool + eb + xb + l);
+    const unsigned gb = 3u * (unsigned)__ldg(a.ibool + eb + xb + l) * S + shot;
 #pragma unroll
-    for (int c = 0; c < 3; ++c) u[c][l] = a.displ[(3 * g + c) * S + shot];
+    for (int c = 0; c < 3; ++c) u[c][l] = a.displ[gb + c * S];
   }
   __syncthreads();  // s_gll
   const float* hp = a.hp;                   // hprime(i2,i1) = hp[i2 + 5 i1], parameter bank
@@ -237,14 +239,14 @@ __global__ void __launch_bounds__(kPencils * W, MINB) batch_pencil_kernel(const 
     for (int o = 0; o < NGLLX; ++o) {
       const int p = zb + NGLL2 * o;
       const float fac2 = s_gll[3 * NGLL2 + pa + NGLLX * o];  // wgllwgll_xz(i, k)
-      const long g = __ldg(a.ibool + eb + p);
+      const unsigned gb = 3u * (unsigned)__ldg(a.ibool + eb + p) * S + shot;
 #pragma unroll
       for (int c = 0; c < 3; ++c) {
         float n = 0.f;
 #pragma unroll
         for (int l = 0; l < NGLLX; ++l) n = fmaf(fz[c][l], hpw[l + NGLLX * o], n);
         const float r = fmaf(fac2, ROW(3 + c, p), ROW(c, p));
-        atomicAdd(a.accel + (3 * g + c) * S + shot, -(r + fac3 * n));
+        atomicAdd(a.accel + gb + c * S, -(r + fac3 * n));
       }
     }
   }
