@@ -439,7 +439,21 @@ def smooth_leg(nx: int = 64, sigma: float = 312.5):
             "finite": bool(np.isfinite(out).all())}
 
 
+def stiffness_variant_name(v: int) -> str:
+    """The kernel build a stiffness variant number selects (sf3d_set_stiffness_variant)."""
+    if v == 1:
+        return "stiffness_pipe_kernel<att>"
+    ctas = [4, 0, 5, 6, 7, 6, 7, 8, 6, 7, 3, 4, 6, 7, 8][v]
+    kind = ("cp.async-staged memory variables" if 5 <= v <= 7 else
+            "evict-first element streams" if v in (8, 9) else
+            "3 threads per point" if v in (10, 11) else
+            "bulk-copy-staged memory variables" if v >= 12 else "")
+    name = "stiffness_split_kernel" if v in (10, 11) else "stiffness_kernel"
+    return f"{name}<att, {ctas} CTAs/SM" + (f", {kind}>" if kind else ">")
+
+
 REFERENCE_MAX_STEPS = 40
+STIFFNESS_VARIANTS = 15          # sf3d_autotune_stiffness writes one time per variant
 SIMT_TFLOPS = 152 * 128 * 2 * 2.07e9 / 1e12
 
 
@@ -569,7 +583,7 @@ def main():
         autotune = None
     else:
         # fields are at rest: time every stiffness variant and keep the fastest
-        ms = (ctypes.c_float * 12)()
+        ms = (ctypes.c_float * STIFFNESS_VARIANTS)()
         best = ctypes.c_int()
         if L.sf3d_autotune_stiffness(g.mp, 3, ms, ctypes.addressof(best)) != 0:
             abi.check()
@@ -580,7 +594,7 @@ def main():
     geom_variant = {}
     for fmt in ("fp16", "bf16", "packed-fp32"):
         g.set_geometry_format(fmt)
-        msf = (ctypes.c_float * 12)()
+        msf = (ctypes.c_float * STIFFNESS_VARIANTS)()
         bestf = ctypes.c_int()
         if L.sf3d_autotune_stiffness(g.mp, 3, msf, ctypes.addressof(bestf)) != 0:
             abi.check()
@@ -679,12 +693,7 @@ def main():
                      "traffic_kind": "constant from a committed ncu profile, not measured in this run",
                      "traffic_note": ("ncu dram__bytes_read.sum + dram__bytes_write.sum of one stiffness launch "
                                       "of this mesh, read from profiles/stiffness_kernel_att_traffic_layered_128x128x64.md"),
-                     "kernel": ("stiffness_pipe_kernel<att>" if args.variant == 1 else
-                                f"stiffness_{'split_' if args.variant >= 10 else ''}kernel<att, "
-                                f"{[4, 0, 5, 6, 7, 6, 7, 8, 6, 7, 3, 4][args.variant]} CTAs/SM"
-                                + (", cp.async-staged memory variables>" if 5 <= args.variant <= 7 else
-                                   ", evict-first element streams>" if args.variant in (8, 9) else
-                                   ", 3 threads per point>" if args.variant >= 10 else ">")),
+                     "kernel": stiffness_variant_name(args.variant),
                      "autotune": autotune,
                      "algorithmic_bytes_per_launch": bytes_launch,
                      "mean_launch_ms": stiff_ms, "timed_launches": tk["stiffness_launches"]},

@@ -356,7 +356,11 @@ int sf3d_last_timing(long *Mesh_pointer, float *stiffness_ms, int *stiffness_lau
  *   8, 9:       one CTA per element, evict-first cache hints on the element
  *               streams (read and written once per launch), 6 and 7 CTAs/SM;
  *   10, 11:     three threads per GLL point (one per displacement component),
- *               384-thread CTAs, 3 and 4 CTAs/SM.
+ *               384-thread CTAs, 3 and 4 CTAs/SM;
+ *   12, 13, 14: one CTA per element with the memory variables, strains and
+ *               attenuation factors brought into shared memory by 14 bulk
+ *               copies (one thread, one mbarrier with a bounded wait), for 6,
+ *               7, 8 CTAs per SM (register budget 80, 72, 64).
  * Under a packed geometry format (sf3d_set_geometry_format) the variant picks
  * the packed build: 4 at 7 CTAs/SM; 5, 6, 7 with the memory variables and
  * strains staged by cp.async and the factors read from the element record, at
@@ -390,7 +394,7 @@ int sf3d_geometry_pack_info(long *Mesh_pointer, long *payload_rows, long *device
 /* Time every stiffness variant over `reps` full passes and keep the fastest.
  * Must run on a wavefield at rest (after prepare_fields_elastic_device, before
  * the first step): zero fields make the passes leave every array unchanged;
- * returns SF3D_ERR_STATE otherwise.  ms_per_variant (12 floats) and
+ * returns SF3D_ERR_STATE otherwise.  ms_per_variant (15 floats) and
  * best_variant may be NULL.  No reference counterpart. */
 int sf3d_autotune_stiffness(long *Mesh_pointer, int reps, float *ms_per_variant, int *best_variant);
 

@@ -25,6 +25,11 @@ namespace {
 // each point (15 KB per element) are copied into shared memory with cp.async
 // instead of being held in registers from the start of the kernel to the end,
 // so the kernel fits a smaller register budget (more resident CTAs per SM).
+// BULK (with STAGE): thread 0 brings the same rows in with 14 bulk copies
+// (cp.async.bulk, contiguous per component: R[c] 1536 B, epsilondev 512 B,
+// factors 1536 B) completing on one mbarrier, so no thread spends an
+// instruction or a register per row; every thread waits (bounded) on the
+// mbarrier after the first barrier, where its initialisation is visible.
 // Element streams are read and written exactly once per launch: with STREAM
 // they carry evict-first hints (ld.global.cs / st.global.cs) so that L2 keeps
 // the gathered displacement / velocity and the scattered acceleration, which
@@ -53,9 +58,11 @@ __device__ __forceinline__ void st_state(float* p, float v) {
 // per-element records and payload rows of a.pack / a.pool instead (metric,
 // kappa, mu and, with attenuation, factor_common(_kappa)).
 template <bool ATT, bool STRAIN, int MINB, int GEOM = kGeomFP32, bool STAGE = false, bool ATOMIC = true,
-          bool STREAM = false, bool ANISO = false>
+          bool STREAM = false, bool ANISO = false, bool BULK = false>
 __global__ void __launch_bounds__(NGLL3_PAD, MINB) stiffness_kernel(const StiffnessArgs a) {
   __shared__ __align__(16) float s_att[(ATT && STAGE) ? (GEOM == kGeomFP32 ? 30 : 24) : 1][NGLL3_PAD];
+  __shared__ uint64_t s_bar;
+  bool bulk_failed = false;
   __shared__ float s_gll[NGLL3];
   __shared__ float s_u[3][NGLL3_PAD];
   __shared__ float s_v[ATT ? 3 : 1][NGLL3_PAD];
@@ -84,7 +91,23 @@ __global__ void __launch_bounds__(NGLL3_PAD, MINB) stiffness_kernel(const Stiffn
   }
 #pragma unroll
   for (int s = 0; s < NSLS; ++s) fc[s] = fck[s] = 0.f;
-  if (ATT && STAGE && active) {
+  if (ATT && STAGE && BULK) {
+    if (t == 0) {
+      constexpr int kRows = GEOM == kGeomFP32 ? 30 : 24;
+      const long se0 = (long)e * (NSLS * NGLL3_PAD), ee0 = (long)e * NGLL3_PAD;
+      mbar_init(&s_bar, 1);
+      asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+      mbar_arrive_expect_tx(&s_bar, (uint32_t)(kRows * NGLL3_PAD * sizeof(float)));
+#pragma unroll
+      for (int c = 0; c < 6; ++c) bulk_g2s(&s_att[3 * c][0], a.R[c] + se0, NSLS * NGLL3_PAD * sizeof(float), &s_bar);
+#pragma unroll
+      for (int c = 0; c < 6; ++c) bulk_g2s(&s_att[18 + c][0], a.eps[c] + ee0, NGLL3_PAD * sizeof(float), &s_bar);
+      if (GEOM == kGeomFP32) {
+        bulk_g2s(&s_att[24][0], a.fc + se0, NSLS * NGLL3_PAD * sizeof(float), &s_bar);
+        bulk_g2s(&s_att[27][0], a.fck + se0, NSLS * NGLL3_PAD * sizeof(float), &s_bar);
+      }
+    }
+  } else if (ATT && STAGE && active) {
     // rows: R[c][s] -> 3c+s (0..17), epsilondev[c] -> 18+c, factor_common[s] -> 24+s,
     // factor_common_kappa[s] -> 27+s (FP32 geometry only: the packed formats read
     // the factors from the element record where they are used).  Each thread copies
@@ -267,7 +290,11 @@ __global__ void __launch_bounds__(NGLL3_PAD, MINB) stiffness_kernel(const Stiffn
       sig_xz = mu * (dzx + dxz);
       sig_yz = mu * (dzy + dyz);
     }
-    if (ATT && STAGE) asm volatile("cp.async.wait_all;" ::: "memory");
+    if (ATT && STAGE && !BULK) asm volatile("cp.async.wait_all;" ::: "memory");
+    if (ATT && STAGE && BULK && !mbar_wait_bounded(&s_bar, 0)) {
+      bulk_failed = true;  // the results of this element are not valid; the host is told
+      if (a.err) atomicExch(a.err, 1);
+    }
     if (ATT) {
       float sR[6];
 #pragma unroll
@@ -373,13 +400,16 @@ __global__ void __launch_bounds__(NGLL3_PAD, MINB) stiffness_kernel(const Stiffn
         if (a.eps[c]) st_state<STREAM>(a.eps[c] + eo, epsl[c]);
     }
   }
+  // a bulk copy still in flight must land before the CTA's shared memory is
+  // released: wait once more, with the same bound
+  if (ATT && STAGE && BULK && bulk_failed) mbar_wait_bounded(&s_bar, 0);
 }
 
-template <int MINB, int GEOM, bool STAGE = false, bool STREAM = false>
+template <int MINB, int GEOM, bool STAGE = false, bool STREAM = false, bool BULK = false>
 void launch_minb(const StiffnessArgs& a, bool att, bool store_strain, cudaStream_t s) {
   dim3 grid(a.nelem), block(NGLL3_PAD);
   if (att)
-    stiffness_kernel<true, true, MINB, GEOM, STAGE, true, STREAM><<<grid, block, 0, s>>>(a);
+    stiffness_kernel<true, true, MINB, GEOM, STAGE, true, STREAM, false, BULK><<<grid, block, 0, s>>>(a);
   else if (store_strain)
     stiffness_kernel<false, true, MINB, GEOM, false, true, STREAM><<<grid, block, 0, s>>>(a);
   else
@@ -404,8 +434,17 @@ void launch_packed(const StiffnessArgs& a, bool att, bool store_strain, cudaStre
 // geometry builds exist for 6 and 7 CTAs/SM, and with cp.async-staged memory
 // variables for 8, 9 and 10.
 void launch_stiffness(const StiffnessArgs& a, bool att, bool store_strain, cudaStream_t s, int blocks_per_sm,
-                      int geom_format, bool staged, bool streaming) {
+                      int geom_format, bool staged, bool streaming, bool bulk) {
   if (a.nelem <= 0) return;
+  if (bulk && geom_format == kGeomFP32) {
+    if (blocks_per_sm == 8)
+      launch_minb<8, kGeomFP32, true, false, true>(a, att, store_strain, s);
+    else if (blocks_per_sm == 7)
+      launch_minb<7, kGeomFP32, true, false, true>(a, att, store_strain, s);
+    else
+      launch_minb<6, kGeomFP32, true, false, true>(a, att, store_strain, s);
+    return;
+  }
   if (geom_format != kGeomFP32 && staged) {
     // staged memory variables and record-resident constants leave 48-64
     // registers a thread (no spills): 8, 9 or 10 CTAs/SM of 20.5 KB shared memory

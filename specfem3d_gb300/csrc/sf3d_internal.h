@@ -81,6 +81,60 @@ __device__ __forceinline__ float pool_value(const void* pool, long i) {
   return __ldg(static_cast<const float*>(pool) + i);
 }
 
+// mbarrier and bulk-copy (TMA, non-tensor) helpers.  Every wait is bounded:
+// mbar_wait_bounded gives up after ~2 s of %globaltimer and returns false, and
+// the caller records an error word instead of spinning on.
+__device__ __forceinline__ uint32_t smem_addr(const void* p) {
+  return static_cast<uint32_t>(__cvta_generic_to_shared(p));
+}
+
+__device__ __forceinline__ void mbar_init(uint64_t* bar, uint32_t count) {
+  asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(smem_addr(bar)), "r"(count) : "memory");
+}
+
+__device__ __forceinline__ void mbar_arrive_expect_tx(uint64_t* bar, uint32_t bytes) {
+  asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(smem_addr(bar)), "r"(bytes)
+               : "memory");
+}
+
+__device__ __forceinline__ bool mbar_try_wait(uint64_t* bar, uint32_t parity) {
+  uint32_t ok;
+  asm volatile(
+      "{\n\t.reg .pred p;\n\t"
+      "mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n\t"
+      "selp.u32 %0, 1, 0, p;\n\t}"
+      : "=r"(ok)
+      : "r"(smem_addr(bar)), "r"(parity)
+      : "memory");
+  return ok != 0;
+}
+
+__device__ __forceinline__ uint64_t global_ns() {
+  uint64_t t;
+  asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t));
+  return t;
+}
+
+// bounded wait: true when the phase completed, false after ~2 s
+__device__ __forceinline__ bool mbar_wait_bounded(uint64_t* bar, uint32_t parity) {
+  if (mbar_try_wait(bar, parity)) return true;
+  const uint64_t t0 = global_ns();
+  while (true) {
+    if (mbar_try_wait(bar, parity)) return true;
+    if (global_ns() - t0 > 2000000000ull) return false;
+  }
+}
+
+__device__ __forceinline__ void bulk_g2s(void* dst_smem, const void* src_gmem, uint32_t bytes, uint64_t* bar) {
+  asm volatile(
+      "cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];" ::"r"(
+          smem_addr(dst_smem)),
+      "l"(reinterpret_cast<uint64_t>(src_gmem)), "r"(bytes), "r"(smem_addr(bar))
+      : "memory");
+}
+
+__device__ __forceinline__ void fence_proxy_async() { asm volatile("fence.proxy.async.shared::cta;" ::: "memory"); }
+
 // 4-byte asynchronous global -> shared copy (cp.async; completes at
 // cp.async.wait_all of the issuing thread)
 __device__ __forceinline__ void cp_async4(void* smem, const void* gmem) {
@@ -400,13 +454,14 @@ struct StiffnessArgs {
   const ElemPack* pack;         // [nspec]
   const void* pool;             // payload rows
   int nonatomic;                // 1: the elements of this launch share no point (one colour)
+  int* err;                     // kernel error word (a bounded wait that timed out), or nullptr
   // ANISOTROPY: c11 c12 c13 c14 c15 c16 c22 c23 c24 c25 c26 c33 c34 c35 c36 c44
   // c45 c46 c55 c56 c66, each [nspec][128]; nullptr for isotropic meshes
   const float* c[21];
 };
 
 void launch_stiffness(const StiffnessArgs& a, bool att, bool store_strain, cudaStream_t s, int blocks_per_sm,
-                      int geom_format = kGeomFP32, bool staged = false, bool streaming = false);
+                      int geom_format = kGeomFP32, bool staged = false, bool streaming = false, bool bulk = false);
 // batched-shots stiffness with register-blocked pencils (sf3d_batch_pencil.cu):
 // elements of a phase list x shots [shot_offset, shot_offset + shot_tiles * lanes)
 // of fields stacked shot-innermost with nshots shots per point
@@ -441,18 +496,22 @@ void launch_stiffness_pipelined(const StiffnessArgs& a, bool att, bool store_str
 //   0, 2, 3, 4: one CTA per element at 4, 5, 6, 7 CTAs/SM; 1: persistent bulk-copy pipeline;
 //   5, 6, 7: one CTA per element with cp.async-staged memory variables at 6, 7, 8 CTAs/SM;
 //   8, 9: one CTA per element, evict-first hints on the element streams, 6 and 7 CTAs/SM;
-//   10, 11: three threads per point (384-thread CTAs), 3 and 4 CTAs/SM
+//   10, 11: three threads per point (384-thread CTAs), 3 and 4 CTAs/SM;
+//   12, 13, 14: one CTA per element with the memory variables, strains and
+//   attenuation factors brought into shared memory by 14 bulk copies (one
+//   thread, one mbarrier) at 6, 7, 8 CTAs/SM
 // Under a packed geometry format (sf3d_set_geometry_format) 4 selects the packed
 // build at 7 CTAs/SM, 5, 6, 7 the packed builds with staged memory variables at
 // 8, 9, 10 CTAs/SM, and every other variant the packed build at 6.
-constexpr int kNumStiffnessVariants = 12;
+constexpr int kNumStiffnessVariants = 15;
 inline int variant_blocks_per_sm(int v) {
-  const int t[kNumStiffnessVariants] = {4, 0, 5, 6, 7, 6, 7, 8, 6, 7, 3, 4};
+  const int t[kNumStiffnessVariants] = {4, 0, 5, 6, 7, 6, 7, 8, 6, 7, 3, 4, 6, 7, 8};
   return (v >= 0 && v < kNumStiffnessVariants) ? t[v] : 4;
 }
 inline bool variant_staged(int v) { return v >= 5 && v <= 7; }
+inline bool variant_bulk(int v) { return v >= 12 && v <= 14; }
 inline bool variant_streaming(int v) { return v == 8 || v == 9; }
-inline bool variant_split(int v) { return v >= 10; }
+inline bool variant_split(int v) { return v == 10 || v == 11; }
 void launch_stiffness_split(const StiffnessArgs& a, bool att, bool store_strain, cudaStream_t s, int blocks_per_sm);
 void free_grad(Mesh* mp);
 void free_batch(Mesh* mp);
@@ -523,7 +582,8 @@ inline void run_stiffness(Mesh* mp, const StiffnessArgs& a, bool att, bool store
     launch_stiffness_split(a, att, store_strain, s, variant_blocks_per_sm(mp->stiffness_variant));
   } else {
     launch_stiffness(a, att, store_strain, s, variant_blocks_per_sm(mp->stiffness_variant), false,
-                     variant_staged(mp->stiffness_variant), variant_streaming(mp->stiffness_variant));
+                     variant_staged(mp->stiffness_variant), variant_streaming(mp->stiffness_variant),
+                     variant_bulk(mp->stiffness_variant));
   }
 }
 void launch_pressure_seismograms(Mesh* mp, int slot);

@@ -328,6 +328,7 @@ StiffnessArgs stiffness_args(Mesh* mp, Fields& F, int iphase, float deltat, bool
   a.eps_trace_over_3 = (mp->simulation_type == 3) ? F.eps_trace_over_3 : nullptr;
   a.fc = mp->d_factor_common;
   a.fck = mp->d_factor_common_kappa;
+  a.err = mp->d_kerr;
   for (int s = 0; s < NSLS; ++s) {
     a.alpha[s] = backward ? mp->b_alphaval[s] : mp->alphaval[s];
     a.beta[s] = backward ? mp->b_betaval[s] : mp->betaval[s];

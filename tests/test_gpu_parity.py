@@ -68,7 +68,8 @@ def test_stiffness_pass_random_fields(gpulib, att):
 def test_stiffness_variants_agree(gpulib, att):
     """All stiffness variants (one CTA per element at 4-7 CTAs/SM, the pipelined
     persistent kernel, the cp.async-staged builds at 6-8 CTAs/SM, the builds with
-    evict-first hints, three threads per point) do the same
+    evict-first hints, three threads per point, the bulk-copy-staged builds at
+    6-8 CTAs/SM) do the same
     arithmetic in the same order; the scatter-added acceleration differs
     only by the order of the atomic additions, the memory variables and strains
     at most by FMA contraction choices of the compiler."""
@@ -80,7 +81,7 @@ def test_stiffness_variants_agree(gpulib, att):
     d = rng.standard_normal(n3).astype(np.float32) * 1e-3
     v = rng.standard_normal(n3).astype(np.float32) * 1e-2
     out = []
-    for variant in range(12):
+    for variant in range(15):
         g = _solver(db, cfg)
         g.set_stiffness_variant(variant)
         g.set_fields(d, v, np.zeros(n3, np.float32))
@@ -90,7 +91,7 @@ def test_stiffness_variants_agree(gpulib, att):
         mem = g.memory_variables() if att else None
         out.append((acc, mem))
         g.close()
-    for v in range(1, 12):
+    for v in range(1, 15):
         assert rel_l2(out[v][0], out[0][0]) < 1e-6, v
         if att:
             same = []
