@@ -443,7 +443,7 @@ def stiffness_variant_name(v: int) -> str:
     """The kernel build a stiffness variant number selects (sf3d_set_stiffness_variant)."""
     if v == 1:
         return "stiffness_pipe_kernel<att>"
-    ctas = [4, 0, 5, 6, 7, 6, 7, 8, 6, 7, 3, 4, 6, 7, 8][v]
+    ctas = [4, 0, 5, 6, 7, 6, 7, 8, 6, 7, 3, 4, 7, 8, 9][v]
     kind = ("cp.async-staged memory variables" if 5 <= v <= 7 else
             "evict-first element streams" if v in (8, 9) else
             "3 threads per point" if v in (10, 11) else

@@ -416,14 +416,14 @@ void launch_minb(const StiffnessArgs& a, bool att, bool store_strain, cudaStream
     stiffness_kernel<false, false, MINB, GEOM, false, true, STREAM><<<grid, block, 0, s>>>(a);
 }
 
-template <int MINB, bool STAGE = false>
+template <int MINB, bool STAGE = false, bool BULK = false>
 void launch_packed(const StiffnessArgs& a, bool att, bool store_strain, cudaStream_t s, int geom) {
   if (geom == kGeomPackF16)
-    launch_minb<MINB, kGeomPackF16, STAGE>(a, att, store_strain, s);
+    launch_minb<MINB, kGeomPackF16, STAGE, false, BULK>(a, att, store_strain, s);
   else if (geom == kGeomPackBF16)
-    launch_minb<MINB, kGeomPackBF16, STAGE>(a, att, store_strain, s);
+    launch_minb<MINB, kGeomPackBF16, STAGE, false, BULK>(a, att, store_strain, s);
   else
-    launch_minb<MINB, kGeomPackF32, STAGE>(a, att, store_strain, s);
+    launch_minb<MINB, kGeomPackF32, STAGE, false, BULK>(a, att, store_strain, s);
 }
 
 }  // namespace
@@ -437,12 +437,24 @@ void launch_stiffness(const StiffnessArgs& a, bool att, bool store_strain, cudaS
                       int geom_format, bool staged, bool streaming, bool bulk) {
   if (a.nelem <= 0) return;
   if (bulk && geom_format == kGeomFP32) {
-    if (blocks_per_sm == 8)
+    // 23.5 KB of shared memory and 72 / 64 / 56 registers a thread: 7, 8 or 9 CTAs/SM
+    if (blocks_per_sm >= 9)
+      launch_minb<9, kGeomFP32, true, false, true>(a, att, store_strain, s);
+    else if (blocks_per_sm == 8)
       launch_minb<8, kGeomFP32, true, false, true>(a, att, store_strain, s);
-    else if (blocks_per_sm == 7)
-      launch_minb<7, kGeomFP32, true, false, true>(a, att, store_strain, s);
     else
-      launch_minb<6, kGeomFP32, true, false, true>(a, att, store_strain, s);
+      launch_minb<7, kGeomFP32, true, false, true>(a, att, store_strain, s);
+    return;
+  }
+  if (geom_format != kGeomFP32 && bulk) {
+    // 24 bulk-copied rows (factors from the element record): 20.5 KB of shared
+    // memory, 64 / 56 / 48 registers a thread for 8, 9 or 10 CTAs/SM
+    if (blocks_per_sm >= 10)
+      launch_packed<10, true, true>(a, att, store_strain, s, geom_format);
+    else if (blocks_per_sm == 9)
+      launch_packed<9, true, true>(a, att, store_strain, s, geom_format);
+    else
+      launch_packed<8, true, true>(a, att, store_strain, s, geom_format);
     return;
   }
   if (geom_format != kGeomFP32 && staged) {

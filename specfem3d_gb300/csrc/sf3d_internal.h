@@ -499,13 +499,14 @@ void launch_stiffness_pipelined(const StiffnessArgs& a, bool att, bool store_str
 //   10, 11: three threads per point (384-thread CTAs), 3 and 4 CTAs/SM;
 //   12, 13, 14: one CTA per element with the memory variables, strains and
 //   attenuation factors brought into shared memory by 14 bulk copies (one
-//   thread, one mbarrier) at 6, 7, 8 CTAs/SM
+//   thread, one mbarrier) at 7, 8, 9 CTAs/SM
 // Under a packed geometry format (sf3d_set_geometry_format) 4 selects the packed
-// build at 7 CTAs/SM, 5, 6, 7 the packed builds with staged memory variables at
-// 8, 9, 10 CTAs/SM, and every other variant the packed build at 6.
+// build at 7 CTAs/SM, 5, 6, 7 the packed builds with cp.async-staged memory
+// variables at 8, 9, 10 CTAs/SM, 12, 13, 14 the packed builds with bulk-copied
+// ones at 8, 9, 10, and every other variant the packed build at 6.
 constexpr int kNumStiffnessVariants = 15;
 inline int variant_blocks_per_sm(int v) {
-  const int t[kNumStiffnessVariants] = {4, 0, 5, 6, 7, 6, 7, 8, 6, 7, 3, 4, 6, 7, 8};
+  const int t[kNumStiffnessVariants] = {4, 0, 5, 6, 7, 6, 7, 8, 6, 7, 3, 4, 7, 8, 9};
   return (v >= 0 && v < kNumStiffnessVariants) ? t[v] : 4;
 }
 inline bool variant_staged(int v) { return v >= 5 && v <= 7; }
@@ -567,13 +568,15 @@ inline void run_stiffness(Mesh* mp, const StiffnessArgs& a, bool att, bool store
   if (mp->geom_format) {
     // packed static streams: the one-CTA-per-element kernel at 6 or 7 CTAs/SM
     // (variant 4: 7), or with cp.async-staged memory variables at 8, 9 or 10
-    // (variants 5, 6, 7)
+    // (variants 5, 6, 7), or with bulk-copied ones at 8, 9 or 10 (12, 13, 14)
     StiffnessArgs h = a;
     h.pack = mp->d_pack;
     h.pool = mp->d_pack_pool;
     const int v = mp->stiffness_variant;
     if (variant_staged(v))
       launch_stiffness(h, att, store_strain, s, v + 3, mp->geom_format, true);
+    else if (variant_bulk(v))
+      launch_stiffness(h, att, store_strain, s, v - 4, mp->geom_format, true, false, true);
     else
       launch_stiffness(h, att, store_strain, s, v == 4 ? 7 : 6, mp->geom_format);
   } else if (mp->stiffness_variant == 1 && mp->d_kerr) {

@@ -46,11 +46,12 @@ def test_packed_formats_exact_on_layered_block(gpulib):
         assert rel_l2(out[fmt], out["fp32"]) < 1e-6, fmt
 
 
-@pytest.mark.parametrize("variant", [3, 4, 5, 6, 7])
+@pytest.mark.parametrize("variant", [3, 4, 5, 6, 7, 12, 13, 14])
 def test_packed_formats_one_pass_on_full_metric_tensors(gpulib, variant):
     """variants 3 / 4: packed builds at 6 / 7 CTAs/SM; 5 / 6 / 7: packed builds with
     cp.async-staged memory variables at 8 / 9 / 10 CTAs/SM (factors read from the
-    element record where they are used)."""
+    element record where they are used); 12 / 13 / 14: the same with bulk-copied
+    memory variables and strains."""
     from specfem3d_gb300 import configs, hexmesh
     from specfem3d_gb300.solver import GPUSolver
     cfg = configs.small_layered(nstep=4, attenuation=True)
