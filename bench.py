@@ -396,11 +396,12 @@ def aniso_leg(db: dict, cfg: dict, steps: int):
     g = solver.GPUSolver(d, cfg, nlength=1)
     g.run(3, steps_per_graph=0)
     per = {}
-    for variant, bps in ((2, 4), (3, 5), (4, 6)):        # anisotropic builds: 4, 5, 6 CTAs per SM
+    # anisotropic builds: 4, 5, 6 CTAs per SM
+    for variant, name in ((2, "4"), (3, "5"), (4, "6")):
         g.set_stiffness_variant(variant)
         g.run(steps, steps_per_graph=0, timing=True)
         t = g.last_timing()
-        per[bps] = t["stiffness_ms"] / max(t["stiffness_launches"], 1)
+        per[name] = t["stiffness_ms"] / max(t["stiffness_launches"], 1)
     g.close()
     best = min(per, key=per.get)
     ms = per[best]
@@ -563,7 +564,7 @@ def main():
         L.initialize_gpu_device_(A.i(lr), A.i(0))
     W, K = max(3, args.warmup), max(1, args.steps)
     Kr = max(3, min(K, args.roofline_steps))
-    nstep_total = W + 2 * K + 4 * Kr + args.e2e_steps + 4
+    nstep_total = W + 2 * K + 4 * Kr + args.e2e_steps + 4 + (3 * args.aniso + 3 if args.aniso > 0 else 0)
     if args.small:
         cfg = configs.layered_viscoelastic(nstep=nstep_total, nx=32, ny=32, counts=(4, 6, 6))
         workload = "layered viscoelastic 32x32x16 block (reduced)"

@@ -60,6 +60,7 @@ __device__ __forceinline__ void st_state(float* p, float v) {
 template <bool ATT, bool STRAIN, int MINB, int GEOM = kGeomFP32, bool STAGE = false, bool ATOMIC = true,
           bool STREAM = false, bool ANISO = false, bool BULK = false>
 __global__ void __launch_bounds__(NGLL3_PAD, MINB) stiffness_kernel(const StiffnessArgs a) {
+  constexpr bool kBulkAtt = ATT && STAGE && BULK;   // the attenuation rows by bulk copy
   __shared__ __align__(16) float s_att[(ATT && STAGE) ? (GEOM == kGeomFP32 ? 30 : 24) : 1][NGLL3_PAD];
   __shared__ uint64_t s_bar;
   bool bulk_failed = false;
@@ -91,7 +92,7 @@ __global__ void __launch_bounds__(NGLL3_PAD, MINB) stiffness_kernel(const Stiffn
   }
 #pragma unroll
   for (int s = 0; s < NSLS; ++s) fc[s] = fck[s] = 0.f;
-  if (ATT && STAGE && BULK) {
+  if (kBulkAtt) {
     if (t == 0) {
       constexpr int kRows = GEOM == kGeomFP32 ? 30 : 24;
       const long se0 = (long)e * (NSLS * NGLL3_PAD), ee0 = (long)e * NGLL3_PAD;
@@ -107,7 +108,8 @@ __global__ void __launch_bounds__(NGLL3_PAD, MINB) stiffness_kernel(const Stiffn
         bulk_g2s(&s_att[27][0], a.fck + se0, NSLS * NGLL3_PAD * sizeof(float), &s_bar);
       }
     }
-  } else if (ATT && STAGE && active) {
+  }
+  if (ATT && STAGE && !BULK && active) {
     // rows: R[c][s] -> 3c+s (0..17), epsilondev[c] -> 18+c, factor_common[s] -> 24+s,
     // factor_common_kappa[s] -> 27+s (FP32 geometry only: the packed formats read
     // the factors from the element record where they are used).  Each thread copies
@@ -291,7 +293,9 @@ __global__ void __launch_bounds__(NGLL3_PAD, MINB) stiffness_kernel(const Stiffn
       sig_yz = mu * (dzy + dyz);
     }
     if (ATT && STAGE && !BULK) asm volatile("cp.async.wait_all;" ::: "memory");
-    if (ATT && STAGE && BULK && !mbar_wait_bounded(&s_bar, 0)) {
+    // every bulk-copied row is needed from here on (first use: the
+    // memory-variable sums of the stress)
+    if (kBulkAtt && !mbar_wait_bounded(&s_bar, 0)) {
       bulk_failed = true;  // the results of this element are not valid; the host is told
       if (a.err) atomicExch(a.err, 1);
     }
@@ -402,7 +406,7 @@ __global__ void __launch_bounds__(NGLL3_PAD, MINB) stiffness_kernel(const Stiffn
   }
   // a bulk copy still in flight must land before the CTA's shared memory is
   // released: wait once more, with the same bound
-  if (ATT && STAGE && BULK && bulk_failed) mbar_wait_bounded(&s_bar, 0);
+  if (kBulkAtt && bulk_failed) mbar_wait_bounded(&s_bar, 0);
 }
 
 template <int MINB, int GEOM, bool STAGE = false, bool STREAM = false, bool BULK = false>

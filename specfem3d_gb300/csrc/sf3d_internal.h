@@ -557,7 +557,11 @@ inline void run_stiffness(Mesh* mp, const StiffnessArgs& a, bool att, bool store
     // (atomic assembly, which is correct with or without a colouring)
     // the 21 extra moduli take registers: one CTA/SM fewer than the isotropic
     // build of the same variant (the default, 6, becomes the measured best, 5)
-    const int bps = variant_blocks_per_sm(mp->stiffness_variant) - 1;
+    // the bulk-copy variants (12-14) map to the measured best anisotropic build (5):
+    // with the 21 c_ij rows bulk-copied as well, 34 KB of shared memory a CTA
+    // held it to 6 CTAs/SM and 9.5-9.7 ms against 8.96 ms on the main workload
+    const int v = mp->stiffness_variant;
+    const int bps = variant_bulk(v) ? 5 : variant_blocks_per_sm(v) - 1;
     launch_stiffness_aniso(a, att, store_strain, s, bps < 4 ? 4 : bps);
     return;
   }

@@ -18,9 +18,11 @@ from conftest import rel_l2
 pytestmark = pytest.mark.gpu
 
 
-def _run(db, cfg):
+def _run(db, cfg, variant=None):
     from specfem3d_gb300.solver import GPUSolver
     g = GPUSolver(db, cfg)
+    if variant is not None:
+        g.set_stiffness_variant(variant)
     g.run(cfg["nstep"], steps_per_graph=50)
     s, d = g.seismograms(), g.fields()[0]
     g.close()
@@ -44,8 +46,11 @@ def test_isotropic_cij_equal_isotropic_path(gpulib, att):
     assert e < 2e-6
 
 
+@pytest.mark.parametrize("variant", [None, 12, 14])
 @pytest.mark.parametrize("att", [False, True])
-def test_tilted_ti_vs_oracle(gpulib, att):
+def test_tilted_ti_vs_oracle(gpulib, att, variant):
+    """variant None: the default build; 12 / 14: the bulk-copy variants, which map
+    to the 5-CTA/SM anisotropic build."""
     from oracle import oracle as O
     from specfem3d_gb300 import configs, meshgen, models as M
     cfg = configs.small_layered(nstep=400, attenuation=att)
@@ -56,8 +61,8 @@ def test_tilted_ti_vs_oracle(gpulib, att):
     sim = O.make_sim(dba, cfg, "f32", nthreads=os.cpu_count() or 1)
     sim.step(cfg["nstep"])
     ref = O.seismograms(sim)
-    s, d = _run(dba, cfg)
-    s_iso, _ = _run(db, cfg)
+    s, d = _run(dba, cfg, variant)
+    s_iso, _ = _run(db, cfg, variant)
     es, ed = rel_l2(s, ref), rel_l2(d, sim.get("displ"))
     print(f"tilted TI (att={att}): seismograms {es:.2e}, displacement {ed:.2e}; "
           f"differs from the isotropic run by {rel_l2(s, s_iso):.2e}")
