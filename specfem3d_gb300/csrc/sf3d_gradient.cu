@@ -131,6 +131,7 @@ struct GradArgs {
   const float* kappav; // fused form: moduli and the K p accumulator
   const float* muv;
   float* kp;
+  int* err;            // kernel error word (a bounded wait that timed out)
 };
 
 // Gradient of the 3x3 displacement derivative of a field staged in shared memory.
@@ -229,12 +230,17 @@ __global__ void __launch_bounds__(NGLL3_PAD) grad_accum_kernel(const GradArgs a)
 // Fused form of one element's part of the transposed step: K p (the elastic
 // stiffness applied to p, arithmetic of stiffness_kernel<ATT=0>) scatter-added
 // into kp, and the gradient contributions of grad_accum_kernel, from one gather
-// of p and one set of p derivatives.
+// of p and one set of p derivatives.  The element's three FP64 gradient rows
+// (3 KB) come into shared memory by bulk copy at the start, so their load
+// latency runs under the gathers; every thread waits for them (bounded) where
+// it adds its contributions.
 __global__ void __launch_bounds__(NGLL3_PAD, 5) adj_stiffness_grad_kernel(const GradArgs a) {
   __shared__ float s_gll[NGLL3];
   __shared__ float s_p[3][NGLL3_PAD];
   __shared__ float s_u[3][NGLL3_PAD];
   __shared__ float s_t[9][NGLL3_PAD];
+  __shared__ __align__(16) double s_g[3][NGLL3_PAD];   // rho, kappa, mu
+  __shared__ uint64_t s_bar;
   const int t = threadIdx.x;
   const int e = a.phase ? __ldg(a.phase + blockIdx.x) : (int)blockIdx.x;
   const bool active = t < NGLL3;
@@ -242,6 +248,16 @@ __global__ void __launch_bounds__(NGLL3_PAD, 5) adj_stiffness_grad_kernel(const 
   const long eo = (long)e * NGLL3_PAD + t;
   float pa = 0.f, kap = 0.f, mu = 0.f;
   int g = 0;
+  bool bulk_failed = false;
+  if (t == 0) {
+    const long eb = (long)e * NGLL3_PAD;
+    mbar_init(&s_bar, 1);
+    asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+    mbar_arrive_expect_tx(&s_bar, (uint32_t)(3 * NGLL3_PAD * sizeof(double)));
+    bulk_g2s(&s_g[0][0], a.g_rho + eb, NGLL3_PAD * sizeof(double), &s_bar);
+    bulk_g2s(&s_g[1][0], a.g_kappa + eb, NGLL3_PAD * sizeof(double), &s_bar);
+    bulk_g2s(&s_g[2][0], a.g_mu + eb, NGLL3_PAD * sizeof(double), &s_bar);
+  }
   if (active) {
     s_gll[t] = __ldg(a.gll + t);
     g = __ldg(a.ibool + eo);
@@ -301,9 +317,13 @@ __global__ void __launch_bounds__(NGLL3_PAD, 5) adj_stiffness_grad_kernel(const 
     dd += 2.f * (exy_p * exy_u + exz_p * exz_u + eyz_p * eyz_u);
     // products in FP32, time integration in FP64 (as grad_accum_kernel)
     const float wj = (a.w[i] * a.w[j] * a.w[k]) * jac;
-    a.g_kappa[eo] += (double)(wj * trp * tru);
-    a.g_mu[eo] += (double)(wj * 2.f * dd);
-    a.g_rho[eo] += (double)(wj * pa);
+    if (!mbar_wait_bounded(&s_bar, 0)) {
+      bulk_failed = true;  // this element's gradient is not valid; the host is told
+      if (a.err) atomicExch(a.err, 1);
+    }
+    a.g_kappa[eo] = s_g[1][t] + (double)(wj * trp * tru);
+    a.g_mu[eo] = s_g[2][t] + (double)(wj * 2.f * dd);
+    a.g_rho[eo] = s_g[0][t] + (double)(wj * pa);
     // stress of p (stiffness_kernel<ATT=0> arithmetic)
     const float dxx = dp[0][0], dxy = dp[0][1], dxz = dp[0][2];
     const float dyx = dp[1][0], dyy = dp[1][1], dyz = dp[1][2];
@@ -354,6 +374,9 @@ __global__ void __launch_bounds__(NGLL3_PAD, 5) adj_stiffness_grad_kernel(const 
     atomicAdd(a.kp + 3L * g + 1, -(fac1 * n1y + fac2 * n2y + fac3 * n3y));
     atomicAdd(a.kp + 3L * g + 2, -(fac1 * n1z + fac2 * n2z + fac3 * n3z));
   }
+  // a bulk copy still in flight must land before the CTA's shared memory is
+  // released: wait once more, with the same bound
+  if (bulk_failed) mbar_wait_bounded(&s_bar, 0);
 }
 
 bool alloc_f(float** d, size_t n) { return alloc_zero((void**)d, sizeof(float) * n); }
@@ -446,6 +469,7 @@ void adjoint_step(Mesh* mp, int n, const float* u, const float* araw, float dt, 
     ga.kappav = mp->d_kappav;
     ga.muv = mp->d_muv;
     ga.kp = G->kp;
+    ga.err = mp->d_kerr;
     if (G->fused)
       adj_stiffness_grad_kernel<<<a.nelem, NGLL3_PAD, 0, s>>>(ga);
     else
