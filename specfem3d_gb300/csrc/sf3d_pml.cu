@@ -81,6 +81,7 @@ struct PmlArgs {
   const float* coef;
   float* rmem;
   float* eps[5];                 // epsilondev xx yy xy xz yz (COMPUTE_AND_STORE_STRAIN) or null
+  int* err;                      // kernel error word (a bounded wait that timed out)
 };
 
 // gradient in the reference cube of the three components of s (3 x 128 values)
@@ -115,8 +116,22 @@ __device__ __forceinline__ void phys_grad(const float T[3][3], const float* m, i
   }
 }
 
-// one CTA per CPML element of the phase, thread p < 125 owns GLL point p
+// dynamic shared memory of pml_stiffness_kernel: the element's coefficient rows
+// and convolution memory variables
+constexpr size_t kPmlStageBytes = sizeof(float) * (kPmlCoefRows + kPmlMemRows) * NGLL3_PAD;
+
+// one CTA per CPML element of the phase, thread p < 125 owns GLL point p.  The
+// element's 41 coefficient rows and 48 memory-variable rows are contiguous in
+// HBM ([cpml][41][128], [cpml][48][128]): thread 0 brings them into shared
+// memory with two bulk copies on one mbarrier while the CTA gathers the fields,
+// and every thread waits for them (bounded; error word on timeout) before the
+// convolutions.  The updated memory variables go back with coalesced stores.
 __global__ void __launch_bounds__(NGLL3_PAD) pml_stiffness_kernel(const PmlArgs a) {
+  extern __shared__ __align__(16) float s_stage[];
+  float* s_cf = s_stage;                              // [41][128]
+  float* s_rm = s_stage + kPmlCoefRows * NGLL3_PAD;   // [48][128]
+  __shared__ uint64_t s_bar;
+  bool bulk_failed = false;
   __shared__ float s_gll[NGLL3];
   __shared__ float s_u[3][NGLL3_PAD];
   __shared__ float s_o[3][NGLL3_PAD];
@@ -134,6 +149,13 @@ __global__ void __launch_bounds__(NGLL3_PAD) pml_stiffness_kernel(const PmlArgs 
   const int ir = __ldg(a.irregular + e);
   long g = 0;
   float vel[3] = {0.f, 0.f, 0.f};
+  if (t == 0) {
+    mbar_init(&s_bar, 1);
+    asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+    mbar_arrive_expect_tx(&s_bar, (uint32_t)kPmlStageBytes);
+    bulk_g2s(s_cf, a.coef + (long)ec * kPmlCoefRows * NGLL3_PAD, kPmlCoefRows * NGLL3_PAD * sizeof(float), &s_bar);
+    bulk_g2s(s_rm, a.rmem + (long)ec * kPmlMemRows * NGLL3_PAD, kPmlMemRows * NGLL3_PAD * sizeof(float), &s_bar);
+  }
   if (active) {
     s_gll[t] = __ldg(a.gll + t);
     g = __ldg(a.ibool + eo);
@@ -174,8 +196,12 @@ __global__ void __launch_bounds__(NGLL3_PAD) pml_stiffness_kernel(const PmlArgs 
       a.eps[3][eo] = 0.5f * (du[2][0] + du[0][2]);
       a.eps[4][eo] = 0.5f * (du[2][1] + du[1][2]);
     }
-#define CF(r) __ldg(a.coef + co + (long)(r) * NGLL3_PAD)
-#define RM(r) a.rmem[mo + (long)(r) * NGLL3_PAD]
+    if (!mbar_wait_bounded(&s_bar, 0)) {
+      bulk_failed = true;  // this element's results are not valid; the host is told
+      if (a.err) atomicExch(a.err, 1);
+    }
+#define CF(r) s_cf[(r) * NGLL3_PAD + t]
+#define RM(r) s_rm[(r) * NGLL3_PAD + t]
     // convolution memory variables: r <- c0 r + new c1 + old c2
     auto upd = [&](int row, int set_row, float vnew, float vold) {
       float& r = RM(row);
@@ -255,6 +281,9 @@ __global__ void __launch_bounds__(NGLL3_PAD) pml_stiffness_kernel(const PmlArgs 
 #pragma unroll
     for (int c = 0; c < 3; ++c)
       acc[c] = wrj * (A1 * vel[c] + A2 * s_u[c][t] + A3 * rd[c][0] + A4 * rd[c][1] + A5 * rd[c][2]);
+    // the updated memory variables back to HBM (coalesced rows)
+#pragma unroll 8
+    for (int r = 0; r < kPmlMemRows; ++r) a.rmem[mo + (long)r * NGLL3_PAD] = RM(r);
 #undef CF
 #undef RM
     // non-symmetric stress dotted with the rows of the metric (get_dot_product)
@@ -300,6 +329,9 @@ __global__ void __launch_bounds__(NGLL3_PAD) pml_stiffness_kernel(const PmlArgs 
     for (int c = 0; c < 3; ++c)
       atomicAdd(a.accel + 3 * g + c, -(fac1 * n[c][0] + fac2 * n[c][1] + fac3 * n[c][2] + vel[c]));
   }
+  // a bulk copy still in flight must land before the CTA's shared memory is
+  // released: wait once more, with the same bound
+  if (bulk_failed) mbar_wait_bounded(&s_bar, 0);
 }
 
 __global__ void pml_boundary_kernel(int nfaces, const int* __restrict__ abs_ispec, const int* __restrict__ abs_pt,
@@ -359,9 +391,18 @@ int launch_pml_stiffness(Mesh* mp, int iphase, bool strain, cudaStream_t s) {
   a.pnew = mp->d_pml_displ_new;
   a.coef = mp->d_pml_coef;
   a.rmem = mp->d_pml_rmem;
+  a.err = mp->d_kerr;
   if (strain)
     for (int c = 0; c < 5; ++c) a.eps[c] = mp->f.eps[c];
-  pml_stiffness_kernel<<<a.nelem, NGLL3_PAD, 0, s>>>(a);
+  static bool configured = false;  // opt in to > 48 KB of shared memory once
+  if (!configured) {
+    if (!cuda_ok(cudaFuncSetAttribute(pml_stiffness_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                      (int)kPmlStageBytes),
+                 "cudaFuncSetAttribute(pml_stiffness_kernel)"))
+      return 0;
+    configured = true;
+  }
+  pml_stiffness_kernel<<<a.nelem, NGLL3_PAD, kPmlStageBytes, s>>>(a);
   return 1;
 }
 
