@@ -253,7 +253,8 @@ def batch_leg(nshots: int, steps: int, nx: int = 64):
     perturbed model, no attenuation): all shots advancing together with
     shot-innermost fields (autotuned stiffness kernel; FP32 arrays, then packed FP16
     moduli) against the plain single-shot path on the same mesh."""
-    from specfem3d_gb300 import configs, gradient as G, meshgen
+    import ctypes
+    from specfem3d_gb300 import abi, configs, gradient as G, meshgen
     from specfem3d_gb300.batch import BatchSolver
     from specfem3d_gb300.solver import GPUSolver
     cfg = configs.batched_shots(nstep=4 * steps + 32, nshots=nshots, nx=nx)
@@ -278,6 +279,11 @@ def batch_leg(nshots: int, steps: int, nx: int = 64):
     ms_h = b.run(steps, steps_per_graph=50)
     b.close()
     plain = GPUSolver(db, G.shot_config(cfg, 0), nlength=steps + 8)
+    # the plain path at its best: every stiffness variant timed at rest, the fastest kept
+    msp = (ctypes.c_float * STIFFNESS_VARIANTS)()
+    bestp = ctypes.c_int()
+    if plain.L.sf3d_autotune_stiffness(plain.mp, 3, msp, ctypes.addressof(bestp)) != 0:
+        abi.check()
     plain.run(3, steps_per_graph=50)
     plain.run(steps, steps_per_graph=50)
     ms_p = plain.last_timing()["total_ms"]
@@ -308,7 +314,8 @@ def batch_leg(nshots: int, steps: int, nx: int = 64):
             "nspec": nspec, "batched": rate_b, "batched_fp16_moduli": rate_h, "plain_single_shot": rate_p,
             "speedup_per_shot": rate_b / rate_p, "speedup_per_shot_fp16_moduli": rate_h / rate_p,
             "batched_ms_per_step": ms_b / steps, "batched_fp16_ms_per_step": ms_h / steps,
-            "plain_ms_per_step": ms_p / steps, "tiling": tune, "halves": halves,
+            "plain_ms_per_step": ms_p / steps, "plain_stiffness_variant": stiffness_variant_name(bestp.value),
+            "tiling": tune, "halves": halves,
             "ms_per_step_one_stream": ms_one / steps,
             "ms_per_step_two_halves": None if ms_two is None else ms_two / steps,
             "step_hbm_frac": (dyn + static32) / (ms_b / steps / 1000.0) / 1e9 / peak,

@@ -122,6 +122,8 @@ class MisfitGradient:
         self.nstep = int(cfg["nstep"])
         self.solver = GPUSolver(db, cfg, nlength=self.nstep)
         self.L = self.solver.L
+        # the fastest stiffness build for this mesh, timed at rest (a few ms)
+        self.stiffness_variant, _ = self.solver.autotune_stiffness()
         nbytes = ctypes.c_double()
         rc = self.L.sf3d_gradient_setup(self.solver.mp, self.nstep, int(checkpoint_every), ctypes.addressof(nbytes))
         if rc != 0:

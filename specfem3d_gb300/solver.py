@@ -386,9 +386,18 @@ class GPUSolver:
         abi.check()
 
     def set_stiffness_variant(self, variant: int):
-        """0: one CTA per element; 1: persistent bulk-copy pipelined kernel (default)."""
+        """Stiffness kernel build (sf3d_set_stiffness_variant: 0-14; 3 is the default)."""
         if self.L.sf3d_set_stiffness_variant(self.mp, int(variant)) != 0:
             abi.check()
+
+    def autotune_stiffness(self, reps: int = 3):
+        """Time every stiffness variant on the wavefield at rest (before the first
+        step) and keep the fastest; returns (variant, ms per variant)."""
+        ms = (ctypes.c_float * 15)()
+        best = ctypes.c_int()
+        if self.L.sf3d_autotune_stiffness(self.mp, int(reps), ms, ctypes.addressof(best)) != 0:
+            abi.check()
+        return best.value, [float(x) for x in ms]
 
     def set_geometry_precision(self, bits: int):
         """32: FP32 geometry and moduli; 16: the "fp16" packed format."""
