@@ -314,7 +314,7 @@ def batch_leg(nshots: int, steps: int, nx: int = 64):
             "nspec": nspec, "batched": rate_b, "batched_fp16_moduli": rate_h, "plain_single_shot": rate_p,
             "speedup_per_shot": rate_b / rate_p, "speedup_per_shot_fp16_moduli": rate_h / rate_p,
             "batched_ms_per_step": ms_b / steps, "batched_fp16_ms_per_step": ms_h / steps,
-            "plain_ms_per_step": ms_p / steps, "plain_stiffness_variant": stiffness_variant_name(bestp.value),
+            "plain_ms_per_step": ms_p / steps, "plain_stiffness_variant": stiffness_variant_name(bestp.value, att=False),
             "tiling": tune, "halves": halves,
             "ms_per_step_one_stream": ms_one / steps,
             "ms_per_step_two_halves": None if ms_two is None else ms_two / steps,
@@ -336,6 +336,7 @@ def coupled_leg(steps: int):
     cfg = configs.coupled_fluid_solid(nstep=steps + 5)
     db = meshgen.build_database(cfg)
     g = GPUSolver(db, cfg)
+    variant, _ = g.autotune_stiffness()          # at rest, before the first step
     g.run_per_call(3)
     g.L.sf3d_synchronize(g.mp)
     t0 = time.perf_counter()
@@ -347,7 +348,8 @@ def coupled_leg(steps: int):
     g.close()
     return {"unit": UNIT, "value": nglob * steps / dt, "ms_per_step": 1000 * dt / steps, "steps": steps,
             "nglob": nglob, "nspec": int(db["nspec"]), "fluid_elements": int(db["ispec_is_acoustic"].sum()),
-            "finite": ok, "path": "per-call FC_FUNC_ entry points, host stf per step, pressure traces",
+            "finite": ok, "stiffness_variant": stiffness_variant_name(variant, att=False),
+            "path": "per-call FC_FUNC_ entry points, host stf per step, pressure traces",
             "workload": "coupled fluid/solid 96x96x48 hexes, 20x20x10 km"}
 
 
@@ -374,6 +376,7 @@ def pml_leg(steps: int):
         if name == "cpml":
             d = pml.setup(d, c, nel=c["pml_elements"], f0=c["pml_f0"])
         g = GPUSolver(d, c)
+        g.autotune_stiffness()                  # the elastic elements outside the layers
         g.run(5, steps_per_graph=0)
         g.run(steps, steps_per_graph=50)
         t = g.last_timing()
@@ -447,17 +450,19 @@ def smooth_leg(nx: int = 64, sigma: float = 312.5):
             "finite": bool(np.isfinite(out).all())}
 
 
-def stiffness_variant_name(v: int) -> str:
-    """The kernel build a stiffness variant number selects (sf3d_set_stiffness_variant)."""
+def stiffness_variant_name(v: int, att: bool = True) -> str:
+    """The kernel build a stiffness variant number selects (sf3d_set_stiffness_variant);
+    without attenuation the staged builds have no memory variables to stage."""
     if v == 1:
-        return "stiffness_pipe_kernel<att>"
+        return "stiffness_pipe_kernel<att>" if att else "stiffness_pipe_kernel<no att>"
     ctas = [4, 0, 5, 6, 7, 6, 7, 8, 6, 7, 3, 4, 7, 8, 9][v]
-    kind = ("cp.async-staged memory variables" if 5 <= v <= 7 else
-            "evict-first element streams" if v in (8, 9) else
+    kind = ("evict-first element streams" if v in (8, 9) else
             "3 threads per point" if v in (10, 11) else
+            "" if not att else
+            "cp.async-staged memory variables" if 5 <= v <= 7 else
             "bulk-copy-staged memory variables" if v >= 12 else "")
     name = "stiffness_split_kernel" if v in (10, 11) else "stiffness_kernel"
-    return f"{name}<att, {ctas} CTAs/SM" + (f", {kind}>" if kind else ">")
+    return f"{name}<{'att' if att else 'no att'}, {ctas} CTAs/SM" + (f", {kind}>" if kind else ">")
 
 
 REFERENCE_MAX_STEPS = 40
