@@ -87,11 +87,12 @@ __global__ void adj_p_kernel(const float* __restrict__ vh, const float* __restri
 // kp = -K p and bp = -B p: uth = uh - kp, vth = vh - bp; back through the
 // predictor; then p of the previous step, -M^-1 (ah + dt/2 vh), from the new
 // adjoints (the residual enters uh only, so p does not depend on it), and the
-// K p / B p accumulators cleared for that step
-__global__ void adj_update_kernel(float* __restrict__ uh, float* __restrict__ vh, float* __restrict__ ah,
-                                  float* __restrict__ kp, float* __restrict__ bp, float* __restrict__ p,
-                                  const float* __restrict__ rmx, const float* __restrict__ rmy,
-                                  const float* __restrict__ rmz, long nglob, float dt, float dt2, float dtsq2) {
+// K p / B p accumulators cleared for that step.  The adjoint of the
+// acceleration is used only through p, so it is not stored.
+__global__ void adj_update_kernel(float* __restrict__ uh, float* __restrict__ vh, float* __restrict__ kp,
+                                  float* __restrict__ bp, float* __restrict__ p, const float* __restrict__ rmx,
+                                  const float* __restrict__ rmy, const float* __restrict__ rmz, long nglob,
+                                  float dt, float dt2, float dtsq2) {
   const long i = (long)blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= 3 * nglob) return;
   const float ut = uh[i] - kp[i];
@@ -100,7 +101,6 @@ __global__ void adj_update_kernel(float* __restrict__ uh, float* __restrict__ vh
   const float an = dtsq2 * ut + dt2 * vt;
   uh[i] = ut;
   vh[i] = vn;
-  ah[i] = an;
   const long g = i / 3;
   const int c = (int)(i - 3 * g);
   const float rm = c == 0 ? __ldg(rmx + g) : (c == 1 ? __ldg(rmy + g) : __ldg(rmz + g));
@@ -475,7 +475,7 @@ void adjoint_step(Mesh* mp, int n, const float* u, const float* araw, float dt, 
     else
       grad_accum_kernel<<<a.nelem, NGLL3_PAD, 0, s>>>(ga);
   }
-  adj_update_kernel<<<nblk(n3, 256), 256, 0, s>>>(G->adj_u, G->adj_v, G->adj_a, G->kp, G->bp, G->p, mp->d_rmassx,
+  adj_update_kernel<<<nblk(n3, 256), 256, 0, s>>>(G->adj_u, G->adj_v, G->kp, G->bp, G->p, mp->d_rmassx,
                                                   mp->d_rmassy, mp->d_rmassz, mp->nglob, dt, dt2, dtsq2);
 }
 
