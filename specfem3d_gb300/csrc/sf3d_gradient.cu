@@ -234,7 +234,10 @@ __global__ void __launch_bounds__(NGLL3_PAD) grad_accum_kernel(const GradArgs a)
 // (3 KB) come into shared memory by bulk copy at the start, so their load
 // latency runs under the gathers; every thread waits for them (bounded) where
 // it adds its contributions.
-__global__ void __launch_bounds__(NGLL3_PAD, 5) adj_stiffness_grad_kernel(const GradArgs a) {
+// Register budget of 10 CTAs/SM (48 registers, no spills; 11 KB of shared
+// memory a CTA): measured against 6 and 8 CTAs/SM, the most resident elements
+// hide the gathers best (reverse sweep 3.96 / 3.88 / 3.84 s per shot).
+__global__ void __launch_bounds__(NGLL3_PAD, 10) adj_stiffness_grad_kernel(const GradArgs a) {
   __shared__ float s_gll[NGLL3];
   __shared__ float s_p[3][NGLL3_PAD];
   __shared__ float s_u[3][NGLL3_PAD];
