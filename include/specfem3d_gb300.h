@@ -360,7 +360,8 @@ int sf3d_last_timing(long *Mesh_pointer, float *stiffness_ms, int *stiffness_lau
  *   12, 13, 14: one CTA per element with the memory variables, strains and
  *               attenuation factors brought into shared memory by 14 bulk
  *               copies (one thread, one mbarrier with a bounded wait), for 7,
- *               8, 9 CTAs per SM (register budget 72, 64, 56).
+ *               8, 9 CTAs per SM (register budget 72, 64, 56); without
+ *               attenuation the plain build at 8, 10, 12 CTAs per SM.
  * Under a packed geometry format (sf3d_set_geometry_format) the variant picks
  * the packed build: 4 at 7 CTAs/SM; 5, 6, 7 with the memory variables and
  * strains staged by cp.async and the factors read from the element record, at

@@ -409,15 +409,17 @@ __global__ void __launch_bounds__(NGLL3_PAD, MINB) stiffness_kernel(const Stiffn
   if (kBulkAtt && bulk_failed) mbar_wait_bounded(&s_bar, 0);
 }
 
-template <int MINB, int GEOM, bool STAGE = false, bool STREAM = false, bool BULK = false>
+// MINB_NOATT: the register budget of the builds without attenuation (no memory
+// variables: they fit more CTAs per SM than the attenuation build of the variant)
+template <int MINB, int GEOM, bool STAGE = false, bool STREAM = false, bool BULK = false, int MINB_NOATT = MINB>
 void launch_minb(const StiffnessArgs& a, bool att, bool store_strain, cudaStream_t s) {
   dim3 grid(a.nelem), block(NGLL3_PAD);
   if (att)
     stiffness_kernel<true, true, MINB, GEOM, STAGE, true, STREAM, false, BULK><<<grid, block, 0, s>>>(a);
   else if (store_strain)
-    stiffness_kernel<false, true, MINB, GEOM, false, true, STREAM><<<grid, block, 0, s>>>(a);
+    stiffness_kernel<false, true, MINB_NOATT, GEOM, false, true, STREAM><<<grid, block, 0, s>>>(a);
   else
-    stiffness_kernel<false, false, MINB, GEOM, false, true, STREAM><<<grid, block, 0, s>>>(a);
+    stiffness_kernel<false, false, MINB_NOATT, GEOM, false, true, STREAM><<<grid, block, 0, s>>>(a);
 }
 
 template <int MINB, bool STAGE = false, bool BULK = false>
@@ -441,13 +443,14 @@ void launch_stiffness(const StiffnessArgs& a, bool att, bool store_strain, cudaS
                       int geom_format, bool staged, bool streaming, bool bulk) {
   if (a.nelem <= 0) return;
   if (bulk && geom_format == kGeomFP32) {
-    // 23.5 KB of shared memory and 72 / 64 / 56 registers a thread: 7, 8 or 9 CTAs/SM
+    // 23.5 KB of shared memory and 72 / 64 / 56 registers a thread: 7, 8 or 9 CTAs/SM;
+    // without attenuation (nothing to stage, 10 KB) 8, 10 or 12 CTAs/SM
     if (blocks_per_sm >= 9)
-      launch_minb<9, kGeomFP32, true, false, true>(a, att, store_strain, s);
+      launch_minb<9, kGeomFP32, true, false, true, 12>(a, att, store_strain, s);
     else if (blocks_per_sm == 8)
-      launch_minb<8, kGeomFP32, true, false, true>(a, att, store_strain, s);
+      launch_minb<8, kGeomFP32, true, false, true, 10>(a, att, store_strain, s);
     else
-      launch_minb<7, kGeomFP32, true, false, true>(a, att, store_strain, s);
+      launch_minb<7, kGeomFP32, true, false, true, 8>(a, att, store_strain, s);
     return;
   }
   if (geom_format != kGeomFP32 && bulk) {
