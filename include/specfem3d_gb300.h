@@ -484,6 +484,15 @@ int sf3d_gradient_release(long *Mesh_pointer);
  *   - returns after the result is on the host (synchronises `stream`). */
 int sf3d_field_maxabs_noalloc(const realw *d_field, long n, void *stream, realw *max_abs);
 
+/* Self-check of the bounded mbarrier wait behind every bulk copy of the
+ * stiffness, C-PML and adjoint kernels: one CTA waits, with a limit of limit_s
+ * seconds (0 < limit_s <= 2), on an mbarrier that expects 16 bytes no copy
+ * delivers; *timed_out = 1 when the wait gave up and set the error word the way
+ * the kernels do, *waited_s (may be NULL) the time the wait took.  Nothing is
+ * in flight and nothing faults; the context stays usable.  No reference
+ * counterpart. */
+int sf3d_check_bounded_wait(double limit_s, int *timed_out, double *waited_s);
+
 /* ------------------------------------------------------------------------
  * Misfit post-processing on the device (FP64).  No Mesh handle needed. */
 /* Adjoint sources of the reference's tools utils/adjoint_sources/

@@ -97,6 +97,8 @@ def load() -> ctypes.CDLL:
     L.sf3d_gradient_release.argtypes = [P]
     L.sf3d_field_maxabs_noalloc.restype = ctypes.c_int
     L.sf3d_field_maxabs_noalloc.argtypes = [P, ctypes.c_long, P, P]
+    L.sf3d_check_bounded_wait.restype = ctypes.c_int
+    L.sf3d_check_bounded_wait.argtypes = [ctypes.c_double, P, P]
     L.sf3d_batch_prepare.restype = ctypes.c_int
     L.sf3d_batch_prepare.argtypes = [P, ctypes.c_int, P, P, P, ctypes.c_int, ctypes.c_int, P]
     L.sf3d_batch_set_tiling.restype = ctypes.c_int

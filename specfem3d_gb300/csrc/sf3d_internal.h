@@ -115,13 +115,15 @@ __device__ __forceinline__ uint64_t global_ns() {
   return t;
 }
 
-// bounded wait: true when the phase completed, false after ~2 s
-__device__ __forceinline__ bool mbar_wait_bounded(uint64_t* bar, uint32_t parity) {
+// bounded wait: true when the phase completed, false after limit_ns (2 s unless
+// a caller asks for another bound)
+constexpr uint64_t kWaitLimitNs = 2000000000ull;
+__device__ __forceinline__ bool mbar_wait_bounded(uint64_t* bar, uint32_t parity, uint64_t limit_ns = kWaitLimitNs) {
   if (mbar_try_wait(bar, parity)) return true;
   const uint64_t t0 = global_ns();
   while (true) {
     if (mbar_try_wait(bar, parity)) return true;
-    if (global_ns() - t0 > 2000000000ull) return false;
+    if (global_ns() - t0 > limit_ns) return false;
   }
 }
 
