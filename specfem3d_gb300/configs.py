@@ -167,6 +167,26 @@ def refex_cpml(nstep: int = 2400) -> dict:
     return cfg
 
 
+def refex_acoustic(nstep: int = 1000) -> dict:
+    """The reference example homogeneous_acoustic: the 36 x 36 x 16 block of the
+    Stacey example (134 x 134 x 60 km) filled with one fluid (rho 2300, vp 2800:
+    nummaterial_velocity_file), Stacey faces on the five sides and a free surface
+    on top; the CMTSOLUTION explosion (Mrr = Mtt = Mpp = 7.7e27 dyne.cm, half
+    duration 2 s) at (67, 67, -30) km, a mesh vertex (its REF_SEIS run logged
+    element 2772, local (1, 1, 1)); in a fluid element the reference takes a
+    Gaussian time function and t0 = 3 half durations = 6 s; four hydrophones 50 m
+    below the surface record pressure; dt 0.1136 s."""
+    cfg = refex(nstep)
+    M0 = 7.7e27 * 1e-7
+    cfg["layers"] = [dict(rho=2300.0, vp=2800.0, vs=0.0)]
+    cfg["dt"] = 0.1136
+    cfg["sources"] = [dict(type="cmt", x=67000.0, y=67000.0, z=-30000.0, M=[M0, M0, M0, 0.0, 0.0, 0.0],
+                           stf="heaviside", hdur=2.0, octant=(-1, -1, -1))]
+    cfg["receivers"] = [(x, 67000.0, -50.0) for x in (22732.14, 34696.43, 46660.71, 58625.0)]
+    cfg["record"] = ("pressure",)
+    return cfg
+
+
 def attenuation_benchmark(nstep: int = 1300) -> dict:
     """The reference benchmark EXAMPLES/benchmarks/attenuation/viscoelastic: an
     80 x 80 x 80 regular mesh of 37.5 m cubes spanning [-1500, 1500]^3 m

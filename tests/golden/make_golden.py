@@ -96,6 +96,14 @@ def main():
     np.savez_compressed(os.path.join(out, "refex_stacey5sides.npz"), displ=d, t=t, stations=np.array(STATIONS))
     nd, t2 = read(root, "homogeneous_halfspace_HEX8_elastic_no_absorbing", "semd")
     np.savez_compressed(os.path.join(out, "refex_no_absorbing.npz"), displ=nd, t=t2, stations=np.array(STATIONS))
+    # pure-fluid example: pressure traces (.semp, band code M, component P)
+    ap, tp = [], None
+    for st in STATIONS:
+        a = np.loadtxt(os.path.join(root, EX, "homogeneous_acoustic", "REF_SEIS", f"DB.{st}.MXP.semp"))
+        tp = a[:, 0]
+        ap.append(a[:, 1])
+    np.savez_compressed(os.path.join(out, "refex_acoustic.npz"), pressure=np.asarray(ap, np.float32),
+                        t=np.asarray(tp, np.float64), stations=np.array(STATIONS))
     # C-PML example (dt 0.11 s: band code M)
     cd, t3 = read(root, "CPML_examples/homogeneous_halfspace_HEX8_elastic_absorbing_CPML_5sides", "semd", "MX")
     np.savez_compressed(os.path.join(out, "refex_cpml5sides.npz"), displ=cd, t=t3, stations=np.array(STATIONS))
