@@ -263,7 +263,8 @@ def batch_leg(nshots: int, steps: int, nx: int = 64):
     b = BatchSolver(db, cfg, nlength=4 * steps + 32)
     tune = b.autotune(reps=3)
     b.run(3, steps_per_graph=0)
-    ms_one = b.run(steps, steps_per_graph=50)
+    with ClockSampler() as clk:
+        ms_one = b.run(steps, steps_per_graph=50)
     ms_two = None
     if tune["kernel"] == "pencil" and nshots % (2 * tune["shots_per_block"]) == 0:
         # the two shot halves on two streams, correctors under the other half's stiffness
@@ -315,6 +316,7 @@ def batch_leg(nshots: int, steps: int, nx: int = 64):
             "speedup_per_shot": rate_b / rate_p, "speedup_per_shot_fp16_moduli": rate_h / rate_p,
             "batched_ms_per_step": ms_b / steps, "batched_fp16_ms_per_step": ms_h / steps,
             "plain_ms_per_step": ms_p / steps, "plain_stiffness_variant": stiffness_variant_name(bestp.value, att=False),
+            "clocks_one_stream": clk.summary(),
             "tiling": tune, "halves": halves,
             "ms_per_step_one_stream": ms_one / steps,
             "ms_per_step_two_halves": None if ms_two is None else ms_two / steps,
