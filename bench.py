@@ -457,7 +457,7 @@ def stiffness_variant_name(v: int, att: bool = True) -> str:
     without attenuation the staged builds have no memory variables to stage."""
     if v == 1:
         return "stiffness_pipe_kernel<att>" if att else "stiffness_pipe_kernel<no att>"
-    ctas = [4, 0, 5, 6, 7, 6, 7, 8, 6, 7, 3, 4, 7, 8, 9][v] if att or v < 12 else [8, 10, 12][v - 12]
+    ctas = [4, 0, 5, 6, 7, 6, 7, 8, 6, 7, 3, 4, 8, 9, 10][v] if att or v < 12 else [8, 10, 12][v - 12]
     kind = ("evict-first element streams" if v in (8, 9) else
             "3 threads per point" if v in (10, 11) else
             "" if not att else

@@ -359,16 +359,16 @@ int sf3d_last_timing(long *Mesh_pointer, float *stiffness_ms, int *stiffness_lau
  *               384-thread CTAs, 3 and 4 CTAs/SM;
  *   12, 13, 14: one CTA per element with the memory variables, strains and
  *               attenuation factors brought into shared memory by 14 bulk
- *               copies (one thread, one mbarrier with a bounded wait), for 7,
- *               8, 9 CTAs per SM (register budget 72, 64, 56); without
+ *               copies (one thread, one mbarrier with a bounded wait), for 8,
+ *               9, 10 CTAs per SM (register budget 64, 56, 48); without
  *               attenuation the plain build at 8, 10, 12 CTAs per SM.
  * Under a packed geometry format (sf3d_set_geometry_format) the variant picks
  * the packed build: 4 at 7 CTAs/SM; 5, 6, 7 with the memory variables and
  * strains staged by cp.async and the factors read from the element record, at
  * 8, 9, 10 CTAs/SM (register budget 64, 56, 48); 12, 13, 14 the same with the
  * memory variables and strains bulk-copied, at 8, 9, 10 CTAs/SM; any other at 6.
- * Default 3; the autotuner picks among all of them (14, the bulk-copy build
- * at 9 CTAs/SM, is the fastest on GB300 for the layered viscoelastic workload).
+ * Default 3; the autotuner picks among all of them (the bulk-copy builds are
+ * the fastest on GB300 for the layered viscoelastic workload).
  * No reference counterpart (the reference compiles one Kernel_2 per
  * configuration). */
 int sf3d_set_stiffness_variant(long *Mesh_pointer, int variant);

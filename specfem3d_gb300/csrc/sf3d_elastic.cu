@@ -65,9 +65,14 @@ __global__ void __launch_bounds__(NGLL3_PAD, MINB) stiffness_kernel(const Stiffn
   __shared__ uint64_t s_bar;
   bool bulk_failed = false;
   __shared__ float s_gll[NGLL3];
-  __shared__ float s_u[3][NGLL3_PAD];
-  __shared__ float s_v[ATT ? 3 : 1][NGLL3_PAD];
   __shared__ float s_t[9][NGLL3_PAD];
+  // the bulk-copy builds keep the displacement / velocity rows in rows 0-5 of
+  // s_t (a barrier separates their last read from the first stress write): 3 KB
+  // less shared memory a CTA, so one CTA more fits an SM
+  constexpr bool kAlias = kBulkAtt;
+  __shared__ float s_uv_own[kAlias ? 1 : (ATT ? 6 : 3)][NGLL3_PAD];
+  float (*s_u)[NGLL3_PAD] = kAlias ? s_t : s_uv_own;
+  float (*s_v)[NGLL3_PAD] = kAlias ? s_t + 3 : s_uv_own + (ATT ? 3 : 0);
 
   const int t = threadIdx.x;
   const int e = a.phase ? __ldg(a.phase + blockIdx.x) : (int)blockIdx.x;
@@ -193,9 +198,10 @@ __global__ void __launch_bounds__(NGLL3_PAD, MINB) stiffness_kernel(const Stiffn
 
   // ---- gradient, strain, stress ---------------------------------------------
   float epsl[6] = {0.f, 0.f, 0.f, 0.f, 0.f, 0.f};
+  float t1x = 0.f, t2x = 0.f, t3x = 0.f, t1y = 0.f, t2y = 0.f, t3y = 0.f, t1z = 0.f, t2z = 0.f, t3z = 0.f;
+  float a1x = 0.f, a2x = 0.f, a3x = 0.f, a1y = 0.f, a2y = 0.f, a3y = 0.f, a1z = 0.f, a2z = 0.f, a3z = 0.f;
   if (active) {
     const float* hp = s_gll;  // hprime(i2,i1) = hp[i2 + 5 i1]
-    float t1x = 0.f, t2x = 0.f, t3x = 0.f, t1y = 0.f, t2y = 0.f, t3y = 0.f, t1z = 0.f, t2z = 0.f, t3z = 0.f;
 #pragma unroll
     for (int l = 0; l < NGLLX; ++l) {
       const float h1 = hp[i + NGLLX * l], h2 = hp[j + NGLLX * l], h3 = hp[k + NGLLX * l];
@@ -204,7 +210,7 @@ __global__ void __launch_bounds__(NGLL3_PAD, MINB) stiffness_kernel(const Stiffn
       t2x = fmaf(s_u[0][p2], h2, t2x); t2y = fmaf(s_u[1][p2], h2, t2y); t2z = fmaf(s_u[2][p2], h2, t2z);
       t3x = fmaf(s_u[0][p3], h3, t3x); t3y = fmaf(s_u[1][p3], h3, t3y); t3z = fmaf(s_u[2][p3], h3, t3z);
     }
-    float a1x = t1x, a2x = t2x, a3x = t3x, a1y = t1y, a2y = t2y, a3y = t3y, a1z = t1z, a2z = t2z, a3z = t3z;
+    a1x = t1x; a2x = t2x; a3x = t3x; a1y = t1y; a2y = t2y; a3y = t3y; a1z = t1z; a2z = t2z; a3z = t3z;
     if (ATT) {
 #pragma unroll
       for (int l = 0; l < NGLLX; ++l) {
@@ -215,6 +221,9 @@ __global__ void __launch_bounds__(NGLL3_PAD, MINB) stiffness_kernel(const Stiffn
         a3x = fmaf(s_v[0][p3], h3, a3x); a3y = fmaf(s_v[1][p3], h3, a3y); a3z = fmaf(s_v[2][p3], h3, a3z);
       }
     }
+  }
+  if (kAlias) __syncthreads();  // every read of s_u / s_v done: s_t may be written
+  if (active) {
     const float xr = a.xix_regular;
     const float xix = m[0], xiy = m[1], xiz = m[2], etax = m[3], etay = m[4], etaz = m[5];
     const float gammax = m[6], gammay = m[7], gammaz = m[8];
@@ -443,14 +452,14 @@ void launch_stiffness(const StiffnessArgs& a, bool att, bool store_strain, cudaS
                       int geom_format, bool staged, bool streaming, bool bulk) {
   if (a.nelem <= 0) return;
   if (bulk && geom_format == kGeomFP32) {
-    // 23.5 KB of shared memory and 72 / 64 / 56 registers a thread: 7, 8 or 9 CTAs/SM;
-    // without attenuation (nothing to stage, 10 KB) 8, 10 or 12 CTAs/SM
-    if (blocks_per_sm >= 9)
-      launch_minb<9, kGeomFP32, true, false, true, 12>(a, att, store_strain, s);
-    else if (blocks_per_sm == 8)
-      launch_minb<8, kGeomFP32, true, false, true, 10>(a, att, store_strain, s);
+    // 20.5 KB of shared memory and 64 / 56 / 48 registers a thread: 8, 9 or 10 CTAs/SM;
+    // without attenuation (nothing to stage) 8, 10 or 12 CTAs/SM
+    if (blocks_per_sm >= 10)
+      launch_minb<10, kGeomFP32, true, false, true, 12>(a, att, store_strain, s);
+    else if (blocks_per_sm == 9)
+      launch_minb<9, kGeomFP32, true, false, true, 10>(a, att, store_strain, s);
     else
-      launch_minb<7, kGeomFP32, true, false, true, 8>(a, att, store_strain, s);
+      launch_minb<8, kGeomFP32, true, false, true, 8>(a, att, store_strain, s);
     return;
   }
   if (geom_format != kGeomFP32 && bulk) {

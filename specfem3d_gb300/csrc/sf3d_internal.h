@@ -501,7 +501,7 @@ void launch_stiffness_pipelined(const StiffnessArgs& a, bool att, bool store_str
 //   10, 11: three threads per point (384-thread CTAs), 3 and 4 CTAs/SM;
 //   12, 13, 14: one CTA per element with the memory variables, strains and
 //   attenuation factors brought into shared memory by 14 bulk copies (one
-//   thread, one mbarrier) at 7, 8, 9 CTAs/SM (without attenuation: the plain
+//   thread, one mbarrier) at 8, 9, 10 CTAs/SM (without attenuation: the plain
 //   build at 8, 10, 12 CTAs/SM)
 // Under a packed geometry format (sf3d_set_geometry_format) 4 selects the packed
 // build at 7 CTAs/SM, 5, 6, 7 the packed builds with cp.async-staged memory
@@ -509,7 +509,7 @@ void launch_stiffness_pipelined(const StiffnessArgs& a, bool att, bool store_str
 // ones at 8, 9, 10, and every other variant the packed build at 6.
 constexpr int kNumStiffnessVariants = 15;
 inline int variant_blocks_per_sm(int v) {
-  const int t[kNumStiffnessVariants] = {4, 0, 5, 6, 7, 6, 7, 8, 6, 7, 3, 4, 7, 8, 9};
+  const int t[kNumStiffnessVariants] = {4, 0, 5, 6, 7, 6, 7, 8, 6, 7, 3, 4, 8, 9, 10};
   return (v >= 0 && v < kNumStiffnessVariants) ? t[v] : 4;
 }
 inline bool variant_staged(int v) { return v >= 5 && v <= 7; }

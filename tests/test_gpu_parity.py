@@ -69,7 +69,7 @@ def test_stiffness_variants_agree(gpulib, att):
     """All stiffness variants (one CTA per element at 4-7 CTAs/SM, the pipelined
     persistent kernel, the cp.async-staged builds at 6-8 CTAs/SM, the builds with
     evict-first hints, three threads per point, the bulk-copy-staged builds at
-    7-9 CTAs/SM) do the same
+    8-10 CTAs/SM) do the same
     arithmetic in the same order; the scatter-added acceleration differs
     only by the order of the atomic additions, the memory variables and strains
     at most by FMA contraction choices of the compiler."""
