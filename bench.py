@@ -329,29 +329,41 @@ def batch_leg(nshots: int, steps: int, nx: int = 64):
 
 def coupled_leg(steps: int):
     """GLL-point updates/s of the coupled fluid-solid workload (96x96x48 hexes, top sixth
-    water over a perturbed solid, pressure source, 256 hydrophones) through the per-call
-    entry points in the reference's order (acoustic and elastic predictors, fluid
-    stiffness, Sommerfeld faces, both coupling terms, sources, correctors, pressure
-    seismograms), wall clock with the device synchronised on both sides."""
+    water over a perturbed solid, pressure source, 256 hydrophones): device-resident
+    graph-captured steps (value), and the per-call entry points in the reference's order
+    (acoustic and elastic predictors, fluid stiffness, Sommerfeld faces, both coupling
+    terms, sources, correctors, pressure seismograms), wall clock with the device
+    synchronised on both sides (per_call)."""
     from specfem3d_gb300 import configs, meshgen
     from specfem3d_gb300.solver import GPUSolver
-    cfg = configs.coupled_fluid_solid(nstep=steps + 5)
+    cfg = configs.coupled_fluid_solid(nstep=2 * steps + 10)
     db = meshgen.build_database(cfg)
     g = GPUSolver(db, cfg)
-    variant, _ = g.autotune_stiffness()          # at rest, before the first step
+    variant, ms_var = g.autotune_stiffness()     # at rest, before the first step
     g.run_per_call(3)
     g.L.sf3d_synchronize(g.mp)
     t0 = time.perf_counter()
     g.run_per_call(steps)
     g.L.sf3d_synchronize(g.mp)
     dt = time.perf_counter() - t0
+    # the same steps device-resident: graph-captured blocks of sf3d_iterate_time
+    # (device stf table, pressure traces kept on the device), CUDA events
+    g.run(3, steps_per_graph=50)
+    with ClockSampler() as clk:
+        g.run(steps, steps_per_graph=50)
+    tm = g.last_timing()
     ok = bool(np.isfinite(g.seismograms()).all())
     nglob = int(db["nglob"])
     g.close()
-    return {"unit": UNIT, "value": nglob * steps / dt, "ms_per_step": 1000 * dt / steps, "steps": steps,
-            "nglob": nglob, "nspec": int(db["nspec"]), "fluid_elements": int(db["ispec_is_acoustic"].sum()),
-            "finite": ok, "stiffness_variant": stiffness_variant_name(variant, att=False),
-            "path": "per-call FC_FUNC_ entry points, host stf per step, pressure traces",
+    return {"unit": UNIT, "value": nglob * steps / (tm["total_ms"] / 1000.0), "ms_per_step": tm["total_ms"] / steps,
+            "path": "sf3d_iterate_time, graph-captured blocks of 50 steps, CUDA events", "clocks": clk.summary(),
+            "per_call": {"value": nglob * steps / dt, "ms_per_step": 1000 * dt / steps,
+                         "path": "per-call FC_FUNC_ entry points, host stf per step, pressure traces, wall clock "
+                                 "with the device synchronised on both sides"},
+            "steps": steps, "nglob": nglob, "nspec": int(db["nspec"]),
+            "fluid_elements": int(db["ispec_is_acoustic"].sum()), "finite": ok,
+            "stiffness_variant": stiffness_variant_name(variant, att=False),
+            "stiffness_ms_per_variant": [round(x, 4) for x in ms_var],
             "workload": "coupled fluid/solid 96x96x48 hexes, 20x20x10 km"}
 
 
@@ -457,6 +469,9 @@ def stiffness_variant_name(v: int, att: bool = True) -> str:
     without attenuation the staged builds have no memory variables to stage."""
     if v == 1:
         return "stiffness_pipe_kernel<att>" if att else "stiffness_pipe_kernel<no att>"
+    if v in (15, 16):
+        return (f"elem_pencil_kernel<no att, 5 elements per CTA, {8 if v == 15 else 7} CTAs/SM>" if not att else
+                "stiffness_kernel<att, 6 CTAs/SM>")
     ctas = [4, 0, 5, 6, 7, 6, 7, 8, 6, 7, 3, 4, 8, 9, 10][v] if att or v < 12 else [8, 10, 12][v - 12]
     kind = ("evict-first element streams" if v in (8, 9) else
             "3 threads per point" if v in (10, 11) else
@@ -468,7 +483,7 @@ def stiffness_variant_name(v: int, att: bool = True) -> str:
 
 
 REFERENCE_MAX_STEPS = 40
-STIFFNESS_VARIANTS = 15          # sf3d_autotune_stiffness writes one time per variant
+STIFFNESS_VARIANTS = 17          # sf3d_autotune_stiffness writes one time per variant
 SIMT_TFLOPS = 152 * 128 * 2 * 2.07e9 / 1e12
 
 

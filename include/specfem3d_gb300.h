@@ -361,7 +361,12 @@ int sf3d_last_timing(long *Mesh_pointer, float *stiffness_ms, int *stiffness_lau
  *               attenuation factors brought into shared memory by 14 bulk
  *               copies (one thread, one mbarrier with a bounded wait), for 8,
  *               9, 10 CTAs per SM (register budget 64, 56, 48); without
- *               attenuation the plain build at 8, 10, 12 CTAs per SM.
+ *               attenuation the plain build at 8, 10, 12 CTAs per SM;
+ *   15, 16:     without attenuation or strain storage, FP32 arrays: a thread per
+ *               (element, z-line) holding its five points in registers, five
+ *               elements per 125-thread CTA, for 8 and 7 CTAs per SM (register
+ *               budget 64, 72); every other case runs the default build
+ *               (variant 3) under these numbers.
  * Under a packed geometry format (sf3d_set_geometry_format) the variant picks
  * the packed build: 4 at 7 CTAs/SM; 5, 6, 7 with the memory variables and
  * strains staged by cp.async and the factors read from the element record, at
@@ -396,7 +401,7 @@ int sf3d_geometry_pack_info(long *Mesh_pointer, long *payload_rows, long *device
 /* Time every stiffness variant over `reps` full passes and keep the fastest.
  * Must run on a wavefield at rest (after prepare_fields_elastic_device, before
  * the first step): zero fields make the passes leave every array unchanged;
- * returns SF3D_ERR_STATE otherwise.  ms_per_variant (15 floats) and
+ * returns SF3D_ERR_STATE otherwise.  ms_per_variant (17 floats) and
  * best_variant may be NULL.  No reference counterpart. */
 int sf3d_autotune_stiffness(long *Mesh_pointer, int reps, float *ms_per_variant, int *best_variant);
 

@@ -464,6 +464,27 @@ struct StiffnessArgs {
 
 void launch_stiffness(const StiffnessArgs& a, bool att, bool store_strain, cudaStream_t s, int blocks_per_sm,
                       int geom_format = kGeomFP32, bool staged = false, bool streaming = false, bool bulk = false);
+// one wavefield without attenuation, register-blocked pencils (sf3d_elastic_pencil.cu):
+// five elements per CTA, a thread per (element, z-line), 8 or 7 CTAs/SM
+struct ElemPencilArgs {
+  int nelem;
+  const int* phase;             // element list (0-based) or nullptr (identity)
+  const int* ibool;
+  const int* irregular;
+  const float* m[9];
+  const float* kappav;
+  const float* muv;
+  const float* gll;             // hprime, hprimewgll, wxy, wxz, wyz
+  float xix_regular;
+  float jacobian_regular;
+  const float* displ;
+  float* accel;
+  float hp[NGLL2];              // hprime, hprimewgll by value (parameter bank)
+  float hpw[NGLL2];
+};
+bool launch_elem_pencil(const ElemPencilArgs& a, int blocks_per_sm, cudaStream_t s);
+struct Mesh;
+void run_elem_pencil(Mesh* mp, const StiffnessArgs& a, int blocks_per_sm, cudaStream_t s);
 // batched-shots stiffness with register-blocked pencils (sf3d_batch_pencil.cu):
 // elements of a phase list x shots [shot_offset, shot_offset + shot_tiles * lanes)
 // of fields stacked shot-innermost with nshots shots per point
@@ -507,11 +528,15 @@ void launch_stiffness_pipelined(const StiffnessArgs& a, bool att, bool store_str
 // build at 7 CTAs/SM, 5, 6, 7 the packed builds with cp.async-staged memory
 // variables at 8, 9, 10 CTAs/SM, 12, 13, 14 the packed builds with bulk-copied
 // ones at 8, 9, 10, and every other variant the packed build at 6.
-constexpr int kNumStiffnessVariants = 15;
+constexpr int kNumStiffnessVariants = 17;
 inline int variant_blocks_per_sm(int v) {
-  const int t[kNumStiffnessVariants] = {4, 0, 5, 6, 7, 6, 7, 8, 6, 7, 3, 4, 8, 9, 10};
+  // 15, 16: the register-blocked pencil kernel without attenuation (five
+  // elements a CTA, 8 and 7 CTAs/SM); the other builds (attenuation, strain,
+  // packed or anisotropic streams) run the default 6-CTA build under these numbers
+  const int t[kNumStiffnessVariants] = {4, 0, 5, 6, 7, 6, 7, 8, 6, 7, 3, 4, 8, 9, 10, 6, 6};
   return (v >= 0 && v < kNumStiffnessVariants) ? t[v] : 4;
 }
+inline bool variant_pencil(int v) { return v == 15 || v == 16; }
 inline bool variant_staged(int v) { return v >= 5 && v <= 7; }
 inline bool variant_bulk(int v) { return v >= 12 && v <= 14; }
 inline bool variant_streaming(int v) { return v == 8 || v == 9; }
@@ -586,6 +611,8 @@ inline void run_stiffness(Mesh* mp, const StiffnessArgs& a, bool att, bool store
       launch_stiffness(h, att, store_strain, s, v - 4, mp->geom_format, true, false, true);
     else
       launch_stiffness(h, att, store_strain, s, v == 4 ? 7 : 6, mp->geom_format);
+  } else if (variant_pencil(mp->stiffness_variant) && !att && !store_strain) {
+    run_elem_pencil(mp, a, mp->stiffness_variant == 15 ? 8 : 7, s);
   } else if (mp->stiffness_variant == 1 && mp->d_kerr) {
     launch_stiffness_pipelined(a, att, store_strain, mp->d_kerr, s);
   } else if (variant_split(mp->stiffness_variant)) {

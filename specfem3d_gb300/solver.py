@@ -20,6 +20,7 @@ from . import abi
 
 NGLL3 = 125
 N_SLS = 3
+NUM_STIFFNESS_VARIANTS = 17       # sf3d_set_stiffness_variant accepts 0 .. 16
 
 
 # the 21 anisotropic moduli per GLL point, in the order prepare_fields_elastic_device takes them
@@ -386,14 +387,14 @@ class GPUSolver:
         abi.check()
 
     def set_stiffness_variant(self, variant: int):
-        """Stiffness kernel build (sf3d_set_stiffness_variant: 0-14; 3 is the default)."""
+        """Stiffness kernel build (sf3d_set_stiffness_variant: 0-16; 3 is the default)."""
         if self.L.sf3d_set_stiffness_variant(self.mp, int(variant)) != 0:
             abi.check()
 
     def autotune_stiffness(self, reps: int = 3):
         """Time every stiffness variant on the wavefield at rest (before the first
         step) and keep the fastest; returns (variant, ms per variant)."""
-        ms = (ctypes.c_float * 15)()
+        ms = (ctypes.c_float * NUM_STIFFNESS_VARIANTS)()
         best = ctypes.c_int()
         if self.L.sf3d_autotune_stiffness(self.mp, int(reps), ms, ctypes.addressof(best)) != 0:
             abi.check()

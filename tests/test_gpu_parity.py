@@ -34,8 +34,12 @@ def _solver(db, cfg, **kw):
     return solver.GPUSolver(db, cfg, **kw)
 
 
-@pytest.mark.parametrize("att", [False, True])
-def test_stiffness_pass_random_fields(gpulib, att):
+@pytest.mark.parametrize("att,variant", [(False, None), (True, None), (False, 15), (False, 16)])
+def test_stiffness_pass_random_fields(gpulib, att, variant):
+    """One stiffness pass on random fields against the FP32 oracle: the default
+    build with and without attenuation, and the register-blocked pencil kernel
+    (variants 15, 16: five elements a CTA at 8 and 7 CTAs/SM; every element of
+    the layered mesh is irregular, so the metric path runs)."""
     from specfem3d_gb300 import configs, meshgen
     cfg = configs.small_layered(nstep=4, attenuation=att)
     db = meshgen.build_database(cfg)
@@ -45,6 +49,8 @@ def test_stiffness_pass_random_fields(gpulib, att):
     v = rng.standard_normal(n3).astype(np.float32) * 1e-2
     a = np.zeros(n3, np.float32)
     g = _solver(db, cfg)
+    if variant is not None:
+        g.set_stiffness_variant(variant)
     g.set_fields(d, v, a)
     g.forces_only()
     _, _, acc_gpu = g.fields()
@@ -64,24 +70,33 @@ def test_stiffness_pass_random_fields(gpulib, att):
     g.close()
 
 
-@pytest.mark.parametrize("att", [False, True])
-def test_stiffness_variants_agree(gpulib, att):
+@pytest.mark.parametrize("att,mesh", [(False, "layered"), (True, "layered"), (False, "regular")])
+def test_stiffness_variants_agree(gpulib, att, mesh):
     """All stiffness variants (one CTA per element at 4-7 CTAs/SM, the pipelined
     persistent kernel, the cp.async-staged builds at 6-8 CTAs/SM, the builds with
     evict-first hints, three threads per point, the bulk-copy-staged builds at
-    8-10 CTAs/SM) do the same
+    8-10 CTAs/SM, without attenuation the register-blocked pencil kernel) do the same
     arithmetic in the same order; the scatter-added acceleration differs
     only by the order of the atomic additions, the memory variables and strains
-    at most by FMA contraction choices of the compiler."""
-    from specfem3d_gb300 import configs, meshgen
-    cfg = configs.small_layered(nx=9, ny=7, counts=(3, 3, 4), nstep=4, attenuation=att)
-    db = meshgen.build_database(cfg)
+    at most by FMA contraction choices of the compiler.  Meshes: the layered block
+    (every element irregular) and a perturbed block of cubes (every element
+    regular, moduli varying per point; 324 elements, so the pencil kernel's last
+    CTA holds 4 of its 5 elements)."""
+    from specfem3d_gb300 import configs, gradient as G, meshgen
+    if mesh == "layered":
+        cfg = configs.small_layered(nx=9, ny=7, counts=(3, 3, 4), nstep=4, attenuation=att)
+        db = meshgen.build_database(cfg)
+    else:
+        cfg = configs.small_adjoint(nstep=4, nshots=1, n=9)
+        db = meshgen.build_database(cfg, material=G.background_material(cfg))
+        assert db["nspec"] == 324 and db["nspec_irregular"] == 0
     rng = np.random.default_rng(5)
     n3 = 3 * db["nglob"]
     d = rng.standard_normal(n3).astype(np.float32) * 1e-3
     v = rng.standard_normal(n3).astype(np.float32) * 1e-2
     out = []
-    for variant in range(15):
+    from specfem3d_gb300.solver import NUM_STIFFNESS_VARIANTS
+    for variant in range(NUM_STIFFNESS_VARIANTS):
         g = _solver(db, cfg)
         g.set_stiffness_variant(variant)
         g.set_fields(d, v, np.zeros(n3, np.float32))
@@ -91,7 +106,7 @@ def test_stiffness_variants_agree(gpulib, att):
         mem = g.memory_variables() if att else None
         out.append((acc, mem))
         g.close()
-    for v in range(1, 15):
+    for v in range(1, NUM_STIFFNESS_VARIANTS):
         assert rel_l2(out[v][0], out[0][0]) < 1e-6, v
         if att:
             same = []
