@@ -407,9 +407,12 @@ void launch_pressure_seismograms(Mesh* mp, int slot) {
 int enqueue_acoustic_step(Mesh* mp, float dt, float dt2, float dtsq2) {
   cudaStream_t s = mp->stream;
   int launches = 0;
-  const long n = mp->nglob;
-  predictor_scalar_kernel<<<nblk(n, 256), 256, 0, s>>>(mp->d_potential, mp->d_potential_dot, mp->d_potential_dot_dot,
-                                                        n, dt, dt2, dtsq2);
+  // the fluid elements' points only, when their span is known: the potentials
+  // are zero at points of solid elements alone, and no kernel writes them there
+  const long g0 = mp->ac_count >= 0 ? mp->ac_first : 0;
+  const long n = mp->ac_count >= 0 ? mp->ac_count : mp->nglob;
+  predictor_scalar_kernel<<<nblk(n, 256), 256, 0, s>>>(mp->d_potential + g0, mp->d_potential_dot + g0,
+                                                        mp->d_potential_dot_dot + g0, n, dt, dt2, dtsq2);
   ++launches;
   const long nfs = (long)mp->num_free_surface_faces * NGLL2;
   if (nfs > 0) {
@@ -454,8 +457,8 @@ int enqueue_acoustic_step(Mesh* mp, float dt, float dt2, float dtsq2) {
                                                                 mp->d_stf_table, mp->d_it, mp->stf_nstep);
     ++launches;
   }
-  mass_corrector_scalar_kernel<<<nblk(n, 256), 256, 0, s>>>(mp->d_potential_dot, mp->d_potential_dot_dot,
-                                                            mp->d_rmass_acoustic, n, dt2);
+  mass_corrector_scalar_kernel<<<nblk(n, 256), 256, 0, s>>>(mp->d_potential_dot + g0, mp->d_potential_dot_dot + g0,
+                                                            mp->d_rmass_acoustic + g0, n, dt2);
   ++launches;
   if (nfs > 0) {
     free_surface_kernel<<<nblk(nfs, 128), 128, 0, s>>>(mp->num_free_surface_faces, mp->d_fs_ispec, mp->d_fs_pt,

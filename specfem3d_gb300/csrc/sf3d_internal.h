@@ -347,6 +347,11 @@ struct Mesh {
   // device step counter for graph-captured time loops, and completion counter
   int* d_it = nullptr;
   unsigned int* d_done = nullptr;
+  // fluid-solid meshes: the global points (0-based, first and count) spanned by
+  // the solid and by the fluid elements; the fused time loop runs the solid and
+  // fluid predictor/corrector passes over these spans only (count -1: not
+  // computed, the passes cover every point)
+  long el_first = 0, el_count = -1, ac_first = 0, ac_count = -1;
   float* d_scratch = nullptr;             // reduction scratch
   int* d_kerr = nullptr;                  // kernel error word (bounded waits that timed out)
   GradState* grad = nullptr;              // checkpointed adjoint gradient (optional)
@@ -631,6 +636,8 @@ int enqueue_pressure_seismograms(Mesh* mp);
 // one fused forward elastic step of sf3d_iterate_time (predictor fused with the
 // previous corrector unless first_step); returns the number of launches
 int enqueue_step(Mesh* mp, float dt, float dt2, float dtsq2, bool first_step, cudaEvent_t* ev);
+// fills Mesh::el_first/el_count/ac_first/ac_count from ibool (synchronises the stream)
+bool compute_point_spans(Mesh* mp);
 void launch_stacey(Mesh* mp, const float* veloc, float* accel, cudaStream_t s);
 void launch_set_it(Mesh* mp, int it, cudaStream_t s);
 void launch_mass_corrector(Mesh* mp, float dt2, cudaStream_t s);

@@ -10,6 +10,7 @@
 // predictor of step n into one streaming pass, reads the step index from device
 // memory, and captures blocks of steps into CUDA graphs, so a step costs a few
 // graph nodes and no host round trip.
+#include <limits.h>
 #include <math.h>
 #include <string.h>
 
@@ -75,6 +76,17 @@ __global__ void corrector_predictor_kernel(float* __restrict__ d, float* __restr
   d[i] = d[i] + dt * vh + dtsq2 * ac;
   v[i] = vh + dt2 * ac;
   a[i] = 0.f;
+}
+
+// lowest and highest global point (0-based) of the solid elements (out[0],
+// out[1]) and of the fluid elements (out[2], out[3])
+__global__ void point_span_kernel(const int* __restrict__ ibool, const int* __restrict__ is_ac, int* out) {
+  const int t = threadIdx.x;
+  if (t >= NGLL3) return;
+  const int g = __ldg(ibool + (long)blockIdx.x * NGLL3_PAD + t);
+  const int k = (is_ac && __ldg(is_ac + blockIdx.x)) ? 2 : 0;
+  atomicMin(out + k, g);
+  atomicMax(out + k + 1, g);
 }
 
 // Stacey absorbing traction (compute_stacey_viscoelastic.F90:90-130,
@@ -375,13 +387,23 @@ int enqueue_step(Mesh* mp, float dt, float dt2, float dtsq2, bool first_step, cu
     predictor_kernel<<<nblk(n, 256), 256, 0, s>>>(F.displ, F.veloc, F.accel, n, dt, dt2, dtsq2);
     launch_pml_displ(mp, true, dt2, dtsq2, s);
     launches += 2;
-  } else if (first_step) {
-    const long n = 3L * mp->nglob;
-    predictor_kernel<<<nblk(n, 256), 256, 0, s>>>(F.displ, F.veloc, F.accel, n, dt, dt2, dtsq2);
   } else {
-    corrector_predictor_kernel<<<nblk(3L * mp->nglob, 256), 256, 0, s>>>(F.displ, F.veloc, F.accel, mp->d_rmassx,
-                                                                    mp->d_rmassy, mp->d_rmassz, mp->nglob, dt, dt2,
+    // the solid's points only, when the fluid elements' span is known: the
+    // solid fields are zero at points of fluid elements alone, and no kernel
+    // writes them there
+    const long g0 = mp->el_count >= 0 ? mp->el_first : 0;
+    const long ng = mp->el_count >= 0 ? mp->el_count : mp->nglob;
+    if (ng == 0) {
+      --launches;   // no solid element: nothing to advance
+    } else if (first_step) {
+      predictor_kernel<<<nblk(3 * ng, 256), 256, 0, s>>>(F.displ + 3 * g0, F.veloc + 3 * g0, F.accel + 3 * g0,
+                                                          3 * ng, dt, dt2, dtsq2);
+    } else {
+      corrector_predictor_kernel<<<nblk(3 * ng, 256), 256, 0, s>>>(F.displ + 3 * g0, F.veloc + 3 * g0,
+                                                                    F.accel + 3 * g0, mp->d_rmassx + g0,
+                                                                    mp->d_rmassy + g0, mp->d_rmassz + g0, ng, dt, dt2,
                                                                     dtsq2);
+    }
   }
   ++launches;
   // fluid domain: its whole step (it reads the solid displacement just predicted)
@@ -427,6 +449,25 @@ int enqueue_step(Mesh* mp, float dt, float dt2, float dtsq2, bool first_step, cu
   }
   ++launches;
   return launches;
+}
+
+bool compute_point_spans(Mesh* mp) {
+  int* d = nullptr;
+  const int init[4] = {INT_MAX, -1, INT_MAX, -1};
+  int h[4];
+  bool ok = cuda_ok(cudaMalloc(&d, sizeof(init)), "cudaMalloc") &&
+            copy_sync(d, init, sizeof(init), cudaMemcpyHostToDevice, mp->stream);
+  if (ok) {
+    point_span_kernel<<<(unsigned)mp->nspec, NGLL3_PAD, 0, mp->stream>>>(mp->d_ibool, mp->d_ispec_is_acoustic, d);
+    ok = copy_sync(h, d, sizeof(h), cudaMemcpyDeviceToHost, mp->stream);
+  }
+  cudaFree(d);
+  if (!ok) return false;
+  mp->el_first = h[1] >= 0 ? h[0] : 0;
+  mp->el_count = h[1] >= 0 ? h[1] - h[0] + 1 : 0;
+  mp->ac_first = h[3] >= 0 ? h[2] : 0;
+  mp->ac_count = h[3] >= 0 ? h[3] - h[2] + 1 : 0;
+  return true;
 }
 
 // Stacey traction of a velocity-like field into an acceleration-like buffer.
@@ -732,6 +773,7 @@ int sf3d_iterate_time(long* Mesh_pointer, int it_begin, int it_end, realw deltat
     }
   }
   cudaStream_t s = mp->stream;
+  if (mp->has_acoustic && mp->el_count < 0 && !mp->pml && !compute_point_spans(mp)) return SF3D_ERR_CUDA;
   set_it_kernel<<<1, 1, 0, s>>>(mp->d_it, it_begin);
   SF3D_CUDA_RET(cudaMemsetAsync(mp->d_done, 0, sizeof(unsigned int), s), SF3D_ERR_CUDA);
   SF3D_CUDA_RET(cudaEventRecord(mp->ev0, s), SF3D_ERR_CUDA);
@@ -762,8 +804,16 @@ int sf3d_iterate_time(long* Mesh_pointer, int it_begin, int it_end, realw deltat
     cudaGraphDestroy(graph);
   }
   while (remaining > 0) { step(false); --remaining; }
-  mass_corrector_kernel<<<nblk(3L * mp->nglob, 256), 256, 0, s>>>(mp->f.veloc, mp->f.accel, mp->d_rmassx, mp->d_rmassy,
-                                                             mp->d_rmassz, mp->nglob, dt2);
+  {
+    const long g0 = mp->el_count >= 0 ? mp->el_first : 0;
+    const long ng = mp->el_count >= 0 ? mp->el_count : mp->nglob;
+    if (ng > 0)
+      mass_corrector_kernel<<<nblk(3 * ng, 256), 256, 0, s>>>(mp->f.veloc + 3 * g0, mp->f.accel + 3 * g0,
+                                                              mp->d_rmassx + g0, mp->d_rmassy + g0,
+                                                              mp->d_rmassz + g0, ng, dt2);
+    else
+      --launches;
+  }
   ++launches;
   SF3D_CUDA_RET(cudaEventRecord(mp->ev1, s), SF3D_ERR_CUDA);
   SF3D_CUDA_RET(cudaEventSynchronize(mp->ev1), SF3D_ERR_CUDA);

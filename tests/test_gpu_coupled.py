@@ -53,6 +53,17 @@ def test_coupled_fused_loop_equals_per_call(gpulib):
     assert np.abs(s1[:, 0]).max() > 0
     assert rel_l2(s2[:, 0], s1[:, 0]) < 5e-5
     assert rel_l2(p2, p1) < 5e-5 and rel_l2(d2, d1) < 5e-5
+    # the fused loop advances the solid fields over the solid elements' span of
+    # points and the potentials over the fluid elements' span: outside its own
+    # elements each field stays exactly zero, as in the per-call path
+    ib = np.asarray(db["ibool"]).reshape(db["nspec"], -1) - 1
+    isac = np.asarray(db["ispec_is_acoustic"]).astype(bool)
+    fluid_only = np.setdiff1d(np.unique(ib[isac]), np.unique(ib[~isac]))
+    solid_only = np.setdiff1d(np.unique(ib[~isac]), np.unique(ib[isac]))
+    assert len(fluid_only) > 0 and len(solid_only) > 0
+    assert not np.any(p1[solid_only]) and not np.any(p2[solid_only])
+    d1p, d2p = d1.reshape(-1, 3), d2.reshape(-1, 3)
+    assert not np.any(d1p[fluid_only]) and not np.any(d2p[fluid_only])
 
 
 def test_fluid_receiver_vector_seismograms_vs_oracle(gpulib):
