@@ -48,8 +48,12 @@ bool ac_field(Mesh* mp, const int* fa, AcField* F) {
 }
 
 // chi_dot_dot -= w . hprimewgll^T ( J/rho grad(xi) . grad chi )
-// (compute_forces_acoustic.F90:130-340); one 128-thread CTA per element.
-__global__ void __launch_bounds__(NGLL3_PAD, 8)
+// (compute_forces_acoustic.F90:130-340); one 128-thread CTA per element.  An
+// element moves 1 KB (ibool, rho) and its gather depends on ibool, so the
+// kernel is bound by that load chain: it is compiled for 16 resident CTAs per
+// SM (32 registers, no spills), which took the fluid pass of the coupled
+// 96x96x48 step from about 150 to 115 us against 8 CTAs/SM.
+__global__ void __launch_bounds__(NGLL3_PAD, 16)
     acoustic_stiffness_kernel(int nelem, const int* __restrict__ phase, const int* __restrict__ ibool,
                               const int* __restrict__ irregular, const float* __restrict__ m0,
                               const float* __restrict__ m1, const float* __restrict__ m2, const float* __restrict__ m3,
