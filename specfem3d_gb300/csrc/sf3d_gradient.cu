@@ -109,6 +109,26 @@ __global__ void adj_update_kernel(float* __restrict__ uh, float* __restrict__ vh
   bp[i] = 0.f;
 }
 
+// The same update when K p and B p were scatter-added straight into the adjoint
+// fields (uh already holds uh - kp, vh holds vh - bp): vh and p of the previous
+// step, no accumulators to read or clear.
+__global__ void adj_update_direct_kernel(const float* __restrict__ uh, float* __restrict__ vh,
+                                         float* __restrict__ p, const float* __restrict__ rmx,
+                                         const float* __restrict__ rmy, const float* __restrict__ rmz, long nglob,
+                                         float dt, float dt2, float dtsq2) {
+  const long i = (long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= 3 * nglob) return;
+  const float ut = uh[i];
+  const float vt = vh[i];
+  const float vn = dt * ut + vt;
+  const float an = dtsq2 * ut + dt2 * vt;
+  vh[i] = vn;
+  const long g = i / 3;
+  const int c = (int)(i - 3 * g);
+  const float rm = c == 0 ? __ldg(rmx + g) : (c == 1 ? __ldg(rmy + g) : __ldg(rmz + g));
+  p[i] = -rm * (an + dt2 * vn);
+}
+
 struct GradArgs {
   int nelem;
   const int* phase;
@@ -130,7 +150,8 @@ struct GradArgs {
   double* g_mu;
   const float* kappav; // fused form: moduli and the K p accumulator
   const float* muv;
-  float* kp;
+  float* kp;           // K p scatter target, kp_sign times the force: -1 into the
+  float kp_sign;       // kp accumulator, +1 straight into the adjoint displacement
   int* err;            // kernel error word (a bounded wait that timed out)
 };
 
@@ -373,9 +394,9 @@ __global__ void __launch_bounds__(NGLL3_PAD, 10) adj_stiffness_grad_kernel(const
     const float fac1 = s_gll[4 * NGLL2 + j + NGLLX * k];
     const float fac2 = s_gll[3 * NGLL2 + i + NGLLX * k];
     const float fac3 = s_gll[2 * NGLL2 + i + NGLLX * j];
-    atomicAdd(a.kp + 3L * g, -(fac1 * n1x + fac2 * n2x + fac3 * n3x));
-    atomicAdd(a.kp + 3L * g + 1, -(fac1 * n1y + fac2 * n2y + fac3 * n3y));
-    atomicAdd(a.kp + 3L * g + 2, -(fac1 * n1z + fac2 * n2z + fac3 * n3z));
+    atomicAdd(a.kp + 3L * g, a.kp_sign * (fac1 * n1x + fac2 * n2x + fac3 * n3x));
+    atomicAdd(a.kp + 3L * g + 1, a.kp_sign * (fac1 * n1y + fac2 * n2y + fac3 * n3y));
+    atomicAdd(a.kp + 3L * g + 2, a.kp_sign * (fac1 * n1z + fac2 * n2z + fac3 * n3z));
   }
   // a bulk copy still in flight must land before the CTA's shared memory is
   // released: wait once more, with the same bound
@@ -437,9 +458,14 @@ void adjoint_step(Mesh* mp, int n, const float* u, const float* araw, float dt, 
     adj_residual_kernel<<<mp->nrec_local, NGLL3_PAD, 0, s>>>(mp->nrec_local, mp->d_ispec_rec, mp->d_hxir,
                                                              mp->d_hetar, mp->d_hgammar, mp->d_nu_rec, mp->d_ibool,
                                                              G->residual, n, G->adj_u);
-  // p, kp, bp of this step were produced by the previous transposed step (or the
-  // start of the sweep)
-  launch_stacey(mp, G->p, G->bp, s);
+  // p (and with the separate kernels kp, bp) of this step were produced by the
+  // previous transposed step (or the start of the sweep).  The fused kernel adds
+  // B p and K p straight into the adjoint velocity and displacement: they are
+  // read only by the update below, so its kp and bp reads and clears go away.
+  if (G->fused)
+    launch_stacey(mp, G->p, G->adj_v, s, 1.f);
+  else
+    launch_stacey(mp, G->p, G->bp, s);
   Fields tmp;
   tmp.displ = G->p;
   tmp.veloc = G->p;
@@ -471,15 +497,20 @@ void adjoint_step(Mesh* mp, int n, const float* u, const float* araw, float dt, 
     ga.g_mu = G->g_mu;
     ga.kappav = mp->d_kappav;
     ga.muv = mp->d_muv;
-    ga.kp = G->kp;
+    ga.kp = G->fused ? G->adj_u : G->kp;
+    ga.kp_sign = G->fused ? 1.f : -1.f;
     ga.err = mp->d_kerr;
     if (G->fused)
       adj_stiffness_grad_kernel<<<a.nelem, NGLL3_PAD, 0, s>>>(ga);
     else
       grad_accum_kernel<<<a.nelem, NGLL3_PAD, 0, s>>>(ga);
   }
-  adj_update_kernel<<<nblk(n3, 256), 256, 0, s>>>(G->adj_u, G->adj_v, G->kp, G->bp, G->p, mp->d_rmassx,
-                                                  mp->d_rmassy, mp->d_rmassz, mp->nglob, dt, dt2, dtsq2);
+  if (G->fused)
+    adj_update_direct_kernel<<<nblk(n3, 256), 256, 0, s>>>(G->adj_u, G->adj_v, G->p, mp->d_rmassx, mp->d_rmassy,
+                                                           mp->d_rmassz, mp->nglob, dt, dt2, dtsq2);
+  else
+    adj_update_kernel<<<nblk(n3, 256), 256, 0, s>>>(G->adj_u, G->adj_v, G->kp, G->bp, G->p, mp->d_rmassx,
+                                                    mp->d_rmassy, mp->d_rmassz, mp->nglob, dt, dt2, dtsq2);
 }
 
 }  // namespace

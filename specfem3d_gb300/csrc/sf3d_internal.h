@@ -638,7 +638,9 @@ int enqueue_pressure_seismograms(Mesh* mp);
 int enqueue_step(Mesh* mp, float dt, float dt2, float dtsq2, bool first_step, cudaEvent_t* ev);
 // fills Mesh::el_first/el_count/ac_first/ac_count from ibool (synchronises the stream)
 bool compute_point_spans(Mesh* mp);
-void launch_stacey(Mesh* mp, const float* veloc, float* accel, cudaStream_t s);
+// accel += sign * (Stacey traction of veloc) on the absorbing faces (sign -1:
+// the force of the absorbing boundary)
+void launch_stacey(Mesh* mp, const float* veloc, float* accel, cudaStream_t s, float sign = -1.f);
 void launch_set_it(Mesh* mp, int it, cudaStream_t s);
 void launch_mass_corrector(Mesh* mp, float dt2, cudaStream_t s);
 StiffnessArgs stiffness_args(Mesh* mp, Fields& F, int iphase, float deltat, bool att, bool strain, bool backward);

@@ -96,7 +96,7 @@ __global__ void stacey_kernel(int nfaces, const int* __restrict__ abs_ispec, con
                               const int* __restrict__ ibool, const float* __restrict__ rho_vp,
                               const float* __restrict__ rho_vs, const float* __restrict__ veloc,
                               float* __restrict__ accel, float* __restrict__ record,
-                              const int* __restrict__ is_acoustic) {
+                              const int* __restrict__ is_acoustic, float sign = -1.f) {
   long idx = (long)blockIdx.x * blockDim.x + threadIdx.x;
   if (idx >= (long)nfaces * NGLL2) return;
   const int f = (int)(idx / NGLL2);
@@ -112,9 +112,9 @@ __global__ void stacey_kernel(int nfaces, const int* __restrict__ abs_ispec, con
   const float ty = rvp * vn * ny + rvs * (vy - vn * ny);
   const float tz = rvp * vn * nz + rvs * (vz - vn * nz);
   const float w = jw[idx];
-  atomicAdd(accel + 3L * g, -tx * w);
-  atomicAdd(accel + 3L * g + 1, -ty * w);
-  atomicAdd(accel + 3L * g + 2, -tz * w);
+  atomicAdd(accel + 3L * g, sign * tx * w);
+  atomicAdd(accel + 3L * g + 1, sign * ty * w);
+  atomicAdd(accel + 3L * g + 2, sign * tz * w);
   if (record) {
     record[3 * idx] = tx * w;
     record[3 * idx + 1] = ty * w;
@@ -471,12 +471,12 @@ bool compute_point_spans(Mesh* mp) {
 }
 
 // Stacey traction of a velocity-like field into an acceleration-like buffer.
-void launch_stacey(Mesh* mp, const float* veloc, float* accel, cudaStream_t s) {
+void launch_stacey(Mesh* mp, const float* veloc, float* accel, cudaStream_t s, float sign) {
   if (!mp->stacey || mp->num_abs_faces == 0) return;
   const long n = (long)mp->num_abs_faces * NGLL2;
   stacey_kernel<<<nblk(n, 128), 128, 0, s>>>(mp->num_abs_faces, mp->d_abs_ispec, mp->d_abs_pt, mp->d_abs_normal,
                                               mp->d_abs_jw, mp->d_ibool, mp->d_rho_vp, mp->d_rho_vs, veloc, accel,
-                                              nullptr, mp->d_ispec_is_acoustic);
+                                              nullptr, mp->d_ispec_is_acoustic, sign);
 }
 
 void launch_set_it(Mesh* mp, int it, cudaStream_t s) { set_it_kernel<<<1, 1, 0, s>>>(mp->d_it, it); }
