@@ -678,11 +678,20 @@ int sf3d_gradient_backward(long* Mesh_pointer, realw deltat) {
     else
       load_state(mp, G->ckpt + (size_t)(j - 1) * 3 * n3, s);
     launch_set_it(mp, n0 + 1, s);
+    // each recomputed step writes its displacement and force straight into the
+    // segment's buffers (and reads the previous step's from there)
+    float* const base_d = mp->f.displ;
+    float* const base_a = mp->f.accel;
     for (int q = 0; q < len; ++q) {
-      enqueue_step(mp, dt, dt2, dtsq2, j == 0 && q == 0, nullptr);
-      cudaMemcpyAsync(G->seg_u + (size_t)q * n3, mp->f.displ, sizeof(float) * n3, cudaMemcpyDeviceToDevice, s);
-      cudaMemcpyAsync(G->seg_a + (size_t)q * n3, mp->f.accel, sizeof(float) * n3, cudaMemcpyDeviceToDevice, s);
+      StepIO io;
+      io.d_in = q == 0 ? base_d : G->seg_u + (size_t)(q - 1) * n3;
+      io.d_out = G->seg_u + (size_t)q * n3;
+      io.a_in = q == 0 ? base_a : G->seg_a + (size_t)(q - 1) * n3;
+      io.a_out = G->seg_a + (size_t)q * n3;
+      enqueue_step(mp, dt, dt2, dtsq2, j == 0 && q == 0, nullptr, &io);
     }
+    mp->f.displ = base_d;
+    mp->f.accel = base_a;
     for (int q = len - 1; q >= 0; --q)
       adjoint_step(mp, n0 + q, G->seg_u + (size_t)q * n3, G->seg_a + (size_t)q * n3, dt, dt2, dtsq2);
     if (!cuda_ok(cudaGetLastError(), "sf3d_gradient_backward")) return SF3D_ERR_CUDA;

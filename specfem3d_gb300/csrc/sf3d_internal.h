@@ -635,7 +635,15 @@ int enqueue_coupling_el_ac(Mesh* mp);
 int enqueue_pressure_seismograms(Mesh* mp);
 // one fused forward elastic step of sf3d_iterate_time (predictor fused with the
 // previous corrector unless first_step); returns the number of launches
-int enqueue_step(Mesh* mp, float dt, float dt2, float dtsq2, bool first_step, cudaEvent_t* ev);
+// out-of-place displacement / force buffers of one step (the gradient's reverse sweep)
+struct StepIO {
+  const float* d_in;
+  float* d_out;
+  const float* a_in;
+  float* a_out;
+};
+int enqueue_step(Mesh* mp, float dt, float dt2, float dtsq2, bool first_step, cudaEvent_t* ev,
+                 const StepIO* io = nullptr);
 // fills Mesh::el_first/el_count/ac_first/ac_count from ibool (synchronises the stream)
 bool compute_point_spans(Mesh* mp);
 // accel += sign * (Stacey traction of veloc) on the absorbing faces (sign -1:

@@ -36,6 +36,37 @@ __global__ void predictor_kernel(float* __restrict__ d, float* __restrict__ v, f
   a[i] = 0.f;
 }
 
+// The predictor (first step) and the corrector/predictor with the displacement
+// written to a buffer of its own and the force left in place: the reverse sweep
+// of the checkpointed gradient keeps every step's displacement and force of a
+// segment, and these forms let the step write them where they are kept instead
+// of copying them there afterwards.  Same arithmetic as predictor_kernel and
+// corrector_predictor_kernel.
+__global__ void predictor_oop_kernel(const float* __restrict__ d_in, float* __restrict__ d_out,
+                                     float* __restrict__ v, const float* __restrict__ a, long n, float dt, float dt2,
+                                     float dtsq2) {
+  long i = (long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  const float ai = a[i], vi = v[i];
+  d_out[i] = d_in[i] + dt * vi + dtsq2 * ai;
+  v[i] = vi + dt2 * ai;
+}
+__global__ void corrector_predictor_oop_kernel(const float* __restrict__ d_in, float* __restrict__ d_out,
+                                               float* __restrict__ v, const float* __restrict__ a,
+                                               const float* __restrict__ rmx, const float* __restrict__ rmy,
+                                               const float* __restrict__ rmz, long nglob, float dt, float dt2,
+                                               float dtsq2) {
+  const long i = (long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= 3 * nglob) return;
+  const long g = i / 3;
+  const int c = (int)(i - 3 * g);
+  const float rm = c == 0 ? __ldg(rmx + g) : (c == 1 ? __ldg(rmy + g) : __ldg(rmz + g));
+  const float ac = a[i] * rm;
+  const float vh = v[i] + dt2 * ac;
+  d_out[i] = d_in[i] + dt * vh + dtsq2 * ac;
+  v[i] = vh + dt2 * ac;
+}
+
 // Mass matrix + corrector (kernels/kernel_3_cuda_device.cu,
 // compute_forces_viscoelastic_calling_routine.F90:369-416), unit-stride over (3, NGLOB).
 __global__ void mass_corrector_kernel(float* __restrict__ v, float* __restrict__ a, const float* __restrict__ rmx,
@@ -369,12 +400,27 @@ bool check_kernel_error(Mesh* mp) {
 // One fused forward step on the compute stream; the predictor of this step is
 // fused with the corrector of the previous one unless first_step.
 // ev (optional): events recorded on the compute stream around the stiffness
-// launches of the step.
-int enqueue_step(Mesh* mp, float dt, float dt2, float dtsq2, bool first_step, cudaEvent_t* ev) {
+// launches of the step.  io (optional, elastic meshes without C-PML): the step
+// reads the displacement from io->d_in and the previous step's force from
+// io->a_in, leaves the force there, writes the new displacement to io->d_out and
+// scatters this step's force into io->a_out (cleared first); Mesh::f.displ and
+// f.accel are pointed at d_out and a_out for the rest of the step.
+int enqueue_step(Mesh* mp, float dt, float dt2, float dtsq2, bool first_step, cudaEvent_t* ev, const StepIO* io) {
   Fields& F = mp->f;
   cudaStream_t s = mp->stream;
   int launches = 0;
-  if (mp->pml) {
+  if (io) {
+    const long n = 3L * mp->nglob;
+    cudaMemsetAsync(io->a_out, 0, sizeof(float) * n, s);
+    if (first_step)
+      predictor_oop_kernel<<<nblk(n, 256), 256, 0, s>>>(io->d_in, io->d_out, F.veloc, io->a_in, n, dt, dt2, dtsq2);
+    else
+      corrector_predictor_oop_kernel<<<nblk(n, 256), 256, 0, s>>>(io->d_in, io->d_out, F.veloc, io->a_in,
+                                                                  mp->d_rmassx, mp->d_rmassy, mp->d_rmassz,
+                                                                  mp->nglob, dt, dt2, dtsq2);
+    F.displ = io->d_out;
+    F.accel = io->a_out;
+  } else if (mp->pml) {
     // C-PML stores predictions of the field before and after the predictor, so
     // the corrector of the previous step runs on its own
     const long n = 3L * mp->nglob;
