@@ -314,6 +314,13 @@ int sf3d_get_kernels_f64(long *Mesh_pointer, double *h_rho_kl, double *h_mu_kl, 
  * the device copy is rounded to FP32 like the per-step stf of the reference. */
 int sf3d_set_stf_table(long *Mesh_pointer, const double *h_stf, int nsources, int nstep);
 
+/* Replace the sources of a prepared mesh (another shot on the same mesh and
+ * model): ispec_selected_source (1-based), sourcearrays in the layout of
+ * prepare_constants_device (NSOURCES,3,5,5,5), and the whole-run stf table as
+ * sf3d_set_stf_table takes it.  Waits for the compute stream first. */
+int sf3d_set_sources(long *Mesh_pointer, int nsources, const int *ispec_selected_source,
+                     const realw *sourcearrays, const double *h_stf, int nstep);
+
 /* Run time steps it_begin..it_end (1-based, inclusive) of the forward scheme
  * entirely on the device: fused corrector+predictor, Stacey, sources,
  * stiffness, displacement seismograms (trace slot (it-1) mod nlength_seismogram);

@@ -62,6 +62,8 @@ def load() -> ctypes.CDLL:
     L.sf3d_version.restype = ctypes.c_int
     L.sf3d_set_stf_table.restype = ctypes.c_int
     L.sf3d_set_stf_table.argtypes = [P, P, ctypes.c_int, ctypes.c_int]
+    L.sf3d_set_sources.restype = ctypes.c_int
+    L.sf3d_set_sources.argtypes = [P, ctypes.c_int, P, P, P, ctypes.c_int]
     L.sf3d_iterate_time.restype = ctypes.c_int
     L.sf3d_iterate_time.argtypes = [P, ctypes.c_int, ctypes.c_int, ctypes.c_float, ctypes.c_int, ctypes.c_int]
     L.sf3d_get_seismograms.restype = ctypes.c_int

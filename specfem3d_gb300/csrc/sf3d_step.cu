@@ -796,6 +796,44 @@ int sf3d_set_stf_table(long* Mesh_pointer, const double* h_stf, int nsources, in
   return SF3D_OK;
 }
 
+int sf3d_set_sources(long* Mesh_pointer, int nsources, const int* ispec_selected_source, const realw* sourcearrays,
+                     const double* h_stf, int nstep) {
+  Mesh* mp = get_mesh(Mesh_pointer);
+  if (!mp) return SF3D_ERR_STATE;
+  if (nsources < 1 || nstep < 1 || !ispec_selected_source || !sourcearrays || !h_stf) {
+    set_error(SF3D_ERR_ARG, "sf3d_set_sources: invalid arguments");
+    return SF3D_ERR_ARG;
+  }
+  std::vector<float> sa((size_t)nsources * NGLL3_PAD * 3, 0.f);
+  std::vector<int> isp(nsources);
+  for (int is = 0; is < nsources; ++is) {
+    isp[is] = ispec_selected_source[is] - 1;
+    if (isp[is] < 0 || isp[is] >= mp->nspec) {
+      set_error(SF3D_ERR_ARG, "sf3d_set_sources: ispec_selected_source out of range");
+      return SF3D_ERR_ARG;
+    }
+    for (int p = 0; p < NGLL3; ++p)
+      for (int c = 0; c < 3; ++c)
+        sa[((size_t)is * NGLL3_PAD + p) * 3 + c] = sourcearrays[is + (size_t)nsources * (c + 3 * p)];
+  }
+  SF3D_CUDA_RET(cudaStreamSynchronize(mp->stream), SF3D_ERR_CUDA);
+  if (nsources != mp->nsources) {
+    cudaFree(mp->d_sourcearrays); cudaFree(mp->d_ispec_src); cudaFree(mp->d_stf_step);
+    mp->d_sourcearrays = nullptr; mp->d_ispec_src = nullptr; mp->d_stf_step = nullptr;
+    if (!alloc_zero((void**)&mp->d_sourcearrays, sizeof(float) * sa.size()) ||
+        !alloc_zero((void**)&mp->d_ispec_src, sizeof(int) * nsources) ||
+        !alloc_zero((void**)&mp->d_stf_step, sizeof(float) * nsources)) {
+      mp->nsources = 0;
+      return SF3D_ERR_CUDA;
+    }
+    mp->nsources = mp->nsources_local = nsources;
+  }
+  if (!copy_sync(mp->d_sourcearrays, sa.data(), sizeof(float) * sa.size(), cudaMemcpyHostToDevice, mp->stream) ||
+      !copy_sync(mp->d_ispec_src, isp.data(), sizeof(int) * nsources, cudaMemcpyHostToDevice, mp->stream))
+    return SF3D_ERR_CUDA;
+  return sf3d_set_stf_table(Mesh_pointer, h_stf, nsources, nstep);
+}
+
 int sf3d_iterate_time(long* Mesh_pointer, int it_begin, int it_end, realw deltat, int steps_per_graph, int flags) {
   NvtxRange nvtx_range("sf3d_iterate_time");
   Mesh* mp = get_mesh(Mesh_pointer);

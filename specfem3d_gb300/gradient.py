@@ -136,6 +136,10 @@ class MisfitGradient:
     def dt(self) -> float:
         return float(self.solver.deltat)
 
+    def set_shot(self, db: dict):
+        """Next shot on the same mesh and model: ``db`` carries its sources."""
+        self.solver.set_sources(db)
+
     def forward(self) -> np.ndarray:
         """Seismograms (nrec, 3, nstep) of the forward run from rest."""
         if self.L.sf3d_gradient_forward(self.solver.mp, float(self.solver.deltat)) != 0:
@@ -185,13 +189,23 @@ def misfit_gradient(db_of_shot, cfg: dict, observed, checkpoint_every: int = 200
     total = 0.0
     grad = None
     timing = []
-    for i, obs in enumerate(observed):
-        mg = MisfitGradient(db_of_shot(i), shot_config(cfg, i), checkpoint_every, fused)
-        seis = mg.forward()
-        J, res = misfit(seis, obs, mg.dt)
-        g = mg.gradient(res)
-        timing.append((mg.forward_ms, mg.backward_ms))
+    # one device set-up for every shot (mesh, model, autotuned stiffness build and
+    # gradient buffers are shared); each shot replaces only the sources
+    mg = MisfitGradient(db_of_shot(0), shot_config(cfg, 0), checkpoint_every, fused)
+    try:
+        for i, obs in enumerate(observed):
+            if i > 0:
+                mg.set_shot(db_of_shot(i))
+            seis = mg.forward()
+            J, res = misfit(seis, obs, mg.dt)
+            g = mg.gradient(res)
+            timing.append((mg.forward_ms, mg.backward_ms))
+            total += J
+            if grad is None:
+                grad = g
+            else:
+                for k in grad:
+                    grad[k] += g[k]
+    finally:
         mg.close()
-        total += J
-        grad = g if grad is None else {k: grad[k] + g[k] for k in grad}
     return total, grad, timing

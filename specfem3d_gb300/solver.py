@@ -192,6 +192,20 @@ class GPUSolver:
             if self.L.sf3d_set_stf_table(self.mp, stf.ctypes.data, self.nsources, stf.shape[0]) != 0:
                 abi.check()
 
+    def set_sources(self, db: dict):
+        """Replace the sources by those of ``db`` (another shot on the same mesh and
+        model: its sourcearrays, ispec_selected_source, stf): sf3d_set_sources."""
+        ns = int(db["nsources"])
+        sa = np.ascontiguousarray(np.asarray(db["sourcearrays"], np.float32).reshape(-1))
+        isp = np.ascontiguousarray(np.asarray(db["ispec_selected_source"], np.int32).reshape(-1))
+        stf = np.ascontiguousarray(np.asarray(db["stf"], np.float64).reshape(ns, -1).T)
+        if self.L.sf3d_set_sources(self.mp, ns, isp.ctypes.data, sa.ctypes.data, stf.ctypes.data, stf.shape[0]) != 0:
+            abi.check()
+        self.db = dict(self.db)
+        for k in ("sourcearrays", "ispec_selected_source", "stf", "nsources"):
+            self.db[k] = db[k]
+        self.nsources = ns
+
     def _prepare_acoustic(self, db):
         """prepare_fields_acoustic_device (specfem3D/prepare_gpu.f90:170-200)."""
         A = abi.Args()
@@ -360,6 +374,15 @@ class GPUSolver:
                                                self.mp)
         abi.check()
         return d, v, a
+
+    def reset(self):
+        """Back to rest at step 1 (elastic meshes without attenuation or fluid: the
+        displacement, velocity and acceleration are the whole state)."""
+        if self.attenuation or getattr(self, "nspec_acoustic", 0):
+            raise NotImplementedError("reset: the wavefield at rest is set up again by a new solver here")
+        z = np.zeros(3 * self.nglob, np.float32)
+        self.set_fields(z, z, z)
+        self.it = 1
 
     def set_fields(self, d, v, a):
         A = abi.Args()

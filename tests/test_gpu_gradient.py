@@ -134,3 +134,35 @@ def test_gradient_matches_reference_style_kernels(problem):
         print(f"{k}: discrete adjoint vs SIMULATION_TYPE=3 kernels: rel L2 {e:.3e}, correlation {cc:.6f}")
         assert np.abs(ref[k]).max() > 0
         assert e < 1e-4 and cc > 0.99999
+
+
+def test_set_sources_equals_a_fresh_solver(problem):
+    """sf3d_set_sources: a solver prepared for shot 0 and given shot 1's sources
+    records shot 1's traces as a solver prepared for shot 1 does (same build;
+    atomics reorder sums, which over 200 steps gives ~2e-6: <= 1e-5), and returns
+    to shot 0's traces after the sources are set back."""
+    from specfem3d_gb300 import gradient as G
+    from specfem3d_gb300.solver import GPUSolver
+    cfg, db0 = problem.cfg, problem.db
+    nstep = 200
+    dbs = [G.shot_database(db0, cfg, i) for i in range(2)]
+    cfgs = []
+    for i in range(2):
+        c = G.shot_config(cfg, i)
+        c["record"] = ("displ",)
+        c["nstep"] = nstep
+        cfgs.append(c)
+    ref = []
+    for i in range(2):
+        s = GPUSolver(dbs[i], cfgs[i], nlength=nstep)
+        s.run(nstep, steps_per_graph=50)
+        ref.append(s.seismograms())
+        s.close()
+    assert rel_l2(ref[1], ref[0]) > 1e-2      # the shots differ
+    s = GPUSolver(dbs[0], cfgs[0], nlength=nstep)
+    for i in (1, 0):
+        s.set_sources(dbs[i])
+        s.reset()
+        s.run(nstep, steps_per_graph=50)
+        assert rel_l2(s.seismograms(), ref[i]) < 1e-5, i
+    s.close()
