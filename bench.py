@@ -520,7 +520,9 @@ def main():
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--small", action="store_true", help="scaled-down mesh for quick checks")
     ap.add_argument("--graph", type=int, default=50, help="steps per captured CUDA graph")
-    ap.add_argument("--tile", type=int, default=0, help="process elements in tiles of tile^3 (0: mesh order)")
+    ap.add_argument("--tile", type=int, default=4,
+                    help="process elements in tiles of tile^3 (0: mesh order); 4 measured 1.3 %% faster "
+                         "stiffness launches on the layered workload (L2 reuse of the gathered fields)")
     ap.add_argument("--e2e-steps", type=int, default=50)
     ap.add_argument("--cpu-steps", type=int, default=10, help="timed CPU-oracle steps on the full bench mesh")
     ap.add_argument("--no-cpu", action="store_true")
@@ -716,6 +718,8 @@ def main():
         "dtype": "f32", "data": "synthetic (seeded moment tensor, layered model of the benchmark definition)",
         "config": {"workload": workload, "nspec": nspec, "nglob": nglob, "nsteps_timed": K,
                    "steps_per_graph": args.graph, "l2": "inputs (~25 GB) far larger than L2; no flush needed",
+                   "element_order": (f"phase lists in {args.tile}x{args.tile}x{args.tile} tiles of the block"
+                                     if args.tile > 0 else "mesh order"),
                    "parallelism": "replicas" if world > 1 else "single GPU"},
         "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
                      "peak_kind": peak_kind,
