@@ -155,11 +155,14 @@ struct GradArgs {
   int* err;            // kernel error word (a bounded wait that timed out)
 };
 
-// Gradient of the 3x3 displacement derivative of a field staged in shared memory.
-__device__ __forceinline__ void local_grad(const float (*s)[NGLL3_PAD], const float* hp, int i, int j, int k,
-                                           float t[3][3]) {
+// Local derivatives (d/dxi, d/deta, d/dgamma of each component) of two fields
+// staged in shared memory, t of s and q of r, in one loop: each hprime
+// coefficient is read from shared memory once for both fields; every output is
+// the same 5-term FMA chain as a loop over one field would form.
+__device__ __forceinline__ void local_grad_pair(const float (*s)[NGLL3_PAD], const float (*r)[NGLL3_PAD],
+                                            const float* hp, int i, int j, int k, float t[3][3], float q[3][3]) {
 #pragma unroll
-  for (int c = 0; c < 3; ++c) t[c][0] = t[c][1] = t[c][2] = 0.f;
+  for (int c = 0; c < 3; ++c) t[c][0] = t[c][1] = t[c][2] = q[c][0] = q[c][1] = q[c][2] = 0.f;
 #pragma unroll
   for (int l = 0; l < NGLLX; ++l) {
     const float h1 = hp[i + NGLLX * l], h2 = hp[j + NGLLX * l], h3 = hp[k + NGLLX * l];
@@ -169,6 +172,9 @@ __device__ __forceinline__ void local_grad(const float (*s)[NGLL3_PAD], const fl
       t[c][0] = fmaf(s[c][p1], h1, t[c][0]);
       t[c][1] = fmaf(s[c][p2], h2, t[c][1]);
       t[c][2] = fmaf(s[c][p3], h3, t[c][2]);
+      q[c][0] = fmaf(r[c][p1], h1, q[c][0]);
+      q[c][1] = fmaf(r[c][p2], h2, q[c][1]);
+      q[c][2] = fmaf(r[c][p3], h3, q[c][2]);
     }
   }
 }
@@ -199,8 +205,7 @@ __global__ void __launch_bounds__(NGLL3_PAD) grad_accum_kernel(const GradArgs a)
   __syncthreads();
   if (!active) return;
   float tp[3][3], tu[3][3];
-  local_grad(s_p, s_h, i, j, k, tp);
-  local_grad(s_u, s_h, i, j, k, tu);
+  local_grad_pair(s_p, s_u, s_h, i, j, k, tp, tu);
   const int ir = __ldg(a.irregular + e);
   // d[c][x]: derivative of component c along x, y, z
   float dp[3][3], du[3][3], jac;
@@ -300,8 +305,7 @@ __global__ void __launch_bounds__(NGLL3_PAD, 10) adj_stiffness_grad_kernel(const
   const int ir = __ldg(a.irregular + e);
   if (active) {
     float tp[3][3], tu[3][3];
-    local_grad(s_p, s_gll, i, j, k, tp);
-    local_grad(s_u, s_gll, i, j, k, tu);
+    local_grad_pair(s_p, s_u, s_gll, i, j, k, tp, tu);
     float dp[3][3], du[3][3], jac, m[9];
 #pragma unroll
     for (int q = 0; q < 9; ++q) m[q] = 0.f;
