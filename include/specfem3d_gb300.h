@@ -328,8 +328,14 @@ int sf3d_set_sources(long *Mesh_pointer, int nsources, const int *ispec_selected
  * both coupling terms and the pressure traces, in the order of
  * iterate_time.F90.  Steps are captured in CUDA graphs of
  * steps_per_graph steps (0 = no graphs).  Leaves the fields as the per-call
- * ABI leaves them after the same steps.  flags bit 0: record the device time
- * of every stiffness launch (read back with sf3d_last_timing). */
+ * ABI leaves them after the same steps.  On a fluid-solid mesh the solid
+ * predictor/corrector passes cover the span of global points of the solid
+ * elements and the fluid passes that of the fluid elements (the first call
+ * finds the spans): the solid fields at points of fluid elements alone, and the
+ * potentials at points of solid elements alone, are not touched (they stay zero
+ * from rest; the per-call entry points advance every point, as the reference
+ * does).  flags bit 0: record the device time of every stiffness launch (read
+ * back with sf3d_last_timing). */
 int sf3d_iterate_time(long *Mesh_pointer, int it_begin, int it_end, realw deltat, int steps_per_graph,
                       int flags);
 
