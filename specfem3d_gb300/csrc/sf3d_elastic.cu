@@ -65,14 +65,16 @@ __global__ void __launch_bounds__(NGLL3_PAD, MINB) stiffness_kernel(const Stiffn
   __shared__ uint64_t s_bar;
   bool bulk_failed = false;
   __shared__ float s_gll[NGLL3];
-  __shared__ float s_t[9][NGLL3_PAD];
+  __shared__ __align__(16) float s_t[9][NGLL3_PAD];
   // the bulk-copy builds keep the displacement / velocity rows in rows 0-5 of
   // s_t (a barrier separates their last read from the first stress write): 3 KB
   // less shared memory a CTA, so one CTA more fits an SM
   constexpr bool kAlias = kBulkAtt;
-  __shared__ float s_uv_own[kAlias ? 1 : (ATT ? 6 : 3)][NGLL3_PAD];
+  __shared__ __align__(16) float s_uv_own[kAlias ? 1 : (ATT ? 6 : 3)][NGLL3_PAD];
   float (*s_u)[NGLL3_PAD] = kAlias ? s_t : s_uv_own;
-  float (*s_v)[NGLL3_PAD] = kAlias ? s_t + 3 : s_uv_own + (ATT ? 3 : 0);
+  // with attenuation a point's displacement and dt * velocity sit side by side
+  // (float2): one shared load serves both gradients
+  float2 (*s_uv)[NGLL3_PAD] = reinterpret_cast<float2 (*)[NGLL3_PAD]>(kAlias ? &s_t[0][0] : &s_uv_own[0][0]);
 
   const int t = threadIdx.x;
   const int e = a.phase ? __ldg(a.phase + blockIdx.x) : (int)blockIdx.x;
@@ -186,13 +188,14 @@ __global__ void __launch_bounds__(NGLL3_PAD, MINB) stiffness_kernel(const Stiffn
     }
   }
   if (t < NGLL3) s_gll[t] = __ldg(a.gll + t);
-  s_u[0][t] = ux;
-  s_u[1][t] = uy;
-  s_u[2][t] = uz;
   if (ATT) {
-    s_v[0][t] = vx;
-    s_v[1][t] = vy;
-    s_v[2][t] = vz;
+    s_uv[0][t] = make_float2(ux, vx);
+    s_uv[1][t] = make_float2(uy, vy);
+    s_uv[2][t] = make_float2(uz, vz);
+  } else {
+    s_u[0][t] = ux;
+    s_u[1][t] = uy;
+    s_u[2][t] = uz;
   }
   __syncthreads();
 
@@ -202,27 +205,39 @@ __global__ void __launch_bounds__(NGLL3_PAD, MINB) stiffness_kernel(const Stiffn
   float a1x = 0.f, a2x = 0.f, a3x = 0.f, a1y = 0.f, a2y = 0.f, a3y = 0.f, a1z = 0.f, a2z = 0.f, a3z = 0.f;
   if (active) {
     const float* hp = s_gll;  // hprime(i2,i1) = hp[i2 + 5 i1]
-#pragma unroll
-    for (int l = 0; l < NGLLX; ++l) {
-      const float h1 = hp[i + NGLLX * l], h2 = hp[j + NGLLX * l], h3 = hp[k + NGLLX * l];
-      const int p1 = l + NGLLX * j + NGLL2 * k, p2 = i + NGLLX * l + NGLL2 * k, p3 = i + NGLLX * j + NGLL2 * l;
-      t1x = fmaf(s_u[0][p1], h1, t1x); t1y = fmaf(s_u[1][p1], h1, t1y); t1z = fmaf(s_u[2][p1], h1, t1z);
-      t2x = fmaf(s_u[0][p2], h2, t2x); t2y = fmaf(s_u[1][p2], h2, t2y); t2z = fmaf(s_u[2][p2], h2, t2z);
-      t3x = fmaf(s_u[0][p3], h3, t3x); t3y = fmaf(s_u[1][p3], h3, t3y); t3z = fmaf(s_u[2][p3], h3, t3z);
-    }
-    a1x = t1x; a2x = t2x; a3x = t3x; a1y = t1y; a2y = t2y; a3y = t3y; a1z = t1z; a2z = t2z; a3z = t3z;
     if (ATT) {
+      // gradients of u and of dt v in one loop; the strain of u + dt v is their sum
+      float b1x = 0.f, b2x = 0.f, b3x = 0.f, b1y = 0.f, b2y = 0.f, b3y = 0.f, b1z = 0.f, b2z = 0.f, b3z = 0.f;
 #pragma unroll
       for (int l = 0; l < NGLLX; ++l) {
         const float h1 = hp[i + NGLLX * l], h2 = hp[j + NGLLX * l], h3 = hp[k + NGLLX * l];
         const int p1 = l + NGLLX * j + NGLL2 * k, p2 = i + NGLLX * l + NGLL2 * k, p3 = i + NGLLX * j + NGLL2 * l;
-        a1x = fmaf(s_v[0][p1], h1, a1x); a1y = fmaf(s_v[1][p1], h1, a1y); a1z = fmaf(s_v[2][p1], h1, a1z);
-        a2x = fmaf(s_v[0][p2], h2, a2x); a2y = fmaf(s_v[1][p2], h2, a2y); a2z = fmaf(s_v[2][p2], h2, a2z);
-        a3x = fmaf(s_v[0][p3], h3, a3x); a3y = fmaf(s_v[1][p3], h3, a3y); a3z = fmaf(s_v[2][p3], h3, a3z);
+        float2 q;
+        q = s_uv[0][p1]; t1x = fmaf(q.x, h1, t1x); b1x = fmaf(q.y, h1, b1x);
+        q = s_uv[1][p1]; t1y = fmaf(q.x, h1, t1y); b1y = fmaf(q.y, h1, b1y);
+        q = s_uv[2][p1]; t1z = fmaf(q.x, h1, t1z); b1z = fmaf(q.y, h1, b1z);
+        q = s_uv[0][p2]; t2x = fmaf(q.x, h2, t2x); b2x = fmaf(q.y, h2, b2x);
+        q = s_uv[1][p2]; t2y = fmaf(q.x, h2, t2y); b2y = fmaf(q.y, h2, b2y);
+        q = s_uv[2][p2]; t2z = fmaf(q.x, h2, t2z); b2z = fmaf(q.y, h2, b2z);
+        q = s_uv[0][p3]; t3x = fmaf(q.x, h3, t3x); b3x = fmaf(q.y, h3, b3x);
+        q = s_uv[1][p3]; t3y = fmaf(q.x, h3, t3y); b3y = fmaf(q.y, h3, b3y);
+        q = s_uv[2][p3]; t3z = fmaf(q.x, h3, t3z); b3z = fmaf(q.y, h3, b3z);
+      }
+      a1x = t1x + b1x; a2x = t2x + b2x; a3x = t3x + b3x;
+      a1y = t1y + b1y; a2y = t2y + b2y; a3y = t3y + b3y;
+      a1z = t1z + b1z; a2z = t2z + b2z; a3z = t3z + b3z;
+    } else {
+#pragma unroll
+      for (int l = 0; l < NGLLX; ++l) {
+        const float h1 = hp[i + NGLLX * l], h2 = hp[j + NGLLX * l], h3 = hp[k + NGLLX * l];
+        const int p1 = l + NGLLX * j + NGLL2 * k, p2 = i + NGLLX * l + NGLL2 * k, p3 = i + NGLLX * j + NGLL2 * l;
+        t1x = fmaf(s_u[0][p1], h1, t1x); t1y = fmaf(s_u[1][p1], h1, t1y); t1z = fmaf(s_u[2][p1], h1, t1z);
+        t2x = fmaf(s_u[0][p2], h2, t2x); t2y = fmaf(s_u[1][p2], h2, t2y); t2z = fmaf(s_u[2][p2], h2, t2z);
+        t3x = fmaf(s_u[0][p3], h3, t3x); t3y = fmaf(s_u[1][p3], h3, t3y); t3z = fmaf(s_u[2][p3], h3, t3z);
       }
     }
   }
-  if (kAlias) __syncthreads();  // every read of s_u / s_v done: s_t may be written
+  if (kAlias) __syncthreads();  // every read of s_uv done: s_t may be written
   if (active) {
     const float xr = a.xix_regular;
     const float xix = m[0], xiy = m[1], xiz = m[2], etax = m[3], etay = m[4], etaz = m[5];
