@@ -102,6 +102,29 @@ __device__ __forceinline__ void ref_grad(const float (*s)[NGLL3_PAD], const floa
   }
 }
 
+// the same for two fields stored side by side (float2 .x, .y), one shared load
+// per neighbour for both; each output is the FMA chain of ref_grad
+__device__ __forceinline__ void ref_grad_pair(const float2 (*s)[NGLL3_PAD], const float* hp, int i, int j, int k,
+                                              float T[3][3], float U[3][3]) {
+#pragma unroll
+  for (int c = 0; c < 3; ++c) T[c][0] = T[c][1] = T[c][2] = U[c][0] = U[c][1] = U[c][2] = 0.f;
+#pragma unroll
+  for (int l = 0; l < NGLLX; ++l) {
+    const float h1 = hp[i + NGLLX * l], h2 = hp[j + NGLLX * l], h3 = hp[k + NGLLX * l];
+    const int p1 = l + NGLLX * j + NGLL2 * k, p2 = i + NGLLX * l + NGLL2 * k, p3 = i + NGLLX * j + NGLL2 * l;
+#pragma unroll
+    for (int c = 0; c < 3; ++c) {
+      const float2 q1 = s[c][p1], q2 = s[c][p2], q3 = s[c][p3];
+      T[c][0] = fmaf(q1.x, h1, T[c][0]);
+      T[c][1] = fmaf(q2.x, h2, T[c][1]);
+      T[c][2] = fmaf(q3.x, h3, T[c][2]);
+      U[c][0] = fmaf(q1.y, h1, U[c][0]);
+      U[c][1] = fmaf(q2.y, h2, U[c][1]);
+      U[c][2] = fmaf(q3.y, h3, U[c][2]);
+    }
+  }
+}
+
 // physical gradient D[c][x] = d u_c / d x from the reference-cube gradient
 __device__ __forceinline__ void phys_grad(const float T[3][3], const float* m, int ir, float xr, float D[3][3]) {
 #pragma unroll
@@ -134,8 +157,7 @@ __global__ void __launch_bounds__(NGLL3_PAD) pml_stiffness_kernel(const PmlArgs 
   bool bulk_failed = false;
   __shared__ float s_gll[NGLL3];
   __shared__ float s_u[3][NGLL3_PAD];
-  __shared__ float s_o[3][NGLL3_PAD];
-  __shared__ float s_n[3][NGLL3_PAD];
+  __shared__ __align__(8) float2 s_on[3][NGLL3_PAD];   // PML displacement predictions (old, new)
   __shared__ float s_t[9][NGLL3_PAD];
   const int t = threadIdx.x;
   const int e = __ldg(a.list + blockIdx.x);
@@ -163,8 +185,7 @@ __global__ void __launch_bounds__(NGLL3_PAD) pml_stiffness_kernel(const PmlArgs 
     for (int c = 0; c < 3; ++c) {
       s_u[c][t] = a.displ[3 * g + c];
       vel[c] = a.veloc[3 * g + c];
-      s_o[c][t] = a.pold[po + c * NGLL3_PAD];
-      s_n[c][t] = a.pnew[po + c * NGLL3_PAD];
+      s_on[c][t] = make_float2(a.pold[po + c * NGLL3_PAD], a.pnew[po + c * NGLL3_PAD]);
     }
   }
   __syncthreads();
@@ -180,13 +201,12 @@ __global__ void __launch_bounds__(NGLL3_PAD) pml_stiffness_kernel(const PmlArgs 
                    m[2] * (m[3] * m[7] - m[4] * m[6]));
     }
     const float xr = a.xix_regular;
-    float T[3][3], du[3][3], dold[3][3], dnew[3][3];
+    float T[3][3], U[3][3], du[3][3], dold[3][3], dnew[3][3];
     ref_grad(s_u, s_gll, i, j, k, T);
     phys_grad(T, m, ir, xr, du);
-    ref_grad(s_o, s_gll, i, j, k, T);
+    ref_grad_pair(s_on, s_gll, i, j, k, T, U);
     phys_grad(T, m, ir, xr, dold);
-    ref_grad(s_n, s_gll, i, j, k, T);
-    phys_grad(T, m, ir, xr, dnew);
+    phys_grad(U, m, ir, xr, dnew);
     if (a.eps[0]) {
       // deviatoric strain of u (kept for kernels as the reference does for PML elements)
       const float templ = (1.f / 3.f) * (du[0][0] + du[1][1] + du[2][2]);
@@ -272,7 +292,7 @@ __global__ void __launch_bounds__(NGLL3_PAD) pml_stiffness_kernel(const PmlArgs 
 #pragma unroll
       for (int c = 0; c < 3; ++c) {
         float& r = RM(39 + 3 * d + c);
-        r = CF(3 * d) * r + s_n[c][t] * CF(3 * d + 1) + s_o[c][t] * CF(3 * d + 2);
+        r = CF(3 * d) * r + s_on[c][t].y * CF(3 * d + 1) + s_on[c][t].x * CF(3 * d + 2);
         rd[c][d] = r;
       }
     const float wrj = __ldg(a.wgll_cube + t) * __ldg(a.rho + eo) * jac;
