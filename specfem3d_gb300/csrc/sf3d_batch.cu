@@ -694,6 +694,10 @@ void launch_batch_stiffness(Mesh* mp, int iphase, cudaStream_t s, int soff = 0, 
     q.accel = B->accel;
     memcpy(q.hp, mp->h_hprime, sizeof(q.hp));
     memcpy(q.hpw, mp->h_hprimewgll, sizeof(q.hpw));
+    // hp[i2 + 5 i1] = hprime(i2, i1): M[o][l] = hp[o + 5 l]; the transposed
+    // contraction takes M[o][l] = hprimewgll(l, o) = hpw[l + 5 o]
+    even_odd_coefficients(mp->h_hprime, 1, NGLLX, q.ek);
+    even_odd_coefficients(mp->h_hprimewgll, NGLLX, 1, q.ekw);
     launch_batch_pencil(q, B->pencil_lanes, mp->geom_format, s);
     return;
   }

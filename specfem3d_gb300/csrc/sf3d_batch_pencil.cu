@@ -21,15 +21,37 @@
 // pencils of a warp are consecutive in line order, whose point offsets (5, 1,
 // 1, or 5, 21, 1 on a wrap) are odd, so every pass is free of bank conflicts.
 // The arithmetic per point and shot is that of stiffness_kernel<ATT=0>
-// (compute_forces_viscoelastic.F90:250-860): the same 5-term FMA chains in the
-// same order, the same stress and J sigma grad(xi); only the sum of the three
-// weighted contraction directions is formed in two steps.
+// (compute_forces_viscoelastic.F90:250-860): the same stress and J sigma
+// grad(xi); the 5-wide contractions use the even / odd split of the derivative
+// matrices (eo5: 20 operations per line of five instead of 25 FMAs, equal to
+// the FMA chains up to rounding), and the sum of the three weighted contraction
+// directions is formed in two steps.
 #include "sf3d_internal.h"
 
 namespace sf3d {
 namespace {
 
 constexpr int kPencils = 25;
+
+// out[o] = sum_l M[o][l] v[l] for the 5x5 GLL derivative matrices, which are
+// centro-antisymmetric (M[4-o][4-l] = -M[o][l], the GLL points being symmetric):
+// from the even and odd parts e_l = v_l + v_{4-l}, d_l = v_l - v_{4-l},
+//   out_o, out_{4-o} = S_o +- A_o,  S_o = a_o0 d_0 + a_o1 d_1,
+//   A_o = b_o0 e_0 + b_o1 e_1 + c_o v_2   (o = 0, 1),   out_2 = m_20 d_0 + m_21 d_1,
+// 20 operations instead of 25 FMAs (k: a00 a01 b00 b01 c0 a10 a11 b10 b11 c1 m20 m21)
+__device__ __forceinline__ void eo5(const float v[NGLLX], const float* k, float out[NGLLX]) {
+  const float e0 = v[0] + v[4], e1 = v[1] + v[3], d0 = v[0] - v[4], d1 = v[1] - v[3];
+  const float v2 = v[2];
+#pragma unroll
+  for (int o = 0; o < 2; ++o) {
+    const float* q = k + 5 * o;
+    const float S = fmaf(q[1], d1, q[0] * d0);
+    const float A = fmaf(q[4], v2, fmaf(q[3], e1, q[2] * e0));
+    out[o] = S + A;
+    out[4 - o] = S - A;
+  }
+  out[2] = fmaf(k[11], d1, k[10] * d0);
+}
 
 template <int GEOM>
 __device__ __forceinline__ float moduli_value(const PencilArgs& a, const ElemPack* pk, unsigned vary, int base,
@@ -78,16 +100,13 @@ __global__ void __launch_bounds__(kPencils * W, MINB) batch_pencil_kernel(const 
     for (int c = 0; c < 3; ++c) u[c][l] = a.displ[gb + c * S];
   }
   __syncthreads();  // s_gll
-  const float* hp = a.hp;                   // hprime(i2,i1) = hp[i2 + 5 i1], parameter bank
-  const float* hpw = a.hpw;                 // hprimewgll(i2,i1) = hpw[i2 + 5 i1]
 #pragma unroll
   for (int c = 0; c < 3; ++c) {
+    float t[NGLLX];
+    eo5(u[c], a.ek, t);
 #pragma unroll
     for (int o = 0; o < NGLLX; ++o) {
-      float t = 0.f;
-#pragma unroll
-      for (int l = 0; l < NGLLX; ++l) t = fmaf(u[c][l], hp[o + NGLLX * l], t);
-      ROW(3 + c, xb + o) = t;               // rows 3-5: d/dxi
+      ROW(3 + c, xb + o) = t[o];            // rows 3-5: d/dxi
       ROW(c, xb + o) = u[c][o];             // rows 0-2: displacement
     }
   }
@@ -99,13 +118,10 @@ __global__ void __launch_bounds__(kPencils * W, MINB) batch_pencil_kernel(const 
     float v[NGLLX];
 #pragma unroll
     for (int l = 0; l < NGLLX; ++l) v[l] = ROW(c, yb + NGLLX * l);
+    float t[NGLLX];
+    eo5(v, a.ek, t);
 #pragma unroll
-    for (int o = 0; o < NGLLX; ++o) {
-      float t = 0.f;
-#pragma unroll
-      for (int l = 0; l < NGLLX; ++l) t = fmaf(v[l], hp[o + NGLLX * l], t);
-      ROW(6 + c, yb + NGLLX * o) = t;       // rows 6-8: d/deta
-    }
+    for (int o = 0; o < NGLLX; ++o) ROW(6 + c, yb + NGLLX * o) = t[o];   // rows 6-8: d/deta
   }
   // ---- z pass: d/dgamma along the z-line (kept in registers until the stress) ---
   float t3[3][NGLLX];
@@ -114,13 +130,7 @@ __global__ void __launch_bounds__(kPencils * W, MINB) batch_pencil_kernel(const 
     float v[NGLLX];
 #pragma unroll
     for (int l = 0; l < NGLLX; ++l) v[l] = ROW(c, zb + NGLL2 * l);
-#pragma unroll
-    for (int o = 0; o < NGLLX; ++o) {
-      float t = 0.f;
-#pragma unroll
-      for (int l = 0; l < NGLLX; ++l) t = fmaf(v[l], hp[o + NGLLX * l], t);
-      t3[c][o] = t;
-    }
+    eo5(v, a.ek, t3[c]);
   }
   __syncthreads();  // rows 3-8 complete; every read of rows 0-2 done
 
@@ -208,26 +218,20 @@ __global__ void __launch_bounds__(kPencils * W, MINB) batch_pencil_kernel(const 
       float v[NGLLX];
 #pragma unroll
       for (int l = 0; l < NGLLX; ++l) v[l] = ROW(c, xb + l);
+      float n[NGLLX];
+      eo5(v, a.ekw, n);
 #pragma unroll
-      for (int o = 0; o < NGLLX; ++o) {
-        float n = 0.f;
-#pragma unroll
-        for (int l = 0; l < NGLLX; ++l) n = fmaf(v[l], hpw[l + NGLLX * o], n);
-        ROW(c, xb + o) = fac1 * n;
-      }
+      for (int o = 0; o < NGLLX; ++o) ROW(c, xb + o) = fac1 * n[o];
     }
 #pragma unroll
     for (int c = 0; c < 3; ++c) {
       float v[NGLLX];
 #pragma unroll
       for (int l = 0; l < NGLLX; ++l) v[l] = ROW(3 + c, yb + NGLLX * l);
+      float n[NGLLX];
+      eo5(v, a.ekw, n);
 #pragma unroll
-      for (int o = 0; o < NGLLX; ++o) {
-        float n = 0.f;
-#pragma unroll
-        for (int l = 0; l < NGLLX; ++l) n = fmaf(v[l], hpw[l + NGLLX * o], n);
-        ROW(3 + c, yb + NGLLX * o) = n;      // unweighted: fac2 applied in the sum below
-      }
+      for (int o = 0; o < NGLLX; ++o) ROW(3 + c, yb + NGLLX * o) = n[o];   // fac2 applied in the sum below
     }
   }
   __syncthreads();
@@ -235,6 +239,9 @@ __global__ void __launch_bounds__(kPencils * W, MINB) batch_pencil_kernel(const 
   // order and rounding) and the scatter-add ------------------------------------------
   {
     const float fac3 = s_gll[2 * NGLL2 + pa + NGLLX * pb];  // wgllwgll_xy(i, j)
+    float nz[3][NGLLX];
+#pragma unroll
+    for (int c = 0; c < 3; ++c) eo5(fz[c], a.ekw, nz[c]);
 #pragma unroll
     for (int o = 0; o < NGLLX; ++o) {
       const int p = zb + NGLL2 * o;
@@ -242,11 +249,8 @@ __global__ void __launch_bounds__(kPencils * W, MINB) batch_pencil_kernel(const 
       const unsigned gb = 3u * (unsigned)__ldg(a.ibool + eb + p) * S + shot;
 #pragma unroll
       for (int c = 0; c < 3; ++c) {
-        float n = 0.f;
-#pragma unroll
-        for (int l = 0; l < NGLLX; ++l) n = fmaf(fz[c][l], hpw[l + NGLLX * o], n);
         const float r = fmaf(fac2, ROW(3 + c, p), ROW(c, p));
-        atomicAdd(a.accel + gb + c * S, -(r + fac3 * n));
+        atomicAdd(a.accel + gb + c * S, -(r + fac3 * nz[c][o]));
       }
     }
   }
@@ -279,6 +283,19 @@ bool launch_geom(const PencilArgs& a, int lanes, cudaStream_t s) {
 }
 
 }  // namespace
+
+void even_odd_coefficients(const float* m, int so, int sl, float k[12]) {
+  auto M = [&](int o, int l) { return (double)m[o * so + l * sl]; };
+  for (int o = 0; o < 2; ++o) {
+    k[5 * o + 0] = (float)(0.5 * (M(o, 0) - M(o, 4)));
+    k[5 * o + 1] = (float)(0.5 * (M(o, 1) - M(o, 3)));
+    k[5 * o + 2] = (float)(0.5 * (M(o, 0) + M(o, 4)));
+    k[5 * o + 3] = (float)(0.5 * (M(o, 1) + M(o, 3)));
+    k[5 * o + 4] = (float)M(o, 2);
+  }
+  k[10] = (float)M(2, 0);
+  k[11] = (float)M(2, 1);
+}
 
 // lanes: shots per CTA (8, 16 or 32; divides the launch's shot count);
 // geom_format: the Mesh's packed static streams (kGeomFP32: the FP32 arrays)

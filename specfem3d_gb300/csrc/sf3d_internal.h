@@ -516,7 +516,13 @@ struct PencilArgs {
   // kernel's parameter bank instead of shared memory
   float hp[NGLL2];
   float hpw[NGLL2];
+  // even / odd coefficients of hprime (ek: out_o = sum_l hprime(o, l) v_l) and of
+  // hprimewgll transposed (ekw: out_o = sum_l hprimewgll(l, o) v_l), see eo5
+  float ek[12];
+  float ekw[12];
 };
+// even / odd coefficients of a centro-antisymmetric 5x5 matrix M[o][l] = m[o * so + l * sl]
+void even_odd_coefficients(const float* m, int so, int sl, float k[12]);
 bool launch_batch_pencil(const PencilArgs& a, int lanes, int geom_format, cudaStream_t s);
 
 void launch_stiffness_pipelined(const StiffnessArgs& a, bool att, bool store_strain, int* err, cudaStream_t s);
