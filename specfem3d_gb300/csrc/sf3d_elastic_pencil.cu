@@ -7,9 +7,8 @@
 // element moves only 1.5 KB of static streams, and that kernel is bound by
 // instruction issue and the shared-memory pipe, not by HBM.  Here a thread owns
 // a pencil: the five points of one line of an element, held in registers, so
-// all five outputs of a contraction come from five loads (25 FMAs), the
-// coefficients are compile-time-indexed kernel parameters, and every value
-// crosses shared memory once per direction.  Per element:
+// all five outputs of a contraction come from five loads, the coefficients are
+// kernel parameters, and every value crosses shared memory once per direction.  Per element:
 //   gather   the thread's z-line from HBM into shared memory
 //   x pass   x-line from shared memory -> d/dxi
 //   y pass   y-line from shared memory -> d/deta
@@ -28,8 +27,9 @@
 // The element's kappa / mu (and metric) rows are prefetched into L1 at kernel
 // start, since the stress stage is their first use.
 // The arithmetic per point is that of stiffness_kernel<ATT=0, STRAIN=0>
-// (compute_forces_viscoelastic.F90:250-860): the same 5-term FMA chains in the
-// same order, the same stress and J sigma grad(xi); the three weighted
+// (compute_forces_viscoelastic.F90:250-860): the same stress and J sigma
+// grad(xi); the 5-wide contractions use the even / odd split of the derivative
+// matrices (eo5, equal to the FMA chains up to rounding), and the three weighted
 // transposed contractions are summed as fac1 nx + fac2 ny + fac3 nz.
 #include "sf3d_internal.h"
 
@@ -61,8 +61,6 @@ __global__ void __launch_bounds__(kPencils * W, MINB) elem_pencil_kernel(const E
   const int xb = NGLLX * pa + NGLL2 * pb;   // x-line (l, pa, pb)
   const int yb = pa + NGLL2 * pb;           // y-line (pa, l, pb)
   const int zb = pa + NGLLX * pb;           // z-line (pa, pb, l)
-  const float* hp = a.hp;                   // hprime(i2,i1) = hp[i2 + 5 i1], parameter bank
-  const float* hpw = a.hpw;                 // hprimewgll(i2,i1) = hpw[i2 + 5 i1]
 
   // the element's kappa / mu rows and, if irregular, its nine metric rows (128-byte
   // lines, 4 a row) are first read in the stress stage: the element's lanes
@@ -99,26 +97,20 @@ __global__ void __launch_bounds__(kPencils * W, MINB) elem_pencil_kernel(const E
     float v[NGLLX];
 #pragma unroll
     for (int l = 0; l < NGLLX; ++l) v[l] = ROW(c, xb + l);
+    float t[NGLLX];
+    eo5(v, a.ek, t);
 #pragma unroll
-    for (int o = 0; o < NGLLX; ++o) {
-      float t = 0.f;
-#pragma unroll
-      for (int l = 0; l < NGLLX; ++l) t = fmaf(v[l], hp[o + NGLLX * l], t);
-      ROW(3 + c, xb + o) = t;
-    }
+    for (int o = 0; o < NGLLX; ++o) ROW(3 + c, xb + o) = t[o];
   }
 #pragma unroll
   for (int c = 0; c < 3; ++c) {
     float v[NGLLX];
 #pragma unroll
     for (int l = 0; l < NGLLX; ++l) v[l] = ROW(c, yb + NGLLX * l);
+    float t[NGLLX];
+    eo5(v, a.ek, t);
 #pragma unroll
-    for (int o = 0; o < NGLLX; ++o) {
-      float t = 0.f;
-#pragma unroll
-      for (int l = 0; l < NGLLX; ++l) t = fmaf(v[l], hp[o + NGLLX * l], t);
-      ROW(6 + c, yb + NGLLX * o) = t;
-    }
+    for (int o = 0; o < NGLLX; ++o) ROW(6 + c, yb + NGLLX * o) = t[o];
   }
   // ---- z pass: d/dgamma along the thread's own z-line, kept in registers ------
   float t3[3][NGLLX];
@@ -127,13 +119,7 @@ __global__ void __launch_bounds__(kPencils * W, MINB) elem_pencil_kernel(const E
     float v[NGLLX];
 #pragma unroll
     for (int l = 0; l < NGLLX; ++l) v[l] = ROW(c, zb + NGLL2 * l);
-#pragma unroll
-    for (int o = 0; o < NGLLX; ++o) {
-      float t = 0.f;
-#pragma unroll
-      for (int l = 0; l < NGLLX; ++l) t = fmaf(v[l], hp[o + NGLLX * l], t);
-      t3[c][o] = t;
-    }
+    eo5(v, a.ek, t3[c]);
   }
   __syncthreads();  // rows 3-8 complete; every read of rows 0-2 done
 
@@ -216,32 +202,29 @@ __global__ void __launch_bounds__(kPencils * W, MINB) elem_pencil_kernel(const E
       float v[NGLLX];
 #pragma unroll
       for (int l = 0; l < NGLLX; ++l) v[l] = ROW(c, xb + l);
+      float n[NGLLX];
+      eo5(v, a.ekw, n);
 #pragma unroll
-      for (int o = 0; o < NGLLX; ++o) {
-        float n = 0.f;
-#pragma unroll
-        for (int l = 0; l < NGLLX; ++l) n = fmaf(v[l], hpw[l + NGLLX * o], n);
-        ROW(c, xb + o) = fac1 * n;
-      }
+      for (int o = 0; o < NGLLX; ++o) ROW(c, xb + o) = fac1 * n[o];
     }
 #pragma unroll
     for (int c = 0; c < 3; ++c) {
       float v[NGLLX];
 #pragma unroll
       for (int l = 0; l < NGLLX; ++l) v[l] = ROW(3 + c, yb + NGLLX * l);
+      float n[NGLLX];
+      eo5(v, a.ekw, n);
 #pragma unroll
-      for (int o = 0; o < NGLLX; ++o) {
-        float n = 0.f;
-#pragma unroll
-        for (int l = 0; l < NGLLX; ++l) n = fmaf(v[l], hpw[l + NGLLX * o], n);
-        ROW(3 + c, yb + NGLLX * o) = n;      // unweighted: fac2 applied in the sum below
-      }
+      for (int o = 0; o < NGLLX; ++o) ROW(3 + c, yb + NGLLX * o) = n[o];   // fac2 applied in the sum below
     }
   }
   __syncthreads();
   // ---- z from registers, the weighted sum and the scatter-add ---------------------
   if (live) {
     const float fac3 = s_gll[2 * NGLL2 + pa + NGLLX * pb];  // wgllwgll_xy(i, j)
+    float nz[3][NGLLX];
+#pragma unroll
+    for (int c = 0; c < 3; ++c) eo5(fz[c], a.ekw, nz[c]);
 #pragma unroll
     for (int o = 0; o < NGLLX; ++o) {
       const int p = zb + NGLL2 * o;
@@ -249,11 +232,8 @@ __global__ void __launch_bounds__(kPencils * W, MINB) elem_pencil_kernel(const E
       const long g = __ldg(a.ibool + eb + p);
 #pragma unroll
       for (int c = 0; c < 3; ++c) {
-        float n = 0.f;
-#pragma unroll
-        for (int l = 0; l < NGLLX; ++l) n = fmaf(fz[c][l], hpw[l + NGLLX * o], n);
         const float r = fmaf(fac2, ROW(3 + c, p), ROW(c, p));
-        atomicAdd(a.accel + 3 * g + c, -(r + fac3 * n));
+        atomicAdd(a.accel + 3 * g + c, -(r + fac3 * nz[c][o]));
       }
     }
   }
@@ -303,6 +283,8 @@ void run_elem_pencil(Mesh* mp, const StiffnessArgs& a, int blocks_per_sm, cudaSt
   q.accel = a.accel;
   memcpy(q.hp, mp->h_hprime, sizeof(q.hp));
   memcpy(q.hpw, mp->h_hprimewgll, sizeof(q.hpw));
+  even_odd_coefficients(mp->h_hprime, 1, NGLLX, q.ek);
+  even_odd_coefficients(mp->h_hprimewgll, NGLLX, 1, q.ekw);
   launch_elem_pencil(q, blocks_per_sm, s);
 }
 

@@ -486,6 +486,8 @@ struct ElemPencilArgs {
   float* accel;
   float hp[NGLL2];              // hprime, hprimewgll by value (parameter bank)
   float hpw[NGLL2];
+  float ek[12];                 // their even / odd coefficients (eo5)
+  float ekw[12];
 };
 bool launch_elem_pencil(const ElemPencilArgs& a, int blocks_per_sm, cudaStream_t s);
 struct Mesh;
@@ -523,6 +525,26 @@ struct PencilArgs {
 };
 // even / odd coefficients of a centro-antisymmetric 5x5 matrix M[o][l] = m[o * so + l * sl]
 void even_odd_coefficients(const float* m, int so, int sl, float k[12]);
+// out[o] = sum_l M[o][l] v[l] for the 5x5 GLL derivative matrices, which are
+// centro-antisymmetric (M[4-o][4-l] = -M[o][l], the GLL points being symmetric):
+// from the even and odd parts e_l = v_l + v_{4-l}, d_l = v_l - v_{4-l},
+//   out_o, out_{4-o} = S_o +- A_o,  S_o = a_o0 d_0 + a_o1 d_1,
+//   A_o = b_o0 e_0 + b_o1 e_1 + c_o v_2   (o = 0, 1),   out_2 = m_20 d_0 + m_21 d_1,
+// 20 operations instead of 25 FMAs (k: a00 a01 b00 b01 c0 a10 a11 b10 b11 c1 m20 m21)
+__device__ __forceinline__ void eo5(const float v[NGLLX], const float* k, float out[NGLLX]) {
+  const float e0 = v[0] + v[4], e1 = v[1] + v[3], d0 = v[0] - v[4], d1 = v[1] - v[3];
+  const float v2 = v[2];
+#pragma unroll
+  for (int o = 0; o < 2; ++o) {
+    const float* q = k + 5 * o;
+    const float S = fmaf(q[1], d1, q[0] * d0);
+    const float A = fmaf(q[4], v2, fmaf(q[3], e1, q[2] * e0));
+    out[o] = S + A;
+    out[4 - o] = S - A;
+  }
+  out[2] = fmaf(k[11], d1, k[10] * d0);
+}
+
 bool launch_batch_pencil(const PencilArgs& a, int lanes, int geom_format, cudaStream_t s);
 
 void launch_stiffness_pipelined(const StiffnessArgs& a, bool att, bool store_strain, int* err, cudaStream_t s);
