@@ -120,6 +120,50 @@ __global__ void point_span_kernel(const int* __restrict__ ibool, const int* __re
   atomicMax(out + k + 1, g);
 }
 
+// corrector_predictor_kernel over four consecutive values of the (3, NGLOB) arrays
+// per thread (16-byte loads and stores; the mass of each value by its own point
+// and component); thread n4 also takes the n - 4 n4 values of the tail.  d, v, a
+// 16-byte aligned; n = 3 * nglob < 2^31.
+__global__ void corrector_predictor4_kernel(float* __restrict__ d, float* __restrict__ v, float* __restrict__ a,
+                                            const float* __restrict__ rmx, const float* __restrict__ rmy,
+                                            const float* __restrict__ rmz, int n, float dt, float dt2,
+                                            float dtsq2) {
+  const int q = blockIdx.x * blockDim.x + threadIdx.x;
+  const int n4 = n >> 2;
+  if (q > n4) return;
+  auto rm_of = [&](int i) {
+    const int g = i / 3;
+    const int c = i - 3 * g;
+    return c == 0 ? __ldg(rmx + g) : (c == 1 ? __ldg(rmy + g) : __ldg(rmz + g));
+  };
+  if (q == n4) {
+    for (int i = 4 * n4; i < n; ++i) {
+      const float ac = a[i] * rm_of(i);
+      const float vh = v[i] + dt2 * ac;
+      d[i] = d[i] + dt * vh + dtsq2 * ac;
+      v[i] = vh + dt2 * ac;
+      a[i] = 0.f;
+    }
+    return;
+  }
+  const int i0 = 4 * q;
+  const float4 a4 = reinterpret_cast<const float4*>(a)[q];
+  float4 v4 = reinterpret_cast<const float4*>(v)[q];
+  float4 d4 = reinterpret_cast<const float4*>(d)[q];
+#define SF3D_NEWMARK(x, k)                   \
+  {                                          \
+    const float ac = a4.x * rm_of(i0 + k);   \
+    const float vh = v4.x + dt2 * ac;        \
+    d4.x = d4.x + dt * vh + dtsq2 * ac;      \
+    v4.x = vh + dt2 * ac;                    \
+  }
+  SF3D_NEWMARK(x, 0) SF3D_NEWMARK(y, 1) SF3D_NEWMARK(z, 2) SF3D_NEWMARK(w, 3)
+#undef SF3D_NEWMARK
+  reinterpret_cast<float4*>(d)[q] = d4;
+  reinterpret_cast<float4*>(v)[q] = v4;
+  reinterpret_cast<float4*>(a)[q] = make_float4(0.f, 0.f, 0.f, 0.f);
+}
+
 // Stacey absorbing traction (compute_stacey_viscoelastic.F90:90-130,
 // kernels/compute_stacey_elastic_kernel.cu): one thread per face GLL point.
 __global__ void stacey_kernel(int nfaces, const int* __restrict__ abs_ispec, const int* __restrict__ abs_pt,
@@ -444,6 +488,12 @@ int enqueue_step(Mesh* mp, float dt, float dt2, float dtsq2, bool first_step, cu
     } else if (first_step) {
       predictor_kernel<<<nblk(3 * ng, 256), 256, 0, s>>>(F.displ + 3 * g0, F.veloc + 3 * g0, F.accel + 3 * g0,
                                                           3 * ng, dt, dt2, dtsq2);
+    } else if (g0 % 4 == 0 && 3 * ng < (1L << 31)) {
+      // 16-byte vectors (the span starts on a 16-byte boundary: 3 g0 floats, g0 % 4 == 0)
+      const int n = (int)(3 * ng);
+      corrector_predictor4_kernel<<<nblk((n >> 2) + 1, 256), 256, 0, s>>>(
+          F.displ + 3 * g0, F.veloc + 3 * g0, F.accel + 3 * g0, mp->d_rmassx + g0, mp->d_rmassy + g0,
+          mp->d_rmassz + g0, n, dt, dt2, dtsq2);
     } else {
       corrector_predictor_kernel<<<nblk(3 * ng, 256), 256, 0, s>>>(F.displ + 3 * g0, F.veloc + 3 * g0,
                                                                     F.accel + 3 * g0, mp->d_rmassx + g0,
