@@ -112,21 +112,37 @@ __global__ void adj_update_kernel(float* __restrict__ uh, float* __restrict__ vh
 // The same update when K p and B p were scatter-added straight into the adjoint
 // fields (uh already holds uh - kp, vh holds vh - bp): vh and p of the previous
 // step, no accumulators to read or clear.
+// Four consecutive values per thread (16-byte accesses), thread n4 also taking
+// the tail; n = 3 * nglob < 2^31.
 __global__ void adj_update_direct_kernel(const float* __restrict__ uh, float* __restrict__ vh,
                                          float* __restrict__ p, const float* __restrict__ rmx,
-                                         const float* __restrict__ rmy, const float* __restrict__ rmz, long nglob,
+                                         const float* __restrict__ rmy, const float* __restrict__ rmz, int n,
                                          float dt, float dt2, float dtsq2) {
-  const long i = (long)blockIdx.x * blockDim.x + threadIdx.x;
-  if (i >= 3 * nglob) return;
-  const float ut = uh[i];
-  const float vt = vh[i];
-  const float vn = dt * ut + vt;
-  const float an = dtsq2 * ut + dt2 * vt;
-  vh[i] = vn;
-  const long g = i / 3;
-  const int c = (int)(i - 3 * g);
-  const float rm = c == 0 ? __ldg(rmx + g) : (c == 1 ? __ldg(rmy + g) : __ldg(rmz + g));
-  p[i] = -rm * (an + dt2 * vn);
+  const int q = blockIdx.x * blockDim.x + threadIdx.x;
+  const int n4 = n >> 2;
+  if (q > n4) return;
+  auto one = [&](float ut, float vt, int i, float& vn, float& pn) {
+    vn = dt * ut + vt;
+    const float an = dtsq2 * ut + dt2 * vt;
+    const int g = i / 3;
+    const int c = i - 3 * g;
+    const float rm = c == 0 ? __ldg(rmx + g) : (c == 1 ? __ldg(rmy + g) : __ldg(rmz + g));
+    pn = -rm * (an + dt2 * vn);
+  };
+  if (q == n4) {
+    for (int i = 4 * n4; i < n; ++i) one(uh[i], vh[i], i, vh[i], p[i]);
+    return;
+  }
+  const int i0 = 4 * q;
+  const float4 u4 = reinterpret_cast<const float4*>(uh)[q];
+  const float4 v4 = reinterpret_cast<const float4*>(vh)[q];
+  float4 vn, pn;
+  one(u4.x, v4.x, i0, vn.x, pn.x);
+  one(u4.y, v4.y, i0 + 1, vn.y, pn.y);
+  one(u4.z, v4.z, i0 + 2, vn.z, pn.z);
+  one(u4.w, v4.w, i0 + 3, vn.w, pn.w);
+  reinterpret_cast<float4*>(vh)[q] = vn;
+  reinterpret_cast<float4*>(p)[q] = pn;
 }
 
 struct GradArgs {
@@ -510,8 +526,9 @@ void adjoint_step(Mesh* mp, int n, const float* u, const float* araw, float dt, 
       grad_accum_kernel<<<a.nelem, NGLL3_PAD, 0, s>>>(ga);
   }
   if (G->fused)
-    adj_update_direct_kernel<<<nblk(n3, 256), 256, 0, s>>>(G->adj_u, G->adj_v, G->p, mp->d_rmassx, mp->d_rmassy,
-                                                           mp->d_rmassz, mp->nglob, dt, dt2, dtsq2);
+    adj_update_direct_kernel<<<nblk((n3 >> 2) + 1, 256), 256, 0, s>>>(G->adj_u, G->adj_v, G->p, mp->d_rmassx,
+                                                                      mp->d_rmassy, mp->d_rmassz, (int)n3, dt,
+                                                                      dt2, dtsq2);
   else
     adj_update_kernel<<<nblk(n3, 256), 256, 0, s>>>(G->adj_u, G->adj_v, G->kp, G->bp, G->p, mp->d_rmassx,
                                                     mp->d_rmassy, mp->d_rmassz, mp->nglob, dt, dt2, dtsq2);
@@ -564,7 +581,9 @@ int sf3d_gradient_setup(long* Mesh_pointer, int nstep, int checkpoint_every, dou
   const size_t npt = (size_t)mp->nspec * NGLL3_PAD;
   bool ok = true;
   if (G->nckpt > 0) ok = ok && alloc_f(&G->ckpt, (size_t)G->nckpt * 3 * n3);
-  ok = ok && alloc_f(&G->seg_u, (size_t)G->every * n3) && alloc_f(&G->seg_a, (size_t)G->every * n3);
+  G->seg_stride = (n3 + 3) & ~(size_t)3;
+  ok = ok && alloc_f(&G->seg_u, (size_t)G->every * G->seg_stride) &&
+       alloc_f(&G->seg_a, (size_t)G->every * G->seg_stride);
   ok = ok && alloc_f(&G->adj_u, n3) && alloc_f(&G->adj_v, n3) && alloc_f(&G->adj_a, n3);
   ok = ok && alloc_f(&G->p, n3) && alloc_f(&G->kp, n3) && alloc_f(&G->bp, n3);
   ok = ok && alloc_f(&G->residual, 3ull * (mp->nrec_local > 0 ? mp->nrec_local : 1) * nstep);
@@ -575,7 +594,7 @@ int sf3d_gradient_setup(long* Mesh_pointer, int nstep, int checkpoint_every, dou
     return SF3D_ERR_CUDA;
   }
   for (int q = 0; q < NGLLX; ++q) G->wgll[q] = (float)sqrt((double)mp->h_wxy[q + NGLLX * q]);
-  G->bytes = sizeof(float) * ((size_t)G->nckpt * 3 * n3 + 2ull * G->every * n3 + 6 * n3 +
+  G->bytes = sizeof(float) * ((size_t)G->nckpt * 3 * n3 + 2ull * G->every * G->seg_stride + 6 * n3 +
                               3ull * (mp->nrec_local > 0 ? mp->nrec_local : 1) * nstep) +
              3 * sizeof(double) * npt;
   if (device_bytes) *device_bytes = (double)G->bytes;
@@ -688,16 +707,18 @@ int sf3d_gradient_backward(long* Mesh_pointer, realw deltat) {
     float* const base_a = mp->f.accel;
     for (int q = 0; q < len; ++q) {
       StepIO io;
-      io.d_in = q == 0 ? base_d : G->seg_u + (size_t)(q - 1) * n3;
-      io.d_out = G->seg_u + (size_t)q * n3;
-      io.a_in = q == 0 ? base_a : G->seg_a + (size_t)(q - 1) * n3;
-      io.a_out = G->seg_a + (size_t)q * n3;
+      const size_t st = G->seg_stride;
+      io.d_in = q == 0 ? base_d : G->seg_u + (size_t)(q - 1) * st;
+      io.d_out = G->seg_u + (size_t)q * st;
+      io.a_in = q == 0 ? base_a : G->seg_a + (size_t)(q - 1) * st;
+      io.a_out = G->seg_a + (size_t)q * st;
       enqueue_step(mp, dt, dt2, dtsq2, j == 0 && q == 0, nullptr, &io);
     }
     mp->f.displ = base_d;
     mp->f.accel = base_a;
     for (int q = len - 1; q >= 0; --q)
-      adjoint_step(mp, n0 + q, G->seg_u + (size_t)q * n3, G->seg_a + (size_t)q * n3, dt, dt2, dtsq2);
+      adjoint_step(mp, n0 + q, G->seg_u + (size_t)q * G->seg_stride, G->seg_a + (size_t)q * G->seg_stride, dt, dt2,
+                   dtsq2);
     if (!cuda_ok(cudaGetLastError(), "sf3d_gradient_backward")) return SF3D_ERR_CUDA;
   }
   SF3D_CUDA_RET(cudaEventRecord(mp->ev1, s), SF3D_ERR_CUDA);

@@ -170,8 +170,12 @@ struct Fields {
 struct GradState {
   int nstep = 0, every = 0, nckpt = 0;
   float* ckpt = nullptr;       // [nckpt][3][3*nglob]: displ, veloc, accel at segment starts
-  float* seg_u = nullptr;      // [every][3*nglob]: displacement after each step of a segment
-  float* seg_a = nullptr;      // [every][3*nglob]: force after each step (before the mass matrix)
+  // [every][seg_stride]: displacement / force (before the mass matrix) after each step
+  // of a segment; seg_stride = 3*nglob rounded up to a multiple of 4, so that every
+  // step's slice starts on a 16-byte boundary (the step kernels use 16-byte accesses)
+  float* seg_u = nullptr;
+  float* seg_a = nullptr;
+  size_t seg_stride = 0;
   float* adj_u = nullptr;      // adjoint of displacement, velocity, acceleration [3*nglob]
   float* adj_v = nullptr;
   float* adj_a = nullptr;

@@ -51,20 +51,42 @@ __global__ void predictor_oop_kernel(const float* __restrict__ d_in, float* __re
   d_out[i] = d_in[i] + dt * vi + dtsq2 * ai;
   v[i] = vi + dt2 * ai;
 }
+// four consecutive values per thread (16-byte accesses; all buffers 16-byte
+// aligned), thread n4 also taking the tail; n = 3 * nglob < 2^31
 __global__ void corrector_predictor_oop_kernel(const float* __restrict__ d_in, float* __restrict__ d_out,
                                                float* __restrict__ v, const float* __restrict__ a,
                                                const float* __restrict__ rmx, const float* __restrict__ rmy,
-                                               const float* __restrict__ rmz, long nglob, float dt, float dt2,
+                                               const float* __restrict__ rmz, int n, float dt, float dt2,
                                                float dtsq2) {
-  const long i = (long)blockIdx.x * blockDim.x + threadIdx.x;
-  if (i >= 3 * nglob) return;
-  const long g = i / 3;
-  const int c = (int)(i - 3 * g);
-  const float rm = c == 0 ? __ldg(rmx + g) : (c == 1 ? __ldg(rmy + g) : __ldg(rmz + g));
-  const float ac = a[i] * rm;
-  const float vh = v[i] + dt2 * ac;
-  d_out[i] = d_in[i] + dt * vh + dtsq2 * ac;
-  v[i] = vh + dt2 * ac;
+  const int q = blockIdx.x * blockDim.x + threadIdx.x;
+  const int n4 = n >> 2;
+  if (q > n4) return;
+  auto rm_of = [&](int i) {
+    const int g = i / 3;
+    const int c = i - 3 * g;
+    return c == 0 ? __ldg(rmx + g) : (c == 1 ? __ldg(rmy + g) : __ldg(rmz + g));
+  };
+  auto one = [&](float ai, float vi, float di, float rm, float& dn, float& vn) {
+    const float ac = ai * rm;
+    const float vh = vi + dt2 * ac;
+    dn = di + dt * vh + dtsq2 * ac;
+    vn = vh + dt2 * ac;
+  };
+  if (q == n4) {
+    for (int i = 4 * n4; i < n; ++i) one(a[i], v[i], d_in[i], rm_of(i), d_out[i], v[i]);
+    return;
+  }
+  const int i0 = 4 * q;
+  const float4 a4 = reinterpret_cast<const float4*>(a)[q];
+  const float4 v4 = reinterpret_cast<const float4*>(v)[q];
+  const float4 d4 = reinterpret_cast<const float4*>(d_in)[q];
+  float4 dn, vn;
+  one(a4.x, v4.x, d4.x, rm_of(i0), dn.x, vn.x);
+  one(a4.y, v4.y, d4.y, rm_of(i0 + 1), dn.y, vn.y);
+  one(a4.z, v4.z, d4.z, rm_of(i0 + 2), dn.z, vn.z);
+  one(a4.w, v4.w, d4.w, rm_of(i0 + 3), dn.w, vn.w);
+  reinterpret_cast<float4*>(d_out)[q] = dn;
+  reinterpret_cast<float4*>(v)[q] = vn;
 }
 
 // Mass matrix + corrector (kernels/kernel_3_cuda_device.cu,
@@ -459,9 +481,8 @@ int enqueue_step(Mesh* mp, float dt, float dt2, float dtsq2, bool first_step, cu
     if (first_step)
       predictor_oop_kernel<<<nblk(n, 256), 256, 0, s>>>(io->d_in, io->d_out, F.veloc, io->a_in, n, dt, dt2, dtsq2);
     else
-      corrector_predictor_oop_kernel<<<nblk(n, 256), 256, 0, s>>>(io->d_in, io->d_out, F.veloc, io->a_in,
-                                                                  mp->d_rmassx, mp->d_rmassy, mp->d_rmassz,
-                                                                  mp->nglob, dt, dt2, dtsq2);
+      corrector_predictor_oop_kernel<<<nblk((n >> 2) + 1, 256), 256, 0, s>>>(
+          io->d_in, io->d_out, F.veloc, io->a_in, mp->d_rmassx, mp->d_rmassy, mp->d_rmassz, (int)n, dt, dt2, dtsq2);
     F.displ = io->d_out;
     F.accel = io->a_out;
   } else if (mp->pml) {
