@@ -11,6 +11,7 @@
 // memory, and captures blocks of steps into CUDA graphs, so a step costs a few
 // graph nodes and no host round trip.
 #include <limits.h>
+#include <stdint.h>
 #include <math.h>
 #include <string.h>
 
@@ -184,6 +185,20 @@ __global__ void corrector_predictor4_kernel(float* __restrict__ d, float* __rest
   reinterpret_cast<float4*>(d)[q] = d4;
   reinterpret_cast<float4*>(v)[q] = v4;
   reinterpret_cast<float4*>(a)[q] = make_float4(0.f, 0.f, 0.f, 0.f);
+}
+
+// corrector/predictor over (3, nglob) arrays: the 16-byte vector kernel where the
+// arrays start on 16-byte boundaries, else one value per thread
+void launch_corrector_predictor(float* d, float* v, float* a, const float* rmx, const float* rmy, const float* rmz,
+                                long nglob, float dt, float dt2, float dtsq2, cudaStream_t s) {
+  const bool aligned = ((reinterpret_cast<uintptr_t>(d) | reinterpret_cast<uintptr_t>(v) |
+                         reinterpret_cast<uintptr_t>(a)) & 15) == 0;
+  if (aligned && 3 * nglob < (1L << 31)) {
+    const int n = (int)(3 * nglob);
+    corrector_predictor4_kernel<<<nblk((n >> 2) + 1, 256), 256, 0, s>>>(d, v, a, rmx, rmy, rmz, n, dt, dt2, dtsq2);
+  } else {
+    corrector_predictor_kernel<<<nblk(3 * nglob, 256), 256, 0, s>>>(d, v, a, rmx, rmy, rmz, nglob, dt, dt2, dtsq2);
+  }
 }
 
 // Stacey absorbing traction (compute_stacey_viscoelastic.F90:90-130,
@@ -509,17 +524,9 @@ int enqueue_step(Mesh* mp, float dt, float dt2, float dtsq2, bool first_step, cu
     } else if (first_step) {
       predictor_kernel<<<nblk(3 * ng, 256), 256, 0, s>>>(F.displ + 3 * g0, F.veloc + 3 * g0, F.accel + 3 * g0,
                                                           3 * ng, dt, dt2, dtsq2);
-    } else if (g0 % 4 == 0 && 3 * ng < (1L << 31)) {
-      // 16-byte vectors (the span starts on a 16-byte boundary: 3 g0 floats, g0 % 4 == 0)
-      const int n = (int)(3 * ng);
-      corrector_predictor4_kernel<<<nblk((n >> 2) + 1, 256), 256, 0, s>>>(
-          F.displ + 3 * g0, F.veloc + 3 * g0, F.accel + 3 * g0, mp->d_rmassx + g0, mp->d_rmassy + g0,
-          mp->d_rmassz + g0, n, dt, dt2, dtsq2);
     } else {
-      corrector_predictor_kernel<<<nblk(3 * ng, 256), 256, 0, s>>>(F.displ + 3 * g0, F.veloc + 3 * g0,
-                                                                    F.accel + 3 * g0, mp->d_rmassx + g0,
-                                                                    mp->d_rmassy + g0, mp->d_rmassz + g0, ng, dt, dt2,
-                                                                    dtsq2);
+      launch_corrector_predictor(F.displ + 3 * g0, F.veloc + 3 * g0, F.accel + 3 * g0, mp->d_rmassx + g0,
+                                 mp->d_rmassy + g0, mp->d_rmassz + g0, ng, dt, dt2, dtsq2, s);
     }
   }
   ++launches;
@@ -655,9 +662,8 @@ void update_displacement_cuda_(long* Mesh_pointer, realw* deltat_F, realw* delta
   if (mp->pend_corrector[idx] && mp->pend_dt2[idx] == *deltatover2_F) {
     // the deferred corrector of the previous step fused with this predictor
     mp->pend_corrector[idx] = 0;
-    corrector_predictor_kernel<<<nblk(n, 256), 256, 0, mp->stream>>>(F->displ, F->veloc, F->accel, mp->d_rmassx,
-                                                                    mp->d_rmassy, mp->d_rmassz, mp->nglob,
-                                                                    *deltat_F, *deltatover2_F, *deltatsqover2_F);
+    launch_corrector_predictor(F->displ, F->veloc, F->accel, mp->d_rmassx, mp->d_rmassy, mp->d_rmassz, mp->nglob,
+                               *deltat_F, *deltatover2_F, *deltatsqover2_F, mp->stream);
     cuda_ok(cudaGetLastError(), "corrector_predictor_kernel");
     return;
   }
