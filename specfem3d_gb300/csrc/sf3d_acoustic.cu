@@ -301,6 +301,59 @@ __global__ void predictor_scalar_kernel(float* __restrict__ d, float* __restrict
   a[i] = 0.f;
 }
 
+// predictor_scalar_kernel over four consecutive values per thread (16-byte
+// accesses; d, v, a 16-byte aligned), thread n4 also taking the tail; n < 2^31
+__global__ void predictor_scalar4_kernel(float* __restrict__ d, float* __restrict__ v, float* __restrict__ a, int n,
+                                         float dt, float dt2, float dtsq2) {
+  const int q = blockIdx.x * blockDim.x + threadIdx.x;
+  const int n4 = n >> 2;
+  if (q > n4) return;
+  if (q == n4) {
+    for (int i = 4 * n4; i < n; ++i) {
+      const float ai = a[i], vi = v[i];
+      d[i] = d[i] + dt * vi + dtsq2 * ai;
+      v[i] = vi + dt2 * ai;
+      a[i] = 0.f;
+    }
+    return;
+  }
+  const float4 a4 = reinterpret_cast<const float4*>(a)[q];
+  float4 v4 = reinterpret_cast<const float4*>(v)[q];
+  float4 d4 = reinterpret_cast<const float4*>(d)[q];
+  d4.x = d4.x + dt * v4.x + dtsq2 * a4.x; v4.x = v4.x + dt2 * a4.x;
+  d4.y = d4.y + dt * v4.y + dtsq2 * a4.y; v4.y = v4.y + dt2 * a4.y;
+  d4.z = d4.z + dt * v4.z + dtsq2 * a4.z; v4.z = v4.z + dt2 * a4.z;
+  d4.w = d4.w + dt * v4.w + dtsq2 * a4.w; v4.w = v4.w + dt2 * a4.w;
+  reinterpret_cast<float4*>(d)[q] = d4;
+  reinterpret_cast<float4*>(v)[q] = v4;
+  reinterpret_cast<float4*>(a)[q] = make_float4(0.f, 0.f, 0.f, 0.f);
+}
+
+// mass_corrector_scalar_kernel over four consecutive values per thread (as above)
+__global__ void mass_corrector_scalar4_kernel(float* __restrict__ v, float* __restrict__ a,
+                                              const float* __restrict__ rmass, int n, float dt2) {
+  const int q = blockIdx.x * blockDim.x + threadIdx.x;
+  const int n4 = n >> 2;
+  if (q > n4) return;
+  if (q == n4) {
+    for (int i = 4 * n4; i < n; ++i) {
+      const float ai = a[i] * rmass[i];
+      a[i] = ai;
+      v[i] += dt2 * ai;
+    }
+    return;
+  }
+  float4 a4 = reinterpret_cast<const float4*>(a)[q];
+  float4 v4 = reinterpret_cast<const float4*>(v)[q];
+  const float4 r4 = reinterpret_cast<const float4*>(rmass)[q];
+  a4.x *= r4.x; v4.x += dt2 * a4.x;
+  a4.y *= r4.y; v4.y += dt2 * a4.y;
+  a4.z *= r4.z; v4.z += dt2 * a4.z;
+  a4.w *= r4.w; v4.w += dt2 * a4.w;
+  reinterpret_cast<float4*>(a)[q] = a4;
+  reinterpret_cast<float4*>(v)[q] = v4;
+}
+
 // kernel_3_acoustic: chi_dd *= rmass_acoustic; chi_dot += dt/2 chi_dd
 __global__ void mass_corrector_scalar_kernel(float* __restrict__ v, float* __restrict__ a,
                                              const float* __restrict__ rmass, long n, float dt2) {
@@ -415,8 +468,15 @@ int enqueue_acoustic_step(Mesh* mp, float dt, float dt2, float dtsq2) {
   // are zero at points of solid elements alone, and no kernel writes them there
   const long g0 = mp->ac_count >= 0 ? mp->ac_first : 0;
   const long n = mp->ac_count >= 0 ? mp->ac_count : mp->nglob;
-  predictor_scalar_kernel<<<nblk(n, 256), 256, 0, s>>>(mp->d_potential + g0, mp->d_potential_dot + g0,
-                                                        mp->d_potential_dot_dot + g0, n, dt, dt2, dtsq2);
+  // 16-byte vectors where the span starts on a 16-byte boundary
+  const bool vec = g0 % 4 == 0 && n < (1L << 31);
+  if (vec)
+    predictor_scalar4_kernel<<<nblk((n >> 2) + 1, 256), 256, 0, s>>>(mp->d_potential + g0, mp->d_potential_dot + g0,
+                                                                      mp->d_potential_dot_dot + g0, (int)n, dt, dt2,
+                                                                      dtsq2);
+  else
+    predictor_scalar_kernel<<<nblk(n, 256), 256, 0, s>>>(mp->d_potential + g0, mp->d_potential_dot + g0,
+                                                          mp->d_potential_dot_dot + g0, n, dt, dt2, dtsq2);
   ++launches;
   const long nfs = (long)mp->num_free_surface_faces * NGLL2;
   if (nfs > 0) {
@@ -461,8 +521,13 @@ int enqueue_acoustic_step(Mesh* mp, float dt, float dt2, float dtsq2) {
                                                                 mp->d_stf_table, mp->d_it, mp->stf_nstep);
     ++launches;
   }
-  mass_corrector_scalar_kernel<<<nblk(n, 256), 256, 0, s>>>(mp->d_potential_dot + g0, mp->d_potential_dot_dot + g0,
-                                                            mp->d_rmass_acoustic + g0, n, dt2);
+  if (vec)
+    mass_corrector_scalar4_kernel<<<nblk((n >> 2) + 1, 256), 256, 0, s>>>(
+        mp->d_potential_dot + g0, mp->d_potential_dot_dot + g0, mp->d_rmass_acoustic + g0, (int)n, dt2);
+  else
+    mass_corrector_scalar_kernel<<<nblk(n, 256), 256, 0, s>>>(mp->d_potential_dot + g0,
+                                                              mp->d_potential_dot_dot + g0,
+                                                              mp->d_rmass_acoustic + g0, n, dt2);
   ++launches;
   if (nfs > 0) {
     free_surface_kernel<<<nblk(nfs, 128), 128, 0, s>>>(mp->num_free_surface_faces, mp->d_fs_ispec, mp->d_fs_pt,
