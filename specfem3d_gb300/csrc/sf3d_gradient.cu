@@ -557,6 +557,11 @@ int sf3d_gradient_setup(long* Mesh_pointer, int nstep, int checkpoint_every, dou
     set_error(SF3D_ERR_UNSUPPORTED, "sf3d_gradient: C-PML layers are not supported in the adjoint sweep");
     return SF3D_ERR_UNSUPPORTED;
   }
+  if (3L * mp->nglob >= (1L << 31)) {
+    // the sweep's vector passes index the (3, NGLOB) arrays in 32 bits
+    set_error(SF3D_ERR_ARG, "sf3d_gradient: 3 * NGLOB must stay below 2^31");
+    return SF3D_ERR_ARG;
+  }
   if (mp->has_acoustic) {
     set_error(SF3D_ERR_ARG, "sf3d_gradient: acoustic elements are not supported");
     return SF3D_ERR_ARG;
